@@ -1,0 +1,222 @@
+"""Input decks for the Euler1D / Euler2D / NavierStokes3D workloads.
+
+Writes HyPar's own input files (``solver.inp``, ``physics.inp``,
+``boundary.inp``, ``weno.inp`` and a binary ``initial.inp``) for the synthetic
+workloads: the Sod shock tube, the isentropic vortex and the Taylor-Green
+vortex.  The formats follow the reference readers: ``ReadInputs``
+(src/Simulation/ReadInputs.c:94-440), ``InitializeBoundaries``
+(src/Simulation/InitializeBoundaries.c:75-180), ``WENOInitialize``
+(src/InterpolationFunctions/WENOInitialize.c:62-96) and the binary
+``ReadArraySerial`` layout (src/IOFunctions/ReadArray.c:215-240: the grid
+coordinates of every dimension, then the solution with the components of a
+point contiguous and dimension 0 fastest).
+
+The initial conditions restate the reference's example generators
+(Examples/1D/Euler1D/SodShockTube/aux/init.c:38-60 and
+Examples/2D/Euler2D/VortexConvection/aux/init.C:48-80, with the vortex
+strength and centre as parameters) and the Taylor-Green vortex in acoustic
+scaling (rho = 1, p = 1/gamma, Mach M).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Case:
+    """A complete HyPar input deck held in memory."""
+
+    model: str                      # "euler1d" | "euler2d" | "navierstokes3d"
+    size: List[int]
+    x: List[np.ndarray]             # grid coordinates per dimension
+    u: np.ndarray                   # (prod(size), nvars), dimension 0 fastest
+    dt: float
+    n_iter: int
+    time_scheme_type: str           # "44" | "ssprk3" | "22" | "33" | "1fe"
+    interp: str = "components"      # "components" | "characteristic"
+    upwinding: str = "roe"
+    gamma: float = 1.4
+    eps: float = 1e-6
+    bc: str = "periodic"            # "periodic" | "extrapolate"
+    Re: Optional[float] = None      # NavierStokes3D physics.inp values
+    Pr: float = 0.72
+    Minf: float = 1.0
+    file_op_iter: Optional[int] = None
+
+    @property
+    def ndims(self) -> int:
+        return len(self.size)
+
+    @property
+    def nvars(self) -> int:
+        return {"euler1d": 3, "euler2d": 4, "navierstokes3d": 5}[self.model]
+
+    def solver_inp(self) -> str:
+        nd = self.ndims
+        lines = [
+            "begin",
+            f"  ndims             {nd}",
+            f"  nvars             {self.nvars}",
+            "  size              " + " ".join(str(s) for s in self.size),
+            "  iproc             " + " ".join("1" for _ in self.size),
+            "  ghost             3",
+            f"  n_iter            {self.n_iter}",
+            "  time_scheme       rk",
+            f"  time_scheme_type  {self.time_scheme_type}",
+            "  hyp_space_scheme  weno5",
+            f"  hyp_interp_type   {self.interp}",
+        ]
+        if self.model == "navierstokes3d":
+            lines += ["  par_space_type    nonconservative-2stage", "  par_space_scheme  4"]
+        lines += [
+            f"  dt                {self.dt!r}",
+            f"  screen_op_iter    {max(self.n_iter, 1)}",
+            f"  file_op_iter      {self.file_op_iter or max(self.n_iter, 1)}",
+            "  ip_file_type      binary",
+            "  op_file_format    binary",
+            "  op_overwrite      yes",
+            f"  model             {self.model}",
+            "end",
+        ]
+        return "\n".join(lines) + "\n"
+
+    def physics_inp(self) -> str:
+        lines = ["begin", f"  gamma      {self.gamma!r}", f"  upwinding  {self.upwinding}"]
+        if self.model == "navierstokes3d":
+            lines += [f"  Pr         {self.Pr!r}", f"  Minf       {self.Minf!r}"]
+            if self.Re is not None:
+                lines.append(f"  Re         {self.Re!r}")
+        lines.append("end")
+        return "\n".join(lines) + "\n"
+
+    def weno_inp(self) -> str:
+        return ("begin\n  mapped 0\n  borges 0\n  yc 0\n  no_limiting 0\n"
+                f"  epsilon {self.eps!r}\n  p 2.0\nend\n")
+
+    def boundary_inp(self) -> str:
+        nd = self.ndims
+        # transverse extents padded so that they cover the whole grid
+        lo = [float(xx[0]) - 1.0 for xx in self.x]
+        hi = [float(xx[-1]) + 1.0 for xx in self.x]
+        rows = []
+        for d in range(nd):
+            for face in (1, -1):
+                ext = []
+                for e in range(nd):
+                    ext += ["0", "0"] if e == d else [repr(lo[e]), repr(hi[e])]
+                rows.append(f"{self.bc} {d} {face} " + " ".join(ext))
+        return f"{len(rows)}\n" + "\n".join(rows) + "\n"
+
+    def initial_bytes(self) -> bytes:
+        xs = np.concatenate([np.asarray(xx, dtype=np.float64) for xx in self.x])
+        return xs.tobytes() + np.ascontiguousarray(self.u, dtype=np.float64).tobytes()
+
+    def write(self, directory: str) -> str:
+        os.makedirs(directory, exist_ok=True)
+        files = {
+            "solver.inp": self.solver_inp(),
+            "physics.inp": self.physics_inp(),
+            "boundary.inp": self.boundary_inp(),
+            "weno.inp": self.weno_inp(),
+        }
+        for name, text in files.items():
+            with open(os.path.join(directory, name), "w") as f:
+                f.write(text)
+        with open(os.path.join(directory, "initial.inp"), "wb") as f:
+            f.write(self.initial_bytes())
+        return directory
+
+
+def sod(n: int = 1024, n_iter: int = 1000, dt: float = 1e-4, interp: str = "components",
+        upwinding: str = "roe", scheme: str = "44") -> Case:
+    """Sod shock tube on x_i = i/(n-1) with mirror ("extrapolate") ends."""
+    x = np.arange(n, dtype=np.float64) * (1.0 / float(n - 1))
+    left = x < 0.5
+    rho = np.where(left, 1.0, 0.125)
+    P = np.where(left, 1.0, 0.1)
+    U = np.zeros(n)
+    e = P / 0.4 + 0.5 * rho * U * U
+    u = np.stack([rho, rho * U, e], axis=1)
+    return Case("euler1d", [n], [x], u, dt, n_iter, scheme, interp, upwinding, bc="extrapolate")
+
+
+def vortex_state(n: int, b: float = 5.0, xc: float = 5.0, yc: float = 5.0, gamma: float = 1.4,
+                 length: float = 10.0, uinf: float = 0.5, vinf: float = 0.0):
+    """Isentropic vortex of strength b centred at (xc, yc) on an n x n periodic grid."""
+    h = length / float(n)
+    x = np.arange(n, dtype=np.float64) * h
+    X, Y = np.meshgrid(x, x, indexing="xy")  # X[j, i] = x_i : dimension 0 fastest
+    rsq = (X - xc) ** 2 + (Y - yc) ** 2
+    pi = math.pi
+    rho = np.power(1.0 - ((gamma - 1.0) * b * b) / (8.0 * gamma * pi * pi) * np.exp(1.0 - rsq),
+                   1.0 / (gamma - 1.0))
+    P = np.power(rho, gamma)
+    du = -b / (2.0 * pi) * np.exp(0.5 * (1.0 - rsq)) * (Y - yc)
+    dv = b / (2.0 * pi) * np.exp(0.5 * (1.0 - rsq)) * (X - xc)
+    uu = uinf + du
+    vv = vinf + dv
+    e = P / (gamma - 1.0) + 0.5 * rho * (uu * uu + vv * vv)
+    u = np.stack([rho, rho * uu, rho * vv, e], axis=-1).reshape(n * n, 4)
+    return x, u
+
+
+def vortex(n: int = 1024, n_iter: int = 200, dt: Optional[float] = None, b: float = 5.0,
+           xc: float = 5.0, yc: float = 5.0, interp: str = "characteristic",
+           upwinding: str = "roe", scheme: str = "ssprk3", cfl: float = 0.5) -> Case:
+    """Isentropic vortex convection on [0,10)^2, periodic; dt from the CFL target if not given."""
+    x, u = vortex_state(n, b, xc, yc)
+    if dt is None:
+        dt = cfl_dt(u, 4, [10.0 / n, 10.0 / n], cfl)
+    return Case("euler2d", [n, n], [x, x.copy()], u, dt, n_iter, scheme, interp, upwinding)
+
+
+def cfl_dt(u: np.ndarray, nvars: int, h: Sequence[float], cfl: float, gamma: float = 1.4) -> float:
+    """Time step for a target CFL with the reference's CFL measure
+    max_d (|v_d| + c) dt / h_d (Euler2DComputeCFL.c:21-39)."""
+    rho = u[:, 0]
+    vel = [u[:, 1 + d] / rho for d in range(len(h))]
+    vsq = sum(v * v for v in vel)
+    P = (u[:, nvars - 1] - 0.5 * rho * vsq) * (gamma - 1.0)
+    c = np.sqrt(gamma * P / rho)
+    rate = max(float(np.max((np.abs(v) + c) / hd)) for v, hd in zip(vel, h))
+    return cfl / rate
+
+
+def tgv(n: int = 256, n_iter: int = 100, dt: float = 2e-3, mach: float = 0.1, Re: float = 1600.0,
+        Pr: float = 0.72, interp: str = "components", upwinding: str = "roe",
+        scheme: str = "44", gamma: float = 1.4) -> Case:
+    """Taylor-Green vortex on [0, 2 pi)^3, periodic, acoustic scaling."""
+    h = 2.0 * math.pi / n
+    x = np.arange(n, dtype=np.float64) * h
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")  # X[k, j, i] = x_i
+    rho = np.ones_like(X)
+    M = mach
+    P = 1.0 / gamma + (M * M / 16.0) * (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0)
+    uu = M * np.sin(X) * np.cos(Y) * np.cos(Z)
+    vv = -M * np.cos(X) * np.sin(Y) * np.cos(Z)
+    ww = np.zeros_like(X)
+    e = P / (gamma - 1.0) + 0.5 * rho * (uu * uu + vv * vv + ww * ww)
+    u = np.stack([rho, rho * uu, rho * vv, rho * ww, e], axis=-1).reshape(n ** 3, 5)
+    return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme,
+                interp, upwinding, gamma=gamma, Re=Re, Pr=Pr, Minf=mach)
+
+
+def read_op_bin(path: str) -> Dict[str, np.ndarray]:
+    """Read a HyPar binary solution file (src/IOFunctions/WriteBinary.c): int32
+    ndims, nvars, dim[ndims], float64 grid, float64 solution."""
+    with open(path, "rb") as f:
+        buf = f.read()
+    ndims, nvars = np.frombuffer(buf, np.int32, 2, 0)
+    dims = np.frombuffer(buf, np.int32, ndims, 8)
+    off = 8 + 4 * int(ndims)
+    nx = int(dims.sum())
+    x = np.frombuffer(buf, np.float64, nx, off)
+    off += 8 * nx
+    npts = int(np.prod(dims))
+    u = np.frombuffer(buf, np.float64, npts * int(nvars), off).reshape(npts, int(nvars))
+    return {"ndims": int(ndims), "nvars": int(nvars), "dims": dims.copy(), "x": x.copy(), "u": u.copy()}

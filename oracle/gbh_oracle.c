@@ -1,0 +1,969 @@
+/*
+ * gbh_oracle.c -- CPU restatement of HyPar's explicit WENO5 RHS and RK step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the parity checker for the CUDA
+ * product and the timed CPU baseline; it is never linked into libgbhypar.
+ *
+ * It restates the reference's formulas in the reference's operation order and
+ * must be compiled with -ffp-contract=off (no fused multiply-add), like the
+ * reference's own -std=c99 build, so that it reproduces the reference CPU
+ * results bit for bit.  Each routine cites the reference file:line it follows
+ * (paths relative to the HyPar source tree).
+ *
+ * Organisation differs from the reference where that changes no value: the
+ * reference stores WENO weights for the whole grid (WENOInitialize.c:135-205)
+ * and interface arrays per dimension; here each grid line is processed on its
+ * own (OpenMP over lines), computing every weight exactly where it is used.
+ */
+#include "gbh_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MAXV 5
+
+static int g_threads = 0;
+void orc_set_threads(int n) { g_threads = n; }
+int orc_get_threads(void) {
+#ifdef _OPENMP
+  return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+#ifdef _OPENMP
+#define NTHR (g_threads > 0 ? g_threads : omp_get_max_threads())
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* problem set-up                                                            */
+/* ------------------------------------------------------------------------ */
+
+orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts,
+                                int upwind, int interp, double gamma, double eps,
+                                double Re_over_Minf, double Pr, int nzones,
+                                const int *zones, const double *dxinv) {
+  if (ndims < 1 || ndims > 3 || nzones < 0 || nzones > 12) return NULL;
+  orc_problem *p = (orc_problem *)calloc(1, sizeof(orc_problem));
+  p->model = model;
+  p->ndims = ndims;
+  p->nvars = (model == ORC_EULER1D) ? 3 : (model == ORC_EULER2D ? 4 : 5);
+  p->ghosts = ghosts;
+  for (int d = 0; d < 3; d++) p->dim[d] = (d < ndims) ? dim[d] : 1;
+  p->upwind = upwind;
+  p->interp = interp;
+  p->gamma = gamma;
+  p->eps = eps;
+  p->Re = Re_over_Minf;
+  p->Pr = Pr;
+  p->nzones = nzones;
+  for (int z = 0; z < nzones; z++) {
+    const int *q = zones + 9 * z;
+    p->zones[z].type = q[0];
+    p->zones[z].dim = q[1];
+    p->zones[z].face = q[2];
+    for (int d = 0; d < 3; d++) {
+      p->zones[z].is[d] = q[3 + d];
+      p->zones[z].ie[d] = q[6 + d];
+    }
+  }
+  int nx = 0;
+  for (int d = 0; d < ndims; d++) nx += dim[d] + 2 * ghosts;
+  p->dxinv = (double *)malloc(sizeof(double) * nx);
+  memcpy(p->dxinv, dxinv, sizeof(double) * nx);
+  return p;
+}
+
+void orc_problem_destroy(orc_problem *p) {
+  if (!p) return;
+  free(p->dxinv);
+  free(p);
+}
+
+long orc_npoints_wghosts(const orc_problem *p) {
+  long n = 1;
+  for (int d = 0; d < p->ndims; d++) n *= (p->dim[d] + 2 * p->ghosts);
+  return n;
+}
+
+static void strides_wg(const orc_problem *p, long *s) {
+  s[0] = 1;
+  for (int d = 1; d < 3; d++)
+    s[d] = (d < p->ndims) ? s[d - 1] * (p->dim[d - 1] + 2 * p->ghosts) : 0;
+}
+
+/* 1-D point index of an interior-relative multi-index (include/arrayfunctions.h:40-47). */
+static long pidx(const orc_problem *p, const long *s, const int *i) {
+  long q = 0;
+  for (int d = 0; d < p->ndims; d++) q += (long)(i[d] + p->ghosts) * s[d];
+  return q;
+}
+
+/* ------------------------------------------------------------------------ */
+/* boundary conditions                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* BCPeriodicU (src/BoundaryConditions/BCPeriodic.c:36-56, single rank along dim)
+ * and BCExtrapolateU (src/BoundaryConditions/BCExtrapolate.c:29-46, a mirror copy). */
+int orc_apply_bc(const orc_problem *p, double *u) {
+  long s[3];
+  strides_wg(p, s);
+  int nd = p->ndims, nv = p->nvars, g = p->ghosts;
+  for (int z = 0; z < p->nzones; z++) {
+    const orc_zone *b = &p->zones[z];
+    int bounds[3] = {1, 1, 1}, ib[3] = {0, 0, 0};
+    long count = 1;
+    for (int d = 0; d < nd; d++) {
+      bounds[d] = b->ie[d] - b->is[d];
+      if (bounds[d] <= 0) count = 0;
+      count *= (bounds[d] > 0 ? bounds[d] : 0);
+    }
+    if (!count) continue;
+    for (long c = 0; c < count; c++) {
+      long r = c;
+      for (int d = 0; d < nd; d++) { ib[d] = (int)(r % bounds[d]); r /= bounds[d]; }
+      int ig[3], isrc[3];
+      for (int d = 0; d < nd; d++) { ig[d] = ib[d] + b->is[d]; isrc[d] = ig[d]; }
+      int dd = b->dim, N = p->dim[dd];
+      if (b->type == ORC_BC_PERIODIC) {
+        if (b->face == 1) isrc[dd] = ib[dd] + N - g;
+        else isrc[dd] = ib[dd];
+      } else if (b->type == ORC_BC_EXTRAPOLATE) {
+        if (b->face == 1) isrc[dd] = g - 1 - ib[dd];
+        else isrc[dd] = N - ib[dd] - 1;
+      } else {
+        return 1;
+      }
+      long p1 = pidx(p, s, ig), p2 = pidx(p, s, isrc);
+      for (int v = 0; v < nv; v++) u[nv * p1 + v] = u[nv * p2 + v];
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* physical models: flux, Roe average, eigen-structure                        */
+/* ------------------------------------------------------------------------ */
+
+/* Euler1D -- include/physicalmodels/euler1d.h:81-270 */
+static void e1_flux(double *f, const double *u, double gamma) {
+  double rho = u[0], v = u[1] / rho, e = u[2];
+  double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+  f[0] = rho * v;
+  f[1] = rho * v * v + P;
+  f[2] = (e + P) * v;
+}
+static void e1_roeavg(double *ua, const double *uL, const double *uR, double gamma) {
+  double rhoL = uL[0], vL = uL[1] / rhoL, eL = uL[2];
+  double PL = (eL - 0.5 * rhoL * vL * vL) * (gamma - 1.0);
+  double cLsq = gamma * PL / rhoL;
+  double HL = 0.5 * vL * vL + cLsq / (gamma - 1.0);
+  double rhoR = uR[0], vR = uR[1] / rhoR, eR = uR[2];
+  double PR = (eR - 0.5 * rhoR * vR * vR) * (gamma - 1.0);
+  double cRsq = gamma * PR / rhoR;
+  double HR = 0.5 * vR * vR + cRsq / (gamma - 1.0);
+  double tL = sqrt(rhoL), tR = sqrt(rhoR);
+  double rho = tL * tR;
+  double v = (tL * vL + tR * vR) / (tL + tR);
+  double H = (tL * HL + tR * HR) / (tL + tR);
+  double csq = (gamma - 1.0) * (H - 0.5 * v * v);
+  double P = csq * rho / gamma;
+  double e = P / (gamma - 1.0) + 0.5 * rho * v * v;
+  ua[0] = rho;
+  ua[1] = rho * v;
+  ua[2] = e;
+}
+static void e1_eig(double *D, const double *u, double gamma) {
+  double rho = u[0], v = u[1] / rho, e = u[2];
+  double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+  double c = sqrt(gamma * P / rho);
+  D[0] = v;
+  D[1] = (v - c);
+  D[2] = (v + c);
+}
+static void e1_left(double *L, const double *u, double gamma) {
+  double rho = u[0], v = u[1] / rho, e = u[2];
+  double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+  double c = sqrt(gamma * P / rho);
+  L[1 * 3 + 0] = ((gamma - 1) / (rho * c)) * (-(v * v) / 2 - c * v / (gamma - 1));
+  L[1 * 3 + 1] = ((gamma - 1) / (rho * c)) * (v + c / (gamma - 1));
+  L[1 * 3 + 2] = ((gamma - 1) / (rho * c)) * (-1);
+  L[0 * 3 + 0] = ((gamma - 1) / (rho * c)) * (rho * (-(v * v) / 2 + c * c / (gamma - 1)) / c);
+  L[0 * 3 + 1] = ((gamma - 1) / (rho * c)) * (rho * v / c);
+  L[0 * 3 + 2] = ((gamma - 1) / (rho * c)) * (-rho / c);
+  L[2 * 3 + 0] = ((gamma - 1) / (rho * c)) * ((v * v) / 2 - c * v / (gamma - 1));
+  L[2 * 3 + 1] = ((gamma - 1) / (rho * c)) * (-v + c / (gamma - 1));
+  L[2 * 3 + 2] = ((gamma - 1) / (rho * c)) * (1);
+}
+static void e1_right(double *R, const double *u, double gamma) {
+  double rho = u[0], v = u[1] / rho, e = u[2];
+  double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+  double c = sqrt(gamma * P / rho);
+  R[0 * 3 + 1] = -rho / (2 * c);
+  R[1 * 3 + 1] = -rho * (v - c) / (2 * c);
+  R[2 * 3 + 1] = -rho * ((v * v) / 2 + (c * c) / (gamma - 1) - c * v) / (2 * c);
+  R[0 * 3 + 0] = 1;
+  R[1 * 3 + 0] = v;
+  R[2 * 3 + 0] = v * v / 2;
+  R[0 * 3 + 2] = rho / (2 * c);
+  R[1 * 3 + 2] = rho * (v + c) / (2 * c);
+  R[2 * 3 + 2] = rho * ((v * v) / 2 + (c * c) / (gamma - 1) + c * v) / (2 * c);
+}
+
+/* Euler2D -- include/physicalmodels/euler2d.h:44-230 */
+static void e2_flux(double *f, const double *u, int dir, double gamma) {
+  double rho = u[0], vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+  double vsq = (vx * vx) + (vy * vy);
+  double P = (e - 0.5 * rho * vsq) * (gamma - 1.0);
+  if (dir == 0) {
+    f[0] = rho * vx;
+    f[1] = rho * vx * vx + P;
+    f[2] = rho * vx * vy;
+    f[3] = (e + P) * vx;
+  } else {
+    f[0] = rho * vy;
+    f[1] = rho * vy * vx;
+    f[2] = rho * vy * vy + P;
+    f[3] = (e + P) * vy;
+  }
+}
+static void e2_roeavg(double *ua, const double *uL, const double *uR, double gamma) {
+  double rhoL = uL[0], vxL = uL[1] / rhoL, vyL = uL[2] / rhoL, eL = uL[3];
+  double vsqL = (vxL * vxL) + (vyL * vyL);
+  double PL = (eL - 0.5 * rhoL * vsqL) * (gamma - 1.0);
+  double cLsq = gamma * PL / rhoL;
+  double HL = 0.5 * (vxL * vxL + vyL * vyL) + cLsq / (gamma - 1.0);
+  double rhoR = uR[0], vxR = uR[1] / rhoR, vyR = uR[2] / rhoR, eR = uR[3];
+  double vsqR = (vxR * vxR) + (vyR * vyR);
+  double PR = (eR - 0.5 * rhoR * vsqR) * (gamma - 1.0);
+  double cRsq = gamma * PR / rhoR;
+  double HR = 0.5 * (vxR * vxR + vyR * vyR) + cRsq / (gamma - 1.0);
+  double tL = sqrt(rhoL), tR = sqrt(rhoR);
+  double rho = tL * tR;
+  double vx = (tL * vxL + tR * vxR) / (tL + tR);
+  double vy = (tL * vyL + tR * vyR) / (tL + tR);
+  double H = (tL * HL + tR * HR) / (tL + tR);
+  double vsq = vx * vx + vy * vy;
+  double csq = (gamma - 1.0) * (H - 0.5 * vsq);
+  double P = csq * rho / gamma;
+  double e = P / (gamma - 1.0) + 0.5 * rho * vsq;
+  ua[0] = rho;
+  ua[1] = rho * vx;
+  ua[2] = rho * vy;
+  ua[3] = e;
+}
+static void e2_eig(double *D, const double *u, int dir, double gamma) {
+  double rho = u[0], vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+  double vsq = (vx * vx) + (vy * vy);
+  double P = (e - 0.5 * rho * vsq) * (gamma - 1.0);
+  double c = sqrt(gamma * P / rho);
+  double vn = (dir == 0) ? vx : vy;
+  if (dir == 0) { D[0] = vn - c; D[1] = vn + c; D[2] = vn; D[3] = vn; }
+  else { D[0] = vn - c; D[1] = vn; D[2] = vn + c; D[3] = vn; }
+}
+static void e2_left(double *L, const double *u, int dir, double ga) {
+  double gm1 = ga - 1.0;
+  double rho = u[0], vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+  double vsq = (vx * vx) + (vy * vy);
+  double P = (e - 0.5 * rho * vsq) * (ga - 1.0);
+  double ek = 0.5 * (vx * vx + vy * vy);
+  double a = sqrt(ga * P / rho);
+  double nx = 0, ny = 0, un;
+  if (dir == 0) {
+    un = vx; nx = 1.0;
+    L[0 * 4 + 0] = (gm1 * ek + a * un) / (2 * a * a);
+    L[0 * 4 + 1] = ((-gm1) * vx - a * nx) / (2 * a * a);
+    L[0 * 4 + 2] = ((-gm1) * vy - a * ny) / (2 * a * a);
+    L[0 * 4 + 3] = gm1 / (2 * a * a);
+    L[3 * 4 + 0] = (a * a - gm1 * ek) / (a * a);
+    L[3 * 4 + 1] = (gm1 * vx) / (a * a);
+    L[3 * 4 + 2] = (gm1 * vy) / (a * a);
+    L[3 * 4 + 3] = (-gm1) / (a * a);
+    L[1 * 4 + 0] = (gm1 * ek - a * un) / (2 * a * a);
+    L[1 * 4 + 1] = ((-gm1) * vx + a * nx) / (2 * a * a);
+    L[1 * 4 + 2] = ((-gm1) * vy + a * ny) / (2 * a * a);
+    L[1 * 4 + 3] = gm1 / (2 * a * a);
+    L[2 * 4 + 0] = (vy - un * ny) / nx;
+    L[2 * 4 + 1] = ny;
+    L[2 * 4 + 2] = (ny * ny - 1.0) / nx;
+    L[2 * 4 + 3] = 0.0;
+  } else {
+    un = vy; ny = 1.0;
+    L[0 * 4 + 0] = (gm1 * ek + a * un) / (2 * a * a);
+    L[0 * 4 + 1] = ((1.0 - ga) * vx - a * nx) / (2 * a * a);
+    L[0 * 4 + 2] = ((1.0 - ga) * vy - a * ny) / (2 * a * a);
+    L[0 * 4 + 3] = gm1 / (2 * a * a);
+    L[3 * 4 + 0] = (a * a - gm1 * ek) / (a * a);
+    L[3 * 4 + 1] = gm1 * vx / (a * a);
+    L[3 * 4 + 2] = gm1 * vy / (a * a);
+    L[3 * 4 + 3] = (1.0 - ga) / (a * a);
+    L[2 * 4 + 0] = (gm1 * ek - a * un) / (2 * a * a);
+    L[2 * 4 + 1] = ((1.0 - ga) * vx + a * nx) / (2 * a * a);
+    L[2 * 4 + 2] = ((1.0 - ga) * vy + a * ny) / (2 * a * a);
+    L[2 * 4 + 3] = gm1 / (2 * a * a);
+    L[1 * 4 + 0] = (un * nx - vx) / ny;
+    L[1 * 4 + 1] = (1.0 - nx * nx) / ny;
+    L[1 * 4 + 2] = -nx;
+    L[1 * 4 + 3] = 0;
+  }
+}
+static void e2_right(double *R, const double *u, int dir, double ga) {
+  double gm1 = ga - 1.0;
+  double rho = u[0], vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+  double vsq = (vx * vx) + (vy * vy);
+  double P = (e - 0.5 * rho * vsq) * (ga - 1.0);
+  double ek = 0.5 * (vx * vx + vy * vy);
+  double a = sqrt(ga * P / rho);
+  double h0 = a * a / gm1 + ek;
+  double nx = 0, ny = 0, un;
+  if (dir == 0) {
+    un = vx; nx = 1.0;
+    R[0 * 4 + 0] = 1.0; R[1 * 4 + 0] = vx - a * nx; R[2 * 4 + 0] = vy - a * ny; R[3 * 4 + 0] = h0 - a * un;
+    R[0 * 4 + 3] = 1.0; R[1 * 4 + 3] = vx; R[2 * 4 + 3] = vy; R[3 * 4 + 3] = ek;
+    R[0 * 4 + 1] = 1.0; R[1 * 4 + 1] = vx + a * nx; R[2 * 4 + 1] = vy + a * ny; R[3 * 4 + 1] = h0 + a * un;
+    R[0 * 4 + 2] = 0.0; R[1 * 4 + 2] = ny; R[2 * 4 + 2] = -nx; R[3 * 4 + 2] = vx * ny - vy * nx;
+  } else {
+    un = vy; ny = 1.0;
+    R[0 * 4 + 0] = 1.0; R[1 * 4 + 0] = vx - a * nx; R[2 * 4 + 0] = vy - a * ny; R[3 * 4 + 0] = h0 - a * un;
+    R[0 * 4 + 3] = 1.0; R[1 * 4 + 3] = vx; R[2 * 4 + 3] = vy; R[3 * 4 + 3] = ek;
+    R[0 * 4 + 2] = 1.0; R[1 * 4 + 2] = vx + a * nx; R[2 * 4 + 2] = vy + a * ny; R[3 * 4 + 2] = h0 + a * un;
+    R[0 * 4 + 1] = 0; R[1 * 4 + 1] = ny; R[2 * 4 + 1] = -nx; R[3 * 4 + 1] = vx * ny - vy * nx;
+  }
+}
+
+/* NavierStokes3D -- include/physicalmodels/navierstokes3d.h:98-480 */
+#define NS_FLOWVAR(u, rho, vx, vy, vz, e, P, gamma)       \
+  do {                                                    \
+    double vsq_;                                          \
+    rho = (u)[0];                                         \
+    vx = (rho == 0) ? 0 : (u)[1] / rho;                   \
+    vy = (rho == 0) ? 0 : (u)[2] / rho;                   \
+    vz = (rho == 0) ? 0 : (u)[3] / rho;                   \
+    e = (u)[4];                                           \
+    vsq_ = vx * vx + vy * vy + vz * vz;                   \
+    P = (e - 0.5 * rho * vsq_) * (gamma - 1.0);           \
+  } while (0)
+
+static void ns_flux(double *f, const double *u, int dir, double gamma) {
+  double rho, vx, vy, vz, e, P;
+  NS_FLOWVAR(u, rho, vx, vy, vz, e, P, gamma);
+  if (dir == 0) {
+    f[0] = rho * vx; f[1] = rho * vx * vx + P; f[2] = rho * vx * vy; f[3] = rho * vx * vz; f[4] = (e + P) * vx;
+  } else if (dir == 1) {
+    f[0] = rho * vy; f[1] = rho * vy * vx; f[2] = rho * vy * vy + P; f[3] = rho * vy * vz; f[4] = (e + P) * vy;
+  } else {
+    f[0] = rho * vz; f[1] = rho * vz * vx; f[2] = rho * vz * vy; f[3] = rho * vz * vz + P; f[4] = (e + P) * vz;
+  }
+}
+static void ns_roeavg(double *ua, const double *uL, const double *uR, double gamma) {
+  double rho, vx, vy, vz, e, P, H;
+  double rhoL, vxL, vyL, vzL, eL, PL, HL, cLsq;
+  double rhoR, vxR, vyR, vzR, eR, PR, HR, cRsq;
+  NS_FLOWVAR(uL, rhoL, vxL, vyL, vzL, eL, PL, gamma);
+  cLsq = gamma * PL / rhoL;
+  HL = 0.5 * (vxL * vxL + vyL * vyL + vzL * vzL) + cLsq / (gamma - 1.0);
+  NS_FLOWVAR(uR, rhoR, vxR, vyR, vzR, eR, PR, gamma);
+  cRsq = gamma * PR / rhoR;
+  HR = 0.5 * (vxR * vxR + vyR * vyR + vzR * vzR) + cRsq / (gamma - 1.0);
+  double tL = sqrt(rhoL), tR = sqrt(rhoR);
+  rho = tL * tR;
+  vx = (tL * vxL + tR * vxR) / (tL + tR);
+  vy = (tL * vyL + tR * vyR) / (tL + tR);
+  vz = (tL * vzL + tR * vzR) / (tL + tR);
+  H = (tL * HL + tR * HR) / (tL + tR);
+  P = (H - 0.5 * (vx * vx + vy * vy + vz * vz)) * (rho * (gamma - 1.0)) / gamma;
+  e = P / (gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy + vz * vz);
+  ua[0] = rho; ua[1] = rho * vx; ua[2] = rho * vy; ua[3] = rho * vz; ua[4] = e;
+}
+static void ns_eig(double *D, const double *u, int dir, double gamma) {
+  double rho, vx, vy, vz, e, P;
+  NS_FLOWVAR(u, rho, vx, vy, vz, e, P, gamma);
+  double c = sqrt(gamma * P / rho);
+  if (dir == 0) { D[0] = vx; D[1] = vx - c; D[2] = vx; D[3] = vx; D[4] = vx + c; }
+  else if (dir == 1) { D[0] = vy; D[1] = vy; D[2] = vy - c; D[3] = vy; D[4] = vy + c; }
+  else { D[0] = vz; D[1] = vz; D[2] = vz; D[3] = vz - c; D[4] = vz + c; }
+}
+static void ns_left(double *L, const double *u, int dir, double ga) {
+  double gm1 = ga - 1.0;
+  double rho, vx, vy, vz, e, P, a, ek;
+  NS_FLOWVAR(u, rho, vx, vy, vz, e, P, ga);
+  ek = 0.5 * (vx * vx + vy * vy + vz * vz);
+  a = sqrt(ga * P / rho);
+  if (dir == 0) {
+    L[1 * 5 + 0] = (gm1 * ek + a * vx) / (2 * a * a);
+    L[1 * 5 + 1] = ((-gm1) * vx - a) / (2 * a * a);
+    L[1 * 5 + 2] = ((-gm1) * vy) / (2 * a * a);
+    L[1 * 5 + 3] = ((-gm1) * vz) / (2 * a * a);
+    L[1 * 5 + 4] = gm1 / (2 * a * a);
+    L[0 * 5 + 0] = (a * a - gm1 * ek) / (a * a);
+    L[0 * 5 + 1] = (gm1 * vx) / (a * a);
+    L[0 * 5 + 2] = (gm1 * vy) / (a * a);
+    L[0 * 5 + 3] = (gm1 * vz) / (a * a);
+    L[0 * 5 + 4] = (-gm1) / (a * a);
+    L[4 * 5 + 0] = (gm1 * ek - a * vx) / (2 * a * a);
+    L[4 * 5 + 1] = ((-gm1) * vx + a) / (2 * a * a);
+    L[4 * 5 + 2] = ((-gm1) * vy) / (2 * a * a);
+    L[4 * 5 + 3] = ((-gm1) * vz) / (2 * a * a);
+    L[4 * 5 + 4] = gm1 / (2 * a * a);
+    L[2 * 5 + 0] = vy; L[2 * 5 + 1] = 0.0; L[2 * 5 + 2] = -1.0; L[2 * 5 + 3] = 0.0; L[2 * 5 + 4] = 0.0;
+    L[3 * 5 + 0] = -vz; L[3 * 5 + 1] = 0.0; L[3 * 5 + 2] = 0.0; L[3 * 5 + 3] = 1.0; L[3 * 5 + 4] = 0.0;
+  } else if (dir == 1) {
+    L[2 * 5 + 0] = (gm1 * ek + a * vy) / (2 * a * a);
+    L[2 * 5 + 1] = ((1.0 - ga) * vx) / (2 * a * a);
+    L[2 * 5 + 2] = ((1.0 - ga) * vy - a) / (2 * a * a);
+    L[2 * 5 + 3] = ((1.0 - ga) * vz) / (2 * a * a);
+    L[2 * 5 + 4] = gm1 / (2 * a * a);
+    L[0 * 5 + 0] = (a * a - gm1 * ek) / (a * a);
+    L[0 * 5 + 1] = gm1 * vx / (a * a);
+    L[0 * 5 + 2] = gm1 * vy / (a * a);
+    L[0 * 5 + 3] = gm1 * vz / (a * a);
+    L[0 * 5 + 4] = (1.0 - ga) / (a * a);
+    L[4 * 5 + 0] = (gm1 * ek - a * vy) / (2 * a * a);
+    L[4 * 5 + 1] = ((1.0 - ga) * vx) / (2 * a * a);
+    L[4 * 5 + 2] = ((1.0 - ga) * vy + a) / (2 * a * a);
+    L[4 * 5 + 3] = ((1.0 - ga) * vz) / (2 * a * a);
+    L[4 * 5 + 4] = gm1 / (2 * a * a);
+    L[1 * 5 + 0] = -vx; L[1 * 5 + 1] = 1.0; L[1 * 5 + 2] = 0.0; L[1 * 5 + 3] = 0.0; L[1 * 5 + 4] = 0;
+    L[3 * 5 + 0] = vz; L[3 * 5 + 1] = 0.0; L[3 * 5 + 2] = 0.0; L[3 * 5 + 3] = -1.0; L[3 * 5 + 4] = 0;
+  } else {
+    L[3 * 5 + 0] = (gm1 * ek + a * vz) / (2 * a * a);
+    L[3 * 5 + 1] = ((1.0 - ga) * vx) / (2 * a * a);
+    L[3 * 5 + 2] = ((1.0 - ga) * vy) / (2 * a * a);
+    L[3 * 5 + 3] = ((1.0 - ga) * vz - a) / (2 * a * a);
+    L[3 * 5 + 4] = gm1 / (2 * a * a);
+    L[0 * 5 + 0] = (a * a - gm1 * ek) / (a * a);
+    L[0 * 5 + 1] = gm1 * vx / (a * a);
+    L[0 * 5 + 2] = gm1 * vy / (a * a);
+    L[0 * 5 + 3] = gm1 * vz / (a * a);
+    L[0 * 5 + 4] = (1.0 - ga) / (a * a);
+    L[4 * 5 + 0] = (gm1 * ek - a * vz) / (2 * a * a);
+    L[4 * 5 + 1] = ((1.0 - ga) * vx) / (2 * a * a);
+    L[4 * 5 + 2] = ((1.0 - ga) * vy) / (2 * a * a);
+    L[4 * 5 + 3] = ((1.0 - ga) * vz + a) / (2 * a * a);
+    L[4 * 5 + 4] = gm1 / (2 * a * a);
+    L[1 * 5 + 0] = vx; L[1 * 5 + 1] = -1.0; L[1 * 5 + 2] = 0.0; L[1 * 5 + 3] = 0.0; L[1 * 5 + 4] = 0;
+    L[2 * 5 + 0] = -vy; L[2 * 5 + 1] = 0.0; L[2 * 5 + 2] = 1.0; L[2 * 5 + 3] = 0.0; L[2 * 5 + 4] = 0;
+  }
+}
+static void ns_right(double *R, const double *u, int dir, double ga) {
+  double gm1 = ga - 1.0;
+  double rho, vx, vy, vz, e, P, ek, a, h0;
+  NS_FLOWVAR(u, rho, vx, vy, vz, e, P, ga);
+  ek = 0.5 * (vx * vx + vy * vy + vz * vz);
+  a = sqrt(ga * P / rho);
+  h0 = a * a / gm1 + ek;
+#define RR(r, c) R[(r) * 5 + (c)]
+  if (dir == 0) {
+    RR(0, 1) = 1.0; RR(1, 1) = vx - a; RR(2, 1) = vy; RR(3, 1) = vz; RR(4, 1) = h0 - a * vx;
+    RR(0, 0) = 1.0; RR(1, 0) = vx; RR(2, 0) = vy; RR(3, 0) = vz; RR(4, 0) = ek;
+    RR(0, 4) = 1.0; RR(1, 4) = vx + a; RR(2, 4) = vy; RR(3, 4) = vz; RR(4, 4) = h0 + a * vx;
+    RR(0, 2) = 0.0; RR(1, 2) = 0.0; RR(2, 2) = -1.0; RR(3, 2) = 0.0; RR(4, 2) = -vy;
+    RR(0, 3) = 0.0; RR(1, 3) = 0.0; RR(2, 3) = 0.0; RR(3, 3) = 1.0; RR(4, 3) = vz;
+  } else if (dir == 1) {
+    RR(0, 2) = 1.0; RR(1, 2) = vx; RR(2, 2) = vy - a; RR(3, 2) = vz; RR(4, 2) = h0 - a * vy;
+    RR(0, 0) = 1.0; RR(1, 0) = vx; RR(2, 0) = vy; RR(3, 0) = vz; RR(4, 0) = ek;
+    RR(0, 4) = 1.0; RR(1, 4) = vx; RR(2, 4) = vy + a; RR(3, 4) = vz; RR(4, 4) = h0 + a * vy;
+    RR(0, 1) = 0.0; RR(1, 1) = 1.0; RR(2, 1) = 0.0; RR(3, 1) = 0.0; RR(4, 1) = vx;
+    RR(0, 3) = 0.0; RR(1, 3) = 0.0; RR(2, 3) = 0.0; RR(3, 3) = -1.0; RR(4, 3) = -vz;
+  } else {
+    RR(0, 3) = 1.0; RR(1, 3) = vx; RR(2, 3) = vy; RR(3, 3) = vz - a; RR(4, 3) = h0 - a * vz;
+    RR(0, 0) = 1.0; RR(1, 0) = vx; RR(2, 0) = vy; RR(3, 0) = vz; RR(4, 0) = ek;
+    RR(0, 4) = 1.0; RR(1, 4) = vx; RR(2, 4) = vy; RR(3, 4) = vz + a; RR(4, 4) = h0 + a * vz;
+    RR(0, 1) = 0.0; RR(1, 1) = -1.0; RR(2, 1) = 0.0; RR(3, 1) = 0.0; RR(4, 1) = -vx;
+    RR(0, 2) = 0.0; RR(1, 2) = 0.0; RR(2, 2) = 1.0; RR(3, 2) = 0.0; RR(4, 2) = vy;
+  }
+#undef RR
+}
+
+/* Model dispatch. */
+static void m_flux(const orc_problem *p, double *f, const double *u, int dir) {
+  if (p->model == ORC_EULER1D) e1_flux(f, u, p->gamma);
+  else if (p->model == ORC_EULER2D) e2_flux(f, u, dir, p->gamma);
+  else ns_flux(f, u, dir, p->gamma);
+}
+static void m_roeavg(const orc_problem *p, double *ua, const double *uL, const double *uR) {
+  if (p->model == ORC_EULER1D) e1_roeavg(ua, uL, uR, p->gamma);
+  else if (p->model == ORC_EULER2D) e2_roeavg(ua, uL, uR, p->gamma);
+  else ns_roeavg(ua, uL, uR, p->gamma);
+}
+static void m_eig(const orc_problem *p, double *D, const double *u, int dir) {
+  if (p->model == ORC_EULER1D) e1_eig(D, u, p->gamma);
+  else if (p->model == ORC_EULER2D) e2_eig(D, u, dir, p->gamma);
+  else ns_eig(D, u, dir, p->gamma);
+}
+static void m_left(const orc_problem *p, double *L, const double *u, int dir) {
+  if (p->model == ORC_EULER1D) e1_left(L, u, p->gamma);
+  else if (p->model == ORC_EULER2D) e2_left(L, u, dir, p->gamma);
+  else ns_left(L, u, dir, p->gamma);
+}
+static void m_right(const orc_problem *p, double *R, const double *u, int dir) {
+  if (p->model == ORC_EULER1D) e1_right(R, u, p->gamma);
+  else if (p->model == ORC_EULER2D) e2_right(R, u, dir, p->gamma);
+  else ns_right(R, u, dir, p->gamma);
+}
+
+/* UFunction: Euler1D u*(1/grav_field) with grav_field = exp(0) = 1
+ * (Euler1DModifiedSolution.c:23-50); NavierStokes3D recomputes the energy
+ * (NavierStokes3DModifiedSolution.c:31-70) with f = g = 1 at zero gravity;
+ * Euler2D has none (uC = u). */
+static void m_ufunc(const orc_problem *p, double *uC, const double *u) {
+  int nv = p->nvars;
+  if (p->model == ORC_NS3D) {
+    double inv_gamma_m1 = 1.0 / (p->gamma - 1.0);
+    double rho, uvel, vvel, wvel, E, P;
+    NS_FLOWVAR(u, rho, uvel, vvel, wvel, E, P, p->gamma);
+    (void)E;
+    uC[0] = u[0] * 1.0;
+    uC[1] = u[1] * 1.0;
+    uC[2] = u[2] * 1.0;
+    uC[3] = u[3] * 1.0;
+    uC[4] = (P * inv_gamma_m1) * (1.0 / 1.0) + (0.5 * rho * (uvel * uvel + vvel * vvel + wvel * wvel)) * 1.0;
+  } else if (p->model == ORC_EULER1D) {
+    for (int v = 0; v < nv; v++) uC[v] = u[v] * (1.0 / 1.0);
+  } else {
+    for (int v = 0; v < nv; v++) uC[v] = u[v];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* WENO5 (Jiang-Shu weights)                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* _WENOWeights_v_JS_ (include/interpolation.h:265-285), one component. */
+static inline void weno_js(double m3, double m2, double m1, double p1, double p2, double eps,
+                           double *w1, double *w2, double *w3) {
+  static const double thirteen_by_twelve = 13.0 / 12.0;
+  static const double one_fourth = 1.0 / 4.0;
+  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  double b1, b2, b3, a1, a2, a3, a_sum_inv;
+  b1 = thirteen_by_twelve * (m3 - 2 * m2 + m1) * (m3 - 2 * m2 + m1)
+       + one_fourth * (m3 - 4 * m2 + 3 * m1) * (m3 - 4 * m2 + 3 * m1);
+  a1 = c1 / ((b1 + eps) * (b1 + eps));
+  b2 = thirteen_by_twelve * (m2 - 2 * m1 + p1) * (m2 - 2 * m1 + p1)
+       + one_fourth * (m2 - p1) * (m2 - p1);
+  a2 = c2 / ((b2 + eps) * (b2 + eps));
+  b3 = thirteen_by_twelve * (m1 - 2 * p1 + p2) * (m1 - 2 * p1 + p2)
+       + one_fourth * (3 * m1 - 4 * p1 + p2) * (3 * m1 - 4 * p1 + p2);
+  a3 = c3 / ((b3 + eps) * (b3 + eps));
+  a_sum_inv = 1.0 / (a1 + a2 + a3);
+  *w1 = a1 * a_sum_inv;
+  *w2 = a2 * a_sum_inv;
+  *w3 = a3 * a_sum_inv;
+}
+
+/* Interp1PrimFifthOrderWENO (Interp1PrimFifthOrderWENO.c:143-158), one component. */
+static inline double weno_interp(double w1, double w2, double w3, double fm3, double fm2,
+                                 double fm1, double fp1, double fp2) {
+  static const double one_sixth = 1.0 / 6.0;
+  double f1 = (2 * one_sixth) * fm3 + (-7 * one_sixth) * fm2 + (11 * one_sixth) * fm1;
+  double f2 = (-one_sixth) * fm2 + (5 * one_sixth) * fm1 + (2 * one_sixth) * fp1;
+  double f3 = (2 * one_sixth) * fm1 + (5 * one_sixth) * fp1 + (-one_sixth) * fp2;
+  return w1 * f1 + w2 * f2 + w3 * f3;
+}
+
+/* Interp1PrimFifthOrderWENOChar (Interp1PrimFifthOrderWENOChar.c:170-188): the
+ * characteristic candidate stencils and their weighted sum. */
+static inline double weno_interp_char(double w1, double w2, double w3, double fm3, double fm2,
+                                      double fm1, double fp1, double fp2) {
+  static const double one_sixth = 1.0 / 6.0;
+  double f1 = (2 * one_sixth) * fm3 - (7.0 * one_sixth) * fm2 + (11.0 * one_sixth) * fm1;
+  double f2 = (-one_sixth) * fm2 + (5.0 * one_sixth) * fm1 + (2 * one_sixth) * fp1;
+  double f3 = (2 * one_sixth) * fm1 + (5 * one_sixth) * fp1 - (one_sixth) * fp2;
+  return w1 * f1 + w2 * f2 + w3 * f3;
+}
+
+/* MatVecMult (include/matmult_native.h:116-123): y = A x, sums from zero. */
+static inline void matvec(int n, double *y, const double *A, const double *x) {
+  for (int i = 0; i < n; i++) {
+    y[i] = 0;
+    for (int j = 0; j < n; j++) y[i] += A[i * n + j] * x[j];
+  }
+}
+/* MatMult (include/matmult_native.h:18-27). */
+static inline void matmul(int n, double *C, const double *X, const double *Y) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) {
+      C[i * n + j] = 0.0;
+      for (int k = 0; k < n; k++) C[i * n + j] += X[i * n + k] * Y[k * n + j];
+    }
+}
+
+#define absolute(a) ((a) < 0 ? -(a) : (a))
+#define max2(a, b) ((a) > (b) ? (a) : (b))
+#define max3(a, b, c) max2(max2((a), (b)), max2((b), (c)))
+
+/* ------------------------------------------------------------------------ */
+/* Upwinding (one interface)                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* fI from fL,fR,uL,uR and the cell-centre states uCL (cell left of the
+ * interface) and uCR (right).  Roe: Euler1DUpwindRoe (Euler1DUpwind.c:30-113),
+ * Euler2DUpwindRoe (Euler2DUpwind.c:10-66), NavierStokes3DUpwindRoe
+ * (NavierStokes3DUpwind.c:40-139).  LLF: Euler1DUpwindLLF (Euler1DUpwind.c:212-290),
+ * Euler2DUpwindLLF (Euler2DUpwind.c:139-210), NavierStokes3DUpwindLLF
+ * (NavierStokes3DUpwind.c:244-318).  RF: Euler2DUpwindRF (Euler2DUpwind.c:68-137),
+ * and the same form for Euler1D/NavierStokes3D. */
+static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, const double *fR,
+                   const double *uL, const double *uR, const double *uCL, const double *uCR) {
+  int nv = p->nvars;
+  double uavg[MAXV], D[MAXV], L[MAXV * MAXV], R[MAXV * MAXV];
+  if (p->upwind == ORC_UPW_ROE) {
+    double udiff[MAXV], DL[MAXV * MAXV], modA[MAXV * MAXV], udiss[MAXV];
+    for (int v = 0; v < nv; v++) udiff[v] = 0.5 * (uR[v] - uL[v]);
+    if (p->model == ORC_EULER2D) m_roeavg(p, uavg, uL, uR);
+    else m_roeavg(p, uavg, uCL, uCR);
+    m_eig(p, D, uavg, dir);
+    m_left(p, L, uavg, dir);
+    m_right(p, R, uavg, dir);
+    if (p->model == ORC_EULER1D) {
+      double kappa = max2(1.0, 1.0);
+      for (int k = 0; k < nv; k++) D[k] = kappa * absolute(D[k]);
+    } else {
+      double delta = 0.000001, delta2 = delta * delta;
+      for (int k = 0; k < nv; k++)
+        D[k] = (absolute(D[k]) < delta ? (D[k] * D[k] + delta2) / (2 * delta) : absolute(D[k]));
+    }
+    double Dm[MAXV * MAXV];
+    for (int i = 0; i < nv * nv; i++) Dm[i] = 0;
+    for (int k = 0; k < nv; k++) Dm[k * nv + k] = D[k];
+    matmul(nv, DL, Dm, L);
+    matmul(nv, modA, R, DL);
+    matvec(nv, udiss, modA, udiff);
+    for (int v = 0; v < nv; v++) fI[v] = 0.5 * (fL[v] + fR[v]) - udiss[v];
+  } else {
+    double fcL[MAXV], fcR[MAXV], ucL[MAXV], ucR[MAXV], fc[MAXV];
+    double eigL[MAXV], eigC[MAXV], eigR[MAXV];
+    int cellcentre = (p->model == ORC_EULER1D);
+    if (cellcentre) m_roeavg(p, uavg, uCL, uCR);
+    else m_roeavg(p, uavg, uL, uR);
+    m_left(p, L, uavg, dir);
+    m_right(p, R, uavg, dir);
+    matvec(nv, ucL, L, uL);
+    matvec(nv, ucR, L, uR);
+    matvec(nv, fcL, L, fL);
+    matvec(nv, fcR, L, fR);
+    m_eig(p, eigL, cellcentre ? uCL : uL, dir);
+    m_eig(p, eigR, cellcentre ? uCR : uR, dir);
+    m_eig(p, eigC, uavg, dir);
+    for (int k = 0; k < nv; k++) {
+      if (p->upwind == ORC_UPW_RF) {
+        if ((eigL[k] > 0) && (eigC[k] > 0) && (eigR[k] > 0)) { fc[k] = fcL[k]; continue; }
+        if ((eigL[k] < 0) && (eigC[k] < 0) && (eigR[k] < 0)) { fc[k] = fcR[k]; continue; }
+      }
+      double alpha = max3(absolute(eigL[k]), absolute(eigC[k]), absolute(eigR[k]));
+      if (p->model == ORC_EULER1D && p->upwind == ORC_UPW_LLF) alpha = 1.0 * alpha;
+      fc[k] = 0.5 * (fcL[k] + fcR[k] + alpha * (ucL[k] - ucR[k]));
+    }
+    matvec(nv, fI, R, fc);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Hyperbolic term                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* HyperbolicFunction (src/HyParFunctions/HyperbolicFunction.c:31-126) with
+ * ReconstructHyperbolic (:167-222): per dimension, the cell flux, the WENO
+ * weights from (fC, u) (WENOFifthOrderCalculateWeights.c:111-236 / :760-896),
+ * uC = UFunction(u), the four interpolations, upwinding, and
+ * hyp += dxinv*(F[j+1/2]-F[j-1/2]) accumulated dimension by dimension. */
+int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
+  int nd = p->ndims, nv = p->nvars, g = p->ghosts;
+  long s[3];
+  strides_wg(p, s);
+  long np = orc_npoints_wghosts(p);
+  for (long i = 0; i < np * nv; i++) hyp[i] = 0.0;
+  double *fC = (double *)malloc(sizeof(double) * np * nv);
+  double *uC = (double *)malloc(sizeof(double) * np * nv);
+  long offset = 0;
+  for (int d = 0; d < nd; d++) {
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+    for (long q = 0; q < np; q++) {
+      m_flux(p, fC + nv * q, u + nv * q, d);
+      m_ufunc(p, uC + nv * q, u + nv * q);
+    }
+    int N = p->dim[d];
+    long sd = s[d];
+    long nouter = 1;
+    int ob[3] = {1, 1, 1};
+    for (int e = 0; e < nd; e++) if (e != d) { ob[e] = p->dim[e]; nouter *= p->dim[e]; }
+    const double *dxinv = p->dxinv + offset;
+#pragma omp parallel num_threads(NTHR)
+    {
+      double *FI = (double *)malloc(sizeof(double) * (N + 1) * nv);
+#pragma omp for schedule(static)
+      for (long lo = 0; lo < nouter; lo++) {
+        int idx[3] = {0, 0, 0};
+        long r = lo;
+        for (int e = 0; e < nd; e++) if (e != d) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
+        idx[d] = 0;
+        long base = pidx(p, s, idx); /* cell 0 of this line */
+        for (int I = 0; I <= N; I++) {
+          long qm1L = base + (long)(I - 1) * sd, qm1R = base + (long)I * sd;
+          long L3 = qm1L - 2 * sd, L2 = qm1L - sd, L1 = qm1L, L4 = qm1L + sd, L5 = qm1L + 2 * sd;
+          long R3 = qm1R + 2 * sd, R2 = qm1R + sd, R1 = qm1R, R4 = qm1R - sd, R5 = qm1R - 2 * sd;
+          double fL[MAXV], fR[MAXV], uL[MAXV], uR[MAXV];
+          if (p->interp == ORC_INTERP_COMP) {
+            for (int v = 0; v < nv; v++) {
+              double w1, w2, w3;
+              weno_js(fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
+              fL[v] = weno_interp(w1, w2, w3, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v]);
+              weno_js(fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v], p->eps, &w1, &w2, &w3);
+              fR[v] = weno_interp(w1, w2, w3, fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v]);
+              weno_js(u[nv * L3 + v], u[nv * L2 + v], u[nv * L1 + v], u[nv * L4 + v], u[nv * L5 + v], p->eps, &w1, &w2, &w3);
+              uL[v] = weno_interp(w1, w2, w3, uC[nv * L3 + v], uC[nv * L2 + v], uC[nv * L1 + v], uC[nv * L4 + v], uC[nv * L5 + v]);
+              weno_js(u[nv * R3 + v], u[nv * R2 + v], u[nv * R1 + v], u[nv * R4 + v], u[nv * R5 + v], p->eps, &w1, &w2, &w3);
+              uR[v] = weno_interp(w1, w2, w3, uC[nv * R3 + v], uC[nv * R2 + v], uC[nv * R1 + v], uC[nv * R4 + v], uC[nv * R5 + v]);
+            }
+          } else {
+            double uavg[MAXV], L[MAXV * MAXV], R[MAXV * MAXV];
+            m_roeavg(p, uavg, u + nv * qm1L, u + nv * qm1R);
+            m_left(p, L, uavg, d);
+            m_right(p, R, uavg, d);
+            long sl[5] = {L3, L2, L1, L4, L5}, sr[5] = {R3, R2, R1, R4, R5};
+            double cfl[5][MAXV], cfr[5][MAXV], cul[5][MAXV], cur[5][MAXV];  /* weights' stencils */
+            double ifl[5][MAXV], ifr[5][MAXV], iul[5][MAXV], iur[5][MAXV];  /* interpolants' stencils */
+            for (int k = 0; k < 5; k++) {
+              matvec(nv, cfl[k], L, fC + nv * sl[k]);
+              matvec(nv, cfr[k], L, fC + nv * sr[k]);
+              matvec(nv, cul[k], L, u + nv * sl[k]);
+              matvec(nv, cur[k], L, u + nv * sr[k]);
+              matvec(nv, ifl[k], L, fC + nv * sl[k]);
+              matvec(nv, ifr[k], L, fC + nv * sr[k]);
+              matvec(nv, iul[k], L, uC + nv * sl[k]);
+              matvec(nv, iur[k], L, uC + nv * sr[k]);
+            }
+            double xfl[MAXV], xfr[MAXV], xul[MAXV], xur[MAXV];
+            for (int v = 0; v < nv; v++) {
+              double w1, w2, w3;
+              weno_js(cfl[0][v], cfl[1][v], cfl[2][v], cfl[3][v], cfl[4][v], p->eps, &w1, &w2, &w3);
+              xfl[v] = weno_interp_char(w1, w2, w3, ifl[0][v], ifl[1][v], ifl[2][v], ifl[3][v], ifl[4][v]);
+              weno_js(cfr[0][v], cfr[1][v], cfr[2][v], cfr[3][v], cfr[4][v], p->eps, &w1, &w2, &w3);
+              xfr[v] = weno_interp_char(w1, w2, w3, ifr[0][v], ifr[1][v], ifr[2][v], ifr[3][v], ifr[4][v]);
+              weno_js(cul[0][v], cul[1][v], cul[2][v], cul[3][v], cul[4][v], p->eps, &w1, &w2, &w3);
+              xul[v] = weno_interp_char(w1, w2, w3, iul[0][v], iul[1][v], iul[2][v], iul[3][v], iul[4][v]);
+              weno_js(cur[0][v], cur[1][v], cur[2][v], cur[3][v], cur[4][v], p->eps, &w1, &w2, &w3);
+              xur[v] = weno_interp_char(w1, w2, w3, iur[0][v], iur[1][v], iur[2][v], iur[3][v], iur[4][v]);
+            }
+            matvec(nv, fL, R, xfl);
+            matvec(nv, fR, R, xfr);
+            matvec(nv, uL, R, xul);
+            matvec(nv, uR, R, xur);
+          }
+          upwind(p, d, FI + (long)I * nv, fL, fR, uL, uR, u + nv * qm1L, u + nv * qm1R);
+        }
+        for (int i = 0; i < N; i++) {
+          long q = base + (long)i * sd;
+          for (int v = 0; v < nv; v++)
+            hyp[nv * q + v] += dxinv[g + i] * (FI[(long)(i + 1) * nv + v] - FI[(long)i * nv + v]);
+        }
+      }
+      free(FI);
+    }
+    offset += p->dim[d] + 2 * g;
+  }
+  free(fC);
+  free(uC);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* NavierStokes3D viscous term                                               */
+/* ------------------------------------------------------------------------ */
+
+/* FirstDerivativeFourthOrderCentral (src/FirstDerivative/FirstDerivativeFourthOrder.c:36-129):
+ * lines along dir over the full ghost extent, for interior transverse indices only. */
+static void deriv4(const orc_problem *p, double *Df, const double *f, int dir) {
+  int nd = p->ndims, nv = p->nvars, g = p->ghosts;
+  long s[3];
+  strides_wg(p, s);
+  static const double one_twelve = 1.0 / 12.0;
+  int N = p->dim[dir];
+  long sd = s[dir];
+  long nouter = 1;
+  int ob[3] = {1, 1, 1};
+  for (int e = 0; e < nd; e++) if (e != dir) { ob[e] = p->dim[e]; nouter *= p->dim[e]; }
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+  for (long lo = 0; lo < nouter; lo++) {
+    int idx[3] = {0, 0, 0};
+    long r = lo;
+    for (int e = 0; e < nd; e++) if (e != dir) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
+    idx[dir] = -g;
+    long b = pidx(p, s, idx); /* first ghost point of the line */
+    for (int i = -g; i < N + g; i++) {
+      long qC = b + (long)(i + g) * sd;
+      for (int v = 0; v < nv; v++) {
+        double val;
+#define F(k) f[(qC + (long)(k) * sd) * nv + v]
+        if (i == -g)
+          val = (-25 * F(0) + 48 * F(1) - 36 * F(2) + 16 * F(3) - 3 * F(4)) * one_twelve;
+        else if (i == -g + 1)
+          val = (-3 * F(-1) - 10 * F(0) + 18 * F(1) - 6 * F(2) + F(3)) * one_twelve;
+        else if (i < N + g - 2)
+          val = (F(-2) - 8 * F(-1) + 8 * F(1) - F(2)) * one_twelve;
+        else if (i == N + g - 2)
+          val = (-F(-3) + 6 * F(-2) - 18 * F(-1) + 10 * F(0) + 3 * F(1)) * one_twelve;
+        else
+          val = (3 * F(-4) - 16 * F(-3) + 36 * F(-2) - 48 * F(-1) + 25 * F(0)) * one_twelve;
+#undef F
+        Df[qC * nv + v] = val;
+      }
+    }
+  }
+}
+
+/* NavierStokes3DParabolicFunction (NavierStokes3DParabolicFunction.c:50-325),
+ * including its single-rank behaviour: derivative arrays start at zero and are
+ * filled only on lines with interior transverse indices, so cross derivatives
+ * at ghost points stay zero. */
+int orc_parabolic(const orc_problem *p, const double *u, double *par) {
+  long np = orc_npoints_wghosts(p);
+  int nv = p->nvars, g = p->ghosts;
+  for (long i = 0; i < np * nv; i++) par[i] = 0.0;
+  if (p->model != ORC_NS3D || p->Re <= 0) return 0;
+  static const double two_third = 2.0 / 3.0;
+  double inv_gamma_m1 = 1.0 / (p->gamma - 1.0);
+  double inv_Re = 1.0 / p->Re;
+  double inv_Pr = 1.0 / p->Pr;
+  double *Q = (double *)calloc(np * nv, sizeof(double));
+  double *QX = (double *)calloc(np * nv, sizeof(double));
+  double *QY = (double *)calloc(np * nv, sizeof(double));
+  double *QZ = (double *)calloc(np * nv, sizeof(double));
+  double *FV = (double *)calloc(np * nv, sizeof(double));
+  double *FD = (double *)calloc(np * nv, sizeof(double));
+  int imax = p->dim[0], jmax = p->dim[1], kmax = p->dim[2];
+  long s[3];
+  strides_wg(p, s);
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+  for (long q = 0; q < np; q++) {
+    double energy, pressure;
+    double *Qp = Q + q * nv;
+    NS_FLOWVAR(u + q * nv, Qp[0], Qp[1], Qp[2], Qp[3], energy, pressure, p->gamma);
+    (void)energy;
+    Qp[4] = p->gamma * pressure / Qp[0];
+  }
+  deriv4(p, QX, Q, 0);
+  deriv4(p, QY, Q, 1);
+  deriv4(p, QZ, Q, 2);
+  const double *dxi = p->dxinv, *dyi = p->dxinv + imax + 2 * g, *dzi = dyi + jmax + 2 * g;
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+  for (int k = -g; k < kmax + g; k++)
+    for (int j = -g; j < jmax + g; j++)
+      for (int i = -g; i < imax + g; i++) {
+        long q = ((long)(i + g) * s[0] + (long)(j + g) * s[1] + (long)(k + g) * s[2]) * nv;
+        for (int v = 0; v < nv; v++) {
+          QX[q + v] *= dxi[i + g];
+          QY[q + v] *= dyi[j + g];
+          QZ[q + v] *= dzi[k + g];
+        }
+      }
+  for (int dir = 0; dir < 3; dir++) {
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+    for (long q = 0; q < np; q++) {
+      const double *Qp = Q + q * nv, *X = QX + q * nv, *Y = QY + q * nv, *Z = QZ + q * nv;
+      double *Fv = FV + q * nv;
+      double uvel = Qp[1], vvel = Qp[2], wvel = Qp[3], T = Qp[4];
+      double mu = exp(0.76 * log(T));
+      if (dir == 0) {
+        double Tx = X[4], ux = X[1], vx = X[2], wx = X[3], uy = Y[1], vy = Y[2], uz = Z[1], wz = Z[3];
+        double tau_xx = two_third * (mu * inv_Re) * (2 * ux - vy - wz);
+        double tau_xy = (mu * inv_Re) * (uy + vx);
+        double tau_xz = (mu * inv_Re) * (uz + wx);
+        double qx = (mu * inv_Re * inv_gamma_m1 * inv_Pr) * Tx;
+        Fv[0] = 0.0; Fv[1] = tau_xx; Fv[2] = tau_xy; Fv[3] = tau_xz;
+        Fv[4] = uvel * tau_xx + vvel * tau_xy + wvel * tau_xz + qx;
+      } else if (dir == 1) {
+        double Ty = Y[4], ux = X[1], vx = X[2], uy = Y[1], vy = Y[2], wy = Y[3], vz = Z[2], wz = Z[3];
+        double tau_yx = (mu * inv_Re) * (uy + vx);
+        double tau_yy = two_third * (mu * inv_Re) * (-ux + 2 * vy - wz);
+        double tau_yz = (mu * inv_Re) * (vz + wy);
+        double qy = (mu * inv_Re * inv_gamma_m1 * inv_Pr) * Ty;
+        Fv[0] = 0.0; Fv[1] = tau_yx; Fv[2] = tau_yy; Fv[3] = tau_yz;
+        Fv[4] = uvel * tau_yx + vvel * tau_yy + wvel * tau_yz + qy;
+      } else {
+        double Tz = Z[4], ux = X[1], wx = X[3], vy = Y[2], wy = Y[3], uz = Z[1], vz = Z[2], wz = Z[3];
+        double tau_zx = (mu * inv_Re) * (uz + wx);
+        double tau_zy = (mu * inv_Re) * (vz + wy);
+        double tau_zz = two_third * (mu * inv_Re) * (-ux - vy + 2 * wz);
+        double qz = (mu * inv_Re * inv_gamma_m1 * inv_Pr) * Tz;
+        Fv[0] = 0.0; Fv[1] = tau_zx; Fv[2] = tau_zy; Fv[3] = tau_zz;
+        Fv[4] = uvel * tau_zx + vvel * tau_zy + wvel * tau_zz + qz;
+      }
+    }
+    deriv4(p, FD, FV, dir);
+    const double *di = (dir == 0) ? dxi : (dir == 1 ? dyi : dzi);
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+    for (int k = 0; k < kmax; k++)
+      for (int j = 0; j < jmax; j++)
+        for (int i = 0; i < imax; i++) {
+          long q = ((long)(i + g) * s[0] + (long)(j + g) * s[1] + (long)(k + g) * s[2]) * nv;
+          int id = (dir == 0) ? i : (dir == 1 ? j : k);
+          double dinv = di[id + g];
+          for (int v = 0; v < nv; v++) par[q + v] += (dinv * FD[q + v]);
+        }
+  }
+  free(Q); free(QX); free(QY); free(QZ); free(FV); free(FD);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RHS and RK                                                                */
+/* ------------------------------------------------------------------------ */
+
+/* TimeRHSFunctionExplicit (src/TimeIntegration/TimeRHSFunctionExplicit.c:30-98):
+ * rhs = 0; rhs += -1*hyp; rhs += par; rhs += source (zero here). */
+int orc_rhs(const orc_problem *p, double *u, double *rhs) {
+  long n = orc_npoints_wghosts(p) * p->nvars;
+  double *hyp = (double *)malloc(sizeof(double) * n);
+  double *par = (double *)malloc(sizeof(double) * n);
+  orc_apply_bc(p, u);
+  orc_hyperbolic(p, u, hyp);
+  orc_parabolic(p, u, par);
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+  for (long i = 0; i < n; i++) {
+    double r = 0.0;
+    r += -1.0 * hyp[i];
+    r += 1.0 * par[i];
+    r += 1.0 * 0.0;
+    rhs[i] = r;
+  }
+  free(hyp);
+  free(par);
+  return 0;
+}
+
+/* TimeRK (src/TimeIntegration/TimeRK.c:126-195) for one simulation:
+ * U[s] = u + sum_{i<s} (dt*A[s][i]) Udot[i];  Udot[s] = RHS(U[s]);
+ * u += (dt*b[s]) Udot[s], all over the full array including ghost points. */
+int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
+           double *u, double dt, int nsteps) {
+  long n = orc_npoints_wghosts(p) * p->nvars;
+  double *U = (double *)malloc(sizeof(double) * n);
+  double *Udot = (double *)malloc(sizeof(double) * n * nstages);
+  for (int step = 0; step < nsteps; step++) {
+    orc_apply_bc(p, u); /* TimePreStep */
+    for (int st = 0; st < nstages; st++) {
+      memcpy(U, u, sizeof(double) * n);
+      for (int i = 0; i < st; i++) {
+        double a = dt * A[st * nstages + i];
+        const double *k = Udot + (long)i * n;
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+        for (long q = 0; q < n; q++) U[q] += a * k[q];
+      }
+      orc_rhs(p, U, Udot + (long)st * n);
+    }
+    for (int st = 0; st < nstages; st++) {
+      double a = dt * b[st];
+      const double *k = Udot + (long)st * n;
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+      for (long q = 0; q < n; q++) u[q] += a * k[q];
+    }
+  }
+  free(U);
+  free(Udot);
+  return 0;
+}

@@ -1,0 +1,75 @@
+/*
+ * gbh_oracle.h -- CPU restatement of HyPar's explicit WENO5 right-hand side
+ * and Runge-Kutta step, used ONLY as the parity checker and as the timed CPU
+ * baseline.  It is test infrastructure: the GPU product never links it.
+ *
+ * Every routine restates the reference's arithmetic in the same operation
+ * order (compiled with -ffp-contract=off), so that on the same inputs it
+ * reproduces the reference CPU build bit for bit; the pinning test compares it
+ * against the reference itself, built from source into oracle/_ref/.
+ *
+ * Layout (as the reference, include/arrayfunctions.h:40-47): arrays carry
+ * `ghosts` ghost points on every side, dimension 0 is the fastest index and
+ * the `nvars` components of a point are contiguous (u[nvars*p + v]).
+ */
+#ifndef GBH_ORACLE_H
+#define GBH_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_EULER1D = 1, ORC_EULER2D = 2, ORC_NS3D = 3 };
+enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2 };
+enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
+enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2 };
+
+/* One boundary zone, as DomainBoundary after CalculateLocalExtent
+ * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index
+ * range [is[d], ie[d]) in every dimension d, with is[dim] = -ghosts,
+ * ie[dim] = 0 on face +1 and is[dim] = N, ie[dim] = N+ghosts on face -1. */
+typedef struct {
+  int type, dim, face;
+  int is[3], ie[3];
+} orc_zone;
+
+typedef struct {
+  int model, ndims, nvars, ghosts, dim[3];
+  int upwind, interp;
+  double gamma, eps;
+  double Re, Pr;        /* Re already divided by Minf (NavierStokes3DInitialize.c:368); Re<=0: inviscid */
+  int nzones;
+  orc_zone zones[12];
+  double *dxinv;        /* sum_d (dim[d]+2*ghosts), per point 2/(x[i+1]-x[i-1]) */
+} orc_problem;
+
+/* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
+ * dxinv: sum_d (dim[d]+2g) doubles (copied). */
+orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts,
+                                int upwind, int interp, double gamma, double eps,
+                                double Re_over_Minf, double Pr, int nzones,
+                                const int *zones, const double *dxinv);
+void orc_problem_destroy(orc_problem *p);
+
+/* Number of points with ghosts. */
+long orc_npoints_wghosts(const orc_problem *p);
+
+/* Boundary ghost fill on u in place (ApplyBoundaryConditions). */
+int orc_apply_bc(const orc_problem *p, double *u);
+/* Hyperbolic term hyp (with ghosts, ghosts zero) from a BC-filled u. */
+int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp);
+/* NavierStokes3D viscous term par (with ghosts) from a BC-filled u. */
+int orc_parabolic(const orc_problem *p, const double *u, double *par);
+/* TimeRHSFunctionExplicit: fills u's ghosts in place, rhs = -hyp + par. */
+int orc_rhs(const orc_problem *p, double *u, double *rhs);
+/* TimeRK over nsteps steps of the Butcher tableau (A: ns x ns row major, b). */
+int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
+           double *u, double dt, int nsteps);
+/* Set the OpenMP thread count used by the oracle (<=0: library default). */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
