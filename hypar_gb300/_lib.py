@@ -1,0 +1,119 @@
+"""ctypes binding of libgbhypar's C ABI (include/gbhypar.h).
+
+The library is loaded from this package's directory; there is no fallback:
+if libgbhypar.so is missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgbhypar.so")
+
+GB_OK = 0
+GB_ERR = {1: "GB_ERR_ARG", 2: "GB_ERR_CUDA", 3: "GB_ERR_INPUT", 4: "GB_ERR_UNSUPPORTED", 5: "GB_ERR_NOMEM",
+          6: "GB_ERR_NONFINITE"}
+MODEL = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
+UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2}
+INTERP = {"components": 0, "characteristic": 1}
+LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
+MEM_HOST, MEM_DEVICE = 0, 1
+
+# Every symbol include/gbhypar.h declares.
+EXPORTS = [
+    "gb_last_error", "gb_inputs_read", "gb_inputs_free", "gb_inputs_config", "gb_inputs_x", "gb_inputs_dxinv",
+    "gb_inputs_u0", "gb_rk_table", "gb_solver_create", "gb_solver_destroy", "gb_solver_config",
+    "gb_solver_set_stream", "gb_solver_sync", "gb_solver_set_state", "gb_solver_get_state", "gb_solver_state",
+    "gb_solver_step", "gb_solver_time", "gb_solver_set_launch", "gb_solver_check_finite", "gb_run_case",
+    "gb_write_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
+    "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
+    "gb_TimeRK", "gb_probe_fp64_peak",
+]
+
+
+class GbConfig(ctypes.Structure):
+    _fields_ = [
+        ("model", ctypes.c_int), ("ndims", ctypes.c_int), ("nvars", ctypes.c_int), ("ghosts", ctypes.c_int),
+        ("dim", ctypes.c_int * 3), ("interp", ctypes.c_int), ("upwind", ctypes.c_int),
+        ("gamma", ctypes.c_double), ("weno_eps", ctypes.c_double),
+        ("Re", ctypes.c_double), ("Pr", ctypes.c_double), ("Minf", ctypes.c_double),
+        ("nzones", ctypes.c_int), ("zones", (ctypes.c_int * 9) * 12),
+        ("rk_nstages", ctypes.c_int), ("rk_A", ctypes.c_double * 16), ("rk_b", ctypes.c_double * 4),
+        ("rk_c", ctypes.c_double * 4), ("dt", ctypes.c_double), ("n_iter", ctypes.c_int),
+        ("file_op_iter", ctypes.c_int),
+    ]
+
+
+class GbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{GB_ERR.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+VP = ctypes.c_void_p
+DP = ctypes.POINTER(ctypes.c_double)
+FFUNC = ctypes.CFUNCTYPE(ctypes.c_int, DP, DP, ctypes.c_int, VP, ctypes.c_double)
+UPWFUNC = ctypes.CFUNCTYPE(ctypes.c_int, DP, DP, DP, DP, DP, DP, ctypes.c_int, VP, ctypes.c_double)
+
+
+def lib():
+    """Load libgbhypar.so (raises if it is absent: there is no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with hypar_gb300.build.build()")
+    L = ctypes.CDLL(LIB_PATH)
+    L.gb_last_error.restype = ctypes.c_char_p
+    L.gb_inputs_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(VP)]
+    L.gb_inputs_free.argtypes = [VP]
+    L.gb_inputs_free.restype = None
+    L.gb_inputs_config.argtypes = [VP]
+    L.gb_inputs_config.restype = ctypes.POINTER(GbConfig)
+    for n in ("gb_inputs_x", "gb_inputs_dxinv", "gb_inputs_u0"):
+        getattr(L, n).argtypes = [VP]
+        getattr(L, n).restype = DP
+    L.gb_rk_table.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), DP, DP, DP]
+    L.gb_solver_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.POINTER(VP)]
+    L.gb_solver_destroy.argtypes = [VP]
+    L.gb_solver_destroy.restype = None
+    L.gb_solver_config.argtypes = [VP]
+    L.gb_solver_config.restype = ctypes.POINTER(GbConfig)
+    L.gb_solver_set_stream.argtypes = [VP, VP]
+    L.gb_solver_sync.argtypes = [VP]
+    L.gb_solver_set_state.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int]
+    L.gb_solver_get_state.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int]
+    L.gb_solver_state.argtypes = [VP]
+    L.gb_solver_state.restype = VP
+    L.gb_solver_step.argtypes = [VP, ctypes.c_int]
+    L.gb_solver_time.argtypes = [VP]
+    L.gb_solver_time.restype = ctypes.c_double
+    L.gb_solver_set_launch.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.gb_solver_check_finite.argtypes = [VP, ctypes.POINTER(ctypes.c_int)]
+    L.gb_run_case.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
+    L.gb_write_binary.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP, DP]
+    L.gb_HyperbolicFunction.argtypes = [VP, VP, VP, VP, ctypes.c_double, ctypes.c_int, VP, VP]
+    for n in ("gb_ParabolicFunction", "gb_SourceFunction", "gb_RHSFunctionExplicit"):
+        getattr(L, n).argtypes = [VP, VP, VP, VP, ctypes.c_double]
+    for n in ("gb_FFunction", "gb_GFunction"):
+        getattr(L, n).argtypes = [VP, VP, ctypes.c_int, VP, ctypes.c_double]
+    L.gb_UFunction.argtypes = [VP, VP, ctypes.c_int, VP, VP, ctypes.c_double]
+    L.gb_Upwind.argtypes = [VP, VP, VP, VP, VP, VP, ctypes.c_int, VP, ctypes.c_double]
+    L.gb_ApplyBoundaryConditions.argtypes = [VP, VP, VP, VP, ctypes.c_double]
+    L.gb_TimeRK.argtypes = [VP]
+    L.gb_probe_fp64_peak.argtypes = [DP]
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != GB_OK:
+        raise GbError(rc, lib().gb_last_error().decode(errors="replace"))
+
+
+def fn_address(name: str) -> int:
+    """Address of an exported function (to pass as a HyPar function pointer)."""
+    return ctypes.cast(getattr(lib(), name), ctypes.c_void_p).value

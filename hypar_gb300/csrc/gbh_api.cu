@@ -1,0 +1,565 @@
+// gbh_api.cu -- the solver object, the Runge-Kutta driver and the C ABI of
+// libgbhypar (declared in include/gbhypar.h).
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbh_internal.h"
+#include "gbhypar.h"
+
+namespace gbh {
+cudaError_t launch_hyp_euler1d(int, int, int, const double*, double*, const double*, const DevGeom&,
+                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_euler2d(int, int, int, const double*, double*, const double*, const DevGeom&,
+                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_ns3d(int, int, int, const double*, double*, const double*, const DevGeom&,
+                            const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_unfused_euler1d(int, int, int, double*, const double*, const double*, const double*,
+                                   const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
+cudaError_t launch_unfused_euler2d(int, int, int, double*, const double*, const double*, const double*,
+                                   const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
+cudaError_t launch_unfused_ns3d(int, int, int, double*, const double*, const double*, const double*,
+                                const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
+cudaError_t launch_visc(const double*, double*, double*, double*, const double*, const DevGeom&,
+                        const ViscParams&, int, cudaStream_t);
+cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, cudaStream_t);
+cudaError_t launch_finite_check(const double*, const DevGeom&, int, int*, cudaStream_t);
+cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
+}  // namespace gbh
+
+using namespace gbh;
+
+static thread_local char g_err[1024] = "";
+
+extern "C" void gbh_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+extern "C" const char* gb_last_error(void) { return g_err; }
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      gbh_set_error("%s:%d: %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+      return GB_ERR_CUDA;                                                         \
+    }                                                                             \
+  } while (0)
+
+struct gb_solver {
+  gb_config cfg;
+  DevGeom G;
+  PhysParams pp;
+  ViscParams vp;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  long long npts_wg = 0;
+  size_t nvals = 0;
+  double* d_u = nullptr;
+  double* d_acc = nullptr;
+  double* d_P[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* d_H = nullptr;
+  double* d_par = nullptr;
+  double* d_Q = nullptr;
+  double* d_Gr = nullptr;
+  double* d_dxinv = nullptr;
+  int* d_flag = nullptr;
+  std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
+  HypLaunch hl[3];
+  int visc_seg = 16;
+  double t = 0.0;
+  long long dx_off[3] = {0, 0, 0};
+  bool viscous = false;
+};
+
+static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const StageEpi& ep) {
+  const gb_config& c = s->cfg;
+  const double* dx = s->d_dxinv + s->dx_off[dir];
+  if (c.model == GB_MODEL_EULER1D)
+    return launch_hyp_euler1d(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+  if (c.model == GB_MODEL_EULER2D)
+    return launch_hyp_euler2d(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+  return launch_hyp_ns3d(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+}
+
+static cudaError_t launch_unfused(gb_solver* s, int kind, int dir, double* out, const double* a, const double* b,
+                                  const double* c2, const double* d, const double* u) {
+  const gb_config& c = s->cfg;
+  if (c.model == GB_MODEL_EULER1D)
+    return launch_unfused_euler1d(kind, dir, c.upwind, out, a, b, c2, d, u, s->G, s->pp, s->stream);
+  if (c.model == GB_MODEL_EULER2D)
+    return launch_unfused_euler2d(kind, dir, c.upwind, out, a, b, c2, d, u, s->G, s->pp, s->stream);
+  return launch_unfused_ns3d(kind, dir, c.upwind, out, a, b, c2, d, u, s->G, s->pp, s->stream);
+}
+
+static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
+  for (int z = 0; z < s->cfg.nzones; z++) {
+    bool use = all;
+    if (!use)
+      for (int k : s->mem_zones)
+        if (k == z) use = true;
+    if (use) CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->stream));
+  }
+  return GB_OK;
+}
+
+// Right-hand side of U into `epi` (EPI_RHS or EPI_RK): boundary zones kept in
+// memory, the viscous term, then one fused hyperbolic launch per direction.
+static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
+  int rc = apply_mem_bcs(s, U, false);
+  if (rc) return rc;
+  ep.par = nullptr;
+  if (s->viscous) {
+    CK(launch_visc(U, s->d_Q, s->d_Gr, s->d_par, s->d_dxinv, s->G, s->vp, s->visc_seg, s->stream));
+    ep.par = s->d_par;
+  }
+  int nd = s->cfg.ndims;
+  for (int d = 0; d < nd; d++) {
+    StageEpi e = ep;
+    e.first = (d == 0);
+    e.last = (d == nd - 1);
+    CK(launch_hyp(s, d, U, e));
+  }
+  return GB_OK;
+}
+
+static int validate(const gb_config* c) {
+  if (!c) { gbh_set_error("null config"); return GB_ERR_ARG; }
+  int nd = c->model == GB_MODEL_EULER1D ? 1 : c->model == GB_MODEL_EULER2D ? 2 : c->model == GB_MODEL_NS3D ? 3 : 0;
+  if (!nd) { gbh_set_error("unknown model %d", c->model); return GB_ERR_ARG; }
+  if (c->ndims != nd || c->nvars != nd + 2) { gbh_set_error("ndims/nvars do not match the model"); return GB_ERR_ARG; }
+  if (c->ghosts != 3) { gbh_set_error("ghosts must be 3"); return GB_ERR_ARG; }
+  for (int d = 0; d < nd; d++)
+    if (c->dim[d] < 4) { gbh_set_error("dim[%d] = %d < 4", d, c->dim[d]); return GB_ERR_ARG; }
+  if (c->interp != GB_INTERP_COMPONENTS && c->interp != GB_INTERP_CHARACTERISTIC) { gbh_set_error("bad interp"); return GB_ERR_ARG; }
+  if (c->upwind < 0 || c->upwind > 2) { gbh_set_error("bad upwind"); return GB_ERR_ARG; }
+  if (c->rk_nstages < 1 || c->rk_nstages > 4) { gbh_set_error("rk_nstages must be 1..4"); return GB_ERR_ARG; }
+  if (!(c->gamma > 1.0)) { gbh_set_error("gamma must exceed 1"); return GB_ERR_ARG; }
+  if (!(c->weno_eps > 0.0)) { gbh_set_error("weno_eps must be positive"); return GB_ERR_ARG; }
+  if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
+  for (int z = 0; z < c->nzones; z++) {
+    const int* q = c->zones[z];
+    if ((q[0] != GB_BC_PERIODIC && q[0] != GB_BC_EXTRAPOLATE) || q[1] < 0 || q[1] >= nd || (q[2] != 1 && q[2] != -1)) {
+      gbh_set_error("bad zone %d", z);
+      return GB_ERR_ARG;
+    }
+    for (int d = 0; d < nd; d++) {
+      int lo = -c->ghosts, hi = c->dim[d] + c->ghosts;
+      if (q[3 + d] < lo || q[6 + d] > hi) { gbh_set_error("zone %d extent out of range", z); return GB_ERR_ARG; }
+    }
+    int d = q[1];
+    bool ok = (q[2] == 1) ? (q[3 + d] == -c->ghosts && q[6 + d] == 0) : (q[3 + d] == c->dim[d] && q[6 + d] == c->dim[d] + c->ghosts);
+    if (!ok) { gbh_set_error("zone %d: extent along its own dimension must be the ghost layer", z); return GB_ERR_ARG; }
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int device, gb_solver** out) {
+  if (!out || !dxinv) { gbh_set_error("gb_solver_create: null argument"); return GB_ERR_ARG; }
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  gb_solver* s = new gb_solver();
+  s->cfg = *cfg;
+  const gb_config& c = s->cfg;
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { gbh_set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); delete s; return GB_ERR_CUDA; }
+  }
+  cudaGetDevice(&s->device);
+  DevGeom& G = s->G;
+  G.nd = c.ndims;
+  G.g = c.ghosts;
+  long long st = 1;
+  for (int d = 0; d < 3; d++) {
+    G.dim[d] = d < c.ndims ? c.dim[d] : 1;
+    G.stride[d] = d < c.ndims ? st : 0;
+    if (d < c.ndims) st *= (c.dim[d] + 2 * c.ghosts);
+    G.bclo[d] = G.bchi[d] = FOLD_MEMORY;
+  }
+  s->npts_wg = st;
+  s->nvals = (size_t)st * c.nvars;
+  // Fold a face into the halo loads when exactly one zone covers all of it.
+  for (int d = 0; d < c.ndims; d++)
+    for (int side = 0; side < 2; side++) {
+      int face = side == 0 ? 1 : -1, cnt = 0, which = -1;
+      for (int z = 0; z < c.nzones; z++)
+        if (c.zones[z][1] == d && c.zones[z][2] == face) { cnt++; which = z; }
+      bool full = false;
+      if (cnt == 1) {
+        full = true;
+        for (int e = 0; e < c.ndims; e++)
+          if (e != d && (c.zones[which][3 + e] > 0 || c.zones[which][6 + e] < c.dim[e])) full = false;
+      }
+      int mode = FOLD_MEMORY;
+      if (full) mode = c.zones[which][0] == GB_BC_PERIODIC ? FOLD_PERIODIC : FOLD_MIRROR;
+      if (side == 0) G.bclo[d] = mode; else G.bchi[d] = mode;
+      for (int z = 0; z < c.nzones; z++)
+        if (c.zones[z][1] == d && c.zones[z][2] == face && !full) s->mem_zones.push_back(z);
+    }
+  s->pp.gamma = c.gamma;
+  s->pp.gm1 = c.gamma - 1.0;
+  s->pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
+  s->pp.eps = c.weno_eps;
+  s->viscous = (c.model == GB_MODEL_NS3D) && (c.Re > 0);
+  double Re_eff = c.Re / c.Minf;  // NavierStokes3DInitialize.c:368
+  s->vp.gamma = c.gamma;
+  s->vp.gm1 = c.gamma - 1.0;
+  s->vp.inv_gm1 = 1.0 / (c.gamma - 1.0);
+  s->vp.inv_Re = 1.0 / Re_eff;
+  s->vp.inv_Pr = 1.0 / c.Pr;
+  for (int d = 0; d < 3; d++) {
+    s->hl[d].seg = 32;
+    s->hl[d].block = 128;
+  }
+  long long off = 0;
+  for (int d = 0; d < c.ndims; d++) {
+    s->dx_off[d] = off;
+    off += c.dim[d] + 2 * c.ghosts;
+  }
+  size_t bytes = s->nvals * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  auto A = [&](double** p, size_t n) {
+    if (e == cudaSuccess) e = cudaMalloc((void**)p, n);
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, n);
+  };
+  A(&s->d_u, bytes);
+  A(&s->d_acc, bytes);
+  for (int k = 1; k < c.rk_nstages; k++) A(&s->d_P[k], bytes);
+  if (c.ndims > 1) A(&s->d_H, bytes);
+  if (s->viscous) {
+    A(&s->d_par, bytes);
+    A(&s->d_Q, (size_t)st * 6 * sizeof(double));
+    A(&s->d_Gr, (size_t)st * 12 * sizeof(double));
+  }
+  A(&s->d_dxinv, off * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&s->d_flag, sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) s->own_stream = true;
+  if (e == cudaSuccess) e = cudaMemcpy(s->d_dxinv, dxinv, off * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    gbh_set_error("gb_solver_create: %s", cudaGetErrorString(e));
+    gb_solver_destroy(s);
+    return e == cudaErrorMemoryAllocation ? GB_ERR_NOMEM : GB_ERR_CUDA;
+  }
+  *out = s;
+  return GB_OK;
+}
+
+extern "C" void gb_solver_destroy(gb_solver* s) {
+  if (!s) return;
+  cudaFree(s->d_u);
+  cudaFree(s->d_acc);
+  for (int k = 0; k < 4; k++) cudaFree(s->d_P[k]);
+  cudaFree(s->d_H);
+  cudaFree(s->d_par);
+  cudaFree(s->d_Q);
+  cudaFree(s->d_Gr);
+  cudaFree(s->d_dxinv);
+  cudaFree(s->d_flag);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+extern "C" const gb_config* gb_solver_config(const gb_solver* s) { return s ? &s->cfg : nullptr; }
+
+extern "C" int gb_solver_set_stream(gb_solver* s, void* stream) {
+  if (!s) { gbh_set_error("null solver"); return GB_ERR_ARG; }
+  if (s->own_stream && s->stream) {
+    cudaStreamSynchronize(s->stream);
+    cudaStreamDestroy(s->stream);
+    s->own_stream = false;
+    s->stream = nullptr;
+  }
+  if (stream) {
+    s->stream = (cudaStream_t)stream;
+  } else {
+    CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    s->own_stream = true;
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_solver_sync(gb_solver* s) {
+  if (!s) { gbh_set_error("null solver"); return GB_ERR_ARG; }
+  CK(cudaStreamSynchronize(s->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_solver_set_launch(gb_solver* s, int dir, int seg, int block) {
+  if (!s || dir < 0 || dir >= s->cfg.ndims) { gbh_set_error("gb_solver_set_launch: bad argument"); return GB_ERR_ARG; }
+  if (seg > 0) s->hl[dir].seg = seg;
+  if (block > 0) {
+    if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
+    s->hl[dir].block = block;
+  }
+  return GB_OK;
+}
+
+// Copy between the interior (no ghosts) and ghosted layouts on the device.
+extern "C" int gb_solver_set_state(gb_solver* s, const double* u, int layout, int mem) {
+  if (!s || !u) { gbh_set_error("gb_solver_set_state: null argument"); return GB_ERR_ARG; }
+  size_t bytes = s->nvals * sizeof(double);
+  if (layout == GB_LAYOUT_GHOSTED) {
+    CK(cudaMemcpyAsync(s->d_u, u, bytes, mem == GB_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                       s->stream));
+  } else {
+    size_t nint = 1;
+    for (int d = 0; d < s->cfg.ndims; d++) nint *= s->cfg.dim[d];
+    const double* src = u;
+    double* tmp = nullptr;
+    if (mem == GB_MEM_HOST) {
+      CK(cudaMallocAsync((void**)&tmp, nint * s->cfg.nvars * sizeof(double), s->stream));
+      CK(cudaMemcpyAsync(tmp, u, nint * s->cfg.nvars * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+      src = tmp;
+    }
+    CK(launch_pack(s->d_u, src, s->G, s->cfg.nvars, 0, s->stream));
+    if (tmp) CK(cudaFreeAsync(tmp, s->stream));
+  }
+  // every work array starts with the same ghost values as u
+  CK(cudaMemcpyAsync(s->d_acc, s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  for (int k = 1; k < s->cfg.rk_nstages; k++)
+    CK(cudaMemcpyAsync(s->d_P[k], s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  s->t = 0.0;
+  return GB_OK;
+}
+
+extern "C" int gb_solver_get_state(gb_solver* s, double* u, int layout, int mem) {
+  if (!s || !u) { gbh_set_error("gb_solver_get_state: null argument"); return GB_ERR_ARG; }
+  size_t bytes = s->nvals * sizeof(double);
+  if (layout == GB_LAYOUT_GHOSTED) {
+    CK(cudaMemcpyAsync(u, s->d_u, bytes, mem == GB_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                       s->stream));
+  } else {
+    size_t nint = 1;
+    for (int d = 0; d < s->cfg.ndims; d++) nint *= s->cfg.dim[d];
+    size_t ib = nint * s->cfg.nvars * sizeof(double);
+    double* dst = u;
+    double* tmp = nullptr;
+    if (mem == GB_MEM_HOST) {
+      CK(cudaMallocAsync((void**)&tmp, ib, s->stream));
+      dst = tmp;
+    }
+    CK(launch_pack(dst, s->d_u, s->G, s->cfg.nvars, 1, s->stream));
+    if (tmp) {
+      CK(cudaMemcpyAsync(u, tmp, ib, cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaFreeAsync(tmp, s->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return GB_OK;
+}
+
+extern "C" double* gb_solver_state(gb_solver* s) { return s ? s->d_u : nullptr; }
+extern "C" double gb_solver_time(const gb_solver* s) { return s ? s->t : 0.0; }
+
+// One Runge-Kutta step (TimeRK, src/TimeIntegration/TimeRK.c:126-195) as
+// nstages x ndims fused launches.
+static int rk_step(gb_solver* s) {
+  const gb_config& c = s->cfg;
+  const int ns = c.rk_nstages;
+  const double dt = c.dt;
+  int touched[4] = {0, 0, 0, 0};
+  for (int st = 0; st < ns; st++) {
+    double* U = (st == 0 || !touched[st]) ? s->d_u : s->d_P[st];
+    StageEpi ep;
+    memset(&ep, 0, sizeof(ep));
+    ep.mode = EPI_RK;
+    ep.stage = st;
+    ep.nstages = ns;
+    ep.cb = dt * c.rk_b[st];
+    ep.need_u = (st == 0);
+    for (int t = 0; t < 4; t++) {
+      ep.ca[t] = 0.0;
+      ep.touched[t] = touched[t];
+      ep.P[t] = s->d_P[t];
+      if (t > st && t < ns) {
+        ep.ca[t] = dt * c.rk_A[4 * t + st];
+        if (ep.ca[t] != 0.0 && !touched[t]) ep.need_u = 1;
+      }
+    }
+    ep.u = s->d_u;
+    ep.acc = s->d_acc;
+    ep.uout = (ns == 1) ? s->d_acc : s->d_u;
+    int rc = rhs_launches(s, U, ep);
+    if (rc) return rc;
+    for (int t = st + 1; t < ns; t++)
+      if (ep.ca[t] != 0.0) touched[t] = 1;
+  }
+  if (ns == 1) {
+    double* tmp = s->d_u;
+    s->d_u = s->d_acc;
+    s->d_acc = tmp;
+  }
+  s->t += dt;
+  return GB_OK;
+}
+
+extern "C" int gb_solver_step(gb_solver* s, int nsteps) {
+  if (!s || nsteps < 0) { gbh_set_error("gb_solver_step: bad argument"); return GB_ERR_ARG; }
+  for (int n = 0; n < nsteps; n++) {
+    int rc = rk_step(s);
+    if (rc) return rc;
+  }
+  CK(cudaGetLastError());
+  return GB_OK;
+}
+
+extern "C" int gb_solver_check_finite(gb_solver* s, int* finite) {
+  if (!s || !finite) { gbh_set_error("null argument"); return GB_ERR_ARG; }
+  int h = 0;
+  CK(cudaMemsetAsync(s->d_flag, 0, sizeof(int), s->stream));
+  CK(launch_finite_check(s->d_u, s->G, s->cfg.nvars, s->d_flag, s->stream));
+  CK(cudaMemcpyAsync(&h, s->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  *finite = h ? 0 : 1;
+  return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// HyPar function-pointer surface.
+// ---------------------------------------------------------------------------
+extern "C" int gb_FFunction(double* f, double* u, int dir, void* sv, double t);
+extern "C" int gb_Upwind(double* fI, double* fL, double* fR, double* uL, double* uR, double* u, int dir, void* sv,
+                         double t);
+
+static gb_solver* S(void* sv) { return (gb_solver*)sv; }
+
+extern "C" int gb_HyperbolicFunction(double* hyp, double* u, void* sv, void* m, double t, int LimFlag,
+                                     int (*F)(double*, double*, int, void*, double),
+                                     int (*Upw)(double*, double*, double*, double*, double*, double*, int, void*,
+                                                double)) {
+  (void)m;
+  (void)t;
+  (void)LimFlag;
+  gb_solver* s = S(sv);
+  if (!s || !hyp || !u) { gbh_set_error("gb_HyperbolicFunction: null argument"); return GB_ERR_ARG; }
+  if (F == nullptr && Upw == nullptr) {
+    // HyperbolicFunction.c:66: no flux function means a zero hyperbolic term
+    CK(cudaMemsetAsync(hyp, 0, s->nvals * sizeof(double), s->stream));
+    return GB_OK;
+  }
+  if (F != gb_FFunction || (Upw != nullptr && Upw != gb_Upwind)) {
+    gbh_set_error("gb_HyperbolicFunction: flux/upwind must be gb_FFunction/gb_Upwind");
+    return GB_ERR_UNSUPPORTED;
+  }
+  CK(cudaMemsetAsync(hyp, 0, s->nvals * sizeof(double), s->stream));
+  StageEpi ep;
+  memset(&ep, 0, sizeof(ep));
+  ep.mode = EPI_HYP;
+  double* H = s->d_H;
+  s->d_H = hyp;  // accumulate straight into the caller's array
+  int rc = GB_OK;
+  for (int d = 0; d < s->cfg.ndims && !rc; d++) {
+    StageEpi e = ep;
+    e.first = (d == 0);
+    e.last = (d == s->cfg.ndims - 1);
+    cudaError_t ce = launch_hyp(s, d, u, e);
+    if (ce != cudaSuccess) { gbh_set_error("gb_HyperbolicFunction: %s", cudaGetErrorString(ce)); rc = GB_ERR_CUDA; }
+  }
+  s->d_H = H;
+  return rc;
+}
+
+extern "C" int gb_ParabolicFunction(double* par, double* u, void* sv, void* m, double t) {
+  (void)m;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !par || !u) { gbh_set_error("gb_ParabolicFunction: null argument"); return GB_ERR_ARG; }
+  CK(cudaMemsetAsync(par, 0, s->nvals * sizeof(double), s->stream));
+  if (!s->viscous) return GB_OK;
+  CK(launch_visc(u, s->d_Q, s->d_Gr, par, s->d_dxinv, s->G, s->vp, s->visc_seg, s->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_SourceFunction(double* source, double* u, void* sv, void* m, double t) {
+  (void)u;
+  (void)m;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !source) { gbh_set_error("gb_SourceFunction: null argument"); return GB_ERR_ARG; }
+  CK(cudaMemsetAsync(source, 0, s->nvals * sizeof(double), s->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_FFunction(double* f, double* u, int dir, void* sv, double t) {
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !f || !u || dir < 0 || dir >= s->cfg.ndims) { gbh_set_error("gb_FFunction: bad argument"); return GB_ERR_ARG; }
+  CK(launch_unfused(s, 0, dir, f, nullptr, nullptr, nullptr, nullptr, u));
+  return GB_OK;
+}
+
+extern "C" int gb_GFunction(double* f, double* u, int dir, void* sv, double t) {
+  (void)u;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !f || dir < 0 || dir >= s->cfg.ndims) { gbh_set_error("gb_GFunction: bad argument"); return GB_ERR_ARG; }
+  CK(cudaMemsetAsync(f, 0, s->nvals * sizeof(double), s->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_UFunction(double* uC, double* u, int dir, void* sv, void* m, double t) {
+  (void)m;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !uC || !u) { gbh_set_error("gb_UFunction: bad argument"); return GB_ERR_ARG; }
+  CK(launch_unfused(s, 1, dir < 0 ? 0 : dir, uC, nullptr, nullptr, nullptr, nullptr, u));
+  return GB_OK;
+}
+
+extern "C" int gb_Upwind(double* fI, double* fL, double* fR, double* uL, double* uR, double* u, int dir, void* sv,
+                         double t) {
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !fI || !fL || !fR || !uL || !uR || !u || dir < 0 || dir >= s->cfg.ndims) {
+    gbh_set_error("gb_Upwind: bad argument");
+    return GB_ERR_ARG;
+  }
+  CK(launch_unfused(s, 2, dir, fI, fL, fR, uL, uR, u));
+  return GB_OK;
+}
+
+extern "C" int gb_ApplyBoundaryConditions(void* sv, void* m, double* u, double* uref, double t) {
+  (void)m;
+  (void)uref;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !u) { gbh_set_error("gb_ApplyBoundaryConditions: null argument"); return GB_ERR_ARG; }
+  return apply_mem_bcs(s, u, true);
+}
+
+extern "C" int gb_RHSFunctionExplicit(double* rhs, double* u, void* sv, void* m, double t) {
+  (void)m;
+  (void)t;
+  gb_solver* s = S(sv);
+  if (!s || !rhs || !u) { gbh_set_error("gb_RHSFunctionExplicit: null argument"); return GB_ERR_ARG; }
+  int rc = apply_mem_bcs(s, u, true);  // TimeRHSFunctionExplicit.c:46 fills u's ghosts in place
+  if (rc) return rc;
+  CK(cudaMemsetAsync(rhs, 0, s->nvals * sizeof(double), s->stream));
+  StageEpi ep;
+  memset(&ep, 0, sizeof(ep));
+  ep.mode = EPI_RHS;
+  ep.rhs = rhs;
+  std::vector<int> keep;
+  keep.swap(s->mem_zones);  // already applied above
+  rc = rhs_launches(s, u, ep);
+  keep.swap(s->mem_zones);
+  return rc;
+}
+
+extern "C" int gb_TimeRK(void* ts) {
+  gb_solver* s = S(ts);
+  if (!s) { gbh_set_error("gb_TimeRK: null argument"); return GB_ERR_ARG; }
+  int rc = rk_step(s);
+  if (rc) return rc;
+  CK(cudaGetLastError());
+  return GB_OK;
+}

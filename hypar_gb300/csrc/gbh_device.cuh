@@ -1,0 +1,305 @@
+// gbh_device.cuh -- FP64 device math for the fused WENO5 right-hand side.
+//
+// Physics (Euler1D, Euler2D, NavierStokes3D), Jiang-Shu WENO5 and Roe / LLF /
+// RF upwinding, written for the GB300 FP64 pipe: every formula is the
+// reference's (file:line cited per routine) rearranged so that one interface
+// costs as few FP64 instructions as possible.  Results agree with the
+// reference to rounding (the parity tests hold them to a relative L2 of 1e-12
+// per right-hand side); nothing here is bit-for-bit by design.
+#pragma once
+
+#include <cstdint>
+
+namespace gbh {
+
+enum { MODEL_EULER1D = 1, MODEL_EULER2D = 2, MODEL_NS3D = 3 };
+enum { UPW_ROE = 0, UPW_LLF = 1, UPW_RF = 2 };
+
+template <int M> struct ModelTraits;
+template <> struct ModelTraits<MODEL_EULER1D> { static constexpr int NV = 3, ND = 1; };
+template <> struct ModelTraits<MODEL_EULER2D> { static constexpr int NV = 4, ND = 2; };
+template <> struct ModelTraits<MODEL_NS3D>    { static constexpr int NV = 5, ND = 3; };
+
+struct PhysParams {
+  double gamma, gm1, inv_gm1, eps;
+};
+
+// ---------------------------------------------------------------------------
+// Reciprocal and square root.
+//
+// The FP64 pipe of a GB300 SM retires only a few operations per clock, so a
+// correctly rounded IEEE division (a multi-instruction sequence) is replaced by
+// Newton-Raphson refinement of the hardware reciprocal / reciprocal-square-root
+// estimates (rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64, PTX ISA): each
+// iteration r' = r + r(1 - x r) doubles the number of correct bits.  Two
+// iterations from the ~2^-22 estimate give a result within one ulp, which the
+// parity tolerance absorbs.  Inputs are positive normal numbers on this path
+// (densities, squared sound speeds, WENO denominators >= eps^2).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double rcp_approx(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+__device__ __forceinline__ double rsqrt_approx(double x) {
+  double r;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+__device__ __forceinline__ double nr_rcp(double x) {
+  double r = rcp_approx(x);
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  return r;
+}
+// sqrt(x) via y ~ 1/sqrt(x):  y' = y + y(1 - x y^2)/2, then s = x y refined once
+// with s' = s + y (x - s^2)/2 (Newton on s^2 = x).
+__device__ __forceinline__ double nr_sqrt(double x) {
+  double y = rsqrt_approx(x);
+  double h = 0.5 * y;
+  double e = fma(-x * y, y, 1.0);
+  y = fma(y, 0.5 * e, y);
+  double s = x * y;
+  h = 0.5 * y;
+  double d = fma(-s, s, x);
+  s = fma(d, h, s);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Conserved -> primitive.  Euler1D: include/physicalmodels/euler1d.h:81-89,
+// Euler2D: euler2d.h:44-54, NavierStokes3D (with its rho == 0 guard):
+// navierstokes3d.h:98-108.
+// ---------------------------------------------------------------------------
+template <int M>
+struct Prim {
+  double rho, rinv, vel[3], P, e;
+};
+
+template <int M>
+__device__ __forceinline__ Prim<M> to_prim(const double* u, const PhysParams& pp) {
+  constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
+  Prim<M> q;
+  q.rho = u[0];
+  q.rinv = nr_rcp(q.rho);
+  double vsq = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) q.vel[k] = 0.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    double v = u[1 + k] * q.rinv;
+    if (M == MODEL_NS3D) v = (q.rho == 0.0) ? 0.0 : v;
+    q.vel[k] = v;
+    vsq = fma(v, v, vsq);
+  }
+  q.e = u[NV - 1];
+  q.P = (q.e - 0.5 * q.rho * vsq) * pp.gm1;
+  return q;
+}
+
+// Cell flux along DIR (Euler1DFlux.c:16-45, Euler2DFlux.c:7-36, NavierStokes3DFlux.c:23-60).
+template <int M, int DIR>
+__device__ __forceinline__ void cell_flux(const Prim<M>& q, double* f) {
+  constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
+  double vn = q.vel[DIR];
+  double mn = q.rho * vn;
+  f[0] = mn;
+#pragma unroll
+  for (int k = 0; k < ND; k++) f[1 + k] = mn * q.vel[k];
+  f[1 + DIR] += q.P;
+  f[NV - 1] = (q.e + q.P) * vn;
+}
+
+// UFunction value of the energy component: NavierStokes3D recomputes it
+// (NavierStokes3DModifiedSolution.c:56-65, gravity fields = 1); Euler1D
+// (gravity field exp(0) = 1) and Euler2D (no UFunction) leave u unchanged.
+template <int M>
+__device__ __forceinline__ double ufunc_energy(const Prim<M>& q, const PhysParams& pp, double e) {
+  if (M == MODEL_NS3D) {
+    double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
+    return q.P * pp.inv_gm1 + 0.5 * q.rho * vsq;
+  }
+  return e;
+}
+
+// Roe-average ingredients of a state: sqrt(rho), velocity, total enthalpy.
+struct RoeSide {
+  double t, vel[3], H;
+};
+template <int M>
+__device__ __forceinline__ RoeSide roe_side(const Prim<M>& q) {
+  RoeSide s;
+  s.t = nr_sqrt(q.rho);
+#pragma unroll
+  for (int k = 0; k < 3; k++) s.vel[k] = q.vel[k];
+  s.H = (q.e + q.P) * q.rinv;
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Eigen-structure at a Roe-averaged state (_Euler1DRoeAverage_ euler1d.h:134-160,
+// _Euler2DRoeAverage_ euler2d.h:70-108, _NavierStokes3DRoeAverage_
+// navierstokes3d.h:147-180) in factored form.  With
+//   s = (gamma-1) (ek q0 - v.q_mom + q_E),  t = a (u_n q0 - q_{1+d}),
+// the reference's left eigenvectors (euler1d.h:209-228, euler2d.h:128-175,
+// navierstokes3d.h:317-408) are, row by row,
+//   acoustic u_n-a :  (s + t) * hac      acoustic u_n+a :  (s - t) * hac
+//   entropy        :  q0 - s / a^2       shear (each transverse e): v_e q0 - q_{1+e}
+// with hac = 1/(2a^2) (Euler2D, NavierStokes3D) or 1/(rho a) (Euler1D), up to
+// row signs, which neither the WENO weights (squares) nor the interpolation
+// (linear) see.  The matching right eigenvectors (columns) are
+//   (1, v -+ a e_d, H -+ a u_n) * rs,  (1, v, ek),  -(e_{1+e} + v_e e_E)
+// with rs = 1/(2 a^2 hac).
+// ---------------------------------------------------------------------------
+struct Eig {
+  double vel[3], un, a, ek, H, hac, rs, inv_a2, rho;
+};
+
+template <int M, int DIR>
+__device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const PhysParams& pp) {
+  constexpr int ND = ModelTraits<M>::ND;
+  Eig E;
+  double inv = nr_rcp(L.t + R.t);
+  double vsq = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) E.vel[k] = 0.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    E.vel[k] = fma(L.t, L.vel[k], R.t * R.vel[k]) * inv;
+    vsq = fma(E.vel[k], E.vel[k], vsq);
+  }
+  E.H = fma(L.t, L.H, R.t * R.H) * inv;
+  E.ek = 0.5 * vsq;
+  double a2 = pp.gm1 * (E.H - E.ek);
+  E.inv_a2 = nr_rcp(a2);
+  E.a = nr_sqrt(a2);
+  E.un = E.vel[DIR];
+  E.rho = L.t * R.t;
+  if (M == MODEL_EULER1D) {
+    // hac = 1/(rho a), rs = rho/(2a) = 1/(2 a^2 hac)
+    double ia = E.a * E.inv_a2;  // 1/a
+    E.hac = nr_rcp(E.rho) * ia;
+    E.rs = 0.5 * E.rho * ia;
+  } else {
+    E.hac = 0.5 * E.inv_a2;
+    E.rs = 1.0;
+  }
+  return E;
+}
+
+// Characteristic fields, in this order: 0 acoustic (u_n - a), 1 acoustic
+// (u_n + a), 2 entropy, 3.. shear components (transverse directions ascending).
+template <int M, int DIR>
+__device__ __forceinline__ void projL(const Eig& E, const PhysParams& pp, const double* q, double* w) {
+  constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
+  double s = E.ek * q[0];
+#pragma unroll
+  for (int k = 0; k < ND; k++) s = fma(-E.vel[k], q[1 + k], s);
+  s = pp.gm1 * (s + q[NV - 1]);
+  double t = E.a * fma(E.un, q[0], -q[1 + DIR]);
+  w[0] = (s + t) * E.hac;
+  w[1] = (s - t) * E.hac;
+  w[2] = fma(-s, E.inv_a2, q[0]);
+  int j = 3;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    if (k == DIR) continue;
+    w[j++] = fma(E.vel[k], q[0], -q[1 + k]);
+  }
+}
+
+template <int M, int DIR>
+__device__ __forceinline__ void projR(const Eig& E, const double* w, double* y) {
+  constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
+  double Wm = E.rs * w[0], Wp = E.rs * w[1];
+  double sa = Wm + Wp;
+  double da = Wp - Wm;
+  double y0 = sa + w[2];
+  double yE = fma(E.H, sa, fma(E.a * E.un, da, E.ek * w[2]));
+  int j = 3;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    if (k == DIR) {
+      y[1 + k] = fma(E.un, y0, E.a * da);
+    } else {
+      y[1 + k] = fma(E.vel[k], y0, -w[j]);
+      yE = fma(-E.vel[k], w[j], yE);
+      j++;
+    }
+  }
+  y[0] = y0;
+  y[NV - 1] = yE;
+}
+
+// Eigenvalues in the same field order.
+template <int M>
+__device__ __forceinline__ void eigvals(double un, double a, double* lam) {
+  constexpr int NV = ModelTraits<M>::NV;
+  lam[0] = un - a;
+  lam[1] = un + a;
+#pragma unroll
+  for (int k = 2; k < NV; k++) lam[k] = un;
+}
+
+// ---------------------------------------------------------------------------
+// WENO5, Jiang-Shu weights (_WENOWeights_v_JS_, include/interpolation.h:265-285,
+// optimal weights 0.1/0.6/0.3 at :228-232) and the fifth-order interpolant
+// (Interp1PrimFifthOrderWENO.c:143-158), for a stencil (m3,m2,m1,p1,p2) biased
+// towards m1.  The normalisation uses one reciprocal:
+//   w_k = c_k/q_k / sum_j c_j/q_j = c_k prod_{j!=k} q_j / sum(...),  q = (beta+eps)^2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double weno5(double m3, double m2, double m1, double p1, double p2,
+                                        double eps) {
+  const double k13 = 13.0 / 12.0, k14 = 0.25;
+  double d1 = fma(-2.0, m2, m3) + m1;
+  double g1 = fma(3.0, m1, fma(-4.0, m2, m3));
+  double d2 = fma(-2.0, m1, m2) + p1;
+  double g2 = m2 - p1;
+  double d3 = fma(-2.0, p1, m1) + p2;
+  double g3 = fma(3.0, m1, fma(-4.0, p1, p2));
+  double b1 = fma(k13 * d1, d1, k14 * g1 * g1) + eps;
+  double b2 = fma(k13 * d2, d2, k14 * g2 * g2) + eps;
+  double b3 = fma(k13 * d3, d3, k14 * g3 * g3) + eps;
+  double q1 = b1 * b1, q2 = b2 * b2, q3 = b3 * b3;
+  double a1 = 0.1 * (q2 * q3);
+  double a2 = 0.6 * (q1 * q3);
+  double a3 = 0.3 * (q1 * q2);
+  double r = nr_rcp(6.0 * (a1 + a2 + a3));
+  double f1 = fma(2.0, m3, fma(-7.0, m2, 11.0 * m1));
+  double f2 = fma(-1.0, m2, fma(5.0, m1, 2.0 * p1));
+  double f3 = fma(2.0, m1, fma(5.0, p1, -p2));
+  return fma(a1, f1, fma(a2, f2, a3 * f3)) * r;
+}
+
+// Same, with the weights taken from one stencil (ws*) and the interpolated
+// values from another (v*): the u-reconstruction weights come from u while the
+// values come from uC = UFunction(u) (HyperbolicFunction.c:201-215).
+__device__ __forceinline__ double weno5_split(double wm3, double wm2, double wm1, double wp1, double wp2,
+                                              double m3, double m2, double m1, double p1, double p2,
+                                              double eps) {
+  const double k13 = 13.0 / 12.0, k14 = 0.25;
+  double d1 = fma(-2.0, wm2, wm3) + wm1;
+  double g1 = fma(3.0, wm1, fma(-4.0, wm2, wm3));
+  double d2 = fma(-2.0, wm1, wm2) + wp1;
+  double g2 = wm2 - wp1;
+  double d3 = fma(-2.0, wp1, wm1) + wp2;
+  double g3 = fma(3.0, wm1, fma(-4.0, wp1, wp2));
+  double b1 = fma(k13 * d1, d1, k14 * g1 * g1) + eps;
+  double b2 = fma(k13 * d2, d2, k14 * g2 * g2) + eps;
+  double b3 = fma(k13 * d3, d3, k14 * g3 * g3) + eps;
+  double q1 = b1 * b1, q2 = b2 * b2, q3 = b3 * b3;
+  double a1 = 0.1 * (q2 * q3);
+  double a2 = 0.6 * (q1 * q3);
+  double a3 = 0.3 * (q1 * q2);
+  double r = nr_rcp(6.0 * (a1 + a2 + a3));
+  double f1 = fma(2.0, m3, fma(-7.0, m2, 11.0 * m1));
+  double f2 = fma(-1.0, m2, fma(5.0, m1, 2.0 * p1));
+  double f3 = fma(2.0, m1, fma(5.0, p1, -p2));
+  return fma(a1, f1, fma(a2, f2, a3 * f3)) * r;
+}
+
+__device__ __forceinline__ double dabs(double x) { return fabs(x); }
+
+}  // namespace gbh

@@ -1,0 +1,476 @@
+// gbh_hyp_impl.cuh -- the fused hyperbolic kernel, one launch per direction.
+//
+// Replaces, for one direction d, HyPar's FFunction -> SetInterpLimiterVar ->
+// UFunction -> 4x InterpolateInterfacesHyp -> Upwind -> flux difference chain
+// (src/HyParFunctions/HyperbolicFunction.c:75-117 with ReconstructHyperbolic
+// :167-222), and, on the last direction of a Runge-Kutta stage, the
+// right-hand-side assembly (TimeRHSFunctionExplicit.c:89-92) and the stage
+// update of TimeRK (TimeRK.c:126-195).
+//
+// Each thread walks `seg` consecutive interfaces of one grid line along d,
+// keeping a six-cell window (cells j-3..j+2 of interface j-1/2) in registers:
+// a cell's flux, Roe-average ingredients and modified state are computed once,
+// when the cell enters the window, and the flux difference of cell j-1 is
+// formed from the previous interface's flux held in registers, so no interface
+// array ever reaches memory.  Ghost cells outside the domain are read through
+// the boundary fold (periodic wrap / mirror) or from memory.
+#pragma once
+
+#include "gbh_internal.h"
+
+namespace gbh {
+
+__device__ __forceinline__ int fold_index(int i, int N, int lo, int hi) {
+  if (i < 0) {
+    if (lo == FOLD_PERIODIC) return i + N;
+    if (lo == FOLD_MIRROR) return -1 - i;
+    return i;
+  }
+  if (i >= N) {
+    if (hi == FOLD_PERIODIC) return i - N;
+    if (hi == FOLD_MIRROR) return 2 * N - 1 - i;
+    return i;
+  }
+  return i;
+}
+
+// Sound speed of a state (for LLF / RF eigenvalues at the left/right states).
+template <int M>
+__device__ __forceinline__ double sound_speed(const Prim<M>& q, const PhysParams& pp) {
+  return nr_sqrt(pp.gamma * q.P * q.rinv);
+}
+
+template <int M>
+struct CellAux {
+  RoeSide rs;
+  double c;
+};
+
+template <int M, bool CHAR, int UPW>
+struct NeedCC {
+  // cell-centre Roe average needed: characteristic WENO (WENOFifthOrderCalculateWeights.c:832),
+  // Euler1D upwinding (Euler1DUpwind.c:74, :259), NavierStokes3D Roe (NavierStokes3DUpwind.c:90)
+  static constexpr bool value = CHAR || (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE);
+};
+
+// Upwind flux at one interface from the reconstructed fL, fR, uL, uR and the
+// two cell-centre neighbours (their Roe-average ingredients `cl`, `cr` and,
+// when CC, the eigen-system `Ecc` of their Roe average).
+template <int M, bool CHAR, int UPW, int DIR>
+__device__ __forceinline__ void upwind_iface(const double* fL, const double* fR, const double* uL,
+                                             const double* uR, const Eig& Ecc, const CellAux<M>& cl,
+                                             const CellAux<M>& cr, const PhysParams& pp, double* fI) {
+  constexpr int NV = ModelTraits<M>::NV;
+  if (UPW == UPW_ROE) {
+    // Roe: fI = (fL+fR)/2 - R|Lambda|L (uR-uL)/2, Roe average of the
+    // reconstructed states for Euler2D (Euler2DUpwind.c:39) and of the
+    // cell-centre states otherwise; Harten's fix except for Euler1D.
+    Eig Eu;
+    if (M == MODEL_EULER2D) {
+      Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+      Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
+    } else {
+      Eu = Ecc;
+    }
+    double ud[NV], w[NV], lam[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) ud[v] = 0.5 * (uR[v] - uL[v]);
+    projL<M, DIR>(Eu, pp, ud, w);
+    eigvals<M>(Eu.un, Eu.a, lam);
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double d = fabs(lam[k]);
+      if (M != MODEL_EULER1D) {
+        const double delta = 0.000001, delta2 = delta * delta;
+        d = (d < delta) ? (lam[k] * lam[k] + delta2) * (0.5 / delta) : d;
+      }
+      w[k] *= d;
+    }
+    projR<M, DIR>(Eu, w, ud);
+#pragma unroll
+    for (int v = 0; v < NV; v++) fI[v] = 0.5 * (fL[v] + fR[v]) - ud[v];
+  } else {
+    // LLF / RF in the Roe eigenbasis (Euler2DUpwind.c:68-210 and the Euler1D /
+    // NavierStokes3D counterparts): alpha = max |lambda| over left, average, right.
+    Eig Eu;
+    double unL, cL, unR, cR;
+    if (M == MODEL_EULER1D) {
+      Eu = Ecc;
+      unL = cl.rs.vel[DIR];
+      cL = cl.c;
+      unR = cr.rs.vel[DIR];
+      cR = cr.c;
+    } else {
+      Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+      Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
+      unL = qL.vel[DIR];
+      cL = sound_speed<M>(qL, pp);
+      unR = qR.vel[DIR];
+      cR = sound_speed<M>(qR, pp);
+    }
+    double lamL[NV], lamC[NV], lamR[NV];
+    eigvals<M>(unL, cL, lamL);
+    eigvals<M>(Eu.un, Eu.a, lamC);
+    eigvals<M>(unR, cR, lamR);
+    double fc[NV];
+    if (UPW == UPW_LLF) {
+      double sf[NV], du[NV], ws[NV], wd[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        sf[v] = fL[v] + fR[v];
+        du[v] = uL[v] - uR[v];
+      }
+      projL<M, DIR>(Eu, pp, sf, ws);
+      projL<M, DIR>(Eu, pp, du, wd);
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        double al = fmax(fmax(fabs(lamL[k]), fabs(lamC[k])), fabs(lamR[k]));
+        fc[k] = 0.5 * fma(al, wd[k], ws[k]);
+      }
+    } else {
+      double fcL[NV], fcR[NV], du[NV], wd[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) du[v] = uL[v] - uR[v];
+      projL<M, DIR>(Eu, pp, fL, fcL);
+      projL<M, DIR>(Eu, pp, fR, fcR);
+      projL<M, DIR>(Eu, pp, du, wd);
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        if (lamL[k] > 0 && lamC[k] > 0 && lamR[k] > 0) {
+          fc[k] = fcL[k];
+        } else if (lamL[k] < 0 && lamC[k] < 0 && lamR[k] < 0) {
+          fc[k] = fcR[k];
+        } else {
+          double al = fmax(fmax(fabs(lamL[k]), fabs(lamC[k])), fabs(lamR[k]));
+          fc[k] = 0.5 * fma(al, wd[k], fcL[k] + fcR[k]);
+        }
+      }
+    }
+    projR<M, DIR>(Eu, fc, fI);
+  }
+}
+
+template <int M, bool CHAR, int UPW, int DIR>
+__global__ void __launch_bounds__(128)
+hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
+               DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= ntrans * (long long)nseg) return;
+  long long tr = tid % ntrans;
+  const int sg = (int)(tid / ntrans);
+
+  long long pbase = (long long)G.g * G.stride[DIR];
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    if (e == DIR) continue;
+    int ie = (int)(tr % G.dim[e]);
+    tr /= G.dim[e];
+    pbase += (long long)(ie + G.g) * G.stride[e];
+  }
+  const int N = G.dim[DIR];
+  const long long sd = G.stride[DIR];
+  const int lo = G.bclo[DIR], hi = G.bchi[DIR];
+  const int I0 = sg * seg;
+  const int I1 = min(I0 + seg, N);
+  const double eps = pp.eps;
+
+  double wu[6][NV], wf[6][NV], wuc[6];
+  CellAux<M> ax[6];
+
+  auto load = [&](int i) {
+    const double* src = U + (pbase + (long long)fold_index(i, N, lo, hi) * sd) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; v++) wu[5][v] = src[v];
+    Prim<M> q = to_prim<M>(wu[5], pp);
+    cell_flux<M, DIR>(q, wf[5]);
+    wuc[5] = ufunc_energy<M>(q, pp, wu[5][NV - 1]);
+    if (CC) ax[5].rs = roe_side<M>(q);
+    if (M == MODEL_EULER1D && UPW != UPW_ROE) ax[5].c = sound_speed<M>(q, pp);
+  };
+  auto shift = [&]() {
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        wu[p][v] = wu[p + 1][v];
+        wf[p][v] = wf[p + 1][v];
+      }
+      wuc[p] = wuc[p + 1];
+      ax[p] = ax[p + 1];
+    }
+  };
+
+  for (int k = 0; k < 5; k++) {
+    load(I0 - 3 + k);
+    shift();
+  }
+
+  double fIp[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) fIp[v] = 0.0;
+
+  for (int I = I0; I <= I1; I++) {
+    load(I + 2);
+    double fL[NV], fR[NV], uL[NV], uR[NV];
+    Eig Ecc;
+    if (CC) Ecc = roe_eig<M, DIR>(ax[2].rs, ax[3].rs, pp);
+
+    if (!CHAR) {
+      // Component-wise WENO5: weights of the u-reconstruction from u, values from uC.
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        fL[v] = weno5(wf[0][v], wf[1][v], wf[2][v], wf[3][v], wf[4][v], eps);
+        fR[v] = weno5(wf[5][v], wf[4][v], wf[3][v], wf[2][v], wf[1][v], eps);
+        if (M == MODEL_NS3D && v == NV - 1) {
+          uL[v] = weno5_split(wu[0][v], wu[1][v], wu[2][v], wu[3][v], wu[4][v],
+                              wuc[0], wuc[1], wuc[2], wuc[3], wuc[4], eps);
+          uR[v] = weno5_split(wu[5][v], wu[4][v], wu[3][v], wu[2][v], wu[1][v],
+                              wuc[5], wuc[4], wuc[3], wuc[2], wuc[1], eps);
+        } else {
+          uL[v] = weno5(wu[0][v], wu[1][v], wu[2][v], wu[3][v], wu[4][v], eps);
+          uR[v] = weno5(wu[5][v], wu[4][v], wu[3][v], wu[2][v], wu[1][v], eps);
+        }
+      }
+    } else {
+      // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
+      // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
+      // from the Roe average of the two cell-centre states.
+      double cf[6][NV], cu[6][NV], cuc[6][3];
+#pragma unroll
+      for (int p = 0; p < 6; p++) {
+        projL<M, DIR>(Ecc, pp, wf[p], cf[p]);
+        projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
+        if (M == MODEL_NS3D) {
+          // uC differs from u in the energy only: add that column of L.
+          double de = pp.gm1 * (wuc[p] - wu[p][NV - 1]);
+          cuc[p][0] = fma(de, Ecc.hac, cu[p][0]);
+          cuc[p][1] = fma(de, Ecc.hac, cu[p][1]);
+          cuc[p][2] = fma(-de, Ecc.inv_a2, cu[p][2]);
+        }
+      }
+      double xfL[NV], xfR[NV], xuL[NV], xuR[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        xfL[v] = weno5(cf[0][v], cf[1][v], cf[2][v], cf[3][v], cf[4][v], eps);
+        xfR[v] = weno5(cf[5][v], cf[4][v], cf[3][v], cf[2][v], cf[1][v], eps);
+        if (M == MODEL_NS3D && v < 3) {
+          xuL[v] = weno5_split(cu[0][v], cu[1][v], cu[2][v], cu[3][v], cu[4][v],
+                               cuc[0][v], cuc[1][v], cuc[2][v], cuc[3][v], cuc[4][v], eps);
+          xuR[v] = weno5_split(cu[5][v], cu[4][v], cu[3][v], cu[2][v], cu[1][v],
+                               cuc[5][v], cuc[4][v], cuc[3][v], cuc[2][v], cuc[1][v], eps);
+        } else {
+          xuL[v] = weno5(cu[0][v], cu[1][v], cu[2][v], cu[3][v], cu[4][v], eps);
+          xuR[v] = weno5(cu[5][v], cu[4][v], cu[3][v], cu[2][v], cu[1][v], eps);
+        }
+      }
+      projR<M, DIR>(Ecc, xfL, fL);
+      projR<M, DIR>(Ecc, xfR, fR);
+      projR<M, DIR>(Ecc, xuL, uL);
+      projR<M, DIR>(Ecc, xuR, uR);
+    }
+
+    // Upwinding.
+    double fI[NV];
+    upwind_iface<M, CHAR, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);
+
+    if (I > I0) {
+      // Flux difference of cell I-1 and the stage epilogue.
+      const int c = I - 1;
+      const long long off = (pbase + (long long)c * sd) * NV;
+      const double dxi = dxinv[G.g + c];
+      const bool finish = ep.last && ep.mode != EPI_HYP;
+      double kv[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        double h = dxi * (fI[v] - fIp[v]);
+        double hyp = ep.first ? h : H[off + v] + h;
+        if (!finish) {
+          H[off + v] = hyp;
+        } else {
+          kv[v] = (ep.par ? ep.par[off + v] : 0.0) - hyp;
+        }
+      }
+      if (finish) {
+        if (ep.mode == EPI_RHS) {
+#pragma unroll
+          for (int v = 0; v < NV; v++) ep.rhs[off + v] = kv[v];
+        } else {
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            const double uv = ep.need_u ? ep.u[off + v] : 0.0;
+            double av = fma(ep.cb, kv[v], ep.stage == 0 ? uv : ep.acc[off + v]);
+            if (ep.stage == ep.nstages - 1) ep.uout[off + v] = av;
+            else ep.acc[off + v] = av;
+#pragma unroll
+            for (int t = 1; t < 4; t++) {
+              if (t > ep.stage && t < ep.nstages && ep.ca[t] != 0.0) {
+                double base = ep.touched[t] ? ep.P[t][off + v] : uv;
+                ep.P[t][off + v] = fma(ep.ca[t], kv[v], base);
+              }
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; v++) fIp[v] = fI[v];
+    shift();
+  }
+}
+
+// Host launcher for one direction.
+template <int M, bool CHAR, int UPW, int DIR>
+cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
+                       const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
+  long long ntrans = 1;
+  for (int e = 0; e < G.nd; e++)
+    if (e != DIR) ntrans *= G.dim[e];
+  int seg = L.seg > 0 ? L.seg : 32;
+  int N = G.dim[DIR];
+  int nseg = (N + seg - 1) / seg;
+  long long nthr = ntrans * nseg;
+  int block = L.block > 0 ? L.block : 128;
+  long long grid = (nthr + block - 1) / block;
+  hyp_dir_kernel<M, CHAR, UPW, DIR><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg, nseg, ntrans);
+  return cudaGetLastError();
+}
+
+template <int M, bool CHAR, int UPW>
+cudaError_t launch_dir_any(int dir, const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
+                           const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
+  constexpr int ND = ModelTraits<M>::ND;
+  if (dir == 0) return launch_dir<M, CHAR, UPW, 0>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (ND > 1 && dir == 1) return launch_dir<M, CHAR, UPW, (ND > 1 ? 1 : 0)>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (ND > 2 && dir == 2) return launch_dir<M, CHAR, UPW, (ND > 2 ? 2 : 0)>(U, H, dxinv_dir, G, pp, ep, L, s);
+  return cudaErrorInvalidValue;
+}
+
+template <int M>
+cudaError_t launch_hyp_model(int dir, int chr, int upw, const double* U, double* H, const double* dxinv_dir,
+                             const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
+                             cudaStream_t s) {
+  if (chr) {
+    if (upw == UPW_ROE) return launch_dir_any<M, true, UPW_ROE>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_LLF) return launch_dir_any<M, true, UPW_LLF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir_any<M, true, UPW_RF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+  } else {
+    if (upw == UPW_ROE) return launch_dir_any<M, false, UPW_ROE>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_LLF) return launch_dir_any<M, false, UPW_LLF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir_any<M, false, UPW_RF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Unfused pieces of the HyPar function-pointer surface (FFunction, UFunction,
+// Upwind), one thread per point / interface, on HyPar's own array layouts.
+// ---------------------------------------------------------------------------
+template <int M, int DIR>
+__global__ void flux_kernel(double* __restrict__ f, const double* __restrict__ u, long long npts, PhysParams pp) {
+  constexpr int NV = ModelTraits<M>::NV;
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  double uu[NV], ff[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) uu[v] = u[p * NV + v];
+  Prim<M> q = to_prim<M>(uu, pp);
+  cell_flux<M, DIR>(q, ff);
+#pragma unroll
+  for (int v = 0; v < NV; v++) f[p * NV + v] = ff[v];
+}
+
+template <int M>
+__global__ void ufunc_kernel(double* __restrict__ uC, const double* __restrict__ u, long long npts, PhysParams pp) {
+  constexpr int NV = ModelTraits<M>::NV;
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npts) return;
+  double uu[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) uu[v] = u[p * NV + v];
+  Prim<M> q = to_prim<M>(uu, pp);
+#pragma unroll
+  for (int v = 0; v < NV - 1; v++) uC[p * NV + v] = uu[v];
+  uC[p * NV + NV - 1] = ufunc_energy<M>(q, pp, uu[NV - 1]);
+}
+
+// Interface arrays have no ghost points and dim[DIR]+1 entries along DIR
+// (include/hypar.h:133-145); u is the ghosted cell-centre solution.
+template <int M, int UPW, int DIR>
+__global__ void upwind_kernel(double* __restrict__ fI, const double* __restrict__ fL, const double* __restrict__ fR,
+                              const double* __restrict__ uL, const double* __restrict__ uR,
+                              const double* __restrict__ u, DevGeom G, PhysParams pp, long long nint) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nint) return;
+  int idx[3] = {0, 0, 0};
+  long long r = p;
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    int n = G.dim[e] + (e == DIR ? 1 : 0);
+    idx[e] = (int)(r % n);
+    r /= n;
+  }
+  long long pc = 0;
+#pragma unroll
+  for (int e = 0; e < ND; e++) pc += (long long)(idx[e] + G.g) * G.stride[e];
+  long long pL = pc - G.stride[DIR], pR = pc;
+  double a[NV], b[NV], c[NV], d[NV], ucl[NV], ucr[NV], out[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    a[v] = fL[p * NV + v];
+    b[v] = fR[p * NV + v];
+    c[v] = uL[p * NV + v];
+    d[v] = uR[p * NV + v];
+    ucl[v] = u[pL * NV + v];
+    ucr[v] = u[pR * NV + v];
+  }
+  Prim<M> ql = to_prim<M>(ucl, pp), qr = to_prim<M>(ucr, pp);
+  CellAux<M> cl, cr;
+  cl.rs = roe_side<M>(ql);
+  cr.rs = roe_side<M>(qr);
+  cl.c = sound_speed<M>(ql, pp);
+  cr.c = sound_speed<M>(qr, pp);
+  Eig Ecc = roe_eig<M, DIR>(cl.rs, cr.rs, pp);
+  upwind_iface<M, true, UPW, DIR>(a, b, c, d, Ecc, cl, cr, pp, out);
+#pragma unroll
+  for (int v = 0; v < NV; v++) fI[p * NV + v] = out[v];
+}
+
+enum { UNFUSED_FLUX = 0, UNFUSED_UFUNC = 1, UNFUSED_UPWIND = 2 };
+
+template <int M, int DIR>
+cudaError_t launch_unfused_dir(int kind, int upw, double* out, const double* a, const double* b, const double* c,
+                               const double* d, const double* u, const DevGeom& G, const PhysParams& pp,
+                               cudaStream_t s) {
+  long long npts = 1, nint = 1;
+  for (int e = 0; e < G.nd; e++) {
+    npts *= G.dim[e] + 2 * G.g;
+    nint *= G.dim[e] + (e == DIR ? 1 : 0);
+  }
+  const int blk = 128;
+  if (kind == UNFUSED_FLUX) {
+    flux_kernel<M, DIR><<<(unsigned)((npts + blk - 1) / blk), blk, 0, s>>>(out, u, npts, pp);
+  } else if (kind == UNFUSED_UFUNC) {
+    ufunc_kernel<M><<<(unsigned)((npts + blk - 1) / blk), blk, 0, s>>>(out, u, npts, pp);
+  } else {
+    unsigned grid = (unsigned)((nint + blk - 1) / blk);
+    if (upw == UPW_ROE) upwind_kernel<M, UPW_ROE, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+    else if (upw == UPW_LLF) upwind_kernel<M, UPW_LLF, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+    else upwind_kernel<M, UPW_RF, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+  }
+  return cudaGetLastError();
+}
+
+template <int M>
+cudaError_t launch_unfused_model(int kind, int dir, int upw, double* out, const double* a, const double* b,
+                                 const double* c, const double* d, const double* u, const DevGeom& G,
+                                 const PhysParams& pp, cudaStream_t s) {
+  constexpr int ND = ModelTraits<M>::ND;
+  if (dir == 0) return launch_unfused_dir<M, 0>(kind, upw, out, a, b, c, d, u, G, pp, s);
+  if (ND > 1 && dir == 1) return launch_unfused_dir<M, (ND > 1 ? 1 : 0)>(kind, upw, out, a, b, c, d, u, G, pp, s);
+  if (ND > 2 && dir == 2) return launch_unfused_dir<M, (ND > 2 ? 2 : 0)>(kind, upw, out, a, b, c, d, u, G, pp, s);
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gbh

@@ -1,0 +1,536 @@
+/*
+ * gbh_inputs.c -- HyPar input decks on the host (C).
+ *
+ * Reads the files HyPar reads for this path, with the reference's formats and
+ * defaults:
+ *   solver.inp   ReadInputs           (src/Simulation/ReadInputs.c:94-440)
+ *   physics.inp  Euler1DInitialize / Euler2DInitialize / NavierStokes3DInitialize
+ *                (src/PhysicalModels/Euler1D/Euler1DInitialize.c:71-140,
+ *                 Euler2D/Euler2DInitialize.c:21-70, NavierStokes3D/NavierStokes3DInitialize.c:116-370)
+ *   weno.inp     WENOInitialize       (src/InterpolationFunctions/WENOInitialize.c:34-112)
+ *   boundary.inp InitializeBoundaries (src/Simulation/InitializeBoundaries.c:75-180)
+ *                with the index extents of CalculateLocalExtent (:365-420) and
+ *                FindInterval (src/MathFunctions/FindInterval.c:19-45)
+ *   initial.inp  ReadArraySerial      (src/IOFunctions/ReadArray.c:150-300), ghost grid
+ *                extrapolation (:68-88) and dxinv (src/Simulation/InitialSolution.c:69-99)
+ * Options outside this library's path (other models, schemes, boundary types,
+ * gravity, MPI decompositions) are rejected with GB_ERR_UNSUPPORTED.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gbhypar.h"
+
+void gbh_set_error(const char *fmt, ...);
+
+struct gb_inputs {
+  gb_config cfg;
+  double *x;      /* interior grid, sum dim */
+  double *dxinv;  /* with ghosts */
+  double *u0;     /* interior solution */
+  char op_overwrite[64];
+};
+
+#define MAXS 512
+
+static FILE *open_in(const char *dir, const char *name, const char *mode) {
+  char path[4096];
+  if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s", dir, name);
+  else snprintf(path, sizeof(path), "%s", name);
+  return fopen(path, mode);
+}
+
+int gb_rk_table(const char *type, int *ns, double *A, double *b, double *c) {
+  /* TimeExplicitRKInitialize (src/TimeIntegration/TimeExplicitRKInitialize.c:28-80) */
+  for (int i = 0; i < 16; i++) A[i] = 0.0;
+  for (int i = 0; i < 4; i++) b[i] = c[i] = 0.0;
+  if (!strcmp(type, "1fe")) {
+    *ns = 1;
+    b[0] = 1.0;
+  } else if (!strcmp(type, "22")) {
+    *ns = 2;
+    A[2] = 1.0;
+    c[1] = 1.0;
+    b[0] = b[1] = 0.5;
+  } else if (!strcmp(type, "33")) {
+    *ns = 3;
+    A[3] = 2.0 / 3.0;
+    A[6] = 2.0 / 3.0 - 1.0 / 4.0;
+    A[7] = 1.0 / 4.0;
+    c[1] = 2.0 / 3.0;
+    c[2] = 2.0 / 3.0;
+    b[0] = 1.0 / 4.0;
+    b[1] = -1.0 / 4.0;
+    b[2] = 1.0;
+  } else if (!strcmp(type, "44")) {
+    *ns = 4;
+    A[4] = 0.5;
+    A[9] = 0.5;
+    A[14] = 1.0;
+    c[1] = c[2] = 0.5;
+    c[3] = 1.0;
+    b[0] = 1.0 / 6.0;
+    b[1] = 1.0 / 3.0;
+    b[2] = 1.0 / 3.0;
+    b[3] = 1.0 / 6.0;
+  } else if (!strcmp(type, "ssprk3") || !strcmp(type, "tvdrk3")) {
+    *ns = 3;
+    A[3] = 1.0;
+    A[6] = 0.25;
+    A[7] = 0.25;
+    c[1] = 1.0;
+    c[2] = 0.5;
+    b[0] = b[1] = 1.0 / 6.0;
+    b[2] = 2.0 / 3.0;
+  } else {
+    gbh_set_error("time_scheme_type %s is not an explicit RK scheme of this library", type);
+    return GB_ERR_UNSUPPORTED;
+  }
+  /* store A with row stride 4 */
+  double T[16];
+  for (int i = 0; i < 16; i++) T[i] = 0.0;
+  for (int i = 0; i < *ns; i++)
+    for (int j = 0; j < *ns; j++) T[4 * i + j] = A[(*ns) * i + j];
+  for (int i = 0; i < 16; i++) A[i] = T[i];
+  return GB_OK;
+}
+
+/* FindInterval (src/MathFunctions/FindInterval.c:19-45). */
+static void find_interval(double a, double b, const double *x, int N, int *imin, int *imax) {
+  *imax = -1;
+  *imin = N;
+  double min_dx = x[1] - x[0];
+  for (int i = 2; i < N; i++) {
+    double dx = x[i] - x[i - 1];
+    if (dx < min_dx) min_dx = dx;
+  }
+  double tol = 1e-10 * min_dx;
+  for (int i = 0; i < N; i++)
+    if (x[i] <= (b + tol)) *imax = i + 1;
+  for (int i = N - 1; i > -1; i--)
+    if (x[i] >= (a - tol)) *imin = i;
+}
+
+typedef struct {
+  int ndims, nvars, ghosts, n_iter, file_op_iter;
+  int size[3], iproc[3];
+  double dt;
+  char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
+  char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
+  char op_overwrite[MAXS], hyp_flux_split[MAXS];
+} solver_inp;
+
+static int read_solver_inp(const char *dir, solver_inp *si) {
+  memset(si, 0, sizeof(*si));
+  si->ndims = 1;
+  si->nvars = 1;
+  si->ghosts = 1;
+  si->file_op_iter = 1000;
+  strcpy(si->time_scheme, "euler");
+  strcpy(si->time_scheme_type, " ");
+  strcpy(si->hyp_space_scheme, "1");
+  strcpy(si->interp_type, "characteristic");
+  strcpy(si->par_space_type, "nonconservative-1stage");
+  strcpy(si->par_space_scheme, "2");
+  strcpy(si->ip_file_type, "ascii");
+  strcpy(si->op_overwrite, "no");
+  strcpy(si->model, "none");
+  strcpy(si->hyp_flux_split, "no");
+  FILE *in = open_in(dir, "solver.inp", "r");
+  if (!in) {
+    gbh_set_error("file solver.inp not found");
+    return GB_ERR_INPUT;
+  }
+  char w[MAXS];
+  int ok = 1;
+  if (fscanf(in, "%511s", w) != 1 || strcmp(w, "begin")) {
+    fclose(in);
+    gbh_set_error("illegal format in solver.inp");
+    return GB_ERR_INPUT;
+  }
+  int have_ndims = 0;
+  while (ok) {
+    if (fscanf(in, "%511s", w) != 1) { ok = 0; break; }
+    if (!strcmp(w, "end")) break;
+    int r = 1;
+    if (!strcmp(w, "ndims")) { r = fscanf(in, "%d", &si->ndims); have_ndims = 1; }
+    else if (!strcmp(w, "nvars")) r = fscanf(in, "%d", &si->nvars);
+    else if (!strcmp(w, "size") || !strcmp(w, "iproc") || !strcmp(w, "size_exact")) {
+      if (!have_ndims || si->ndims < 1 || si->ndims > 3) { ok = 0; break; }
+      int *dst = !strcmp(w, "size") ? si->size : (!strcmp(w, "iproc") ? si->iproc : NULL);
+      for (int d = 0; d < si->ndims; d++) {
+        int val;
+        r = fscanf(in, "%d", &val);
+        if (r != 1) break;
+        if (dst) dst[d] = val;
+      }
+    }
+    else if (!strcmp(w, "ghost")) r = fscanf(in, "%d", &si->ghosts);
+    else if (!strcmp(w, "n_iter")) r = fscanf(in, "%d", &si->n_iter);
+    else if (!strcmp(w, "time_scheme")) r = fscanf(in, "%511s", si->time_scheme);
+    else if (!strcmp(w, "time_scheme_type")) r = fscanf(in, "%511s", si->time_scheme_type);
+    else if (!strcmp(w, "hyp_space_scheme")) r = fscanf(in, "%511s", si->hyp_space_scheme);
+    else if (!strcmp(w, "hyp_flux_split")) r = fscanf(in, "%511s", si->hyp_flux_split);
+    else if (!strcmp(w, "hyp_interp_type")) r = fscanf(in, "%511s", si->interp_type);
+    else if (!strcmp(w, "par_space_type")) r = fscanf(in, "%511s", si->par_space_type);
+    else if (!strcmp(w, "par_space_scheme")) r = fscanf(in, "%511s", si->par_space_scheme);
+    else if (!strcmp(w, "dt")) r = fscanf(in, "%lf", &si->dt);
+    else if (!strcmp(w, "file_op_iter")) r = fscanf(in, "%d", &si->file_op_iter);
+    else if (!strcmp(w, "ip_file_type")) r = fscanf(in, "%511s", si->ip_file_type);
+    else if (!strcmp(w, "op_overwrite")) r = fscanf(in, "%511s", si->op_overwrite);
+    else if (!strcmp(w, "model")) r = fscanf(in, "%511s", si->model);
+    else if (!strcmp(w, "input_mode") || !strcmp(w, "output_mode")) {
+      char mode[MAXS];
+      r = fscanf(in, "%511s", mode);
+      if (r == 1 && strcmp(mode, "serial")) { int nio; r = fscanf(in, "%d", &nio); }
+    } else {
+      char useless[MAXS];  /* every other keyword takes one value (restart_iter, screen_op_iter, ...) */
+      r = fscanf(in, "%511s", useless);
+    }
+    if (r != 1) ok = 0;
+  }
+  fclose(in);
+  if (!ok) {
+    gbh_set_error("could not parse solver.inp");
+    return GB_ERR_INPUT;
+  }
+  return GB_OK;
+}
+
+/* Generic "begin key value ... end" reader for physics.inp / weno.inp. */
+typedef struct { const char *key; char type; void *dst; } kv_t;
+
+static int read_kv_file(const char *dir, const char *name, kv_t *kv, int nkv, int required) {
+  FILE *in = open_in(dir, name, "r");
+  if (!in) {
+    if (required) {
+      gbh_set_error("file %s not found", name);
+      return GB_ERR_INPUT;
+    }
+    return GB_OK; /* reference: optional, defaults apply */
+  }
+  char w[MAXS];
+  if (fscanf(in, "%511s", w) != 1 || strcmp(w, "begin")) {
+    fclose(in);
+    gbh_set_error("illegal format in %s", name);
+    return GB_ERR_INPUT;
+  }
+  for (;;) {
+    if (fscanf(in, "%511s", w) != 1) {
+      fclose(in);
+      gbh_set_error("could not parse %s", name);
+      return GB_ERR_INPUT;
+    }
+    if (!strcmp(w, "end")) break;
+    int found = 0, r = 1;
+    for (int i = 0; i < nkv; i++) {
+      if (strcmp(w, kv[i].key)) continue;
+      found = 1;
+      if (kv[i].type == 'd') r = fscanf(in, "%lf", (double *)kv[i].dst);
+      else if (kv[i].type == 'i') r = fscanf(in, "%d", (int *)kv[i].dst);
+      else r = fscanf(in, "%511s", (char *)kv[i].dst);
+      break;
+    }
+    if (!found) {
+      char useless[MAXS];
+      r = fscanf(in, "%511s", useless);
+    }
+    if (r != 1) {
+      fclose(in);
+      gbh_set_error("could not parse %s", name);
+      return GB_ERR_INPUT;
+    }
+  }
+  fclose(in);
+  return GB_OK;
+}
+
+static void grid_ghosts(const double *x, int n, int g, double *X) {
+  for (int i = 0; i < n; i++) X[g + i] = x[i];
+  for (int i = 0; i < g; i++) {
+    int delta = g - i;
+    X[i] = X[g] + ((double)delta) * (X[g] - X[g + 1]);
+  }
+  for (int i = n + g; i < n + 2 * g; i++) {
+    int delta = i - (n + g - 1);
+    X[i] = X[n + g - 1] + ((double)delta) * (X[n + g - 1] - X[n + g - 2]);
+  }
+}
+
+void gb_inputs_free(gb_inputs *in) {
+  if (!in) return;
+  free(in->x);
+  free(in->dxinv);
+  free(in->u0);
+  free(in);
+}
+
+const gb_config *gb_inputs_config(const gb_inputs *in) { return in ? &in->cfg : NULL; }
+const double *gb_inputs_x(const gb_inputs *in) { return in ? in->x : NULL; }
+const double *gb_inputs_dxinv(const gb_inputs *in) { return in ? in->dxinv : NULL; }
+const double *gb_inputs_u0(const gb_inputs *in) { return in ? in->u0 : NULL; }
+const char *gbh_inputs_op_overwrite(const gb_inputs *in) { return in ? in->op_overwrite : "yes"; }
+
+int gb_inputs_read(const char *dir, gb_inputs **out) {
+  if (!out) {
+    gbh_set_error("gb_inputs_read: null output");
+    return GB_ERR_ARG;
+  }
+  *out = NULL;
+  solver_inp si;
+  int rc = read_solver_inp(dir, &si);
+  if (rc) return rc;
+  gb_config c;
+  memset(&c, 0, sizeof(c));
+  if (!strcmp(si.model, "euler1d")) c.model = GB_MODEL_EULER1D;
+  else if (!strcmp(si.model, "euler2d")) c.model = GB_MODEL_EULER2D;
+  else if (!strcmp(si.model, "navierstokes3d")) c.model = GB_MODEL_NS3D;
+  else {
+    gbh_set_error("model %s is not one of euler1d, euler2d, navierstokes3d", si.model);
+    return GB_ERR_UNSUPPORTED;
+  }
+  int want_nd = c.model == GB_MODEL_EULER1D ? 1 : (c.model == GB_MODEL_EULER2D ? 2 : 3);
+  int want_nv = want_nd + 2;
+  if (si.ndims != want_nd || si.nvars != want_nv) {
+    gbh_set_error("%s needs ndims %d and nvars %d", si.model, want_nd, want_nv);
+    return GB_ERR_INPUT;
+  }
+  c.ndims = si.ndims;
+  c.nvars = si.nvars;
+  c.ghosts = si.ghosts;
+  for (int d = 0; d < 3; d++) c.dim[d] = d < c.ndims ? si.size[d] : 1;
+  for (int d = 0; d < c.ndims; d++) {
+    if (c.dim[d] < 4) {
+      gbh_set_error("size along dimension %d is %d (at least 4 needed)", d, c.dim[d]);
+      return GB_ERR_INPUT;
+    }
+    if (si.iproc[d] > 1) fprintf(stderr, "gbhypar: iproc %d along dimension %d ignored (one GPU holds the whole domain)\n", si.iproc[d], d);
+  }
+  if (c.ghosts != 3) {
+    gbh_set_error("ghost must be 3 for weno5 (got %d)", c.ghosts);
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (strcmp(si.hyp_space_scheme, "weno5")) {
+    gbh_set_error("hyp_space_scheme %s not supported (weno5 only)", si.hyp_space_scheme);
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (strcmp(si.hyp_flux_split, "no")) {
+    gbh_set_error("hyp_flux_split %s not supported", si.hyp_flux_split);
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (!strcmp(si.interp_type, "components")) c.interp = GB_INTERP_COMPONENTS;
+  else if (!strcmp(si.interp_type, "characteristic")) c.interp = GB_INTERP_CHARACTERISTIC;
+  else {
+    gbh_set_error("hyp_interp_type %s invalid", si.interp_type);
+    return GB_ERR_INPUT;
+  }
+  if (strcmp(si.time_scheme, "rk")) {
+    gbh_set_error("time_scheme %s not supported (rk only)", si.time_scheme);
+    return GB_ERR_UNSUPPORTED;
+  }
+  rc = gb_rk_table(si.time_scheme_type, &c.rk_nstages, c.rk_A, c.rk_b, c.rk_c);
+  if (rc) return rc;
+  c.dt = si.dt;
+  c.n_iter = si.n_iter;
+  c.file_op_iter = si.file_op_iter;
+
+  /* physics.inp */
+  char upw[MAXS] = "roe";
+  c.gamma = 1.4;
+  c.Re = -1.0;
+  c.Pr = 0.72;
+  c.Minf = 1.0;
+  double grav = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+  kv_t pk[] = {{"gamma", 'd', &c.gamma}, {"upwinding", 's', upw}, {"gravity", 'd', &grav},
+               {"Pr", 'd', &c.Pr}, {"Re", 'd', &c.Re}, {"Minf", 'd', &c.Minf},
+               {"gravity_x", 'd', &gx}, {"gravity_y", 'd', &gy}, {"gravity_z", 'd', &gz}};
+  rc = read_kv_file(dir, "physics.inp", pk, 9, 0);
+  if (rc) return rc;
+  if (grav != 0.0 || gx != 0.0 || gy != 0.0 || gz != 0.0) {
+    gbh_set_error("gravity is not supported on this path");
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (!strcmp(upw, "roe")) c.upwind = GB_UPWIND_ROE;
+  else if (!strcmp(upw, "llf-char")) c.upwind = GB_UPWIND_LLF;
+  else if (!strcmp(upw, "rf-char")) c.upwind = GB_UPWIND_RF;
+  else {
+    gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char)", upw);
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (c.model == GB_MODEL_NS3D && c.Re > 0) {
+    if (strcmp(si.par_space_type, "nonconservative-2stage")) {
+      gbh_set_error("NavierStokes3D needs par_space_type nonconservative-2stage");
+      return GB_ERR_INPUT;
+    }
+    if (strcmp(si.par_space_scheme, "4")) {
+      gbh_set_error("par_space_scheme %s not supported (4 only)", si.par_space_scheme);
+      return GB_ERR_UNSUPPORTED;
+    }
+  }
+
+  /* weno.inp */
+  int mapped = 0, borges = 0, yc = 0, no_limiting = 0;
+  c.weno_eps = 1e-6;
+  kv_t wk[] = {{"mapped", 'i', &mapped}, {"borges", 'i', &borges}, {"yc", 'i', &yc},
+               {"no_limiting", 'i', &no_limiting}, {"epsilon", 'd', &c.weno_eps}};
+  rc = read_kv_file(dir, "weno.inp", wk, 5, 0);
+  if (rc) return rc;
+  if (mapped || borges || yc || no_limiting) {
+    gbh_set_error("only Jiang-Shu WENO5 weights are supported (mapped/borges/yc/no_limiting must be 0)");
+    return GB_ERR_UNSUPPORTED;
+  }
+
+  gb_inputs *res = (gb_inputs *)calloc(1, sizeof(gb_inputs));
+  strncpy(res->op_overwrite, si.op_overwrite, sizeof(res->op_overwrite) - 1);
+  long nx = 0, nxg = 0, npts = 1;
+  for (int d = 0; d < c.ndims; d++) {
+    nx += c.dim[d];
+    nxg += c.dim[d] + 2 * c.ghosts;
+    npts *= c.dim[d];
+  }
+  res->x = (double *)calloc(nx, sizeof(double));
+  res->dxinv = (double *)calloc(nxg, sizeof(double));
+  res->u0 = (double *)calloc(npts * c.nvars, sizeof(double));
+
+  /* initial.inp */
+  if (!strcmp(si.ip_file_type, "bin") || !strcmp(si.ip_file_type, "binary")) {
+    FILE *in = open_in(dir, "initial.inp", "rb");
+    if (!in) {
+      gb_inputs_free(res);
+      gbh_set_error("initial solution file initial.inp not found");
+      return GB_ERR_INPUT;
+    }
+    size_t a = fread(res->x, sizeof(double), nx, in);
+    size_t b = fread(res->u0, sizeof(double), npts * c.nvars, in);
+    fclose(in);
+    if ((long)a != nx || (long)b != npts * c.nvars) {
+      gb_inputs_free(res);
+      gbh_set_error("initial.inp is too short");
+      return GB_ERR_INPUT;
+    }
+  } else if (!strcmp(si.ip_file_type, "ascii")) {
+    FILE *in = open_in(dir, "initial.inp", "r");
+    if (!in) {
+      gb_inputs_free(res);
+      gbh_set_error("initial solution file initial.inp not found");
+      return GB_ERR_INPUT;
+    }
+    int bad = 0;
+    for (long i = 0; i < nx && !bad; i++) bad = fscanf(in, "%lf", &res->x[i]) != 1;
+    for (int v = 0; v < c.nvars && !bad; v++)
+      for (long p = 0; p < npts && !bad; p++) bad = fscanf(in, "%lf", &res->u0[p * c.nvars + v]) != 1;
+    fclose(in);
+    if (bad) {
+      gb_inputs_free(res);
+      gbh_set_error("could not read initial.inp");
+      return GB_ERR_INPUT;
+    }
+  } else {
+    gb_inputs_free(res);
+    gbh_set_error("ip_file_type %s invalid", si.ip_file_type);
+    return GB_ERR_INPUT;
+  }
+
+  /* dxinv with ghosts */
+  {
+    long off = 0, offg = 0;
+    for (int d = 0; d < c.ndims; d++) {
+      int n = c.dim[d], g = c.ghosts;
+      double *X = (double *)malloc(sizeof(double) * (n + 2 * g));
+      grid_ghosts(res->x + off, n, g, X);
+      double *D = res->dxinv + offg;
+      for (int i = 0; i < n; i++) D[i + g] = 2.0 / (X[i + 1 + g] - X[i - 1 + g]);
+      for (int i = 0; i < g; i++) D[i] = D[g];
+      for (int i = n + g; i < n + 2 * g; i++) D[i] = D[n + g - 1];
+      free(X);
+      off += n;
+      offg += n + 2 * g;
+    }
+  }
+
+  /* boundary.inp */
+  {
+    FILE *in = open_in(dir, "boundary.inp", "r");
+    if (!in) {
+      gb_inputs_free(res);
+      gbh_set_error("boundary condition file boundary.inp not found");
+      return GB_ERR_INPUT;
+    }
+    int nb = 0;
+    if (fscanf(in, "%d", &nb) != 1 || nb < 0 || nb > GB_MAX_ZONES) {
+      fclose(in);
+      gb_inputs_free(res);
+      gbh_set_error("boundary.inp: bad zone count");
+      return GB_ERR_INPUT;
+    }
+    c.nzones = nb;
+    for (int z = 0; z < nb; z++) {
+      char type[MAXS];
+      int dim, face;
+      double xmin[3], xmax[3];
+      int bad = fscanf(in, "%511s %d %d", type, &dim, &face) != 3;
+      for (int d = 0; d < c.ndims && !bad; d++) bad = fscanf(in, "%lf %lf", &xmin[d], &xmax[d]) != 2;
+      if (bad || dim < 0 || dim >= c.ndims || (face != 1 && face != -1)) {
+        fclose(in);
+        gb_inputs_free(res);
+        gbh_set_error("boundary.inp: bad zone %d", z);
+        return GB_ERR_INPUT;
+      }
+      int tcode = 0;
+      if (!strcmp(type, "periodic")) tcode = GB_BC_PERIODIC;
+      else if (!strcmp(type, "extrapolate")) tcode = GB_BC_EXTRAPOLATE;
+      else {
+        fclose(in);
+        gb_inputs_free(res);
+        gbh_set_error("boundary type %s not supported (periodic, extrapolate)", type);
+        return GB_ERR_UNSUPPORTED;
+      }
+      int *zz = c.zones[z];
+      zz[0] = tcode;
+      zz[1] = dim;
+      zz[2] = face;
+      long off = 0;
+      for (int d = 0; d < 3; d++) {
+        int is = 0, ie = 1;
+        if (d < c.ndims) {
+          if (d == dim) {
+            if (face == 1) { is = -c.ghosts; ie = 0; }
+            else { is = c.dim[d]; ie = c.dim[d] + c.ghosts; }
+          } else {
+            find_interval(xmin[d], xmax[d], res->x + off, c.dim[d], &is, &ie);
+          }
+          off += c.dim[d];
+        }
+        zz[3 + d] = is;
+        zz[6 + d] = ie;
+      }
+    }
+    fclose(in);
+  }
+  res->cfg = c;
+  *out = res;
+  return GB_OK;
+}
+
+int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u) {
+  /* WriteBinary (src/IOFunctions/WriteBinary.c) */
+  FILE *out = fopen(path, "wb");
+  if (!out) {
+    gbh_set_error("could not open %s for writing", path);
+    return GB_ERR_INPUT;
+  }
+  long nx = 0, n = 1;
+  for (int d = 0; d < ndims; d++) {
+    nx += dim[d];
+    n *= dim[d];
+  }
+  fwrite(&ndims, sizeof(int), 1, out);
+  fwrite(&nvars, sizeof(int), 1, out);
+  fwrite(dim, sizeof(int), ndims, out);
+  fwrite(x, sizeof(double), nx, out);
+  fwrite(u, sizeof(double), n * nvars, out);
+  fclose(out);
+  return GB_OK;
+}

@@ -1,0 +1,62 @@
+// gbh_internal.h -- structures shared by the CUDA translation units of
+// libgbhypar (not part of the public C ABI, which is include/gbhypar.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gbh_device.cuh"
+
+namespace gbh {
+
+// Ghost-cell source along one face, folded into every halo load:
+// memory = read the ghost point stored in the array (filled by the boundary
+// kernel), periodic = wrap to the opposite interior cell, mirror = HyPar's
+// "extrapolate" boundary (a mirror copy, BCExtrapolate.c:37-38).
+enum { FOLD_MEMORY = 0, FOLD_PERIODIC = 1, FOLD_MIRROR = 2 };
+
+struct DevGeom {
+  int nd, g;
+  int dim[3];
+  long long stride[3];   // point strides including ghosts
+  int bclo[3], bchi[3];  // FOLD_* per face
+};
+
+// What the last direction of a stage does with the accumulated hyperbolic
+// term (hyp = sum over directions of dxinv (F[j+1/2]-F[j-1/2])):
+//   EPI_HYP  : store hyp into H (first direction) or add it to H
+//   EPI_RHS  : rhs = -hyp + par  into `rhs`
+//   EPI_RK   : k = -hyp + par, then the Runge-Kutta stage update
+enum { EPI_HYP = 0, EPI_RHS = 1, EPI_RK = 2 };
+
+struct StageEpi {
+  int mode;        // EPI_*
+  int first;       // this direction is the first one (H is not read)
+  int last;        // this direction is the last one
+  const double* par;  // viscous term or nullptr
+  double* rhs;        // EPI_RHS output
+  // Runge-Kutta stage update (EPI_RK): with k this stage's right-hand side,
+  //   acc   = (stage == 0 ? u : acc) + cb k        (u = acc on the last stage)
+  //   P[t]  = (touched[t] ? P[t] : u) + ca[t] k    for later stages t with ca[t] != 0
+  int stage, nstages;
+  double cb;
+  double ca[4];
+  int touched[4];
+  int need_u;      // u is read this stage (first stage, or a P[t] is first touched)
+  double* u;       // current solution (read)
+  double* uout;    // where the last stage writes the new solution
+  double* acc;
+  double* P[4];
+};
+
+// NavierStokes3D viscous-term constants (NavierStokes3DParabolicFunction.c:76-79).
+struct ViscParams {
+  double gamma, gm1, inv_Re, inv_Pr, inv_gm1;
+};
+
+// Per-launch configuration of the hyperbolic kernels.
+struct HypLaunch {
+  int seg;         // interfaces walked by one thread
+  int block;       // threads per block
+};
+
+}  // namespace gbh

@@ -1,0 +1,53 @@
+// gbh_probe.cu -- FP64 FMA throughput probe: the denominator of the FP64-pipe
+// roofline reported next to the fused kernels (the chip's measured DFMA rate,
+// not a datasheet figure).  Eight independent FMA chains per thread, all
+// operands in registers, enough blocks to fill every SM several times.
+#include <cuda_runtime.h>
+
+#include "gbhypar.h"
+
+extern "C" void gbh_set_error(const char* fmt, ...);
+
+namespace gbh {
+__global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+  }
+  double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+}  // namespace gbh
+
+extern "C" int gb_probe_fp64_peak(double* tflops) {
+  if (!tflops) { gbh_set_error("gb_probe_fp64_peak: null argument"); return GB_ERR_ARG; }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) { gbh_set_error("cudaMalloc failed"); return GB_ERR_CUDA; }
+  const int threads = 256, iters = 2048;
+  const int blocks = sms * 8;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  gbh::dfma_probe_kernel<<<blocks, threads>>>(out, 64, 0.999999, 1e-7);  // warm-up
+  cudaEventRecord(e0);
+  gbh::dfma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess || ms <= 0.f) { gbh_set_error("probe failed: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+  double flops = 2.0 * 8.0 * 16.0 * (double)iters * threads * (double)blocks;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return GB_OK;
+}

@@ -1,0 +1,223 @@
+"""Python mirror of libgbhypar's C ABI.
+
+``Solver`` wraps a gb_solver: HyPar's function-pointer surface
+(``hyperbolic``, ``parabolic``, ``flux``, ``ufunc``, ``upwind``, ``apply_bc``,
+``rhs``, ``time_rk``) on device arrays, and the fused fast path (``step``).
+Device arrays are torch CUDA tensors (torch supplies device memory and
+streams only); host arrays are numpy.  Arrays use HyPar's layout: ghost points
+on every side, dimension 0 fastest, the nvars components of a point
+contiguous.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import GbConfig, check, lib
+
+
+def _ptr(a) -> int:
+    """Device or host address of a torch tensor / numpy array."""
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class Inputs:
+    """A HyPar input deck read by the library's C reader (gb_inputs_read)."""
+
+    def __init__(self, directory: str):
+        h = ctypes.c_void_p()
+        check(lib().gb_inputs_read(directory.encode(), ctypes.byref(h)))
+        self._h = h
+        c = lib().gb_inputs_config(h).contents
+        self.config = GbConfig()
+        ctypes.pointer(self.config)[0] = c
+        nd = c.ndims
+        dims = [c.dim[d] for d in range(nd)]
+        nx = sum(dims)
+        nxg = sum(d + 2 * c.ghosts for d in dims)
+        npts = int(np.prod(dims))
+        self.x = np.ctypeslib.as_array(lib().gb_inputs_x(h), shape=(nx,)).copy()
+        self.dxinv = np.ctypeslib.as_array(lib().gb_inputs_dxinv(h), shape=(nxg,)).copy()
+        self.u0 = np.ctypeslib.as_array(lib().gb_inputs_u0(h), shape=(npts * c.nvars,)).copy()
+        lib().gb_inputs_free(h)
+        self._h = None
+
+
+def rk_table(name: str):
+    ns = ctypes.c_int()
+    A = (ctypes.c_double * 16)()
+    b = (ctypes.c_double * 4)()
+    c = (ctypes.c_double * 4)()
+    check(lib().gb_rk_table(name.encode(), ctypes.byref(ns), A, b, c))
+    return ns.value, list(A), list(b), list(c)
+
+
+class Solver:
+    def __init__(self, config: GbConfig, dxinv: np.ndarray, device: int = 0):
+        self.config = config
+        self.dxinv = np.ascontiguousarray(dxinv, dtype=np.float64)
+        h = ctypes.c_void_p()
+        check(lib().gb_solver_create(ctypes.byref(config), self.dxinv.ctypes.data_as(_lib.DP), device,
+                                     ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_dir(cls, directory: str, device: int = 0) -> "Solver":
+        inp = Inputs(directory)
+        s = cls(inp.config, inp.dxinv, device)
+        s.inputs = inp
+        s.set_state(inp.u0)
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gb_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    @property
+    def ndims(self) -> int:
+        return self.config.ndims
+
+    @property
+    def nvars(self) -> int:
+        return self.config.nvars
+
+    @property
+    def dims(self):
+        return [self.config.dim[d] for d in range(self.config.ndims)]
+
+    @property
+    def ghosts(self) -> int:
+        return self.config.ghosts
+
+    @property
+    def npts_wg(self) -> int:
+        return int(np.prod([d + 2 * self.ghosts for d in self.dims]))
+
+    @property
+    def npts(self) -> int:
+        return int(np.prod(self.dims))
+
+    # ---- fused fast path ----
+    def set_state(self, u, ghosted: bool = False):
+        layout = _lib.LAYOUT_GHOSTED if ghosted else _lib.LAYOUT_INTERIOR
+        if hasattr(u, "is_cuda") and u.is_cuda:
+            import torch
+            torch.cuda.synchronize()
+            check(lib().gb_solver_set_state(self._h, _ptr(u), layout, _lib.MEM_DEVICE))
+        else:
+            arr = np.ascontiguousarray(u, dtype=np.float64)
+            check(lib().gb_solver_set_state(self._h, arr.ctypes.data, layout, _lib.MEM_HOST))
+            self.sync()
+
+    def get_state(self, ghosted: bool = False) -> np.ndarray:
+        n = (self.npts_wg if ghosted else self.npts) * self.nvars
+        out = np.empty(n, dtype=np.float64)
+        check(lib().gb_solver_get_state(self._h, out.ctypes.data,
+                                        _lib.LAYOUT_GHOSTED if ghosted else _lib.LAYOUT_INTERIOR, _lib.MEM_HOST))
+        return out
+
+    def step(self, nsteps: int = 1):
+        check(lib().gb_solver_step(self._h, int(nsteps)))
+
+    def sync(self):
+        check(lib().gb_solver_sync(self._h))
+
+    def set_stream(self, stream_handle: Optional[int]):
+        check(lib().gb_solver_set_stream(self._h, stream_handle))
+
+    def set_launch(self, dim: int, seg: int = 0, block: int = 0):
+        check(lib().gb_solver_set_launch(self._h, dim, seg, block))
+
+    @property
+    def time(self) -> float:
+        return lib().gb_solver_time(self._h)
+
+    def state_ptr(self) -> int:
+        return lib().gb_solver_state(self._h)
+
+    def check_finite(self) -> bool:
+        f = ctypes.c_int()
+        check(lib().gb_solver_check_finite(self._h, ctypes.byref(f)))
+        return bool(f.value)
+
+    # ---- HyPar function-pointer surface (device tensors) ----
+    def _dev(self):
+        import torch
+        torch.cuda.synchronize()
+
+    def hyperbolic(self, hyp, u, t: float = 0.0):
+        self._dev()
+        F = _lib.fn_address("gb_FFunction")
+        U = _lib.fn_address("gb_Upwind")
+        check(lib().gb_HyperbolicFunction(_ptr(hyp), _ptr(u), self._h, None, t, 1, F, U))
+        self.sync()
+
+    def parabolic(self, par, u, t: float = 0.0):
+        self._dev()
+        check(lib().gb_ParabolicFunction(_ptr(par), _ptr(u), self._h, None, t))
+        self.sync()
+
+    def source(self, src, u, t: float = 0.0):
+        self._dev()
+        check(lib().gb_SourceFunction(_ptr(src), _ptr(u), self._h, None, t))
+        self.sync()
+
+    def flux(self, f, u, dim: int, t: float = 0.0):
+        self._dev()
+        check(lib().gb_FFunction(_ptr(f), _ptr(u), dim, self._h, t))
+        self.sync()
+
+    def gflux(self, f, u, dim: int, t: float = 0.0):
+        self._dev()
+        check(lib().gb_GFunction(_ptr(f), _ptr(u), dim, self._h, t))
+        self.sync()
+
+    def ufunc(self, uC, u, dim: int = 0, t: float = 0.0):
+        self._dev()
+        check(lib().gb_UFunction(_ptr(uC), _ptr(u), dim, self._h, None, t))
+        self.sync()
+
+    def upwind(self, fI, fL, fR, uL, uR, u, dim: int, t: float = 0.0):
+        self._dev()
+        check(lib().gb_Upwind(_ptr(fI), _ptr(fL), _ptr(fR), _ptr(uL), _ptr(uR), _ptr(u), dim, self._h, t))
+        self.sync()
+
+    def apply_bc(self, u, t: float = 0.0):
+        self._dev()
+        check(lib().gb_ApplyBoundaryConditions(self._h, None, _ptr(u), None, t))
+        self.sync()
+
+    def rhs(self, out, u, t: float = 0.0):
+        self._dev()
+        check(lib().gb_RHSFunctionExplicit(_ptr(out), _ptr(u), self._h, None, t))
+        self.sync()
+
+    def time_rk(self):
+        check(lib().gb_TimeRK(self._h))
+
+
+def run_case(directory: str, device: int = 0, verbose: bool = False) -> None:
+    """gb_run_case: the HyPar driver for one deck directory (writes op*.bin)."""
+    check(lib().gb_run_case(directory.encode(), device, 1 if verbose else 0))
+
+
+def read_op(path: str):
+    from .cases import read_op_bin
+    return read_op_bin(path)

@@ -1,0 +1,169 @@
+/*
+ * gbhypar.h -- C ABI of libgbhypar, a GB300 (sm_103a) implementation of
+ * HyPar's explicit finite-difference right-hand side (WENO5 + Roe/LLF/RF
+ * upwinding + flux difference, NavierStokes3D viscous term) and explicit
+ * Runge-Kutta step, for the Euler1D, Euler2D and NavierStokes3D models.
+ *
+ * Two layers:
+ *
+ *  1. HyPar's solver / physics-model function-pointer surface, with the
+ *     reference's exact signatures (include/hypar.h:211-359 of HyPar).  Each
+ *     gb_* function can be assigned to the matching HyPar pointer; `void *s`
+ *     is a gb_solver handle instead of HyPar's solver struct and `void *m`
+ *     (the MPI object) is ignored.  Array arguments are DEVICE pointers in
+ *     HyPar's layout: ghost points on every side, dimension 0 fastest, the
+ *     nvars components of a point contiguous (include/arrayfunctions.h:40-47).
+ *
+ *  2. A fused fast path: the solver keeps the solution resident on the GPU
+ *     and gb_solver_step() advances whole Runge-Kutta steps, one fused kernel
+ *     per direction per stage (the stage update folded into the last one).
+ *
+ * Every function returns GB_OK (0) or a GB_ERR_* code; gb_last_error() gives
+ * the message.  Nothing aborts the process.
+ */
+#ifndef GBHYPAR_H
+#define GBHYPAR_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_OK 0
+#define GB_ERR_ARG 1          /* invalid argument or configuration */
+#define GB_ERR_CUDA 2         /* a CUDA call failed */
+#define GB_ERR_INPUT 3        /* an input file is missing or malformed */
+#define GB_ERR_UNSUPPORTED 4  /* valid HyPar option outside this library's path */
+#define GB_ERR_NOMEM 5        /* device or host allocation failed */
+#define GB_ERR_NONFINITE 6    /* the solution contains NaN or Inf */
+
+enum { GB_MODEL_EULER1D = 1, GB_MODEL_EULER2D = 2, GB_MODEL_NS3D = 3 };
+enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2 };
+enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
+enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2 };
+enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
+enum { GB_MEM_HOST = 0, GB_MEM_DEVICE = 1 };
+
+#define GB_MAX_ZONES 12
+
+/* Solver configuration: what HyPar reads from solver.inp, physics.inp,
+ * weno.inp and boundary.inp (after CalculateLocalExtent). */
+typedef struct gb_config {
+  int model;                /* GB_MODEL_* */
+  int ndims, nvars, ghosts; /* ghosts must be 3 (WENO5) */
+  int dim[3];               /* interior points per dimension */
+  int interp;               /* GB_INTERP_* (hyp_interp_type) */
+  int upwind;               /* GB_UPWIND_* (physics.inp "upwinding") */
+  double gamma;             /* physics.inp gamma */
+  double weno_eps;          /* weno.inp epsilon (Jiang-Shu weights) */
+  double Re, Pr, Minf;      /* NavierStokes3D physics.inp; Re <= 0: inviscid */
+  int nzones;               /* boundary zones */
+  int zones[GB_MAX_ZONES][9];  /* type, dim, face, is[3], ie[3] (index extents) */
+  int rk_nstages;           /* explicit Runge-Kutta Butcher table */
+  double rk_A[16], rk_b[4], rk_c[4];
+  double dt;                /* time step */
+  int n_iter;               /* number of steps (solver.inp n_iter) */
+  int file_op_iter;         /* output interval (solver.inp file_op_iter) */
+} gb_config;
+
+typedef struct gb_solver gb_solver;
+typedef struct gb_inputs gb_inputs;
+
+/* Message of the last failed call on this thread. */
+const char *gb_last_error(void);
+
+/* ---- input decks (the reference's readers: src/Simulation/ReadInputs.c,
+ *      InitializeBoundaries.c, WENOInitialize.c, <Model>Initialize.c,
+ *      src/IOFunctions/ReadArray.c, src/Simulation/InitialSolution.c) ---- */
+
+/* Read solver.inp, physics.inp, boundary.inp, weno.inp and initial.inp from
+ * `dir` (NULL: current directory). */
+int gb_inputs_read(const char *dir, gb_inputs **out);
+void gb_inputs_free(gb_inputs *in);
+const gb_config *gb_inputs_config(const gb_inputs *in);
+/* Interior grid coordinates, sum_d dim[d] values. */
+const double *gb_inputs_x(const gb_inputs *in);
+/* 2/(x[i+1]-x[i-1]) per point with ghosts, sum_d (dim[d]+2*ghosts) values. */
+const double *gb_inputs_dxinv(const gb_inputs *in);
+/* Initial solution, interior points, nvars per point, dimension 0 fastest. */
+const double *gb_inputs_u0(const gb_inputs *in);
+/* Runge-Kutta Butcher table of TimeExplicitRKInitialize for a solver.inp
+ * time_scheme_type ("1fe", "22", "33", "44", "ssprk3"). */
+int gb_rk_table(const char *type, int *nstages, double *A, double *b, double *c);
+
+/* ---- solver lifetime and the fused fast path ---- */
+
+/* Create a solver on CUDA device `device` (-1: current).  dxinv: host array
+ * of sum_d (dim[d]+2*ghosts) values. */
+int gb_solver_create(const gb_config *cfg, const double *dxinv, int device, gb_solver **out);
+void gb_solver_destroy(gb_solver *s);
+const gb_config *gb_solver_config(const gb_solver *s);
+/* Use a caller-owned cudaStream_t (NULL: the solver's own stream). */
+int gb_solver_set_stream(gb_solver *s, void *stream);
+/* Wait for all work queued by the solver. */
+int gb_solver_sync(gb_solver *s);
+/* Copy a solution in or out (layout GB_LAYOUT_*, memory GB_MEM_*). */
+int gb_solver_set_state(gb_solver *s, const double *u, int layout, int mem);
+int gb_solver_get_state(gb_solver *s, double *u, int layout, int mem);
+/* Device pointer of the resident ghosted solution (valid until the next step). */
+double *gb_solver_state(gb_solver *s);
+/* Advance nsteps Runge-Kutta steps of size cfg->dt on the resident solution. */
+int gb_solver_step(gb_solver *s, int nsteps);
+/* Simulation time of the resident solution. */
+double gb_solver_time(const gb_solver *s);
+/* Launch shape of the fused kernels: interfaces walked per thread (seg) and
+ * threads per block, per direction (values <= 0 keep the current ones). */
+int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
+/* 1 if every value of the resident interior solution is finite, else 0. */
+int gb_solver_check_finite(gb_solver *s, int *finite);
+
+/* Read the deck in `dir`, run n_iter steps on the GPU and write op.bin (and
+ * op_NNNNN.bin every file_op_iter steps when op_overwrite is "no") in HyPar's
+ * binary format (src/IOFunctions/WriteBinary.c).  The drop-in for HyPar's
+ * main() on this path. */
+int gb_run_case(const char *dir, int device, int verbose);
+/* Write a HyPar binary solution file from an interior solution. */
+int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
+
+/* Measure the device's FP64 fused-multiply-add throughput (TFLOP/s, an FMA
+ * counted as two operations) with a register-resident DFMA loop: the
+ * denominator of the FP64-pipe roofline of the fused kernels. */
+int gb_probe_fp64_peak(double *tflops);
+
+/* ---- HyPar's function-pointer surface (device arrays, HyPar layout) ---- */
+
+/* HyperbolicFunction (include/hypar.h:250-253, src/HyParFunctions/HyperbolicFunction.c:31).
+ * FluxFunction / UpwindFunction must be gb_FFunction / gb_Upwind (or NULL for
+ * the solver's configured ones): the pair selects the fused kernels. */
+int gb_HyperbolicFunction(double *hyp, double *u, void *s, void *m, double t, int LimFlag,
+                          int (*FluxFunction)(double *, double *, int, void *, double),
+                          int (*UpwindFunction)(double *, double *, double *, double *, double *, double *,
+                                                int, void *, double));
+/* ParabolicFunction (include/hypar.h:256; NavierStokes3DParabolicFunction.c:50).
+ * Zero for the Euler models. */
+int gb_ParabolicFunction(double *par, double *u, void *s, void *m, double t);
+/* SourceFunction (include/hypar.h:259): zero (no gravity on this path). */
+int gb_SourceFunction(double *source, double *u, void *s, void *m, double t);
+/* FFunction (include/hypar.h:276): cell flux along dir at every point. */
+int gb_FFunction(double *f, double *u, int dir, void *s, double t);
+/* GFunction (include/hypar.h:310): these models define none; writes zeros. */
+int gb_GFunction(double *f, double *u, int dir, void *s, double t);
+/* UFunction (include/hypar.h:321): modified solution uC at every point. */
+int gb_UFunction(double *uC, double *u, int dir, void *s, void *m, double t);
+/* Upwind (include/hypar.h:295): interface flux from reconstructed values;
+ * fI, fL, fR, uL, uR are interface arrays (no ghosts, dim[dir]+1 along dir). */
+int gb_Upwind(double *fI, double *fL, double *fR, double *uL, double *uR, double *u, int dir, void *s,
+              double t);
+/* ApplyBoundaryConditions (include/hypar.h:214): fills ghost points of u in place. */
+int gb_ApplyBoundaryConditions(void *s, void *m, double *u, double *uref, double t);
+/* TimeIntegration.RHSFunction = TimeRHSFunctionExplicit
+ * (include/timeintegration_struct.h:98, src/TimeIntegration/TimeRHSFunctionExplicit.c:30):
+ * applies the boundary conditions to u in place, rhs = -hyp + par + source. */
+int gb_RHSFunctionExplicit(double *rhs, double *u, void *s, void *m, double t);
+/* TimeRK (src/TimeIntegration/TimeRK.c:35) for `ts` = a gb_solver: one
+ * Runge-Kutta step of the resident solution. */
+int gb_TimeRK(void *ts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

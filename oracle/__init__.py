@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import platform
 import subprocess
 from typing import List, Optional, Sequence
 
@@ -23,6 +24,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+# The same restatement compiled with fused multiply-add contraction: it differs
+# from the reference only by rounding, so its distance from liboracle.so
+# measures how strongly a state amplifies rounding differences.
+FMA_LIB_PATH = os.path.join(HERE, "liboracle_fma.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 MODELS = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
@@ -34,36 +39,54 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile liboracle.so (gcc, OpenMP, no FMA contraction)."""
+    """Compile liboracle.so (gcc, OpenMP, no FMA contraction) and liboracle_fma.so."""
     src = os.path.join(HERE, "gbh_oracle.c")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    if (not force and all(os.path.exists(p) and os.path.getmtime(p) >= os.path.getmtime(src)
+                          for p in (LIB_PATH, FMA_LIB_PATH))):
         return LIB_PATH
     cmd = ["gcc", "-O3", "-std=c99", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
            "-o", LIB_PATH, src, "-lm"]
     subprocess.check_call(cmd)
+    fma = ["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []
+    subprocess.check_call(["gcc", "-O3", "-std=gnu99", "-ffp-contract=fast"] + fma +
+                          ["-fopenmp", "-fPIC", "-shared", "-o", FMA_LIB_PATH, src, "-lm"])
     return LIB_PATH
+
+
+def _bind(path):
+    L = ctypes.CDLL(path)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.orc_problem_create.restype = ctypes.c_void_p
+    L.orc_problem_create.argtypes = [ctypes.c_int, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_int, ip, dp]
+    L.orc_problem_destroy.argtypes = [ctypes.c_void_p]
+    L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
+    for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs"):
+        getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
+    L.orc_rk.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int]
+    L.orc_set_threads.argtypes = [ctypes.c_int]
+    L.orc_get_threads.restype = ctypes.c_int
+    return L
+
+
+_fma_lib = None
+
+
+def fma_lib():
+    global _fma_lib
+    if _fma_lib is None:
+        build()
+        _fma_lib = _bind(FMA_LIB_PATH)
+    return _fma_lib
 
 
 def lib():
     global _lib
     if _lib is None:
         build()
-        L = ctypes.CDLL(LIB_PATH)
-        dp = ctypes.POINTER(ctypes.c_double)
-        ip = ctypes.POINTER(ctypes.c_int)
-        L.orc_problem_create.restype = ctypes.c_void_p
-        L.orc_problem_create.argtypes = [ctypes.c_int, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int,
-                                         ctypes.c_int, ctypes.c_double, ctypes.c_double,
-                                         ctypes.c_double, ctypes.c_double, ctypes.c_int, ip, dp]
-        L.orc_problem_destroy.argtypes = [ctypes.c_void_p]
-        for name in ("orc_apply_bc",):
-            getattr(L, name).argtypes = [ctypes.c_void_p, dp]
-        for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs"):
-            getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
-        L.orc_rk.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int]
-        L.orc_set_threads.argtypes = [ctypes.c_int]
-        L.orc_get_threads.restype = ctypes.c_int
-        _lib = L
+        _lib = _bind(LIB_PATH)
     return _lib
 
 
@@ -183,7 +206,7 @@ RK_TABLES = {
 class Problem:
     """One oracle problem built from a case deck (hypar_gb300.cases.Case)."""
 
-    def __init__(self, case, ghosts: int = 3, boundary_rows=None):
+    def __init__(self, case, ghosts: int = 3, boundary_rows=None, fma: bool = False):
         self.case = case
         self.g = ghosts
         self.size = list(case.size)
@@ -197,7 +220,8 @@ class Problem:
         if case.model == "navierstokes3d" and case.Re is not None:
             Re = case.Re / case.Minf
         dims = np.asarray(self.size, np.int32)
-        L = lib()
+        L = fma_lib() if fma else lib()
+        self._L = L
         self.h = L.orc_problem_create(MODELS[case.model], len(self.size), _ip(dims), ghosts,
                                       UPWIND[case.upwinding], INTERP[case.interp], case.gamma,
                                       case.eps, Re, case.Pr, len(self.zones),
@@ -208,7 +232,7 @@ class Problem:
     def __del__(self):
         try:
             if getattr(self, "h", None):
-                lib().orc_problem_destroy(self.h)
+                self._L.orc_problem_destroy(self.h)
         except Exception:
             pass
 
@@ -222,19 +246,19 @@ class Problem:
     def rhs(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
         out = np.zeros_like(u)
-        lib().orc_rhs(self.h, _dp(u), _dp(out))
+        self._L.orc_rhs(self.h, _dp(u), _dp(out))
         return out
 
     def hyperbolic(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
-        lib().orc_apply_bc(self.h, _dp(u))
+        self._L.orc_apply_bc(self.h, _dp(u))
         out = np.zeros_like(u)
-        lib().orc_hyperbolic(self.h, _dp(u), _dp(out))
+        self._L.orc_hyperbolic(self.h, _dp(u), _dp(out))
         return out
 
     def apply_bc(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
-        lib().orc_apply_bc(self.h, _dp(u))
+        self._L.orc_apply_bc(self.h, _dp(u))
         return u
 
     def rk(self, u_wg: np.ndarray, nsteps: int, dt: Optional[float] = None, scheme: Optional[str] = None):
@@ -243,7 +267,7 @@ class Problem:
         A = np.asarray(A, np.float64)
         b = np.asarray(b, np.float64)
         u = np.ascontiguousarray(u_wg, np.float64).copy()
-        lib().orc_rk(self.h, ns, _dp(A), _dp(b), _dp(u), float(self.case.dt if dt is None else dt), int(nsteps))
+        self._L.orc_rk(self.h, ns, _dp(A), _dp(b), _dp(u), float(self.case.dt if dt is None else dt), int(nsteps))
         return u
 
 

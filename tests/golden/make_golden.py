@@ -1,0 +1,65 @@
+"""Regenerate the golden fixtures in this directory from the REFERENCE HyPar.
+
+Runs the reference CPU build (oracle/_ref/HyPar and oracle/_ref/ref_rhs_harness,
+compiled from the reference sources by oracle/Makefile.ref) on small input
+decks written by hypar_gb300.cases, single-threaded (OMP_NUM_THREADS=1: the
+reference's OpenMP build races on shared scratch in
+WENOFifthOrderCalculateWeightsCharJS), and stores, per case, the initial
+interior solution, the reference right-hand side of that state (interior) and
+the reference solution after n_iter Runge-Kutta steps (op.bin).
+
+    make -f oracle/Makefile.ref REF=<hypar source tree> -j8
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from hypar_gb300 import cases as C  # noqa: E402
+import oracle as O  # noqa: E402
+
+CASES = {
+    "sod64_comp_roe": lambda: C.sod(64, n_iter=20, dt=1e-3),
+    "sod64_char_llf_ssprk3": lambda: C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                           upwinding="llf-char", scheme="ssprk3"),
+    "sod64_char_rf": lambda: C.sod(64, n_iter=20, dt=1e-3, interp="characteristic", upwinding="rf-char"),
+    "vortex24_char_roe_ssprk3": lambda: C.vortex(24, n_iter=5, dt=0.02),
+    "vortex24_comp_llf_rk4": lambda: C.vortex(24, n_iter=5, dt=0.02, interp="components",
+                                              upwinding="llf-char", scheme="44"),
+    "vortex24_char_rf_rk22": lambda: C.vortex(24, n_iter=5, dt=0.02, upwinding="rf-char", scheme="22"),
+    "tgv12_comp_roe_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02),
+    "tgv12_char_llf_rk33": lambda: C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
+                                         upwinding="llf-char", scheme="33"),
+}
+
+
+def main() -> None:
+    if not O.ref_available():
+        raise SystemExit("oracle/_ref is not built (make -f oracle/Makefile.ref)")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    for name, mk in CASES.items():
+        case = mk()
+        with tempfile.TemporaryDirectory() as d:
+            case.write(d)
+            subprocess.check_call([os.path.join(O.REF_DIR, "ref_rhs_harness"), "dump.bin"], cwd=d,
+                                  stdout=subprocess.DEVNULL, env=env)
+            dump = O.read_harness_dump(os.path.join(d, "dump.bin"))
+            subprocess.check_call([os.path.join(O.REF_DIR, "HyPar")], cwd=d, stdout=subprocess.DEVNULL, env=env)
+            op = C.read_op_bin(os.path.join(d, "op.bin"))
+        rhs = O.interior(dump["rhs"], case.size, case.nvars, 3)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), u0=case.u, rhs=rhs, uN=op["u"],
+                            n_iter=case.n_iter, dt=case.dt)
+        print(name, rhs.shape, op["u"].shape)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,121 @@
+"""CPU-side checks of the C ABI: every declared symbol is exported, the input
+reader reproduces the reference's set-up, and bad decks fail cleanly."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+from hypar_gb300 import _lib, cases as C
+from hypar_gb300.solver import Inputs, rk_table
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "gbhypar.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gb_[A-Za-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    names = declared_functions()
+    assert len(names) >= 30
+    L = ctypes.CDLL(built_lib)
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(_lib.EXPORTS) == names
+
+
+@pytest.mark.parametrize("mk", [
+    lambda: C.sod(50, n_iter=3),
+    lambda: C.vortex(20, n_iter=2, dt=0.01, interp="components", upwinding="llf-char"),
+    lambda: C.tgv(10, n_iter=1, upwinding="rf-char", interp="characteristic", scheme="33"),
+])
+def test_reader_matches_reference_setup(built_lib, oracle_lib, tmp_path, mk):
+    case = mk()
+    case.write(str(tmp_path))
+    inp = Inputs(str(tmp_path))
+    c = inp.config
+    P = O.Problem(case)
+    assert np.array_equal(inp.dxinv, P.dxinv)
+    zones = np.array([list(c.zones[z]) for z in range(c.nzones)], dtype=np.int32)
+    assert np.array_equal(zones, P.zones)
+    assert np.array_equal(inp.u0, case.u.reshape(-1))
+    assert np.array_equal(inp.x, np.concatenate(case.x))
+    assert c.model == _lib.MODEL[case.model]
+    assert c.interp == _lib.INTERP[case.interp] and c.upwind == _lib.UPWIND[case.upwinding]
+    assert c.dt == case.dt and c.n_iter == case.n_iter
+    ns, A, b, cc = rk_table(case.time_scheme_type)
+    ons, oA, ob = O.RK_TABLES[case.time_scheme_type]
+    assert ns == ons and c.rk_nstages == ns
+    for i in range(ns):
+        assert b[i] == ob[i]
+        for j in range(ns):
+            assert A[4 * i + j] == oA[ns * i + j] == c.rk_A[4 * i + j]
+    if case.model == "navierstokes3d":
+        assert c.Re == case.Re and c.Minf == case.Minf and c.Pr == case.Pr
+
+
+def test_ascii_initial_file(built_lib, tmp_path):
+    case = C.sod(16, n_iter=1)
+    case.write(str(tmp_path))
+    txt = open(tmp_path / "solver.inp").read().replace("ip_file_type      binary", "ip_file_type      ascii")
+    open(tmp_path / "solver.inp", "w").write(txt)
+    with open(tmp_path / "initial.inp", "w") as f:
+        f.write(" ".join(repr(float(v)) for v in case.x[0]) + "\n")
+        for v in range(3):
+            f.write(" ".join(repr(float(a)) for a in case.u[:, v]) + "\n")
+    inp = Inputs(str(tmp_path))
+    assert np.array_equal(inp.u0, case.u.reshape(-1))
+
+
+def _expect(code, directory):
+    with pytest.raises(_lib.GbError) as e:
+        Inputs(directory)
+    assert e.value.code == code, str(e.value)
+
+
+def test_reader_errors(built_lib, tmp_path):
+    _expect(3, str(tmp_path / "nowhere"))
+    case = C.vortex(12, n_iter=1, dt=0.01)
+    d = tmp_path / "a"
+    case.write(str(d))
+    open(d / "weno.inp", "w").write("begin\n mapped 1\nend\n")
+    _expect(4, str(d))
+    d = tmp_path / "b"
+    case.write(str(d))
+    t = open(d / "boundary.inp").read().replace("periodic", "slip-wall", 1)
+    open(d / "boundary.inp", "w").write(t)
+    _expect(4, str(d))
+    d = tmp_path / "c"
+    case.write(str(d))
+    t = open(d / "solver.inp").read().replace("euler2d", "shallowwater2d")
+    open(d / "solver.inp", "w").write(t)
+    _expect(4, str(d))
+    d = tmp_path / "e"
+    case.write(str(d))
+    t = open(d / "solver.inp").read().replace("weno5", "crweno5")
+    open(d / "solver.inp", "w").write(t)
+    _expect(4, str(d))
+    d = tmp_path / "f"
+    case.write(str(d))
+    with open(d / "initial.inp", "r+b") as f:
+        f.truncate(100)
+    _expect(3, str(d))
+    d = tmp_path / "g"
+    case.write(str(d))
+    open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding steger-warming\nend\n")
+    _expect(4, str(d))
+
+
+def test_solver_create_rejects_bad_config(built_lib):
+    cfg = _lib.GbConfig()
+    cfg.model = 9
+    dx = np.zeros(10)
+    h = ctypes.c_void_p()
+    rc = _lib.lib().gb_solver_create(ctypes.byref(cfg), dx.ctypes.data_as(_lib.DP), -1, ctypes.byref(h))
+    assert rc == 1 and not h.value
+    assert b"unknown model" in _lib.lib().gb_last_error()
