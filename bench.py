@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of HyPar's explicit WENO5 RHS + Runge-Kutta step on GB300.
+
+Default workload (the configuration the headline metric is quoted on): 2-D
+Euler isentropic vortex, 1024 x 1024 periodic grid on [0,10)^2, b = 5,
+characteristic WENO5 (Jiang-Shu) + Roe, SSPRK3, dt at CFL 0.5, FP64.  A
+"step" is one SSPRK3 step of that grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload vortex|tgv|sod]
+
+--impl ours       the fused CUDA path through libgbhypar's C ABI (value: device
+                  time of the resident solution; e2e: host buffers copied in and
+                  out every step through gb_solver_set_state/step/get_state).
+--impl reference  the reference algorithm on the host cores (the CPU oracle,
+                  a restatement of the reference's C; the reference's own build
+                  needs its source tree, which only the build container has).
+N > 1 runs N independent replicas (one per GPU, weak scaling); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 cell-updates/s & HBM%; ensemble vs serial speedup; adjoint/forward cost"
+UNIT = "cell-component updates/s"
+
+# Interfaces walked per thread, per direction, chosen by sweeps on GB300.
+TUNED_SEG = {"vortex": [32, 32], "tgv": [32, 32, 32], "sod": [4]}
+
+# FP64 floating-point operations per cell per Runge-Kutta step of the fused
+# kernels (FMA = 2), from ncu instruction counts
+# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum; see profiles/).
+FP64_FLOPS_PER_CELL_STEP = {"vortex": None, "tgv": None, "sod": None}
+
+
+def workload(name: str, size: int = 0):
+    from hypar_gb300 import cases as C
+    if name == "vortex":
+        n = size or 1024
+        case = C.vortex(n, n_iter=200)
+        desc = (f"Euler2D isentropic vortex {n}x{n} periodic [0,10)^2, b=5, char-WENO5(JS)+Roe, "
+                "SSPRK3, CFL 0.5")
+    elif name == "tgv":
+        n = size or 256
+        case = C.tgv(n, n_iter=100)
+        desc = (f"NavierStokes3D Taylor-Green vortex {n}^3 periodic [0,2pi)^3, Mach 0.1, Re 1600, Pr 0.72, "
+                "comp-WENO5(JS)+Roe + 4th-order viscous, RK4, dt 2e-3")
+    elif name == "sod":
+        n = size or 1024
+        case = C.sod(n, n_iter=1000)
+        desc = f"Euler1D Sod shock tube {n} cells, comp-WENO5(JS)+Roe, RK4, dt 1e-4, extrapolate BCs"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return case, desc
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def stage_bytes(cfg, s) -> float:
+    """Algorithmic HBM bytes per cell of the last-direction kernel of stage s
+    (stencil input, accumulated hyperbolic term, viscous term, RK arrays)."""
+    nv, ns = cfg.nvars, cfg.rk_nstages
+    reads = 1 + (1 if cfg.ndims > 1 else 0)
+    writes = 1
+    need_u = s == 0
+    for t in range(s + 1, ns):
+        a = cfg.rk_A[4 * t + s]
+        if a != 0.0:
+            writes += 1
+            touched = any(cfg.rk_A[4 * t + i] != 0.0 for i in range(s))
+            reads += 1 if touched else 0
+            need_u = need_u or not touched
+    if s > 0:
+        reads += 1 + (1 if need_u else 0)
+    return 8.0 * nv * (reads + writes)
+
+
+def run_ours(args, case, desc, ws, rank, local):
+    import ctypes
+    import numpy as np
+    import torch
+    from hypar_gb300 import _lib
+    from hypar_gb300.solver import Solver
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    tmp = tempfile.mkdtemp(prefix="gbh_bench_")
+    case.write(tmp)
+    s = Solver.from_dir(tmp, device=local)
+    stream = torch.cuda.Stream()  # a real stream: handle 0 would mean "the solver's own"
+    torch.cuda.set_stream(stream)
+    s.set_stream(stream.cuda_stream)
+    for d, seg in enumerate(TUNED_SEG.get(args.workload, [32] * case.ndims)[:case.ndims]):
+        s.set_launch(d, seg, 128)
+    cells = int(np.prod(case.size))
+    nv = case.nvars
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    for _ in range(args.warmup):
+        s.step(1)
+    torch.cuda.synchronize()
+    s.profile(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            ev[k][0].record(stream)
+            s.step(1)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = sum(step_ms) / 1e3
+    prof = s.profile_read()
+    s.profile(False)
+    if dist:
+        tt = torch.tensor([t_dev], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    finite = s.check_finite()
+
+    # e2e: the user call with host buffers, copies in and out every step
+    host = torch.from_numpy(s.get_state()).pin_memory()
+    hp = host.data_ptr()
+    L = _lib.lib()
+    torch.cuda.synchronize()
+    n_e2e = max(1, min(args.steps, 10))
+    te = time.perf_counter()
+    for _ in range(n_e2e):
+        _lib.check(L.gb_solver_set_state(s._h, hp, _lib.LAYOUT_INTERIOR, _lib.MEM_HOST))
+        _lib.check(L.gb_solver_step(s._h, 1))
+        _lib.check(L.gb_solver_get_state(s._h, hp, _lib.LAYOUT_INTERIOR, _lib.MEM_HOST))
+    t_e2e = (time.perf_counter() - te) / n_e2e
+    if dist:
+        tt = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return None
+
+    pk = ctypes.c_double()
+    _lib.check(L.gb_probe_fp64_peak(ctypes.byref(pk)))
+    fp64_peak = pk.value
+
+    value = ws * cells * nv * args.steps / t_dev
+    e2e_value = ws * cells * nv / t_e2e
+    # dominant kernel: largest accumulated time among the launch classes
+    cls, (ms_tot, nl) = max(prof.items(), key=lambda kv: kv[1][0])
+    avg_launch_s = ms_tot / 1e3 / max(nl, 1)
+    cfg = s.config
+    hbm_peak, hbm_src = measured_peaks()
+    last_dir = f"hyp_{'xyz'[cfg.ndims - 1]}"
+    if cls == last_dir:
+        bytes_per_launch = cells * sum(stage_bytes(cfg, st) for st in range(cfg.rk_nstages)) / cfg.rk_nstages
+    else:
+        bytes_per_launch = cells * 8.0 * nv * 2  # read U, write the partial hyperbolic term
+    achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": None, "kernel": cls,
+                "avg_launch_ms": avg_launch_s * 1e3, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": bytes_per_launch}
+    step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
+                             for st in range(cfg.rk_nstages))
+    fl = FP64_FLOPS_PER_CELL_STEP.get(args.workload)
+    roofline_fp64 = {"bound": "fp64", "peak": fp64_peak, "unit": "TFLOP/s",
+                     "peak_source": "measured DFMA loop (gb_probe_fp64_peak) on this GPU"}
+    if fl:
+        ach = fl * cells * args.steps / t_dev / 1e12
+        roofline_fp64.update({"achieved": ach, "frac": ach / fp64_peak, "flops_per_cell_step": fl,
+                              "flops_source": "ncu FP64 instruction counts (profiles/)"})
+    launches_per_step = 0
+    for k, (ms_k, n_k) in prof.items():
+        per = 5 if k == "viscous" else 1
+        launches_per_step += per * n_k
+    gpu_launches = launches_per_step  # counted over the timed region
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "cells": cells, "nvars": nv, "dt": case.dt, "steps": args.steps,
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "256 MB buffer written between timed steps (L2 flush)"},
+        "hbm_pct_step": 100.0 * (step_bytes / (t_dev / args.steps)) / 1e9 / hbm_peak,
+        "roofline": roofline, "roofline_fp64": roofline_fp64,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": cells * nv * 8,
+                "d2h_bytes_per_step": cells * nv * 8,
+                "path": "gb_solver_set_state(host) + gb_solver_step(1) + gb_solver_get_state(host)"},
+        "gpu_launches": gpu_launches, "clocks": clocks, "wall_s": wall, "finite": finite,
+        "kernel_ms": {k: v[0] for k, v in prof.items() if v[1]},
+    }
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(case, budget_s=args.cpu_budget)
+    if dist:
+        dist.destroy_process_group()
+    return out
+
+
+def cpu_baseline(case, budget_s: float = 15.0, threads: int = 0):
+    """The oracle (the reference algorithm restated in C) on the host cores,
+    timed on whole steps of the same workload until budget_s has elapsed."""
+    import numpy as np
+    import oracle as O
+    O.build()
+    n = threads or os.cpu_count() or 1
+    O.set_threads(n)
+    P = O.Problem(case)
+    u = P.u0()
+    cells = int(np.prod(case.size))
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        u = P.rk(u, 1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s:
+            break
+    return {"value": cells * case.nvars * steps / el, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": f"{steps} full step(s) of the same workload in {el:.1f} s, {n} OpenMP threads",
+            "seconds_per_step": el / steps}
+
+
+def run_reference(args, case, desc, ws, rank):
+    if rank != 0:
+        return None
+    import numpy as np
+    import oracle as O
+    O.build()
+    n = os.cpu_count() or 1
+    O.set_threads(n)
+    P = O.Problem(case)
+    u = P.u0()
+    cells = int(np.prod(case.size))
+    sub = case
+    # keep the whole run within a few minutes: time one step first
+    t0 = time.perf_counter()
+    u = P.rk(u, 1)
+    t1 = time.perf_counter() - t0
+    total = t1 * (args.steps + args.warmup)
+    sample = "full grid"
+    if total > 180.0 and case.model == "euler2d":
+        from hypar_gb300 import cases as C
+        sub = C.vortex(512, n_iter=1, dt=case.dt, interp=case.interp, upwinding=case.upwinding,
+                       scheme=case.time_scheme_type)
+        P = O.Problem(sub)
+        u = P.u0()
+        cells = int(np.prod(sub.size))
+        sample = "512x512 sub-grid of the same vortex (same dt, scheme)"
+    for _ in range(max(args.warmup - 1, 0)):
+        u = P.rk(u, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        u = P.rk(u, 1)
+    el = time.perf_counter() - t0
+    value = cells * sub.nvars * args.steps / el
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "cells": cells, "nvars": sub.nvars, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
+                         "sample": f"{args.steps} timed steps ({sample}), {n} OpenMP threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--size", type=int, default=0, help="override the grid size (profiling of small cases)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_env()
+    case, desc = workload(args.workload, args.size)
+    if args.impl == "reference":
+        out = run_reference(args, case, desc, ws, rank)
+    else:
+        from hypar_gb300 import build as B
+        B.build()
+        out = run_ours(args, case, desc, ws, rank, local)
+    if out is not None and rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

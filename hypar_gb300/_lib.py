@@ -28,7 +28,7 @@ EXPORTS = [
     "gb_solver_step", "gb_solver_time", "gb_solver_set_launch", "gb_solver_check_finite", "gb_run_case",
     "gb_write_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
     "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
-    "gb_TimeRK", "gb_probe_fp64_peak",
+    "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
 ]
 
 
@@ -105,6 +105,8 @@ def lib():
     L.gb_ApplyBoundaryConditions.argtypes = [VP, VP, VP, VP, ctypes.c_double]
     L.gb_TimeRK.argtypes = [VP]
     L.gb_probe_fp64_peak.argtypes = [DP]
+    L.gb_solver_profile.argtypes = [VP, ctypes.c_int]
+    L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     _lib = L
     return L
 

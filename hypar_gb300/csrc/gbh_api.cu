@@ -77,7 +77,55 @@ struct gb_solver {
   double t = 0.0;
   long long dx_off[3] = {0, 0, 0};
   bool viscous = false;
+  // launch profiler: an event pair around every launch group, read on demand
+  bool prof = false;
+  struct Rec { int cls; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[GB_PROF_CLASSES] = {0};
+  long long prof_n[GB_PROF_CLASSES] = {0};
 };
+
+static cudaEvent_t ev_get(gb_solver* s) {
+  if (!s->pool.empty()) {
+    cudaEvent_t e = s->pool.back();
+    s->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+// Record the start of a launch group of class `cls` (returns the record index).
+static int prof_begin(gb_solver* s, int cls) {
+  if (!s->prof) return -1;
+  gb_solver::Rec r;
+  r.cls = cls;
+  r.a = ev_get(s);
+  r.b = ev_get(s);
+  cudaEventRecord(r.a, s->stream);
+  s->recs.push_back(r);
+  return (int)s->recs.size() - 1;
+}
+static void prof_end(gb_solver* s, int idx) {
+  if (idx < 0) return;
+  cudaEventRecord(s->recs[idx].b, s->stream);
+}
+static int prof_drain(gb_solver* s) {
+  for (auto& r : s->recs) {
+    cudaError_t e = cudaEventSynchronize(r.b);
+    if (e != cudaSuccess) { gbh_set_error("profiler: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    s->prof_ms[r.cls] += ms;
+    s->prof_n[r.cls] += 1;
+    s->pool.push_back(r.a);
+    s->pool.push_back(r.b);
+  }
+  s->recs.clear();
+  return GB_OK;
+}
 
 static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const StageEpi& ep) {
   const gb_config& c = s->cfg;
@@ -100,13 +148,18 @@ static cudaError_t launch_unfused(gb_solver* s, int kind, int dir, double* out, 
 }
 
 static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
+  int pr = -1;
   for (int z = 0; z < s->cfg.nzones; z++) {
     bool use = all;
     if (!use)
       for (int k : s->mem_zones)
         if (k == z) use = true;
-    if (use) CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->stream));
+    if (use) {
+      if (pr < 0) pr = prof_begin(s, GB_PROF_BC);
+      CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->stream));
+    }
   }
+  prof_end(s, pr);
   return GB_OK;
 }
 
@@ -117,7 +170,9 @@ static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
   if (rc) return rc;
   ep.par = nullptr;
   if (s->viscous) {
+    int pr = prof_begin(s, GB_PROF_VISC);
     CK(launch_visc(U, s->d_Q, s->d_Gr, s->d_par, s->d_dxinv, s->G, s->vp, s->visc_seg, s->stream));
+    prof_end(s, pr);
     ep.par = s->d_par;
   }
   int nd = s->cfg.ndims;
@@ -125,7 +180,9 @@ static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
     StageEpi e = ep;
     e.first = (d == 0);
     e.last = (d == nd - 1);
+    int pr = prof_begin(s, GB_PROF_HYP_X + d);
     CK(launch_hyp(s, d, U, e));
+    prof_end(s, pr);
   }
   return GB_OK;
 }
@@ -264,8 +321,31 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_Gr);
   cudaFree(s->d_dxinv);
   cudaFree(s->d_flag);
+  prof_drain(s);
+  for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
+}
+
+extern "C" int gb_solver_profile(gb_solver* s, int enable) {
+  if (!s) { gbh_set_error("null solver"); return GB_ERR_ARG; }
+  int rc = prof_drain(s);
+  for (int k = 0; k < GB_PROF_CLASSES; k++) {
+    s->prof_ms[k] = 0.0;
+    s->prof_n[k] = 0;
+  }
+  s->prof = enable != 0;
+  return rc;
+}
+
+extern "C" int gb_solver_profile_read(gb_solver* s, double* ms, long long* launches) {
+  if (!s || !ms || !launches) { gbh_set_error("null argument"); return GB_ERR_ARG; }
+  int rc = prof_drain(s);
+  for (int k = 0; k < GB_PROF_CLASSES; k++) {
+    ms[k] = s->prof_ms[k];
+    launches[k] = s->prof_n[k];
+  }
+  return rc;
 }
 
 extern "C" const gb_config* gb_solver_config(const gb_solver* s) { return s ? &s->cfg : nullptr; }

@@ -152,6 +152,18 @@ class Solver:
     def state_ptr(self) -> int:
         return lib().gb_solver_state(self._h)
 
+    PROF_CLASSES = ("hyp_x", "hyp_y", "hyp_z", "viscous", "bc")
+
+    def profile(self, enable: bool = True):
+        check(lib().gb_solver_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self):
+        """{class: (milliseconds, launches)} accumulated since profiling was enabled."""
+        ms = (ctypes.c_double * 5)()
+        n = (ctypes.c_longlong * 5)()
+        check(lib().gb_solver_profile_read(self._h, ms, n))
+        return {k: (ms[i], n[i]) for i, k in enumerate(self.PROF_CLASSES)}
+
     def check_finite(self) -> bool:
         f = ctypes.c_int()
         check(lib().gb_solver_check_finite(self._h, ctypes.byref(f)))

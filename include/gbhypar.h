@@ -116,6 +116,16 @@ int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
 /* 1 if every value of the resident interior solution is finite, else 0. */
 int gb_solver_check_finite(gb_solver *s, int *finite);
 
+/* Launch-group profiler (the counterpart of the reference's GPU_STAT timers):
+ * when enabled, a CUDA event pair on the solver's stream brackets every launch
+ * group; gb_solver_profile_read() waits for them and returns, per class, the
+ * accumulated milliseconds and the number of kernel launches.  Enabling or
+ * disabling resets the counters. */
+enum { GB_PROF_HYP_X = 0, GB_PROF_HYP_Y = 1, GB_PROF_HYP_Z = 2, GB_PROF_VISC = 3, GB_PROF_BC = 4,
+       GB_PROF_CLASSES = 5 };
+int gb_solver_profile(gb_solver *s, int enable);
+int gb_solver_profile_read(gb_solver *s, double *ms, long long *launches);
+
 /* Read the deck in `dir`, run n_iter steps on the GPU and write op.bin (and
  * op_NNNNN.bin every file_op_iter steps when op_overwrite is "no") in HyPar's
  * binary format (src/IOFunctions/WriteBinary.c).  The drop-in for HyPar's
