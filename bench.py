@@ -35,13 +35,13 @@ sys.path.insert(0, ROOT)
 METRIC = "FP64 cell-updates/s & HBM%; ensemble vs serial speedup; adjoint/forward cost"
 UNIT = "cell-component updates/s"
 
-# Interfaces walked per thread, per direction, chosen by sweeps on GB300.
-TUNED_SEG = {"vortex": [32, 32], "tgv": [32, 32, 32], "sod": [4]}
-
-# FP64 floating-point operations per cell per Runge-Kutta step of the fused
-# kernels (FMA = 2), from ncu instruction counts
-# (sm__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on.sum; see profiles/).
-FP64_FLOPS_PER_CELL_STEP = {"vortex": None, "tgv": None, "sod": None}
+# FP64 floating-point operations per interface per direction of the fused
+# kernels (FMA = 2), from ncu instruction counts of one launch
+# (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on x elapsed cycles,
+# profiles/hyp_dir_kernel_euler2d_char_roe_vortex2048_ncu_full.md); per cell per
+# step this is x (ndims * nstages).  FP64 instructions per interface in brackets.
+FP64_FLOPS_PER_INTERFACE = {"vortex": 1640.2}
+FP64_INSTR_PER_INTERFACE = {"vortex": 1024.3}
 
 
 def workload(name: str, size: int = 0):
@@ -175,8 +175,7 @@ def run_ours(args, case, desc, ws, rank, local):
     stream = torch.cuda.Stream()  # a real stream: handle 0 would mean "the solver's own"
     torch.cuda.set_stream(stream)
     s.set_stream(stream.cuda_stream)
-    for d, seg in enumerate(TUNED_SEG.get(args.workload, [32] * case.ndims)[:case.ndims]):
-        s.set_launch(d, seg, 128)
+    tuned = s.autotune(2)  # launch shape per direction (state restored), outside the timed region
     cells = int(np.prod(case.size))
     nv = case.nvars
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
@@ -255,12 +254,16 @@ def run_ours(args, case, desc, ws, rank, local):
                 "algorithmic_bytes_per_launch": bytes_per_launch}
     step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
                              for st in range(cfg.rk_nstages))
-    fl = FP64_FLOPS_PER_CELL_STEP.get(args.workload)
+    fl = FP64_FLOPS_PER_INTERFACE.get(args.workload)
     roofline_fp64 = {"bound": "fp64", "peak": fp64_peak, "unit": "TFLOP/s",
                      "peak_source": "measured DFMA loop (gb_probe_fp64_peak) on this GPU"}
     if fl:
-        ach = fl * cells * args.steps / t_dev / 1e12
-        roofline_fp64.update({"achieved": ach, "frac": ach / fp64_peak, "flops_per_cell_step": fl,
+        fl_step = fl * cfg.ndims * cfg.rk_nstages
+        ach = fl_step * cells * args.steps / t_dev / 1e12
+        ins = FP64_INSTR_PER_INTERFACE[args.workload] * cfg.ndims * cfg.rk_nstages * cells * args.steps
+        pipe = ins / t_dev / (fp64_peak * 1e12 / 2.0)  # the pipe issues one FP64 instruction per FMA slot
+        roofline_fp64.update({"achieved": ach, "frac": ach / fp64_peak, "flops_per_cell_step": fl_step,
+                              "fp64_pipe_busy_frac": pipe,
                               "flops_source": "ncu FP64 instruction counts (profiles/)"})
     launches_per_step = 0
     for k, (ms_k, n_k) in prof.items():
@@ -274,6 +277,7 @@ def run_ours(args, case, desc, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": desc, "cells": cells, "nvars": nv, "dt": case.dt, "steps": args.steps,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "launch_seg_block_per_dir": tuned,
                    "l2": "256 MB buffer written between timed steps (L2 flush)"},
         "hbm_pct_step": 100.0 * (step_bytes / (t_dev / args.steps)) / 1e9 / hbm_peak,
         "roofline": roofline, "roofline_fp64": roofline_fp64,

@@ -29,6 +29,7 @@ EXPORTS = [
     "gb_write_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
     "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
     "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
+    "gb_solver_get_launch", "gb_solver_autotune",
 ]
 
 
@@ -106,6 +107,8 @@ def lib():
     L.gb_TimeRK.argtypes = [VP]
     L.gb_probe_fp64_peak.argtypes = [DP]
     L.gb_solver_profile.argtypes = [VP, ctypes.c_int]
+    L.gb_solver_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.gb_solver_autotune.argtypes = [VP, ctypes.c_int]
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     _lib = L
     return L

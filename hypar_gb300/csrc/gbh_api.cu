@@ -492,6 +492,81 @@ extern "C" int gb_solver_step(gb_solver* s, int nsteps) {
   return GB_OK;
 }
 
+extern "C" int gb_solver_get_launch(gb_solver* s, int dir, int* seg, int* block) {
+  if (!s || dir < 0 || dir >= s->cfg.ndims || !seg || !block) { gbh_set_error("gb_solver_get_launch: bad argument"); return GB_ERR_ARG; }
+  *seg = s->hl[dir].seg;
+  *block = s->hl[dir].block;
+  return GB_OK;
+}
+
+// Launch-shape autotuner.  The fused kernels are bound by the FP64 pipe, which
+// a few warps per SM saturate, so the shape mostly decides how evenly the
+// walk segments spread over the SMs (a partial last wave idles SMs) against the
+// per-segment overhead (a six-cell window warm-up and one extra interface).
+// Candidates: segment lengths that give 1..4 full waves of 4 warps per SM, plus
+// fixed lengths; each is timed on `reps` steps of the resident solution, which
+// is restored afterwards.
+extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
+  if (!s) { gbh_set_error("null solver"); return GB_ERR_ARG; }
+  if (reps < 1) reps = 1;
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device));
+  size_t bytes = s->nvals * sizeof(double);
+  double* save = nullptr;
+  CK(cudaMallocAsync((void**)&save, bytes, s->stream));
+  CK(cudaMemcpyAsync(save, s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  double t0 = s->t;
+  bool prof_was = s->prof;
+  const gb_config& c = s->cfg;
+  int rc = GB_OK;
+  for (int d = 0; d < c.ndims && !rc; d++) {
+    int N = c.dim[d];
+    long long ntrans = 1;
+    for (int e = 0; e < c.ndims; e++)
+      if (e != d) ntrans *= c.dim[e];
+    std::vector<int> segs;
+    for (int w = 1; w <= 4; w++) {
+      double lanes = (double)w * sms * 4 * 32;
+      long long nseg = (long long)(lanes / (double)ntrans + 0.5);
+      if (nseg < 1) nseg = 1;
+      int sg = (int)((N + nseg - 1) / nseg);
+      segs.push_back(sg);
+    }
+    for (int sg : {8, 16, 24, 32, 48, 64}) segs.push_back(sg);
+    double best = 1e30;
+    HypLaunch bestL = s->hl[d];
+    for (int sg : segs) {
+      if (sg < 4 || sg > N) continue;
+      for (int blk : {128, 64}) {
+        s->hl[d].seg = sg;
+        s->hl[d].block = blk;
+        rc = rk_step(s);  // warm
+        if (!rc) rc = gb_solver_profile(s, 1);
+        for (int r = 0; r < reps && !rc; r++) rc = rk_step(s);
+        double ms[GB_PROF_CLASSES];
+        long long nl[GB_PROF_CLASSES];
+        if (!rc) rc = gb_solver_profile_read(s, ms, nl);
+        if (rc) break;
+        if (ms[GB_PROF_HYP_X + d] < best) {
+          best = ms[GB_PROF_HYP_X + d];
+          bestL = s->hl[d];
+        }
+      }
+      if (rc) break;
+    }
+    s->hl[d] = bestL;
+  }
+  gb_solver_profile(s, prof_was ? 1 : 0);
+  CK(cudaMemcpyAsync(s->d_u, save, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_acc, save, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  for (int k = 1; k < c.rk_nstages; k++)
+    CK(cudaMemcpyAsync(s->d_P[k], save, bytes, cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaFreeAsync(save, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->t = t0;
+  return rc;
+}
+
 extern "C" int gb_solver_check_finite(gb_solver* s, int* finite) {
   if (!s || !finite) { gbh_set_error("null argument"); return GB_ERR_ARG; }
   int h = 0;

@@ -155,7 +155,19 @@ __device__ __forceinline__ RoeSide roe_side(const Prim<M>& q) {
 // ---------------------------------------------------------------------------
 struct Eig {
   double vel[3], un, a, ek, H, hac, rs, inv_a2, rho;
+  double gh, gi, ah, aun;  // (gamma-1) hac, (gamma-1)/a^2, a hac, a u_n
 };
+
+// 1/sqrt(x) refined by two Newton steps y' = y + y (1 - x y^2)/2 from the
+// hardware estimate (same method and error bound as nr_rcp).
+__device__ __forceinline__ double nr_rsqrt(double x) {
+  double y = rsqrt_approx(x);
+  double e = fma(-x * y, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  e = fma(-x * y, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  return y;
+}
 
 template <int M, int DIR>
 __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const PhysParams& pp) {
@@ -173,19 +185,23 @@ __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const
   E.H = fma(L.t, L.H, R.t * R.H) * inv;
   E.ek = 0.5 * vsq;
   double a2 = pp.gm1 * (E.H - E.ek);
-  E.inv_a2 = nr_rcp(a2);
-  E.a = nr_sqrt(a2);
+  double ia = nr_rsqrt(a2);  // 1/a
+  E.a = a2 * ia;
+  E.inv_a2 = ia * ia;
   E.un = E.vel[DIR];
   E.rho = L.t * R.t;
   if (M == MODEL_EULER1D) {
     // hac = 1/(rho a), rs = rho/(2a) = 1/(2 a^2 hac)
-    double ia = E.a * E.inv_a2;  // 1/a
     E.hac = nr_rcp(E.rho) * ia;
     E.rs = 0.5 * E.rho * ia;
   } else {
     E.hac = 0.5 * E.inv_a2;
     E.rs = 1.0;
   }
+  E.gh = pp.gm1 * E.hac;
+  E.gi = pp.gm1 * E.inv_a2;
+  E.ah = E.a * E.hac;
+  E.aun = E.a * E.un;
   return E;
 }
 
@@ -194,14 +210,14 @@ __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const
 template <int M, int DIR>
 __device__ __forceinline__ void projL(const Eig& E, const PhysParams& pp, const double* q, double* w) {
   constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
-  double s = E.ek * q[0];
+  (void)pp;
+  double s = fma(E.ek, q[0], q[NV - 1]);  // s / (gamma-1)
 #pragma unroll
   for (int k = 0; k < ND; k++) s = fma(-E.vel[k], q[1 + k], s);
-  s = pp.gm1 * (s + q[NV - 1]);
-  double t = E.a * fma(E.un, q[0], -q[1 + DIR]);
-  w[0] = (s + t) * E.hac;
-  w[1] = (s - t) * E.hac;
-  w[2] = fma(-s, E.inv_a2, q[0]);
+  double th = E.ah * fma(E.un, q[0], -q[1 + DIR]);  // t hac
+  w[0] = fma(s, E.gh, th);
+  w[1] = fma(s, E.gh, -th);
+  w[2] = fma(-s, E.gi, q[0]);
   int j = 3;
 #pragma unroll
   for (int k = 0; k < ND; k++) {
@@ -213,11 +229,15 @@ __device__ __forceinline__ void projL(const Eig& E, const PhysParams& pp, const 
 template <int M, int DIR>
 __device__ __forceinline__ void projR(const Eig& E, const double* w, double* y) {
   constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
-  double Wm = E.rs * w[0], Wp = E.rs * w[1];
+  double Wm = w[0], Wp = w[1];
+  if (M == MODEL_EULER1D) {
+    Wm *= E.rs;
+    Wp *= E.rs;
+  }
   double sa = Wm + Wp;
   double da = Wp - Wm;
   double y0 = sa + w[2];
-  double yE = fma(E.H, sa, fma(E.a * E.un, da, E.ek * w[2]));
+  double yE = fma(E.H, sa, fma(E.aun, da, E.ek * w[2]));
   int j = 3;
 #pragma unroll
   for (int k = 0; k < ND; k++) {
@@ -244,60 +264,62 @@ __device__ __forceinline__ void eigvals(double un, double a, double* lam) {
 }
 
 // ---------------------------------------------------------------------------
-// WENO5, Jiang-Shu weights (_WENOWeights_v_JS_, include/interpolation.h:265-285,
+// WENO5 with Jiang-Shu weights (_WENOWeights_v_JS_, include/interpolation.h:265-285,
 // optimal weights 0.1/0.6/0.3 at :228-232) and the fifth-order interpolant
-// (Interp1PrimFifthOrderWENO.c:143-158), for a stencil (m3,m2,m1,p1,p2) biased
-// towards m1.  The normalisation uses one reciprocal:
-//   w_k = c_k/q_k / sum_j c_j/q_j = c_k prod_{j!=k} q_j / sum(...),  q = (beta+eps)^2.
+// (Interp1PrimFifthOrderWENO.c:143-158), evaluated for the left- AND the
+// right-biased reconstruction of one interface together.
+//
+// p[0..5] are the six cells j-2..j+3 of interface j+1/2; the left-biased
+// stencil (m3..p2) is p[0..4], the right-biased one p[5..1].  The two share
+// the second differences of the sub-stencils centred at p[2] and p[3] and two
+// of their candidate polynomials.  Per side, with beta_k the smoothness
+// indicators and q_k = (beta_k + eps)^2,
+//   w_k = c_k/q_k / sum_j c_j/q_j = c_k prod_{j!=k} q_j / sum_j c_j prod_{i!=j} q_i,
+// and because the weights are ratios, every beta_k + eps may be scaled by the
+// same factor: B_k = 4 (beta_k + eps) = (13/3) d_k^2 + g_k^2 + 4 eps.  The
+// candidates are kept unnormalised (f = (2 m3 - 7 m2 + 11 m1)/6, ...): the 1/6
+// and the optimal weights (0.1, 0.6, 0.3) = 0.1 (1, 6, 3) fold into the final
+// normalisation.  The weights come from `w`, the interpolated values from `v`
+// (they differ for the u-reconstruction, whose weights are computed from u
+// while the values are uC = UFunction(u), HyperbolicFunction.c:201-215).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double weno5(double m3, double m2, double m1, double p1, double p2,
-                                        double eps) {
-  const double k13 = 13.0 / 12.0, k14 = 0.25;
-  double d1 = fma(-2.0, m2, m3) + m1;
-  double g1 = fma(3.0, m1, fma(-4.0, m2, m3));
-  double d2 = fma(-2.0, m1, m2) + p1;
-  double g2 = m2 - p1;
-  double d3 = fma(-2.0, p1, m1) + p2;
-  double g3 = fma(3.0, m1, fma(-4.0, p1, p2));
-  double b1 = fma(k13 * d1, d1, k14 * g1 * g1) + eps;
-  double b2 = fma(k13 * d2, d2, k14 * g2 * g2) + eps;
-  double b3 = fma(k13 * d3, d3, k14 * g3 * g3) + eps;
-  double q1 = b1 * b1, q2 = b2 * b2, q3 = b3 * b3;
-  double a1 = 0.1 * (q2 * q3);
-  double a2 = 0.6 * (q1 * q3);
-  double a3 = 0.3 * (q1 * q2);
-  double r = nr_rcp(6.0 * (a1 + a2 + a3));
-  double f1 = fma(2.0, m3, fma(-7.0, m2, 11.0 * m1));
-  double f2 = fma(-1.0, m2, fma(5.0, m1, 2.0 * p1));
-  double f3 = fma(2.0, m1, fma(5.0, p1, -p2));
-  return fma(a1, f1, fma(a2, f2, a3 * f3)) * r;
-}
-
-// Same, with the weights taken from one stencil (ws*) and the interpolated
-// values from another (v*): the u-reconstruction weights come from u while the
-// values come from uC = UFunction(u) (HyperbolicFunction.c:201-215).
-__device__ __forceinline__ double weno5_split(double wm3, double wm2, double wm1, double wp1, double wp2,
-                                              double m3, double m2, double m1, double p1, double p2,
-                                              double eps) {
-  const double k13 = 13.0 / 12.0, k14 = 0.25;
-  double d1 = fma(-2.0, wm2, wm3) + wm1;
-  double g1 = fma(3.0, wm1, fma(-4.0, wm2, wm3));
-  double d2 = fma(-2.0, wm1, wm2) + wp1;
-  double g2 = wm2 - wp1;
-  double d3 = fma(-2.0, wp1, wm1) + wp2;
-  double g3 = fma(3.0, wm1, fma(-4.0, wp1, wp2));
-  double b1 = fma(k13 * d1, d1, k14 * g1 * g1) + eps;
-  double b2 = fma(k13 * d2, d2, k14 * g2 * g2) + eps;
-  double b3 = fma(k13 * d3, d3, k14 * g3 * g3) + eps;
-  double q1 = b1 * b1, q2 = b2 * b2, q3 = b3 * b3;
-  double a1 = 0.1 * (q2 * q3);
-  double a2 = 0.6 * (q1 * q3);
-  double a3 = 0.3 * (q1 * q2);
-  double r = nr_rcp(6.0 * (a1 + a2 + a3));
-  double f1 = fma(2.0, m3, fma(-7.0, m2, 11.0 * m1));
-  double f2 = fma(-1.0, m2, fma(5.0, m1, 2.0 * p1));
-  double f3 = fma(2.0, m1, fma(5.0, p1, -p2));
-  return fma(a1, f1, fma(a2, f2, a3 * f3)) * r;
+__device__ __forceinline__ void weno5_pair(const double* w, const double* v, double eps4, double& outL,
+                                           double& outR) {
+  const double k13 = 13.0 / 3.0;
+  // second differences, sub-stencils centred at p1..p4
+  double d1 = fma(-2.0, w[1], w[0]) + w[2];
+  double d2 = fma(-2.0, w[2], w[1]) + w[3];
+  double d3 = fma(-2.0, w[3], w[2]) + w[4];
+  double d4 = fma(-2.0, w[4], w[3]) + w[5];
+  double kd1 = k13 * d1, kd2 = k13 * d2, kd3 = k13 * d3, kd4 = k13 * d4;
+  // first-difference terms
+  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
+  double gL2 = w[1] - w[3];
+  double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
+  double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
+  double gR2 = w[4] - w[2];
+  double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
+  double BL1 = fma(kd1, d1, fma(gL1, gL1, eps4));
+  double BL2 = fma(kd2, d2, fma(gL2, gL2, eps4));
+  double BL3 = fma(kd3, d3, fma(gL3, gL3, eps4));
+  double BR1 = fma(kd4, d4, fma(gR1, gR1, eps4));
+  double BR2 = fma(kd3, d3, fma(gR2, gR2, eps4));
+  double BR3 = fma(kd2, d2, fma(gR3, gR3, eps4));
+  double qL1 = BL1 * BL1, qL2 = BL2 * BL2, qL3 = BL3 * BL3;
+  double qR1 = BR1 * BR1, qR2 = BR2 * BR2, qR3 = BR3 * BR3;
+  double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;  // x (1, 1/6, 1/3) of the weights
+  double aR1 = qR2 * qR3, aR2 = qR1 * qR3, aR3 = qR1 * qR2;
+  // candidates (times 6): two of them shared between the sides
+  double cL1 = fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
+  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3]));
+  double cA = fma(5.0, v[2], fma(2.0, v[3], -v[1]));  // left #2, right #3
+  double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4]));  // left #3, right #2
+  double nL = fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
+  double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
+  double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
+  double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
+  outL = nL * nr_rcp(DL);
+  outR = nR * nr_rcp(DR);
 }
 
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }

@@ -150,6 +150,85 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
   }
 }
 
+// Upwinding from characteristic reconstructions xfL, xfR, xuL, xuR in the
+// basis of the cell-centre Roe average Ecc (the characteristic-WENO basis).
+// When the upwind scheme uses the same eigen-system (Roe for Euler1D and
+// NavierStokes3D, which average the cell-centre states, NavierStokes3DUpwind.c:90,
+// Euler1DUpwind.c:74; LLF/RF for Euler1D, Euler1DUpwind.c:259) the projections
+// cancel (L R = I): fI = R ((xfL+xfR)/2 - |Lambda| (xuR-xuL)/2).  Otherwise the
+// conserved interface values are rebuilt (fL+fR in one projection) and the
+// conserved-variable upwinding applies.
+template <int M, int UPW, int DIR>
+__device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR, const double* xuL,
+                                            const double* xuR, const Eig& Ecc, const CellAux<M>& cl,
+                                            const CellAux<M>& cr, const PhysParams& pp, double* fI) {
+  constexpr int NV = ModelTraits<M>::NV;
+  constexpr bool SAME_BASIS = (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE);
+  if (SAME_BASIS) {
+    double lamC[NV], fc[NV];
+    eigvals<M>(Ecc.un, Ecc.a, lamC);
+    if (UPW == UPW_ROE) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        double d = fabs(lamC[k]);
+        if (M != MODEL_EULER1D) {
+          const double delta = 0.000001, delta2 = delta * delta;
+          d = (d < delta) ? (lamC[k] * lamC[k] + delta2) * (0.5 / delta) : d;
+        }
+        fc[k] = 0.5 * fma(-d, xuR[k] - xuL[k], xfL[k] + xfR[k]);
+      }
+    } else {
+      double lamL[NV], lamR[NV];
+      eigvals<M>(cl.rs.vel[DIR], cl.c, lamL);
+      eigvals<M>(cr.rs.vel[DIR], cr.c, lamR);
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        double al = fmax(fmax(fabs(lamL[k]), fabs(lamC[k])), fabs(lamR[k]));
+        double llf = 0.5 * fma(al, xuL[k] - xuR[k], xfL[k] + xfR[k]);
+        if (UPW == UPW_RF) {
+          if (lamL[k] > 0 && lamC[k] > 0 && lamR[k] > 0) llf = xfL[k];
+          else if (lamL[k] < 0 && lamC[k] < 0 && lamR[k] < 0) llf = xfR[k];
+        }
+        fc[k] = llf;
+      }
+    }
+    projR<M, DIR>(Ecc, fc, fI);
+    return;
+  }
+  double uL[NV], uR[NV];
+  projR<M, DIR>(Ecc, xuL, uL);
+  projR<M, DIR>(Ecc, xuR, uR);
+  if (UPW == UPW_ROE) {
+    // Euler2D: Roe average of the reconstructed states (Euler2DUpwind.c:39)
+    double xs[NV], fs[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) xs[k] = xfL[k] + xfR[k];
+    projR<M, DIR>(Ecc, xs, fs);
+    Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+    Eig Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
+    double ud[NV], w[NV], lam[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) ud[v] = 0.5 * (uR[v] - uL[v]);
+    projL<M, DIR>(Eu, pp, ud, w);
+    eigvals<M>(Eu.un, Eu.a, lam);
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+      double d = fabs(lam[k]);
+      const double delta = 0.000001, delta2 = delta * delta;
+      d = (d < delta) ? (lam[k] * lam[k] + delta2) * (0.5 / delta) : d;
+      w[k] *= d;
+    }
+    projR<M, DIR>(Eu, w, ud);
+#pragma unroll
+    for (int v = 0; v < NV; v++) fI[v] = fma(0.5, fs[v], -ud[v]);
+  } else {
+    double fL[NV], fR[NV];
+    projR<M, DIR>(Ecc, xfL, fL);
+    projR<M, DIR>(Ecc, xfR, fR);
+    upwind_iface<M, true, UPW, DIR>(fL, fR, uL, uR, Ecc, cl, cr, pp, fI);
+  }
+}
+
 template <int M, bool CHAR, int UPW, int DIR>
 __global__ void __launch_bounds__(128)
 hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
@@ -174,7 +253,7 @@ hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
   const int lo = G.bclo[DIR], hi = G.bchi[DIR];
   const int I0 = sg * seg;
   const int I1 = min(I0 + seg, N);
-  const double eps = pp.eps;
+  const double eps4 = 4.0 * pp.eps;
 
   double wu[6][NV], wf[6][NV], wuc[6];
   CellAux<M> ax[6];
@@ -217,22 +296,29 @@ hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
     Eig Ecc;
     if (CC) Ecc = roe_eig<M, DIR>(ax[2].rs, ax[3].rs, pp);
 
+    double fI[NV];
     if (!CHAR) {
       // Component-wise WENO5: weights of the u-reconstruction from u, values from uC.
+      double fL[NV], fR[NV], uL[NV], uR[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) {
-        fL[v] = weno5(wf[0][v], wf[1][v], wf[2][v], wf[3][v], wf[4][v], eps);
-        fR[v] = weno5(wf[5][v], wf[4][v], wf[3][v], wf[2][v], wf[1][v], eps);
+        double sf[6], su[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) {
+          sf[p] = wf[p][v];
+          su[p] = wu[p][v];
+        }
+        weno5_pair(sf, sf, eps4, fL[v], fR[v]);
         if (M == MODEL_NS3D && v == NV - 1) {
-          uL[v] = weno5_split(wu[0][v], wu[1][v], wu[2][v], wu[3][v], wu[4][v],
-                              wuc[0], wuc[1], wuc[2], wuc[3], wuc[4], eps);
-          uR[v] = weno5_split(wu[5][v], wu[4][v], wu[3][v], wu[2][v], wu[1][v],
-                              wuc[5], wuc[4], wuc[3], wuc[2], wuc[1], eps);
+          double sc[6];
+#pragma unroll
+          for (int p = 0; p < 6; p++) sc[p] = wuc[p];
+          weno5_pair(su, sc, eps4, uL[v], uR[v]);
         } else {
-          uL[v] = weno5(wu[0][v], wu[1][v], wu[2][v], wu[3][v], wu[4][v], eps);
-          uR[v] = weno5(wu[5][v], wu[4][v], wu[3][v], wu[2][v], wu[1][v], eps);
+          weno5_pair(su, su, eps4, uL[v], uR[v]);
         }
       }
+      upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);
     } else {
       // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
       // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
@@ -244,36 +330,33 @@ hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
         projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
         if (M == MODEL_NS3D) {
           // uC differs from u in the energy only: add that column of L.
-          double de = pp.gm1 * (wuc[p] - wu[p][NV - 1]);
-          cuc[p][0] = fma(de, Ecc.hac, cu[p][0]);
-          cuc[p][1] = fma(de, Ecc.hac, cu[p][1]);
-          cuc[p][2] = fma(-de, Ecc.inv_a2, cu[p][2]);
+          double de = wuc[p] - wu[p][NV - 1];
+          cuc[p][0] = fma(de, Ecc.gh, cu[p][0]);
+          cuc[p][1] = fma(de, Ecc.gh, cu[p][1]);
+          cuc[p][2] = fma(-de, Ecc.gi, cu[p][2]);
         }
       }
       double xfL[NV], xfR[NV], xuL[NV], xuR[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) {
-        xfL[v] = weno5(cf[0][v], cf[1][v], cf[2][v], cf[3][v], cf[4][v], eps);
-        xfR[v] = weno5(cf[5][v], cf[4][v], cf[3][v], cf[2][v], cf[1][v], eps);
+        double sf[6], su[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) {
+          sf[p] = cf[p][v];
+          su[p] = cu[p][v];
+        }
+        weno5_pair(sf, sf, eps4, xfL[v], xfR[v]);
         if (M == MODEL_NS3D && v < 3) {
-          xuL[v] = weno5_split(cu[0][v], cu[1][v], cu[2][v], cu[3][v], cu[4][v],
-                               cuc[0][v], cuc[1][v], cuc[2][v], cuc[3][v], cuc[4][v], eps);
-          xuR[v] = weno5_split(cu[5][v], cu[4][v], cu[3][v], cu[2][v], cu[1][v],
-                               cuc[5][v], cuc[4][v], cuc[3][v], cuc[2][v], cuc[1][v], eps);
+          double sc[6];
+#pragma unroll
+          for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
+          weno5_pair(su, sc, eps4, xuL[v], xuR[v]);
         } else {
-          xuL[v] = weno5(cu[0][v], cu[1][v], cu[2][v], cu[3][v], cu[4][v], eps);
-          xuR[v] = weno5(cu[5][v], cu[4][v], cu[3][v], cu[2][v], cu[1][v], eps);
+          weno5_pair(su, su, eps4, xuL[v], xuR[v]);
         }
       }
-      projR<M, DIR>(Ecc, xfL, fL);
-      projR<M, DIR>(Ecc, xfR, fR);
-      projR<M, DIR>(Ecc, xuL, uL);
-      projR<M, DIR>(Ecc, xuR, uR);
+      upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI);
     }
-
-    // Upwinding.
-    double fI[NV];
-    upwind_iface<M, CHAR, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);
 
     if (I > I0) {
       // Flux difference of cell I-1 and the stage epilogue.

@@ -145,6 +145,16 @@ class Solver:
     def set_launch(self, dim: int, seg: int = 0, block: int = 0):
         check(lib().gb_solver_set_launch(self._h, dim, seg, block))
 
+    def get_launch(self, dim: int):
+        seg, blk = ctypes.c_int(), ctypes.c_int()
+        check(lib().gb_solver_get_launch(self._h, dim, ctypes.byref(seg), ctypes.byref(blk)))
+        return seg.value, blk.value
+
+    def autotune(self, reps: int = 2):
+        """Pick the launch shape per direction by timing (state restored)."""
+        check(lib().gb_solver_autotune(self._h, int(reps)))
+        return [self.get_launch(d) for d in range(self.ndims)]
+
     @property
     def time(self) -> float:
         return lib().gb_solver_time(self._h)

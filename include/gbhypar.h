@@ -113,6 +113,11 @@ double gb_solver_time(const gb_solver *s);
 /* Launch shape of the fused kernels: interfaces walked per thread (seg) and
  * threads per block, per direction (values <= 0 keep the current ones). */
 int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
+int gb_solver_get_launch(gb_solver *s, int dir, int *seg, int *block);
+/* Choose seg/block per direction by timing candidates on `reps` steps of the
+ * resident solution (restored afterwards): segment lengths that spread the
+ * walk evenly over the SMs in 1..4 waves, and fixed lengths 8..64. */
+int gb_solver_autotune(gb_solver *s, int reps);
 /* 1 if every value of the resident interior solution is finite, else 0. */
 int gb_solver_check_finite(gb_solver *s, int *finite);
 
