@@ -29,7 +29,10 @@ EXPORTS = [
     "gb_write_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
     "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
     "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
-    "gb_solver_get_launch", "gb_solver_autotune",
+    "gb_solver_get_launch", "gb_solver_autotune", "gb_inputs_nsims", "gb_inputs_read_member",
+    "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
+    "gb_ensemble_set_state", "gb_ensemble_get_state", "gb_ensemble_step", "gb_ensemble_time",
+    "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune",
 ]
 
 
@@ -109,6 +112,23 @@ def lib():
     L.gb_solver_profile.argtypes = [VP, ctypes.c_int]
     L.gb_solver_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gb_solver_autotune.argtypes = [VP, ctypes.c_int]
+    L.gb_inputs_nsims.argtypes = [ctypes.c_char_p]
+    L.gb_inputs_read_member.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(VP)]
+    L.gb_ensemble_create.argtypes = [ctypes.POINTER(GbConfig), ctypes.POINTER(DP), ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(VP)]
+    L.gb_ensemble_destroy.argtypes = [VP]
+    L.gb_ensemble_destroy.restype = None
+    L.gb_ensemble_size.argtypes = [VP]
+    L.gb_ensemble_set_stream.argtypes = [VP, VP]
+    L.gb_ensemble_sync.argtypes = [VP]
+    L.gb_ensemble_set_state.argtypes = [VP, ctypes.c_int, VP, ctypes.c_int, ctypes.c_int]
+    L.gb_ensemble_get_state.argtypes = [VP, ctypes.c_int, VP, ctypes.c_int, ctypes.c_int]
+    L.gb_ensemble_step.argtypes = [VP, ctypes.c_int]
+    L.gb_ensemble_time.argtypes = [VP]
+    L.gb_ensemble_time.restype = ctypes.c_double
+    L.gb_ensemble_set_launch.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.gb_ensemble_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.gb_ensemble_autotune.argtypes = [VP, ctypes.c_int]
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     _lib = L
     return L

@@ -229,3 +229,64 @@ def read_op_bin(path: str) -> Dict[str, np.ndarray]:
     npts = int(np.prod(dims))
     u = np.frombuffer(buf, np.float64, npts * int(nvars), off).reshape(npts, int(nvars))
     return {"ndims": int(ndims), "nvars": int(nvars), "dims": dims.copy(), "x": x.copy(), "u": u.copy()}
+
+
+def ensemble_sizes(nmembers: int = 64, seed: int = 20261203, lo: int = 128, hi: int = 1024, step: int = 64):
+    """Square grid sizes drawn uniformly (seeded) from {lo, lo+step, ..., hi}."""
+    rng = np.random.default_rng(seed)
+    choices = np.arange(lo, hi + 1, step)
+    return [int(v) for v in rng.choice(choices, size=nmembers)]
+
+
+def ensemble_vortex(nmembers: int = 64, seed: int = 20261203, n_iter: int = 100, sizes=None,
+                    interp: str = "characteristic", upwinding: str = "roe", scheme: str = "ssprk3",
+                    cfl: float = 0.5):
+    """Ensemble of isentropic vortices: sizes from ensemble_sizes, strength
+    b ~ U[1,5], centre ~ U[3,7]^2 (seeded), one common dt = the CFL-0.5 step of
+    the most restrictive member.  Returns a list of Cases sharing dt."""
+    rng = np.random.default_rng(seed + 1)
+    if sizes is None:
+        sizes = ensemble_sizes(nmembers, seed)
+    members = []
+    dts = []
+    for n in sizes:
+        b = float(rng.uniform(1.0, 5.0))
+        xc, yc = (float(v) for v in rng.uniform(3.0, 7.0, size=2))
+        c = vortex(n, n_iter=n_iter, dt=1.0, b=b, xc=xc, yc=yc, interp=interp, upwinding=upwinding,
+                   scheme=scheme)
+        dts.append(cfl_dt(c.u, 4, [10.0 / n, 10.0 / n], cfl))
+        members.append(c)
+    dt = min(dts)
+    for c in members:
+        c.dt = dt
+    return members
+
+
+def write_ensemble(members, directory: str) -> str:
+    """HyPar ensemble deck: simulation.inp, one solver.inp listing every size,
+    initial_<k>.inp and boundary_<k>.inp (k zero-padded to log10(n)+1 digits)."""
+    os.makedirs(directory, exist_ok=True)
+    n = len(members)
+    width = int(math.log10(n)) + 1
+    c0 = members[0]
+    # "size" and "iproc" list ndims values for every simulation (ReadInputs.c:189-230)
+    txt = c0.solver_inp().replace("  size              " + " ".join(str(s) for s in c0.size),
+                                  "  size              " + "  ".join(" ".join(str(s) for s in c.size)
+                                                                     for c in members))
+    txt = txt.replace("  iproc             " + " ".join("1" for _ in c0.size),
+                      "  iproc             " + "  ".join(" ".join("1" for _ in c.size) for c in members))
+    with open(os.path.join(directory, "simulation.inp"), "w") as f:
+        f.write(f"begin\n  nsims {n}\nend\n")
+    with open(os.path.join(directory, "solver.inp"), "w") as f:
+        f.write(txt)
+    with open(os.path.join(directory, "physics.inp"), "w") as f:
+        f.write(c0.physics_inp())
+    with open(os.path.join(directory, "weno.inp"), "w") as f:
+        f.write(c0.weno_inp())
+    for k, c in enumerate(members):
+        idx = str(k).zfill(width)
+        with open(os.path.join(directory, f"boundary_{idx}.inp"), "w") as f:
+            f.write(c.boundary_inp())
+        with open(os.path.join(directory, f"initial_{idx}.inp"), "wb") as f:
+            f.write(c.initial_bytes())
+    return directory

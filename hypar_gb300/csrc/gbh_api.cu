@@ -187,7 +187,7 @@ static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
   return GB_OK;
 }
 
-static int validate(const gb_config* c) {
+int gbh_validate(const gb_config* c) {
   if (!c) { gbh_set_error("null config"); return GB_ERR_ARG; }
   int nd = c->model == GB_MODEL_EULER1D ? 1 : c->model == GB_MODEL_EULER2D ? 2 : c->model == GB_MODEL_NS3D ? 3 : 0;
   if (!nd) { gbh_set_error("unknown model %d", c->model); return GB_ERR_ARG; }
@@ -218,20 +218,10 @@ static int validate(const gb_config* c) {
   return GB_OK;
 }
 
-extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int device, gb_solver** out) {
-  if (!out || !dxinv) { gbh_set_error("gb_solver_create: null argument"); return GB_ERR_ARG; }
-  *out = nullptr;
-  int rc = validate(cfg);
-  if (rc) return rc;
-  gb_solver* s = new gb_solver();
-  s->cfg = *cfg;
-  const gb_config& c = s->cfg;
-  if (device >= 0) {
-    cudaError_t e = cudaSetDevice(device);
-    if (e != cudaSuccess) { gbh_set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); delete s; return GB_ERR_CUDA; }
-  }
-  cudaGetDevice(&s->device);
-  DevGeom& G = s->G;
+// Geometry of a configuration: strides with ghosts, and per face whether the
+// boundary is folded into the halo loads (exactly one zone covering the whole
+// face) or applied in memory by bc_zone_kernel (zone indices into mem_zones).
+long long gbh_geometry(const gb_config& c, DevGeom& G, std::vector<int>* mem_zones) {
   G.nd = c.ndims;
   G.g = c.ghosts;
   long long st = 1;
@@ -241,9 +231,6 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
     if (d < c.ndims) st *= (c.dim[d] + 2 * c.ghosts);
     G.bclo[d] = G.bchi[d] = FOLD_MEMORY;
   }
-  s->npts_wg = st;
-  s->nvals = (size_t)st * c.nvars;
-  // Fold a face into the halo loads when exactly one zone covers all of it.
   for (int d = 0; d < c.ndims; d++)
     for (int side = 0; side < 2; side++) {
       int face = side == 0 ? 1 : -1, cnt = 0, which = -1;
@@ -258,9 +245,29 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
       int mode = FOLD_MEMORY;
       if (full) mode = c.zones[which][0] == GB_BC_PERIODIC ? FOLD_PERIODIC : FOLD_MIRROR;
       if (side == 0) G.bclo[d] = mode; else G.bchi[d] = mode;
-      for (int z = 0; z < c.nzones; z++)
-        if (c.zones[z][1] == d && c.zones[z][2] == face && !full) s->mem_zones.push_back(z);
+      if (mem_zones)
+        for (int z = 0; z < c.nzones; z++)
+          if (c.zones[z][1] == d && c.zones[z][2] == face && !full) mem_zones->push_back(z);
     }
+  return st;
+}
+
+extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int device, gb_solver** out) {
+  if (!out || !dxinv) { gbh_set_error("gb_solver_create: null argument"); return GB_ERR_ARG; }
+  *out = nullptr;
+  int rc = gbh_validate(cfg);
+  if (rc) return rc;
+  gb_solver* s = new gb_solver();
+  s->cfg = *cfg;
+  const gb_config& c = s->cfg;
+  if (device >= 0) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { gbh_set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); delete s; return GB_ERR_CUDA; }
+  }
+  cudaGetDevice(&s->device);
+  s->npts_wg = gbh_geometry(c, s->G, &s->mem_zones);
+  long long st = s->npts_wg;
+  s->nvals = (size_t)st * c.nvars;
   s->pp.gamma = c.gamma;
   s->pp.gm1 = c.gamma - 1.0;
   s->pp.inv_gm1 = 1.0 / (c.gamma - 1.0);

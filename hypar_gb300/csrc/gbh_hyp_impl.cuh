@@ -229,16 +229,16 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
   }
 }
 
+// One thread's share of a launch: interfaces [sg*seg, min((sg+1)*seg, N)] of
+// the grid line with transverse index `tr` (other dimensions ascending, first
+// fastest), and the flux difference / epilogue of the cells in between.
 template <int M, bool CHAR, int UPW, int DIR>
-__global__ void __launch_bounds__(128)
-hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
-               DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
+__device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double* __restrict__ H,
+                                            const double* __restrict__ dxinv, const DevGeom& G,
+                                            const PhysParams& pp, const StageEpi& ep, int seg, long long tr,
+                                            int sg) {
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
-  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= ntrans * (long long)nseg) return;
-  long long tr = tid % ntrans;
-  const int sg = (int)(tid / ntrans);
 
   long long pbase = (long long)G.g * G.stride[DIR];
 #pragma unroll
@@ -401,6 +401,83 @@ hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
     for (int v = 0; v < NV; v++) fIp[v] = fI[v];
     shift();
   }
+}
+
+template <int M, bool CHAR, int UPW, int DIR>
+__global__ void __launch_bounds__(128)
+hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
+               DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= ntrans * (long long)nseg) return;
+  hyp_segment<M, CHAR, UPW, DIR>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
+}
+
+// All members of an ensemble advanced by one launch per direction: a thread
+// finds its member by binary search over the start offsets, then walks its
+// segment exactly as in the single-grid kernel.
+template <int M, bool CHAR, int UPW, int DIR>
+__global__ void __launch_bounds__(128)
+hyp_batched_kernel(const MemberDev* __restrict__ mem, int nmem, long long total, const double* __restrict__ U,
+                   double* __restrict__ H, const double* __restrict__ dxinv, PhysParams pp, StageEpi ep) {
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= total) return;
+  int lo = 0, hi = nmem - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (mem[mid].start[DIR] <= tid) lo = mid;
+    else hi = mid - 1;
+  }
+  const MemberDev& m = mem[lo];
+  long long lt = tid - m.start[DIR];
+  long long ntr = m.ntrans[DIR];
+  StageEpi e = ep;
+  const long long o = m.off;
+  if (e.par) e.par += o;
+  if (e.rhs) e.rhs += o;
+  if (e.u) e.u += o;
+  if (e.uout) e.uout += o;
+  if (e.acc) e.acc += o;
+#pragma unroll
+  for (int t = 0; t < 4; t++)
+    if (e.P[t]) e.P[t] += o;
+  hyp_segment<M, CHAR, UPW, DIR>(U + o, H ? H + o : nullptr, dxinv + m.dx_off[DIR], m.G, pp, e, m.seg[DIR],
+                                 lt % ntr, (int)(lt / ntr));
+}
+
+template <int M, bool CHAR, int UPW, int DIR>
+cudaError_t launch_batched_dir(const MemberDev* mem, int nmem, long long total, const double* U, double* H,
+                               const double* dxinv, const PhysParams& pp, const StageEpi& ep, int block,
+                               cudaStream_t s) {
+  if (block <= 0) block = 128;
+  long long grid = (total + block - 1) / block;
+  hyp_batched_kernel<M, CHAR, UPW, DIR><<<(unsigned)grid, block, 0, s>>>(mem, nmem, total, U, H, dxinv, pp, ep);
+  return cudaGetLastError();
+}
+
+template <int M>
+cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
+                                 const double* U, double* H, const double* dxinv, const PhysParams& pp,
+                                 const StageEpi& ep, int block, cudaStream_t s) {
+  constexpr int ND = ModelTraits<M>::ND;
+#define GBH_B(C, W)                                                                                          \
+  do {                                                                                                       \
+    if (dir == 0) return launch_batched_dir<M, C, W, 0>(mem, nmem, total, U, H, dxinv, pp, ep, block, s);  \
+    if (ND > 1 && dir == 1)                                                                                  \
+      return launch_batched_dir<M, C, W, (ND > 1 ? 1 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, s); \
+    if (ND > 2 && dir == 2)                                                                                  \
+      return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, s); \
+    return cudaErrorInvalidValue;                                                                            \
+  } while (0)
+  if (chr) {
+    if (upw == UPW_ROE) GBH_B(true, UPW_ROE);
+    if (upw == UPW_LLF) GBH_B(true, UPW_LLF);
+    GBH_B(true, UPW_RF);
+  } else {
+    if (upw == UPW_ROE) GBH_B(false, UPW_ROE);
+    if (upw == UPW_LLF) GBH_B(false, UPW_LLF);
+    GBH_B(false, UPW_RF);
+  }
+#undef GBH_B
 }
 
 // Host launcher for one direction.

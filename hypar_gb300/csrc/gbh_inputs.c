@@ -116,14 +116,17 @@ static void find_interval(double a, double b, const double *x, int N, int *imin,
 typedef struct {
   int ndims, nvars, ghosts, n_iter, file_op_iter;
   int size[3], iproc[3];
+  int member, nsims;   /* which simulation of an ensemble (simulation.inp) */
   double dt;
   char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
   char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
   char op_overwrite[MAXS], hyp_flux_split[MAXS];
 } solver_inp;
 
-static int read_solver_inp(const char *dir, solver_inp *si) {
+static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsims) {
   memset(si, 0, sizeof(*si));
+  si->member = member;
+  si->nsims = nsims;
   si->ndims = 1;
   si->nvars = 1;
   si->ghosts = 1;
@@ -159,13 +162,16 @@ static int read_solver_inp(const char *dir, solver_inp *si) {
     else if (!strcmp(w, "nvars")) r = fscanf(in, "%d", &si->nvars);
     else if (!strcmp(w, "size") || !strcmp(w, "iproc") || !strcmp(w, "size_exact")) {
       if (!have_ndims || si->ndims < 1 || si->ndims > 3) { ok = 0; break; }
+      /* "size" lists ndims values for every simulation of an ensemble
+         (ReadInputs.c:189-206); "iproc" and "size_exact" likewise per simulation */
       int *dst = !strcmp(w, "size") ? si->size : (!strcmp(w, "iproc") ? si->iproc : NULL);
-      for (int d = 0; d < si->ndims; d++) {
-        int val;
-        r = fscanf(in, "%d", &val);
-        if (r != 1) break;
-        if (dst) dst[d] = val;
-      }
+      for (int n = 0; n < si->nsims && r == 1; n++)
+        for (int d = 0; d < si->ndims; d++) {
+          int val;
+          r = fscanf(in, "%d", &val);
+          if (r != 1) break;
+          if (dst && n == si->member) dst[d] = val;
+        }
     }
     else if (!strcmp(w, "ghost")) r = fscanf(in, "%d", &si->ghosts);
     else if (!strcmp(w, "n_iter")) r = fscanf(in, "%d", &si->n_iter);
@@ -273,14 +279,49 @@ const double *gb_inputs_dxinv(const gb_inputs *in) { return in ? in->dxinv : NUL
 const double *gb_inputs_u0(const gb_inputs *in) { return in ? in->u0 : NULL; }
 const char *gbh_inputs_op_overwrite(const gb_inputs *in) { return in ? in->op_overwrite : "yes"; }
 
-int gb_inputs_read(const char *dir, gb_inputs **out) {
-  if (!out) {
-    gbh_set_error("gb_inputs_read: null output");
+int gb_inputs_nsims(const char *dir) {
+  /* simulation.inp (src/Simulation/EnsembleSimulationsDefine.cpp:41-70): "begin nsims N end" */
+  FILE *in = open_in(dir, "simulation.inp", "r");
+  if (!in) return 1;
+  char w[MAXS];
+  int n = 1;
+  if (fscanf(in, "%511s", w) == 1 && !strcmp(w, "begin")) {
+    while (fscanf(in, "%511s", w) == 1 && strcmp(w, "end")) {
+      if (!strcmp(w, "nsims")) {
+        if (fscanf(in, "%d", &n) != 1) n = -1;
+      } else {
+        char useless[MAXS];
+        if (fscanf(in, "%511s", useless) != 1) break;
+      }
+    }
+  } else {
+    n = -1;
+  }
+  fclose(in);
+  return n;
+}
+
+static void member_name(char *out, size_t sz, const char *root, int member, int nsims) {
+  /* <root>_<index>.inp with the index zero-padded to (int)log10(nsims)+1 digits
+     (InitialSolution.c:36-41, GetStringFromInteger) */
+  if (nsims <= 1) {
+    snprintf(out, sz, "%s.inp", root);
+    return;
+  }
+  int width = (int)log10((double)nsims) + 1;
+  snprintf(out, sz, "%s_%0*d.inp", root, width, member);
+}
+
+int gb_inputs_read(const char *dir, gb_inputs **out) { return gb_inputs_read_member(dir, 0, 1, out); }
+
+int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **out) {
+  if (!out || nsims < 1 || member < 0 || member >= nsims) {
+    gbh_set_error("gb_inputs_read_member: bad argument");
     return GB_ERR_ARG;
   }
   *out = NULL;
   solver_inp si;
-  int rc = read_solver_inp(dir, &si);
+  int rc = read_solver_inp(dir, &si, member, nsims);
   if (rc) return rc;
   gb_config c;
   memset(&c, 0, sizeof(c));
@@ -395,8 +436,11 @@ int gb_inputs_read(const char *dir, gb_inputs **out) {
   res->u0 = (double *)calloc(npts * c.nvars, sizeof(double));
 
   /* initial.inp */
+  char iname[256], bname[256];
+  member_name(iname, sizeof(iname), "initial", member, nsims);
+  member_name(bname, sizeof(bname), "boundary", member, nsims);
   if (!strcmp(si.ip_file_type, "bin") || !strcmp(si.ip_file_type, "binary")) {
-    FILE *in = open_in(dir, "initial.inp", "rb");
+    FILE *in = open_in(dir, iname, "rb");
     if (!in) {
       gb_inputs_free(res);
       gbh_set_error("initial solution file initial.inp not found");
@@ -411,7 +455,7 @@ int gb_inputs_read(const char *dir, gb_inputs **out) {
       return GB_ERR_INPUT;
     }
   } else if (!strcmp(si.ip_file_type, "ascii")) {
-    FILE *in = open_in(dir, "initial.inp", "r");
+    FILE *in = open_in(dir, iname, "r");
     if (!in) {
       gb_inputs_free(res);
       gbh_set_error("initial solution file initial.inp not found");
@@ -450,9 +494,10 @@ int gb_inputs_read(const char *dir, gb_inputs **out) {
     }
   }
 
-  /* boundary.inp */
+  /* boundary_<index>.inp, else boundary.inp (InitializeBoundaries.c:55-75) */
   {
-    FILE *in = open_in(dir, "boundary.inp", "r");
+    FILE *in = open_in(dir, bname, "r");
+    if (!in) in = open_in(dir, "boundary.inp", "r");
     if (!in) {
       gb_inputs_free(res);
       gbh_set_error("boundary condition file boundary.inp not found");

@@ -4,6 +4,10 @@
 
 #include <cuda_runtime.h>
 
+#include <vector>
+
+#include "gbhypar.h"
+
 #include "gbh_device.cuh"
 
 namespace gbh {
@@ -59,4 +63,20 @@ struct HypLaunch {
   int block;       // threads per block
 };
 
+// Ensemble member as seen by the batched kernel: its geometry, where its
+// arrays start inside the batched arrays, and which threads of a launch along
+// each direction are its (start[d] .. start[d] + ntrans[d]*nseg[d]).
+struct MemberDev {
+  DevGeom G;
+  long long off;         // first value of the member in every state array
+  long long dx_off[3];   // first dxinv value of each direction
+  long long start[3];    // first thread of the member per direction
+  long long ntrans[3];
+  int nseg[3], seg[3];
+};
+
 }  // namespace gbh
+
+int gbh_validate(const gb_config* c);
+long long gbh_geometry(const gb_config& c, gbh::DevGeom& G, std::vector<int>* mem_zones);
+extern "C" void gbh_set_error(const char* fmt, ...);

@@ -26,7 +26,70 @@ static int write_op(const char *dir, const char *name, const gb_config *c, const
   return gb_write_binary(path, c->ndims, c->nvars, c->dim, x, buf);
 }
 
+static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
+  gb_inputs **in = (gb_inputs **)calloc(nsims, sizeof(gb_inputs *));
+  gb_config *cf = (gb_config *)calloc(nsims, sizeof(gb_config));
+  const double **dx = (const double **)calloc(nsims, sizeof(double *));
+  int rc = GB_OK;
+  for (int m = 0; m < nsims && !rc; m++) {
+    rc = gb_inputs_read_member(dir, m, nsims, &in[m]);
+    if (!rc) {
+      cf[m] = *gb_inputs_config(in[m]);
+      dx[m] = gb_inputs_dxinv(in[m]);
+    }
+  }
+  gb_ensemble *e = NULL;
+  if (!rc) rc = gb_ensemble_create(cf, dx, nsims, device, &e);
+  long nmax = 0;
+  for (int m = 0; m < nsims && !rc; m++) {
+    long n = cf[m].nvars;
+    for (int d = 0; d < cf[m].ndims; d++) n *= cf[m].dim[d];
+    if (n > nmax) nmax = n;
+    rc = gb_ensemble_set_state(e, m, gb_inputs_u0(in[m]), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
+  }
+  double *buf = (double *)malloc(sizeof(double) * (nmax > 0 ? nmax : 1));
+  int overwrite = !rc && !strcmp(gbh_inputs_op_overwrite(in[0]), "yes");
+  int every = cf[0].file_op_iter > 0 ? cf[0].file_op_iter : cf[0].n_iter;
+  int width = 1;
+  for (int n = nsims; n >= 10; n /= 10) width++;
+  int k = 0;
+  char name[160], path[4400];
+  if (width > 9) width = 9;
+  for (int it = 0; !rc && it <= cf[0].n_iter;) {
+    int write = (!overwrite && (it % every == 0 || it == cf[0].n_iter)) || (overwrite && it == cf[0].n_iter);
+    for (int m = 0; write && m < nsims && !rc; m++) {
+      rc = gb_ensemble_get_state(e, m, buf, GB_LAYOUT_INTERIOR, GB_MEM_HOST);
+      if (overwrite) snprintf(name, sizeof(name), "op_%0*d.bin", width, m);
+      else snprintf(name, sizeof(name), "op_%0*d_%05d.bin", width, m, k);
+      if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s", dir, name);
+      else snprintf(path, sizeof(path), "%s", name);
+      if (!rc) rc = gb_write_binary(path, cf[m].ndims, cf[m].nvars, cf[m].dim, gb_inputs_x(in[m]), buf);
+    }
+    if (write && !overwrite) k++;
+    if (it == cf[0].n_iter) break;
+    int chunk = every;
+    if (it + chunk > cf[0].n_iter) chunk = cf[0].n_iter - it;
+    if (!rc) rc = gb_ensemble_step(e, chunk);
+    it += chunk;
+    if (!rc && verbose) printf("gbhypar: ensemble of %d, iteration %d / %d\n", nsims, it, cf[0].n_iter);
+  }
+  if (!rc) rc = gb_ensemble_sync(e);
+  free(buf);
+  gb_ensemble_destroy(e);
+  for (int m = 0; m < nsims; m++) gb_inputs_free(in[m]);
+  free(in);
+  free(cf);
+  free(dx);
+  return rc;
+}
+
 int gb_run_case(const char *dir, int device, int verbose) {
+  int nsims = gb_inputs_nsims(dir);
+  if (nsims < 1) {
+    gbh_set_error("simulation.inp is malformed");
+    return GB_ERR_INPUT;
+  }
+  if (nsims > 1) return run_ensemble(dir, device, verbose, nsims);
   gb_inputs *in = NULL;
   int rc = gb_inputs_read(dir, &in);
   if (rc) return rc;

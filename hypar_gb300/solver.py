@@ -243,3 +243,91 @@ def run_case(directory: str, device: int = 0, verbose: bool = False) -> None:
 def read_op(path: str):
     from .cases import read_op_bin
     return read_op_bin(path)
+
+
+class Ensemble:
+    """gb_ensemble: members of one HyPar ensemble deck advanced together."""
+
+    def __init__(self, configs, dxinvs, device: int = 0):
+        n = len(configs)
+        self.configs = list(configs)
+        arr = (GbConfig * n)(*configs)
+        self._dx = [np.ascontiguousarray(d, dtype=np.float64) for d in dxinvs]
+        ptrs = (_lib.DP * n)(*[d.ctypes.data_as(_lib.DP) for d in self._dx])
+        h = ctypes.c_void_p()
+        check(lib().gb_ensemble_create(arr, ptrs, n, device, ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def from_dir(cls, directory: str, device: int = 0) -> "Ensemble":
+        n = lib().gb_inputs_nsims(directory.encode())
+        if n < 1:
+            raise _lib.GbError(3, "simulation.inp is malformed")
+        inputs = []
+        for m in range(n):
+            h = ctypes.c_void_p()
+            check(lib().gb_inputs_read_member(directory.encode(), m, n, ctypes.byref(h)))
+            c = lib().gb_inputs_config(h).contents
+            cfg = GbConfig()
+            ctypes.pointer(cfg)[0] = c
+            dims = [c.dim[d] for d in range(c.ndims)]
+            nxg = sum(d + 2 * c.ghosts for d in dims)
+            npts = int(np.prod(dims))
+            dx = np.ctypeslib.as_array(lib().gb_inputs_dxinv(h), shape=(nxg,)).copy()
+            u0 = np.ctypeslib.as_array(lib().gb_inputs_u0(h), shape=(npts * c.nvars,)).copy()
+            lib().gb_inputs_free(h)
+            inputs.append((cfg, dx, u0))
+        e = cls([i[0] for i in inputs], [i[1] for i in inputs], device)
+        for m, (_, _, u0) in enumerate(inputs):
+            e.set_state(m, u0)
+        return e
+
+    def __len__(self):
+        return lib().gb_ensemble_size(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gb_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, m: int, u):
+        arr = np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().gb_ensemble_set_state(self._h, m, arr.ctypes.data, _lib.LAYOUT_INTERIOR, _lib.MEM_HOST))
+
+    def get_state(self, m: int) -> np.ndarray:
+        c = self.configs[m]
+        n = int(np.prod([c.dim[d] for d in range(c.ndims)])) * c.nvars
+        out = np.empty(n, dtype=np.float64)
+        check(lib().gb_ensemble_get_state(self._h, m, out.ctypes.data, _lib.LAYOUT_INTERIOR, _lib.MEM_HOST))
+        return out
+
+    def step(self, nsteps: int = 1):
+        check(lib().gb_ensemble_step(self._h, int(nsteps)))
+
+    def sync(self):
+        check(lib().gb_ensemble_sync(self._h))
+
+    def set_stream(self, stream_handle):
+        check(lib().gb_ensemble_set_stream(self._h, stream_handle))
+
+    def set_launch(self, dim: int, seg: int = 0, block: int = 0):
+        check(lib().gb_ensemble_set_launch(self._h, dim, seg, block))
+
+    def get_launch(self, dim: int):
+        seg, blk = ctypes.c_int(), ctypes.c_int()
+        check(lib().gb_ensemble_get_launch(self._h, dim, ctypes.byref(seg), ctypes.byref(blk)))
+        return seg.value, blk.value
+
+    def autotune(self, reps: int = 2):
+        check(lib().gb_ensemble_autotune(self._h, int(reps)))
+        return [self.get_launch(d) for d in range(self.configs[0].ndims)]
+
+    @property
+    def time(self) -> float:
+        return lib().gb_ensemble_time(self._h)

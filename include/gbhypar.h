@@ -86,6 +86,13 @@ const double *gb_inputs_x(const gb_inputs *in);
 const double *gb_inputs_dxinv(const gb_inputs *in);
 /* Initial solution, interior points, nvars per point, dimension 0 fastest. */
 const double *gb_inputs_u0(const gb_inputs *in);
+/* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
+ * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
+ * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
+ * number of simulations in `dir` (1 without simulation.inp, -1 if malformed),
+ * and the deck of simulation `member`. */
+int gb_inputs_nsims(const char *dir);
+int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **out);
 /* Runge-Kutta Butcher table of TimeExplicitRKInitialize for a solver.inp
  * time_scheme_type ("1fe", "22", "33", "44", "ssprk3"). */
 int gb_rk_table(const char *type, int *nstages, double *A, double *b, double *c);
@@ -131,10 +138,32 @@ enum { GB_PROF_HYP_X = 0, GB_PROF_HYP_Y = 1, GB_PROF_HYP_Z = 2, GB_PROF_VISC = 3
 int gb_solver_profile(gb_solver *s, int enable);
 int gb_solver_profile_read(gb_solver *s, double *ms, long long *launches);
 
+/* ---- batched ensemble: HyPar's ensemble mode (several independent
+ *      simulations, possibly of different sizes, one TimeRK) ----
+ * Members share model, schemes, time step and Butcher table and differ in size,
+ * boundaries and initial data.  Every Runge-Kutta stage is one launch per
+ * direction over all members; gb_ensemble_step replays one captured CUDA graph
+ * per step.  Inviscid models only; boundary zones must cover whole faces. */
+typedef struct gb_ensemble gb_ensemble;
+int gb_ensemble_create(const gb_config *cfgs, const double *const *dxinvs, int nsims, int device, gb_ensemble **out);
+void gb_ensemble_destroy(gb_ensemble *e);
+int gb_ensemble_size(const gb_ensemble *e);
+int gb_ensemble_set_stream(gb_ensemble *e, void *stream);
+int gb_ensemble_sync(gb_ensemble *e);
+int gb_ensemble_set_state(gb_ensemble *e, int member, const double *u, int layout, int mem);
+int gb_ensemble_get_state(gb_ensemble *e, int member, double *u, int layout, int mem);
+int gb_ensemble_step(gb_ensemble *e, int nsteps);
+double gb_ensemble_time(const gb_ensemble *e);
+int gb_ensemble_set_launch(gb_ensemble *e, int dir, int seg, int block);
+int gb_ensemble_get_launch(gb_ensemble *e, int dir, int *seg, int *block);
+/* Choose seg/block per direction by timing graph-replayed steps (state restored). */
+int gb_ensemble_autotune(gb_ensemble *e, int reps);
+
 /* Read the deck in `dir`, run n_iter steps on the GPU and write op.bin (and
  * op_NNNNN.bin every file_op_iter steps when op_overwrite is "no") in HyPar's
- * binary format (src/IOFunctions/WriteBinary.c).  The drop-in for HyPar's
- * main() on this path. */
+ * binary format (src/IOFunctions/WriteBinary.c); an ensemble deck
+ * (simulation.inp) runs as one batched ensemble and writes op_<k>.bin /
+ * op_<k>_NNNNN.bin per simulation.  The drop-in for HyPar's main() on this path. */
 int gb_run_case(const char *dir, int device, int verbose);
 /* Write a HyPar binary solution file from an interior solution. */
 int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);

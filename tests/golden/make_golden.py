@@ -13,6 +13,7 @@ the reference solution after n_iter Runge-Kutta steps (op.bin).
 """
 from __future__ import annotations
 
+import math
 import os
 import subprocess
 import sys
@@ -42,6 +43,11 @@ CASES = {
 }
 
 
+ENSEMBLES = {
+    "ens3_vortex_char_roe_ssprk3": lambda: C.ensemble_vortex(3, sizes=[16, 24, 20], n_iter=4, seed=7),
+}
+
+
 def main() -> None:
     if not O.ref_available():
         raise SystemExit("oracle/_ref is not built (make -f oracle/Makefile.ref)")
@@ -59,6 +65,16 @@ def main() -> None:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), u0=case.u, rhs=rhs, uN=op["u"],
                             n_iter=case.n_iter, dt=case.dt)
         print(name, rhs.shape, op["u"].shape)
+    for name, mk in ENSEMBLES.items():
+        members = mk()
+        with tempfile.TemporaryDirectory() as d:
+            C.write_ensemble(members, d)
+            subprocess.check_call([os.path.join(O.REF_DIR, "HyPar")], cwd=d, stdout=subprocess.DEVNULL, env=env)
+            width = int(math.log10(len(members))) + 1
+            outs = {f"uN_{k}": C.read_op_bin(os.path.join(d, f"op_{str(k).zfill(width)}.bin"))["u"]
+                    for k in range(len(members))}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), n_iter=members[0].n_iter, dt=members[0].dt, **outs)
+        print(name, [v.shape for v in outs.values()])
 
 
 if __name__ == "__main__":

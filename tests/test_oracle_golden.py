@@ -71,3 +71,26 @@ def test_oracle_matches_live_reference(oracle_lib, tmp_path):
     P = O.Problem(case)
     u = O.interior(P.rk(P.u0(), 2), case.size, case.nvars, 3)
     assert np.array_equal(u, ref)
+
+
+def _ensembles():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.ENSEMBLES
+
+
+ENSEMBLES = _ensembles()
+
+
+@pytest.mark.parametrize("name", sorted(ENSEMBLES))
+def test_ensemble_members_are_independent_runs(oracle_lib, name):
+    """The reference's ensemble mode advances every member exactly as a single
+    run with the common time step would (each member against the oracle)."""
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    members = ENSEMBLES[name]()
+    for k, case in enumerate(members):
+        P = O.Problem(case)
+        u = O.interior(P.rk(P.u0(), int(g["n_iter"])), case.size, case.nvars, 3)
+        assert relerr(u, g[f"uN_{k}"]) <= 1e-13
