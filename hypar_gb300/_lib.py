@@ -32,7 +32,7 @@ EXPORTS = [
     "gb_solver_get_launch", "gb_solver_autotune", "gb_inputs_nsims", "gb_inputs_read_member",
     "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
     "gb_ensemble_set_state", "gb_ensemble_get_state", "gb_ensemble_step", "gb_ensemble_time",
-    "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune",
+    "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune", "gb_rhs_explicit_noalloc",
 ]
 
 
@@ -130,6 +130,7 @@ def lib():
     L.gb_ensemble_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gb_ensemble_autotune.argtypes = [VP, ctypes.c_int]
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
+    L.gb_rhs_explicit_noalloc.argtypes = [ctypes.POINTER(GbConfig), VP, VP, VP, VP]
     _lib = L
     return L
 

@@ -207,6 +207,30 @@ int gb_RHSFunctionExplicit(double *rhs, double *u, void *s, void *m, double t);
  * Runge-Kutta step of the resident solution. */
 int gb_TimeRK(void *ts);
 
+/* ---- right-hand side without device allocation ----
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory (code running inside a memory pool or arena it does not own, hosts
+ * with a locked-down allocator, allocation-free sections of a time loop): the
+ * rhs of gb_RHSFunctionExplicit for an INVISCID configuration, with no
+ * gb_solver and no device allocation.  cfg: the configuration (the
+ * Runge-Kutta fields are ignored); dxinv: DEVICE array of sum_d
+ * (dim[d]+2*ghosts) values; u, rhs: DEVICE arrays in HyPar's ghosted layout
+ * (u's ghost points are filled in place, as gb_RHSFunctionExplicit does);
+ * stream: a cudaStream_t (NULL: the legacy default stream).  Work is queued on
+ * `stream`; the call does not wait for it.
+ * The directions before the last accumulate into a library-wide device array
+ * of GB_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading the library
+ * holds until exit; a 2-D or 3-D grid whose ghosted solution is larger is
+ * rejected with GB_ERR_ARG (1-D grids need no scratch).  Viscous NS3D (Re > 0)
+ * returns GB_ERR_UNSUPPORTED.  All calls on a device share that array: calls
+ * whose work overlaps on the GPU (different streams, no ordering between
+ * them) race and give wrong results; keep them on one stream or order them.
+ * The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress) with that device current: make it before any stream
+ * capture begins. */
+#define GB_NOALLOC_SCRATCH_BYTES (64ull << 20)
+int gb_rhs_explicit_noalloc(const gb_config *cfg, const double *dxinv, double *rhs, double *u, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
