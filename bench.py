@@ -7,7 +7,7 @@ characteristic WENO5 (Jiang-Shu) + Roe, SSPRK3, dt at CFL 0.5, FP64.  A
 "step" is one SSPRK3 step of that grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload vortex|tgv|sod]
+                  [--workload vortex|tgv|sod|ensemble|adjoint]
 
 --impl ours       the fused CUDA path through libgbhypar's C ABI (value: device
                   time of the resident solution; e2e: host buffers copied in and
@@ -376,6 +376,172 @@ def run_ensemble(args, ws, rank, local):
     return out
 
 
+def run_adjoint(args, ws, rank, local):
+    """Gradient of 0.5 ||rho(T) - rho_target||^2 with respect to the initial
+    density (2D Euler 256^2 periodic, comp-WENO5 + Roe, RK4, 400 steps,
+    ceil(sqrt(400)) = 20 checkpoints) against the plain fused forward solve of
+    the same 400 steps: a "step" is one gradient evaluation (forward sweep with
+    checkpoints + backward sweep).  Also checks the gradient against central
+    differences (h = 1e-6) on 16 random density directions and the adjoint
+    against the tangent-linear model (dot-product test), on the full problem."""
+    import numpy as np
+    import torch
+    from hypar_gb300 import cases as C
+    from hypar_gb300 import _lib
+    from hypar_gb300.adjoint import Adjoint
+    from hypar_gb300.solver import Inputs, Solver
+
+    torch.cuda.set_device(local)
+    n = args.size or 256
+    nsteps = 400
+    case, u_true = C.adjoint_problem(n, nsteps)
+    tmp = tempfile.mkdtemp(prefix="gbh_adj_")
+    case.write(tmp)
+    inp = Inputs(tmp)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    s = Solver(inp.config, inp.dxinv, device=local)
+    s.set_stream(stream.cuda_stream)
+    s.set_state(case.u)
+    fwd_shape = s.autotune(1)
+    L = _lib.lib()
+    results = {}
+    for ncheck, tag in ((0, "sqrt"), (1, "store_all")):
+        adj = Adjoint(inp.config, inp.dxinv, nsteps, ncheck=ncheck, device=local)
+        adj.set_stream(stream.cuda_stream)
+        for d, (sg, bl) in enumerate(fwd_shape):
+            adj.set_launch(d, sg, bl)
+        u_t = adj.ghosted(torch.from_numpy(u_true.reshape(n, n, 4).copy()).cuda()).contiguous()
+        u0_int = torch.from_numpy(case.u.reshape(n, n, 4).copy()).cuda()
+        u0 = adj.ghosted(u0_int).contiguous()
+        vjp_shape = adj.autotune(u0)
+        uT = adj.empty()
+        adj.forward(u_t, uT)
+        rho_tgt = adj.interior(uT)[..., 0].clone()
+        adj.forward(u0, uT)
+        ubarT = adj.empty()
+        adj.interior(ubarT)[..., 0] = adj.interior(uT)[..., 0] - rho_tgt
+        ub0 = adj.empty()
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        K = max(1, min(args.steps, 5))
+        for _ in range(2):
+            adj.forward(u0, uT)
+            adj.backward(ubarT, ub0)
+        torch.cuda.synchronize()
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+        with ClockSampler(local) as clk:
+            for k in range(K):
+                flush.fill_(float(k))
+                ev[k][0].record(stream)
+                _lib.check(L.gb_adjoint_forward(adj._h, u0.data_ptr(), uT.data_ptr()))
+                ev[k][1].record(stream)
+                _lib.check(L.gb_adjoint_backward(adj._h, ubarT.data_ptr(), ub0.data_ptr()))
+                ev[k][2].record(stream)
+            torch.cuda.synchronize()
+        t_fs = sum(e[0].elapsed_time(e[1]) for e in ev) / K
+        t_bs = sum(e[1].elapsed_time(e[2]) for e in ev) / K
+        info = adj.info()
+        results[tag] = {"ncheck": ncheck, "adj": adj, "t_fs": t_fs, "t_bs": t_bs, "info": info,
+                        "vjp_seg": vjp_shape, "clocks": clk.summary(), "u0": u0, "u0_int": u0_int,
+                        "rho_tgt": rho_tgt, "ub0": ub0.clone()}
+    # the plain forward solve: the solver's fused steps over the same 400 steps
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    s.set_state(case.u)
+    s.step(nsteps)
+    K = max(1, min(args.steps, 5))
+    tf = []
+    for k in range(K):
+        s.set_state(case.u)
+        flush.fill_(float(k))
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _lib.check(L.gb_solver_step(s.handle, nsteps))
+        b.record(stream)
+        torch.cuda.synchronize()
+        tf.append(a.elapsed_time(b))
+    t_f = sum(tf) / K
+    # accuracy on the full problem: central differences and the dot-product test
+    R = results["sqrt"]
+    adj, u0_int, rho_tgt = R["adj"], R["u0_int"], R["rho_tgt"]
+    grad = adj.interior(R["ub0"])[..., 0]
+
+    def misfit(u_int):
+        out = adj.empty()
+        adj.forward(adj.ghosted(u_int).contiguous(), out)
+        r = adj.interior(out)[..., 0] - rho_tgt
+        return 0.5 * float((r * r).sum())
+
+    h = 1e-6
+    gen = torch.Generator(device="cpu").manual_seed(20261203)
+    rng = np.random.default_rng(20261203)
+    xg = np.arange(n) / n
+    X, Y = np.meshgrid(xg, xg, indexing="xy")
+
+    def smooth_field():
+        f = np.zeros((n, n))
+        for _ in range(6):
+            kx, ky = rng.integers(-4, 5, size=2)
+            f += rng.normal() * np.sin(2 * np.pi * (kx * X + ky * Y) + rng.uniform(0, 2 * np.pi))
+        return torch.from_numpy(f).cuda()
+
+    fd = {"smooth": [], "noise": []}
+    for kind in ("smooth", "noise"):
+        for _ in range(16):
+            v = smooth_field() if kind == "smooth" else torch.randn((n, n), generator=gen,
+                                                                     dtype=torch.float64).cuda()
+            up, um = u0_int.clone(), u0_int.clone()
+            up[..., 0] += h * v
+            um[..., 0] -= h * v
+            d = (misfit(up) - misfit(um)) / (2 * h)
+            g = float((grad * v).sum())
+            fd[kind].append(abs(d - g) / max(abs(d), abs(g)))
+    v = adj.ghosted(torch.randn((n, n, 4), generator=gen, dtype=torch.float64).cuda()).contiguous()
+    w = adj.ghosted(torch.randn((n, n, 4), generator=gen, dtype=torch.float64).cuda()).contiguous()
+    uT2, Mv, MTw, uT = adj.empty(), adj.empty(), adj.empty(), adj.empty()
+    adj.tlm(R["u0"], v, uT2, Mv)
+    adj.forward(R["u0"], uT)
+    adj.backward(w, MTw)
+    lhs = float((adj.interior(Mv) * adj.interior(w)).sum())
+    rhs_ = float((adj.interior(v) * adj.interior(MTw)).sum())
+    dot_err = abs(lhs - rhs_) / max(abs(lhs), abs(rhs_))
+    grad_ms = R["t_fs"] + R["t_bs"]
+    SA = results["store_all"]
+    ns = inp.config.rk_nstages
+    launches_fs = nsteps * ns * 2
+    launches_bs = R["info"]["recomputed_steps"] * ns * 2 + nsteps * (ns + 1)
+    out = {
+        "metric": METRIC, "value": grad_ms / t_f, "unit": "x (gradient time / forward solve time)",
+        "n_gpus": 1, "steps": K, "warmup": 2, "ms_per_step": grad_ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": (f"adjoint: d/d rho0 of 0.5||rho(T)-rho_target||^2, Euler2D {n}x{n} periodic "
+                                "[0,10)^2, target from the b=5 vortex, guess b=4 shifted by U[-0.5,0.5]^2, "
+                                "comp-WENO5(JS)+Roe, RK4, 400 steps, sqrt checkpointing"),
+                   "cells": n * n, "dt": case.dt, "nsteps": nsteps,
+                   "checkpoints": R["info"]["segments"], "segment_len": R["info"]["segment_len"],
+                   "l2": "256 MB buffer written between timed gradients"},
+        "adjoint": {
+            "forward_solve_ms": t_f,
+            "sqrt": {"forward_sweep_ms": R["t_fs"], "backward_sweep_ms": R["t_bs"], "gradient_ms": grad_ms,
+                     "gradient_over_forward": grad_ms / t_f, "backward_over_forward": R["t_bs"] / t_f,
+                     "recomputed_steps": R["info"]["recomputed_steps"], "device_bytes": R["info"]["bytes"],
+                     "vjp_seg": R["vjp_seg"]},
+            "store_all": {"forward_sweep_ms": SA["t_fs"], "backward_sweep_ms": SA["t_bs"],
+                          "gradient_ms": SA["t_fs"] + SA["t_bs"],
+                          "gradient_over_forward": (SA["t_fs"] + SA["t_bs"]) / t_f,
+                          "backward_over_forward": SA["t_bs"] / t_f, "device_bytes": SA["info"]["bytes"]},
+            "fd_check": {kind: {"directions": 16, "h": h, "max_rel_err": max(e), "median_rel_err":
+                                statistics.median(e)} for kind, e in fd.items()},
+            "fd_directions": ("smooth: 6 random Fourier modes |k| <= 4 per component of the initial density; "
+                              "noise: N(0,1) in every cell; central differences of the misfit through the "
+                              "fused forward solve"),
+            "dot_product_rel_err": dot_err,
+            "forward_launch_seg_block": fwd_shape,
+        },
+        "gpu_launches": K * (launches_fs + launches_bs), "clocks": R["clocks"],
+    }
+    return out
+
+
 def cpu_baseline(case, budget_s: float = 15.0, threads: int = 0):
     """The oracle (the reference algorithm restated in C) on the host cores,
     timed on whole steps of the same workload until budget_s has elapsed."""
@@ -450,7 +616,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "ensemble"])
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "ensemble", "adjoint"])
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -458,10 +624,11 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
-    if args.workload == "ensemble":
+    if args.workload in ("ensemble", "adjoint"):
         from hypar_gb300 import build as B
         B.build()
-        out = run_ensemble(args, ws, rank, local) if args.impl == "ours" else None
+        fn = run_ensemble if args.workload == "ensemble" else run_adjoint
+        out = fn(args, ws, rank, local) if args.impl == "ours" else None
         if out is not None and rank == 0:
             print(json.dumps(out))
         return

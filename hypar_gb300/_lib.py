@@ -33,6 +33,9 @@ EXPORTS = [
     "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
     "gb_ensemble_set_state", "gb_ensemble_get_state", "gb_ensemble_step", "gb_ensemble_time",
     "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune", "gb_rhs_explicit_noalloc",
+    "gb_adjoint_create", "gb_adjoint_destroy", "gb_adjoint_set_stream", "gb_adjoint_sync", "gb_adjoint_set_launch",
+    "gb_adjoint_get_launch", "gb_adjoint_info", "gb_adjoint_rhs_vjp", "gb_adjoint_rhs_jvp", "gb_adjoint_forward",
+    "gb_adjoint_backward", "gb_adjoint_tlm",
 ]
 
 
@@ -131,6 +134,21 @@ def lib():
     L.gb_ensemble_autotune.argtypes = [VP, ctypes.c_int]
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     L.gb_rhs_explicit_noalloc.argtypes = [ctypes.POINTER(GbConfig), VP, VP, VP, VP]
+    L.gb_adjoint_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(VP)]
+    L.gb_adjoint_destroy.argtypes = [VP]
+    L.gb_adjoint_destroy.restype = None
+    L.gb_adjoint_set_stream.argtypes = [VP, VP]
+    L.gb_adjoint_sync.argtypes = [VP]
+    L.gb_adjoint_set_launch.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.gb_adjoint_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.gb_adjoint_info.argtypes = [VP, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    L.gb_adjoint_rhs_vjp.argtypes = [VP, VP, VP, VP]
+    L.gb_adjoint_rhs_jvp.argtypes = [VP, VP, VP, VP, VP]
+    L.gb_adjoint_forward.argtypes = [VP, VP, VP]
+    L.gb_adjoint_backward.argtypes = [VP, VP, VP]
+    L.gb_adjoint_tlm.argtypes = [VP, VP, VP, VP, VP]
     _lib = L
     return L
 

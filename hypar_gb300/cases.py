@@ -290,3 +290,21 @@ def write_ensemble(members, directory: str) -> str:
         with open(os.path.join(directory, f"initial_{idx}.inp"), "wb") as f:
             f.write(c.initial_bytes())
     return directory
+
+
+def adjoint_problem(n: int = 256, n_iter: int = 400, seed: int = 20261203, scheme: str = "44",
+                    cfl: float = 0.5):
+    """Initial-condition inversion for 2D Euler on [0,10)^2, periodic, component-wise
+    WENO5 + Roe: the target is the density after n_iter steps from the b=5 vortex
+    centred at (5, 5); the initial guess is a b=4 vortex whose centre is shifted by
+    U[-0.5, 0.5]^2 (seeded).  One dt (CFL 0.5 of the more restrictive state) serves
+    both runs.  Returns (case, u_true): the deck of the initial guess and the
+    interior state whose run defines the target."""
+    rng = np.random.default_rng(seed)
+    sx, sy = (float(v) for v in rng.uniform(-0.5, 0.5, size=2))
+    _, u_true = vortex_state(n, 5.0, 5.0, 5.0)
+    case = vortex(n, n_iter=n_iter, dt=1.0, b=4.0, xc=5.0 + sx, yc=5.0 + sy, interp="components",
+                  upwinding="roe", scheme=scheme)
+    h = [10.0 / n, 10.0 / n]
+    case.dt = min(cfl_dt(u_true, 4, h, cfl), cfl_dt(case.u, 4, h, cfl))
+    return case, u_true

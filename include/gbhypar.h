@@ -207,6 +207,49 @@ int gb_RHSFunctionExplicit(double *rhs, double *u, void *s, void *m, double t);
  * Runge-Kutta step of the resident solution. */
 int gb_TimeRK(void *ts);
 
+/* ---- discrete adjoint and tangent-linear model ----
+ * No counterpart in the reference (which has no derivative code): derivatives
+ * of this library's own discrete operator -- the right-hand side of Euler2D
+ * with component-wise WENO5 (Jiang-Shu weights, the derivative of the
+ * nonlinear weights included) and Roe upwinding (through the Roe average, the
+ * eigen-structure and Harten's entropy fix), and of n explicit Runge-Kutta
+ * steps.  Every boundary face must be one whole-face periodic or extrapolate
+ * zone.  Arrays are DEVICE arrays in HyPar's ghosted layout; only interior
+ * entries are read or written (ghost entries of outputs are left as they are,
+ * except where a call says it clears them).
+ *
+ * gb_adjoint_create: nsteps steps of cfg->dt; ncheck checkpoints (<= 0:
+ * ceil(sqrt(nsteps)); 1 keeps every state of the whole run).  The run is cut
+ * into ncheck segments: the forward sweep stores u at the start of each and
+ * every stage state of the last; the backward sweep recomputes each earlier
+ * segment once from its checkpoint with the fused forward kernels, keeping its
+ * stage states, then reverses it step by step. */
+typedef struct gb_adjoint gb_adjoint;
+int gb_adjoint_create(const gb_config *cfg, const double *dxinv, int nsteps, int ncheck, int device,
+                      gb_adjoint **out);
+void gb_adjoint_destroy(gb_adjoint *a);
+int gb_adjoint_set_stream(gb_adjoint *a, void *stream);
+int gb_adjoint_sync(gb_adjoint *a);
+/* Launch shape: which = 0, 1 the fused forward kernels along x, y (seg,
+ * block); 2, 3 the adjoint kernel's segment length along x, y. */
+int gb_adjoint_set_launch(gb_adjoint *a, int which, int seg, int block);
+int gb_adjoint_get_launch(const gb_adjoint *a, int which, int *seg, int *block);
+/* Segment length, number of segments, steps recomputed by the last backward
+ * sweep, device bytes held. */
+int gb_adjoint_info(const gb_adjoint *a, int *seglen, int *nseg, long long *recomputed, long long *bytes);
+/* ubar = (dR/du)^T kbar for the right-hand side R (ubar cleared first). */
+int gb_adjoint_rhs_vjp(gb_adjoint *a, const double *u, const double *kbar, double *ubar);
+/* k = R(u), dk = (dR/du) du, by an independent dual-number kernel written in
+ * the reference's dense-matrix form of the Roe flux. */
+int gb_adjoint_rhs_jvp(gb_adjoint *a, const double *u, const double *du, double *k, double *dk);
+/* Forward sweep: uT = nsteps steps from u0, storing the checkpoints. */
+int gb_adjoint_forward(gb_adjoint *a, const double *u0, double *uT);
+/* Backward sweep of the last forward sweep: ubar0 = (duT/du0)^T ubarT. */
+int gb_adjoint_backward(gb_adjoint *a, const double *ubarT, double *ubar0);
+/* Tangent-linear model: uT and duT = (duT/du0) du0 through nsteps steps of
+ * the dual-number right-hand side. */
+int gb_adjoint_tlm(gb_adjoint *a, const double *u0, const double *du0, double *uT, double *duT);
+
 /* ---- right-hand side without device allocation ----
  * No counterpart in the reference.  For callers that must not allocate device
  * memory (code running inside a memory pool or arena it does not own, hosts
