@@ -484,11 +484,13 @@ def run_adjoint(args, ws, rank, local):
             f += rng.normal() * np.sin(2 * np.pi * (kx * X + ky * Y) + rng.uniform(0, 2 * np.pi))
         return torch.from_numpy(f).cuda()
 
-    fd = {"smooth": [], "noise": []}
-    for kind in ("smooth", "noise"):
+    fd = {"smooth": [], "smooth_unit": [], "noise": [], "noise_unit": []}
+    for kind in fd:
         for _ in range(16):
-            v = smooth_field() if kind == "smooth" else torch.randn((n, n), generator=gen,
-                                                                     dtype=torch.float64).cuda()
+            v = smooth_field() if kind.startswith("smooth") else torch.randn((n, n), generator=gen,
+                                                                                dtype=torch.float64).cuda()
+            if kind.endswith("unit"):
+                v /= float(v.norm())
             up, um = u0_int.clone(), u0_int.clone()
             up[..., 0] += h * v
             um[..., 0] -= h * v
@@ -531,9 +533,11 @@ def run_adjoint(args, ws, rank, local):
                           "backward_over_forward": SA["t_bs"] / t_f, "device_bytes": SA["info"]["bytes"]},
             "fd_check": {kind: {"directions": 16, "h": h, "max_rel_err": max(e), "median_rel_err":
                                 statistics.median(e)} for kind, e in fd.items()},
-            "fd_directions": ("smooth: 6 random Fourier modes |k| <= 4 per component of the initial density; "
-                              "noise: N(0,1) in every cell; central differences of the misfit through the "
-                              "fused forward solve"),
+            "fd_directions": ("smooth: 6 random Fourier modes |k| <= 4 of the initial density (amplitude "
+                              "O(1) per cell); noise: N(0,1) in every cell; *_unit: the same scaled to unit "
+                              "2-norm (a per-cell step near 1e-6/256, where rounding in the misfit dominates "
+                              "the difference); central differences of the misfit through the fused forward "
+                              "solve"),
             "dot_product_rel_err": dot_err,
             "forward_launch_seg_block": fwd_shape,
         },

@@ -705,8 +705,16 @@ struct gb_adjoint {
   int touched[4] = {0, 0, 0, 0};  // stage t reads its own stage array (else u_n)
   double* block = nullptr;        // one allocation carved into the arrays below
   std::vector<double*> ck;        // checkpoint of u at the start of every segment
-  std::vector<double*> su;        // u at steps 1..seglen of the segment in hand
-  std::vector<double*> sP;        // stage states of every step of that segment, [i*4 + t]
+  // Two segment buffers: u at steps 1..seglen of a segment (su) and the stage
+  // states of each of its steps (sP, [i*4 + t]).  The backward sweep reverses
+  // one segment from one buffer while the next earlier segment is recomputed
+  // into the other on a second stream.
+  std::vector<double*> su[2];
+  std::vector<double*> sP[2];
+  int nbuf = 1;
+  cudaStream_t aux = nullptr;     // recomputation stream
+  cudaEvent_t ev_start = nullptr;
+  std::vector<cudaEvent_t> ev_rec, ev_back;
   double* acc = nullptr;          // Runge-Kutta accumulator of the fused step
   double* H = nullptr;            // x-direction hyperbolic term of the fused step
   double* Ub[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -768,7 +776,7 @@ static int adj_jvp(gb_adjoint* a, const double* U, const double* dU, double* K, 
 
 // One fused Runge-Kutta step uin -> uout (distinct arrays) keeping the stage
 // states in P[1..ns-1] (the same launches as the solver's step).
-static int adj_step(gb_adjoint* a, const double* uin, double* uout, double* const* P) {
+static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double* uout, double* const* P) {
   const gb_config& c = a->cfg;
   const int ns = c.rk_nstages;
   const double dt = c.dt;
@@ -799,7 +807,7 @@ static int adj_step(gb_adjoint* a, const double* uin, double* uout, double* cons
       e.first = (d == 0);
       e.last = (d == 1);
       AK(launch_hyp_euler2d(d, c.interp, c.upwind, U, a->H, a->d_dxinv + a->dx_off[d], a->G, a->pp, e, a->hl[d],
-                            a->stream));
+                            strm));
     }
     for (int t = st + 1; t < ns; t++)
       if (ep.ca[t] != 0.0) touched[t] = 1;
@@ -836,8 +844,11 @@ static int adj_back_step(gb_adjoint* a, const double* const* U) {
   return GB_OK;
 }
 
-static double* ustate(gb_adjoint* a, int j, int i) { return i == 0 ? a->ck[j] : a->su[i]; }
-static double* const* stages(gb_adjoint* a, int i) { return &a->sP[(size_t)i * 4]; }
+// Buffer of segment j: the last segment (kept by the forward sweep) uses 0,
+// earlier ones alternate.
+static int segbuf(const gb_adjoint* a, int j) { return (a->nseg - 1 - j) & (a->nbuf - 1); }
+static double* ustate(gb_adjoint* a, int j, int i) { return i == 0 ? a->ck[j] : a->su[segbuf(a, j)][i]; }
+static double* const* stages(gb_adjoint* a, int b, int i) { return &a->sP[b][(size_t)i * 4]; }
 
 extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int nsteps, int ncheck, int device,
                                  gb_adjoint** out) {
@@ -881,9 +892,10 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->nseg = (nsteps + a->seglen - 1) / a->seglen;
   a->lastlen = nsteps - (a->nseg - 1) * a->seglen;
   const int ns = cfg->rk_nstages;
-  // arrays: checkpoints, seglen+1 segment states, seglen*(ns-1) stage states,
-  // acc, ns stage adjoints, ubar, hyperbolic accumulator
-  size_t narr = (size_t)a->nseg + (a->seglen + 1) + (size_t)a->seglen * (ns - 1) + 1 + 4 + 1 + 1;
+  // arrays: checkpoints, per segment buffer seglen+1 states and seglen*(ns-1)
+  // stage states, acc, hyperbolic accumulator, 4 stage adjoints, ubar
+  a->nbuf = a->nseg > 1 ? 2 : 1;
+  size_t narr = (size_t)a->nseg + (size_t)a->nbuf * ((a->seglen + 1) + (size_t)a->seglen * (ns - 1)) + 1 + 1 + 4 + 1;
   a->bytes = narr * a->nvals * sizeof(double);
   if (device >= 0) {
     cudaError_t e = cudaSetDevice(device);
@@ -895,21 +907,30 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   if (e == cudaSuccess) e = cudaMalloc((void**)&a->d_dxinv, ndx * sizeof(double));
   if (e == cudaSuccess) e = cudaMemcpy(a->d_dxinv, dxinv, ndx * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->aux, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming);
+  a->ev_rec.assign(a->nseg, nullptr);
+  a->ev_back.assign(a->nseg, nullptr);
+  for (int j = 0; j < a->nseg && e == cudaSuccess; j++) {
+    e = cudaEventCreateWithFlags(&a->ev_rec[j], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&a->ev_back[j], cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     gbh_set_error("gb_adjoint_create: %s", cudaGetErrorString(e));
-    cudaFree(a->block);
-    cudaFree(a->d_dxinv);
-    delete a;
+    a->own_stream = a->stream != nullptr;
+    gb_adjoint_destroy(a);
     return e == cudaErrorMemoryAllocation ? GB_ERR_NOMEM : GB_ERR_CUDA;
   }
   a->own_stream = true;
   double* p = a->block;
   auto take = [&]() { double* r = p; p += a->nvals; return r; };
   for (int j = 0; j < a->nseg; j++) a->ck.push_back(take());
-  for (int i = 0; i <= a->seglen; i++) a->su.push_back(take());
-  a->sP.assign((size_t)a->seglen * 4, nullptr);
-  for (int i = 0; i < a->seglen; i++)
-    for (int t = 1; t < ns; t++) a->sP[(size_t)i * 4 + t] = take();
+  for (int b = 0; b < a->nbuf; b++) {
+    for (int i = 0; i <= a->seglen; i++) a->su[b].push_back(take());
+    a->sP[b].assign((size_t)a->seglen * 4, nullptr);
+    for (int i = 0; i < a->seglen; i++)
+      for (int t = 1; t < ns; t++) a->sP[b][(size_t)i * 4 + t] = take();
+  }
   a->acc = take();
   a->H = take();
   for (int s = 0; s < 4; s++) a->Ub[s] = take();
@@ -925,6 +946,13 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
 extern "C" void gb_adjoint_destroy(gb_adjoint* a) {
   if (!a) return;
   if (a->stream) cudaStreamSynchronize(a->stream);
+  if (a->aux) cudaStreamSynchronize(a->aux);
+  for (cudaEvent_t ev : a->ev_rec)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : a->ev_back)
+    if (ev) cudaEventDestroy(ev);
+  if (a->ev_start) cudaEventDestroy(a->ev_start);
+  if (a->aux) cudaStreamDestroy(a->aux);
   cudaFree(a->block);
   cudaFree(a->tblock);
   cudaFree(a->d_dxinv);
@@ -1011,6 +1039,7 @@ extern "C" int gb_adjoint_forward(gb_adjoint* a, const double* u0, double* uT) {
   const size_t bytes = a->nvals * sizeof(double);
   AK(cudaMemcpyAsync(a->ck[0], u0, bytes, cudaMemcpyDeviceToDevice, a->stream));
   const int L = a->seglen;
+  const int bl = segbuf(a, a->nseg - 1), bt = a->nbuf - 1 - bl;  // last segment's buffer, the other
   for (int j = 0; j < a->nseg; j++) {
     const bool last = (j == a->nseg - 1);
     const int len = last ? a->lastlen : L;
@@ -1021,23 +1050,27 @@ extern "C" int gb_adjoint_forward(gb_adjoint* a, const double* u0, double* uT) {
       if (last) {
         // the last segment keeps every state for the backward sweep
         uin = ustate(a, j, i);
-        uout = a->su[i + 1];
-        P = stages(a, i);
+        uout = a->su[bl][i + 1];
+        P = stages(a, bl, i);
       } else {
-        uin = i == 0 ? a->ck[j] : a->su[1 + (i & 1)];
-        uout = (i + 1 == len) ? a->ck[j + 1] : a->su[1 + ((i + 1) & 1)];
-        P = stages(a, 0);
+        uin = i == 0 ? a->ck[j] : a->su[bt][1 + (i & 1)];
+        uout = (i + 1 == len) ? a->ck[j + 1] : a->su[bt][1 + ((i + 1) & 1)];
+        P = stages(a, bt, 0);
       }
-      int rc = adj_step(a, uin, uout, P);
+      int rc = adj_step(a, a->stream, uin, uout, P);
       if (rc) return rc;
     }
   }
-  AK(cudaMemcpyAsync(uT, a->su[a->lastlen], bytes, cudaMemcpyDeviceToDevice, a->stream));
+  AK(cudaMemcpyAsync(uT, a->su[bl][a->lastlen], bytes, cudaMemcpyDeviceToDevice, a->stream));
   a->forward_done = true;
   a->recomputed = 0;
   return GB_OK;
 }
 
+// Backward sweep.  Segment j is reversed on the main stream from its buffer
+// while segment j-1 is recomputed from its checkpoint into the other buffer
+// on the second stream; reversing j-1 waits for that recomputation, and
+// recomputing j-2 waits until the reversal of j has released the buffer.
 extern "C" int gb_adjoint_backward(gb_adjoint* a, const double* ubarT, double* ubar0) {
   if (!a || !ubarT || !ubar0) { gbh_set_error("gb_adjoint_backward: null argument"); return GB_ERR_ARG; }
   if (!a->forward_done) { gbh_set_error("gb_adjoint_backward: no forward sweep to reverse"); return GB_ERR_ARG; }
@@ -1045,22 +1078,29 @@ extern "C" int gb_adjoint_backward(gb_adjoint* a, const double* ubarT, double* u
   const int ns = a->cfg.rk_nstages;
   AK(cudaMemcpyAsync(a->ubar, ubarT, bytes, cudaMemcpyDeviceToDevice, a->stream));
   for (int s = 0; s < 4; s++) AK(cudaMemsetAsync(a->Ub[s], 0, bytes, a->stream));
+  AK(cudaEventRecord(a->ev_start, a->stream));
+  AK(cudaStreamWaitEvent(a->aux, a->ev_start, 0));
   for (int j = a->nseg - 1; j >= 0; j--) {
-    const bool last = (j == a->nseg - 1);
-    const int len = last ? a->lastlen : a->seglen;
-    if (!last) {
-      for (int i = 0; i < len; i++) {
-        int rc = adj_step(a, ustate(a, j, i), a->su[i + 1], stages(a, i));
+    if (j >= 1) {
+      const int jr = j - 1, b = segbuf(a, jr);
+      if (jr + 2 <= a->nseg - 1) AK(cudaStreamWaitEvent(a->aux, a->ev_back[jr + 2], 0));
+      for (int i = 0; i < a->seglen; i++) {
+        int rc = adj_step(a, a->aux, ustate(a, jr, i), a->su[b][i + 1], stages(a, b, i));
         if (rc) return rc;
       }
-      a->recomputed += len;
+      AK(cudaEventRecord(a->ev_rec[jr], a->aux));
+      a->recomputed += a->seglen;
     }
+    if (j < a->nseg - 1) AK(cudaStreamWaitEvent(a->stream, a->ev_rec[j], 0));
+    const int len = (j == a->nseg - 1) ? a->lastlen : a->seglen;
+    const int b = segbuf(a, j);
     for (int i = len - 1; i >= 0; i--) {
       const double* U[4];
-      for (int t = 0; t < ns; t++) U[t] = (t == 0 || !a->touched[t]) ? ustate(a, j, i) : a->sP[(size_t)i * 4 + t];
+      for (int t = 0; t < ns; t++) U[t] = (t == 0 || !a->touched[t]) ? ustate(a, j, i) : a->sP[b][(size_t)i * 4 + t];
       int rc = adj_back_step(a, U);
       if (rc) return rc;
     }
+    AK(cudaEventRecord(a->ev_back[j], a->stream));
   }
   AK(cudaMemcpyAsync(ubar0, a->ubar, bytes, cudaMemcpyDeviceToDevice, a->stream));
   return GB_OK;
