@@ -36,12 +36,15 @@ METRIC = "FP64 cell-updates/s & HBM%; ensemble vs serial speedup; adjoint/forwar
 UNIT = "cell-component updates/s"
 
 # FP64 floating-point operations per interface per direction of the fused
-# kernels (FMA = 2), from ncu instruction counts of one launch
-# (smsp__sass_thread_inst_executed_op_{dfma,dmul,dadd}_pred_on x elapsed cycles,
-# profiles/hyp_dir_kernel_euler2d_char_roe_vortex2048_ncu_full.md); per cell per
-# step this is x (ndims * nstages).  FP64 instructions per interface in brackets.
-FP64_FLOPS_PER_INTERFACE = {"vortex": 1640.2}
-FP64_INSTR_PER_INTERFACE = {"vortex": 1024.3}
+# kernels (FMA = 2), from one ncu capture of the x and y launches (FP64-pipe
+# instructions x elapsed cycles, DFMA share from the dfma counter; mean of the
+# two directions, profiles/hyp_dir_kernel_euler2d_char_roe_vortex2048_ncu_full.md);
+# per cell per step this is x (ndims * nstages).  FP64 instructions likewise.
+FP64_FLOPS_PER_INTERFACE = {"vortex": 1607.3}
+FP64_INSTR_PER_INTERFACE = {"vortex": 1005.6}
+# DRAM bytes (read + write) per cell of one launch, same capture (2048^2, traffic
+# proportional to cells at these sizes): x launch / y launch with the RK update.
+DRAM_BYTES_PER_CELL = {"vortex": {"hyp_x": 56.13, "hyp_y": 149.99}}
 
 
 def workload(name: str, size: int = 0):
@@ -189,6 +192,7 @@ def run_ours(args, case, desc, ws, rank, local):
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("timed")  # ncu --nvtx --nvtx-include timed/ selects these launches
         t0 = time.perf_counter()
         for k in range(args.steps):
             flush.fill_(float(k))
@@ -197,6 +201,7 @@ def run_ours(args, case, desc, ws, rank, local):
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        torch.cuda.nvtx.range_pop()
     if dist:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -248,8 +253,11 @@ def run_ours(args, case, desc, ws, rank, local):
     else:
         bytes_per_launch = cells * 8.0 * nv * 2  # read U, write the partial hyperbolic term
     achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
+    traffic = DRAM_BYTES_PER_CELL.get(args.workload, {}).get(cls)
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved_gbs / hbm_peak, "traffic": None, "kernel": cls,
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic * cells if traffic else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of a 2048^2 "
+                                  "capture, scaled by cells" if traffic else None, "kernel": cls,
                 "avg_launch_ms": avg_launch_s * 1e3, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": bytes_per_launch}
     step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
