@@ -17,6 +17,7 @@ GB_ERR = {1: "GB_ERR_ARG", 2: "GB_ERR_CUDA", 3: "GB_ERR_INPUT", 4: "GB_ERR_UNSUP
 MODEL = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
 UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2}
 INTERP = {"components": 0, "characteristic": 1}
+WENO_WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
 
@@ -48,7 +49,7 @@ class GbConfig(ctypes.Structure):
         ("nzones", ctypes.c_int), ("zones", (ctypes.c_int * 9) * 12),
         ("rk_nstages", ctypes.c_int), ("rk_A", ctypes.c_double * 16), ("rk_b", ctypes.c_double * 4),
         ("rk_c", ctypes.c_double * 4), ("dt", ctypes.c_double), ("n_iter", ctypes.c_int),
-        ("file_op_iter", ctypes.c_int),
+        ("file_op_iter", ctypes.c_int), ("weno_weights", ctypes.c_int),
     ]
 
 

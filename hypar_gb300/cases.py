@@ -47,6 +47,7 @@ class Case:
     Pr: float = 0.72
     Minf: float = 1.0
     file_op_iter: Optional[int] = None
+    weights: str = "js"             # WENO5 weights: "js" | "mapped" | "borges" | "yc" | "none" (no_limiting)
 
     @property
     def ndims(self) -> int:
@@ -95,8 +96,10 @@ class Case:
         return "\n".join(lines) + "\n"
 
     def weno_inp(self) -> str:
-        return ("begin\n  mapped 0\n  borges 0\n  yc 0\n  no_limiting 0\n"
-                f"  epsilon {float(self.eps)!r}\n  p 2.0\nend\n")
+        flags = {k: int(self.weights == k) for k in ("mapped", "borges", "yc")}
+        flags["no_limiting"] = int(self.weights == "none")
+        return ("begin\n" + "".join(f"  {k} {v}\n" for k, v in flags.items())
+                + f"  epsilon {float(self.eps)!r}\n  p 2.0\nend\n")
 
     def boundary_inp(self) -> str:
         nd = self.ndims

@@ -856,8 +856,10 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   *out = nullptr;
   int rc = gbh_validate(cfg);
   if (rc) return rc;
-  if (cfg->model != GB_MODEL_EULER2D || cfg->interp != GB_INTERP_COMPONENTS || cfg->upwind != GB_UPWIND_ROE) {
-    gbh_set_error("gb_adjoint_create: the adjoint covers Euler2D with component-wise WENO5 and Roe upwinding");
+  if (cfg->model != GB_MODEL_EULER2D || cfg->interp != GB_INTERP_COMPONENTS || cfg->upwind != GB_UPWIND_ROE ||
+      cfg->weno_weights != GB_WENO_JS) {
+    gbh_set_error("gb_adjoint_create: the adjoint covers Euler2D with component-wise Jiang-Shu WENO5 and Roe "
+                  "upwinding");
     return GB_ERR_UNSUPPORTED;
   }
   DevGeom G;
@@ -875,6 +877,7 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->pp.gm1 = cfg->gamma - 1.0;
   a->pp.inv_gm1 = 1.0 / (cfg->gamma - 1.0);
   a->pp.eps = cfg->weno_eps;
+  a->pp.wtype = WENO_W_JS;
   for (int d = 0; d < 2; d++) {
     a->hl[d].seg = 32;
     a->hl[d].block = 128;

@@ -17,6 +17,12 @@ cudaError_t launch_hyp_euler2d(int, int, int, const double*, double*, const doub
                                const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d(int, int, int, const double*, double*, const double*, const DevGeom&,
                             const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_euler1d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                                 const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                                 const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                              const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_unfused_euler1d(int, int, int, double*, const double*, const double*, const double*,
                                    const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
 cudaError_t launch_unfused_euler2d(int, int, int, double*, const double*, const double*, const double*,
@@ -130,6 +136,13 @@ static int prof_drain(gb_solver* s) {
 static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const StageEpi& ep) {
   const gb_config& c = s->cfg;
   const double* dx = s->d_dxinv + s->dx_off[dir];
+  if (s->pp.wtype != WENO_W_JS) {
+    if (c.model == GB_MODEL_EULER1D)
+      return launch_hyp_euler1d_w(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+    if (c.model == GB_MODEL_EULER2D)
+      return launch_hyp_euler2d_w(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+    return launch_hyp_ns3d_w(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+  }
   if (c.model == GB_MODEL_EULER1D)
     return launch_hyp_euler1d(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
   if (c.model == GB_MODEL_EULER2D)
@@ -200,6 +213,7 @@ int gbh_validate(const gb_config* c) {
   if (c->rk_nstages < 1 || c->rk_nstages > 4) { gbh_set_error("rk_nstages must be 1..4"); return GB_ERR_ARG; }
   if (!(c->gamma > 1.0)) { gbh_set_error("gamma must exceed 1"); return GB_ERR_ARG; }
   if (!(c->weno_eps > 0.0)) { gbh_set_error("weno_eps must be positive"); return GB_ERR_ARG; }
+  if (c->weno_weights < GB_WENO_JS || c->weno_weights > GB_WENO_NONE) { gbh_set_error("bad weno_weights"); return GB_ERR_ARG; }
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
@@ -272,6 +286,7 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   s->pp.gm1 = c.gamma - 1.0;
   s->pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   s->pp.eps = c.weno_eps;
+  s->pp.wtype = c.weno_weights;
   s->viscous = (c.model == GB_MODEL_NS3D) && (c.Re > 0);
   double Re_eff = c.Re / c.Minf;  // NavierStokes3DInitialize.c:368
   s->vp.gamma = c.gamma;

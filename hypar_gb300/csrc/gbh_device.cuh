@@ -22,7 +22,12 @@ template <> struct ModelTraits<MODEL_NS3D>    { static constexpr int NV = 5, ND 
 
 struct PhysParams {
   double gamma, gm1, inv_gm1, eps;
+  int wtype;  // WENO weights: WENO_W_* (the kernels take Jiang-Shu unless instantiated for the others)
 };
+
+// WENO5 nonlinear weight formulations (weno.inp flags, WENOFifthOrderCalculateWeights.c:40-64;
+// no_limiting keeps the optimal weights, InitializeSolvers.c:219 / HyperbolicFunction.c:62).
+enum { WENO_W_JS = 0, WENO_W_MAPPED = 1, WENO_W_BORGES = 2, WENO_W_YC = 3, WENO_W_NONE = 4 };
 
 // ---------------------------------------------------------------------------
 // Reciprocal and square root.
@@ -320,6 +325,89 @@ __device__ __forceinline__ void weno5_pair(const double* w, const double* v, dou
   double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
   outL = nL * nr_rcp(DL);
   outR = nR * nr_rcp(DR);
+}
+
+// Left/right WENO5 pair with the other weight formulations (runtime `wtype`).
+// B_k = 4 (beta_k + eps) as in weno5_pair; per side, with optimal weights
+// c = (0.1, 0.6, 0.3) and candidates p_k:
+//   Borges (WENO-Z, _WENOWeights_v_Z_, include/interpolation.h:417-437):
+//     a_k = c_k (1 + (tau/(beta_k+eps))^2), tau = |beta_1 - beta_3|, i.e. 4 tau = |B_1 - B_3|;
+//   Yamaleev-Carpenter (_WENOWeights_v_YC_, :474-494): the same with
+//     tau = (f_{j-2} - 4 f_{j-1} + 6 f_j - 4 f_{j+1} + f_{j+2})^2;
+//   both evaluated as a_k = c_k (B_k^2 + T) prod_{j != k} B_j^2, T = (4 tau)^2, so that one
+//   reciprocal normalises them;
+//   mapped (Henrick et al., _WENOWeights_v_M_, :319-345): JS weights w~ (one reciprocal),
+//     then a_k = w~_k (c_k + c_k^2 - 3 c_k w~_k + w~_k^2) / (c_k^2 + w~_k (1 - 2 c_k)),
+//     normalised as num_k prod_{j != k} den_j (one more reciprocal);
+//   none: the optimal weights.
+// out = sum_k a_k p_k / sum_k a_k.
+__device__ __forceinline__ void weno5_side_alt(int wtype, double B1, double B2, double B3, double tau4,
+                                               double p1, double p2, double p3, double& out) {
+  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  if (wtype == WENO_W_NONE) {
+    out = fma(c1, p1, fma(c2, p2, c3 * p3));
+    return;
+  }
+  const double q1 = B1 * B1, q2 = B2 * B2, q3 = B3 * B3;
+  double a1, a2, a3;
+  if (wtype == WENO_W_MAPPED) {
+    double j1 = c1 * (q2 * q3), j2 = c2 * (q1 * q3), j3 = c3 * (q1 * q2);
+    double r = nr_rcp(j1 + j2 + j3);
+    double w1 = j1 * r, w2 = j2 * r, w3 = j3 * r;
+    double n1 = w1 * fma(w1, w1 - 3.0 * c1, c1 + c1 * c1);
+    double n2 = w2 * fma(w2, w2 - 3.0 * c2, c2 + c2 * c2);
+    double n3 = w3 * fma(w3, w3 - 3.0 * c3, c3 + c3 * c3);
+    double e1 = fma(w1, 1.0 - 2.0 * c1, c1 * c1);
+    double e2 = fma(w2, 1.0 - 2.0 * c2, c2 * c2);
+    double e3 = fma(w3, 1.0 - 2.0 * c3, c3 * c3);
+    a1 = n1 * (e2 * e3);
+    a2 = n2 * (e1 * e3);
+    a3 = n3 * (e1 * e2);
+  } else {
+    // Borges / YC (tau4 = 4 tau); Jiang-Shu would be T = 0
+    const double T = tau4 * tau4;
+    a1 = c1 * ((q1 + T) * (q2 * q3));
+    a2 = c2 * ((q2 + T) * (q1 * q3));
+    a3 = c3 * ((q3 + T) * (q1 * q2));
+  }
+  out = fma(a1, p1, fma(a2, p2, a3 * p3)) * nr_rcp(a1 + a2 + a3);
+}
+
+__device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v, double eps4, int wtype,
+                                               double& outL, double& outR) {
+  const double k13 = 13.0 / 3.0, s6 = 1.0 / 6.0;
+  double d1 = fma(-2.0, w[1], w[0]) + w[2];
+  double d2 = fma(-2.0, w[2], w[1]) + w[3];
+  double d3 = fma(-2.0, w[3], w[2]) + w[4];
+  double d4 = fma(-2.0, w[4], w[3]) + w[5];
+  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
+  double gL2 = w[1] - w[3];
+  double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
+  double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
+  double gR2 = w[4] - w[2];
+  double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
+  double BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
+  double BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
+  double BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
+  double BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
+  double BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
+  double BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
+  double tL = 0.0, tR = 0.0;
+  if (wtype == WENO_W_BORGES) {
+    tL = fabs(BL1 - BL3);
+    tR = fabs(BR1 - BR3);
+  } else if (wtype == WENO_W_YC) {
+    // fourth differences of the left stencil (w0..w4) and of the right one (w5..w1)
+    double eL = d1 - 2.0 * d2 + d3, eR = d4 - 2.0 * d3 + d2;
+    tL = 4.0 * (eL * eL);
+    tR = 4.0 * (eR * eR);
+  }
+  double cL1 = fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2])) * s6;
+  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3])) * s6;
+  double cA = fma(5.0, v[2], fma(2.0, v[3], -v[1])) * s6;
+  double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4])) * s6;
+  weno5_side_alt(wtype, BL1, BL2, BL3, tL, cL1, cA, cB, outL);
+  weno5_side_alt(wtype, BR1, BR2, BR3, tR, cR1, cB, cA, outR);
 }
 
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }

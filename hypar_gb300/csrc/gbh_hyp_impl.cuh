@@ -229,10 +229,19 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
   }
 }
 
+// Jiang-Shu pair (the benchmark path) or, in the kernels instantiated with
+// ALTW, the pair with the weight formulation selected at run time.
+template <bool ALTW>
+__device__ __forceinline__ void wpair(const double* w, const double* v, double eps4, int wtype, double& oL,
+                                      double& oR) {
+  if (ALTW) weno5_pair_alt(w, v, eps4, wtype, oL, oR);
+  else weno5_pair(w, v, eps4, oL, oR);
+}
+
 // One thread's share of a launch: interfaces [sg*seg, min((sg+1)*seg, N)] of
 // the grid line with transverse index `tr` (other dimensions ascending, first
 // fastest), and the flux difference / epilogue of the cells in between.
-template <int M, bool CHAR, int UPW, int DIR>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW = false>
 __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double* __restrict__ H,
                                             const double* __restrict__ dxinv, const DevGeom& G,
                                             const PhysParams& pp, const StageEpi& ep, int seg, long long tr,
@@ -308,14 +317,14 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           sf[p] = wf[p][v];
           su[p] = wu[p][v];
         }
-        weno5_pair(sf, sf, eps4, fL[v], fR[v]);
+        wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
         if (M == MODEL_NS3D && v == NV - 1) {
           double sc[6];
 #pragma unroll
           for (int p = 0; p < 6; p++) sc[p] = wuc[p];
-          weno5_pair(su, sc, eps4, uL[v], uR[v]);
+          wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
         } else {
-          weno5_pair(su, su, eps4, uL[v], uR[v]);
+          wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
         }
       }
       upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);
@@ -345,14 +354,14 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           sf[p] = cf[p][v];
           su[p] = cu[p][v];
         }
-        weno5_pair(sf, sf, eps4, xfL[v], xfR[v]);
+        wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
         if (M == MODEL_NS3D && v < 3) {
           double sc[6];
 #pragma unroll
           for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
-          weno5_pair(su, sc, eps4, xuL[v], xuR[v]);
+          wpair<ALTW>(su, sc, eps4, pp.wtype, xuL[v], xuR[v]);
         } else {
-          weno5_pair(su, su, eps4, xuL[v], xuR[v]);
+          wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
         }
       }
       upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI);
@@ -403,13 +412,13 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
   }
 }
 
-template <int M, bool CHAR, int UPW, int DIR>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW>
 __global__ void __launch_bounds__(128)
 hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
                DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
   long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= ntrans * (long long)nseg) return;
-  hyp_segment<M, CHAR, UPW, DIR>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
+  hyp_segment<M, CHAR, UPW, DIR, ALTW>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
 }
 
 // All members of an ensemble advanced by one launch per direction: a thread
@@ -481,7 +490,7 @@ cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem
 }
 
 // Host launcher for one direction.
-template <int M, bool CHAR, int UPW, int DIR>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW>
 cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                        const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
   long long ntrans = 1;
@@ -493,32 +502,36 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   long long nthr = ntrans * nseg;
   int block = L.block > 0 ? L.block : 128;
   long long grid = (nthr + block - 1) / block;
-  hyp_dir_kernel<M, CHAR, UPW, DIR><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg, nseg, ntrans);
+  hyp_dir_kernel<M, CHAR, UPW, DIR, ALTW><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg, nseg,
+                                                                        ntrans);
   return cudaGetLastError();
 }
 
-template <int M, bool CHAR, int UPW>
+template <int M, bool CHAR, int UPW, bool ALTW>
 cudaError_t launch_dir_any(int dir, const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                            const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
   constexpr int ND = ModelTraits<M>::ND;
-  if (dir == 0) return launch_dir<M, CHAR, UPW, 0>(U, H, dxinv_dir, G, pp, ep, L, s);
-  if (ND > 1 && dir == 1) return launch_dir<M, CHAR, UPW, (ND > 1 ? 1 : 0)>(U, H, dxinv_dir, G, pp, ep, L, s);
-  if (ND > 2 && dir == 2) return launch_dir<M, CHAR, UPW, (ND > 2 ? 2 : 0)>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (dir == 0) return launch_dir<M, CHAR, UPW, 0, ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (ND > 1 && dir == 1)
+    return launch_dir<M, CHAR, UPW, (ND > 1 ? 1 : 0), ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (ND > 2 && dir == 2)
+    return launch_dir<M, CHAR, UPW, (ND > 2 ? 2 : 0), ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
   return cudaErrorInvalidValue;
 }
 
-template <int M>
+// ALTW = false: Jiang-Shu weights (pp.wtype ignored); true: pp.wtype selects them.
+template <int M, bool ALTW = false>
 cudaError_t launch_hyp_model(int dir, int chr, int upw, const double* U, double* H, const double* dxinv_dir,
                              const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
                              cudaStream_t s) {
   if (chr) {
-    if (upw == UPW_ROE) return launch_dir_any<M, true, UPW_ROE>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
-    if (upw == UPW_LLF) return launch_dir_any<M, true, UPW_LLF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
-    return launch_dir_any<M, true, UPW_RF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_ROE) return launch_dir_any<M, true, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_LLF) return launch_dir_any<M, true, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir_any<M, true, UPW_RF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
   } else {
-    if (upw == UPW_ROE) return launch_dir_any<M, false, UPW_ROE>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
-    if (upw == UPW_LLF) return launch_dir_any<M, false, UPW_LLF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
-    return launch_dir_any<M, false, UPW_RF>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_ROE) return launch_dir_any<M, false, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_LLF) return launch_dir_any<M, false, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir_any<M, false, UPW_RF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
   }
 }
 

@@ -418,10 +418,13 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
                {"no_limiting", 'i', &no_limiting}, {"epsilon", 'd', &c.weno_eps}};
   rc = read_kv_file(dir, "weno.inp", wk, 5, 0);
   if (rc) return rc;
-  if (mapped || borges || yc || no_limiting) {
-    gbh_set_error("only Jiang-Shu WENO5 weights are supported (mapped/borges/yc/no_limiting must be 0)");
-    return GB_ERR_UNSUPPORTED;
-  }
+  /* WENOFifthOrderCalculateWeights.c:57-60 (yc, then borges, then mapped);
+   * no_limiting skips the weights altogether (InitializeSolvers.c:219) */
+  c.weno_weights = no_limiting ? GB_WENO_NONE
+                 : yc          ? GB_WENO_YC
+                 : borges      ? GB_WENO_BORGES
+                 : mapped      ? GB_WENO_MAPPED
+                               : GB_WENO_JS;
 
   gb_inputs *res = (gb_inputs *)calloc(1, sizeof(gb_inputs));
   strncpy(res->op_overwrite, si.op_overwrite, sizeof(res->op_overwrite) - 1);

@@ -26,6 +26,12 @@ cudaError_t launch_hyp_euler2d(int, int, int, const double*, double*, const doub
                                const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d(int, int, int, const double*, double*, const double*, const DevGeom&,
                             const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_euler1d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                                 const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                                 const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
+                              const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, cudaStream_t);
 }  // namespace gbh
 
@@ -115,6 +121,7 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
   pp.gm1 = c.gamma - 1.0;
   pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   pp.eps = c.weno_eps;
+  pp.wtype = c.weno_weights;
   HypLaunch hl;
   hl.seg = 32;
   hl.block = 128;
@@ -130,9 +137,17 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
     StageEpi e = ep;
     e.first = (d == 0);
     e.last = (d == c.ndims - 1);
-    if (c.model == GB_MODEL_EULER1D) NA_CK(launch_hyp_euler1d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
-    else if (c.model == GB_MODEL_EULER2D) NA_CK(launch_hyp_euler2d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
-    else NA_CK(launch_hyp_ns3d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+    if (pp.wtype != WENO_W_JS) {
+      if (c.model == GB_MODEL_EULER1D) NA_CK(launch_hyp_euler1d_w(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+      else if (c.model == GB_MODEL_EULER2D) NA_CK(launch_hyp_euler2d_w(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+      else NA_CK(launch_hyp_ns3d_w(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+    } else if (c.model == GB_MODEL_EULER1D) {
+      NA_CK(launch_hyp_euler1d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+    } else if (c.model == GB_MODEL_EULER2D) {
+      NA_CK(launch_hyp_euler2d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+    } else {
+      NA_CK(launch_hyp_ns3d(d, c.interp, c.upwind, u, H, dx, G, pp, e, hl, st));
+    }
     dx += c.dim[d] + 2 * c.ghosts;
   }
   return GB_OK;

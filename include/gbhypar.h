@@ -41,6 +41,9 @@ enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2 };
 enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
 enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2 };
 enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
+/* WENO5 nonlinear weights (weno.inp: yc > borges > mapped > Jiang-Shu, and
+ * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
+enum { GB_WENO_JS = 0, GB_WENO_MAPPED = 1, GB_WENO_BORGES = 2, GB_WENO_YC = 3, GB_WENO_NONE = 4 };
 enum { GB_MEM_HOST = 0, GB_MEM_DEVICE = 1 };
 
 #define GB_MAX_ZONES 12
@@ -63,6 +66,7 @@ typedef struct gb_config {
   double dt;                /* time step */
   int n_iter;               /* number of steps (solver.inp n_iter) */
   int file_op_iter;         /* output interval (solver.inp file_op_iter) */
+  int weno_weights;         /* GB_WENO_*; the batched ensemble and the adjoint take Jiang-Shu only */
 } gb_config;
 
 typedef struct gb_solver gb_solver;

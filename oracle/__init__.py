@@ -33,6 +33,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 MODELS = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
 UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2}
 INTERP = {"components": 0, "characteristic": 1}
+WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2}
 
 _lib = None
@@ -62,6 +63,8 @@ def _bind(path):
                                      ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, ctypes.c_int, ip, dp]
     L.orc_problem_destroy.argtypes = [ctypes.c_void_p]
+    L.orc_set_weights.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.orc_set_weights.restype = None
     L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
     for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs"):
         getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
@@ -228,6 +231,7 @@ class Problem:
                                       _ip(np.ascontiguousarray(self.zones)), _dp(self.dxinv))
         if not self.h:
             raise RuntimeError("orc_problem_create failed")
+        L.orc_set_weights(self.h, WEIGHTS[getattr(case, "weights", "js")])
 
     def __del__(self):
         try:

@@ -78,6 +78,8 @@ orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts
   return p;
 }
 
+void orc_set_weights(orc_problem *p, int weights) { p->weights = weights; }
+
 void orc_problem_destroy(orc_problem *p) {
   if (!p) return;
   free(p->dxinv);
@@ -555,6 +557,73 @@ static inline void weno_js(double m3, double m2, double m1, double p1, double p2
   *w3 = a3 * a_sum_inv;
 }
 
+/* _WENOWeights_v_M_ (include/interpolation.h:319-345): JS weights, then the
+ * mapping of Henrick, Aslam & Powers and a second normalisation. */
+static inline void weno_m(double m3, double m2, double m1, double p1, double p2, double eps,
+                          double *w1, double *w2, double *w3) {
+  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  double a1, a2, a3, a_sum_inv;
+  weno_js(m3, m2, m1, p1, p2, eps, w1, w2, w3);
+  a1 = *w1 * (c1 + c1 * c1 - 3 * c1 * *w1 + *w1 * *w1) / (c1 * c1 + *w1 * (1.0 - 2.0 * c1));
+  a2 = *w2 * (c2 + c2 * c2 - 3 * c2 * *w2 + *w2 * *w2) / (c2 * c2 + *w2 * (1.0 - 2.0 * c2));
+  a3 = *w3 * (c3 + c3 * c3 - 3 * c3 * *w3 + *w3 * *w3) / (c3 * c3 + *w3 * (1.0 - 2.0 * c3));
+  a_sum_inv = 1.0 / (a1 + a2 + a3);
+  *w1 = a1 * a_sum_inv;
+  *w2 = a2 * a_sum_inv;
+  *w3 = a3 * a_sum_inv;
+}
+
+/* Smoothness indicators of _WENOWeights_v_* (include/interpolation.h). */
+static inline void weno_betas(double m3, double m2, double m1, double p1, double p2, double *b1,
+                              double *b2, double *b3) {
+  static const double thirteen_by_twelve = 13.0 / 12.0;
+  static const double one_fourth = 1.0 / 4.0;
+  *b1 = thirteen_by_twelve * (m3 - 2 * m2 + m1) * (m3 - 2 * m2 + m1)
+        + one_fourth * (m3 - 4 * m2 + 3 * m1) * (m3 - 4 * m2 + 3 * m1);
+  *b2 = thirteen_by_twelve * (m2 - 2 * m1 + p1) * (m2 - 2 * m1 + p1)
+        + one_fourth * (m2 - p1) * (m2 - p1);
+  *b3 = thirteen_by_twelve * (m1 - 2 * p1 + p2) * (m1 - 2 * p1 + p2)
+        + one_fourth * (3 * m1 - 4 * p1 + p2) * (3 * m1 - 4 * p1 + p2);
+}
+
+/* _WENOWeights_v_Z_ (tau = |b3-b1|, include/interpolation.h:417-437) and
+ * _WENOWeights_v_YC_ (tau = (m3-4m2+6m1-4p1+p2)^2, :474-494). */
+static inline void weno_tau(double tau, double b1, double b2, double b3, double eps, double *w1,
+                            double *w2, double *w3) {
+  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  double a1, a2, a3, a_sum_inv;
+  a1 = c1 * (1.0 + (tau / (b1 + eps)) * (tau / (b1 + eps)));
+  a2 = c2 * (1.0 + (tau / (b2 + eps)) * (tau / (b2 + eps)));
+  a3 = c3 * (1.0 + (tau / (b3 + eps)) * (tau / (b3 + eps)));
+  a_sum_inv = 1.0 / (a1 + a2 + a3);
+  *w1 = a1 * a_sum_inv;
+  *w2 = a2 * a_sum_inv;
+  *w3 = a3 * a_sum_inv;
+}
+
+/* The weights of one biased stencil for the problem's formulation
+ * (WENOFifthOrderCalculateWeights.c:57-60; no_limiting keeps the optimal
+ * weights of WENOFifthOrderInitializeWeights). */
+static inline void weno_w(int type, double m3, double m2, double m1, double p1, double p2, double eps,
+                          double *w1, double *w2, double *w3) {
+  double b1, b2, b3, tau;
+  switch (type) {
+    case ORC_WENO_MAPPED: weno_m(m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
+    case ORC_WENO_BORGES:
+      weno_betas(m3, m2, m1, p1, p2, &b1, &b2, &b3);
+      tau = fabs(b3 - b1);
+      weno_tau(tau, b1, b2, b3, eps, w1, w2, w3);
+      return;
+    case ORC_WENO_YC:
+      weno_betas(m3, m2, m1, p1, p2, &b1, &b2, &b3);
+      tau = (m3 - 4 * m2 + 6 * m1 - 4 * p1 + p2) * (m3 - 4 * m2 + 6 * m1 - 4 * p1 + p2);
+      weno_tau(tau, b1, b2, b3, eps, w1, w2, w3);
+      return;
+    case ORC_WENO_NONE: *w1 = 0.1; *w2 = 0.6; *w3 = 0.3; return;
+    default: weno_js(m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
+  }
+}
+
 /* Interp1PrimFifthOrderWENO (Interp1PrimFifthOrderWENO.c:143-158), one component. */
 static inline double weno_interp(double w1, double w2, double w3, double fm3, double fm2,
                                  double fm1, double fp1, double fp2) {
@@ -710,13 +779,13 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
           if (p->interp == ORC_INTERP_COMP) {
             for (int v = 0; v < nv; v++) {
               double w1, w2, w3;
-              weno_js(fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
               fL[v] = weno_interp(w1, w2, w3, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v]);
-              weno_js(fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v], p->eps, &w1, &w2, &w3);
               fR[v] = weno_interp(w1, w2, w3, fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v]);
-              weno_js(u[nv * L3 + v], u[nv * L2 + v], u[nv * L1 + v], u[nv * L4 + v], u[nv * L5 + v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, u[nv * L3 + v], u[nv * L2 + v], u[nv * L1 + v], u[nv * L4 + v], u[nv * L5 + v], p->eps, &w1, &w2, &w3);
               uL[v] = weno_interp(w1, w2, w3, uC[nv * L3 + v], uC[nv * L2 + v], uC[nv * L1 + v], uC[nv * L4 + v], uC[nv * L5 + v]);
-              weno_js(u[nv * R3 + v], u[nv * R2 + v], u[nv * R1 + v], u[nv * R4 + v], u[nv * R5 + v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, u[nv * R3 + v], u[nv * R2 + v], u[nv * R1 + v], u[nv * R4 + v], u[nv * R5 + v], p->eps, &w1, &w2, &w3);
               uR[v] = weno_interp(w1, w2, w3, uC[nv * R3 + v], uC[nv * R2 + v], uC[nv * R1 + v], uC[nv * R4 + v], uC[nv * R5 + v]);
             }
           } else {
@@ -740,13 +809,13 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
             double xfl[MAXV], xfr[MAXV], xul[MAXV], xur[MAXV];
             for (int v = 0; v < nv; v++) {
               double w1, w2, w3;
-              weno_js(cfl[0][v], cfl[1][v], cfl[2][v], cfl[3][v], cfl[4][v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, cfl[0][v], cfl[1][v], cfl[2][v], cfl[3][v], cfl[4][v], p->eps, &w1, &w2, &w3);
               xfl[v] = weno_interp_char(w1, w2, w3, ifl[0][v], ifl[1][v], ifl[2][v], ifl[3][v], ifl[4][v]);
-              weno_js(cfr[0][v], cfr[1][v], cfr[2][v], cfr[3][v], cfr[4][v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, cfr[0][v], cfr[1][v], cfr[2][v], cfr[3][v], cfr[4][v], p->eps, &w1, &w2, &w3);
               xfr[v] = weno_interp_char(w1, w2, w3, ifr[0][v], ifr[1][v], ifr[2][v], ifr[3][v], ifr[4][v]);
-              weno_js(cul[0][v], cul[1][v], cul[2][v], cul[3][v], cul[4][v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, cul[0][v], cul[1][v], cul[2][v], cul[3][v], cul[4][v], p->eps, &w1, &w2, &w3);
               xul[v] = weno_interp_char(w1, w2, w3, iul[0][v], iul[1][v], iul[2][v], iul[3][v], iul[4][v]);
-              weno_js(cur[0][v], cur[1][v], cur[2][v], cur[3][v], cur[4][v], p->eps, &w1, &w2, &w3);
+              weno_w(p->weights, cur[0][v], cur[1][v], cur[2][v], cur[3][v], cur[4][v], p->eps, &w1, &w2, &w3);
               xur[v] = weno_interp_char(w1, w2, w3, iur[0][v], iur[1][v], iur[2][v], iur[3][v], iur[4][v]);
             }
             matvec(nv, fL, R, xfl);

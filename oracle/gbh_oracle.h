@@ -41,7 +41,13 @@ typedef struct {
   int nzones;
   orc_zone zones[12];
   double *dxinv;        /* sum_d (dim[d]+2*ghosts), per point 2/(x[i+1]-x[i-1]) */
+  int weights;          /* ORC_WENO_*: nonlinear weight formulation */
 } orc_problem;
+
+/* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
+ * Yamaleev-Carpenter, or the optimal weights (no_limiting). */
+enum { ORC_WENO_JS = 0, ORC_WENO_MAPPED = 1, ORC_WENO_BORGES = 2, ORC_WENO_YC = 3, ORC_WENO_NONE = 4 };
+void orc_set_weights(orc_problem *p, int weights);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

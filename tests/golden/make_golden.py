@@ -40,7 +40,22 @@ CASES = {
     "tgv12_comp_roe_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02),
     "tgv12_char_llf_rk33": lambda: C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
                                          upwinding="llf-char", scheme="33"),
+    # the other WENO5 weight formulations (weno.inp mapped / borges / yc / no_limiting)
+    "sod64_comp_roe_mapped": lambda: _w(C.sod(64, n_iter=20, dt=1e-3), "mapped"),
+    "sod64_char_llf_borges": lambda: _w(C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                              upwinding="llf-char"), "borges"),
+    "vortex24_char_roe_yc_ssprk3": lambda: _w(C.vortex(24, n_iter=5, dt=0.02), "yc"),
+    "vortex24_comp_llf_none_rk4": lambda: _w(C.vortex(24, n_iter=5, dt=0.02, interp="components",
+                                                      upwinding="llf-char", scheme="44"), "none"),
+    "tgv12_char_rf_mapped_rk4": lambda: _w(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
+                                                 upwinding="rf-char"), "mapped"),
+    "tgv12_comp_roe_borges_rk4": lambda: _w(C.tgv(12, n_iter=3, dt=0.02), "borges"),
 }
+
+
+def _w(case, weights):
+    case.weights = weights
+    return case
 
 
 ENSEMBLES = {
@@ -49,10 +64,14 @@ ENSEMBLES = {
 
 
 def main() -> None:
+    """python tests/golden/make_golden.py [name ...]: all fixtures, or the named ones."""
     if not O.ref_available():
         raise SystemExit("oracle/_ref is not built (make -f oracle/Makefile.ref)")
+    only = set(sys.argv[1:])
     env = dict(os.environ, OMP_NUM_THREADS="1")
     for name, mk in CASES.items():
+        if only and name not in only:
+            continue
         case = mk()
         with tempfile.TemporaryDirectory() as d:
             case.write(d)
@@ -66,6 +85,8 @@ def main() -> None:
                             n_iter=case.n_iter, dt=case.dt)
         print(name, rhs.shape, op["u"].shape)
     for name, mk in ENSEMBLES.items():
+        if only and name not in only:
+            continue
         members = mk()
         with tempfile.TemporaryDirectory() as d:
             C.write_ensemble(members, d)

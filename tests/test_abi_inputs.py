@@ -81,10 +81,6 @@ def _expect(code, directory):
 def test_reader_errors(built_lib, tmp_path):
     _expect(3, str(tmp_path / "nowhere"))
     case = C.vortex(12, n_iter=1, dt=0.01)
-    d = tmp_path / "a"
-    case.write(str(d))
-    open(d / "weno.inp", "w").write("begin\n mapped 1\nend\n")
-    _expect(4, str(d))
     d = tmp_path / "b"
     case.write(str(d))
     t = open(d / "boundary.inp").read().replace("periodic", "slip-wall", 1)
@@ -109,6 +105,19 @@ def test_reader_errors(built_lib, tmp_path):
     case.write(str(d))
     open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding steger-warming\nend\n")
     _expect(4, str(d))
+
+
+@pytest.mark.parametrize("flags,expect", [
+    ("", 0), ("mapped 1", 1), ("borges 1", 2), ("yc 1", 3), ("no_limiting 1", 4),
+    ("mapped 1\n borges 1", 2), ("borges 1\n yc 1", 3), ("mapped 1\n no_limiting 1", 4)])
+def test_reader_weno_weights(built_lib, tmp_path, flags, expect):
+    """weno.inp flags -> gb_config.weno_weights with the reference's precedence
+    (yc, borges, mapped; no_limiting keeps the optimal weights)."""
+    case = C.vortex(12, n_iter=1, dt=0.01)
+    d = str(tmp_path / "deck")
+    case.write(d)
+    open(os.path.join(d, "weno.inp"), "w").write(f"begin\n {flags}\n epsilon 1e-6\nend\n")
+    assert Inputs(d).config.weno_weights == expect
 
 
 def test_solver_create_rejects_bad_config(built_lib):

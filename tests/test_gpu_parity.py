@@ -66,6 +66,31 @@ def test_rhs_matches_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw)
     assert np.count_nonzero(got) == np.count_nonzero(gi)
 
 
+WEIGHT_COMBOS = [(m, i, w) for m in ("euler1d", "euler2d", "navierstokes3d")
+                 for i in ("components", "characteristic") for w in ("mapped", "borges", "yc", "none")]
+
+
+@pytest.mark.parametrize("model,interp,weights", WEIGHT_COMBOS)
+def test_rhs_weights_match_oracle(built_lib, oracle_lib, tmp_path, model, interp, weights):
+    """Mapped / Borges / Yamaleev-Carpenter / optimal weights: one RHS and a few steps."""
+    upw = {"euler1d": "roe", "euler2d": "llf-char", "navierstokes3d": "rf-char"}[model]
+    case = make(model, interp, upw)
+    case.weights = weights
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    ref = P.rhs(u0)
+    u = torch.from_numpy(u0).cuda()
+    out = torch.full_like(u, 7.0)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
+    assert relerr(got, O.interior(ref, case.size, case.nvars, 3)) <= RHS_TOL
+    s.set_state(case.u)
+    s.step(case.n_iter)
+    refN = O.interior(P.rk(u0, case.n_iter), case.size, case.nvars, 3).reshape(-1)
+    assert relerr(s.get_state(), refN) <= STEP_TOL
+
+
 @pytest.mark.parametrize("model,interp,upw", [c for c in COMBOS if c[2] != "rf-char"])
 def test_steps_match_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw):
     case = make(model, interp, upw, n_iter=6)
