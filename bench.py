@@ -7,7 +7,7 @@ characteristic WENO5 (Jiang-Shu) + Roe, SSPRK3, dt at CFL 0.5, FP64.  A
 "step" is one SSPRK3 step of that grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload vortex|tgv|sod|ensemble|adjoint]
+                  [--workload vortex|tgv|sod|ensemble|adjoint|convergence]
 
 --impl ours       the fused CUDA path through libgbhypar's C ABI (value: device
                   time of the resident solution; e2e: host buffers copied in and
@@ -554,6 +554,55 @@ def run_adjoint(args, ws, rank, local):
     return out
 
 
+def run_convergence(args, ws, rank, local):
+    """Grid convergence on the smooth isentropic vortex (b = 5, periodic [0,10)^2,
+    characteristic WENO5 + Roe): grids 64^2..512^2, one small dt for all (RK4,
+    dt = 1e-3, so the time error is ~1e-13 and the spatial error dominates),
+    T = 0.5; errors against the translated exact vortex through the library's
+    CalculateError (gb_solver_error, the whole domain, relative), and the L2 error
+    over the centre [2,8]^2 (away from the periodic seam, where the vortex's
+    exp(-12) tail leaves a 5e-5 jump in v that no grid resolves)."""
+    import numpy as np
+    import torch
+    from hypar_gb300 import cases as C
+    from hypar_gb300.solver import Solver
+
+    torch.cuda.set_device(local)
+    dt, T = 1e-3, 0.5
+    nsteps = int(round(T / dt))
+    rows = []
+    t0 = time.perf_counter()
+    for n in (64, 128, 256, 512):
+        case = C.vortex(n, n_iter=nsteps, dt=dt, interp="characteristic", upwinding="roe", scheme="44")
+        d = tempfile.mkdtemp(prefix=f"gbh_conv{n}_")
+        case.write(d)
+        s = Solver.from_dir(d, device=local)
+        s.step(nsteps)
+        x, uex = C.vortex_state(n, 5.0, 5.0 + 0.5 * T, 5.0)
+        err = s.error(uex)
+        u = s.get_state().reshape(n, n, 4)
+        ue = uex.reshape(n, n, 4)
+        m = (x >= 2.0) & (x <= 8.0)
+        e = (u - ue)[m][:, m]
+        centre_l2 = float(np.sqrt(np.mean(e * e)) / np.sqrt(np.mean(ue[m][:, m] ** 2)))
+        rows.append({"n": n, "L1": err[0], "L2": err[1], "Linf": err[2], "centre_L2": centre_l2})
+        s.close()
+    wall = time.perf_counter() - t0
+    for a, b in zip(rows, rows[1:]):
+        for k in ("L1", "L2", "Linf", "centre_L2"):
+            b["order_" + k] = float(np.log2(a[k] / b[k]))
+    last = rows[-1]
+    return {
+        "metric": "spatial convergence order (L2, 256^2 -> 512^2)", "value": last["order_L2"], "unit": "order",
+        "n_gpus": 1, "steps": nsteps, "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ("Euler2D isentropic vortex b=5 on [0,10)^2 periodic, char-WENO5(JS)+Roe, RK4, "
+                                f"dt={dt}, T={T}, grids 64..512"),
+                   "exact": "translated vortex (centre + 0.5 T, 0)"},
+        "convergence": rows, "wall_s": wall,
+    }
+
+
 def cpu_baseline(case, budget_s: float = 15.0, threads: int = 0):
     """The oracle (the reference algorithm restated in C) on the host cores,
     timed on whole steps of the same workload until budget_s has elapsed."""
@@ -628,7 +677,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "ensemble", "adjoint",
+                                                          "convergence"])
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
@@ -636,10 +686,10 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
-    if args.workload in ("ensemble", "adjoint"):
+    if args.workload in ("ensemble", "adjoint", "convergence"):
         from hypar_gb300 import build as B
         B.build()
-        fn = run_ensemble if args.workload == "ensemble" else run_adjoint
+        fn = {"ensemble": run_ensemble, "adjoint": run_adjoint, "convergence": run_convergence}[args.workload]
         out = fn(args, ws, rank, local) if args.impl == "ours" else None
         if out is not None and rank == 0:
             print(json.dumps(out))

@@ -36,7 +36,8 @@ EXPORTS = [
     "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune", "gb_rhs_explicit_noalloc",
     "gb_adjoint_create", "gb_adjoint_destroy", "gb_adjoint_set_stream", "gb_adjoint_sync", "gb_adjoint_set_launch",
     "gb_adjoint_get_launch", "gb_adjoint_info", "gb_adjoint_rhs_vjp", "gb_adjoint_rhs_jvp", "gb_adjoint_forward",
-    "gb_adjoint_backward", "gb_adjoint_tlm",
+    "gb_adjoint_backward", "gb_adjoint_tlm", "gb_inputs_exact", "gb_solver_set_time", "gb_solver_cfl",
+    "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial",
 ]
 
 
@@ -49,7 +50,8 @@ class GbConfig(ctypes.Structure):
         ("nzones", ctypes.c_int), ("zones", (ctypes.c_int * 9) * 12),
         ("rk_nstages", ctypes.c_int), ("rk_A", ctypes.c_double * 16), ("rk_b", ctypes.c_double * 4),
         ("rk_c", ctypes.c_double * 4), ("dt", ctypes.c_double), ("n_iter", ctypes.c_int),
-        ("file_op_iter", ctypes.c_int), ("weno_weights", ctypes.c_int),
+        ("file_op_iter", ctypes.c_int), ("weno_weights", ctypes.c_int), ("restart_iter", ctypes.c_int),
+        ("screen_op_iter", ctypes.c_int), ("write_residual", ctypes.c_int),
     ]
 
 
@@ -81,7 +83,7 @@ def lib():
     L.gb_inputs_free.restype = None
     L.gb_inputs_config.argtypes = [VP]
     L.gb_inputs_config.restype = ctypes.POINTER(GbConfig)
-    for n in ("gb_inputs_x", "gb_inputs_dxinv", "gb_inputs_u0"):
+    for n in ("gb_inputs_x", "gb_inputs_dxinv", "gb_inputs_u0", "gb_inputs_exact"):
         getattr(L, n).argtypes = [VP]
         getattr(L, n).restype = DP
     L.gb_rk_table.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), DP, DP, DP]
@@ -135,6 +137,11 @@ def lib():
     L.gb_ensemble_autotune.argtypes = [VP, ctypes.c_int]
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     L.gb_rhs_explicit_noalloc.argtypes = [ctypes.POINTER(GbConfig), VP, VP, VP, VP]
+    L.gb_solver_set_time.argtypes = [VP, ctypes.c_double]
+    L.gb_solver_cfl.argtypes = [VP, DP]
+    L.gb_solver_step_report.argtypes = [VP, ctypes.c_int, DP, DP]
+    L.gb_solver_error.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, DP]
+    L.gb_op_to_initial.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
     L.gb_adjoint_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(VP)]
     L.gb_adjoint_destroy.argtypes = [VP]

@@ -48,6 +48,9 @@ class Case:
     Minf: float = 1.0
     file_op_iter: Optional[int] = None
     weights: str = "js"             # WENO5 weights: "js" | "mapped" | "borges" | "yc" | "none" (no_limiting)
+    op_overwrite: str = "yes"       # solver.inp op_overwrite ("no": op_NNNNN.bin every file_op_iter)
+    restart_iter: int = 0           # solver.inp restart_iter
+    screen_op_iter: Optional[int] = None
 
     @property
     def ndims(self) -> int:
@@ -76,14 +79,16 @@ class Case:
             lines += ["  par_space_type    nonconservative-2stage", "  par_space_scheme  4"]
         lines += [
             f"  dt                {float(self.dt)!r}",
-            f"  screen_op_iter    {max(self.n_iter, 1)}",
+            f"  screen_op_iter    {self.screen_op_iter or max(self.n_iter, 1)}",
             f"  file_op_iter      {self.file_op_iter or max(self.n_iter, 1)}",
             "  ip_file_type      binary",
             "  op_file_format    binary",
-            "  op_overwrite      yes",
+            f"  op_overwrite      {self.op_overwrite}",
             f"  model             {self.model}",
-            "end",
         ]
+        if self.restart_iter:
+            lines.append(f"  restart_iter      {self.restart_iter}")
+        lines.append("end")
         return "\n".join(lines) + "\n"
 
     def physics_inp(self) -> str:

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "gbh_internal.h"
+#include "gbh_solver.h"
 #include "gbhypar.h"
 
 namespace gbh {
@@ -58,39 +59,6 @@ extern "C" const char* gb_last_error(void) { return g_err; }
     }                                                                             \
   } while (0)
 
-struct gb_solver {
-  gb_config cfg;
-  DevGeom G;
-  PhysParams pp;
-  ViscParams vp;
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  long long npts_wg = 0;
-  size_t nvals = 0;
-  double* d_u = nullptr;
-  double* d_acc = nullptr;
-  double* d_P[4] = {nullptr, nullptr, nullptr, nullptr};
-  double* d_H = nullptr;
-  double* d_par = nullptr;
-  double* d_Q = nullptr;
-  double* d_Gr = nullptr;
-  double* d_dxinv = nullptr;
-  int* d_flag = nullptr;
-  std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
-  HypLaunch hl[3];
-  int visc_seg = 16;
-  double t = 0.0;
-  long long dx_off[3] = {0, 0, 0};
-  bool viscous = false;
-  // launch profiler: an event pair around every launch group, read on demand
-  bool prof = false;
-  struct Rec { int cls; cudaEvent_t a, b; };
-  std::vector<Rec> recs;
-  std::vector<cudaEvent_t> pool;
-  double prof_ms[GB_PROF_CLASSES] = {0};
-  long long prof_n[GB_PROF_CLASSES] = {0};
-};
 
 static cudaEvent_t ev_get(gb_solver* s) {
   if (!s->pool.empty()) {
@@ -343,6 +311,8 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_Gr);
   cudaFree(s->d_dxinv);
   cudaFree(s->d_flag);
+  cudaFree(s->d_snap);
+  cudaFree(s->d_red);
   prof_drain(s);
   for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -461,10 +431,15 @@ extern "C" int gb_solver_get_state(gb_solver* s, double* u, int layout, int mem)
 
 extern "C" double* gb_solver_state(gb_solver* s) { return s ? s->d_u : nullptr; }
 extern "C" double gb_solver_time(const gb_solver* s) { return s ? s->t : 0.0; }
+extern "C" int gb_solver_set_time(gb_solver* s, double t) {
+  if (!s) { gbh_set_error("gb_solver_set_time: null solver"); return GB_ERR_ARG; }
+  s->t = t;
+  return GB_OK;
+}
 
 // One Runge-Kutta step (TimeRK, src/TimeIntegration/TimeRK.c:126-195) as
 // nstages x ndims fused launches.
-static int rk_step(gb_solver* s) {
+int gbh_rk_step(gb_solver* s) {
   const gb_config& c = s->cfg;
   const int ns = c.rk_nstages;
   const double dt = c.dt;
@@ -507,7 +482,7 @@ static int rk_step(gb_solver* s) {
 extern "C" int gb_solver_step(gb_solver* s, int nsteps) {
   if (!s || nsteps < 0) { gbh_set_error("gb_solver_step: bad argument"); return GB_ERR_ARG; }
   for (int n = 0; n < nsteps; n++) {
-    int rc = rk_step(s);
+    int rc = gbh_rk_step(s);
     if (rc) return rc;
   }
   CK(cudaGetLastError());
@@ -562,9 +537,9 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
       for (int blk : {128, 64}) {
         s->hl[d].seg = sg;
         s->hl[d].block = blk;
-        rc = rk_step(s);  // warm
+        rc = gbh_rk_step(s);  // warm
         if (!rc) rc = gb_solver_profile(s, 1);
-        for (int r = 0; r < reps && !rc; r++) rc = rk_step(s);
+        for (int r = 0; r < reps && !rc; r++) rc = gbh_rk_step(s);
         double ms[GB_PROF_CLASSES];
         long long nl[GB_PROF_CLASSES];
         if (!rc) rc = gb_solver_profile_read(s, ms, nl);
@@ -735,7 +710,7 @@ extern "C" int gb_RHSFunctionExplicit(double* rhs, double* u, void* sv, void* m,
 extern "C" int gb_TimeRK(void* ts) {
   gb_solver* s = S(ts);
   if (!s) { gbh_set_error("gb_TimeRK: null argument"); return GB_ERR_ARG; }
-  int rc = rk_step(s);
+  int rc = gbh_rk_step(s);
   if (rc) return rc;
   CK(cudaGetLastError());
   return GB_OK;

@@ -30,6 +30,7 @@ struct gb_inputs {
   double *x;      /* interior grid, sum dim */
   double *dxinv;  /* with ghosts */
   double *u0;     /* interior solution */
+  double *uex;    /* exact solution (exact.inp), or NULL */
   char op_overwrite[64];
 };
 
@@ -114,7 +115,7 @@ static void find_interval(double a, double b, const double *x, int N, int *imin,
 }
 
 typedef struct {
-  int ndims, nvars, ghosts, n_iter, file_op_iter;
+  int ndims, nvars, ghosts, n_iter, file_op_iter, restart_iter, screen_op_iter;
   int size[3], iproc[3];
   int member, nsims;   /* which simulation of an ensemble (simulation.inp) */
   double dt;
@@ -131,6 +132,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   si->nvars = 1;
   si->ghosts = 1;
   si->file_op_iter = 1000;
+  si->screen_op_iter = 1;
   strcpy(si->time_scheme, "euler");
   strcpy(si->time_scheme_type, " ");
   strcpy(si->hyp_space_scheme, "1");
@@ -184,6 +186,8 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
     else if (!strcmp(w, "par_space_scheme")) r = fscanf(in, "%511s", si->par_space_scheme);
     else if (!strcmp(w, "dt")) r = fscanf(in, "%lf", &si->dt);
     else if (!strcmp(w, "file_op_iter")) r = fscanf(in, "%d", &si->file_op_iter);
+    else if (!strcmp(w, "restart_iter")) r = fscanf(in, "%d", &si->restart_iter);
+    else if (!strcmp(w, "screen_op_iter")) r = fscanf(in, "%d", &si->screen_op_iter);
     else if (!strcmp(w, "ip_file_type")) r = fscanf(in, "%511s", si->ip_file_type);
     else if (!strcmp(w, "op_overwrite")) r = fscanf(in, "%511s", si->op_overwrite);
     else if (!strcmp(w, "model")) r = fscanf(in, "%511s", si->model);
@@ -192,7 +196,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
       r = fscanf(in, "%511s", mode);
       if (r == 1 && strcmp(mode, "serial")) { int nio; r = fscanf(in, "%d", &nio); }
     } else {
-      char useless[MAXS];  /* every other keyword takes one value (restart_iter, screen_op_iter, ...) */
+      char useless[MAXS];  /* every other keyword takes one value (conservation_check, ...) */
       r = fscanf(in, "%511s", useless);
     }
     if (r != 1) ok = 0;
@@ -200,6 +204,40 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   fclose(in);
   if (!ok) {
     gbh_set_error("could not parse solver.inp");
+    return GB_ERR_INPUT;
+  }
+  return GB_OK;
+}
+
+/* A solution file in HyPar's input format (ReadArray.c): binary = x then u
+ * (point-major); ascii = x then u variable by variable.  Returns -1 (no error
+ * message) when the file is absent and `required` is 0. */
+static int read_solution(const char *dir, const char *name, const char *type, long nx, long npts, int nvars,
+                         double *x, double *u, int required) {
+  int bin = !strcmp(type, "bin") || !strcmp(type, "binary");
+  if (!bin && strcmp(type, "ascii")) {
+    gbh_set_error("ip_file_type %s invalid", type);
+    return GB_ERR_INPUT;
+  }
+  FILE *in = open_in(dir, name, bin ? "rb" : "r");
+  if (!in) {
+    if (!required) return -1;
+    gbh_set_error("solution file %s not found", name);
+    return GB_ERR_INPUT;
+  }
+  int bad = 0;
+  if (bin) {
+    size_t a = fread(x, sizeof(double), nx, in);
+    size_t b = fread(u, sizeof(double), npts * nvars, in);
+    bad = (long)a != nx || (long)b != npts * nvars;
+  } else {
+    for (long i = 0; i < nx && !bad; i++) bad = fscanf(in, "%lf", &x[i]) != 1;
+    for (int v = 0; v < nvars && !bad; v++)
+      for (long p = 0; p < npts && !bad; p++) bad = fscanf(in, "%lf", &u[p * nvars + v]) != 1;
+  }
+  fclose(in);
+  if (bad) {
+    gbh_set_error("%s is too short or malformed", name);
     return GB_ERR_INPUT;
   }
   return GB_OK;
@@ -270,6 +308,7 @@ void gb_inputs_free(gb_inputs *in) {
   free(in->x);
   free(in->dxinv);
   free(in->u0);
+  free(in->uex);
   free(in);
 }
 
@@ -277,6 +316,7 @@ const gb_config *gb_inputs_config(const gb_inputs *in) { return in ? &in->cfg : 
 const double *gb_inputs_x(const gb_inputs *in) { return in ? in->x : NULL; }
 const double *gb_inputs_dxinv(const gb_inputs *in) { return in ? in->dxinv : NULL; }
 const double *gb_inputs_u0(const gb_inputs *in) { return in ? in->u0 : NULL; }
+const double *gb_inputs_exact(const gb_inputs *in) { return in ? in->uex : NULL; }
 const char *gbh_inputs_op_overwrite(const gb_inputs *in) { return in ? in->op_overwrite : "yes"; }
 
 int gb_inputs_nsims(const char *dir) {
@@ -376,6 +416,9 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   c.dt = si.dt;
   c.n_iter = si.n_iter;
   c.file_op_iter = si.file_op_iter;
+  c.restart_iter = si.restart_iter;
+  c.screen_op_iter = si.screen_op_iter > 0 ? si.screen_op_iter : 1;
+  c.write_residual = 0;  /* the reference reads no keyword for it either (ReadInputs.c:125) */
 
   /* physics.inp */
   char upw[MAXS] = "roe";
@@ -427,7 +470,7 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
                                : GB_WENO_JS;
 
   gb_inputs *res = (gb_inputs *)calloc(1, sizeof(gb_inputs));
-  strncpy(res->op_overwrite, si.op_overwrite, sizeof(res->op_overwrite) - 1);
+  snprintf(res->op_overwrite, sizeof(res->op_overwrite), "%s", si.op_overwrite);
   long nx = 0, nxg = 0, npts = 1;
   for (int d = 0; d < c.ndims; d++) {
     nx += c.dim[d];
@@ -438,46 +481,31 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   res->dxinv = (double *)calloc(nxg, sizeof(double));
   res->u0 = (double *)calloc(npts * c.nvars, sizeof(double));
 
-  /* initial.inp */
-  char iname[256], bname[256];
+  /* initial.inp, and exact.inp when present (ExactSolution.c, same format) */
+  char iname[256], bname[256], ename[256];
   member_name(iname, sizeof(iname), "initial", member, nsims);
   member_name(bname, sizeof(bname), "boundary", member, nsims);
-  if (!strcmp(si.ip_file_type, "bin") || !strcmp(si.ip_file_type, "binary")) {
-    FILE *in = open_in(dir, iname, "rb");
-    if (!in) {
-      gb_inputs_free(res);
-      gbh_set_error("initial solution file initial.inp not found");
-      return GB_ERR_INPUT;
-    }
-    size_t a = fread(res->x, sizeof(double), nx, in);
-    size_t b = fread(res->u0, sizeof(double), npts * c.nvars, in);
-    fclose(in);
-    if ((long)a != nx || (long)b != npts * c.nvars) {
-      gb_inputs_free(res);
-      gbh_set_error("initial.inp is too short");
-      return GB_ERR_INPUT;
-    }
-  } else if (!strcmp(si.ip_file_type, "ascii")) {
-    FILE *in = open_in(dir, iname, "r");
-    if (!in) {
-      gb_inputs_free(res);
-      gbh_set_error("initial solution file initial.inp not found");
-      return GB_ERR_INPUT;
-    }
-    int bad = 0;
-    for (long i = 0; i < nx && !bad; i++) bad = fscanf(in, "%lf", &res->x[i]) != 1;
-    for (int v = 0; v < c.nvars && !bad; v++)
-      for (long p = 0; p < npts && !bad; p++) bad = fscanf(in, "%lf", &res->u0[p * c.nvars + v]) != 1;
-    fclose(in);
-    if (bad) {
-      gb_inputs_free(res);
-      gbh_set_error("could not read initial.inp");
-      return GB_ERR_INPUT;
-    }
-  } else {
+  member_name(ename, sizeof(ename), "exact", member, nsims);
+  rc = read_solution(dir, iname, si.ip_file_type, nx, npts, c.nvars, res->x, res->u0, 1);
+  if (rc) {
     gb_inputs_free(res);
-    gbh_set_error("ip_file_type %s invalid", si.ip_file_type);
-    return GB_ERR_INPUT;
+    return rc;
+  }
+  {
+    double *xd = (double *)calloc(nx, sizeof(double));
+    double *ue = (double *)calloc(npts * c.nvars, sizeof(double));
+    rc = read_solution(dir, ename, si.ip_file_type, nx, npts, c.nvars, xd, ue, 0);
+    free(xd);
+    if (rc == GB_OK) {
+      res->uex = ue;
+    } else {
+      free(ue);
+      if (rc != -1) {
+        gb_inputs_free(res);
+        return rc;
+      }
+      rc = GB_OK;
+    }
   }
 
   /* dxinv with ghosts */
@@ -580,5 +608,50 @@ int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, cons
   fwrite(x, sizeof(double), nx, out);
   fwrite(u, sizeof(double), n * nvars, out);
   fclose(out);
+  return GB_OK;
+}
+
+int gb_op_to_initial(const char *op_path, const char *initial_path) {
+  /* Extras/BinaryOPToInitialSolution.c: the header (ndims, nvars, dims) is
+   * dropped, x and u are written as a binary initial.inp. */
+  if (!op_path || !initial_path) {
+    gbh_set_error("gb_op_to_initial: null path");
+    return GB_ERR_ARG;
+  }
+  FILE *in = fopen(op_path, "rb");
+  if (!in) {
+    gbh_set_error("could not open %s", op_path);
+    return GB_ERR_INPUT;
+  }
+  int ndims = 0, nvars = 0, dims[3] = {0, 0, 0};
+  int bad = fread(&ndims, sizeof(int), 1, in) != 1 || fread(&nvars, sizeof(int), 1, in) != 1 || ndims < 1 ||
+            ndims > 3 || nvars < 1 || fread(dims, sizeof(int), ndims, in) != (size_t)ndims;
+  long nx = 0, nu = nvars;
+  for (int d = 0; d < ndims && !bad; d++) {
+    if (dims[d] < 1) bad = 1;
+    nx += dims[d];
+    nu *= dims[d];
+  }
+  double *buf = bad ? NULL : (double *)malloc(sizeof(double) * (nx + nu));
+  if (!bad) bad = !buf || fread(buf, sizeof(double), nx + nu, in) != (size_t)(nx + nu);
+  fclose(in);
+  if (bad) {
+    free(buf);
+    gbh_set_error("%s is not a HyPar binary solution file", op_path);
+    return GB_ERR_INPUT;
+  }
+  FILE *out = fopen(initial_path, "wb");
+  if (!out) {
+    free(buf);
+    gbh_set_error("could not open %s for writing", initial_path);
+    return GB_ERR_INPUT;
+  }
+  size_t w = fwrite(buf, sizeof(double), nx + nu, out);
+  fclose(out);
+  free(buf);
+  if (w != (size_t)(nx + nu)) {
+    gbh_set_error("short write to %s", initial_path);
+    return GB_ERR_INPUT;
+  }
   return GB_OK;
 }

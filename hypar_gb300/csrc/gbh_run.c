@@ -7,9 +7,11 @@
  * op_00000.bin, op_00001.bin, ... every file_op_iter steps
  * (src/Simulation/OutputSolution.cpp:50-140).
  */
+#define _POSIX_C_SOURCE 200809L /* clock_gettime */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "gbhypar.h"
 
@@ -24,6 +26,25 @@ static int write_op(const char *dir, const char *name, const gb_config *c, const
   if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s", dir, name);
   else snprintf(path, sizeof(path), "%s", name);
   return gb_write_binary(path, c->ndims, c->nvars, c->dim, x, buf);
+}
+
+static int write_errors(const char *dir, const gb_config *c, const double *err, double runtime) {
+  /* SimulationWriteErrors.c:74-81: sizes, iproc, dt, L1 L2 Linf, solver and total runtimes */
+  char path[4200];
+  if (dir && dir[0]) snprintf(path, sizeof(path), "%s/errors.dat", dir);
+  else snprintf(path, sizeof(path), "errors.dat");
+  FILE *out = fopen(path, "w");
+  if (!out) {
+    gbh_set_error("could not open %s for writing", path);
+    return GB_ERR_INPUT;
+  }
+  for (int d = 0; d < c->ndims; d++) fprintf(out, "%4d ", c->dim[d]);
+  for (int d = 0; d < c->ndims; d++) fprintf(out, "%4d ", 1);
+  fprintf(out, "%1.16E  ", c->dt);
+  fprintf(out, "%1.16E %1.16E %1.16E   ", err[0], err[1], err[2]);
+  fprintf(out, "%1.16E %1.16E\n", runtime, runtime);
+  fclose(out);
+  return GB_OK;
 }
 
 static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
@@ -104,32 +125,87 @@ int gb_run_case(const char *dir, int device, int verbose) {
   for (int d = 0; d < c->ndims; d++) n *= c->dim[d];
   double *buf = (double *)malloc(sizeof(double) * n);
   rc = gb_solver_set_state(s, gb_inputs_u0(in), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
-  int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");
-  int every = c->file_op_iter > 0 ? c->file_op_iter : c->n_iter;
+  const int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");
+  const int every = c->file_op_iter > 0 ? c->file_op_iter : c->n_iter;
+  const int screen = c->screen_op_iter > 0 ? c->screen_op_iter : 1;
+  const int R = c->restart_iter > 0 ? c->restart_iter : 0;
+  /* a restart run starts at t = restart_iter * dt (TimeInitialize.c:49-52) and
+     fast-forwards the file index over the outputs before it (InitializeSolvers.c:438-442) */
   int k = 0;
+  for (int t = 0; t < R; t++)
+    if ((t + 1) % every == 0) k++;
+  if (!rc) rc = gb_solver_set_time(s, R * c->dt);
   char name[64];
-  if (!rc && !overwrite) {
+  if (!rc && !overwrite && R == 0) {
     snprintf(name, sizeof(name), "op_%05d.bin", k++);
     rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
   }
-  for (int it = 0; it < c->n_iter && !rc;) {
-    int chunk = every;
-    if (it + chunk > c->n_iter) chunk = c->n_iter - it;
-    rc = gb_solver_step(s, chunk);
-    it += chunk;
-    if (!rc && verbose) printf("gbhypar: iteration %d / %d, t = %.6e\n", it, c->n_iter, gb_solver_time(s));
-    if (!rc && !overwrite && (it % every == 0 || it == c->n_iter)) {
+  FILE *resid = NULL;
+  if (!rc && c->write_residual) {
+    char path[4200];
+    if (dir && dir[0]) snprintf(path, sizeof(path), "%s/residual.out", dir);
+    else snprintf(path, sizeof(path), "residual.out");
+    resid = fopen(path, "w");
+  }
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  /* Solve.cpp:97-152: a report every screen_op_iter iterations (TimePreStep CFL,
+     TimePostStep norm, TimePrintStep line), an output every file_op_iter */
+  for (int it = R; it < c->n_iter && !rc;) {
+    int next_screen = (it / screen + 1) * screen;
+    int next_out = (it / every + 1) * every;
+    int target = c->n_iter;
+    if (next_screen < target) target = next_screen;
+    if (next_out < target) target = next_out;
+    const int report = (target % screen == 0);
+    struct timespec a, b;
+    clock_gettime(CLOCK_MONOTONIC, &a);
+    double cfl = -1.0, norm = -1.0;
+    if (report) rc = gb_solver_step_report(s, target - it, &cfl, &norm);
+    else rc = gb_solver_step(s, target - it);
+    clock_gettime(CLOCK_MONOTONIC, &b);
+    double wc = (b.tv_sec - a.tv_sec) + 1e-9 * (b.tv_nsec - a.tv_nsec);
+    it = target;
+    if (rc) break;
+    if (report) {
+      if (verbose)
+        printf("iter=%7d  t=%1.3E  CFL=%1.3E  norm=%1.4E  wctime: %1.1E (s)  \n", it, gb_solver_time(s), cfl,
+               norm, wc);
+      if (resid) fprintf(resid, "%10d\t%E\t%E\n", it, gb_solver_time(s), norm);
+    }
+    if (!overwrite && it % every == 0 && it < c->n_iter) {
       snprintf(name, sizeof(name), "op_%05d.bin", k++);
       rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
     }
   }
-  if (!rc && overwrite) rc = write_op(dir, "op.bin", c, gb_inputs_x(in), s, buf);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  const double solver_runtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+  if (resid) fclose(resid);
+  if (!rc) {
+    if (overwrite) rc = write_op(dir, "op.bin", c, gb_inputs_x(in), s, buf);
+    else {
+      snprintf(name, sizeof(name), "op_%05d.bin", k++);
+      rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
+    }
+  }
   if (!rc) {
     int fin = 1;
     rc = gb_solver_check_finite(s, &fin);
     if (!rc && !fin) {
       gbh_set_error("the solution contains NaN or Inf");
       rc = GB_ERR_NONFINITE;
+    }
+  }
+  /* CalculateError + SimulationWriteErrors: errors.dat (-1 without exact.inp) */
+  if (!rc) {
+    double err[3] = {-1.0, -1.0, -1.0};
+    if (gb_inputs_exact(in)) rc = gb_solver_error(s, gb_inputs_exact(in), GB_LAYOUT_INTERIOR, GB_MEM_HOST, err);
+    if (!rc) rc = write_errors(dir, c, err, solver_runtime);
+    if (!rc && verbose && err[0] >= 0) {
+      printf("Computed errors for domain 0:\n");
+      printf("  L1         Error           : %1.16E\n", err[0]);
+      printf("  L2         Error           : %1.16E\n", err[1]);
+      printf("  Linfinity  Error           : %1.16E\n", err[2]);
     }
   }
   free(buf);

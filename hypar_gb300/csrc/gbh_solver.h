@@ -1,0 +1,46 @@
+// gbh_solver.h -- the gb_solver object, shared by the translation units that
+// operate on a solver (not part of the public C ABI).
+#pragma once
+
+#include <vector>
+
+#include "gbh_internal.h"
+
+struct gb_solver {
+  gb_config cfg;
+  gbh::DevGeom G;
+  gbh::PhysParams pp;
+  gbh::ViscParams vp;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  long long npts_wg = 0;
+  size_t nvals = 0;
+  double* d_u = nullptr;
+  double* d_acc = nullptr;
+  double* d_P[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* d_H = nullptr;
+  double* d_par = nullptr;
+  double* d_Q = nullptr;
+  double* d_Gr = nullptr;
+  double* d_dxinv = nullptr;
+  double* d_snap = nullptr;  // copy of u before a monitored step (allocated on first use)
+  double* d_red = nullptr;   // reduction partials (allocated on first use)
+  int* d_flag = nullptr;
+  std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
+  gbh::HypLaunch hl[3];
+  int visc_seg = 16;
+  double t = 0.0;
+  long long dx_off[3] = {0, 0, 0};
+  bool viscous = false;
+  // launch profiler: an event pair around every launch group, read on demand
+  bool prof = false;
+  struct Rec { int cls; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[GB_PROF_CLASSES] = {0};
+  long long prof_n[GB_PROF_CLASSES] = {0};
+};
+
+// One Runge-Kutta step of the resident solution (the fused launches).
+int gbh_rk_step(gb_solver* s);

@@ -174,6 +174,31 @@ class Solver:
         check(lib().gb_solver_profile_read(self._h, ms, n))
         return {k: (ms[i], n[i]) for i, k in enumerate(self.PROF_CLASSES)}
 
+    def set_time(self, t: float):
+        check(lib().gb_solver_set_time(self._h, float(t)))
+
+    def cfl(self) -> float:
+        """Maximum CFL of the resident solution for the configured dt (device reduction)."""
+        c = ctypes.c_double()
+        check(lib().gb_solver_cfl(self._h, ctypes.byref(c)))
+        return c.value
+
+    def step_report(self, nsteps: int = 1):
+        """Advance nsteps steps; (CFL of the state the last step starts from, norm of its change)."""
+        c, n = ctypes.c_double(), ctypes.c_double()
+        check(lib().gb_solver_step_report(self._h, nsteps, ctypes.byref(c), ctypes.byref(n)))
+        return c.value, n.value
+
+    def error(self, uex, ghosted: bool = False):
+        """(L1, L2, Linf) errors against an exact solution (host numpy array or device tensor)."""
+        err = (ctypes.c_double * 3)()
+        mem = _lib.MEM_DEVICE if hasattr(uex, "data_ptr") else _lib.MEM_HOST
+        if mem == _lib.MEM_HOST:
+            uex = np.ascontiguousarray(uex, dtype=np.float64)
+        layout = _lib.LAYOUT_GHOSTED if ghosted else _lib.LAYOUT_INTERIOR
+        check(lib().gb_solver_error(self._h, _ptr(uex), layout, mem, err))
+        return tuple(err)
+
     def check_finite(self) -> bool:
         f = ctypes.c_int()
         check(lib().gb_solver_check_finite(self._h, ctypes.byref(f)))

@@ -67,6 +67,9 @@ typedef struct gb_config {
   int n_iter;               /* number of steps (solver.inp n_iter) */
   int file_op_iter;         /* output interval (solver.inp file_op_iter) */
   int weno_weights;         /* GB_WENO_*; the batched ensemble and the adjoint take Jiang-Shu only */
+  int restart_iter;         /* solver.inp restart_iter: first iteration, t0 = restart_iter * dt */
+  int screen_op_iter;       /* solver.inp screen_op_iter: CFL / norm report interval */
+  int write_residual;       /* solver.inp write_residual: residual.out with the norms */
 } gb_config;
 
 typedef struct gb_solver gb_solver;
@@ -90,6 +93,9 @@ const double *gb_inputs_x(const gb_inputs *in);
 const double *gb_inputs_dxinv(const gb_inputs *in);
 /* Initial solution, interior points, nvars per point, dimension 0 fastest. */
 const double *gb_inputs_u0(const gb_inputs *in);
+/* Exact solution from exact.inp (same format as initial.inp,
+ * src/HyParFunctions/ExactSolution.c), or NULL when the deck has none. */
+const double *gb_inputs_exact(const gb_inputs *in);
 /* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
  * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
  * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
@@ -119,8 +125,22 @@ int gb_solver_get_state(gb_solver *s, double *u, int layout, int mem);
 double *gb_solver_state(gb_solver *s);
 /* Advance nsteps Runge-Kutta steps of size cfg->dt on the resident solution. */
 int gb_solver_step(gb_solver *s, int nsteps);
-/* Simulation time of the resident solution. */
+/* Simulation time of the resident solution (set_state resets it to 0). */
 double gb_solver_time(const gb_solver *s);
+int gb_solver_set_time(gb_solver *s, double t);
+/* Around-the-step quantities of the reference, reduced on the device:
+ * gb_solver_cfl: maximum CFL of the resident solution with cfg->dt
+ * (<Model>ComputeCFL, the reference's operation order: bit-identical);
+ * gb_solver_step_report: advance nsteps steps and return the CFL of the state
+ * the last step starts from (TimePreStep.c:93-100) and the norm of that step's
+ * change, sqrt(sum (u_new-u_old)^2 / npoints) (TimePostStep.c:38-60) (either
+ * pointer may be NULL);
+ * gb_solver_error: L1, L2, Linf errors of the resident solution against an
+ * exact one (layout GB_LAYOUT_*, memory GB_MEM_*), relative to the exact
+ * solution's norms when those exceed 1e-15 (CalculateError.c:27-110). */
+int gb_solver_cfl(gb_solver *s, double *cfl);
+int gb_solver_step_report(gb_solver *s, int nsteps, double *cfl, double *norm);
+int gb_solver_error(gb_solver *s, const double *uex, int layout, int mem, double *err);
 /* Launch shape of the fused kernels: interfaces walked per thread (seg) and
  * threads per block, per direction (values <= 0 keep the current ones). */
 int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
@@ -171,6 +191,9 @@ int gb_ensemble_autotune(gb_ensemble *e, int reps);
 int gb_run_case(const char *dir, int device, int verbose);
 /* Write a HyPar binary solution file from an interior solution. */
 int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
+/* Convert a binary solution file (op*.bin) into a binary initial.inp, for a
+ * restart (the reference's Extras/BinaryOPToInitialSolution.c). */
+int gb_op_to_initial(const char *op_path, const char *initial_path);
 
 /* Measure the device's FP64 fused-multiply-add throughput (TFLOP/s, an FMA
  * counted as two operations) with a register-resident DFMA loop: the

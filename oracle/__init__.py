@@ -65,6 +65,8 @@ def _bind(path):
     L.orc_problem_destroy.argtypes = [ctypes.c_void_p]
     L.orc_set_weights.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.orc_set_weights.restype = None
+    L.orc_cfl.argtypes = [ctypes.c_void_p, dp, ctypes.c_double]
+    L.orc_cfl.restype = ctypes.c_double
     L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
     for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs"):
         getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
@@ -260,6 +262,10 @@ class Problem:
         self._L.orc_hyperbolic(self.h, _dp(u), _dp(out))
         return out
 
+    def cfl(self, u_wg: np.ndarray, dt: Optional[float] = None) -> float:
+        u = np.ascontiguousarray(u_wg, np.float64)
+        return float(self._L.orc_cfl(self.h, _dp(u), float(self.case.dt if dt is None else dt)))
+
     def apply_bc(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
         self._L.orc_apply_bc(self.h, _dp(u))
@@ -298,6 +304,7 @@ def read_harness_dump(path: str):
     n = int(np.prod([int(d) + 2 * int(g) for d in dims])) * int(nvars)
     u_in = np.frombuffer(buf, np.float64, n, off); off += 8 * n
     u_bc = np.frombuffer(buf, np.float64, n, off); off += 8 * n
-    rhs = np.frombuffer(buf, np.float64, n, off)
+    rhs = np.frombuffer(buf, np.float64, n, off); off += 8 * n
+    cfl = float(np.frombuffer(buf, np.float64, 1, off)[0]) if len(buf) >= off + 8 else None
     return {"dims": dims.copy(), "nvars": int(nvars), "g": int(g), "dxinv": dxinv.copy(),
-            "u_in": u_in.copy(), "u_bc": u_bc.copy(), "rhs": rhs.copy()}
+            "u_in": u_in.copy(), "u_bc": u_bc.copy(), "rhs": rhs.copy(), "cfl": cfl}

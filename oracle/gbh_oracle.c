@@ -985,6 +985,39 @@ int orc_parabolic(const orc_problem *p, const double *u, double *par) {
 
 /* TimeRHSFunctionExplicit (src/TimeIntegration/TimeRHSFunctionExplicit.c:30-98):
  * rhs = 0; rhs += -1*hyp; rhs += par; rhs += source (zero here). */
+/* <Model>ComputeCFL (Euler1DComputeCFL.c:16-44, Euler2DComputeCFL.c:14-39,
+ * NavierStokes3DComputeCFL.c:18-49): max over interior points and dimensions of
+ * (|v_d| + c) dt dxinv_d, with the flow variables of _<Model>GetFlowVar_. */
+double orc_cfl(const orc_problem *p, const double *u, double dt) {
+  const int nd = p->ndims, nv = p->nvars, g = p->ghosts;
+  long stride[3] = {1, 1, 1}, doff[3] = {0, 0, 0};
+  for (int d = 1; d < nd; d++) stride[d] = stride[d - 1] * (p->dim[d - 1] + 2 * g);
+  for (int d = 1; d < nd; d++) doff[d] = doff[d - 1] + p->dim[d - 1] + 2 * g;
+  double max_cfl = 0;
+  int n2 = nd > 1 ? p->dim[1] : 1, n3 = nd > 2 ? p->dim[2] : 1;
+  for (int k = 0; k < n3; k++)
+    for (int j = 0; j < n2; j++)
+      for (int i = 0; i < p->dim[0]; i++) {
+        int idx[3] = {i, j, k};
+        long q = 0;
+        for (int d = 0; d < nd; d++) q += (idx[d] + g) * stride[d];
+        const double *w = u + nv * q;
+        double rho = w[0], vel[3] = {0, 0, 0}, vsq, P, c;
+        for (int d = 0; d < nd; d++) vel[d] = w[1 + d] / rho;
+        vsq = vel[0] * vel[0];
+        if (nd > 1) vsq = vsq + vel[1] * vel[1];
+        if (nd > 2) vsq = vsq + vel[2] * vel[2];
+        P = (w[nv - 1] - 0.5 * rho * vsq) * (p->gamma - 1.0);
+        c = sqrt(p->gamma * P / rho);
+        for (int d = 0; d < nd; d++) {
+          double dxinv = p->dxinv[doff[d] + idx[d] + g];
+          double local = ((vel[d] < 0 ? -vel[d] : vel[d]) + c) * dt * dxinv;
+          if (local > max_cfl) max_cfl = local;
+        }
+      }
+  return max_cfl;
+}
+
 int orc_rhs(const orc_problem *p, double *u, double *rhs) {
   long n = orc_npoints_wghosts(p) * p->nvars;
   double *hyp = (double *)malloc(sizeof(double) * n);

@@ -71,6 +71,8 @@ int orc_rhs(const orc_problem *p, double *u, double *rhs);
 /* TimeRK over nsteps steps of the Butcher tableau (A: ns x ns row major, b). */
 int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
            double *u, double dt, int nsteps);
+/* Maximum CFL of a ghosted solution for time step dt (<Model>ComputeCFL). */
+double orc_cfl(const orc_problem *p, const double *u, double dt);
 /* Set the OpenMP thread count used by the oracle (<=0: library default). */
 void orc_set_threads(int n);
 int orc_get_threads(void);

@@ -52,6 +52,8 @@ int main(int argc, char** argv) {
   std::vector<double> u(u_in);
   std::vector<double> rhs(n, 0.0);
   TimeRHSFunctionExplicit(rhs.data(), u.data(), solver, mpi, 0.0);
+  // the model's CFL of the initial solution (solver->u) for the deck's dt
+  double cfl = solver->ComputeCFL ? solver->ComputeCFL(solver, mpi, solver->dt, 0.0) : -1.0;
 
   FILE* f = fopen(argv[1], "wb");
   if (!f) return 1;
@@ -63,6 +65,7 @@ int main(int argc, char** argv) {
   fwrite(u_in.data(), sizeof(double), n, f);
   fwrite(u.data(), sizeof(double), n, f);
   fwrite(rhs.data(), sizeof(double), n, f);
+  fwrite(&cfl, sizeof(double), 1, f);
   fclose(f);
   printf("ref_rhs_harness: wrote %s (%ld values)\n", argv[1], n);
   return 0;

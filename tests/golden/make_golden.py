@@ -82,7 +82,7 @@ def main() -> None:
             op = C.read_op_bin(os.path.join(d, "op.bin"))
         rhs = O.interior(dump["rhs"], case.size, case.nvars, 3)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), u0=case.u, rhs=rhs, uN=op["u"],
-                            n_iter=case.n_iter, dt=case.dt)
+                            n_iter=case.n_iter, dt=case.dt, cfl=dump["cfl"])
         print(name, rhs.shape, op["u"].shape)
     for name, mk in ENSEMBLES.items():
         if only and name not in only:

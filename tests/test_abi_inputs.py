@@ -128,3 +128,47 @@ def test_solver_create_rejects_bad_config(built_lib):
     rc = _lib.lib().gb_solver_create(ctypes.byref(cfg), dx.ctypes.data_as(_lib.DP), -1, ctypes.byref(h))
     assert rc == 1 and not h.value
     assert b"unknown model" in _lib.lib().gb_last_error()
+
+
+def test_reader_restart_screen_and_exact(built_lib, tmp_path):
+    """restart_iter / screen_op_iter from solver.inp, exact.inp in initial.inp's format."""
+    case = C.vortex(12, n_iter=6, dt=0.01)
+    case.restart_iter = 4
+    case.screen_op_iter = 2
+    d = str(tmp_path / "deck")
+    case.write(d)
+    inp_h = ctypes.c_void_p()
+    L = _lib.lib()
+    _lib.check(L.gb_inputs_read(d.encode(), ctypes.byref(inp_h)))
+    c = L.gb_inputs_config(inp_h).contents
+    assert (c.restart_iter, c.screen_op_iter, c.write_residual) == (4, 2, 0)
+    assert not L.gb_inputs_exact(inp_h)
+    L.gb_inputs_free(inp_h)
+    ex = case.u * 1.5
+    xs = np.concatenate([np.asarray(x, np.float64) for x in case.x])
+    with open(os.path.join(d, "exact.inp"), "wb") as f:
+        f.write(xs.tobytes() + np.ascontiguousarray(ex).tobytes())
+    _lib.check(L.gb_inputs_read(d.encode(), ctypes.byref(inp_h)))
+    p = L.gb_inputs_exact(inp_h)
+    assert p
+    got = np.ctypeslib.as_array(p, shape=(ex.size,)).copy()
+    L.gb_inputs_free(inp_h)
+    assert np.array_equal(got, ex.reshape(-1))
+
+
+def test_op_to_initial_round_trip(built_lib, tmp_path):
+    """gb_write_binary -> gb_op_to_initial -> the deck reader gives back x and u."""
+    case = C.vortex(10, n_iter=1, dt=0.01)
+    d = str(tmp_path / "deck")
+    case.write(d)
+    L = _lib.lib()
+    xs = np.concatenate([np.asarray(x, np.float64) for x in case.x])
+    u = np.ascontiguousarray(case.u * 0.75)
+    dims = (ctypes.c_int * 2)(*case.size)
+    op = os.path.join(d, "op_00003.bin")
+    _lib.check(L.gb_write_binary(op.encode(), 2, 4, dims, xs.ctypes.data_as(_lib.DP), u.ctypes.data_as(_lib.DP)))
+    _lib.check(L.gb_op_to_initial(op.encode(), os.path.join(d, "initial.inp").encode()))
+    inp = Inputs(d)
+    assert np.array_equal(inp.u0, u.reshape(-1))
+    assert np.array_equal(inp.x, xs)
+    assert L.gb_op_to_initial(os.path.join(d, "solver.inp").encode(), os.path.join(d, "junk").encode()) == 3

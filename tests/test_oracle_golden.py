@@ -41,6 +41,15 @@ def test_oracle_rhs_matches_reference(oracle_lib, name):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_cfl_matches_reference(oracle_lib, name):
+    """<Model>ComputeCFL of the initial state, to the bit."""
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    case = CASES[name]()
+    P = O.Problem(case)
+    assert P.cfl(P.u0()) == float(g["cfl"])
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_steps_match_reference(oracle_lib, name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     case = CASES[name]()
