@@ -52,6 +52,7 @@ class GbConfig(ctypes.Structure):
         ("rk_c", ctypes.c_double * 4), ("dt", ctypes.c_double), ("n_iter", ctypes.c_int),
         ("file_op_iter", ctypes.c_int), ("weno_weights", ctypes.c_int), ("restart_iter", ctypes.c_int),
         ("screen_op_iter", ctypes.c_int), ("write_residual", ctypes.c_int),
+        ("zone_data", (ctypes.c_double * 8) * 12),
     ]
 
 

@@ -51,6 +51,9 @@ class Case:
     op_overwrite: str = "yes"       # solver.inp op_overwrite ("no": op_NNNNN.bin every file_op_iter)
     restart_iter: int = 0           # solver.inp restart_iter
     screen_op_iter: Optional[int] = None
+    # per-face boundary types: {(dim, face): (bctype, [values after the extents])};
+    # faces not listed take `bc`
+    bcs: Optional[dict] = None
 
     @property
     def ndims(self) -> int:
@@ -117,7 +120,8 @@ class Case:
                 ext = []
                 for e in range(nd):
                     ext += ["0", "0"] if e == d else [repr(lo[e]), repr(hi[e])]
-                rows.append(f"{self.bc} {d} {face} " + " ".join(ext))
+                bctype, vals = (self.bcs or {}).get((d, face), (self.bc, []))
+                rows.append(f"{bctype} {d} {face} " + " ".join(ext + [repr(float(v)) for v in vals]))
         return f"{len(rows)}\n" + "\n".join(rows) + "\n"
 
     def initial_bytes(self) -> bytes:

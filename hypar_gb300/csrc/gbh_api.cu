@@ -32,7 +32,7 @@ cudaError_t launch_unfused_ns3d(int, int, int, double*, const double*, const dou
                                 const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
 cudaError_t launch_visc(const double*, double*, double*, double*, const double*, const DevGeom&,
                         const ViscParams&, int, cudaStream_t);
-cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, cudaStream_t);
+cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, const double*, double, cudaStream_t);
 cudaError_t launch_finite_check(const double*, const DevGeom&, int, int*, cudaStream_t);
 cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
 }  // namespace gbh
@@ -137,7 +137,7 @@ static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
         if (k == z) use = true;
     if (use) {
       if (pr < 0) pr = prof_begin(s, GB_PROF_BC);
-      CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->stream));
+      CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->cfg.zone_data[z], s->cfg.gamma, s->stream));
     }
   }
   prof_end(s, pr);
@@ -185,9 +185,14 @@ int gbh_validate(const gb_config* c) {
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
-    if ((q[0] != GB_BC_PERIODIC && q[0] != GB_BC_EXTRAPOLATE) || q[1] < 0 || q[1] >= nd || (q[2] != 1 && q[2] != -1)) {
+    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SUPERSONIC_OUTFLOW || q[1] < 0 || q[1] >= nd ||
+        (q[2] != 1 && q[2] != -1)) {
       gbh_set_error("bad zone %d", z);
       return GB_ERR_ARG;
+    }
+    if (q[0] > GB_BC_DIRICHLET && nd < 2) {
+      gbh_set_error("zone %d: wall / inflow / outflow boundaries need Euler2D or NavierStokes3D", z);
+      return GB_ERR_UNSUPPORTED;
     }
     for (int d = 0; d < nd; d++) {
       int lo = -c->ghosts, hi = c->dim[d] + c->ghosts;
@@ -219,6 +224,8 @@ long long gbh_geometry(const gb_config& c, DevGeom& G, std::vector<int>* mem_zon
       for (int z = 0; z < c.nzones; z++)
         if (c.zones[z][1] == d && c.zones[z][2] == face) { cnt++; which = z; }
       bool full = false;
+      // only periodic and extrapolate (a copy of one interior cell) fold into the loads
+      if (cnt == 1 && c.zones[which][0] != GB_BC_PERIODIC && c.zones[which][0] != GB_BC_EXTRAPOLATE) cnt = 0;
       if (cnt == 1) {
         full = true;
         for (int e = 0; e < c.ndims; e++)

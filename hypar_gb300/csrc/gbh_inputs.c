@@ -554,13 +554,40 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         gbh_set_error("boundary.inp: bad zone %d", z);
         return GB_ERR_INPUT;
       }
-      int tcode = 0;
-      if (!strcmp(type, "periodic")) tcode = GB_BC_PERIODIC;
-      else if (!strcmp(type, "extrapolate")) tcode = GB_BC_EXTRAPOLATE;
-      else {
+      /* type-specific values after the extents (InitializeBoundaries.c:109-188) */
+      static const struct { const char *name; int code; int nvals; } bct[] = {
+          {"periodic", GB_BC_PERIODIC, 0},           {"extrapolate", GB_BC_EXTRAPOLATE, 0},
+          {"dirichlet", GB_BC_DIRICHLET, -1},        {"slip-wall", GB_BC_SLIP_WALL, -2},
+          {"noslip-wall", GB_BC_NOSLIP_WALL, -2},    {"subsonic-inflow", GB_BC_SUBSONIC_INFLOW, -3},
+          {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW, 1},
+          {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW, -4},
+          {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW, 0}};
+      int tcode = 0, nvals = 0;
+      for (size_t t = 0; t < sizeof(bct) / sizeof(bct[0]); t++)
+        if (!strcmp(type, bct[t].name)) {
+          tcode = bct[t].code;
+          /* -1: nvars values; -2: ndims; -3: 1 + ndims; -4: 2 + ndims */
+          nvals = bct[t].nvals == -1 ? c.nvars : bct[t].nvals == -2 ? c.ndims
+                : bct[t].nvals == -3 ? 1 + c.ndims : bct[t].nvals == -4 ? 2 + c.ndims : bct[t].nvals;
+        }
+      if (!tcode) {
         fclose(in);
         gb_inputs_free(res);
-        gbh_set_error("boundary type %s not supported (periodic, extrapolate)", type);
+        gbh_set_error("boundary type %s not supported", type);
+        return GB_ERR_UNSUPPORTED;
+      }
+      for (int k = 0; k < 8; k++) c.zone_data[z][k] = 0.0;
+      for (int k = 0; k < nvals && !bad; k++) bad = fscanf(in, "%lf", &c.zone_data[z][k]) != 1;
+      if (bad) {
+        fclose(in);
+        gb_inputs_free(res);
+        gbh_set_error("boundary.inp: zone %d (%s) lacks its values", z, type);
+        return GB_ERR_INPUT;
+      }
+      if (tcode > GB_BC_DIRICHLET && c.ndims < 2) {
+        fclose(in);
+        gb_inputs_free(res);
+        gbh_set_error("boundary type %s needs Euler2D or NavierStokes3D", type);
         return GB_ERR_UNSUPPORTED;
       }
       int *zz = c.zones[z];

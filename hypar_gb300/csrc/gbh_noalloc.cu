@@ -32,7 +32,7 @@ cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const do
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
-cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, cudaStream_t);
+cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, const double*, double, cudaStream_t);
 }  // namespace gbh
 
 using namespace gbh;
@@ -113,7 +113,7 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
 
   // As gb_RHSFunctionExplicit: every boundary zone fills u's ghost points in
   // place, then rhs (ghosts included) is cleared and its interior written.
-  for (int z = 0; z < c.nzones; z++) NA_CK(launch_bc_zone(u, G, c.nvars, c.zones[z], st));
+  for (int z = 0; z < c.nzones; z++) NA_CK(launch_bc_zone(u, G, c.nvars, c.zones[z], c.zone_data[z], c.gamma, st));
   NA_CK(cudaMemsetAsync(rhs, 0, nvals * sizeof(double), st));
 
   PhysParams pp;

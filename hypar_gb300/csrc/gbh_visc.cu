@@ -210,7 +210,51 @@ cudaError_t launch_visc(const double* u, double* Q, double* Gr, double* par, con
 // ---------------------------------------------------------------------------
 struct ZoneDev {
   int type, dim, face, is[3], ie[3];
+  double data[8];
+  double gamma;
 };
+
+// Ghost state from the mirror interior state w, for the wall and inflow /
+// outflow types (BCSlipWall.c, BCNoslipWall.c, BCSubsonicInflow.c,
+// BCSubsonicOutflow.c, BCSupersonicInflow.c, BCSupersonicOutflow.c; 2-D and 3-D
+// branches), in their operation order without contraction.
+template <int ND>
+__device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out) {
+  constexpr int NV = ND + 2;
+  const double gm1 = z.gamma - 1.0;
+  const double inv_gm1 = __ddiv_rn(1.0, gm1);
+  double rho = 0.0, vel[3] = {0.0, 0.0, 0.0}, P = 0.0;
+  if (z.type != GB_BC_SUPERSONIC_INFLOW) {
+    rho = w[0];
+    for (int d = 0; d < ND; d++) vel[d] = (ND == 3 && rho == 0.0) ? 0.0 : __ddiv_rn(w[1 + d], rho);
+    double vsq = __dadd_rn(__dmul_rn(vel[0], vel[0]), __dmul_rn(vel[1], vel[1]));
+    if (ND == 3) vsq = __dadd_rn(vsq, __dmul_rn(vel[2], vel[2]));
+    P = __dmul_rn(__dsub_rn(w[NV - 1], __dmul_rn(__dmul_rn(0.5, rho), vsq)), gm1);
+  }
+  double rg = rho, vg[3] = {vel[0], vel[1], vel[2]}, Pg = P;
+  switch (z.type) {
+    case GB_BC_SLIP_WALL: vg[z.dim] = __dsub_rn(__dmul_rn(2.0, z.data[z.dim]), vel[z.dim]); break;
+    case GB_BC_NOSLIP_WALL:
+      for (int d = 0; d < ND; d++) vg[d] = __dsub_rn(__dmul_rn(2.0, z.data[d]), vel[d]);
+      break;
+    case GB_BC_SUBSONIC_INFLOW:
+      rg = z.data[0];
+      for (int d = 0; d < ND; d++) vg[d] = z.data[1 + d];
+      break;
+    case GB_BC_SUBSONIC_OUTFLOW: Pg = z.data[0]; break;
+    case GB_BC_SUPERSONIC_INFLOW:
+      rg = z.data[0];
+      for (int d = 0; d < ND; d++) vg[d] = z.data[1 + d];
+      Pg = z.data[1 + ND];
+      break;
+    default: break;  // supersonic outflow: the interior state, energy recomputed
+  }
+  double vsq = __dadd_rn(__dmul_rn(vg[0], vg[0]), __dmul_rn(vg[1], vg[1]));
+  if (ND == 3) vsq = __dadd_rn(vsq, __dmul_rn(vg[2], vg[2]));
+  out[0] = rg;
+  for (int d = 0; d < ND; d++) out[1 + d] = __dmul_rn(rg, vg[d]);
+  out[NV - 1] = __dadd_rn(__dmul_rn(inv_gm1, Pg), __dmul_rn(__dmul_rn(0.5, rg), vsq));
+}
 
 __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
   int b[3] = {1, 1, 1};
@@ -225,21 +269,33 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
     is[d] = ig[d];
   }
   int dd = z.dim, N = G.dim[dd];
-  if (z.type == 1) is[dd] = (z.face == 1) ? ib[dd] + N - G.g : ib[dd];
-  else is[dd] = (z.face == 1) ? G.g - 1 - ib[dd] : N - ib[dd] - 1;
+  if (z.type == GB_BC_PERIODIC) is[dd] = (z.face == 1) ? ib[dd] + N - G.g : ib[dd];
+  else is[dd] = (z.face == 1) ? G.g - 1 - ib[dd] : N - ib[dd] - 1;  // the mirror interior point
   long long p1 = 0, p2 = 0;
   for (int d = 0; d < G.nd; d++) {
     p1 += (long long)(ig[d] + G.g) * G.stride[d];
     p2 += (long long)(is[d] + G.g) * G.stride[d];
   }
-  for (int v = 0; v < nv; v++) u[p1 * nv + v] = u[p2 * nv + v];
+  if (z.type == GB_BC_PERIODIC || z.type == GB_BC_EXTRAPOLATE) {
+    for (int v = 0; v < nv; v++) u[p1 * nv + v] = u[p2 * nv + v];
+  } else if (z.type == GB_BC_DIRICHLET) {
+    for (int v = 0; v < nv; v++) u[p1 * nv + v] = z.data[v];
+  } else {
+    double g[5];
+    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g);
+    else bc_ghost<3>(z, u + p2 * nv, g);
+    for (int v = 0; v < nv; v++) u[p1 * nv + v] = g[v];
+  }
 }
 
-cudaError_t launch_bc_zone(double* u, const DevGeom& G, int nv, const int* zone9, cudaStream_t s) {
+cudaError_t launch_bc_zone(double* u, const DevGeom& G, int nv, const int* zone9, const double* data8, double gamma,
+                           cudaStream_t s) {
   ZoneDev z;
   z.type = zone9[0];
   z.dim = zone9[1];
   z.face = zone9[2];
+  z.gamma = gamma;
+  for (int k = 0; k < 8; k++) z.data[k] = data8 ? data8[k] : 0.0;
   long long n = 1;
   for (int d = 0; d < 3; d++) {
     z.is[d] = zone9[3 + d];

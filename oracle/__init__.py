@@ -34,7 +34,14 @@ MODELS = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
 UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2}
 INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
-BCTYPE = {"periodic": 1, "extrapolate": 2}
+BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,
+          "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9}
+
+
+def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
+    """How many values boundary.inp gives after a zone's extents (InitializeBoundaries.c:109-188)."""
+    return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
+            "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims}.get(bctype, 0)
 
 _lib = None
 
@@ -65,6 +72,8 @@ def _bind(path):
     L.orc_problem_destroy.argtypes = [ctypes.c_void_p]
     L.orc_set_weights.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.orc_set_weights.restype = None
+    L.orc_set_zone_data.argtypes = [ctypes.c_void_p, ctypes.c_int, dp]
+    L.orc_set_zone_data.restype = None
     L.orc_cfl.argtypes = [ctypes.c_void_p, dp, ctypes.c_double]
     L.orc_cfl.restype = ctypes.c_double
     L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
@@ -151,7 +160,8 @@ def zones_from_boundary(rows, xs: Sequence[np.ndarray], g: int) -> np.ndarray:
     """rows: [(bctype, dim, face, [(xmin, xmax) per dim])] -> nzones x 9 int array."""
     out = []
     nd = len(xs)
-    for (bctype, dim, face, ext) in rows:
+    for row in rows:
+        bctype, dim, face, ext = row[:4]
         is_ = [0, 0, 0]
         ie = [1, 1, 1]
         for d in range(nd):
@@ -164,7 +174,8 @@ def zones_from_boundary(rows, xs: Sequence[np.ndarray], g: int) -> np.ndarray:
     return np.asarray(out, dtype=np.int32).reshape(-1, 9)
 
 
-def parse_boundary_inp(text: str, ndims: int):
+def parse_boundary_inp(text: str, ndims: int, nvars: int = 0):
+    """rows (bctype, dim, face, extents, values) of a boundary.inp."""
     tok = text.split()
     nz = int(tok[0])
     k = 1
@@ -176,7 +187,10 @@ def parse_boundary_inp(text: str, ndims: int):
         for _d in range(ndims):
             ext.append((float(tok[k]), float(tok[k + 1])))
             k += 2
-        rows.append((bctype, dim, face, ext))
+        nvals = bc_nvalues(bctype, ndims, nvars)
+        vals = [float(t) for t in tok[k:k + nvals]]
+        k += nvals
+        rows.append((bctype, dim, face, ext, vals))
     return rows
 
 
@@ -219,7 +233,7 @@ class Problem:
         xs = [np.asarray(x, np.float64) for x in case.x]
         self.dxinv = dxinv_from_grid(xs, ghosts)
         if boundary_rows is None:
-            boundary_rows = parse_boundary_inp(case.boundary_inp(), case.ndims)
+            boundary_rows = parse_boundary_inp(case.boundary_inp(), case.ndims, case.nvars)
         self.zones = zones_from_boundary(boundary_rows, xs, ghosts)
         Re = -1.0
         if case.model == "navierstokes3d" and case.Re is not None:
@@ -234,6 +248,11 @@ class Problem:
         if not self.h:
             raise RuntimeError("orc_problem_create failed")
         L.orc_set_weights(self.h, WEIGHTS[getattr(case, "weights", "js")])
+        for z, row in enumerate(boundary_rows):
+            vals = list(row[4]) if len(row) > 4 else []
+            data = np.zeros(8)
+            data[:len(vals)] = vals
+            L.orc_set_zone_data(self.h, z, _dp(data))
 
     def __del__(self):
         try:

@@ -80,6 +80,11 @@ orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts
 
 void orc_set_weights(orc_problem *p, int weights) { p->weights = weights; }
 
+void orc_set_zone_data(orc_problem *p, int z, const double *data) {
+  if (z < 0 || z >= p->nzones) return;
+  for (int k = 0; k < 8; k++) p->zones[z].data[k] = data[k];
+}
+
 void orc_problem_destroy(orc_problem *p) {
   if (!p) return;
   free(p->dxinv);
@@ -111,6 +116,57 @@ static long pidx(const orc_problem *p, const long *s, const int *i) {
 
 /* BCPeriodicU (src/BoundaryConditions/BCPeriodic.c:36-56, single rank along dim)
  * and BCExtrapolateU (src/BoundaryConditions/BCExtrapolate.c:29-46, a mirror copy). */
+/* Ghost state of the wall and inflow / outflow types from the mirror interior
+ * state w, 2-D (Euler2D/NavierStokes2D flow variables) and 3-D branches of
+ * BCSlipWall.c, BCNoslipWall.c, BCSubsonicInflow.c, BCSubsonicOutflow.c,
+ * BCSupersonicInflow.c and BCSupersonicOutflow.c. */
+static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, double *out) {
+  double inv_gamma_m1 = 1.0 / (gamma - 1.0);
+  double rho = 0, vel[3] = {0, 0, 0}, energy, pressure = 0, vsq;
+  if (b->type != ORC_BC_SUPERSONIC_INFLOW) {
+    rho = w[0];
+    if (nd == 2) {
+      vel[0] = w[1] / rho;
+      vel[1] = w[2] / rho;
+      energy = w[3];
+      vsq = (vel[0] * vel[0]) + (vel[1] * vel[1]);
+    } else {
+      vel[0] = (rho == 0) ? 0 : w[1] / rho;
+      vel[1] = (rho == 0) ? 0 : w[2] / rho;
+      vel[2] = (rho == 0) ? 0 : w[3] / rho;
+      energy = w[4];
+      vsq = vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2];
+    }
+    pressure = (energy - 0.5 * rho * vsq) * (gamma - 1.0);
+  }
+  double rho_g = rho, v_g[3] = {vel[0], vel[1], vel[2]}, p_g = pressure;
+  switch (b->type) {
+    case ORC_BC_SLIP_WALL: v_g[b->dim] = 2.0 * b->data[b->dim] - vel[b->dim]; break;
+    case ORC_BC_NOSLIP_WALL:
+      for (int d = 0; d < nd; d++) v_g[d] = 2.0 * b->data[d] - vel[d];
+      break;
+    case ORC_BC_SUBSONIC_INFLOW:
+      rho_g = b->data[0];
+      for (int d = 0; d < nd; d++) v_g[d] = b->data[1 + d];
+      break;
+    case ORC_BC_SUBSONIC_OUTFLOW: p_g = b->data[0]; break;
+    case ORC_BC_SUPERSONIC_INFLOW:
+      rho_g = b->data[0];
+      for (int d = 0; d < nd; d++) v_g[d] = b->data[1 + d];
+      p_g = b->data[1 + nd];
+      break;
+    case ORC_BC_SUPERSONIC_OUTFLOW: break;
+    default: return 1;
+  }
+  double e_g;
+  if (nd == 2) e_g = inv_gamma_m1 * p_g + 0.5 * rho_g * (v_g[0] * v_g[0] + v_g[1] * v_g[1]);
+  else e_g = inv_gamma_m1 * p_g + 0.5 * rho_g * (v_g[0] * v_g[0] + v_g[1] * v_g[1] + v_g[2] * v_g[2]);
+  out[0] = rho_g;
+  for (int d = 0; d < nd; d++) out[1 + d] = rho_g * v_g[d];
+  out[nd + 1] = e_g;
+  return 0;
+}
+
 int orc_apply_bc(const orc_problem *p, double *u) {
   long s[3];
   strides_wg(p, s);
@@ -134,14 +190,22 @@ int orc_apply_bc(const orc_problem *p, double *u) {
       if (b->type == ORC_BC_PERIODIC) {
         if (b->face == 1) isrc[dd] = ib[dd] + N - g;
         else isrc[dd] = ib[dd];
-      } else if (b->type == ORC_BC_EXTRAPOLATE) {
+      } else {
+        /* extrapolate and the wall / inflow / outflow types read the mirror point */
         if (b->face == 1) isrc[dd] = g - 1 - ib[dd];
         else isrc[dd] = N - ib[dd] - 1;
+      }
+      long p1 = pidx(p, s, ig), p2 = pidx(p, s, isrc);
+      if (b->type == ORC_BC_PERIODIC || b->type == ORC_BC_EXTRAPOLATE) {
+        for (int v = 0; v < nv; v++) u[nv * p1 + v] = u[nv * p2 + v];
+      } else if (b->type == ORC_BC_DIRICHLET) {
+        /* BCDirichletU (BCDirichlet.c:27-41) */
+        for (int v = 0; v < nv; v++) u[nv * p1 + v] = b->data[v];
+      } else if (nd == 2 || nd == 3) {
+        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1)) return 1;
       } else {
         return 1;
       }
-      long p1 = pidx(p, s, ig), p2 = pidx(p, s, isrc);
-      for (int v = 0; v < nv; v++) u[nv * p1 + v] = u[nv * p2 + v];
     }
   }
   return 0;

@@ -22,7 +22,9 @@ extern "C" {
 enum { ORC_EULER1D = 1, ORC_EULER2D = 2, ORC_NS3D = 3 };
 enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2 };
 enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
-enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2 };
+enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
+       ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,
+       ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9 };
 
 /* One boundary zone, as DomainBoundary after CalculateLocalExtent
  * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index
@@ -31,6 +33,7 @@ enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2 };
 typedef struct {
   int type, dim, face;
   int is[3], ie[3];
+  double data[8];   /* boundary.inp values after the extents (Dirichlet values, wall velocity, ...) */
 } orc_zone;
 
 typedef struct {
@@ -48,6 +51,8 @@ typedef struct {
  * Yamaleev-Carpenter, or the optimal weights (no_limiting). */
 enum { ORC_WENO_JS = 0, ORC_WENO_MAPPED = 1, ORC_WENO_BORGES = 2, ORC_WENO_YC = 3, ORC_WENO_NONE = 4 };
 void orc_set_weights(orc_problem *p, int weights);
+/* The values boundary.inp gives for zone z after its extents (8 doubles). */
+void orc_set_zone_data(orc_problem *p, int z, const double *data);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

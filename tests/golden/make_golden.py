@@ -50,7 +50,27 @@ CASES = {
     "tgv12_char_rf_mapped_rk4": lambda: _w(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
                                                  upwinding="rf-char"), "mapped"),
     "tgv12_comp_roe_borges_rk4": lambda: _w(C.tgv(12, n_iter=3, dt=0.02), "borges"),
+    # wall, inflow / outflow and Dirichlet boundaries (applied in memory before every stage)
+    "vortex24_char_roe_slipwall": lambda: _b(C.vortex(24, n_iter=5, dt=0.02), {
+        (1, 1): ("slip-wall", [0.0, 0.0]), (1, -1): ("slip-wall", [0.0, 0.0])}),
+    "vortex24_comp_llf_subsonic_io_rk4": lambda: _b(C.vortex(24, n_iter=5, dt=0.02, interp="components",
+                                                             upwinding="llf-char", scheme="44"), {
+        (0, 1): ("subsonic-inflow", [1.0, 0.5, 0.0]), (0, -1): ("subsonic-outflow", [1.0])}),
+    "vortex24_comp_roe_supersonic_dirichlet": lambda: _b(C.vortex(24, n_iter=5, dt=0.02, interp="components"), {
+        (0, 1): ("supersonic-inflow", [1.0, 0.5, 0.0, 1.0]), (0, -1): ("supersonic-outflow", []),
+        (1, 1): ("dirichlet", [1.0, 0.5, 0.0, 2.625]), (1, -1): ("dirichlet", [1.0, 0.5, 0.0, 2.625])}),
+    "tgv12_comp_roe_noslip_rk4": lambda: _b(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), {
+        (2, 1): ("noslip-wall", [0.0, 0.0, 0.0]), (2, -1): ("noslip-wall", [0.0, 0.0, 0.0])}),
+    "tgv12_char_llf_slipwall_io_rk4": lambda: _b(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
+                                                      upwinding="llf-char", perturb=0.05), {
+        (0, 1): ("subsonic-inflow", [1.0, 0.1, 0.0, 0.0]), (0, -1): ("subsonic-outflow", [1.0 / 1.4]),
+        (1, 1): ("slip-wall", [0.0, 0.0, 0.0]), (1, -1): ("slip-wall", [0.0, 0.0, 0.0])}),
 }
+
+
+def _b(case, bcs):
+    case.bcs = bcs
+    return case
 
 
 def _w(case, weights):

@@ -83,7 +83,7 @@ def test_reader_errors(built_lib, tmp_path):
     case = C.vortex(12, n_iter=1, dt=0.01)
     d = tmp_path / "b"
     case.write(str(d))
-    t = open(d / "boundary.inp").read().replace("periodic", "slip-wall", 1)
+    t = open(d / "boundary.inp").read().replace("periodic", "sponge", 1)
     open(d / "boundary.inp", "w").write(t)
     _expect(4, str(d))
     d = tmp_path / "c"
@@ -172,3 +172,25 @@ def test_op_to_initial_round_trip(built_lib, tmp_path):
     assert np.array_equal(inp.u0, u.reshape(-1))
     assert np.array_equal(inp.x, xs)
     assert L.gb_op_to_initial(os.path.join(d, "solver.inp").encode(), os.path.join(d, "junk").encode()) == 3
+
+
+def test_reader_boundary_values(built_lib, tmp_path):
+    """Wall / inflow / outflow / Dirichlet zones: type codes and the values after the extents."""
+    case = C.vortex(12, n_iter=1, dt=0.01)
+    case.bcs = {(0, 1): ("supersonic-inflow", [1.0, 0.5, 0.25, 1.0]), (0, -1): ("subsonic-outflow", [0.9]),
+                (1, 1): ("slip-wall", [0.0, 0.125]), (1, -1): ("dirichlet", [1.0, 0.5, 0.0, 2.625])}
+    d = str(tmp_path / "deck")
+    case.write(d)
+    c = Inputs(d).config
+    codes = [c.zones[z][0] for z in range(c.nzones)]
+    assert codes == [8, 7, 4, 3]
+    assert list(c.zone_data[0])[:4] == [1.0, 0.5, 0.25, 1.0]
+    assert c.zone_data[1][0] == 0.9
+    assert list(c.zone_data[2])[:2] == [0.0, 0.125]
+    assert list(c.zone_data[3])[:4] == [1.0, 0.5, 0.0, 2.625]
+    # the wall / inflow / outflow types are 2-D / 3-D only (the reference's 1-D branches are incomplete)
+    sod = C.sod(16, n_iter=1, dt=1e-3)
+    sod.bcs = {(0, 1): ("slip-wall", [0.0])}
+    d = str(tmp_path / "sod")
+    sod.write(d)
+    _expect(4, d)
