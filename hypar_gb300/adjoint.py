@@ -101,31 +101,34 @@ class Adjoint:
         check(lib().gb_adjoint_info(self._h, ctypes.byref(L), ctypes.byref(n), ctypes.byref(r), ctypes.byref(b)))
         return {"segment_len": L.value, "segments": n.value, "recomputed_steps": r.value, "bytes": b.value}
 
-    def autotune(self, u, reps: int = 3, candidates=(2, 3, 4, 6, 8, 12, 16, 24, 32)):
-        """Choose the adjoint kernel's segment length per direction by timing
-        right-hand-side VJPs of the state u (one direction at a time, the other
-        held).  Returns [seg_x, seg_y]."""
+    def autotune(self, u, reps: int = 3, candidates=(2, 3, 4, 6, 8, 12, 16, 24, 32), blocks=(32, 64, 128)):
+        """Choose the adjoint kernel's launch shape by timing right-hand-side
+        VJPs of the state u: the block size (both directions share the launch),
+        then the segment length per direction (one at a time, the other held),
+        twice over.  Returns [seg_x, seg_y, block]."""
         import torch
         kb, ub = self.empty(), self.empty()
         kb.normal_()
         stream = torch.cuda.current_stream()
-        for which in (2, 3):
-            best = None
-            for seg in candidates:
-                self.set_launch(which, seg)
-                self.rhs_vjp(u, kb, ub)
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                for _ in range(reps):
-                    check(lib().gb_adjoint_rhs_vjp(self._h, _p(u), _p(kb), _p(ub)))
-                b.record(stream)
-                self.sync()
-                torch.cuda.synchronize()
-                t = a.elapsed_time(b)
-                if best is None or t < best[0]:
-                    best = (t, seg)
-            self.set_launch(which, best[1])
-        return [self.get_launch(2)[0], self.get_launch(3)[0]]
+
+        def timed():
+            self.rhs_vjp(u, kb, ub)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                check(lib().gb_adjoint_rhs_vjp(self._h, _p(u), _p(kb), _p(ub)))
+            b.record(stream)
+            self.sync()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b)
+
+        for _ in range(2):
+            best = min((timed_with(self, 2, None, blk, timed), blk) for blk in blocks)
+            self.set_launch(2, 0, best[1])
+            for which in (2, 3):
+                best = min((timed_with(self, which, seg, None, timed), seg) for seg in candidates)
+                self.set_launch(which, best[1])
+        return [self.get_launch(2)[0], self.get_launch(3)[0], self.get_launch(2)[1]]
 
     def _pre(self):
         import torch
@@ -155,6 +158,11 @@ class Adjoint:
         self._pre()
         check(lib().gb_adjoint_tlm(self._h, _p(u0), _p(du0), _p(uT), _p(duT)))
         self.sync()
+
+
+def timed_with(adj, which, seg, block, fn):
+    adj.set_launch(which, seg or 0, block or 0)
+    return fn()
 
 
 def _functions():

@@ -695,6 +695,7 @@ struct gb_adjoint {
   PhysParams pp;
   HypLaunch hl[2];
   int vjp_seg[2] = {8, 8};
+  int vjp_block = 128;
   int device = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -759,7 +760,8 @@ static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* U
   int s0 = a->vjp_seg[0], s1 = a->vjp_seg[1];
   int n0s = (G.dim[0] + s0 - 1) / s0, n1s = (G.dim[1] + s1 - 1) / s1;
   long long nthr = (long long)G.dim[1] * n0s + (long long)G.dim[0] * n1s;
-  rhs_vjp_kernel<<<(unsigned)((nthr + 127) / 128), 128, 0, a->stream>>>(
+  const int blk = a->vjp_block;
+  rhs_vjp_kernel<<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
       U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s);
   AK(cudaGetLastError());
   return GB_OK;
@@ -993,8 +995,12 @@ extern "C" int gb_adjoint_set_launch(gb_adjoint* a, int which, int seg, int bloc
       if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
       a->hl[which].block = block;
     }
-  } else if (seg > 0) {
-    a->vjp_seg[which - 2] = seg;
+  } else {
+    if (seg > 0) a->vjp_seg[which - 2] = seg;
+    if (block > 0) {  // one block size for the adjoint kernel's single launch
+      if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
+      a->vjp_block = block;
+    }
   }
   return GB_OK;
 }
@@ -1006,7 +1012,7 @@ extern "C" int gb_adjoint_get_launch(const gb_adjoint* a, int which, int* seg, i
     *block = a->hl[which].block;
   } else {
     *seg = a->vjp_seg[which - 2];
-    *block = 128;
+    *block = a->vjp_block;
   }
   return GB_OK;
 }

@@ -537,11 +537,20 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
       segs.push_back(sg);
     }
     for (int sg : {8, 16, 24, 32, 48, 64}) segs.push_back(sg);
+    // Small grids (at most four waves of 4 warps per SM at one interface per
+    // thread) cannot fill the SMs with long segments: there, also 1-3
+    // interfaces per thread and 32-thread blocks, spreading the few threads
+    // over more SMs at the price of recomputing the segments' first interfaces.
+    const bool small = (double)ntrans * N <= 4.0 * sms * 4 * 32;
+    if (small)
+      for (int sg : {1, 2, 3}) segs.push_back(sg);
+    std::vector<int> blocks = {128, 64};
+    if (small) blocks.push_back(32);
     double best = 1e30;
     HypLaunch bestL = s->hl[d];
     for (int sg : segs) {
-      if (sg < 4 || sg > N) continue;
-      for (int blk : {128, 64}) {
+      if (sg < (small ? 1 : 4) || sg > N) continue;
+      for (int blk : blocks) {
         s->hl[d].seg = sg;
         s->hl[d].block = blk;
         rc = gbh_rk_step(s);  // warm

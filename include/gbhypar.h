@@ -267,7 +267,8 @@ void gb_adjoint_destroy(gb_adjoint *a);
 int gb_adjoint_set_stream(gb_adjoint *a, void *stream);
 int gb_adjoint_sync(gb_adjoint *a);
 /* Launch shape: which = 0, 1 the fused forward kernels along x, y (seg,
- * block); 2, 3 the adjoint kernel's segment length along x, y. */
+ * block); 2, 3 the adjoint kernel's segment length along x, y (block: the
+ * threads per block of its single launch, shared by 2 and 3). */
 int gb_adjoint_set_launch(gb_adjoint *a, int which, int seg, int block);
 int gb_adjoint_get_launch(const gb_adjoint *a, int which, int *seg, int *block);
 /* Segment length, number of segments, steps recomputed by the last backward

@@ -91,6 +91,20 @@ def test_rhs_weights_match_oracle(built_lib, oracle_lib, tmp_path, model, interp
     assert relerr(s.get_state(), refN) <= STEP_TOL
 
 
+@pytest.mark.parametrize("seg,block", [(1, 32), (2, 32), (3, 64), (5, 128)])
+@pytest.mark.parametrize("model", ["euler1d", "euler2d", "navierstokes3d"])
+def test_short_segments_match_oracle(built_lib, oracle_lib, tmp_path, model, seg, block):
+    """Launch shapes of 1-5 interfaces per thread (small grids) give the oracle's steps."""
+    case = make(model, "characteristic", "roe", n_iter=3)
+    s = solver_for(case, tmp_path)
+    for d in range(len(case.size)):
+        s.set_launch(d, seg, block)
+    s.step(case.n_iter)
+    P = O.Problem(case)
+    ref = O.interior(P.rk(P.u0(), case.n_iter), case.size, case.nvars, 3)
+    assert relerr(s.get_state(), ref.reshape(-1)) <= STEP_TOL
+
+
 @pytest.mark.parametrize("model,interp,upw", [c for c in COMBOS if c[2] != "rf-char"])
 def test_steps_match_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw):
     case = make(model, interp, upw, n_iter=6)
