@@ -345,10 +345,13 @@ __device__ __forceinline__ void terms_at(const AdjTerms& t, long long off, doubl
 // adjoint of its state (ab) and of its flux (fbb); a cell leaving the window
 // is finished: u_bar += ab + (df/du)^T fbb, added atomically at the folded
 // index (neighbouring segments and the other direction add to the same cells).
+// tape: the forward kernel's reconstructed states uL, uR of this direction
+// (StageEpi::tape layout), read instead of recomputed when present.
 template <int D>
 __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const AdjTerms& kt, double* Ub,
                                             const double* __restrict__ dxinv, const DevGeom& G,
-                                            const PhysParams& pp, int seg, long long tr, int sg) {
+                                            const PhysParams& pp, int seg, long long tr, int sg,
+                                            const double* __restrict__ tape) {
   constexpr int T = 1 - D;
   const long long pbase = (long long)(tr + G.g) * G.stride[T] + (long long)G.g * G.stride[D];
   const int N = G.dim[D];
@@ -412,12 +415,21 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
       }
     }
     double uL[NV2], uR[NV2];
+    if (tape) {
+      const double* t = tape + (tr * (N + 1) + I) * 8;
 #pragma unroll
-    for (int v = 0; v < NV2; v++) {
-      double su[6];
+      for (int v = 0; v < NV2; v++) {
+        uL[v] = t[v];
+        uR[v] = t[4 + v];
+      }
+    } else {
 #pragma unroll
-      for (int p = 0; p < 6; p++) su[p] = wu[p][v];
-      weno5_pair(su, su, eps4, uL[v], uR[v]);
+      for (int v = 0; v < NV2; v++) {
+        double su[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) su[p] = wu[p][v];
+        weno5_pair(su, su, eps4, uL[v], uR[v]);
+      }
     }
     double uLb[NV2] = {0.0, 0.0, 0.0, 0.0}, uRb[NV2] = {0.0, 0.0, 0.0, 0.0};
     roe_vjp<D>(uL, uR, Fb, uLb, uRb, pp);
@@ -448,14 +460,15 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
 // [0, n0) walk x-lines, [n0, n0 + n1) y-lines.
 __global__ void __launch_bounds__(128)
 rhs_vjp_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
-               const double* __restrict__ dx1, DevGeom G, PhysParams pp, int seg0, int nseg0, int seg1, int nseg1) {
+               const double* __restrict__ dx1, DevGeom G, PhysParams pp, int seg0, int nseg0, int seg1, int nseg1,
+               const double* __restrict__ tape0, const double* __restrict__ tape1) {
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n0 = (long long)G.dim[1] * nseg0, n1 = (long long)G.dim[0] * nseg1;
   if (tid < n0) {
-    vjp_segment<0>(U, kt, Ub, dx0, G, pp, seg0, tid % G.dim[1], (int)(tid / G.dim[1]));
+    vjp_segment<0>(U, kt, Ub, dx0, G, pp, seg0, tid % G.dim[1], (int)(tid / G.dim[1]), tape0);
   } else if (tid < n0 + n1) {
     const long long t = tid - n0;
-    vjp_segment<1>(U, kt, Ub, dx1, G, pp, seg1, t % G.dim[0], (int)(t / G.dim[0]));
+    vjp_segment<1>(U, kt, Ub, dx1, G, pp, seg1, t % G.dim[0], (int)(t / G.dim[0]), tape1);
   }
 }
 
@@ -712,6 +725,8 @@ struct gb_adjoint {
   // into the other on a second stream.
   std::vector<double*> su[2];
   std::vector<double*> sP[2];
+  std::vector<double*> sT[2];     // interface tapes of every stage of every step, [(i*4 + s)*2 + d]
+  double* tblock2 = nullptr;      // their allocation
   int nbuf = 1;
   cudaStream_t aux = nullptr;     // recomputation stream
   cudaEvent_t ev_start = nullptr;
@@ -755,14 +770,15 @@ static int adj_lincomb(gb_adjoint* a, double* out, const double* base, const Adj
   return GB_OK;
 }
 
-static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* Ub) {
+static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* Ub, double* const* tape = nullptr) {
   const DevGeom& G = a->G;
   int s0 = a->vjp_seg[0], s1 = a->vjp_seg[1];
   int n0s = (G.dim[0] + s0 - 1) / s0, n1s = (G.dim[1] + s1 - 1) / s1;
   long long nthr = (long long)G.dim[1] * n0s + (long long)G.dim[0] * n1s;
   const int blk = a->vjp_block;
   rhs_vjp_kernel<<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
-      U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s);
+      U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s,
+      tape ? tape[0] : nullptr, tape ? tape[1] : nullptr);
   AK(cudaGetLastError());
   return GB_OK;
 }
@@ -778,7 +794,10 @@ static int adj_jvp(gb_adjoint* a, const double* U, const double* dU, double* K, 
 
 // One fused Runge-Kutta step uin -> uout (distinct arrays) keeping the stage
 // states in P[1..ns-1] (the same launches as the solver's step).
-static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double* uout, double* const* P) {
+// tapes (optional): per stage s and direction d, tapes[2 s + d] receives the
+// reconstructed interface states for the adjoint kernel.
+static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double* uout, double* const* P,
+                    double* const* tapes = nullptr) {
   const gb_config& c = a->cfg;
   const int ns = c.rk_nstages;
   const double dt = c.dt;
@@ -808,6 +827,7 @@ static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double*
       StageEpi e = ep;
       e.first = (d == 0);
       e.last = (d == 1);
+      e.tape = tapes ? tapes[2 * st + d] : nullptr;
       AK(launch_hyp_euler2d(d, c.interp, c.upwind, U, a->H, a->d_dxinv + a->dx_off[d], a->G, a->pp, e, a->hl[d],
                             strm));
     }
@@ -821,7 +841,7 @@ static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double*
 // a->ubar, the adjoint of its result, leaves the adjoint of its input in a->ubar:
 //   kbar_s = dt b_s ubar + sum_{t>s} dt A_ts Ubar_t,  Ubar_s = J(U_s)^T kbar_s,
 //   ubar  += sum_s Ubar_s.
-static int adj_back_step(gb_adjoint* a, const double* const* U) {
+static int adj_back_step(gb_adjoint* a, const double* const* U, double* const* tapes) {
   const gb_config& c = a->cfg;
   const int ns = c.rk_nstages;
   const double dt = c.dt;
@@ -837,7 +857,7 @@ static int adj_back_step(gb_adjoint* a, const double* const* U) {
         kt.c[kt.n++] = dt * c.rk_A[4 * t + s];
       }
     if (kt.n == 0) continue;
-    int rc = adj_vjp(a, U[s], kt, a->Ub[s]);
+    int rc = adj_vjp(a, U[s], kt, a->Ub[s], tapes ? tapes + 2 * s : nullptr);
     if (rc) return rc;
   }
   adj_gather_kernel<<<interior_grid(a), 256, 0, a->stream>>>(a->ubar, a->Ub[0], a->Ub[1], a->Ub[2], a->Ub[3], ns,
@@ -851,6 +871,7 @@ static int adj_back_step(gb_adjoint* a, const double* const* U) {
 static int segbuf(const gb_adjoint* a, int j) { return (a->nseg - 1 - j) & (a->nbuf - 1); }
 static double* ustate(gb_adjoint* a, int j, int i) { return i == 0 ? a->ck[j] : a->su[segbuf(a, j)][i]; }
 static double* const* stages(gb_adjoint* a, int b, int i) { return &a->sP[b][(size_t)i * 4]; }
+static double* const* tapes(gb_adjoint* a, int b, int i) { return &a->sT[b][(size_t)i * 8]; }
 
 extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int nsteps, int ncheck, int device,
                                  gb_adjoint** out) {
@@ -902,13 +923,19 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->nbuf = a->nseg > 1 ? 2 : 1;
   size_t narr = (size_t)a->nseg + (size_t)a->nbuf * ((a->seglen + 1) + (size_t)a->seglen * (ns - 1)) + 1 + 1 + 4 + 1;
   a->bytes = narr * a->nvals * sizeof(double);
+  // interface tapes: per buffer, step and stage, uL and uR (8 values) at every
+  // interface of both directions
+  const size_t tape_x = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) * 8, tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * 8;
+  const size_t tape_bytes = (size_t)a->nbuf * a->seglen * ns * (tape_x + tape_y) * sizeof(double);
+  a->bytes += tape_bytes;
   if (device >= 0) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { gbh_set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); delete a; return GB_ERR_CUDA; }
   }
   cudaGetDevice(&a->device);
-  cudaError_t e = cudaMalloc((void**)&a->block, a->bytes);
-  if (e == cudaSuccess) e = cudaMemset(a->block, 0, a->bytes);
+  cudaError_t e = cudaMalloc((void**)&a->block, a->bytes - tape_bytes);
+  if (e == cudaSuccess) e = cudaMemset(a->block, 0, a->bytes - tape_bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&a->tblock2, tape_bytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&a->d_dxinv, ndx * sizeof(double));
   if (e == cudaSuccess) e = cudaMemcpy(a->d_dxinv, dxinv, ndx * sizeof(double), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking);
@@ -936,6 +963,17 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
     for (int i = 0; i < a->seglen; i++)
       for (int t = 1; t < ns; t++) a->sP[b][(size_t)i * 4 + t] = take();
   }
+  double* tp = a->tblock2;
+  for (int b = 0; b < a->nbuf; b++) {
+    a->sT[b].assign((size_t)a->seglen * 8, nullptr);
+    for (int i = 0; i < a->seglen; i++)
+      for (int t = 0; t < ns; t++) {
+        a->sT[b][((size_t)i * 4 + t) * 2 + 0] = tp;
+        tp += tape_x;
+        a->sT[b][((size_t)i * 4 + t) * 2 + 1] = tp;
+        tp += tape_y;
+      }
+  }
   a->acc = take();
   a->H = take();
   for (int s = 0; s < 4; s++) a->Ub[s] = take();
@@ -960,6 +998,7 @@ extern "C" void gb_adjoint_destroy(gb_adjoint* a) {
   if (a->aux) cudaStreamDestroy(a->aux);
   cudaFree(a->block);
   cudaFree(a->tblock);
+  cudaFree(a->tblock2);
   cudaFree(a->d_dxinv);
   if (a->own_stream) cudaStreamDestroy(a->stream);
   delete a;
@@ -1056,17 +1095,19 @@ extern "C" int gb_adjoint_forward(gb_adjoint* a, const double* u0, double* uT) {
       const double* uin;
       double* uout;
       double* const* P;
+      double* const* T = nullptr;
       if (last) {
-        // the last segment keeps every state for the backward sweep
+        // the last segment keeps every state (and interface tape) for the backward sweep
         uin = ustate(a, j, i);
         uout = a->su[bl][i + 1];
         P = stages(a, bl, i);
+        T = tapes(a, bl, i);
       } else {
         uin = i == 0 ? a->ck[j] : a->su[bt][1 + (i & 1)];
         uout = (i + 1 == len) ? a->ck[j + 1] : a->su[bt][1 + ((i + 1) & 1)];
         P = stages(a, bt, 0);
       }
-      int rc = adj_step(a, a->stream, uin, uout, P);
+      int rc = adj_step(a, a->stream, uin, uout, P, T);
       if (rc) return rc;
     }
   }
@@ -1094,7 +1135,7 @@ extern "C" int gb_adjoint_backward(gb_adjoint* a, const double* ubarT, double* u
       const int jr = j - 1, b = segbuf(a, jr);
       if (jr + 2 <= a->nseg - 1) AK(cudaStreamWaitEvent(a->aux, a->ev_back[jr + 2], 0));
       for (int i = 0; i < a->seglen; i++) {
-        int rc = adj_step(a, a->aux, ustate(a, jr, i), a->su[b][i + 1], stages(a, b, i));
+        int rc = adj_step(a, a->aux, ustate(a, jr, i), a->su[b][i + 1], stages(a, b, i), tapes(a, b, i));
         if (rc) return rc;
       }
       AK(cudaEventRecord(a->ev_rec[jr], a->aux));
@@ -1106,7 +1147,7 @@ extern "C" int gb_adjoint_backward(gb_adjoint* a, const double* ubarT, double* u
     for (int i = len - 1; i >= 0; i--) {
       const double* U[4];
       for (int t = 0; t < ns; t++) U[t] = (t == 0 || !a->touched[t]) ? ustate(a, j, i) : a->sP[b][(size_t)i * 4 + t];
-      int rc = adj_back_step(a, U);
+      int rc = adj_back_step(a, U, tapes(a, b, i));
       if (rc) return rc;
     }
     AK(cudaEventRecord(a->ev_back[j], a->stream));

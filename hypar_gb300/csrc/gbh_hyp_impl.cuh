@@ -248,6 +248,7 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
                                             int sg) {
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  const long long line = tr;
 
   long long pbase = (long long)G.g * G.stride[DIR];
 #pragma unroll
@@ -325,6 +326,14 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
         } else {
           wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
+        }
+      }
+      if (M == MODEL_EULER2D && ep.tape) {
+        double* t = ep.tape + (line * (N + 1) + I) * 8;
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          t[v] = uL[v];
+          t[4 + v] = uR[v];
         }
       }
       upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);

@@ -50,6 +50,10 @@ struct StageEpi {
   double* uout;    // where the last stage writes the new solution
   double* acc;
   double* P[4];
+  // Euler2D component-wise only: when set, the reconstructed interface states
+  // uL, uR of this direction are written here, 8 values per interface at
+  // ((line * (N + 1)) + interface) * 8 (the adjoint reads them back).
+  double* tape;
 };
 
 // NavierStokes3D viscous-term constants (NavierStokes3DParabolicFunction.c:76-79).
