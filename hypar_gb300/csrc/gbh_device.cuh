@@ -13,7 +13,7 @@
 namespace gbh {
 
 enum { MODEL_EULER1D = 1, MODEL_EULER2D = 2, MODEL_NS3D = 3 };
-enum { UPW_ROE = 0, UPW_LLF = 1, UPW_RF = 2 };
+enum { UPW_ROE = 0, UPW_LLF = 1, UPW_RF = 2, UPW_RUS = 3 };
 
 template <int M> struct ModelTraits;
 template <> struct ModelTraits<MODEL_EULER1D> { static constexpr int NV = 3, ND = 1; };

@@ -50,8 +50,24 @@ template <int M, bool CHAR, int UPW>
 struct NeedCC {
   // cell-centre Roe average needed: characteristic WENO (WENOFifthOrderCalculateWeights.c:832),
   // Euler1D upwinding (Euler1DUpwind.c:74, :259), NavierStokes3D Roe (NavierStokes3DUpwind.c:90)
-  static constexpr bool value = CHAR || (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE);
+  static constexpr bool value = CHAR || (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE) ||
+                                (UPW == UPW_RUS);
 };
+
+// Rusanov's wave speed |v_dir| + c of a cell-centre state (NavierStokes3DUpwind.c:392-403);
+// Euler1DUpwindRusanov takes c = gamma P / rho, without the square root
+// (Euler1DUpwind.c:394-404), which is kept.
+template <int M, int DIR>
+__device__ __forceinline__ double rusanov_speed(const Prim<M>& q, const PhysParams& pp) {
+  const double c2 = pp.gamma * q.P * q.rinv;
+  return (M == MODEL_EULER1D ? c2 : nr_sqrt(c2)) + fabs(q.vel[DIR]);
+}
+
+// The same for the Roe average of the two cell-centre states (eigen-system E).
+template <int M>
+__device__ __forceinline__ double rusanov_speed_avg(const Eig& E) {
+  return (M == MODEL_EULER1D ? E.a * E.a : E.a) + fabs(E.un);
+}
 
 // Upwind flux at one interface from the reconstructed fL, fR, uL, uR and the
 // two cell-centre neighbours (their Roe-average ingredients `cl`, `cr` and,
@@ -61,6 +77,15 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
                                              const double* uR, const Eig& Ecc, const CellAux<M>& cl,
                                              const CellAux<M>& cr, const PhysParams& pp, double* fI) {
   constexpr int NV = ModelTraits<M>::NV;
+  if (UPW == UPW_RUS) {
+    // Rusanov (Euler1DUpwind.c:362-424, NavierStokes3DUpwind.c:349-428):
+    // fI = (fL+fR)/2 - alpha (uR-uL)/2, alpha = max of |v|+c over the two
+    // cell-centre states and their Roe average (times kappa = 1 without gravity)
+    const double alpha = fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
+#pragma unroll
+    for (int v = 0; v < NV; v++) fI[v] = fma(-alpha, 0.5 * (uR[v] - uL[v]), 0.5 * (fL[v] + fR[v]));
+    return;
+  }
   if (UPW == UPW_ROE) {
     // Roe: fI = (fL+fR)/2 - R|Lambda|L (uR-uL)/2, Roe average of the
     // reconstructed states for Euler2D (Euler2DUpwind.c:39) and of the
@@ -163,6 +188,15 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
                                             const double* xuR, const Eig& Ecc, const CellAux<M>& cl,
                                             const CellAux<M>& cr, const PhysParams& pp, double* fI) {
   constexpr int NV = ModelTraits<M>::NV;
+  if (UPW == UPW_RUS) {
+    // a scalar dissipation commutes with the basis: fI = R ((xfL+xfR)/2 - alpha (xuR-xuL)/2)
+    const double alpha = fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
+    double fc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) fc[k] = fma(-alpha, 0.5 * (xuR[k] - xuL[k]), 0.5 * (xfL[k] + xfR[k]));
+    projR<M, DIR>(Ecc, fc, fI);
+    return;
+  }
   constexpr bool SAME_BASIS = (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE);
   if (SAME_BASIS) {
     double lamC[NV], fc[NV];
@@ -276,7 +310,8 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
     cell_flux<M, DIR>(q, wf[5]);
     wuc[5] = ufunc_energy<M>(q, pp, wu[5][NV - 1]);
     if (CC) ax[5].rs = roe_side<M>(q);
-    if (M == MODEL_EULER1D && UPW != UPW_ROE) ax[5].c = sound_speed<M>(q, pp);
+    if (UPW == UPW_RUS) ax[5].c = rusanov_speed<M, DIR>(q, pp);
+    else if (M == MODEL_EULER1D && UPW != UPW_ROE) ax[5].c = sound_speed<M>(q, pp);
   };
   auto shift = [&]() {
 #pragma unroll
@@ -486,13 +521,18 @@ cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem
       return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, s); \
     return cudaErrorInvalidValue;                                                                            \
   } while (0)
+  // Rusanov: Euler1D and NavierStokes3D (Euler2D offers none); the template
+  // argument falls back to RF for Euler2D only to keep that branch compilable.
+  constexpr int RUS = (M != MODEL_EULER2D) ? UPW_RUS : UPW_RF;
   if (chr) {
     if (upw == UPW_ROE) GBH_B(true, UPW_ROE);
     if (upw == UPW_LLF) GBH_B(true, UPW_LLF);
+    if (upw == UPW_RUS && M != MODEL_EULER2D) GBH_B(true, RUS);
     GBH_B(true, UPW_RF);
   } else {
     if (upw == UPW_ROE) GBH_B(false, UPW_ROE);
     if (upw == UPW_LLF) GBH_B(false, UPW_LLF);
+    if (upw == UPW_RUS && M != MODEL_EULER2D) GBH_B(false, RUS);
     GBH_B(false, UPW_RF);
   }
 #undef GBH_B
@@ -533,13 +573,18 @@ template <int M, bool ALTW = false>
 cudaError_t launch_hyp_model(int dir, int chr, int upw, const double* U, double* H, const double* dxinv_dir,
                              const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
                              cudaStream_t s) {
+  constexpr int RUS = (M != MODEL_EULER2D) ? UPW_RUS : UPW_RF;  // Euler2D offers no Rusanov
   if (chr) {
     if (upw == UPW_ROE) return launch_dir_any<M, true, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_LLF) return launch_dir_any<M, true, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_RUS && M != MODEL_EULER2D)
+      return launch_dir_any<M, true, RUS, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     return launch_dir_any<M, true, UPW_RF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
   } else {
     if (upw == UPW_ROE) return launch_dir_any<M, false, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_LLF) return launch_dir_any<M, false, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+    if (upw == UPW_RUS && M != MODEL_EULER2D)
+      return launch_dir_any<M, false, RUS, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     return launch_dir_any<M, false, UPW_RF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
   }
 }
@@ -611,8 +656,8 @@ __global__ void upwind_kernel(double* __restrict__ fI, const double* __restrict_
   CellAux<M> cl, cr;
   cl.rs = roe_side<M>(ql);
   cr.rs = roe_side<M>(qr);
-  cl.c = sound_speed<M>(ql, pp);
-  cr.c = sound_speed<M>(qr, pp);
+  cl.c = UPW == UPW_RUS ? rusanov_speed<M, DIR>(ql, pp) : sound_speed<M>(ql, pp);
+  cr.c = UPW == UPW_RUS ? rusanov_speed<M, DIR>(qr, pp) : sound_speed<M>(qr, pp);
   Eig Ecc = roe_eig<M, DIR>(cl.rs, cr.rs, pp);
   upwind_iface<M, true, UPW, DIR>(a, b, c, d, Ecc, cl, cr, pp, out);
 #pragma unroll
@@ -639,6 +684,9 @@ cudaError_t launch_unfused_dir(int kind, int upw, double* out, const double* a, 
     unsigned grid = (unsigned)((nint + blk - 1) / blk);
     if (upw == UPW_ROE) upwind_kernel<M, UPW_ROE, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
     else if (upw == UPW_LLF) upwind_kernel<M, UPW_LLF, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+    else if (upw == UPW_RUS && M != MODEL_EULER2D)
+      upwind_kernel<M, (M != MODEL_EULER2D ? UPW_RUS : UPW_RF), DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp,
+                                                                                       nint);
     else upwind_kernel<M, UPW_RF, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
   }
   return cudaGetLastError();

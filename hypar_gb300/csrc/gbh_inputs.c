@@ -439,8 +439,9 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   if (!strcmp(upw, "roe")) c.upwind = GB_UPWIND_ROE;
   else if (!strcmp(upw, "llf-char")) c.upwind = GB_UPWIND_LLF;
   else if (!strcmp(upw, "rf-char")) c.upwind = GB_UPWIND_RF;
+  else if (!strcmp(upw, "rusanov") && c.model != GB_MODEL_EULER2D) c.upwind = GB_UPWIND_RUSANOV;
   else {
-    gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char)", upw);
+    gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char; rusanov for Euler1D / NavierStokes3D)", upw);
     return GB_ERR_UNSUPPORTED;
   }
   if (c.model == GB_MODEL_NS3D && c.Re > 0) {

@@ -740,10 +740,44 @@ static inline void matmul(int n, double *C, const double *X, const double *Y) {
  * Euler2DUpwindLLF (Euler2DUpwind.c:139-210), NavierStokes3DUpwindLLF
  * (NavierStokes3DUpwind.c:244-318).  RF: Euler2DUpwindRF (Euler2DUpwind.c:68-137),
  * and the same form for Euler1D/NavierStokes3D. */
+/* Rusanov's wave speed |v_dir| + c of a state (Euler1DUpwindRusanov takes
+ * c = gamma P / rho there, without the square root, Euler1DUpwind.c:394-404;
+ * NavierStokes3DUpwindRusanov, NavierStokes3DUpwind.c:392-403). */
+static double rusanov_speed(const orc_problem *p, const double *u, int dir) {
+  double g = p->gamma;
+  if (p->model == ORC_EULER1D) {
+    double rho = u[0], v = u[1] / rho, e = u[2];
+    double P = (e - 0.5 * rho * v * v) * (g - 1.0);
+    double c = g * P / rho;
+    return c + absolute(v);
+  }
+  double rho = u[0];
+  double vx = (rho == 0) ? 0 : u[1] / rho, vy = (rho == 0) ? 0 : u[2] / rho, vz = (rho == 0) ? 0 : u[3] / rho;
+  double e = u[4], vsq = vx * vx + vy * vy + vz * vz;
+  double P = (e - 0.5 * rho * vsq) * (g - 1.0);
+  double c = sqrt(g * P / rho);
+  double vel[3] = {vx, vy, vz};
+  return c + absolute(vel[dir]);
+}
+
 static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, const double *fR,
                    const double *uL, const double *uR, const double *uCL, const double *uCR) {
   int nv = p->nvars;
   double uavg[MAXV], D[MAXV], L[MAXV * MAXV], R[MAXV * MAXV];
+  if (p->upwind == ORC_UPW_RUSANOV) {
+    /* fI = (fL+fR)/2 - kappa max3(speeds of the cell-centre states and their
+     * Roe average) (uR-uL)/2, kappa = 1 without gravity */
+    double udiff[MAXV];
+    m_roeavg(p, uavg, uCL, uCR);
+    for (int v = 0; v < nv; v++) udiff[v] = 0.5 * (uR[v] - uL[v]);
+    double alphaL = rusanov_speed(p, uCL, dir);
+    double alphaR = rusanov_speed(p, uCR, dir);
+    double alphaavg = rusanov_speed(p, uavg, dir);
+    double kappa = max2(1.0, 1.0);
+    double alpha = kappa * max3(alphaL, alphaR, alphaavg);
+    for (int v = 0; v < nv; v++) fI[v] = 0.5 * (fL[v] + fR[v]) - alpha * udiff[v];
+    return;
+  }
   if (p->upwind == ORC_UPW_ROE) {
     double udiff[MAXV], DL[MAXV * MAXV], modA[MAXV * MAXV], udiss[MAXV];
     for (int v = 0; v < nv; v++) udiff[v] = 0.5 * (uR[v] - uL[v]);

@@ -65,6 +65,13 @@ CASES = {
                                                       upwinding="llf-char", perturb=0.05), {
         (0, 1): ("subsonic-inflow", [1.0, 0.1, 0.0, 0.0]), (0, -1): ("subsonic-outflow", [1.0 / 1.4]),
         (1, 1): ("slip-wall", [0.0, 0.0, 0.0]), (1, -1): ("slip-wall", [0.0, 0.0, 0.0])}),
+    # Rusanov upwinding (Euler1D and NavierStokes3D offer it)
+    "sod64_comp_rusanov": lambda: C.sod(64, n_iter=20, dt=1e-3, upwinding="rusanov"),
+    "sod64_char_rusanov_ssprk3": lambda: C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                               upwinding="rusanov", scheme="ssprk3"),
+    "tgv12_comp_rusanov_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02, upwinding="rusanov", perturb=0.05),
+    "tgv12_char_rusanov_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02, interp="characteristic", upwinding="rusanov",
+                                            perturb=0.05),
 }
 
 
