@@ -37,7 +37,8 @@ EXPORTS = [
     "gb_adjoint_create", "gb_adjoint_destroy", "gb_adjoint_set_stream", "gb_adjoint_sync", "gb_adjoint_set_launch",
     "gb_adjoint_get_launch", "gb_adjoint_info", "gb_adjoint_rhs_vjp", "gb_adjoint_rhs_jvp", "gb_adjoint_forward",
     "gb_adjoint_backward", "gb_adjoint_tlm", "gb_inputs_exact", "gb_solver_set_time", "gb_solver_cfl",
-    "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial",
+    "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
+    "gb_solver_set_gravity_field",
 ]
 
 
@@ -53,6 +54,8 @@ class GbConfig(ctypes.Structure):
         ("file_op_iter", ctypes.c_int), ("weno_weights", ctypes.c_int), ("restart_iter", ctypes.c_int),
         ("screen_op_iter", ctypes.c_int), ("write_residual", ctypes.c_int),
         ("zone_data", (ctypes.c_double * 8) * 12),
+        ("gravity", ctypes.c_double * 3), ("rho_ref", ctypes.c_double), ("p_ref", ctypes.c_double),
+        ("R_gas", ctypes.c_double), ("N_bv", ctypes.c_double), ("HB", ctypes.c_int),
     ]
 
 
@@ -84,7 +87,7 @@ def lib():
     L.gb_inputs_free.restype = None
     L.gb_inputs_config.argtypes = [VP]
     L.gb_inputs_config.restype = ctypes.POINTER(GbConfig)
-    for n in ("gb_inputs_x", "gb_inputs_dxinv", "gb_inputs_u0", "gb_inputs_exact"):
+    for n in ("gb_inputs_x", "gb_inputs_dxinv", "gb_inputs_u0", "gb_inputs_exact", "gb_inputs_gravity_field"):
         getattr(L, n).argtypes = [VP]
         getattr(L, n).restype = DP
     L.gb_rk_table.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), DP, DP, DP]
@@ -139,6 +142,7 @@ def lib():
     L.gb_solver_profile_read.argtypes = [VP, DP, ctypes.POINTER(ctypes.c_longlong)]
     L.gb_rhs_explicit_noalloc.argtypes = [ctypes.POINTER(GbConfig), VP, VP, VP, VP]
     L.gb_solver_set_time.argtypes = [VP, ctypes.c_double]
+    L.gb_solver_set_gravity_field.argtypes = [VP, VP]
     L.gb_solver_cfl.argtypes = [VP, DP]
     L.gb_solver_step_report.argtypes = [VP, ctypes.c_int, DP, DP]
     L.gb_solver_error.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, DP]

@@ -54,6 +54,13 @@ class Case:
     # per-face boundary types: {(dim, face): (bctype, [values after the extents])};
     # faces not listed take `bc`
     bcs: Optional[dict] = None
+    # NavierStokes3D gravity (physics.inp gravity / rho_ref / p_ref / R / HB / N_bv)
+    gravity: Optional[Sequence[float]] = None
+    rho_ref: float = 1.0
+    p_ref: float = 1.0
+    R_gas: float = 1.0
+    HB: int = 0
+    N_bv: float = 0.0
 
     @property
     def ndims(self) -> int:
@@ -100,6 +107,11 @@ class Case:
             lines += [f"  Pr         {float(self.Pr)!r}", f"  Minf       {float(self.Minf)!r}"]
             if self.Re is not None:
                 lines.append(f"  Re         {float(self.Re)!r}")
+            if self.gravity is not None:
+                gx, gy, gz = (float(v) for v in self.gravity)
+                lines += [f"  gravity    {gx!r} {gy!r} {gz!r}", f"  rho_ref    {float(self.rho_ref)!r}",
+                          f"  p_ref      {float(self.p_ref)!r}", f"  R          {float(self.R_gas)!r}"]
+                lines.append(f"  HB         {int(self.HB)}" + (f" {float(self.N_bv)!r}" if self.HB == 3 else ""))
         lines.append("end")
         return "\n".join(lines) + "\n"
 
@@ -225,6 +237,41 @@ def tgv(n: int = 256, n_iter: int = 100, dt: float = 2e-3, mach: float = 0.1, Re
     u = np.stack([rho, rho * uu, rho * vv, rho * ww, e], axis=-1).reshape(n ** 3, 5)
     return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme,
                 interp, upwinding, gamma=gamma, Re=Re, Pr=Pr, Minf=mach)
+
+
+def rising_thermal_bubble(n: int = 64, n_iter: int = 100, dt: float = 0.01, interp: str = "components",
+                          upwinding: str = "rusanov", weights: str = "yc", scheme: str = "ssprk3",
+                          HB: int = 2, perturb: float = 0.0, seed: int = 1) -> Case:
+    """Rising thermal bubble (Kelly & Giraldo, J. Comput. Phys. 231, 2012, sec. 5.1.2):
+    a warm bubble in a hydrostatically balanced, neutrally stratified atmosphere on
+    [0, 1000 m]^3 with n points per side (grid spacing 1000/(n-1)), gravity 9.8 m/s^2
+    along y, slip walls on every face.  The ambient state has constant potential
+    temperature T_ref = p_ref / (R rho_ref) and Exner pressure pi = 1 - g y / (Cp T_ref);
+    a cosine bump of 0.5 K, radius 250 m, centred at (500, 260, 500), raises the
+    potential temperature theta.  Then rho = p_ref / (R theta) pi^(1/(gamma-1)) and the
+    energy is p / (gamma-1) with p = rho R theta pi (at rest).  perturb > 0 multiplies the
+    density pointwise by 1 + perturb*N(0,1) (seeded, clipped at 3 sigma) for parity
+    checks away from the balanced state."""
+    gamma, R, rho_ref, p_ref, g = 1.4, 287.058, 1.1612055171196529, 100000.0, 9.8
+    h = 1000.0 / (n - 1)
+    x = np.arange(n, dtype=np.float64) * h
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")  # X[k, j, i] = x_i
+    Cp = gamma * R / (gamma - 1.0)
+    T_ref = p_ref / (R * rho_ref)
+    r = np.sqrt((X - 500.0) ** 2 + (Y - 260.0) ** 2 + (Z - 500.0) ** 2)
+    theta = T_ref + np.where(r > 250.0, 0.0, 0.5 * (1.0 + np.cos(math.pi * r / 250.0)))
+    exner = 1.0 - g * Y / (Cp * T_ref)
+    rho = p_ref / (R * theta) * np.exp(np.log(exner) / (gamma - 1.0))
+    E = rho * (R / (gamma - 1.0)) * theta * exner
+    if perturb > 0.0:
+        rng = np.random.default_rng(seed)
+        rho = rho * (1.0 + perturb * np.clip(rng.standard_normal(rho.shape), -3, 3))
+    zero = np.zeros_like(rho)
+    u = np.stack([rho, zero, zero, zero, E], axis=-1).reshape(n ** 3, 5)
+    bcs = {(d, f): ("slip-wall", [0.0, 0.0, 0.0]) for d in range(3) for f in (1, -1)}
+    return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme, interp,
+                upwinding, gamma=gamma, weights=weights, bcs=bcs, gravity=(0.0, g, 0.0), rho_ref=rho_ref,
+                p_ref=p_ref, R_gas=R, HB=HB)
 
 
 def read_op_bin(path: str) -> Dict[str, np.ndarray]:

@@ -901,6 +901,7 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->pp.inv_gm1 = 1.0 / (cfg->gamma - 1.0);
   a->pp.eps = cfg->weno_eps;
   a->pp.wtype = WENO_W_JS;
+  a->pp.gf = a->pp.gg = nullptr;
   for (int d = 0; d < 2; d++) {
     a->hl[d].seg = 32;
     a->hl[d].block = 128;

@@ -24,6 +24,8 @@ cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const do
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
+cudaError_t launch_hyp_ns3d_grav(int, int, const double*, double*, const double*, const DevGeom&,
+                                 const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_unfused_euler1d(int, int, int, double*, const double*, const double*, const double*,
                                    const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
 cudaError_t launch_unfused_euler2d(int, int, int, double*, const double*, const double*, const double*,
@@ -104,6 +106,10 @@ static int prof_drain(gb_solver* s) {
 static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const StageEpi& ep) {
   const gb_config& c = s->cfg;
   const double* dx = s->d_dxinv + s->dx_off[dir];
+  if (s->gravity) {
+    if (!s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
+    return launch_hyp_ns3d_grav(dir, c.interp, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
+  }
   if (s->pp.wtype != WENO_W_JS) {
     if (c.model == GB_MODEL_EULER1D)
       return launch_hyp_euler1d_w(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
@@ -146,7 +152,16 @@ static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
 
 // Right-hand side of U into `epi` (EPI_RHS or EPI_RK): boundary zones kept in
 // memory, the viscous term, then one fused hyperbolic launch per direction.
+static int gravity_ready(gb_solver* s) {
+  if (s->gravity && !s->d_grav) {
+    gbh_set_error("gravity: call gb_solver_set_gravity_field before evaluating the right-hand side");
+    return GB_ERR_ARG;
+  }
+  return GB_OK;
+}
+
 static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
+  if (int rc = gravity_ready(s)) return rc;
   int rc = apply_mem_bcs(s, U, false);
   if (rc) return rc;
   ep.par = nullptr;
@@ -186,6 +201,14 @@ int gbh_validate(const gb_config* c) {
   if (!(c->gamma > 1.0)) { gbh_set_error("gamma must exceed 1"); return GB_ERR_ARG; }
   if (!(c->weno_eps > 0.0)) { gbh_set_error("weno_eps must be positive"); return GB_ERR_ARG; }
   if (c->weno_weights < GB_WENO_JS || c->weno_weights > GB_WENO_NONE) { gbh_set_error("bad weno_weights"); return GB_ERR_ARG; }
+  if (c->gravity[0] != 0.0 || c->gravity[1] != 0.0 || c->gravity[2] != 0.0) {
+    if (c->model != GB_MODEL_NS3D) { gbh_set_error("gravity: NavierStokes3D only on this path"); return GB_ERR_UNSUPPORTED; }
+    if (c->upwind != GB_UPWIND_RUSANOV) {
+      gbh_set_error("flows with gravity need rusanov upwinding (NavierStokes3DInitialize.c:371)");
+      return GB_ERR_ARG;
+    }
+    if (!(c->rho_ref > 0.0) || !(c->p_ref > 0.0)) { gbh_set_error("gravity needs positive rho_ref and p_ref"); return GB_ERR_ARG; }
+  }
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
@@ -266,6 +289,10 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   s->pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   s->pp.eps = c.weno_eps;
   s->pp.wtype = c.weno_weights;
+  s->pp.gf = s->pp.gg = nullptr;
+  for (int d = 0; d < 3; d++) s->pp.grav[d] = c.gravity[d];
+  s->pp.RT = c.rho_ref > 0 ? c.p_ref / c.rho_ref : 1.0;
+  s->gravity = c.model == GB_MODEL_NS3D && (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0);
   s->viscous = (c.model == GB_MODEL_NS3D) && (c.Re > 0);
   double Re_eff = c.Re / c.Minf;  // NavierStokes3DInitialize.c:368
   s->vp.gamma = c.gamma;
@@ -324,6 +351,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_flag);
   cudaFree(s->d_snap);
   cudaFree(s->d_red);
+  cudaFree(s->d_grav);
   prof_drain(s);
   for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -373,6 +401,16 @@ extern "C" int gb_solver_set_stream(gb_solver* s, void* stream) {
 extern "C" int gb_solver_sync(gb_solver* s) {
   if (!s) { gbh_set_error("null solver"); return GB_ERR_ARG; }
   CK(cudaStreamSynchronize(s->stream));
+  return GB_OK;
+}
+
+extern "C" int gb_solver_set_gravity_field(gb_solver* s, const double* fg) {
+  if (!s || !fg) { gbh_set_error("gb_solver_set_gravity_field: null argument"); return GB_ERR_ARG; }
+  if (!s->gravity) { gbh_set_error("gb_solver_set_gravity_field: the configuration has no gravity"); return GB_ERR_ARG; }
+  if (!s->d_grav) CK(cudaMalloc((void**)&s->d_grav, 2 * s->npts_wg * sizeof(double)));
+  CK(cudaMemcpy(s->d_grav, fg, 2 * s->npts_wg * sizeof(double), cudaMemcpyHostToDevice));
+  s->pp.gf = s->d_grav;
+  s->pp.gg = s->d_grav + s->npts_wg;
   return GB_OK;
 }
 
@@ -622,6 +660,7 @@ extern "C" int gb_HyperbolicFunction(double* hyp, double* u, void* sv, void* m, 
     gbh_set_error("gb_HyperbolicFunction: flux/upwind must be gb_FFunction/gb_Upwind");
     return GB_ERR_UNSUPPORTED;
   }
+  if (int rc = gravity_ready(s)) return rc;
   CK(cudaMemsetAsync(hyp, 0, s->nvals * sizeof(double), s->stream));
   StageEpi ep;
   memset(&ep, 0, sizeof(ep));
@@ -651,12 +690,50 @@ extern "C" int gb_ParabolicFunction(double* par, double* u, void* sv, void* m, d
   return GB_OK;
 }
 
+// out = a - out, elementwise
+static __global__ void sub_kernel(double* __restrict__ out, const double* __restrict__ a, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - out[i];
+}
+
 extern "C" int gb_SourceFunction(double* source, double* u, void* sv, void* m, double t) {
   (void)u;
   (void)m;
   (void)t;
   gb_solver* s = S(sv);
   if (!s || !source) { gbh_set_error("gb_SourceFunction: null argument"); return GB_ERR_ARG; }
+  if (s->gravity) {
+    // The well-balanced source (NavierStokes3DSource.c) interpolates the gravity
+    // field with the flux's own WENO weights, so the direction kernels evaluate it
+    // in their epilogue.  Here: source = hyp - (hyp - source), the hyperbolic term
+    // without and with the source subtracted.
+    if (!u) { gbh_set_error("gb_SourceFunction: null argument"); return GB_ERR_ARG; }
+    if (int rc = gravity_ready(s)) return rc;
+    double* H = s->d_H;
+    CK(cudaMemsetAsync(source, 0, s->nvals * sizeof(double), s->stream));
+    CK(cudaMemsetAsync(H, 0, s->nvals * sizeof(double), s->stream));
+    int rc = GB_OK;
+    for (int pass = 0; pass < 2 && !rc; pass++) {
+      s->d_H = pass == 0 ? source : H;
+      StageEpi ep;
+      memset(&ep, 0, sizeof(ep));
+      ep.mode = EPI_HYP;
+      ep.with_source = pass == 0;
+      for (int d = 0; d < s->cfg.ndims && !rc; d++) {
+        StageEpi e = ep;
+        e.first = (d == 0);
+        e.last = (d == s->cfg.ndims - 1);
+        cudaError_t ce = launch_hyp(s, d, u, e);
+        if (ce != cudaSuccess) { gbh_set_error("gb_SourceFunction: %s", cudaGetErrorString(ce)); rc = GB_ERR_CUDA; }
+      }
+    }
+    s->d_H = H;
+    if (rc) return rc;
+    const long long n = (long long)s->nvals;
+    sub_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(source, H, n);
+    CK(cudaGetLastError());
+    return GB_OK;
+  }
   CK(cudaMemsetAsync(source, 0, s->nvals * sizeof(double), s->stream));
   return GB_OK;
 }
@@ -683,6 +760,7 @@ extern "C" int gb_UFunction(double* uC, double* u, int dir, void* sv, void* m, d
   (void)t;
   gb_solver* s = S(sv);
   if (!s || !uC || !u) { gbh_set_error("gb_UFunction: bad argument"); return GB_ERR_ARG; }
+  if (s->gravity && !s->d_grav) return gravity_ready(s);
   CK(launch_unfused(s, 1, dir < 0 ? 0 : dir, uC, nullptr, nullptr, nullptr, nullptr, u));
   return GB_OK;
 }
@@ -695,6 +773,7 @@ extern "C" int gb_Upwind(double* fI, double* fL, double* fR, double* uL, double*
     gbh_set_error("gb_Upwind: bad argument");
     return GB_ERR_ARG;
   }
+  if (s->gravity && !s->d_grav) return gravity_ready(s);
   CK(launch_unfused(s, 2, dir, fI, fL, fR, uL, uR, u));
   return GB_OK;
 }

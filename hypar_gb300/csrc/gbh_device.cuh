@@ -23,6 +23,11 @@ template <> struct ModelTraits<MODEL_NS3D>    { static constexpr int NV = 5, ND 
 struct PhysParams {
   double gamma, gm1, inv_gm1, eps;
   int wtype;  // WENO weights: WENO_W_* (the kernels take Jiang-Shu unless instantiated for the others)
+  // NavierStokes3D gravity (kernels instantiated with GRAV): the hydrostatic density and
+  // pressure variations f, g at every point with ghosts, the acceleration and RT = p0 / rho0
+  const double* gf;
+  const double* gg;
+  double grav[3], RT;
 };
 
 // WENO5 nonlinear weight formulations (weno.inp flags, WENOFifthOrderCalculateWeights.c:40-64;
@@ -408,6 +413,72 @@ __device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v,
   double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4])) * s6;
   weno5_side_alt(wtype, BL1, BL2, BL3, tL, cL1, cA, cB, outL);
   weno5_side_alt(wtype, BR1, BR2, BR3, tR, cR1, cB, cA, outR);
+}
+
+// Normalised WENO5 weights of the left- and right-biased stencils of a six-point
+// window (Jiang-Shu, or the formulation `wtype` when ALT), for reconstructing other
+// values with the weights of this stencil (InterpolateInterfacesHyp with stored weights).
+template <bool ALT>
+__device__ __forceinline__ void weno5_weights(const double* w, double eps4, int wtype, double* omL, double* omR) {
+  const double k13 = 13.0 / 3.0, c[3] = {0.1, 0.6, 0.3};
+  double d1 = fma(-2.0, w[1], w[0]) + w[2];
+  double d2 = fma(-2.0, w[2], w[1]) + w[3];
+  double d3 = fma(-2.0, w[3], w[2]) + w[4];
+  double d4 = fma(-2.0, w[4], w[3]) + w[5];
+  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0])), gL2 = w[1] - w[3], gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
+  double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5])), gR2 = w[4] - w[2], gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
+  double BL[3] = {fma(k13 * d1, d1, fma(gL1, gL1, eps4)), fma(k13 * d2, d2, fma(gL2, gL2, eps4)),
+                  fma(k13 * d3, d3, fma(gL3, gL3, eps4))};
+  double BR[3] = {fma(k13 * d4, d4, fma(gR1, gR1, eps4)), fma(k13 * d3, d3, fma(gR2, gR2, eps4)),
+                  fma(k13 * d2, d2, fma(gR3, gR3, eps4))};
+  double T[2] = {0.0, 0.0};
+  if (ALT && wtype == WENO_W_BORGES) {
+    T[0] = (BL[0] - BL[2]) * (BL[0] - BL[2]);
+    T[1] = (BR[0] - BR[2]) * (BR[0] - BR[2]);
+  } else if (ALT && wtype == WENO_W_YC) {
+    double eL = d1 - 2.0 * d2 + d3, eR = d4 - 2.0 * d3 + d2;
+    T[0] = 16.0 * (eL * eL) * (eL * eL);
+    T[1] = 16.0 * (eR * eR) * (eR * eR);
+  }
+  for (int side = 0; side < 2; side++) {
+    const double* B = side ? BR : BL;
+    double* om = side ? omR : omL;
+    if (ALT && wtype == WENO_W_NONE) {
+      for (int k = 0; k < 3; k++) om[k] = c[k];
+      continue;
+    }
+    double q[3] = {B[0] * B[0], B[1] * B[1], B[2] * B[2]};
+    // a_k = c_k prod_{j != k} q_j (Jiang-Shu, and mapped's first stage);
+    // Borges / YC: c_k (q_k + T) prod_{j != k} q_j, as in weno5_side_alt
+    const bool z = ALT && (wtype == WENO_W_BORGES || wtype == WENO_W_YC);
+    double a[3] = {c[0] * ((z ? q[0] + T[side] : 1.0) * (q[1] * q[2])),
+                   c[1] * ((z ? q[1] + T[side] : 1.0) * (q[0] * q[2])),
+                   c[2] * ((z ? q[2] + T[side] : 1.0) * (q[0] * q[1]))};
+    double r = nr_rcp(a[0] + a[1] + a[2]);
+    for (int k = 0; k < 3; k++) om[k] = a[k] * r;
+    if (ALT && wtype == WENO_W_MAPPED) {
+      double n[3], e[3];
+      for (int k = 0; k < 3; k++) {
+        n[k] = om[k] * fma(om[k], om[k] - 3.0 * c[k], c[k] + c[k] * c[k]);
+        e[k] = fma(om[k], 1.0 - 2.0 * c[k], c[k] * c[k]);
+      }
+      double m[3] = {n[0] * (e[1] * e[2]), n[1] * (e[0] * e[2]), n[2] * (e[0] * e[1])};
+      double rm = nr_rcp(m[0] + m[1] + m[2]);
+      for (int k = 0; k < 3; k++) om[k] = m[k] * rm;
+    }
+  }
+}
+
+// Reconstruction of the values v with given weights (left-biased at omL, right at omR).
+__device__ __forceinline__ void weno5_apply(const double* omL, const double* omR, const double* v, double& outL,
+                                            double& outR) {
+  const double s6 = 1.0 / 6.0;
+  double cL1 = fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2])) * s6;
+  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3])) * s6;
+  double cA = fma(5.0, v[2], fma(2.0, v[3], -v[1])) * s6;
+  double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4])) * s6;
+  outL = fma(omL[0], cL1, fma(omL[1], cA, omL[2] * cB));
+  outR = fma(omR[0], cR1, fma(omR[1], cB, omR[2] * cA));
 }
 
 __device__ __forceinline__ double dabs(double x) { return fabs(x); }

@@ -162,6 +162,10 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
       gbh_set_error("viscous NavierStokes3D ensembles are not supported");
       return GB_ERR_UNSUPPORTED;
     }
+    if (b.gravity[0] != 0.0 || b.gravity[1] != 0.0 || b.gravity[2] != 0.0) {
+      gbh_set_error("ensembles with gravity are not supported");
+      return GB_ERR_UNSUPPORTED;
+    }
     if (b.weno_weights != GB_WENO_JS) {
       gbh_set_error("ensembles take Jiang-Shu WENO5 weights only (member %d asks for type %d)", m, b.weno_weights);
       return GB_ERR_UNSUPPORTED;
@@ -182,6 +186,7 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
   e->pp.inv_gm1 = 1.0 / (e->base.gamma - 1.0);
   e->pp.eps = e->base.weno_eps;
   e->pp.wtype = WENO_W_JS;
+  e->pp.gf = e->pp.gg = nullptr;
   e->mem.resize(nsims);
   e->nvals.resize(nsims);
   long long off = 0, dxo = 0;

@@ -72,16 +72,18 @@ __device__ __forceinline__ double rusanov_speed_avg(const Eig& E) {
 // Upwind flux at one interface from the reconstructed fL, fR, uL, uR and the
 // two cell-centre neighbours (their Roe-average ingredients `cl`, `cr` and,
 // when CC, the eigen-system `Ecc` of their Roe average).
+// kappa: the Rusanov dissipation factor max(g_L, g_R) of the gravity field (1 without gravity).
 template <int M, bool CHAR, int UPW, int DIR>
 __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR, const double* uL,
                                              const double* uR, const Eig& Ecc, const CellAux<M>& cl,
-                                             const CellAux<M>& cr, const PhysParams& pp, double* fI) {
+                                             const CellAux<M>& cr, const PhysParams& pp, double* fI,
+                                             double kappa = 1.0) {
   constexpr int NV = ModelTraits<M>::NV;
   if (UPW == UPW_RUS) {
     // Rusanov (Euler1DUpwind.c:362-424, NavierStokes3DUpwind.c:349-428):
     // fI = (fL+fR)/2 - alpha (uR-uL)/2, alpha = max of |v|+c over the two
     // cell-centre states and their Roe average (times kappa = 1 without gravity)
-    const double alpha = fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
+    const double alpha = kappa * fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
 #pragma unroll
     for (int v = 0; v < NV; v++) fI[v] = fma(-alpha, 0.5 * (uR[v] - uL[v]), 0.5 * (fL[v] + fR[v]));
     return;
@@ -186,11 +188,12 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
 template <int M, int UPW, int DIR>
 __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR, const double* xuL,
                                             const double* xuR, const Eig& Ecc, const CellAux<M>& cl,
-                                            const CellAux<M>& cr, const PhysParams& pp, double* fI) {
+                                            const CellAux<M>& cr, const PhysParams& pp, double* fI,
+                                            double kappa = 1.0) {
   constexpr int NV = ModelTraits<M>::NV;
   if (UPW == UPW_RUS) {
     // a scalar dissipation commutes with the basis: fI = R ((xfL+xfR)/2 - alpha (xuR-xuL)/2)
-    const double alpha = fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
+    const double alpha = kappa * fmax(fmax(cl.c, cr.c), rusanov_speed_avg<M>(Ecc));
     double fc[NV];
 #pragma unroll
     for (int k = 0; k < NV; k++) fc[k] = fma(-alpha, 0.5 * (xuR[k] - xuL[k]), 0.5 * (xfL[k] + xfR[k]));
@@ -275,7 +278,13 @@ __device__ __forceinline__ void wpair(const double* w, const double* v, double e
 // One thread's share of a launch: interfaces [sg*seg, min((sg+1)*seg, N)] of
 // the grid line with transverse index `tr` (other dimensions ascending, first
 // fastest), and the flux difference / epilogue of the cells in between.
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW = false>
+// GRAV (NavierStokes3D with Rusanov): the well-balanced gravity treatment --
+// the modified solution uC = [f u_{0..3}, P/(gamma-1)/g + f rho|v|^2/2]
+// (NavierStokes3DModifiedSolution.c:52-66), the dissipation factor
+// max(g_L, g_R) (NavierStokes3DUpwind.c:407) and, along a direction with
+// gravity, the source term of NavierStokes3DSource.c:38-112 subtracted from
+// the hyperbolic term of this direction (except when only that term is asked for).
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW = false, bool GRAV = false>
 __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double* __restrict__ H,
                                             const double* __restrict__ dxinv, const DevGeom& G,
                                             const PhysParams& pp, const StageEpi& ep, int seg, long long tr,
@@ -300,15 +309,25 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
   const double eps4 = 4.0 * pp.eps;
 
   double wu[6][NV], wf[6][NV], wuc[6];
+  double wgf[6], wgg[6];  // gravity fields f, g (GRAV)
   CellAux<M> ax[6];
+  const bool src_dir = GRAV && pp.grav[DIR] != 0.0 && (ep.mode != EPI_HYP || ep.with_source);
 
   auto load = [&](int i) {
-    const double* src = U + (pbase + (long long)fold_index(i, N, lo, hi) * sd) * NV;
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    const double* src = U + pt * NV;
 #pragma unroll
     for (int v = 0; v < NV; v++) wu[5][v] = src[v];
     Prim<M> q = to_prim<M>(wu[5], pp);
     cell_flux<M, DIR>(q, wf[5]);
-    wuc[5] = ufunc_energy<M>(q, pp, wu[5][NV - 1]);
+    if (GRAV) {
+      wgf[5] = pp.gf[pt];
+      wgg[5] = pp.gg[pt];
+      double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
+      wuc[5] = fma(q.P * pp.inv_gm1, nr_rcp(wgg[5]), (0.5 * q.rho * vsq) * wgf[5]);
+    } else {
+      wuc[5] = ufunc_energy<M>(q, pp, wu[5][NV - 1]);
+    }
     if (CC) ax[5].rs = roe_side<M>(q);
     if (UPW == UPW_RUS) ax[5].c = rusanov_speed<M, DIR>(q, pp);
     else if (M == MODEL_EULER1D && UPW != UPW_ROE) ax[5].c = sound_speed<M>(q, pp);
@@ -322,6 +341,10 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
         wf[p][v] = wf[p + 1][v];
       }
       wuc[p] = wuc[p + 1];
+      if (GRAV) {
+        wgf[p] = wgf[p + 1];
+        wgg[p] = wgg[p + 1];
+      }
       ax[p] = ax[p + 1];
     }
   };
@@ -331,9 +354,9 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
     shift();
   }
 
-  double fIp[NV];
+  double fIp[NV], SI[NV], SIp[NV];
 #pragma unroll
-  for (int v = 0; v < NV; v++) fIp[v] = 0.0;
+  for (int v = 0; v < NV; v++) fIp[v] = SI[v] = SIp[v] = 0.0;
 
   for (int I = I0; I <= I1; I++) {
     load(I + 2);
@@ -359,8 +382,20 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
 #pragma unroll
           for (int p = 0; p < 6; p++) sc[p] = wuc[p];
           wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
+        } else if (GRAV) {
+          double sc[6];
+#pragma unroll
+          for (int p = 0; p < 6; p++) sc[p] = su[p] * wgf[p];
+          wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
         } else {
           wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
+        }
+        if (src_dir && (v == 1 + DIR || v == NV - 1)) {
+          // the source function phi = g, reconstructed with this flux component's weights
+          double omL[3], omR[3], sL, sR;
+          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+          weno5_apply(omL, omR, wgg, sL, sR);
+          SI[v] = 0.5 * (sL + sR);
         }
       }
       if (M == MODEL_EULER2D && ep.tape) {
@@ -371,17 +406,26 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           t[4 + v] = uR[v];
         }
       }
-      upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI);
+      upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI,
+                                       GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
     } else {
       // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
       // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
       // from the Roe average of the two cell-centre states.
-      double cf[6][NV], cu[6][NV], cuc[6][3];
+      double cf[6][NV], cu[6][NV], cuc[6][GRAV ? NV : 3];
 #pragma unroll
       for (int p = 0; p < 6; p++) {
         projL<M, DIR>(Ecc, pp, wf[p], cf[p]);
         projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
-        if (M == MODEL_NS3D) {
+        if (GRAV) {
+          // uC = f u + (uC_E - f u_E) e_E: f (L u) plus the energy column of L
+          const double fp = wgf[p], de = fma(-fp, wu[p][NV - 1], wuc[p]);
+          cuc[p][0] = fma(de, Ecc.gh, fp * cu[p][0]);
+          cuc[p][1] = fma(de, Ecc.gh, fp * cu[p][1]);
+          cuc[p][2] = fma(-de, Ecc.gi, fp * cu[p][2]);
+#pragma unroll
+          for (int k = 3; k < NV; k++) cuc[p][k] = fp * cu[p][k];
+        } else if (M == MODEL_NS3D) {
           // uC differs from u in the energy only: add that column of L.
           double de = wuc[p] - wu[p][NV - 1];
           cuc[p][0] = fma(de, Ecc.gh, cu[p][0]);
@@ -389,6 +433,14 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           cuc[p][2] = fma(-de, Ecc.gi, cu[p][2]);
         }
       }
+      double lcol[NV];  // L (e_{1+DIR} + e_E): the projection of the source function per unit phi
+      if (src_dir) {
+        double ev[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) ev[v] = (v == 1 + DIR || v == NV - 1) ? 1.0 : 0.0;
+        projL<M, DIR>(Ecc, pp, ev, lcol);
+      }
+      double sch[NV];
       double xfL[NV], xfR[NV], xuL[NV], xuR[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) {
@@ -399,7 +451,7 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           su[p] = cu[p][v];
         }
         wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
-        if (M == MODEL_NS3D && v < 3) {
+        if (M == MODEL_NS3D && (v < 3 || GRAV)) {
           double sc[6];
 #pragma unroll
           for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
@@ -407,8 +459,17 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
         } else {
           wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
         }
+        if (src_dir) {
+          double omL[3], omR[3], sL, sR, ps[6];
+          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+#pragma unroll
+          for (int p = 0; p < 6; p++) ps[p] = wgg[p] * lcol[v];
+          weno5_apply(omL, omR, ps, sL, sR);
+          sch[v] = 0.5 * (sL + sR);
+        }
       }
-      upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI);
+      if (src_dir) projR<M, DIR>(Ecc, sch, SI);
+      upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
     }
 
     if (I > I0) {
@@ -417,10 +478,20 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
       const long long off = (pbase + (long long)c * sd) * NV;
       const double dxi = dxinv[G.g + c];
       const bool finish = ep.last && ep.mode != EPI_HYP;
-      double kv[NV];
+      double kv[NV], term[NV];
+      if (src_dir) {
+        // [0, rho RT e_DIR, rho RT v_DIR] f of the cell (NavierStokes3DSource.c:92-97)
+        const double rho = wu[2][0], rRT = rho * pp.RT, f = wgf[2];
+        const double vd = rho == 0.0 ? 0.0 : wu[2][1 + DIR] * nr_rcp(rho);
+#pragma unroll
+        for (int v = 0; v < NV; v++) term[v] = 0.0;
+        term[1 + DIR] = rRT * f;
+        term[NV - 1] = (rRT * vd) * f;
+      }
 #pragma unroll
       for (int v = 0; v < NV; v++) {
         double h = dxi * (fI[v] - fIp[v]);
+        if (src_dir) h = fma(-term[v] * (SI[v] - SIp[v]), dxi, h);  // rhs = -hyp + source
         double hyp = ep.first ? h : H[off + v] + h;
         if (!finish) {
           H[off + v] = hyp;
@@ -451,18 +522,21 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
       }
     }
 #pragma unroll
-    for (int v = 0; v < NV; v++) fIp[v] = fI[v];
+    for (int v = 0; v < NV; v++) {
+      fIp[v] = fI[v];
+      SIp[v] = SI[v];
+    }
     shift();
   }
 }
 
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false>
 __global__ void __launch_bounds__(128)
 hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
                DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
   long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= ntrans * (long long)nseg) return;
-  hyp_segment<M, CHAR, UPW, DIR, ALTW>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
+  hyp_segment<M, CHAR, UPW, DIR, ALTW, GRAV>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
 }
 
 // All members of an ensemble advanced by one launch per direction: a thread
@@ -539,7 +613,7 @@ cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem
 }
 
 // Host launcher for one direction.
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false>
 cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                        const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
   long long ntrans = 1;
@@ -551,21 +625,31 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   long long nthr = ntrans * nseg;
   int block = L.block > 0 ? L.block : 128;
   long long grid = (nthr + block - 1) / block;
-  hyp_dir_kernel<M, CHAR, UPW, DIR, ALTW><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg, nseg,
-                                                                        ntrans);
+  hyp_dir_kernel<M, CHAR, UPW, DIR, ALTW, GRAV><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg,
+                                                                              nseg, ntrans);
   return cudaGetLastError();
 }
 
-template <int M, bool CHAR, int UPW, bool ALTW>
+template <int M, bool CHAR, int UPW, bool ALTW, bool GRAV = false>
 cudaError_t launch_dir_any(int dir, const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                            const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
   constexpr int ND = ModelTraits<M>::ND;
-  if (dir == 0) return launch_dir<M, CHAR, UPW, 0, ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
+  if (dir == 0) return launch_dir<M, CHAR, UPW, 0, ALTW, GRAV>(U, H, dxinv_dir, G, pp, ep, L, s);
   if (ND > 1 && dir == 1)
-    return launch_dir<M, CHAR, UPW, (ND > 1 ? 1 : 0), ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir<M, CHAR, UPW, (ND > 1 ? 1 : 0), ALTW, GRAV>(U, H, dxinv_dir, G, pp, ep, L, s);
   if (ND > 2 && dir == 2)
-    return launch_dir<M, CHAR, UPW, (ND > 2 ? 2 : 0), ALTW>(U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir<M, CHAR, UPW, (ND > 2 ? 2 : 0), ALTW, GRAV>(U, H, dxinv_dir, G, pp, ep, L, s);
   return cudaErrorInvalidValue;
+}
+
+// NavierStokes3D with gravity (Rusanov upwinding, as the reference requires):
+// ALTW selects the weight formulation as in launch_hyp_model.
+template <bool ALTW>
+cudaError_t launch_hyp_ns3d_gravity(int dir, int chr, const double* U, double* H, const double* dxinv_dir,
+                                    const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
+                                    cudaStream_t s) {
+  if (chr) return launch_dir_any<MODEL_NS3D, true, UPW_RUS, ALTW, true>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
+  return launch_dir_any<MODEL_NS3D, false, UPW_RUS, ALTW, true>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
 }
 
 // ALTW = false: Jiang-Shu weights (pp.wtype ignored); true: pp.wtype selects them.
@@ -616,6 +700,15 @@ __global__ void ufunc_kernel(double* __restrict__ uC, const double* __restrict__
 #pragma unroll
   for (int v = 0; v < NV; v++) uu[v] = u[p * NV + v];
   Prim<M> q = to_prim<M>(uu, pp);
+  if (M == MODEL_NS3D && pp.gf) {
+    // NavierStokes3DModifiedSolution.c:55-66: u* scaled by the hydrostatic fields
+    const double f = pp.gf[p], g = pp.gg[p];
+    const double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
+#pragma unroll
+    for (int v = 0; v < NV - 1; v++) uC[p * NV + v] = uu[v] * f;
+    uC[p * NV + NV - 1] = fma(q.P * pp.inv_gm1, nr_rcp(g), (0.5 * q.rho * vsq) * f);
+    return;
+  }
 #pragma unroll
   for (int v = 0; v < NV - 1; v++) uC[p * NV + v] = uu[v];
   uC[p * NV + NV - 1] = ufunc_energy<M>(q, pp, uu[NV - 1]);
@@ -659,7 +752,9 @@ __global__ void upwind_kernel(double* __restrict__ fI, const double* __restrict_
   cl.c = UPW == UPW_RUS ? rusanov_speed<M, DIR>(ql, pp) : sound_speed<M>(ql, pp);
   cr.c = UPW == UPW_RUS ? rusanov_speed<M, DIR>(qr, pp) : sound_speed<M>(qr, pp);
   Eig Ecc = roe_eig<M, DIR>(cl.rs, cr.rs, pp);
-  upwind_iface<M, true, UPW, DIR>(a, b, c, d, Ecc, cl, cr, pp, out);
+  // NavierStokes3DUpwind.c: Rusanov's dissipation scaled by max(g_L, g_R) of the gravity field
+  const double kappa = (UPW == UPW_RUS && pp.gg) ? fmax(pp.gg[pL], pp.gg[pR]) : 1.0;
+  upwind_iface<M, true, UPW, DIR>(a, b, c, d, Ecc, cl, cr, pp, out, kappa);
 #pragma unroll
   for (int v = 0; v < NV; v++) fI[p * NV + v] = out[v];
 }

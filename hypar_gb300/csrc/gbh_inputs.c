@@ -31,6 +31,7 @@ struct gb_inputs {
   double *dxinv;  /* with ghosts */
   double *u0;     /* interior solution */
   double *uex;    /* exact solution (exact.inp), or NULL */
+  double *grav;   /* gravity fields f then g at every point with ghosts, or NULL */
   char op_overwrite[64];
 };
 
@@ -209,6 +210,76 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   return GB_OK;
 }
 
+static void grid_ghosts(const double *x, int n, int g, double *X);
+
+/* The hydrostatic fields of NavierStokes3DGravityField.c:36-153: f (density) and g
+ * (pressure) from the grid with ghost coordinates for the balance type HB, then
+ * every face's ghost layer copied from its mirror interior points.
+ * raiseto(x, a) = exp(a log x) (include/math_ops.h:37). */
+static int gravity_fields(const gb_config *c, gb_inputs *res) {
+  const int g = c->ghosts;
+  long n[3] = {c->dim[0] + 2 * g, c->dim[1] + 2 * g, c->dim[2] + 2 * g}, np = n[0] * n[1] * n[2];
+  double *X[3];
+  long off = 0;
+  for (int d = 0; d < 3; d++) {
+    X[d] = (double *)malloc(sizeof(double) * n[d]);
+    grid_ghosts(res->x + off, c->dim[d], g, X[d]);
+    off += c->dim[d];
+  }
+  res->grav = (double *)malloc(sizeof(double) * 2 * np);
+  double *f = res->grav, *gg = res->grav + np;
+  const double gx = c->gravity[0], gy = c->gravity[1], gz = c->gravity[2];
+  const double p0 = c->p_ref, rho0 = c->rho_ref, RT = p0 / rho0, gamma = c->gamma, R = c->R_gas;
+  const double Cp = gamma * R / (gamma - 1.0), T0 = p0 / (rho0 * R), Nbv = c->N_bv;
+  if (c->HB == 3 && (gx != 0 || gy != 0)) {
+    for (int d = 0; d < 3; d++) free(X[d]);
+    gbh_set_error("HB = 3 is implemented only for gravity along z");
+    return GB_ERR_INPUT;
+  }
+  for (long k = 0; k < n[2]; k++)
+    for (long j = 0; j < n[1]; j++)
+      for (long i = 0; i < n[0]; i++) {
+        const long p = i + n[0] * (j + n[1] * k);
+        const double x = X[0][i], y = X[1][j], z = X[2][k];
+        if (c->HB == 1) {
+          f[p] = exp((gx * x + gy * y + gz * z) / RT);
+          gg[p] = exp(-(gx * x + gy * y + gz * z) / RT);
+        } else if (c->HB == 2) {
+          f[p] = exp((-1.0 / (gamma - 1.0)) * log((1.0 - (gx * x + gy * y + gz * z) / (Cp * T0))));
+          gg[p] = exp((gamma / (gamma - 1.0)) * log((1.0 - (gx * x + gy * y + gz * z) / (Cp * T0))));
+        } else if (c->HB == 3) {
+          double Pexner = 1 + ((gz * gz) / (Cp * T0 * Nbv * Nbv)) * (exp(-(Nbv * Nbv / gz) * z) - 1.0);
+          f[p] = exp((-1.0 / (gamma - 1.0)) * log(Pexner)) * exp(Nbv * Nbv * z / gz);
+          gg[p] = exp((gamma / (gamma - 1.0)) * log(Pexner));
+        } else {
+          f[p] = gg[p] = 1.0;
+        }
+      }
+  for (int d = 0; d < 3; d++) {
+    long b[3] = {c->dim[0], c->dim[1], c->dim[2]};
+    b[d] = g;
+    for (int side = 0; side < 2; side++)
+      for (long c2 = 0; c2 < b[2]; c2++)
+        for (long c1 = 0; c1 < b[1]; c1++)
+          for (long c0 = 0; c0 < b[0]; c0++) {
+            long ib[3] = {c0, c1, c2}, gi[3], ii[3];
+            for (int e = 0; e < 3; e++) gi[e] = ii[e] = ib[e] + g;
+            if (side == 0) {
+              gi[d] = ib[d];
+              ii[d] = g + (g - 1 - ib[d]);
+            } else {
+              gi[d] = c->dim[d] + g + ib[d];
+              ii[d] = g + (c->dim[d] - 1 - ib[d]);
+            }
+            long q1 = gi[0] + n[0] * (gi[1] + n[1] * gi[2]), q2 = ii[0] + n[0] * (ii[1] + n[1] * ii[2]);
+            f[q1] = f[q2];
+            gg[q1] = gg[q2];
+          }
+  }
+  for (int d = 0; d < 3; d++) free(X[d]);
+  return GB_OK;
+}
+
 /* A solution file in HyPar's input format (ReadArray.c): binary = x then u
  * (point-major); ascii = x then u variable by variable.  Returns -1 (no error
  * message) when the file is absent and `required` is 0. */
@@ -245,6 +316,7 @@ static int read_solution(const char *dir, const char *name, const char *type, lo
 
 /* Generic "begin key value ... end" reader for physics.inp / weno.inp. */
 typedef struct { const char *key; char type; void *dst; } kv_t;
+typedef struct { int hb; double nbv; } hb_t;
 
 static int read_kv_file(const char *dir, const char *name, kv_t *kv, int nkv, int required) {
   FILE *in = open_in(dir, name, "r");
@@ -274,7 +346,14 @@ static int read_kv_file(const char *dir, const char *name, kv_t *kv, int nkv, in
       found = 1;
       if (kv[i].type == 'd') r = fscanf(in, "%lf", (double *)kv[i].dst);
       else if (kv[i].type == 'i') r = fscanf(in, "%d", (int *)kv[i].dst);
-      else r = fscanf(in, "%511s", (char *)kv[i].dst);
+      else if (kv[i].type == 'v') {  /* three doubles (physics.inp gravity) */
+        double *v3 = (double *)kv[i].dst;
+        r = fscanf(in, "%lf %lf %lf", &v3[0], &v3[1], &v3[2]) == 3;
+      } else if (kv[i].type == 'h') {  /* HB, and N_bv after HB = 3 (NavierStokes3DInitialize.c:238-250) */
+        hb_t *hb = (hb_t *)kv[i].dst;
+        r = fscanf(in, "%d", &hb->hb);
+        if (r == 1 && hb->hb == 3) r = fscanf(in, "%lf", &hb->nbv);
+      } else r = fscanf(in, "%511s", (char *)kv[i].dst);
       break;
     }
     if (!found) {
@@ -309,6 +388,7 @@ void gb_inputs_free(gb_inputs *in) {
   free(in->dxinv);
   free(in->u0);
   free(in->uex);
+  free(in->grav);
   free(in);
 }
 
@@ -317,6 +397,7 @@ const double *gb_inputs_x(const gb_inputs *in) { return in ? in->x : NULL; }
 const double *gb_inputs_dxinv(const gb_inputs *in) { return in ? in->dxinv : NULL; }
 const double *gb_inputs_u0(const gb_inputs *in) { return in ? in->u0 : NULL; }
 const double *gb_inputs_exact(const gb_inputs *in) { return in ? in->uex : NULL; }
+const double *gb_inputs_gravity_field(const gb_inputs *in) { return in ? in->grav : NULL; }
 const char *gbh_inputs_op_overwrite(const gb_inputs *in) { return in ? in->op_overwrite : "yes"; }
 
 int gb_inputs_nsims(const char *dir) {
@@ -426,16 +507,24 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   c.Re = -1.0;
   c.Pr = 0.72;
   c.Minf = 1.0;
-  double grav = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-  kv_t pk[] = {{"gamma", 'd', &c.gamma}, {"upwinding", 's', upw}, {"gravity", 'd', &grav},
+  double grav[3] = {0.0, 0.0, 0.0};
+  hb_t hb = {0, 0.0};
+  c.rho_ref = 1.0;
+  c.p_ref = 1.0;
+  c.R_gas = 1.0;
+  /* NavierStokes3DInitialize.c:141-260; Euler1D's scalar "gravity" is outside this path */
+  kv_t pk[] = {{"gamma", 'd', &c.gamma}, {"upwinding", 's', upw}, {"gravity", c.model == GB_MODEL_NS3D ? 'v' : 'd', grav},
                {"Pr", 'd', &c.Pr}, {"Re", 'd', &c.Re}, {"Minf", 'd', &c.Minf},
-               {"gravity_x", 'd', &gx}, {"gravity_y", 'd', &gy}, {"gravity_z", 'd', &gz}};
-  rc = read_kv_file(dir, "physics.inp", pk, 9, 0);
+               {"rho_ref", 'd', &c.rho_ref}, {"p_ref", 'd', &c.p_ref}, {"R", 'd', &c.R_gas}, {"HB", 'h', &hb}};
+  rc = read_kv_file(dir, "physics.inp", pk, 10, 0);
   if (rc) return rc;
-  if (grav != 0.0 || gx != 0.0 || gy != 0.0 || gz != 0.0) {
-    gbh_set_error("gravity is not supported on this path");
+  if (c.model != GB_MODEL_NS3D && grav[0] != 0.0) {
+    gbh_set_error("gravity is supported for NavierStokes3D only on this path");
     return GB_ERR_UNSUPPORTED;
   }
+  for (int d = 0; d < 3; d++) c.gravity[d] = c.model == GB_MODEL_NS3D ? grav[d] : 0.0;
+  c.HB = hb.hb;
+  c.N_bv = hb.nbv;
   if (!strcmp(upw, "roe")) c.upwind = GB_UPWIND_ROE;
   else if (!strcmp(upw, "llf-char")) c.upwind = GB_UPWIND_LLF;
   else if (!strcmp(upw, "rf-char")) c.upwind = GB_UPWIND_RF;
@@ -443,6 +532,11 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   else {
     gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char; rusanov for Euler1D / NavierStokes3D)", upw);
     return GB_ERR_UNSUPPORTED;
+  }
+  if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.upwind != GB_UPWIND_RUSANOV) {
+    /* NavierStokes3DInitialize.c:370-378 */
+    gbh_set_error("rusanov upwinding is needed for flows with gravitational forces");
+    return GB_ERR_INPUT;
   }
   if (c.model == GB_MODEL_NS3D && c.Re > 0) {
     if (strcmp(si.par_space_type, "nonconservative-2stage")) {
@@ -523,6 +617,15 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
       free(X);
       off += n;
       offg += n + 2 * g;
+    }
+  }
+
+  /* gravity fields (NavierStokes3DGravityField.c:36-153) */
+  if (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) {
+    rc = gravity_fields(&c, res);
+    if (rc) {
+      gb_inputs_free(res);
+      return rc;
     }
   }
 

@@ -54,6 +54,9 @@ struct StageEpi {
   // uL, uR of this direction are written here, 8 values per interface at
   // ((line * (N + 1)) + interface) * 8 (the adjoint reads them back).
   double* tape;
+  // EPI_HYP only: also subtract the gravity source (NavierStokes3D with gravity),
+  // so that the hyperbolic term with and without it give the source by difference.
+  int with_source;
 };
 
 // NavierStokes3D viscous-term constants (NavierStokes3DParabolicFunction.c:76-79).

@@ -91,6 +91,10 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
   int rc = gbh_validate(cfg);
   if (rc) return rc;
   const gb_config& c = *cfg;
+  if (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) {
+    gbh_set_error("gb_rhs_explicit_noalloc: gravity is not available here; use gb_RHSFunctionExplicit");
+    return GB_ERR_UNSUPPORTED;
+  }
   if (c.model == GB_MODEL_NS3D && c.Re > 0) {
     gbh_set_error("gb_rhs_explicit_noalloc: the viscous term is not available here (Re > 0); "
                   "use gb_RHSFunctionExplicit");
@@ -122,6 +126,7 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
   pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   pp.eps = c.weno_eps;
   pp.wtype = c.weno_weights;
+  pp.gf = pp.gg = nullptr;
   HypLaunch hl;
   hl.seg = 32;
   hl.block = 128;

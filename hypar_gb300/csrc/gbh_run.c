@@ -125,6 +125,7 @@ int gb_run_case(const char *dir, int device, int verbose) {
   for (int d = 0; d < c->ndims; d++) n *= c->dim[d];
   double *buf = (double *)malloc(sizeof(double) * n);
   rc = gb_solver_set_state(s, gb_inputs_u0(in), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
+  if (!rc && gb_inputs_gravity_field(in)) rc = gb_solver_set_gravity_field(s, gb_inputs_gravity_field(in));
   const int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");
   const int every = c->file_op_iter > 0 ? c->file_op_iter : c->n_iter;
   const int screen = c->screen_op_iter > 0 ? c->screen_op_iter : 1;

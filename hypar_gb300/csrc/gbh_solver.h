@@ -26,6 +26,8 @@ struct gb_solver {
   double* d_dxinv = nullptr;
   double* d_snap = nullptr;  // copy of u before a monitored step (allocated on first use)
   double* d_red = nullptr;   // reduction partials (allocated on first use)
+  double* d_grav = nullptr;  // gravity fields f, g (NavierStokes3D with gravity)
+  bool gravity = false;
   int* d_flag = nullptr;
   std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
   gbh::HypLaunch hl[3];

@@ -45,6 +45,10 @@ class Inputs:
         self.x = np.ctypeslib.as_array(lib().gb_inputs_x(h), shape=(nx,)).copy()
         self.dxinv = np.ctypeslib.as_array(lib().gb_inputs_dxinv(h), shape=(nxg,)).copy()
         self.u0 = np.ctypeslib.as_array(lib().gb_inputs_u0(h), shape=(npts * c.nvars,)).copy()
+        npts_wg = int(np.prod([d + 2 * c.ghosts for d in dims]))
+        gp = lib().gb_inputs_gravity_field(h)
+        # hydrostatic density and pressure fields f, g with ghost points (NavierStokes3D gravity)
+        self.gravity_field = np.ctypeslib.as_array(gp, shape=(2 * npts_wg,)).copy() if gp else None
         lib().gb_inputs_free(h)
         self._h = None
 
@@ -73,7 +77,16 @@ class Solver:
         s = cls(inp.config, inp.dxinv, device)
         s.inputs = inp
         s.set_state(inp.u0)
+        if inp.gravity_field is not None:
+            s.set_gravity_field(inp.gravity_field)
         return s
+
+    def set_gravity_field(self, fg: np.ndarray):
+        """Upload the hydrostatic fields f then g (ghosted layout, x fastest) that the
+        well-balanced NavierStokes3D gravity formulation scales the state and the
+        source with (NavierStokes3DGravityField.c:36-153)."""
+        fg = np.ascontiguousarray(fg, dtype=np.float64)
+        check(lib().gb_solver_set_gravity_field(self._h, fg.ctypes.data_as(_lib.DP)))
 
     def close(self):
         if getattr(self, "_h", None):

@@ -79,6 +79,11 @@ typedef struct gb_config {
    * slip-wall / noslip-wall: wall velocity (ndims); subsonic-inflow: rho, velocity;
    * subsonic-outflow: pressure; supersonic-inflow: rho, velocity, pressure */
   double zone_data[GB_MAX_ZONES][8];
+  /* NavierStokes3D gravity (physics.inp gravity, rho_ref, p_ref, R, HB, N_bv); a nonzero
+   * acceleration needs upwinding rusanov (NavierStokes3DInitialize.c:371) and the
+   * hydrostatic fields of gb_solver_set_gravity_field */
+  double gravity[3], rho_ref, p_ref, R_gas, N_bv;
+  int HB;
 } gb_config;
 
 typedef struct gb_solver gb_solver;
@@ -105,6 +110,10 @@ const double *gb_inputs_u0(const gb_inputs *in);
 /* Exact solution from exact.inp (same format as initial.inp,
  * src/HyParFunctions/ExactSolution.c), or NULL when the deck has none. */
 const double *gb_inputs_exact(const gb_inputs *in);
+/* NavierStokes3D gravity: the hydrostatic density / pressure variations f and g
+ * (NavierStokes3DGravityField.c) at every point with ghosts, f then g (2 x the
+ * points with ghosts), or NULL without gravity. */
+const double *gb_inputs_gravity_field(const gb_inputs *in);
 /* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
  * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
  * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
@@ -125,6 +134,10 @@ void gb_solver_destroy(gb_solver *s);
 const gb_config *gb_solver_config(const gb_solver *s);
 /* Use a caller-owned cudaStream_t (NULL: the solver's own stream). */
 int gb_solver_set_stream(gb_solver *s, void *stream);
+/* NavierStokes3D gravity: upload the fields f, g (host, 2 x the points with
+ * ghosts, as gb_inputs_gravity_field); required before stepping a configuration
+ * with gravity. */
+int gb_solver_set_gravity_field(gb_solver *s, const double *fg);
 /* Wait for all work queued by the solver. */
 int gb_solver_sync(gb_solver *s);
 /* Copy a solution in or out (layout GB_LAYOUT_*, memory GB_MEM_*). */

@@ -74,10 +74,16 @@ def _bind(path):
     L.orc_set_weights.restype = None
     L.orc_set_zone_data.argtypes = [ctypes.c_void_p, ctypes.c_int, dp]
     L.orc_set_zone_data.restype = None
+    L.orc_set_gravity.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_double]
+    L.orc_set_gravity.restype = ctypes.c_int
+    L.orc_get_gravity.argtypes = [ctypes.c_void_p, dp]
+    L.orc_get_gravity.restype = None
     L.orc_cfl.argtypes = [ctypes.c_void_p, dp, ctypes.c_double]
     L.orc_cfl.restype = ctypes.c_double
     L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
-    for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs"):
+    for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs", "orc_source"):
         getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
     L.orc_rk.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int]
     L.orc_set_threads.argtypes = [ctypes.c_int]
@@ -253,6 +259,22 @@ class Problem:
             data = np.zeros(8)
             data[:len(vals)] = vals
             L.orc_set_zone_data(self.h, z, _dp(data))
+        grav = getattr(case, "gravity", None)
+        if grav is not None and any(float(v) != 0.0 for v in grav):
+            xg = np.concatenate([grid_with_ghosts(x, ghosts) for x in xs])
+            if L.orc_set_gravity(self.h, _dp(xg), float(grav[0]), float(grav[1]), float(grav[2]),
+                                 case.rho_ref, case.p_ref, case.R_gas, int(case.HB), case.N_bv):
+                raise RuntimeError("orc_set_gravity failed")
+
+    def gravity_field(self) -> Optional[np.ndarray]:
+        """The fields f then g with ghost points, as the reader computes them, or None."""
+        grav = getattr(self.case, "gravity", None)
+        if grav is None or not any(float(v) != 0.0 for v in grav):
+            return None
+        n = self.npts_wg
+        out = np.empty(2 * n)
+        self._L.orc_get_gravity(self.h, _dp(out))
+        return out
 
     def __del__(self):
         try:
@@ -279,6 +301,13 @@ class Problem:
         self._L.orc_apply_bc(self.h, _dp(u))
         out = np.zeros_like(u)
         self._L.orc_hyperbolic(self.h, _dp(u), _dp(out))
+        return out
+
+    def source(self, u_wg: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u_wg, np.float64).copy()
+        self._L.orc_apply_bc(self.h, _dp(u))
+        out = np.zeros_like(u)
+        self._L.orc_source(self.h, _dp(u), _dp(out))
         return out
 
     def cfl(self, u_wg: np.ndarray, dt: Optional[float] = None) -> float:

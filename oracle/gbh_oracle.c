@@ -80,6 +80,92 @@ orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts
 
 void orc_set_weights(orc_problem *p, int weights) { p->weights = weights; }
 
+static void strides_wg(const orc_problem *p, long *s);
+static long pidx(const orc_problem *p, const long *s, const int *i);
+
+/* NavierStokes3DGravityField (NavierStokes3DGravityField.c:36-153): the
+ * hydrostatic density / pressure variations f, g from the coordinates (ghost
+ * coordinates included), then every face's ghost layer copied from its mirror
+ * interior points.  raiseto(x, a) = exp(a log x) (include/math_ops.h:37). */
+int orc_set_gravity(orc_problem *p, const double *xg, double gx, double gy, double gz, double rho0, double p0,
+                    double R, int HB, double Nbv) {
+  if (p->model != ORC_NS3D) return 1;
+  long np = orc_npoints_wghosts(p);
+  long s[3];
+  strides_wg(p, s);
+  int g = p->ghosts, *dim = p->dim;
+  free(p->gf);
+  free(p->gg);
+  p->gf = (double *)malloc(sizeof(double) * np);
+  p->gg = (double *)malloc(sizeof(double) * np);
+  p->grav[0] = gx;
+  p->grav[1] = gy;
+  p->grav[2] = gz;
+  p->RT = p0 / rho0;
+  p->has_grav = (gx != 0.0) || (gy != 0.0) || (gz != 0.0);
+  double RT = p0 / rho0, gamma = p->gamma;
+  double Cp = gamma * R / (gamma - 1.0);
+  double T0 = p0 / (rho0 * R);
+  long off[3] = {0, dim[0] + 2 * g, dim[0] + 2 * g + dim[1] + 2 * g};
+  for (int k = 0; k < dim[2] + 2 * g; k++)
+    for (int j = 0; j < dim[1] + 2 * g; j++)
+      for (int i = 0; i < dim[0] + 2 * g; i++) {
+        long q = i * s[0] + j * s[1] + k * s[2];
+        double x = xg[off[0] + i], y = xg[off[1] + j], z = xg[off[2] + k];
+        double f, gv;
+        if (HB == 1) {
+          f = exp((gx * x + gy * y + gz * z) / RT);
+          gv = exp(-(gx * x + gy * y + gz * z) / RT);
+        } else if (HB == 2) {
+          f = exp((-1.0 / (gamma - 1.0)) * log((1.0 - (gx * x + gy * y + gz * z) / (Cp * T0))));
+          gv = exp((gamma / (gamma - 1.0)) * log((1.0 - (gx * x + gy * y + gz * z) / (Cp * T0))));
+        } else if (HB == 3) {
+          if (gx != 0 || gy != 0) return 1;
+          double Pexner = 1 + ((gz * gz) / (Cp * T0 * Nbv * Nbv)) * (exp(-(Nbv * Nbv / gz) * z) - 1.0);
+          f = exp((-1.0 / (gamma - 1.0)) * log(Pexner)) * exp(Nbv * Nbv * z / gz);
+          gv = exp((gamma / (gamma - 1.0)) * log(Pexner));
+        } else {
+          f = gv = 1.0;
+        }
+        p->gf[q] = f;
+        p->gg[q] = gv;
+      }
+  /* ghost layers of each face from the mirror interior points, over the
+     interior transverse range (the reference's loops) */
+  for (int d = 0; d < 3; d++) {
+    for (int side = 0; side < 2; side++) {
+      int b[3] = {dim[0], dim[1], dim[2]};
+      b[d] = g;
+      for (int c2 = 0; c2 < b[2]; c2++)
+        for (int c1 = 0; c1 < b[1]; c1++)
+          for (int c0 = 0; c0 < b[0]; c0++) {
+            int ib[3] = {c0, c1, c2}, gi[3], ii[3];
+            for (int e = 0; e < 3; e++) gi[e] = ii[e] = ib[e];
+            if (side == 0) {
+              gi[d] = ib[d] - g;
+              ii[d] = g - 1 - ib[d];
+            } else {
+              gi[d] = dim[d] + ib[d];
+              ii[d] = dim[d] - 1 - ib[d];
+            }
+            long q1 = pidx(p, s, gi), q2 = pidx(p, s, ii);
+            p->gf[q1] = p->gf[q2];
+            p->gg[q1] = p->gg[q2];
+          }
+    }
+  }
+  return 0;
+}
+
+/* f then g (each with ghost points); zeros when no field is set */
+void orc_get_gravity(const orc_problem *p, double *out) {
+  long np = orc_npoints_wghosts(p);
+  for (long q = 0; q < np; q++) {
+    out[q] = p->gf ? p->gf[q] : 0.0;
+    out[np + q] = p->gg ? p->gg[q] : 0.0;
+  }
+}
+
 void orc_set_zone_data(orc_problem *p, int z, const double *data) {
   if (z < 0 || z >= p->nzones) return;
   for (int k = 0; k < 8; k++) p->zones[z].data[k] = data[k];
@@ -87,6 +173,8 @@ void orc_set_zone_data(orc_problem *p, int z, const double *data) {
 
 void orc_problem_destroy(orc_problem *p) {
   if (!p) return;
+  free(p->gf);
+  free(p->gg);
   free(p->dxinv);
   free(p);
 }
@@ -576,18 +664,20 @@ static void m_right(const orc_problem *p, double *R, const double *u, int dir) {
  * (Euler1DModifiedSolution.c:23-50); NavierStokes3D recomputes the energy
  * (NavierStokes3DModifiedSolution.c:31-70) with f = g = 1 at zero gravity;
  * Euler2D has none (uC = u). */
-static void m_ufunc(const orc_problem *p, double *uC, const double *u) {
+static void m_ufunc(const orc_problem *p, double *uC, const double *u, long q) {
   int nv = p->nvars;
   if (p->model == ORC_NS3D) {
+    /* NavierStokes3DModifiedSolution.c:52-66 */
     double inv_gamma_m1 = 1.0 / (p->gamma - 1.0);
     double rho, uvel, vvel, wvel, E, P;
+    double f = p->gf ? p->gf[q] : 1.0, g = p->gg ? p->gg[q] : 1.0;
     NS_FLOWVAR(u, rho, uvel, vvel, wvel, E, P, p->gamma);
     (void)E;
-    uC[0] = u[0] * 1.0;
-    uC[1] = u[1] * 1.0;
-    uC[2] = u[2] * 1.0;
-    uC[3] = u[3] * 1.0;
-    uC[4] = (P * inv_gamma_m1) * (1.0 / 1.0) + (0.5 * rho * (uvel * uvel + vvel * vvel + wvel * wvel)) * 1.0;
+    uC[0] = u[0] * f;
+    uC[1] = u[1] * f;
+    uC[2] = u[2] * f;
+    uC[3] = u[3] * f;
+    uC[4] = (P * inv_gamma_m1) * (1.0 / g) + (0.5 * rho * (uvel * uvel + vvel * vvel + wvel * wvel)) * f;
   } else if (p->model == ORC_EULER1D) {
     for (int v = 0; v < nv; v++) uC[v] = u[v] * (1.0 / 1.0);
   } else {
@@ -761,7 +851,7 @@ static double rusanov_speed(const orc_problem *p, const double *u, int dir) {
 }
 
 static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, const double *fR,
-                   const double *uL, const double *uR, const double *uCL, const double *uCR) {
+                   const double *uL, const double *uR, const double *uCL, const double *uCR, long qL, long qR) {
   int nv = p->nvars;
   double uavg[MAXV], D[MAXV], L[MAXV * MAXV], R[MAXV * MAXV];
   if (p->upwind == ORC_UPW_RUSANOV) {
@@ -773,7 +863,7 @@ static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, 
     double alphaL = rusanov_speed(p, uCL, dir);
     double alphaR = rusanov_speed(p, uCR, dir);
     double alphaavg = rusanov_speed(p, uavg, dir);
-    double kappa = max2(1.0, 1.0);
+    double kappa = p->gg ? max2(p->gg[qL], p->gg[qR]) : max2(1.0, 1.0);
     double alpha = kappa * max3(alphaL, alphaR, alphaavg);
     for (int v = 0; v < nv; v++) fI[v] = 0.5 * (fL[v] + fR[v]) - alpha * udiff[v];
     return;
@@ -838,7 +928,13 @@ static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, 
  * weights from (fC, u) (WENOFifthOrderCalculateWeights.c:111-236 / :760-896),
  * uC = UFunction(u), the four interpolations, upwinding, and
  * hyp += dxinv*(F[j+1/2]-F[j-1/2]) accumulated dimension by dimension. */
-int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
+/* The hyperbolic term and, with gravity, NavierStokes3DSource
+ * (NavierStokes3DSource.c:38-112): per direction with gravity, the source
+ * function [0, phi e_d, phi] (phi = g field) interpolated with the weights of the
+ * flux (InterpolateInterfacesHyp with uflag = 0 reuses them), averaged
+ * (NavierStokes3DSourceUpwind), differenced and scaled by
+ * [0, rho RT e_d, rho RT v_d] f. */
+static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp, double *src) {
   int nd = p->ndims, nv = p->nvars, g = p->ghosts;
   long s[3];
   strides_wg(p, s);
@@ -851,7 +947,7 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
 #pragma omp parallel for schedule(static) num_threads(NTHR)
     for (long q = 0; q < np; q++) {
       m_flux(p, fC + nv * q, u + nv * q, d);
-      m_ufunc(p, uC + nv * q, u + nv * q);
+      m_ufunc(p, uC + nv * q, u + nv * q, q);
     }
     int N = p->dim[d];
     long sd = s[d];
@@ -859,9 +955,11 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
     int ob[3] = {1, 1, 1};
     for (int e = 0; e < nd; e++) if (e != d) { ob[e] = p->dim[e]; nouter *= p->dim[e]; }
     const double *dxinv = p->dxinv + offset;
+    const int dosrc = src && p->has_grav && p->grav[d] != 0.0;
 #pragma omp parallel num_threads(NTHR)
     {
       double *FI = (double *)malloc(sizeof(double) * (N + 1) * nv);
+      double *SI = (double *)malloc(sizeof(double) * (N + 1) * nv);
 #pragma omp for schedule(static)
       for (long lo = 0; lo < nouter; lo++) {
         int idx[3] = {0, 0, 0};
@@ -879,8 +977,18 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
               double w1, w2, w3;
               weno_w(p->weights, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
               fL[v] = weno_interp(w1, w2, w3, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v]);
+              double sL = 0.0, sR = 0.0;
+              int sv = dosrc && (v == 1 + d || v == 4);
+              if (dosrc)
+                sL = sv ? weno_interp(w1, w2, w3, p->gg[L3], p->gg[L2], p->gg[L1], p->gg[L4], p->gg[L5])
+                        : weno_interp(w1, w2, w3, 0.0, 0.0, 0.0, 0.0, 0.0);
               weno_w(p->weights, fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v], p->eps, &w1, &w2, &w3);
               fR[v] = weno_interp(w1, w2, w3, fC[nv * R3 + v], fC[nv * R2 + v], fC[nv * R1 + v], fC[nv * R4 + v], fC[nv * R5 + v]);
+              if (dosrc) {
+                sR = sv ? weno_interp(w1, w2, w3, p->gg[R3], p->gg[R2], p->gg[R1], p->gg[R4], p->gg[R5])
+                        : weno_interp(w1, w2, w3, 0.0, 0.0, 0.0, 0.0, 0.0);
+                SI[(long)I * nv + v] = 0.5 * (sL + sR);
+              }
               weno_w(p->weights, u[nv * L3 + v], u[nv * L2 + v], u[nv * L1 + v], u[nv * L4 + v], u[nv * L5 + v], p->eps, &w1, &w2, &w3);
               uL[v] = weno_interp(w1, w2, w3, uC[nv * L3 + v], uC[nv * L2 + v], uC[nv * L1 + v], uC[nv * L4 + v], uC[nv * L5 + v]);
               weno_w(p->weights, u[nv * R3 + v], u[nv * R2 + v], u[nv * R1 + v], u[nv * R4 + v], u[nv * R5 + v], p->eps, &w1, &w2, &w3);
@@ -904,13 +1012,25 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
               matvec(nv, iul[k], L, uC + nv * sl[k]);
               matvec(nv, iur[k], L, uC + nv * sr[k]);
             }
-            double xfl[MAXV], xfr[MAXV], xul[MAXV], xur[MAXV];
+            double isl[5][MAXV], isr[5][MAXV];  /* projected source-function stencils */
+            if (dosrc) {
+              for (int k = 0; k < 5; k++) {
+                double phl[MAXV] = {0.0}, phr[MAXV] = {0.0};
+                phl[1 + d] = phl[4] = p->gg[sl[k]];
+                phr[1 + d] = phr[4] = p->gg[sr[k]];
+                matvec(nv, isl[k], L, phl);
+                matvec(nv, isr[k], L, phr);
+              }
+            }
+            double xfl[MAXV], xfr[MAXV], xul[MAXV], xur[MAXV], xsl[MAXV], xsr[MAXV];
             for (int v = 0; v < nv; v++) {
               double w1, w2, w3;
               weno_w(p->weights, cfl[0][v], cfl[1][v], cfl[2][v], cfl[3][v], cfl[4][v], p->eps, &w1, &w2, &w3);
               xfl[v] = weno_interp_char(w1, w2, w3, ifl[0][v], ifl[1][v], ifl[2][v], ifl[3][v], ifl[4][v]);
+              if (dosrc) xsl[v] = weno_interp_char(w1, w2, w3, isl[0][v], isl[1][v], isl[2][v], isl[3][v], isl[4][v]);
               weno_w(p->weights, cfr[0][v], cfr[1][v], cfr[2][v], cfr[3][v], cfr[4][v], p->eps, &w1, &w2, &w3);
               xfr[v] = weno_interp_char(w1, w2, w3, ifr[0][v], ifr[1][v], ifr[2][v], ifr[3][v], ifr[4][v]);
+              if (dosrc) xsr[v] = weno_interp_char(w1, w2, w3, isr[0][v], isr[1][v], isr[2][v], isr[3][v], isr[4][v]);
               weno_w(p->weights, cul[0][v], cul[1][v], cul[2][v], cul[3][v], cul[4][v], p->eps, &w1, &w2, &w3);
               xul[v] = weno_interp_char(w1, w2, w3, iul[0][v], iul[1][v], iul[2][v], iul[3][v], iul[4][v]);
               weno_w(p->weights, cur[0][v], cur[1][v], cur[2][v], cur[3][v], cur[4][v], p->eps, &w1, &w2, &w3);
@@ -920,16 +1040,37 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
             matvec(nv, fR, R, xfr);
             matvec(nv, uL, R, xul);
             matvec(nv, uR, R, xur);
+            if (dosrc) {
+              double sLv[MAXV], sRv[MAXV];
+              matvec(nv, sLv, R, xsl);
+              matvec(nv, sRv, R, xsr);
+              for (int v = 0; v < nv; v++) SI[(long)I * nv + v] = 0.5 * (sLv[v] + sRv[v]);
+            }
           }
-          upwind(p, d, FI + (long)I * nv, fL, fR, uL, uR, u + nv * qm1L, u + nv * qm1R);
+          upwind(p, d, FI + (long)I * nv, fL, fR, uL, uR, u + nv * qm1L, u + nv * qm1R, qm1L, qm1R);
         }
         for (int i = 0; i < N; i++) {
           long q = base + (long)i * sd;
           for (int v = 0; v < nv; v++)
             hyp[nv * q + v] += dxinv[g + i] * (FI[(long)(i + 1) * nv + v] - FI[(long)i * nv + v]);
         }
+        if (dosrc) {
+          for (int i = 0; i < N; i++) {
+            long q = base + (long)i * sd;
+            double rho, vel[3], E, P;
+            NS_FLOWVAR((u + nv * q), rho, vel[0], vel[1], vel[2], E, P, p->gamma);
+            (void)E;
+            (void)P;
+            double term[5] = {0.0, rho * p->RT * (d == 0), rho * p->RT * (d == 1), rho * p->RT * (d == 2),
+                              rho * p->RT * vel[d]};
+            for (int v = 0; v < nv; v++)
+              src[nv * q + v] += ((term[v] * p->gf[q]) * (SI[(long)(i + 1) * nv + v] - SI[(long)i * nv + v]) *
+                                  dxinv[g + i]);
+          }
+        }
       }
       free(FI);
+      free(SI);
     }
     offset += p->dim[d] + 2 * g;
   }
@@ -1116,23 +1257,40 @@ double orc_cfl(const orc_problem *p, const double *u, double dt) {
   return max_cfl;
 }
 
+int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp) {
+  return hyperbolic_source(p, u, hyp, NULL);
+}
+
+/* SourceFunction (NavierStokes3DSource.c): the gravity source at every point
+ * (zero at ghost points and without gravity) */
+int orc_source(const orc_problem *p, const double *u, double *src) {
+  long n = orc_npoints_wghosts(p) * p->nvars;
+  double *hyp = (double *)malloc(sizeof(double) * n);
+  for (long i = 0; i < n; i++) src[i] = 0.0;
+  int rc = hyperbolic_source(p, u, hyp, src);
+  free(hyp);
+  return rc;
+}
+
 int orc_rhs(const orc_problem *p, double *u, double *rhs) {
   long n = orc_npoints_wghosts(p) * p->nvars;
   double *hyp = (double *)malloc(sizeof(double) * n);
   double *par = (double *)malloc(sizeof(double) * n);
+  double *src = (double *)calloc(n, sizeof(double));
   orc_apply_bc(p, u);
-  orc_hyperbolic(p, u, hyp);
+  hyperbolic_source(p, u, hyp, src);
   orc_parabolic(p, u, par);
 #pragma omp parallel for schedule(static) num_threads(NTHR)
   for (long i = 0; i < n; i++) {
     double r = 0.0;
     r += -1.0 * hyp[i];
     r += 1.0 * par[i];
-    r += 1.0 * 0.0;
+    r += 1.0 * src[i];
     rhs[i] = r;
   }
   free(hyp);
   free(par);
+  free(src);
   return 0;
 }
 

@@ -45,12 +45,24 @@ typedef struct {
   orc_zone zones[12];
   double *dxinv;        /* sum_d (dim[d]+2*ghosts), per point 2/(x[i+1]-x[i-1]) */
   int weights;          /* ORC_WENO_*: nonlinear weight formulation */
+  /* NavierStokes3D gravity (well-balanced form): acceleration, RT = p0/rho0 and the
+   * hydrostatic fields f (density) and g (pressure) at every point with ghosts */
+  int has_grav;
+  double grav[3], RT;
+  double *gf, *gg;
 } orc_problem;
 
 /* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
  * Yamaleev-Carpenter, or the optimal weights (no_limiting). */
 enum { ORC_WENO_JS = 0, ORC_WENO_MAPPED = 1, ORC_WENO_BORGES = 2, ORC_WENO_YC = 3, ORC_WENO_NONE = 4 };
 void orc_set_weights(orc_problem *p, int weights);
+/* NavierStokes3D gravity: acceleration (gx, gy, gz), reference density and
+ * pressure, gas constant R, hydrostatic balance type HB (1, 2, 3; N_bv for 3)
+ * and the grid with ghost coordinates, sum_d (dim[d]+2g) values
+ * (NavierStokes3DGravityField.c). */
+int orc_set_gravity(orc_problem *p, const double *xg, double gx, double gy, double gz, double rho0, double p0,
+                    double R, int HB, double Nbv);
+void orc_get_gravity(const orc_problem *p, double *out);
 /* The values boundary.inp gives for zone z after its extents (8 doubles). */
 void orc_set_zone_data(orc_problem *p, int z, const double *data);
 
@@ -72,6 +84,8 @@ int orc_hyperbolic(const orc_problem *p, const double *u, double *hyp);
 /* NavierStokes3D viscous term par (with ghosts) from a BC-filled u. */
 int orc_parabolic(const orc_problem *p, const double *u, double *par);
 /* TimeRHSFunctionExplicit: fills u's ghosts in place, rhs = -hyp + par. */
+/* gravity source term, zero elsewhere (SourceFunction) */
+int orc_source(const orc_problem *p, const double *u, double *src);
 int orc_rhs(const orc_problem *p, double *u, double *rhs);
 /* TimeRK over nsteps steps of the Butcher tableau (A: ns x ns row major, b). */
 int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,

@@ -72,7 +72,36 @@ CASES = {
     "tgv12_comp_rusanov_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02, upwinding="rusanov", perturb=0.05),
     "tgv12_char_rusanov_rk4": lambda: C.tgv(12, n_iter=3, dt=0.02, interp="characteristic", upwinding="rusanov",
                                             perturb=0.05),
+    "rtb12_comp_rusanov_yc_ssprk3": lambda: C.rising_thermal_bubble(12, n_iter=3, dt=0.05),
+    "rtb12_char_rusanov_js_rk4": lambda: C.rising_thermal_bubble(12, n_iter=3, dt=0.05, interp="characteristic",
+                                                                 weights="js", scheme="44", perturb=0.02),
+    "rtb12_comp_rusanov_none_hb1": lambda: C.rising_thermal_bubble(12, n_iter=3, dt=0.05, weights="none", HB=1,
+                                                                   perturb=0.02),
+    "rtb12_char_rusanov_mapped_hb3z": lambda: _g(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                          interp="characteristic", weights="mapped",
+                                                                          perturb=0.02),
+                                                 (0.0, 0.0, 9.8), 3, 0.01),
+    "rtb12_comp_rusanov_yc_stir": lambda: _stir(C.rising_thermal_bubble(12, n_iter=3, dt=0.05, perturb=0.02)),
+    "rtb12_char_rusanov_js_stir_rk4": lambda: _stir(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                            interp="characteristic", weights="js",
+                                                                            scheme="44", perturb=0.02)),
+    "rtb12_char_rusanov_borges_hb3z_stir": lambda: _stir(_g(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                                     interp="characteristic",
+                                                                                     weights="borges"),
+                                                            (0.0, 0.0, 9.8), 3, 0.01)),
 }
+
+
+def _stir(case, speed=0.5, seed=11):
+    """Random velocities of about `speed` on the deck's state (density unchanged)."""
+    rng = np.random.default_rng(seed)
+    case.u[:, 1:4] = speed * rng.standard_normal((case.u.shape[0], 3)) * case.u[:, :1]
+    return case
+
+
+def _g(case, gravity, HB, N_bv):
+    case.gravity, case.HB, case.N_bv = gravity, HB, N_bv
+    return case
 
 
 def _b(case, bcs):

@@ -194,3 +194,60 @@ def test_reader_boundary_values(built_lib, tmp_path):
     d = str(tmp_path / "sod")
     sod.write(d)
     _expect(4, d)
+
+
+@pytest.mark.parametrize("hb,axis", [(1, 1), (2, 1), (3, 2)])
+def test_reader_gravity_fields(built_lib, oracle_lib, tmp_path, hb, axis):
+    """physics.inp gravity / rho_ref / p_ref / R / HB (/ N_bv): the reader's hydrostatic
+    fields f and g, ghost layers included, are bit-identical to the oracle's
+    (NavierStokes3DGravityField.c:36-153)."""
+    case = C.rising_thermal_bubble(10, n_iter=1, HB=hb)
+    if axis == 2:
+        case.gravity, case.N_bv = (0.0, 0.0, 9.8), 0.01
+    d = str(tmp_path / "deck")
+    case.write(d)
+    inp = Inputs(d)
+    c = inp.config
+    assert list(c.gravity) == list(case.gravity) and c.HB == hb
+    assert (c.rho_ref, c.p_ref, c.R_gas) == (case.rho_ref, case.p_ref, case.R_gas)
+    assert c.N_bv == (0.01 if hb == 3 else 0.0)
+    ref = O.Problem(case).gravity_field()
+    assert inp.gravity_field is not None and np.array_equal(inp.gravity_field, ref)
+    assert Inputs(str(_deck(tmp_path / "plain", C.tgv(8, n_iter=1)))).gravity_field is None
+
+
+def _deck(d, case):
+    case.write(str(d))
+    return d
+
+
+def test_reader_gravity_errors(built_lib, tmp_path):
+    """Gravity needs rusanov upwinding (NavierStokes3DInitialize.c:370-378); HB = 3 only
+    along z (NavierStokes3DGravityField.c:98-106); on this path only NavierStokes3D."""
+    case = C.rising_thermal_bubble(8, n_iter=1)
+    case.upwinding = "roe"
+    _expect(3, str(_deck(tmp_path / "a", case)))
+    case = C.rising_thermal_bubble(8, n_iter=1, HB=3)
+    _expect(3, str(_deck(tmp_path / "b", case)))
+    d = _deck(tmp_path / "c", C.sod(16, n_iter=1))
+    open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding roe\n gravity 1.0\nend\n")
+    _expect(4, str(d))
+
+
+def test_solver_create_rejects_bad_gravity(built_lib):
+    """gb_solver_create validates before touching a device: gravity outside
+    NavierStokes3D, or with another upwinding than rusanov, is refused."""
+    L = _lib.lib()
+    dx = np.zeros(64)
+    for model, nd, upw, rc_want, msg in (("euler2d", 2, "roe", 4, b"NavierStokes3D only"),
+                                         ("navierstokes3d", 3, "roe", 1, b"rusanov")):
+        cfg = _lib.GbConfig()
+        cfg.model, cfg.ndims, cfg.nvars, cfg.ghosts = _lib.MODEL[model], nd, nd + 2, 3
+        for dd in range(nd):
+            cfg.dim[dd] = 8
+        cfg.upwind, cfg.rk_nstages, cfg.gamma, cfg.weno_eps = _lib.UPWIND[upw], 1, 1.4, 1e-6
+        cfg.gravity[1], cfg.rho_ref, cfg.p_ref = 9.8, 1.0, 1.0
+        h = ctypes.c_void_p()
+        rc = L.gb_solver_create(ctypes.byref(cfg), dx.ctypes.data_as(_lib.DP), -1, ctypes.byref(h))
+        assert not h.value
+        assert rc == rc_want and msg in L.gb_last_error(), (rc, L.gb_last_error())
