@@ -59,6 +59,11 @@ def workload(name: str, size: int = 0):
         case = C.tgv(n, n_iter=100)
         desc = (f"NavierStokes3D Taylor-Green vortex {n}^3 periodic [0,2pi)^3, Mach 0.1, Re 1600, Pr 0.72, "
                 "comp-WENO5(JS)+Roe + 4th-order viscous, RK4, dt 2e-3")
+    elif name == "rtb":
+        n = size or 201
+        case = C.rising_thermal_bubble(n, n_iter=100)
+        desc = (f"NavierStokes3D rising thermal bubble {n}^3 on [0,1000 m]^3, gravity 9.8 along y (HB 2, "
+                "well-balanced), slip walls, comp-WENO5(YC)+Rusanov, SSPRK3, dt 0.01")
     elif name == "sod":
         n = size or 1024
         case = C.sod(n, n_iter=1000)
@@ -653,6 +658,14 @@ def run_reference(args, case, desc, ws, rank):
         u = P.u0()
         cells = int(np.prod(sub.size))
         sample = "512x512 sub-grid of the same vortex (same dt, scheme)"
+    elif total > 180.0 and case.gravity is not None:
+        from hypar_gb300 import cases as C
+        sub = C.rising_thermal_bubble(64, n_iter=1, dt=case.dt, interp=case.interp, upwinding=case.upwinding,
+                                      weights=case.weights, scheme=case.time_scheme_type, HB=case.HB)
+        P = O.Problem(sub)
+        u = P.u0()
+        cells = int(np.prod(sub.size))
+        sample = "64^3 grid of the same bubble problem (same dt, scheme)"
     for _ in range(max(args.warmup - 1, 0)):
         u = P.rk(u, 1)
     t0 = time.perf_counter()
@@ -677,7 +690,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "ensemble", "adjoint",
+    ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "rtb", "ensemble", "adjoint",
                                                           "convergence"])
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -376,7 +376,16 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           sf[p] = wf[p][v];
           su[p] = wu[p][v];
         }
-        wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
+        // the source function phi = g is reconstructed with this flux component's
+        // weights: evaluate them once and apply them to both
+        const bool srcv = src_dir && (v == 1 + DIR || v == NV - 1);
+        double omL[3], omR[3];
+        if (srcv) {
+          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+          weno5_apply(omL, omR, sf, fL[v], fR[v]);
+        } else {
+          wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
+        }
         if (M == MODEL_NS3D && v == NV - 1) {
           double sc[6];
 #pragma unroll
@@ -390,10 +399,8 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
         } else {
           wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
         }
-        if (src_dir && (v == 1 + DIR || v == NV - 1)) {
-          // the source function phi = g, reconstructed with this flux component's weights
-          double omL[3], omR[3], sL, sR;
-          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+        if (srcv) {
+          double sL, sR;
           weno5_apply(omL, omR, wgg, sL, sR);
           SI[v] = 0.5 * (sL + sR);
         }
@@ -450,7 +457,14 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           sf[p] = cf[p][v];
           su[p] = cu[p][v];
         }
-        wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
+        double omL[3], omR[3];
+        if (src_dir) {
+          // one evaluation of the flux weights for the flux and the source function
+          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+          weno5_apply(omL, omR, sf, xfL[v], xfR[v]);
+        } else {
+          wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
+        }
         if (M == MODEL_NS3D && (v < 3 || GRAV)) {
           double sc[6];
 #pragma unroll
@@ -460,8 +474,7 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
         }
         if (src_dir) {
-          double omL[3], omR[3], sL, sR, ps[6];
-          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+          double sL, sR, ps[6];
 #pragma unroll
           for (int p = 0; p < 6; p++) ps[p] = wgg[p] * lcol[v];
           weno5_apply(omL, omR, ps, sL, sR);
