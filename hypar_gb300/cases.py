@@ -48,6 +48,7 @@ class Case:
     Minf: float = 1.0
     file_op_iter: Optional[int] = None
     weights: str = "js"             # WENO5 weights: "js" | "mapped" | "borges" | "yc" | "none" (no_limiting)
+    hyp_scheme: str = "weno5"       # solver.inp hyp_space_scheme: "weno5" | "crweno5"
     op_overwrite: str = "yes"       # solver.inp op_overwrite ("no": op_NNNNN.bin every file_op_iter)
     restart_iter: int = 0           # solver.inp restart_iter
     screen_op_iter: Optional[int] = None
@@ -82,7 +83,7 @@ class Case:
             f"  n_iter            {self.n_iter}",
             "  time_scheme       rk",
             f"  time_scheme_type  {self.time_scheme_type}",
-            "  hyp_space_scheme  weno5",
+            f"  hyp_space_scheme  {self.hyp_scheme}",
             f"  hyp_interp_type   {self.interp}",
         ]
         if self.model == "navierstokes3d":
@@ -272,6 +273,42 @@ def rising_thermal_bubble(n: int = 64, n_iter: int = 100, dt: float = 0.01, inte
     return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme, interp,
                 upwinding, gamma=gamma, weights=weights, bcs=bcs, gravity=(0.0, g, 0.0), rho_ref=rho_ref,
                 p_ref=p_ref, R_gas=R, HB=HB)
+
+
+def isotropic_turbulence(n: int = 256, n_iter: int = 100, dt: float = 0.005, u0: float = 0.3, kp: float = 4.0,
+                         Re: float = 333.333333333333333, Pr: float = 0.72, weights: str = "mapped",
+                         interp: str = "components", upwinding: str = "roe", scheme: str = "ssprk3",
+                         seed: int = 1) -> Case:
+    """Decaying isotropic turbulence on [0, 2 pi)^3, periodic: rho = 1, p = 1/gamma and a
+    random solenoidal velocity field with the Passot-Pouquet energy spectrum
+    E(k) ~ (k/kp)^4 exp(-2 (k/kp)^2), scaled to a component-wise rms velocity u0 (which is
+    also the reference Mach number: c = 1).  Each Fourier mode gets a seeded random
+    complex amplitude of magnitude sqrt(E(k) / (4 pi k^2)), projected on the plane normal
+    to k (divergence free).  physics.inp: Minf = u0, Re as given."""
+    gamma = 1.4
+    h = 2.0 * math.pi / n
+    x = np.arange(n, dtype=np.float64) * h
+    rng = np.random.default_rng(seed)
+    k1 = np.fft.fftfreq(n, d=1.0 / n)
+    kr = np.fft.rfftfreq(n, d=1.0 / n)
+    KZ, KY, KX = np.meshgrid(k1, k1, kr, indexing="ij")  # field index [z, y, x]
+    kk = np.sqrt(KX * KX + KY * KY + KZ * KZ)
+    ks = np.where(kk > 0.0, kk, 1.0)
+    E = (ks / kp) ** 4 * np.exp(-2.0 * (ks / kp) ** 2)
+    amp = np.where(kk > 0.0, np.sqrt(E / (4.0 * math.pi * ks * ks)), 0.0)
+    vel = []
+    xi = [(rng.standard_normal(kk.shape) + 1j * rng.standard_normal(kk.shape)) * amp for _ in range(3)]
+    kdotxi = (KX * xi[0] + KY * xi[1] + KZ * xi[2]) / (ks * ks)
+    for comp, kc in zip(xi, (KX, KY, KZ)):
+        vel.append(np.fft.irfftn(comp - kdotxi * kc, s=(n, n, n), axes=(0, 1, 2)))
+    rms = math.sqrt(sum(float(np.mean(v * v)) for v in vel) / 3.0)
+    uu, vv, ww = (v * (u0 / rms) for v in vel)
+    rho = np.ones_like(uu)
+    P = np.full_like(uu, 1.0 / gamma)
+    e = P / (gamma - 1.0) + 0.5 * rho * (uu * uu + vv * vv + ww * ww)
+    u = np.stack([rho, rho * uu, rho * vv, rho * ww, e], axis=-1).reshape(n ** 3, 5)
+    return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme, interp, upwinding,
+                gamma=gamma, Re=Re, Pr=Pr, Minf=u0, weights=weights)
 
 
 def read_op_bin(path: str) -> Dict[str, np.ndarray]:

@@ -38,6 +38,9 @@ BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "nosl
           "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9}
 
 
+SCHEMES = {"weno5": 0, "crweno5": 1}
+
+
 def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
     """How many values boundary.inp gives after a zone's extents (InitializeBoundaries.c:109-188)."""
     return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
@@ -85,6 +88,10 @@ def _bind(path):
     L.orc_apply_bc.argtypes = [ctypes.c_void_p, dp]
     for name in ("orc_hyperbolic", "orc_parabolic", "orc_rhs", "orc_source"):
         getattr(L, name).argtypes = [ctypes.c_void_p, dp, dp]
+        getattr(L, name).restype = ctypes.c_int
+    L.orc_set_scheme.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.orc_set_scheme.restype = None
+    L.orc_rk.restype = ctypes.c_int
     L.orc_rk.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_int]
     L.orc_set_threads.argtypes = [ctypes.c_int]
     L.orc_get_threads.restype = ctypes.c_int
@@ -254,6 +261,7 @@ class Problem:
         if not self.h:
             raise RuntimeError("orc_problem_create failed")
         L.orc_set_weights(self.h, WEIGHTS[getattr(case, "weights", "js")])
+        L.orc_set_scheme(self.h, SCHEMES[getattr(case, "hyp_scheme", "weno5")])
         for z, row in enumerate(boundary_rows):
             vals = list(row[4]) if len(row) > 4 else []
             data = np.zeros(8)
@@ -293,14 +301,16 @@ class Problem:
     def rhs(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
         out = np.zeros_like(u)
-        self._L.orc_rhs(self.h, _dp(u), _dp(out))
+        if self._L.orc_rhs(self.h, _dp(u), _dp(out)):
+            raise RuntimeError("orc_rhs failed (a zero pivot, or a configuration the oracle does not restate)")
         return out
 
     def hyperbolic(self, u_wg: np.ndarray) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
         self._L.orc_apply_bc(self.h, _dp(u))
         out = np.zeros_like(u)
-        self._L.orc_hyperbolic(self.h, _dp(u), _dp(out))
+        if self._L.orc_hyperbolic(self.h, _dp(u), _dp(out)):
+            raise RuntimeError("orc_hyperbolic failed")
         return out
 
     def source(self, u_wg: np.ndarray) -> np.ndarray:
@@ -325,7 +335,9 @@ class Problem:
         A = np.asarray(A, np.float64)
         b = np.asarray(b, np.float64)
         u = np.ascontiguousarray(u_wg, np.float64).copy()
-        self._L.orc_rk(self.h, ns, _dp(A), _dp(b), _dp(u), float(self.case.dt if dt is None else dt), int(nsteps))
+        if self._L.orc_rk(self.h, ns, _dp(A), _dp(b), _dp(u), float(self.case.dt if dt is None else dt),
+                          int(nsteps)):
+            raise RuntimeError("orc_rk failed")
         return u
 
 

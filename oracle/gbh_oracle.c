@@ -79,6 +79,7 @@ orc_problem *orc_problem_create(int model, int ndims, const int *dim, int ghosts
 }
 
 void orc_set_weights(orc_problem *p, int weights) { p->weights = weights; }
+void orc_set_scheme(orc_problem *p, int scheme) { p->scheme = scheme; }
 
 static void strides_wg(const orc_problem *p, long *s);
 static long pidx(const orc_problem *p, const long *s, const int *i);
@@ -690,11 +691,11 @@ static void m_ufunc(const orc_problem *p, double *uC, const double *u, long q) {
 /* ------------------------------------------------------------------------ */
 
 /* _WENOWeights_v_JS_ (include/interpolation.h:265-285), one component. */
-static inline void weno_js(double m3, double m2, double m1, double p1, double p2, double eps,
+static inline void weno_js(const double *c, double m3, double m2, double m1, double p1, double p2, double eps,
                            double *w1, double *w2, double *w3) {
   static const double thirteen_by_twelve = 13.0 / 12.0;
   static const double one_fourth = 1.0 / 4.0;
-  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  const double c1 = c[0], c2 = c[1], c3 = c[2];
   double b1, b2, b3, a1, a2, a3, a_sum_inv;
   b1 = thirteen_by_twelve * (m3 - 2 * m2 + m1) * (m3 - 2 * m2 + m1)
        + one_fourth * (m3 - 4 * m2 + 3 * m1) * (m3 - 4 * m2 + 3 * m1);
@@ -713,11 +714,11 @@ static inline void weno_js(double m3, double m2, double m1, double p1, double p2
 
 /* _WENOWeights_v_M_ (include/interpolation.h:319-345): JS weights, then the
  * mapping of Henrick, Aslam & Powers and a second normalisation. */
-static inline void weno_m(double m3, double m2, double m1, double p1, double p2, double eps,
+static inline void weno_m(const double *c, double m3, double m2, double m1, double p1, double p2, double eps,
                           double *w1, double *w2, double *w3) {
-  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  const double c1 = c[0], c2 = c[1], c3 = c[2];
   double a1, a2, a3, a_sum_inv;
-  weno_js(m3, m2, m1, p1, p2, eps, w1, w2, w3);
+  weno_js(c, m3, m2, m1, p1, p2, eps, w1, w2, w3);
   a1 = *w1 * (c1 + c1 * c1 - 3 * c1 * *w1 + *w1 * *w1) / (c1 * c1 + *w1 * (1.0 - 2.0 * c1));
   a2 = *w2 * (c2 + c2 * c2 - 3 * c2 * *w2 + *w2 * *w2) / (c2 * c2 + *w2 * (1.0 - 2.0 * c2));
   a3 = *w3 * (c3 + c3 * c3 - 3 * c3 * *w3 + *w3 * *w3) / (c3 * c3 + *w3 * (1.0 - 2.0 * c3));
@@ -742,9 +743,9 @@ static inline void weno_betas(double m3, double m2, double m1, double p1, double
 
 /* _WENOWeights_v_Z_ (tau = |b3-b1|, include/interpolation.h:417-437) and
  * _WENOWeights_v_YC_ (tau = (m3-4m2+6m1-4p1+p2)^2, :474-494). */
-static inline void weno_tau(double tau, double b1, double b2, double b3, double eps, double *w1,
+static inline void weno_tau(const double *c, double tau, double b1, double b2, double b3, double eps, double *w1,
                             double *w2, double *w3) {
-  const double c1 = 0.1, c2 = 0.6, c3 = 0.3;
+  const double c1 = c[0], c2 = c[1], c3 = c[2];
   double a1, a2, a3, a_sum_inv;
   a1 = c1 * (1.0 + (tau / (b1 + eps)) * (tau / (b1 + eps)));
   a2 = c2 * (1.0 + (tau / (b2 + eps)) * (tau / (b2 + eps)));
@@ -758,24 +759,37 @@ static inline void weno_tau(double tau, double b1, double b2, double b3, double 
 /* The weights of one biased stencil for the problem's formulation
  * (WENOFifthOrderCalculateWeights.c:57-60; no_limiting keeps the optimal
  * weights of WENOFifthOrderInitializeWeights). */
-static inline void weno_w(int type, double m3, double m2, double m1, double p1, double p2, double eps,
-                          double *w1, double *w2, double *w3) {
+/* Optimal weights: WENO5 (include/interpolation.h:228-232) and CRWENO5 at interior
+ * interfaces (:234-238). */
+static const double WENO_C[3] = {0.1, 0.6, 0.3};
+static const double CRWENO_C[3] = {0.2, 0.5, 0.3};
+
+/* The weights of one biased stencil for the problem's formulation and the optimal
+ * weights c (WENOFifthOrderCalculateWeights.c:57-60 and :205-225; no_limiting keeps
+ * the optimal weights of WENOFifthOrderInitializeWeights). */
+static inline void weno_w_c(int type, const double *c, double m3, double m2, double m1, double p1, double p2,
+                            double eps, double *w1, double *w2, double *w3) {
   double b1, b2, b3, tau;
   switch (type) {
-    case ORC_WENO_MAPPED: weno_m(m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
+    case ORC_WENO_MAPPED: weno_m(c, m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
     case ORC_WENO_BORGES:
       weno_betas(m3, m2, m1, p1, p2, &b1, &b2, &b3);
       tau = fabs(b3 - b1);
-      weno_tau(tau, b1, b2, b3, eps, w1, w2, w3);
+      weno_tau(c, tau, b1, b2, b3, eps, w1, w2, w3);
       return;
     case ORC_WENO_YC:
       weno_betas(m3, m2, m1, p1, p2, &b1, &b2, &b3);
       tau = (m3 - 4 * m2 + 6 * m1 - 4 * p1 + p2) * (m3 - 4 * m2 + 6 * m1 - 4 * p1 + p2);
-      weno_tau(tau, b1, b2, b3, eps, w1, w2, w3);
+      weno_tau(c, tau, b1, b2, b3, eps, w1, w2, w3);
       return;
-    case ORC_WENO_NONE: *w1 = 0.1; *w2 = 0.6; *w3 = 0.3; return;
-    default: weno_js(m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
+    case ORC_WENO_NONE: *w1 = c[0]; *w2 = c[1]; *w3 = c[2]; return;
+    default: weno_js(c, m3, m2, m1, p1, p2, eps, w1, w2, w3); return;
   }
+}
+
+static inline void weno_w(int type, double m3, double m2, double m1, double p1, double p2, double eps,
+                          double *w1, double *w2, double *w3) {
+  weno_w_c(type, WENO_C, m3, m2, m1, p1, p2, eps, w1, w2, w3);
 }
 
 /* Interp1PrimFifthOrderWENO (Interp1PrimFifthOrderWENO.c:143-158), one component. */
@@ -928,6 +942,102 @@ static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, 
  * weights from (fC, u) (WENOFifthOrderCalculateWeights.c:111-236 / :760-896),
  * uC = UFunction(u), the four interpolations, upwinding, and
  * hyp += dxinv*(F[j+1/2]-F[j-1/2]) accumulated dimension by dimension. */
+/* tridiagLU (src/TridiagLU/tridiagLU.c:90-274) on one rank, one system of n rows
+ * (a: sub-, b: main, c: super-diagonal, x: right-hand side, overwritten with the
+ * solution): elimination of the sub-diagonal, then back-substitution, with the
+ * reference's operations (the fill-in a[i] = -factor a[i-1] stays zero since
+ * a[0] = 0, and the missing next-rank value xp1 is zero). */
+static int tridiag_solve(int n, double *a, double *b, double *c, double *x) {
+  for (int i = 1; i < n; i++) {
+    if (b[i - 1] == 0) return -1;
+    double factor = a[i] / b[i - 1];
+    b[i] -= factor * c[i - 1];
+    a[i] = -factor * a[i - 1];
+    x[i] -= factor * x[i - 1];
+  }
+  const double xp1 = 0.0;
+  if (b[n - 1] == 0) return -1;
+  x[n - 1] = (x[n - 1] - a[n - 1] * x[0] - c[n - 1] * xp1) / b[n - 1];
+  for (int i = n - 2; i > -1; i--) {
+    if (b[i] == 0) return -1;
+    x[i] = (x[i] - c[i] * x[i + 1] - a[i] * x[0]) / b[i];
+  }
+  return 0;
+}
+
+/* Interp1PrimFifthOrderCRWENO (Interp1PrimFifthOrderCRWENO.c:124-199) on one grid
+ * line of N cells, for the four interface reconstructions k = 0 fL, 1 fR (values fC,
+ * weights from fC), 2 uL, 3 uR (values uC, weights from u), every component: at the
+ * N+1 interfaces the rows
+ *   left-biased:  (2/3 w1 + 1/3 w2) F_{j-1/2} + (1/3 w1 + 2/3 w2 + 2/3 w3) F_{j+1/2}
+ *                 + 1/3 w3 F_{j+3/2} = w1 (f_{j-1} + 5 f_j)/6 + w2 (5 f_j + f_{j+1})/6
+ *                 + w3 (f_j + 5 f_{j+1})/6
+ * (right-biased: mirrored), the weights with the CRWENO5 optimal weights
+ * (WENOFifthOrderCalculateWeights.c:205-225); the first and last interfaces take the
+ * explicit WENO5 value (identity rows, WENO5 optimal weights) on a single rank.
+ * out[(I*4 + k)*nv + v]; work: 4 (N+1) doubles. */
+static int crweno_line(const orc_problem *p, const double *fC, const double *u, const double *uC, long base,
+                       long sd, int N, double *out, double *work) {
+  static const double one_third = 1.0 / 3.0;
+  static const double one_sixth = 1.0 / 6.0;
+  const int nv = p->nvars, n = N + 1;
+  double *a = work, *b = work + n, *c = work + 2 * n, *x = work + 3 * n;
+  for (int k = 0; k < 4; k++) {
+    const double *val = k < 2 ? fC : uC, *wv = k < 2 ? fC : u;
+    const int upw = (k % 2 == 0) ? 1 : -1;
+    for (int v = 0; v < nv; v++) {
+      for (int I = 0; I <= N; I++) {
+        long qm1, qm2, qm3, qp1, qp2;
+        if (upw > 0) {
+          qm1 = base + (long)(I - 1) * sd;
+          qm3 = qm1 - 2 * sd;
+          qm2 = qm1 - sd;
+          qp1 = qm1 + sd;
+          qp2 = qm1 + 2 * sd;
+        } else {
+          qm1 = base + (long)I * sd;
+          qm3 = qm1 + 2 * sd;
+          qm2 = qm1 + sd;
+          qp1 = qm1 - sd;
+          qp2 = qm1 - 2 * sd;
+        }
+        const int bnd = (I == 0) || (I == N);
+        double w1, w2, w3;
+        weno_w_c(p->weights, bnd ? WENO_C : CRWENO_C, wv[nv * qm3 + v], wv[nv * qm2 + v], wv[nv * qm1 + v],
+                 wv[nv * qp1 + v], wv[nv * qp2 + v], p->eps, &w1, &w2, &w3);
+        const double fm3 = val[nv * qm3 + v], fm2 = val[nv * qm2 + v], fm1 = val[nv * qm1 + v];
+        const double fp1 = val[nv * qp1 + v], fp2 = val[nv * qp2 + v];
+        double f1, f2, f3;
+        if (bnd) {
+          f1 = (2 * one_sixth) * fm3 + (-7 * one_sixth) * fm2 + (11 * one_sixth) * fm1;
+          f2 = (-one_sixth) * fm2 + (5 * one_sixth) * fm1 + (2 * one_sixth) * fp1;
+          f3 = (2 * one_sixth) * fm1 + (5 * one_sixth) * fp1 + (-one_sixth) * fp2;
+          a[I] = 0.0;
+          b[I] = 1.0;
+          c[I] = 0.0;
+        } else {
+          f1 = (one_sixth) * fm2 + (5 * one_sixth) * fm1;
+          f2 = (5 * one_sixth) * fm1 + (one_sixth) * fp1;
+          f3 = (one_sixth) * fm1 + (5 * one_sixth) * fp1;
+          if (upw > 0) {
+            a[I] = (2 * one_third) * w1 + (one_third) * w2;
+            b[I] = (one_third) * w1 + (2 * one_third) * w2 + (2 * one_third) * w3;
+            c[I] = (one_third) * w3;
+          } else {
+            c[I] = (2 * one_third) * w1 + (one_third) * w2;
+            b[I] = (one_third) * w1 + (2 * one_third) * w2 + (2 * one_third) * w3;
+            a[I] = (one_third) * w3;
+          }
+        }
+        x[I] = w1 * f1 + w2 * f2 + w3 * f3;
+      }
+      if (tridiag_solve(n, a, b, c, x)) return -1;
+      for (int I = 0; I <= N; I++) out[((long)I * 4 + k) * nv + v] = x[I];
+    }
+  }
+  return 0;
+}
+
 /* The hyperbolic term and, with gravity, NavierStokes3DSource
  * (NavierStokes3DSource.c:38-112): per direction with gravity, the source
  * function [0, phi e_d, phi] (phi = g field) interpolated with the weights of the
@@ -943,6 +1053,12 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
   double *fC = (double *)malloc(sizeof(double) * np * nv);
   double *uC = (double *)malloc(sizeof(double) * np * nv);
   long offset = 0;
+  int crweno_failed = 0;
+  if (p->scheme == ORC_SCHEME_CRWENO5 && (p->interp != ORC_INTERP_COMP || p->has_grav)) {
+    free(fC);
+    free(uC);
+    return -1; /* characteristic CRWENO5 and gravity with CRWENO5: not restated */
+  }
   for (int d = 0; d < nd; d++) {
 #pragma omp parallel for schedule(static) num_threads(NTHR)
     for (long q = 0; q < np; q++) {
@@ -960,6 +1076,9 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
     {
       double *FI = (double *)malloc(sizeof(double) * (N + 1) * nv);
       double *SI = (double *)malloc(sizeof(double) * (N + 1) * nv);
+      const int crweno = p->scheme == ORC_SCHEME_CRWENO5;
+      double *CR = crweno ? (double *)malloc(sizeof(double) * (N + 1) * nv * 4) : NULL;
+      double *CW = crweno ? (double *)malloc(sizeof(double) * (N + 1) * 4) : NULL;
 #pragma omp for schedule(static)
       for (long lo = 0; lo < nouter; lo++) {
         int idx[3] = {0, 0, 0};
@@ -967,12 +1086,23 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
         for (int e = 0; e < nd; e++) if (e != d) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
         idx[d] = 0;
         long base = pidx(p, s, idx); /* cell 0 of this line */
+        if (crweno && crweno_line(p, fC, u, uC, base, sd, N, CR, CW)) {
+          crweno_failed = 1;
+          continue;
+        }
         for (int I = 0; I <= N; I++) {
           long qm1L = base + (long)(I - 1) * sd, qm1R = base + (long)I * sd;
           long L3 = qm1L - 2 * sd, L2 = qm1L - sd, L1 = qm1L, L4 = qm1L + sd, L5 = qm1L + 2 * sd;
           long R3 = qm1R + 2 * sd, R2 = qm1R + sd, R1 = qm1R, R4 = qm1R - sd, R5 = qm1R - 2 * sd;
           double fL[MAXV], fR[MAXV], uL[MAXV], uR[MAXV];
-          if (p->interp == ORC_INTERP_COMP) {
+          if (crweno) {
+            for (int v = 0; v < nv; v++) {
+              fL[v] = CR[((long)I * 4 + 0) * nv + v];
+              fR[v] = CR[((long)I * 4 + 1) * nv + v];
+              uL[v] = CR[((long)I * 4 + 2) * nv + v];
+              uR[v] = CR[((long)I * 4 + 3) * nv + v];
+            }
+          } else if (p->interp == ORC_INTERP_COMP) {
             for (int v = 0; v < nv; v++) {
               double w1, w2, w3;
               weno_w(p->weights, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
@@ -1071,12 +1201,14 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
       }
       free(FI);
       free(SI);
+      free(CR);
+      free(CW);
     }
     offset += p->dim[d] + 2 * g;
   }
   free(fC);
   free(uC);
-  return 0;
+  return crweno_failed ? -1 : 0;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1278,7 +1410,7 @@ int orc_rhs(const orc_problem *p, double *u, double *rhs) {
   double *par = (double *)malloc(sizeof(double) * n);
   double *src = (double *)calloc(n, sizeof(double));
   orc_apply_bc(p, u);
-  hyperbolic_source(p, u, hyp, src);
+  int rc = hyperbolic_source(p, u, hyp, src);
   orc_parabolic(p, u, par);
 #pragma omp parallel for schedule(static) num_threads(NTHR)
   for (long i = 0; i < n; i++) {
@@ -1291,7 +1423,7 @@ int orc_rhs(const orc_problem *p, double *u, double *rhs) {
   free(hyp);
   free(par);
   free(src);
-  return 0;
+  return rc;
 }
 
 /* TimeRK (src/TimeIntegration/TimeRK.c:126-195) for one simulation:
@@ -1312,7 +1444,11 @@ int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
 #pragma omp parallel for schedule(static) num_threads(NTHR)
         for (long q = 0; q < n; q++) U[q] += a * k[q];
       }
-      orc_rhs(p, U, Udot + (long)st * n);
+      if (orc_rhs(p, U, Udot + (long)st * n)) {
+        free(U);
+        free(Udot);
+        return -1;
+      }
     }
     for (int st = 0; st < nstages; st++) {
       double a = dt * b[st];

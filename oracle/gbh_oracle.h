@@ -45,6 +45,7 @@ typedef struct {
   orc_zone zones[12];
   double *dxinv;        /* sum_d (dim[d]+2*ghosts), per point 2/(x[i+1]-x[i-1]) */
   int weights;          /* ORC_WENO_*: nonlinear weight formulation */
+  int scheme;           /* ORC_SCHEME_*: hyp_space_scheme */
   /* NavierStokes3D gravity (well-balanced form): acceleration, RT = p0/rho0 and the
    * hydrostatic fields f (density) and g (pressure) at every point with ghosts */
   int has_grav;
@@ -56,6 +57,10 @@ typedef struct {
  * Yamaleev-Carpenter, or the optimal weights (no_limiting). */
 enum { ORC_WENO_JS = 0, ORC_WENO_MAPPED = 1, ORC_WENO_BORGES = 2, ORC_WENO_YC = 3, ORC_WENO_NONE = 4 };
 void orc_set_weights(orc_problem *p, int weights);
+/* hyp_space_scheme: WENO5, or CRWENO5 (compact, a tridiagonal solve per grid line;
+ * component-wise, without gravity) */
+enum { ORC_SCHEME_WENO5 = 0, ORC_SCHEME_CRWENO5 = 1 };
+void orc_set_scheme(orc_problem *p, int scheme);
 /* NavierStokes3D gravity: acceleration (gx, gy, gz), reference density and
  * pressure, gas constant R, hydrostatic balance type HB (1, 2, 3; N_bv for 3)
  * and the grid with ghost coordinates, sum_d (dim[d]+2g) values

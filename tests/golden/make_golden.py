@@ -89,7 +89,26 @@ CASES = {
                                                                                      interp="characteristic",
                                                                                      weights="borges"),
                                                             (0.0, 0.0, 9.8), 3, 0.01)),
+    "sod64_crweno_roe": lambda: _cr(C.sod(64, n_iter=20, dt=1e-3)),
+    "sod64_crweno_llf_ssprk3": lambda: _cr(C.sod(64, n_iter=20, dt=1e-3, upwinding="llf-char", scheme="ssprk3")),
+    "sod64_crweno_none_rusanov": lambda: _w(_cr(C.sod(64, n_iter=20, dt=1e-3, upwinding="rusanov")), "none"),
+    "vortex24_crweno_roe": lambda: _cr(C.vortex(24, n_iter=4, dt=0.02, interp="components")),
+    "vortex24_crweno_rf_mapped": lambda: _w(_cr(C.vortex(24, n_iter=4, dt=0.02, interp="components",
+                                                          upwinding="rf-char")), "mapped"),
+    "vortex24_crweno_llf_yc_slipwall": lambda: _w(_b(_cr(C.vortex(24, n_iter=4, dt=0.02, interp="components",
+                                                                   upwinding="llf-char")),
+                                                     {(1, 1): ("slip-wall", [0.0, 0.0]),
+                                                      (1, -1): ("slip-wall", [0.0, 0.0])}), "yc"),
+    "tgv12_crweno_roe_rk4": lambda: _cr(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05)),
+    "tgv12_crweno_rusanov_borges": lambda: _w(_cr(C.tgv(12, n_iter=3, dt=0.02, upwinding="rusanov",
+                                                         perturb=0.05)), "borges"),
 }
+
+
+def _cr(case):
+    """The deck with hyp_space_scheme crweno5 (compact WENO5)."""
+    case.hyp_scheme = "crweno5"
+    return case
 
 
 def _stir(case, speed=0.5, seed=11):
