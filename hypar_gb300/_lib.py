@@ -18,6 +18,7 @@ MODEL = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
 UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3}
 INTERP = {"components": 0, "characteristic": 1}
 WENO_WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
+SCHEME = {"weno5": 0, "crweno5": 1}
 LAYOUT_INTERIOR, LAYOUT_GHOSTED = 0, 1
 MEM_HOST, MEM_DEVICE = 0, 1
 
@@ -55,7 +56,7 @@ class GbConfig(ctypes.Structure):
         ("screen_op_iter", ctypes.c_int), ("write_residual", ctypes.c_int),
         ("zone_data", (ctypes.c_double * 8) * 12),
         ("gravity", ctypes.c_double * 3), ("rho_ref", ctypes.c_double), ("p_ref", ctypes.c_double),
-        ("R_gas", ctypes.c_double), ("N_bv", ctypes.c_double), ("HB", ctypes.c_int),
+        ("R_gas", ctypes.c_double), ("N_bv", ctypes.c_double), ("HB", ctypes.c_int), ("hyp_scheme", ctypes.c_int),
     ]
 
 

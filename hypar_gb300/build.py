@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libgbhypar.so")
 CLI = os.path.join(HERE, "gbhypar")
 
 CU_SOURCES = ["gbh_hyp_e1.cu", "gbh_hyp_e2.cu", "gbh_hyp_ns.cu", "gbh_hyp_e1w.cu", "gbh_hyp_e2w.cu", "gbh_hyp_nsw.cu", "gbh_hyp_nsg.cu", "gbh_visc.cu", "gbh_api.cu", "gbh_probe.cu", "gbh_ensemble.cu",
-              "gbh_noalloc.cu", "gbh_adjoint.cu", "gbh_monitor.cu"]
+              "gbh_noalloc.cu", "gbh_adjoint.cu", "gbh_monitor.cu", "gbh_crweno.cu"]
 C_SOURCES = ["gbh_inputs.c", "gbh_run.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

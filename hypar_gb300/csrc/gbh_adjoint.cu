@@ -880,7 +880,7 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   int rc = gbh_validate(cfg);
   if (rc) return rc;
   if (cfg->model != GB_MODEL_EULER2D || cfg->interp != GB_INTERP_COMPONENTS || cfg->upwind != GB_UPWIND_ROE ||
-      cfg->weno_weights != GB_WENO_JS) {
+      cfg->weno_weights != GB_WENO_JS || cfg->hyp_scheme != GB_SCHEME_WENO5) {
     gbh_set_error("gb_adjoint_create: the adjoint covers Euler2D with component-wise Jiang-Shu WENO5 and Roe "
                   "upwinding");
     return GB_ERR_UNSUPPORTED;

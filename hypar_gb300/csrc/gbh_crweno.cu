@@ -1,0 +1,385 @@
+// gbh_crweno.cu -- CRWENO5, the compact fifth-order WENO reconstruction
+// (hyp_space_scheme crweno5, component-wise): Interp1PrimFifthOrderCRWENO
+// (src/InterpolationFunctions/Interp1PrimFifthOrderCRWENO.c:124-237) with the
+// weights of WENOFifthOrderCalculateWeights (.c:205-225) and the tridiagonal
+// solve of tridiagLU (src/TridiagLU/tridiagLU.c).
+//
+// Per direction, two launches replace the fused WENO5 kernel:
+//
+//   cr_solve_kernel   one thread per (grid line, reconstruction, component):
+//                     the reconstructions are fL, fR (values f, weights from f),
+//                     uL, uR (values u*, the modified solution, weights from u).
+//                     Walking the N+1 interfaces of its line with a six-cell
+//                     window, the thread forms each interface's row
+//                       (2 w1 + w2) F_{j-1/2} + (w1 + 2 (w2 + w3)) F_{j+1/2} + w3 F_{j+3/2}
+//                         = [w1 (f_{j-1} + 5 f_j) + w2 (5 f_j + f_{j+1}) + w3 (f_j + 5 f_{j+1})] / 2
+//                     (the reference's rows times 3; right-biased: mirrored), the
+//                     weights taken with the CRWENO5 optimal weights (0.2, 0.5, 0.3),
+//                     and eliminates the sub-diagonal as it goes (Thomas), storing
+//                     the normalised super-diagonal and right-hand side; a backward
+//                     sweep then leaves the interface values in place.  On one
+//                     rank the first and last interfaces of a line take the explicit
+//                     WENO5 value (identity rows, WENO5 optimal weights), as the
+//                     reference's single-rank system does.
+//   cr_flux_kernel    the fused kernel's back half: per segment of a line, the
+//                     upwind flux of each interface from the solved values and the
+//                     cell-centre states, the flux difference and the stage epilogue.
+//
+// Layout of the interface values (and of the elimination scratch):
+// [interface I][reconstruction k][component v][line], so that the threads of a
+// warp, which take consecutive lines, read and write consecutive addresses.
+#include "gbh_hyp_impl.cuh"
+
+namespace gbh {
+
+// Normalised weights of one biased stencil s = (f_{j-2}, f_{j-1}, f_j, f_{j+1}, f_{j+2})
+// with optimal weights (c1, c2, c3): Jiang-Shu (ALT false), or the formulation
+// wtype (mapped, Borges, Yamaleev-Carpenter, none) -- the formulas of weno5_weights
+// with the optimal weights as arguments.  B_k = 4 (beta_k + eps).
+template <bool ALT>
+__device__ __forceinline__ void cr_weights(const double* s, double c1, double c2, double c3, double eps4, int wtype,
+                                           double& w1, double& w2, double& w3) {
+  if (ALT && wtype == WENO_W_NONE) {
+    w1 = c1;
+    w2 = c2;
+    w3 = c3;
+    return;
+  }
+  const double k13 = 13.0 / 3.0;
+  const double d1 = fma(-2.0, s[1], s[0]) + s[2];
+  const double d2 = fma(-2.0, s[2], s[1]) + s[3];
+  const double d3 = fma(-2.0, s[3], s[2]) + s[4];
+  const double g1 = fma(3.0, s[2], fma(-4.0, s[1], s[0]));
+  const double g2 = s[1] - s[3];
+  const double g3 = fma(3.0, s[2], fma(-4.0, s[3], s[4]));
+  const double B1 = fma(k13 * d1, d1, fma(g1, g1, eps4));
+  const double B2 = fma(k13 * d2, d2, fma(g2, g2, eps4));
+  const double B3 = fma(k13 * d3, d3, fma(g3, g3, eps4));
+  const double q1 = B1 * B1, q2 = B2 * B2, q3 = B3 * B3;
+  double a1, a2, a3;
+  if (ALT && (wtype == WENO_W_BORGES || wtype == WENO_W_YC)) {
+    double t;
+    if (wtype == WENO_W_BORGES) {
+      t = fabs(B1 - B3);
+    } else {
+      const double e = d1 - 2.0 * d2 + d3;
+      t = 4.0 * (e * e);
+    }
+    const double T = t * t;
+    a1 = c1 * ((q1 + T) * (q2 * q3));
+    a2 = c2 * ((q2 + T) * (q1 * q3));
+    a3 = c3 * ((q3 + T) * (q1 * q2));
+  } else {
+    a1 = c1 * (q2 * q3);
+    a2 = c2 * (q1 * q3);
+    a3 = c3 * (q1 * q2);
+  }
+  const double r = nr_rcp(a1 + a2 + a3);
+  w1 = a1 * r;
+  w2 = a2 * r;
+  w3 = a3 * r;
+  if (ALT && wtype == WENO_W_MAPPED) {
+    const double n1 = w1 * fma(w1, w1 - 3.0 * c1, c1 + c1 * c1);
+    const double n2 = w2 * fma(w2, w2 - 3.0 * c2, c2 + c2 * c2);
+    const double n3 = w3 * fma(w3, w3 - 3.0 * c3, c3 + c3 * c3);
+    const double e1 = fma(w1, 1.0 - 2.0 * c1, c1 * c1);
+    const double e2 = fma(w2, 1.0 - 2.0 * c2, c2 * c2);
+    const double e3 = fma(w3, 1.0 - 2.0 * c3, c3 * c3);
+    const double m1 = n1 * (e2 * e3), m2 = n2 * (e1 * e3), m3 = n3 * (e1 * e2);
+    const double rm = nr_rcp(m1 + m2 + m3);
+    w1 = m1 * rm;
+    w2 = m2 * rm;
+    w3 = m3 * rm;
+  }
+}
+
+// Grid line `tr` along DIR: offset (in points) of its cell 0.
+template <int ND, int DIR>
+__device__ __forceinline__ long long line_base(const DevGeom& G, long long tr) {
+  long long pbase = (long long)G.g * G.stride[DIR];
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    if (e == DIR) continue;
+    const int ie = (int)(tr % G.dim[e]);
+    tr /= G.dim[e];
+    pbase += (long long)(ie + G.g) * G.stride[e];
+  }
+  return pbase;
+}
+
+// The quantity thread (k, v) reconstructs at a cell, and the one its weights see.
+template <int M, int DIR>
+__device__ __forceinline__ void cr_cell(const double* __restrict__ src, int k, int v, const PhysParams& pp,
+                                        double& val, double& wv) {
+  constexpr int NV = ModelTraits<M>::NV;
+  double uu[NV];
+#pragma unroll
+  for (int e = 0; e < NV; e++) uu[e] = src[e];
+  if (k < 2) {
+    Prim<M> q = to_prim<M>(uu, pp);
+    double f[NV];
+    cell_flux<M, DIR>(q, f);
+    double x = f[0];
+#pragma unroll
+    for (int e = 1; e < NV; e++)
+      if (v == e) x = f[e];
+    val = wv = x;
+  } else {
+    double x = uu[0];
+#pragma unroll
+    for (int e = 1; e < NV; e++)
+      if (v == e) x = uu[e];
+    wv = x;
+    if (M == MODEL_NS3D && v == NV - 1) {
+      // the modified solution's energy (NavierStokes3DModifiedSolution.c:65)
+      Prim<M> q = to_prim<M>(uu, pp);
+      val = ufunc_energy<M>(q, pp, uu[NV - 1]);
+    } else {
+      val = x;
+    }
+  }
+}
+
+template <int M, int DIR, bool ALTW>
+__global__ void __launch_bounds__(128)
+cr_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, double* __restrict__ X,
+                double* __restrict__ Cp, long long ntrans) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  const long long nsys = ntrans * 4 * NV;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nsys) return;
+  const long long line = tid % ntrans;
+  const int kv = (int)(tid / ntrans);
+  const int v = kv % NV, k = kv / NV;
+  const bool left = (k % 2) == 0;
+  const long long pbase = line_base<ND, DIR>(G, line);
+  const int N = G.dim[DIR];
+  const long long sd = G.stride[DIR];
+  const int lo = G.bclo[DIR], hi = G.bchi[DIR];
+  const double eps4 = 4.0 * pp.eps;
+  const double s6 = 1.0 / 6.0;
+
+  // window of cells I-3 .. I+2 for interface I
+  double wval[6], wwv[6];
+  auto load = [&](int i, int slot) {
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    cr_cell<M, DIR>(U + pt * NV, k, v, pp, wval[slot], wwv[slot]);
+  };
+#pragma unroll
+  for (int p = 0; p < 5; p++) load(p - 3, p + 1);
+
+  double cprev = 0.0, xprev = 0.0;
+  for (int I = 0; I <= N; I++) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      wval[p] = wval[p + 1];
+      wwv[p] = wwv[p + 1];
+    }
+    load(I + 2, 5);
+    // the biased stencil (f_{j-2}, f_{j-1}, f_j, f_{j+1}, f_{j+2}) of this interface
+    double sw[5], sv[5];
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      sw[p] = left ? wwv[p] : wwv[5 - p];
+      sv[p] = left ? wval[p] : wval[5 - p];
+    }
+    const bool bnd = (I == 0) || (I == N);
+    double w1, w2, w3;
+    if (bnd) cr_weights<ALTW>(sw, 0.1, 0.6, 0.3, eps4, pp.wtype, w1, w2, w3);
+    else cr_weights<ALTW>(sw, 0.2, 0.5, 0.3, eps4, pp.wtype, w1, w2, w3);
+    double cI, xI;
+    if (bnd) {
+      // explicit WENO5 value: identity row
+      const double f1 = fma(2.0, sv[0], fma(-7.0, sv[1], 11.0 * sv[2]));
+      const double f2 = fma(5.0, sv[2], fma(2.0, sv[3], -sv[1]));
+      const double f3 = fma(5.0, sv[3], fma(2.0, sv[2], -sv[4]));
+      // b = 1, a = c = 0: the elimination leaves the value
+      cI = 0.0;
+      xI = fma(w1, f1, fma(w2, f2, w3 * f3)) * s6;
+    } else {
+      const double f1 = fma(5.0, sv[2], sv[1]);
+      const double f2 = fma(5.0, sv[2], sv[3]);
+      const double f3 = fma(5.0, sv[3], sv[2]);
+      const double r = 0.5 * fma(w1, f1, fma(w2, f2, w3 * f3));
+      const double a = left ? fma(2.0, w1, w2) : w3;
+      const double c = left ? w3 : fma(2.0, w1, w2);
+      const double b = fma(2.0, w2 + w3, w1);
+      const double inv = nr_rcp(fma(-a, cprev, b));
+      cI = c * inv;
+      xI = fma(-a, xprev, r) * inv;
+    }
+    const long long o = (long long)I * nsys + tid;
+    if (I < N) Cp[o] = cI;
+    X[o] = xI;
+    cprev = cI;
+    xprev = xI;
+  }
+  // back-substitution: X[I] = X[I] - Cp[I] X[I+1]
+  double x = xprev;
+  for (int I = N - 1; I >= 0; I--) {
+    const long long o = (long long)I * nsys + tid;
+    x = fma(-Cp[o], x, X[o]);
+    X[o] = x;
+  }
+}
+
+// The stage epilogue of the fused kernel for one cell (hyp_segment's): h is
+// this direction's dxinv (F_{j+1/2} - F_{j-1/2}).
+template <int NV>
+__device__ __forceinline__ void cr_epilogue(const StageEpi& ep, double* __restrict__ H, long long off,
+                                            const double* h) {
+  const bool finish = ep.last && ep.mode != EPI_HYP;
+  double kv[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double hyp = ep.first ? h[v] : H[off + v] + h[v];
+    if (!finish) H[off + v] = hyp;
+    else kv[v] = (ep.par ? ep.par[off + v] : 0.0) - hyp;
+  }
+  if (!finish) return;
+  if (ep.mode == EPI_RHS) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) ep.rhs[off + v] = kv[v];
+    return;
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double uv = ep.need_u ? ep.u[off + v] : 0.0;
+    const double av = fma(ep.cb, kv[v], ep.stage == 0 ? uv : ep.acc[off + v]);
+    if (ep.stage == ep.nstages - 1) ep.uout[off + v] = av;
+    else ep.acc[off + v] = av;
+#pragma unroll
+    for (int t = 1; t < 4; t++) {
+      if (t > ep.stage && t < ep.nstages && ep.ca[t] != 0.0) {
+        const double base = ep.touched[t] ? ep.P[t][off + v] : uv;
+        ep.P[t][off + v] = fma(ep.ca[t], kv[v], base);
+      }
+    }
+  }
+}
+
+template <int M, int UPW, int DIR>
+__global__ void __launch_bounds__(128)
+cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
+               PhysParams pp, StageEpi ep, const double* __restrict__ X, int seg, int nseg, long long ntrans) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  constexpr bool CC = NeedCC<M, false, UPW>::value;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= ntrans * (long long)nseg) return;
+  const long long line = tid % ntrans;
+  const int sg = (int)(tid / ntrans);
+  const long long pbase = line_base<ND, DIR>(G, line);
+  const int N = G.dim[DIR];
+  const long long sd = G.stride[DIR];
+  const int lo = G.bclo[DIR], hi = G.bchi[DIR];
+  const int I0 = sg * seg;
+  const int I1 = min(I0 + seg, N);
+  const long long nsys = ntrans * 4 * NV;
+
+  auto aux = [&](int i) {
+    CellAux<M> a;
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    double uu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = U[pt * NV + v];
+    Prim<M> q = to_prim<M>(uu, pp);
+    if (CC) a.rs = roe_side<M>(q);
+    if (UPW == UPW_RUS) a.c = rusanov_speed<M, DIR>(q, pp);
+    else if (M == MODEL_EULER1D && UPW != UPW_ROE) a.c = sound_speed<M>(q, pp);
+    return a;
+  };
+  CellAux<M> axL = aux(I0 - 1);
+  double fIp[NV];
+  for (int I = I0; I <= I1; I++) {
+    const CellAux<M> axR = aux(I);
+    double fL[NV], fR[NV], uL[NV], uR[NV];
+    const double* q = X + (long long)I * nsys + line;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      fL[v] = q[(0 * NV + v) * ntrans];
+      fR[v] = q[(1 * NV + v) * ntrans];
+      uL[v] = q[(2 * NV + v) * ntrans];
+      uR[v] = q[(3 * NV + v) * ntrans];
+    }
+    Eig Ecc;
+    if (CC) Ecc = roe_eig<M, DIR>(axL.rs, axR.rs, pp);
+    double fI[NV];
+    upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, axL, axR, pp, fI);
+    if (I > I0) {
+      const int c = I - 1;
+      const long long off = (pbase + (long long)c * sd) * NV;
+      const double dxi = dxinv[G.g + c];
+      double h[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) h[v] = dxi * (fI[v] - fIp[v]);
+      cr_epilogue<NV>(ep, H, off, h);
+    }
+#pragma unroll
+    for (int v = 0; v < NV; v++) fIp[v] = fI[v];
+    axL = axR;
+  }
+}
+
+template <int M, int DIR, bool ALTW, int UPW>
+static cudaError_t cr_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
+                          const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
+                          cudaStream_t s) {
+  constexpr int NV = ModelTraits<M>::NV;
+  long long ntrans = 1;
+  for (int e = 0; e < G.nd; e++)
+    if (e != DIR) ntrans *= G.dim[e];
+  const long long nsys = ntrans * 4 * NV;
+  cr_solve_kernel<M, DIR, ALTW><<<(unsigned)((nsys + 127) / 128), 128, 0, s>>>(U, G, pp, X, Cp, ntrans);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int seg = L.seg > 0 ? L.seg : 32;
+  const int nseg = (G.dim[DIR] + seg - 1) / seg;
+  const long long nthr = ntrans * nseg;
+  const int block = L.block > 0 ? L.block : 128;
+  cr_flux_kernel<M, UPW, DIR><<<(unsigned)((nthr + block - 1) / block), block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, X,
+                                                                                     seg, nseg, ntrans);
+  return cudaGetLastError();
+}
+
+template <int M, int DIR, bool ALTW>
+static cudaError_t cr_dir_upw(int upw, const double* U, double* H, const double* dx, const DevGeom& G,
+                              const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
+                              cudaStream_t s) {
+  switch (upw) {
+    case UPW_ROE: return cr_dir<M, DIR, ALTW, UPW_ROE>(U, H, dx, G, pp, ep, L, X, Cp, s);
+    case UPW_LLF: return cr_dir<M, DIR, ALTW, UPW_LLF>(U, H, dx, G, pp, ep, L, X, Cp, s);
+    case UPW_RF: return cr_dir<M, DIR, ALTW, UPW_RF>(U, H, dx, G, pp, ep, L, X, Cp, s);
+    default:
+      if (M == MODEL_EULER2D) return cudaErrorInvalidValue;  // Euler2D has no Rusanov
+      return cr_dir<M, DIR, ALTW, (M == MODEL_EULER2D ? UPW_ROE : UPW_RUS)>(U, H, dx, G, pp, ep, L, X, Cp, s);
+  }
+}
+
+template <int M, bool ALTW>
+static cudaError_t cr_model(int dir, int upw, const double* U, double* H, const double* dx, const DevGeom& G,
+                            const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
+                            cudaStream_t s) {
+  constexpr int ND = ModelTraits<M>::ND;
+  if (dir == 0) return cr_dir_upw<M, 0, ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  if (ND > 1 && dir == 1) return cr_dir_upw<M, (ND > 1 ? 1 : 0), ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  if (ND > 2 && dir == 2) return cr_dir_upw<M, (ND > 2 ? 2 : 0), ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  return cudaErrorInvalidValue;
+}
+
+// One direction of the hyperbolic term with CRWENO5 (component-wise).  X and Cp:
+// (N+1) * ntrans * 4 * nvars doubles each for this direction.
+cudaError_t launch_hyp_crweno(int model, int dir, int upw, const double* U, double* H, const double* dxinv_dir,
+                              const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
+                              double* X, double* Cp, cudaStream_t s) {
+  const bool alt = pp.wtype != WENO_W_JS;
+  if (model == MODEL_EULER1D)
+    return alt ? cr_model<MODEL_EULER1D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+               : cr_model<MODEL_EULER1D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+  if (model == MODEL_EULER2D)
+    return alt ? cr_model<MODEL_EULER2D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+               : cr_model<MODEL_EULER2D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+  return alt ? cr_model<MODEL_NS3D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+             : cr_model<MODEL_NS3D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+}
+
+}  // namespace gbh

@@ -166,6 +166,10 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
       gbh_set_error("ensembles with gravity are not supported");
       return GB_ERR_UNSUPPORTED;
     }
+    if (b.hyp_scheme != GB_SCHEME_WENO5) {
+      gbh_set_error("ensembles take WENO5 only (member %d asks for CRWENO5)", m);
+      return GB_ERR_UNSUPPORTED;
+    }
     if (b.weno_weights != GB_WENO_JS) {
       gbh_set_error("ensembles take Jiang-Shu WENO5 weights only (member %d asks for type %d)", m, b.weno_weights);
       return GB_ERR_UNSUPPORTED;

@@ -474,8 +474,12 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     gbh_set_error("ghost must be 3 for weno5 (got %d)", c.ghosts);
     return GB_ERR_UNSUPPORTED;
   }
-  if (strcmp(si.hyp_space_scheme, "weno5")) {
-    gbh_set_error("hyp_space_scheme %s not supported (weno5 only)", si.hyp_space_scheme);
+  if (!strcmp(si.hyp_space_scheme, "weno5")) {
+    c.hyp_scheme = GB_SCHEME_WENO5;
+  } else if (!strcmp(si.hyp_space_scheme, "crweno5")) {
+    c.hyp_scheme = GB_SCHEME_CRWENO5;
+  } else {
+    gbh_set_error("hyp_space_scheme %s not supported (weno5, crweno5)", si.hyp_space_scheme);
     return GB_ERR_UNSUPPORTED;
   }
   if (strcmp(si.hyp_flux_split, "no")) {
@@ -487,6 +491,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   else {
     gbh_set_error("hyp_interp_type %s invalid", si.interp_type);
     return GB_ERR_INPUT;
+  }
+  if (c.hyp_scheme == GB_SCHEME_CRWENO5 && c.interp == GB_INTERP_CHARACTERISTIC) {
+    gbh_set_error("characteristic CRWENO5 is not available on this path (component-wise only)");
+    return GB_ERR_UNSUPPORTED;
   }
   if (strcmp(si.time_scheme, "rk")) {
     gbh_set_error("time_scheme %s not supported (rk only)", si.time_scheme);
@@ -531,6 +539,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   else if (!strcmp(upw, "rusanov") && c.model != GB_MODEL_EULER2D) c.upwind = GB_UPWIND_RUSANOV;
   else {
     gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char; rusanov for Euler1D / NavierStokes3D)", upw);
+    return GB_ERR_UNSUPPORTED;
+  }
+  if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.hyp_scheme == GB_SCHEME_CRWENO5) {
+    gbh_set_error("gravity with CRWENO5 is not available on this path");
     return GB_ERR_UNSUPPORTED;
   }
   if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.upwind != GB_UPWIND_RUSANOV) {

@@ -95,6 +95,10 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
     gbh_set_error("gb_rhs_explicit_noalloc: gravity is not available here; use gb_RHSFunctionExplicit");
     return GB_ERR_UNSUPPORTED;
   }
+  if (c.hyp_scheme != GB_SCHEME_WENO5) {
+    gbh_set_error("gb_rhs_explicit_noalloc: CRWENO5 needs scratch for its line solves; use gb_RHSFunctionExplicit");
+    return GB_ERR_UNSUPPORTED;
+  }
   if (c.model == GB_MODEL_NS3D && c.Re > 0) {
     gbh_set_error("gb_rhs_explicit_noalloc: the viscous term is not available here (Re > 0); "
                   "use gb_RHSFunctionExplicit");

@@ -27,6 +27,8 @@ struct gb_solver {
   double* d_snap = nullptr;  // copy of u before a monitored step (allocated on first use)
   double* d_red = nullptr;   // reduction partials (allocated on first use)
   double* d_grav = nullptr;  // gravity fields f, g (NavierStokes3D with gravity)
+  double* d_crX = nullptr;   // CRWENO5: interface values / elimination right-hand sides
+  double* d_crC = nullptr;   // CRWENO5: normalised super-diagonal of the elimination
   bool gravity = false;
   int* d_flag = nullptr;
   std::vector<int> mem_zones;  // zone indices applied in memory before each RHS

@@ -50,6 +50,9 @@ enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
  * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
 enum { GB_WENO_JS = 0, GB_WENO_MAPPED = 1, GB_WENO_BORGES = 2, GB_WENO_YC = 3, GB_WENO_NONE = 4 };
 enum { GB_MEM_HOST = 0, GB_MEM_DEVICE = 1 };
+/* hyp_space_scheme: weno5, or crweno5 (compact WENO5, a tridiagonal solve per grid
+ * line: component-wise, without gravity; Interp1PrimFifthOrderCRWENO.c) */
+enum { GB_SCHEME_WENO5 = 0, GB_SCHEME_CRWENO5 = 1 };
 
 #define GB_MAX_ZONES 12
 
@@ -84,6 +87,7 @@ typedef struct gb_config {
    * hydrostatic fields of gb_solver_set_gravity_field */
   double gravity[3], rho_ref, p_ref, R_gas, N_bv;
   int HB;
+  int hyp_scheme;           /* GB_SCHEME_* (solver.inp hyp_space_scheme) */
 } gb_config;
 
 typedef struct gb_solver gb_solver;

@@ -93,7 +93,7 @@ def test_reader_errors(built_lib, tmp_path):
     _expect(4, str(d))
     d = tmp_path / "e"
     case.write(str(d))
-    t = open(d / "solver.inp").read().replace("weno5", "crweno5")
+    t = open(d / "solver.inp").read().replace("weno5", "hcweno5")
     open(d / "solver.inp", "w").write(t)
     _expect(4, str(d))
     d = tmp_path / "f"
@@ -251,3 +251,18 @@ def test_solver_create_rejects_bad_gravity(built_lib):
         rc = L.gb_solver_create(ctypes.byref(cfg), dx.ctypes.data_as(_lib.DP), -1, ctypes.byref(h))
         assert not h.value
         assert rc == rc_want and msg in L.gb_last_error(), (rc, L.gb_last_error())
+
+
+def test_reader_crweno(built_lib, tmp_path):
+    """hyp_space_scheme crweno5 -> gb_config.hyp_scheme; the characteristic form and
+    gravity with it are not on this path."""
+    case = C.sod(16, n_iter=1)
+    case.hyp_scheme = "crweno5"
+    assert Inputs(str(_deck(tmp_path / "a", case))).config.hyp_scheme == _lib.SCHEME["crweno5"]
+    assert Inputs(str(_deck(tmp_path / "b", C.sod(16, n_iter=1)))).config.hyp_scheme == _lib.SCHEME["weno5"]
+    case = C.vortex(12, n_iter=1, dt=0.01)  # characteristic
+    case.hyp_scheme = "crweno5"
+    _expect(4, str(_deck(tmp_path / "c", case)))
+    case = C.rising_thermal_bubble(8, n_iter=1)
+    case.hyp_scheme = "crweno5"
+    _expect(4, str(_deck(tmp_path / "d", case)))
