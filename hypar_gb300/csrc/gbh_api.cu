@@ -24,8 +24,9 @@ cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const do
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
-cudaError_t launch_hyp_crweno(int, int, int, const double*, double*, const double*, const DevGeom&,
+cudaError_t launch_hyp_crweno(int, int, int, bool, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, double*, double*, cudaStream_t);
+size_t crweno_scratch_doubles(int, int, long long, bool, bool);
 cudaError_t launch_hyp_ns3d_grav(int, int, const double*, double*, const double*, const DevGeom&,
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_unfused_euler1d(int, int, int, double*, const double*, const double*, const double*,
@@ -109,8 +110,8 @@ static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const Stag
   const gb_config& c = s->cfg;
   const double* dx = s->d_dxinv + s->dx_off[dir];
   if (c.hyp_scheme == GB_SCHEME_CRWENO5)
-    return launch_hyp_crweno(c.model, dir, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->d_crX,
-                             s->d_crC, s->stream);
+    return launch_hyp_crweno(c.model, dir, c.upwind, c.interp == GB_INTERP_CHARACTERISTIC, U, s->d_H, dx, s->G,
+                             s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->stream);
   if (s->gravity) {
     if (!s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
     return launch_hyp_ns3d_grav(dir, c.interp, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
@@ -207,10 +208,6 @@ int gbh_validate(const gb_config* c) {
   if (!(c->weno_eps > 0.0)) { gbh_set_error("weno_eps must be positive"); return GB_ERR_ARG; }
   if (c->weno_weights < GB_WENO_JS || c->weno_weights > GB_WENO_NONE) { gbh_set_error("bad weno_weights"); return GB_ERR_ARG; }
   if (c->hyp_scheme != GB_SCHEME_WENO5 && c->hyp_scheme != GB_SCHEME_CRWENO5) { gbh_set_error("bad hyp_scheme"); return GB_ERR_ARG; }
-  if (c->hyp_scheme == GB_SCHEME_CRWENO5 && c->interp == GB_INTERP_CHARACTERISTIC) {
-    gbh_set_error("characteristic CRWENO5 is not available on this path (component-wise only)");
-    return GB_ERR_UNSUPPORTED;
-  }
   if (c->gravity[0] != 0.0 || c->gravity[1] != 0.0 || c->gravity[2] != 0.0) {
     if (c->model != GB_MODEL_NS3D) { gbh_set_error("gravity: NavierStokes3D only on this path"); return GB_ERR_UNSUPPORTED; }
     if (c->hyp_scheme == GB_SCHEME_CRWENO5) { gbh_set_error("gravity with CRWENO5 is not available on this path"); return GB_ERR_UNSUPPORTED; }
@@ -331,16 +328,20 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   for (int k = 1; k < c.rk_nstages; k++) A(&s->d_P[k], bytes);
   if (c.ndims > 1) A(&s->d_H, bytes);
   if (c.hyp_scheme == GB_SCHEME_CRWENO5) {
-    // per direction (N+1) interfaces x lines x 4 reconstructions x nvars, the largest
-    size_t ncr = 0;
+    // the largest direction's interface values and elimination scratch
+    const bool chr = c.interp == GB_INTERP_CHARACTERISTIC;
+    size_t nx = 0, nc = 0;
     for (int d = 0; d < c.ndims; d++) {
-      size_t n = (size_t)(c.dim[d] + 1) * 4 * c.nvars;
+      long long lines = 1;
       for (int e = 0; e < c.ndims; e++)
-        if (e != d) n *= (size_t)c.dim[e];
-      ncr = n > ncr ? n : ncr;
+        if (e != d) lines *= c.dim[e];
+      size_t a = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, false);
+      size_t b = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, true);
+      nx = a > nx ? a : nx;
+      nc = b > nc ? b : nc;
     }
-    A(&s->d_crX, ncr * sizeof(double));
-    A(&s->d_crC, ncr * sizeof(double));
+    A(&s->d_crX, nx * sizeof(double));
+    A(&s->d_crC, nc * sizeof(double));
   }
   if (s->viscous) {
     A(&s->d_par, bytes);

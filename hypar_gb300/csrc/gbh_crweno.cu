@@ -223,6 +223,245 @@ cr_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, double* 
   }
 }
 
+// Characteristic CRWENO5 (Interp1PrimFifthOrderCRWENOChar.c:139-230): one thread per
+// (grid line, reconstruction).  At interface I the rows of the nvars characteristic
+// fields share the left eigenvectors L of the Roe average of the two cell-centre
+// states: diag(a) L F_{I-1} + diag(b) L F_I + diag(c) L F_{I+1} = r, with per field
+// the component-wise coefficients (here times 3) and r the weighted compact candidates
+// of the characteristic stencil L f (weights of the characteristic stencils, CRWENO5 /
+// WENO5 optimal weights); the first and last interfaces: L F = r (explicit WENO5).
+// Block elimination, normalised: with F_{I-1} = y'_{I-1} - C'_{I-1} F_I,
+//   D = diag(b) L - diag(a) (L C'_{I-1}),  D [C'_I | y'_I] = [diag(c) L | r - diag(a) L y'_{I-1}],
+// solved by Gaussian elimination with partial pivoting, C'_I and y'_I stored per
+// interface (nvars^2 + nvars doubles, [interface][entry][system] for coalescing),
+// then F_I = y'_I - C'_I F_{I+1}
+// backwards into X in the component-wise layout, which cr_flux_kernel reads.
+template <int M, int DIR, bool ALTW>
+__global__ void __launch_bounds__(64)
+cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, double* __restrict__ X,
+                     double* __restrict__ S, long long ntrans) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND, NE = NV * NV + NV;
+  const long long nsys = ntrans * 4;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= nsys) return;
+  const long long line = tid % ntrans;
+  const int k = (int)(tid / ntrans);
+  const bool left = (k % 2) == 0, fx = k < 2;
+  const long long pbase = line_base<ND, DIR>(G, line);
+  const int N = G.dim[DIR];
+  const long long sd = G.stride[DIR];
+  const int lo = G.bclo[DIR], hi = G.bchi[DIR];
+  const double eps4 = 4.0 * pp.eps;
+  const double s6 = 1.0 / 6.0;
+  const long long nX = ntrans * 4 * NV;
+
+  // window of cells I-3 .. I+2: the weights' quantity (f or u), the modified energy
+  // (u reconstructions of NavierStokes3D), and the Roe-average ingredients
+  double wq[6][NV], wE[6];
+  RoeSide rs[6];
+  auto load = [&](int i, int slot) {
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    double uu[NV];
+#pragma unroll
+    for (int e = 0; e < NV; e++) uu[e] = U[pt * NV + e];
+    Prim<M> q = to_prim<M>(uu, pp);
+    rs[slot] = roe_side<M>(q);
+    if (fx) {
+      cell_flux<M, DIR>(q, wq[slot]);
+    } else {
+#pragma unroll
+      for (int e = 0; e < NV; e++) wq[slot][e] = uu[e];
+    }
+    wE[slot] = (!fx && M == MODEL_NS3D) ? ufunc_energy<M>(q, pp, uu[NV - 1]) : wq[slot][NV - 1];
+  };
+#pragma unroll
+  for (int p = 0; p < 5; p++) load(p - 3, p + 1);
+
+  double Cp[NV][NV], yp[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    yp[i] = 0.0;
+#pragma unroll
+    for (int j = 0; j < NV; j++) Cp[i][j] = 0.0;
+  }
+  for (int I = 0; I <= N; I++) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+#pragma unroll
+      for (int e = 0; e < NV; e++) wq[p][e] = wq[p + 1][e];
+      wE[p] = wE[p + 1];
+      rs[p] = rs[p + 1];
+    }
+    load(I + 2, 5);
+    const Eig E = roe_eig<M, DIR>(rs[2], rs[3], pp);
+    const bool bnd = (I == 0) || (I == N);
+    // characteristic stencils (f_{j-2} .. f_{j+2} of this bias): weights' and values'
+    double pw[5][NV], pv[5][NV];
+#pragma unroll
+    for (int m = 0; m < 5; m++) {
+      const int slot = left ? m : 5 - m;
+      projL<M, DIR>(E, pp, wq[slot], pw[m]);
+      if (!fx && M == MODEL_NS3D) {
+        double t[NV];
+#pragma unroll
+        for (int e = 0; e < NV; e++) t[e] = wq[slot][e];
+        t[NV - 1] = wE[slot];
+        projL<M, DIR>(E, pp, t, pv[m]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < NV; e++) pv[m][e] = pw[m][e];
+      }
+    }
+    double ca[NV], cb[NV], cc[NV], r[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double sw[5], sv[5];
+#pragma unroll
+      for (int m = 0; m < 5; m++) {
+        sw[m] = pw[m][v];
+        sv[m] = pv[m][v];
+      }
+      double w1, w2, w3;
+      if (bnd) {
+        cr_weights<ALTW>(sw, 0.1, 0.6, 0.3, eps4, pp.wtype, w1, w2, w3);
+        const double f1 = fma(2.0, sv[0], fma(-7.0, sv[1], 11.0 * sv[2]));
+        const double f2 = fma(5.0, sv[2], fma(2.0, sv[3], -sv[1]));
+        const double f3 = fma(5.0, sv[3], fma(2.0, sv[2], -sv[4]));
+        r[v] = fma(w1, f1, fma(w2, f2, w3 * f3)) * s6;
+        ca[v] = cc[v] = 0.0;
+        cb[v] = 1.0;
+      } else {
+        cr_weights<ALTW>(sw, 0.2, 0.5, 0.3, eps4, pp.wtype, w1, w2, w3);
+        const double f1 = fma(5.0, sv[2], sv[1]);
+        const double f2 = fma(5.0, sv[2], sv[3]);
+        const double f3 = fma(5.0, sv[3], sv[2]);
+        r[v] = 0.5 * fma(w1, f1, fma(w2, f2, w3 * f3));
+        const double lo3 = fma(2.0, w1, w2);
+        ca[v] = left ? lo3 : w3;
+        cc[v] = left ? w3 : lo3;
+        cb[v] = fma(2.0, w2 + w3, w1);
+      }
+    }
+    double y[NV], Cn[NV][NV];
+    if (bnd) {
+      // L F = r: F = R r
+      projR<M, DIR>(E, r, y);
+#pragma unroll
+      for (int i = 0; i < NV; i++)
+#pragma unroll
+        for (int j = 0; j < NV; j++) Cn[i][j] = 0.0;
+    } else {
+      // D = diag(b) L - diag(a) L C', right-hand sides diag(c) L and r - diag(a) L y'
+      double D[NV][NV], Rh[NV][NV + 1];
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        double ej[NV], lj[NV], col[NV], mj[NV];
+#pragma unroll
+        for (int e = 0; e < NV; e++) {
+          ej[e] = (e == j) ? 1.0 : 0.0;
+          col[e] = Cp[e][j];
+        }
+        projL<M, DIR>(E, pp, ej, lj);   // column j of L
+        projL<M, DIR>(E, pp, col, mj);  // column j of L C'
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+          D[i][j] = fma(-ca[i], mj[i], cb[i] * lj[i]);
+          Rh[i][j] = cc[i] * lj[i];
+        }
+      }
+      double ly[NV];
+      projL<M, DIR>(E, pp, yp, ly);
+#pragma unroll
+      for (int i = 0; i < NV; i++) Rh[i][NV] = fma(-ca[i], ly[i], r[i]);
+      // Gaussian elimination with partial pivoting (the characteristic fields are
+      // ordered differently from the reference's eigenvector rows, so the pivots the
+      // reference meets without pivoting are not the leading ones here: at rest the
+      // first field's row of L starts with a zero), then back-substitution
+      double dinv[NV];
+#pragma unroll
+      for (int i = 0; i < NV; i++) {
+#pragma unroll
+        for (int p = i + 1; p < NV; p++) {
+          const bool sw = fabs(D[p][i]) > fabs(D[i][i]);
+#pragma unroll
+          for (int q = i; q < NV; q++) {
+            const double t = D[i][q];
+            D[i][q] = sw ? D[p][q] : t;
+            D[p][q] = sw ? t : D[p][q];
+          }
+#pragma unroll
+          for (int q = 0; q <= NV; q++) {
+            const double t = Rh[i][q];
+            Rh[i][q] = sw ? Rh[p][q] : t;
+            Rh[p][q] = sw ? t : Rh[p][q];
+          }
+        }
+        dinv[i] = nr_rcp(D[i][i]);
+#pragma unroll
+        for (int j = i + 1; j < NV; j++) {
+          const double f = D[j][i] * dinv[i];
+#pragma unroll
+          for (int q = i + 1; q < NV; q++) D[j][q] = fma(-f, D[i][q], D[j][q]);
+#pragma unroll
+          for (int q = 0; q <= NV; q++) Rh[j][q] = fma(-f, Rh[i][q], Rh[j][q]);
+        }
+      }
+#pragma unroll
+      for (int i = NV - 1; i >= 0; i--) {
+#pragma unroll
+        for (int q = 0; q <= NV; q++) {
+          double t = Rh[i][q];
+#pragma unroll
+          for (int j = i + 1; j < NV; j++) t = fma(-D[i][j], Rh[j][q], t);
+          Rh[i][q] = t * dinv[i];
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NV; i++) {
+        y[i] = Rh[i][NV];
+#pragma unroll
+        for (int j = 0; j < NV; j++) Cn[i][j] = Rh[i][j];
+      }
+    }
+    double* so = S + (long long)I * NE * nsys + tid;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      so[(long long)i * nsys] = y[i];
+#pragma unroll
+      for (int j = 0; j < NV; j++) so[(long long)(NV + i * NV + j) * nsys] = Cn[i][j];
+      yp[i] = y[i];
+#pragma unroll
+      for (int j = 0; j < NV; j++) Cp[i][j] = Cn[i][j];
+    }
+  }
+  // back-substitution: F_N = y'_N, F_I = y'_I - C'_I F_{I+1}
+  double x[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) x[i] = yp[i];
+  {
+    double* xo = X + (long long)N * nX + (long long)k * NV * ntrans + line;
+#pragma unroll
+    for (int i = 0; i < NV; i++) xo[(long long)i * ntrans] = x[i];
+  }
+  for (int I = N - 1; I >= 0; I--) {
+    const double* so = S + (long long)I * NE * nsys + tid;
+    double xn[NV];
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double t = so[(long long)i * nsys];
+#pragma unroll
+      for (int j = 0; j < NV; j++) t = fma(-so[(long long)(NV + i * NV + j) * nsys], x[j], t);
+      xn[i] = t;
+    }
+    double* xo = X + (long long)I * nX + (long long)k * NV * ntrans + line;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      x[i] = xn[i];
+      xo[(long long)i * ntrans] = x[i];
+    }
+  }
+}
+
 // The stage epilogue of the fused kernel for one cell (hyp_segment's): h is
 // this direction's dxinv (F_{j+1/2} - F_{j-1/2}).
 template <int NV>
@@ -321,7 +560,7 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
 }
 
 template <int M, int DIR, bool ALTW, int UPW>
-static cudaError_t cr_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
+static cudaError_t cr_dir(bool chr, const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                           const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
                           cudaStream_t s) {
   constexpr int NV = ModelTraits<M>::NV;
@@ -329,7 +568,12 @@ static cudaError_t cr_dir(const double* U, double* H, const double* dxinv_dir, c
   for (int e = 0; e < G.nd; e++)
     if (e != DIR) ntrans *= G.dim[e];
   const long long nsys = ntrans * 4 * NV;
-  cr_solve_kernel<M, DIR, ALTW><<<(unsigned)((nsys + 127) / 128), 128, 0, s>>>(U, G, pp, X, Cp, ntrans);
+  if (chr) {
+    const long long nchr = ntrans * 4;
+    cr_char_solve_kernel<M, DIR, ALTW><<<(unsigned)((nchr + 63) / 64), 64, 0, s>>>(U, G, pp, X, Cp, ntrans);
+  } else {
+    cr_solve_kernel<M, DIR, ALTW><<<(unsigned)((nsys + 127) / 128), 128, 0, s>>>(U, G, pp, X, Cp, ntrans);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   const int seg = L.seg > 0 ? L.seg : 32;
@@ -342,44 +586,51 @@ static cudaError_t cr_dir(const double* U, double* H, const double* dxinv_dir, c
 }
 
 template <int M, int DIR, bool ALTW>
-static cudaError_t cr_dir_upw(int upw, const double* U, double* H, const double* dx, const DevGeom& G,
+static cudaError_t cr_dir_upw(bool chr, int upw, const double* U, double* H, const double* dx, const DevGeom& G,
                               const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
                               cudaStream_t s) {
   switch (upw) {
-    case UPW_ROE: return cr_dir<M, DIR, ALTW, UPW_ROE>(U, H, dx, G, pp, ep, L, X, Cp, s);
-    case UPW_LLF: return cr_dir<M, DIR, ALTW, UPW_LLF>(U, H, dx, G, pp, ep, L, X, Cp, s);
-    case UPW_RF: return cr_dir<M, DIR, ALTW, UPW_RF>(U, H, dx, G, pp, ep, L, X, Cp, s);
+    case UPW_ROE: return cr_dir<M, DIR, ALTW, UPW_ROE>(chr, U, H, dx, G, pp, ep, L, X, Cp, s);
+    case UPW_LLF: return cr_dir<M, DIR, ALTW, UPW_LLF>(chr, U, H, dx, G, pp, ep, L, X, Cp, s);
+    case UPW_RF: return cr_dir<M, DIR, ALTW, UPW_RF>(chr, U, H, dx, G, pp, ep, L, X, Cp, s);
     default:
       if (M == MODEL_EULER2D) return cudaErrorInvalidValue;  // Euler2D has no Rusanov
-      return cr_dir<M, DIR, ALTW, (M == MODEL_EULER2D ? UPW_ROE : UPW_RUS)>(U, H, dx, G, pp, ep, L, X, Cp, s);
+      return cr_dir<M, DIR, ALTW, (M == MODEL_EULER2D ? UPW_ROE : UPW_RUS)>(chr, U, H, dx, G, pp, ep, L, X, Cp, s);
   }
 }
 
 template <int M, bool ALTW>
-static cudaError_t cr_model(int dir, int upw, const double* U, double* H, const double* dx, const DevGeom& G,
-                            const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
-                            cudaStream_t s) {
+static cudaError_t cr_model(bool chr, int dir, int upw, const double* U, double* H, const double* dx,
+                            const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X,
+                            double* Cp, cudaStream_t s) {
   constexpr int ND = ModelTraits<M>::ND;
-  if (dir == 0) return cr_dir_upw<M, 0, ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
-  if (ND > 1 && dir == 1) return cr_dir_upw<M, (ND > 1 ? 1 : 0), ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
-  if (ND > 2 && dir == 2) return cr_dir_upw<M, (ND > 2 ? 2 : 0), ALTW>(upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  if (dir == 0) return cr_dir_upw<M, 0, ALTW>(chr, upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  if (ND > 1 && dir == 1) return cr_dir_upw<M, (ND > 1 ? 1 : 0), ALTW>(chr, upw, U, H, dx, G, pp, ep, L, X, Cp, s);
+  if (ND > 2 && dir == 2) return cr_dir_upw<M, (ND > 2 ? 2 : 0), ALTW>(chr, upw, U, H, dx, G, pp, ep, L, X, Cp, s);
   return cudaErrorInvalidValue;
 }
 
-// One direction of the hyperbolic term with CRWENO5 (component-wise).  X and Cp:
-// (N+1) * ntrans * 4 * nvars doubles each for this direction.
-cudaError_t launch_hyp_crweno(int model, int dir, int upw, const double* U, double* H, const double* dxinv_dir,
-                              const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
-                              double* X, double* Cp, cudaStream_t s) {
+// Scratch per direction (doubles): X holds (N+1) * lines * 4 * nvars interface values;
+// the second array the elimination: (N+1) * lines * 4 * nvars (component-wise) or
+// (N+1) * lines * 4 * (nvars^2 + nvars) (characteristic).
+size_t crweno_scratch_doubles(int nvars, int n_interfaces, long long lines, bool chr, bool second) {
+  if (!second || !chr) return (size_t)n_interfaces * (size_t)lines * 4 * (size_t)nvars;
+  return (size_t)n_interfaces * (size_t)lines * 4 * (size_t)(nvars * nvars + nvars);
+}
+
+// One direction of the hyperbolic term with CRWENO5, component-wise or characteristic.
+cudaError_t launch_hyp_crweno(int model, int dir, int upw, bool chr, const double* U, double* H,
+                              const double* dxinv_dir, const DevGeom& G, const PhysParams& pp, const StageEpi& ep,
+                              const HypLaunch& L, double* X, double* Cp, cudaStream_t s) {
   const bool alt = pp.wtype != WENO_W_JS;
   if (model == MODEL_EULER1D)
-    return alt ? cr_model<MODEL_EULER1D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
-               : cr_model<MODEL_EULER1D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+    return alt ? cr_model<MODEL_EULER1D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+               : cr_model<MODEL_EULER1D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
   if (model == MODEL_EULER2D)
-    return alt ? cr_model<MODEL_EULER2D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
-               : cr_model<MODEL_EULER2D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
-  return alt ? cr_model<MODEL_NS3D, true>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
-             : cr_model<MODEL_NS3D, false>(dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+    return alt ? cr_model<MODEL_EULER2D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+               : cr_model<MODEL_EULER2D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
+  return alt ? cr_model<MODEL_NS3D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s)
+             : cr_model<MODEL_NS3D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, s);
 }
 
 }  // namespace gbh

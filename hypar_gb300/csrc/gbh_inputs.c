@@ -492,10 +492,6 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     gbh_set_error("hyp_interp_type %s invalid", si.interp_type);
     return GB_ERR_INPUT;
   }
-  if (c.hyp_scheme == GB_SCHEME_CRWENO5 && c.interp == GB_INTERP_CHARACTERISTIC) {
-    gbh_set_error("characteristic CRWENO5 is not available on this path (component-wise only)");
-    return GB_ERR_UNSUPPORTED;
-  }
   if (strcmp(si.time_scheme, "rk")) {
     gbh_set_error("time_scheme %s not supported (rk only)", si.time_scheme);
     return GB_ERR_UNSUPPORTED;

@@ -1038,6 +1038,139 @@ static int crweno_line(const orc_problem *p, const double *fC, const double *u, 
   return 0;
 }
 
+/* _MatrixInvert_ (include/matops.h:93-125): B = A^{-1} for an n x n row-major
+ * matrix by elimination without pivoting on a copy of A applied to the identity,
+ * then the backward sweep, in the reference's operation order. */
+static void mat_invert(int n, const double *A, double *B) {
+  double Ac[MAXV * MAXV];
+  for (int i = 0; i < n * n; i++) Ac[i] = A[i];
+  for (int i = 0; i < n * n; i++) B[i] = 0.0;
+  for (int i = 0; i < n; i++) B[i * n + i] = 1.0;
+  for (int i = 0; i < n - 1; i++)
+    for (int j = i + 1; j < n; j++) {
+      double factor = Ac[j * n + i] / Ac[i * n + i];
+      for (int k = i + 1; k < n; k++) Ac[j * n + k] -= (factor * Ac[i * n + k]);
+      for (int k = 0; k < j; k++) B[j * n + k] -= (factor * B[i * n + k]);
+    }
+  for (int i = n - 1; i >= 0; i--)
+    for (int k = 0; k < n; k++) {
+      double sum = 0.0;
+      for (int j = i + 1; j < n; j++) sum += (Ac[i * n + j] * B[j * n + k]);
+      B[i * n + k] = (B[i * n + k] - sum) / Ac[i * n + i];
+    }
+}
+/* _MatrixMultiplySubtract_: C -= A B, one product at a time. */
+static void mat_mul_sub(int n, double *C, const double *A, const double *B) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) C[i * n + j] -= (A[i * n + k] * B[k * n + j]);
+}
+/* _MatVecMultiplySubtract_: y -= A x. */
+static void matvec_sub(int n, double *y, const double *A, const double *x) {
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++) y[i] -= (A[i * n + j] * x[j]);
+}
+
+/* blocktridiagLU (src/TridiagLU/blocktridiagLU.c) on one rank, one system of n block
+ * rows of size bs (a, b, c: n bs*bs row-major blocks; x: n bs values, the solution on
+ * return): elimination of the sub-diagonal blocks with the inverse of the previous
+ * diagonal block, then block back-substitution (the missing next-rank values are zero). */
+static void block_tridiag_solve(int n, int bs, double *a, double *b, double *c, double *x) {
+  const int bs2 = bs * bs;
+  double binv[MAXV * MAXV], factor[MAXV * MAXV], xt[MAXV];
+  for (int i = 1; i < n; i++) {
+    mat_invert(bs, b + (i - 1) * bs2, binv);
+    matmul(bs, factor, a + i * bs2, binv);
+    mat_mul_sub(bs, b + i * bs2, factor, c + (i - 1) * bs2);
+    for (int q = 0; q < bs2; q++) a[i * bs2 + q] = 0.0;
+    mat_mul_sub(bs, a + i * bs2, factor, a + (i - 1) * bs2);
+    matvec_sub(bs, x + i * bs, factor, x + (i - 1) * bs);
+  }
+  const double xp1[MAXV] = {0.0};
+  mat_invert(bs, b + (n - 1) * bs2, binv);
+  matvec_sub(bs, x + (n - 1) * bs, a + (n - 1) * bs2, x);
+  matvec_sub(bs, x + (n - 1) * bs, c + (n - 1) * bs2, xp1);
+  matvec(bs, xt, binv, x + (n - 1) * bs);
+  for (int j = 0; j < bs; j++) x[(n - 1) * bs + j] = xt[j];
+  for (int i = n - 2; i > -1; i--) {
+    mat_invert(bs, b + i * bs2, binv);
+    matvec_sub(bs, x + i * bs, c + i * bs2, x + (i + 1) * bs);
+    matvec_sub(bs, x + i * bs, a + i * bs2, x);
+    matvec(bs, xt, binv, x + i * bs);
+    for (int j = 0; j < bs; j++) x[i * bs + j] = xt[j];
+  }
+}
+
+/* Interp1PrimFifthOrderCRWENOChar (Interp1PrimFifthOrderCRWENOChar.c:139-230) on one
+ * grid line: per interface the left eigenvectors L of the Roe average of the two
+ * cell-centre states, the characteristic stencils L f, and block rows
+ * A = a L, B = b L, C = c L (a, b, c per characteristic field, as the component-wise
+ * rows with b = w1/3 + 2 (w2 + w3)/3), right-hand side sum_k w_k f_k; the first and last
+ * interfaces: B = L and the explicit WENO5 value.  Weights: the characteristic weights
+ * (WENOFifthOrderCalculateWeightsChar*, projections of f and u) with the CRWENO5 /
+ * WENO5 optimal weights.  out[(I*4 + k)*nv + v]; work: (N+1) (3 nv^2 + nv) doubles. */
+static int crweno_char_line(const orc_problem *p, const double *fC, const double *u, const double *uC, long base,
+                            long sd, int N, int dir, double *out, double *work) {
+  static const double one_third = 1.0 / 3.0;
+  static const double one_sixth = 1.0 / 6.0;
+  const int nv = p->nvars, n = N + 1, nv2 = nv * nv;
+  double *A = work, *B = work + (long)n * nv2, *Cm = work + 2L * n * nv2, *F = work + 3L * n * nv2;
+  for (int k = 0; k < 4; k++) {
+    const double *val = k < 2 ? fC : uC, *wv = k < 2 ? fC : u;
+    const int upw = (k % 2 == 0) ? 1 : -1;
+    for (int I = 0; I <= N; I++) {
+      const long qm1 = upw > 0 ? base + (long)(I - 1) * sd : base + (long)I * sd;
+      const long st = upw > 0 ? sd : -sd;
+      const long q[5] = {qm1 - 2 * st, qm1 - st, qm1, qm1 + st, qm1 + 2 * st}; /* qm3 qm2 qm1 qp1 qp2 */
+      double uavg[MAXV], L[MAXV * MAXV];
+      /* the Roe average of the cells either side (symmetric in its arguments) */
+      m_roeavg(p, uavg, u + nv * (base + (long)(I - 1) * sd), u + nv * (base + (long)I * sd));
+      m_left(p, L, uavg, dir);
+      double pw[5][MAXV], pv[5][MAXV];
+      for (int m = 0; m < 5; m++) {
+        matvec(nv, pw[m], L, wv + nv * q[m]);
+        matvec(nv, pv[m], L, val + nv * q[m]);
+      }
+      const int bnd = (I == 0) || (I == N);
+      double *Ai = A + (long)I * nv2, *Bi = B + (long)I * nv2, *Ci = Cm + (long)I * nv2;
+      for (int v = 0; v < nv; v++) {
+        double w1, w2, w3;
+        weno_w_c(p->weights, bnd ? WENO_C : CRWENO_C, pw[0][v], pw[1][v], pw[2][v], pw[3][v], pw[4][v], p->eps,
+                 &w1, &w2, &w3);
+        const double fm3 = pv[0][v], fm2 = pv[1][v], fm1 = pv[2][v], fp1 = pv[3][v], fp2 = pv[4][v];
+        double f1, f2, f3;
+        if (bnd) {
+          f1 = (2 * one_sixth) * fm3 - (7.0 * one_sixth) * fm2 + (11.0 * one_sixth) * fm1;
+          f2 = (-one_sixth) * fm2 + (5.0 * one_sixth) * fm1 + (2 * one_sixth) * fp1;
+          f3 = (2 * one_sixth) * fm1 + (5 * one_sixth) * fp1 - (one_sixth) * fp2;
+          for (int e = 0; e < nv; e++) {
+            Ai[v * nv + e] = 0.0;
+            Ci[v * nv + e] = 0.0;
+            Bi[v * nv + e] = L[v * nv + e];
+          }
+        } else {
+          f1 = (one_sixth) * (fm2 + 5 * fm1);
+          f2 = (one_sixth) * (5 * fm1 + fp1);
+          f3 = (one_sixth) * (fm1 + 5 * fp1);
+          const double lo = (2 * one_third) * w1 + (one_third) * w2;
+          const double di = (one_third) * w1 + (2 * one_third) * (w2 + w3);
+          const double up = (one_third) * w3;
+          for (int e = 0; e < nv; e++) {
+            Ai[v * nv + e] = (upw > 0 ? lo : up) * L[v * nv + e];
+            Bi[v * nv + e] = di * L[v * nv + e];
+            Ci[v * nv + e] = (upw > 0 ? up : lo) * L[v * nv + e];
+          }
+        }
+        F[(long)I * nv + v] = w1 * f1 + w2 * f2 + w3 * f3;
+      }
+    }
+    block_tridiag_solve(n, nv, A, B, Cm, F);
+    for (int I = 0; I <= N; I++)
+      for (int v = 0; v < nv; v++) out[((long)I * 4 + k) * nv + v] = F[(long)I * nv + v];
+  }
+  return 0;
+}
+
 /* The hyperbolic term and, with gravity, NavierStokes3DSource
  * (NavierStokes3DSource.c:38-112): per direction with gravity, the source
  * function [0, phi e_d, phi] (phi = g field) interpolated with the weights of the
@@ -1054,10 +1187,10 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
   double *uC = (double *)malloc(sizeof(double) * np * nv);
   long offset = 0;
   int crweno_failed = 0;
-  if (p->scheme == ORC_SCHEME_CRWENO5 && (p->interp != ORC_INTERP_COMP || p->has_grav)) {
+  if (p->scheme == ORC_SCHEME_CRWENO5 && p->has_grav) {
     free(fC);
     free(uC);
-    return -1; /* characteristic CRWENO5 and gravity with CRWENO5: not restated */
+    return -1; /* gravity with CRWENO5: not restated */
   }
   for (int d = 0; d < nd; d++) {
 #pragma omp parallel for schedule(static) num_threads(NTHR)
@@ -1077,8 +1210,9 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
       double *FI = (double *)malloc(sizeof(double) * (N + 1) * nv);
       double *SI = (double *)malloc(sizeof(double) * (N + 1) * nv);
       const int crweno = p->scheme == ORC_SCHEME_CRWENO5;
+      const int crchar = crweno && p->interp == ORC_INTERP_CHAR && nv > 1;
       double *CR = crweno ? (double *)malloc(sizeof(double) * (N + 1) * nv * 4) : NULL;
-      double *CW = crweno ? (double *)malloc(sizeof(double) * (N + 1) * 4) : NULL;
+      double *CW = crweno ? (double *)malloc(sizeof(double) * (N + 1) * (crchar ? 3 * nv * nv + nv : 4)) : NULL;
 #pragma omp for schedule(static)
       for (long lo = 0; lo < nouter; lo++) {
         int idx[3] = {0, 0, 0};
@@ -1086,7 +1220,8 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
         for (int e = 0; e < nd; e++) if (e != d) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
         idx[d] = 0;
         long base = pidx(p, s, idx); /* cell 0 of this line */
-        if (crweno && crweno_line(p, fC, u, uC, base, sd, N, CR, CW)) {
+        if (crchar ? crweno_char_line(p, fC, u, uC, base, sd, N, d, CR, CW)
+                   : (crweno && crweno_line(p, fC, u, uC, base, sd, N, CR, CW))) {
           crweno_failed = 1;
           continue;
         }

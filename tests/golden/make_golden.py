@@ -102,6 +102,17 @@ CASES = {
     "tgv12_crweno_roe_rk4": lambda: _cr(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05)),
     "tgv12_crweno_rusanov_borges": lambda: _w(_cr(C.tgv(12, n_iter=3, dt=0.02, upwinding="rusanov",
                                                          perturb=0.05)), "borges"),
+    "sod64_crweno_char_roe": lambda: _cr(C.sod(64, n_iter=20, dt=1e-3, interp="characteristic")),
+    "sod64_crweno_char_llf_yc": lambda: _w(_cr(C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                                      upwinding="llf-char", scheme="ssprk3")), "yc"),
+    "vortex24_crweno_char_roe": lambda: _cr(C.vortex(24, n_iter=4, dt=0.02)),
+    "vortex24_crweno_char_rf_mapped_slipwall": lambda: _w(_b(_cr(C.vortex(24, n_iter=4, dt=0.02,
+                                                                          upwinding="rf-char")),
+                                                             {(1, 1): ("slip-wall", [0.0, 0.0]),
+                                                              (1, -1): ("slip-wall", [0.0, 0.0])}), "mapped"),
+    "tgv12_crweno_char_roe_rk4": lambda: _cr(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic", perturb=0.05)),
+    "tgv12_crweno_char_rusanov_none": lambda: _w(_cr(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
+                                                            upwinding="rusanov", perturb=0.05)), "none"),
 }
 
 

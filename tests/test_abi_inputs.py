@@ -254,15 +254,16 @@ def test_solver_create_rejects_bad_gravity(built_lib):
 
 
 def test_reader_crweno(built_lib, tmp_path):
-    """hyp_space_scheme crweno5 -> gb_config.hyp_scheme; the characteristic form and
-    gravity with it are not on this path."""
+    """hyp_space_scheme crweno5 -> gb_config.hyp_scheme (component-wise and
+    characteristic); gravity with it is not on this path."""
     case = C.sod(16, n_iter=1)
     case.hyp_scheme = "crweno5"
     assert Inputs(str(_deck(tmp_path / "a", case))).config.hyp_scheme == _lib.SCHEME["crweno5"]
     assert Inputs(str(_deck(tmp_path / "b", C.sod(16, n_iter=1)))).config.hyp_scheme == _lib.SCHEME["weno5"]
     case = C.vortex(12, n_iter=1, dt=0.01)  # characteristic
     case.hyp_scheme = "crweno5"
-    _expect(4, str(_deck(tmp_path / "c", case)))
+    c = Inputs(str(_deck(tmp_path / "c", case))).config
+    assert c.hyp_scheme == _lib.SCHEME["crweno5"] and c.interp == _lib.INTERP["characteristic"]
     case = C.rising_thermal_bubble(8, n_iter=1)
     case.hyp_scheme = "crweno5"
     _expect(4, str(_deck(tmp_path / "d", case)))

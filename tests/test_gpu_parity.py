@@ -180,7 +180,9 @@ def test_golden_reference(built_lib, tmp_path, name):
     out = torch.zeros_like(u)
     s.rhs(out, u)
     rhs = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
-    if case.model == "navierstokes3d":
+    # the Taylor-Green decks are near-cancellations, and characteristic CRWENO5's block
+    # line solves amplify rounding: both are held to the FMA build's distance
+    if case.model == "navierstokes3d" or (case.hyp_scheme == "crweno5" and case.interp == "characteristic"):
         err, noise = conditioning_ok(name, rhs, case)
         assert relerr(rhs, g["rhs"]) <= 4.0 * noise + 1e-14
     else:
