@@ -22,6 +22,8 @@
 #include "gbh_internal.h"
 
 namespace gbh {
+cudaError_t launch_hyp_euler2d_wide_tape(int, const double*, double*, const double*, const DevGeom&,
+                                         const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_euler2d(int, int, int, const double*, double*, const double*, const DevGeom&,
                                const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 
@@ -38,8 +40,12 @@ __device__ __forceinline__ int fold2(int i, int N, int lo, int hi) {
 // gL, gR: adjoints of the two outputs; wb, vb: adjoint accumulators of the
 // weight stencil and of the value stencil (the same array when w == v).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v, double eps4, double gL, double gR,
-                                               double* wb, double* vb) {
+// TP: the smoothness terms B and the normalisation reciprocals come from the
+// forward kernel's wide tape tp[0..7] (weno5_pair_tape) instead of being recomputed
+// (bit-identical values: the same expressions).
+template <bool TP>
+__device__ __forceinline__ void weno5_pair_vjp_impl(const double* w, const double* v, double eps4, double gL,
+                                                    double gR, double* wb, double* vb, const double* tp) {
   const double k13 = 13.0 / 3.0;
   double d1 = fma(-2.0, w[1], w[0]) + w[2];
   double d2 = fma(-2.0, w[2], w[1]) + w[3];
@@ -51,12 +57,22 @@ __device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v,
   double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
   double gR2 = w[4] - w[2];
   double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
-  double BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
-  double BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
-  double BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
-  double BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
-  double BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
-  double BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
+  double BL1, BL2, BL3, BR1, BR2, BR3;
+  if (TP) {
+    BL1 = tp[0];
+    BL2 = tp[1];
+    BL3 = tp[2];
+    BR1 = tp[3];
+    BR2 = tp[4];
+    BR3 = tp[5];
+  } else {
+    BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
+    BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
+    BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
+    BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
+    BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
+    BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
+  }
   double qL1 = BL1 * BL1, qL2 = BL2 * BL2, qL3 = BL3 * BL3;
   double qR1 = BR1 * BR1, qR2 = BR2 * BR2, qR3 = BR3 * BR3;
   double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;
@@ -67,9 +83,16 @@ __device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v,
   double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4]));
   double nL = fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
   double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
-  double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
-  double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
-  double rL = nr_rcp(DL), rR = nr_rcp(DR);
+  double rL, rR;
+  if (TP) {
+    rL = tp[6];
+    rR = tp[7];
+  } else {
+    double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
+    double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
+    rL = nr_rcp(DL);
+    rR = nr_rcp(DR);
+  }
   double oL = nL * rL, oR = nR * rR;
   // reverse
   double nLb = gL * rL, DLb = -gL * oL * rL;
@@ -101,6 +124,11 @@ __device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v,
   vb[3] += 11.0 * cR1b + 2.0 * cAb + 5.0 * cBb;
   vb[4] += -7.0 * cR1b - cBb;
   vb[5] += 2.0 * cR1b;
+}
+
+__device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v, double eps4, double gL, double gR,
+                                               double* wb, double* vb) {
+  weno5_pair_vjp_impl<false>(w, v, eps4, gL, gR, wb, vb, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -347,7 +375,9 @@ __device__ __forceinline__ void terms_at(const AdjTerms& t, long long off, doubl
 // index (neighbouring segments and the other direction add to the same cells).
 // tape: the forward kernel's reconstructed states uL, uR of this direction
 // (StageEpi::tape layout), read instead of recomputed when present.
-template <int D>
+// WT: the tape is the wide one (TAPE_WIDE doubles per interface), whose smoothness
+// terms and normalisation reciprocals spare the pairs' forward recomputation.
+template <int D, bool WT>
 __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const AdjTerms& kt, double* Ub,
                                             const double* __restrict__ dxinv, const DevGeom& G,
                                             const PhysParams& pp, int seg, long long tr, int sg,
@@ -415,8 +445,8 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
       }
     }
     double uL[NV2], uR[NV2];
+    const double* t = tape ? tape + (tr * (N + 1) + I) * (WT ? TAPE_WIDE : 8) : nullptr;
     if (tape) {
-      const double* t = tape + (tr * (N + 1) + I) * 8;
 #pragma unroll
       for (int v = 0; v < NV2; v++) {
         uL[v] = t[v];
@@ -441,8 +471,13 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
         sf[p] = wf[p][v];
         su[p] = wu[p][v];
       }
-      weno5_pair_vjp(sf, sf, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf);
-      weno5_pair_vjp(su, su, eps4, uLb[v], uRb[v], gu, gu);
+      if (WT) {
+        weno5_pair_vjp_impl<true>(sf, sf, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf, t + 8 + v * 16);
+        weno5_pair_vjp_impl<true>(su, su, eps4, uLb[v], uRb[v], gu, gu, t + 16 + v * 16);
+      } else {
+        weno5_pair_vjp(sf, sf, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf);
+        weno5_pair_vjp(su, su, eps4, uLb[v], uRb[v], gu, gu);
+      }
 #pragma unroll
       for (int p = 0; p < 6; p++) {
         fbb[p][v] += gf[p];
@@ -458,6 +493,7 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
 
 // Both directions in one launch (they only add into Ub): threads
 // [0, n0) walk x-lines, [n0, n0 + n1) y-lines.
+template <bool WT>
 __global__ void __launch_bounds__(128)
 rhs_vjp_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
                const double* __restrict__ dx1, DevGeom G, PhysParams pp, int seg0, int nseg0, int seg1, int nseg1,
@@ -465,10 +501,10 @@ rhs_vjp_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const doub
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n0 = (long long)G.dim[1] * nseg0, n1 = (long long)G.dim[0] * nseg1;
   if (tid < n0) {
-    vjp_segment<0>(U, kt, Ub, dx0, G, pp, seg0, tid % G.dim[1], (int)(tid / G.dim[1]), tape0);
+    vjp_segment<0, WT>(U, kt, Ub, dx0, G, pp, seg0, tid % G.dim[1], (int)(tid / G.dim[1]), tape0);
   } else if (tid < n0 + n1) {
     const long long t = tid - n0;
-    vjp_segment<1>(U, kt, Ub, dx1, G, pp, seg1, t % G.dim[0], (int)(t / G.dim[0]), tape1);
+    vjp_segment<1, WT>(U, kt, Ub, dx1, G, pp, seg1, t % G.dim[0], (int)(t / G.dim[0]), tape1);
   }
 }
 
@@ -726,6 +762,7 @@ struct gb_adjoint {
   std::vector<double*> su[2];
   std::vector<double*> sP[2];
   std::vector<double*> sT[2];     // interface tapes of every stage of every step, [(i*4 + s)*2 + d]
+  int tape_w = 8;                 // doubles per interface in the tapes (8 or TAPE_WIDE)
   double* tblock2 = nullptr;      // their allocation
   int nbuf = 1;
   cudaStream_t aux = nullptr;     // recomputation stream
@@ -776,9 +813,14 @@ static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* U
   int n0s = (G.dim[0] + s0 - 1) / s0, n1s = (G.dim[1] + s1 - 1) / s1;
   long long nthr = (long long)G.dim[1] * n0s + (long long)G.dim[0] * n1s;
   const int blk = a->vjp_block;
-  rhs_vjp_kernel<<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
-      U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s,
-      tape ? tape[0] : nullptr, tape ? tape[1] : nullptr);
+  if (tape && a->tape_w == TAPE_WIDE)
+    rhs_vjp_kernel<true><<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
+        U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s, tape[0],
+        tape[1]);
+  else
+    rhs_vjp_kernel<false><<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
+        U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s,
+        tape ? tape[0] : nullptr, tape ? tape[1] : nullptr);
   AK(cudaGetLastError());
   return GB_OK;
 }
@@ -828,8 +870,11 @@ static int adj_step(gb_adjoint* a, cudaStream_t strm, const double* uin, double*
       e.first = (d == 0);
       e.last = (d == 1);
       e.tape = tapes ? tapes[2 * st + d] : nullptr;
-      AK(launch_hyp_euler2d(d, c.interp, c.upwind, U, a->H, a->d_dxinv + a->dx_off[d], a->G, a->pp, e, a->hl[d],
-                            strm));
+      if (e.tape && a->tape_w == TAPE_WIDE)
+        AK(launch_hyp_euler2d_wide_tape(d, U, a->H, a->d_dxinv + a->dx_off[d], a->G, a->pp, e, a->hl[d], strm));
+      else
+        AK(launch_hyp_euler2d(d, c.interp, c.upwind, U, a->H, a->d_dxinv + a->dx_off[d], a->G, a->pp, e, a->hl[d],
+                              strm));
     }
     for (int t = st + 1; t < ns; t++)
       if (ep.ca[t] != 0.0) touched[t] = 1;
@@ -924,9 +969,14 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->nbuf = a->nseg > 1 ? 2 : 1;
   size_t narr = (size_t)a->nseg + (size_t)a->nbuf * ((a->seglen + 1) + (size_t)a->seglen * (ns - 1)) + 1 + 1 + 4 + 1;
   a->bytes = narr * a->nvals * sizeof(double);
-  // interface tapes: per buffer, step and stage, uL and uR (8 values) at every
-  // interface of both directions
-  const size_t tape_x = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) * 8, tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * 8;
+  // interface tapes: per buffer, step and stage, at every interface of both
+  // directions uL and uR (8 values), widened to TAPE_WIDE values (the WENO pairs'
+  // smoothness terms and normalisations) while that stays within kWideTapeBytes
+  const size_t nif = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) + (size_t)cfg->dim[0] * (cfg->dim[1] + 1);
+  const size_t kWideTapeBytes = (size_t)24 << 30;
+  a->tape_w = (size_t)a->nbuf * a->seglen * ns * nif * TAPE_WIDE * sizeof(double) <= kWideTapeBytes ? TAPE_WIDE : 8;
+  const size_t tape_x = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) * a->tape_w;
+  const size_t tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * a->tape_w;
   const size_t tape_bytes = (size_t)a->nbuf * a->seglen * ns * (tape_x + tape_y) * sizeof(double);
   a->bytes += tape_bytes;
   if (device >= 0) {

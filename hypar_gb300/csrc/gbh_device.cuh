@@ -293,8 +293,9 @@ __device__ __forceinline__ void eigvals(double un, double a, double* lam) {
 // (they differ for the u-reconstruction, whose weights are computed from u
 // while the values are uC = UFunction(u), HyperbolicFunction.c:201-215).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void weno5_pair(const double* w, const double* v, double eps4, double& outL,
-                                           double& outR) {
+template <bool TP>
+__device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v, double eps4, double& outL,
+                                                double& outR, double* tp) {
   const double k13 = 13.0 / 3.0;
   // second differences, sub-stencils centred at p1..p4
   double d1 = fma(-2.0, w[1], w[0]) + w[2];
@@ -328,8 +329,32 @@ __device__ __forceinline__ void weno5_pair(const double* w, const double* v, dou
   double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
   double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
   double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
-  outL = nL * nr_rcp(DL);
-  outR = nR * nr_rcp(DR);
+  const double rL = nr_rcp(DL), rR = nr_rcp(DR);
+  outL = nL * rL;
+  outR = nR * rR;
+  if (TP) {
+    // the values the reverse pass would otherwise recompute first
+    tp[0] = BL1;
+    tp[1] = BL2;
+    tp[2] = BL3;
+    tp[3] = BR1;
+    tp[4] = BR2;
+    tp[5] = BR3;
+    tp[6] = rL;
+    tp[7] = rR;
+  }
+}
+
+__device__ __forceinline__ void weno5_pair(const double* w, const double* v, double eps4, double& outL,
+                                           double& outR) {
+  weno5_pair_impl<false>(w, v, eps4, outL, outR, nullptr);
+}
+
+// weno5_pair that also stores its smoothness terms B (left 1-3, right 1-3) and the
+// reciprocals of the two normalisations in tp[0..7] (the adjoint's tape).
+__device__ __forceinline__ void weno5_pair_tape(const double* w, const double* v, double eps4, double& outL,
+                                                double& outR, double* tp) {
+  weno5_pair_impl<true>(w, v, eps4, outL, outR, tp);
 }
 
 // Left/right WENO5 pair with the other weight formulations (runtime `wtype`).

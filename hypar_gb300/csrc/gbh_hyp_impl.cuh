@@ -284,7 +284,10 @@ __device__ __forceinline__ void wpair(const double* w, const double* v, double e
 // max(g_L, g_R) (NavierStokes3DUpwind.c:407) and, along a direction with
 // gravity, the source term of NavierStokes3DSource.c:38-112 subtracted from
 // the hyperbolic term of this direction (except when only that term is asked for).
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW = false, bool GRAV = false>
+// WT (Euler2D, component-wise, Jiang-Shu: the adjoint's configuration): the wide
+// tape -- per interface uL, uR and, per component, the smoothness terms and
+// normalisation reciprocals of the f and u pairs (TAPE_WIDE doubles).
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW = false, bool GRAV = false, bool WT = false>
 __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double* __restrict__ H,
                                             const double* __restrict__ dxinv, const DevGeom& G,
                                             const PhysParams& pp, const StageEpi& ep, int seg, long long tr,
@@ -376,6 +379,12 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           sf[p] = wf[p][v];
           su[p] = wu[p][v];
         }
+        if (WT) {
+          double* t = ep.tape + (line * (N + 1) + I) * TAPE_WIDE + 8 + v * 16;
+          weno5_pair_tape(sf, sf, eps4, fL[v], fR[v], t);
+          weno5_pair_tape(su, su, eps4, uL[v], uR[v], t + 8);
+          continue;
+        }
         // the source function phi = g is reconstructed with this flux component's
         // weights: evaluate them once and apply them to both
         const bool srcv = src_dir && (v == 1 + DIR || v == NV - 1);
@@ -405,8 +414,8 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
           SI[v] = 0.5 * (sL + sR);
         }
       }
-      if (M == MODEL_EULER2D && ep.tape) {
-        double* t = ep.tape + (line * (N + 1) + I) * 8;
+      if (M == MODEL_EULER2D && (WT || ep.tape)) {
+        double* t = ep.tape + (line * (N + 1) + I) * (WT ? TAPE_WIDE : 8);
 #pragma unroll
         for (int v = 0; v < NV; v++) {
           t[v] = uL[v];
@@ -543,13 +552,13 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
   }
 }
 
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false, bool WT = false>
 __global__ void __launch_bounds__(128)
 hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
                DevGeom G, PhysParams pp, StageEpi ep, int seg, int nseg, long long ntrans) {
   long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= ntrans * (long long)nseg) return;
-  hyp_segment<M, CHAR, UPW, DIR, ALTW, GRAV>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
+  hyp_segment<M, CHAR, UPW, DIR, ALTW, GRAV, WT>(U, H, dxinv, G, pp, ep, seg, tid % ntrans, (int)(tid / ntrans));
 }
 
 // All members of an ensemble advanced by one launch per direction: a thread
@@ -626,7 +635,7 @@ cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem
 }
 
 // Host launcher for one direction.
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false>
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false, bool WT = false>
 cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                        const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
   long long ntrans = 1;
@@ -638,8 +647,8 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   long long nthr = ntrans * nseg;
   int block = L.block > 0 ? L.block : 128;
   long long grid = (nthr + block - 1) / block;
-  hyp_dir_kernel<M, CHAR, UPW, DIR, ALTW, GRAV><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, seg,
-                                                                              nseg, ntrans);
+  hyp_dir_kernel<M, CHAR, UPW, DIR, ALTW, GRAV, WT><<<(unsigned)grid, block, 0, s>>>(U, H, dxinv_dir, G, pp, ep,
+                                                                                  seg, nseg, ntrans);
   return cudaGetLastError();
 }
 

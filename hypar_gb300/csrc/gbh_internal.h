@@ -32,6 +32,11 @@ struct DevGeom {
 //   EPI_RK   : k = -hyp + par, then the Runge-Kutta stage update
 enum { EPI_HYP = 0, EPI_RHS = 1, EPI_RK = 2 };
 
+// The adjoint's wide interface tape (Euler2D): uL, uR (8 values), then per component
+// the smoothness terms B (6) and normalisation reciprocals (2) of the f pair and of
+// the u pair.
+constexpr int TAPE_WIDE = 8 + 4 * 16;
+
 struct StageEpi {
   int mode;        // EPI_*
   int first;       // this direction is the first one (H is not read)

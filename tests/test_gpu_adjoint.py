@@ -178,8 +178,10 @@ def test_checkpoint_policies_agree(built_lib, problem):
         if ncheck == 1:
             assert adj.info()["recomputed_steps"] == 0
         adj.close()
+    # the reverse kernel adds the stencil adjoints with atomics, whose order varies
+    # from run to run: the same policy twice differs by ~5e-13 after 24 steps
     for g in grads[1:]:
-        assert np.linalg.norm(g - grads[0]) / np.linalg.norm(grads[0]) <= 1e-12
+        assert np.linalg.norm(g - grads[0]) / np.linalg.norm(grads[0]) <= 1e-11
 
 
 def test_misfit_gradient_vs_central_differences(built_lib, problem):
