@@ -25,7 +25,8 @@ cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const do
 cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_crweno(int, int, int, bool, const double*, double*, const double*, const DevGeom&,
-                              const PhysParams&, const StageEpi&, const HypLaunch&, double*, double*, cudaStream_t);
+                              const PhysParams&, const StageEpi&, const HypLaunch&, double*, double*, double*,
+                              cudaStream_t);
 size_t crweno_scratch_doubles(int, int, long long, bool, bool);
 cudaError_t launch_hyp_ns3d_grav(int, int, const double*, double*, const double*, const DevGeom&,
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
@@ -111,7 +112,7 @@ static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const Stag
   const double* dx = s->d_dxinv + s->dx_off[dir];
   if (c.hyp_scheme == GB_SCHEME_CRWENO5)
     return launch_hyp_crweno(c.model, dir, c.upwind, c.interp == GB_INTERP_CHARACTERISTIC, U, s->d_H, dx, s->G,
-                             s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->stream);
+                             s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->d_crF, s->stream);
   if (s->gravity) {
     if (!s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
     return launch_hyp_ns3d_grav(dir, c.interp, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
@@ -342,6 +343,7 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
     }
     A(&s->d_crX, nx * sizeof(double));
     A(&s->d_crC, nc * sizeof(double));
+    if (!chr) A(&s->d_crF, bytes);
   }
   if (s->viscous) {
     A(&s->d_par, bytes);
@@ -370,6 +372,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_H);
   cudaFree(s->d_crX);
   cudaFree(s->d_crC);
+  cudaFree(s->d_crF);
   cudaFree(s->d_par);
   cudaFree(s->d_Q);
   cudaFree(s->d_Gr);

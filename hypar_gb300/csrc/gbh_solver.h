@@ -29,6 +29,7 @@ struct gb_solver {
   double* d_grav = nullptr;  // gravity fields f, g (NavierStokes3D with gravity)
   double* d_crX = nullptr;   // CRWENO5: interface values / elimination right-hand sides
   double* d_crC = nullptr;   // CRWENO5: normalised super-diagonal of the elimination
+  double* d_crF = nullptr;   // CRWENO5 (component-wise): cell fluxes of the current direction
   bool gravity = false;
   int* d_flag = nullptr;
   std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
