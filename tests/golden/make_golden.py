@@ -113,7 +113,18 @@ CASES = {
     "tgv12_crweno_char_roe_rk4": lambda: _cr(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic", perturb=0.05)),
     "tgv12_crweno_char_rusanov_none": lambda: _w(_cr(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
                                                             upwinding="rusanov", perturb=0.05)), "none"),
+    "rtb12_comp_rusanov_visc_stir": lambda: _visc(_stir(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                                 perturb=0.02)), 100.0),
+    "vortex24_crweno_char_roe_subsonic_io": lambda: _b(_cr(C.vortex(24, n_iter=4, dt=0.02)),
+                                                       {(0, 1): ("subsonic-inflow", [1.0, 0.5, 0.0]),
+                                                        (0, -1): ("subsonic-outflow", [1.0 / 1.4])}),
 }
+
+
+def _visc(case, Re):
+    """NavierStokes3D deck with the viscous term (Re, Pr 0.72, Minf 1)."""
+    case.Re, case.Pr, case.Minf = Re, 0.72, 1.0
+    return case
 
 
 def _cr(case):
