@@ -101,11 +101,13 @@ class Adjoint:
         check(lib().gb_adjoint_info(self._h, ctypes.byref(L), ctypes.byref(n), ctypes.byref(r), ctypes.byref(b)))
         return {"segment_len": L.value, "segments": n.value, "recomputed_steps": r.value, "bytes": b.value}
 
-    def autotune(self, u, reps: int = 3, candidates=(2, 3, 4, 6, 8, 12, 16, 24, 32), blocks=(32, 64, 128)):
+    def autotune(self, u, reps: int = 3, candidates=(2, 3, 4, 6, 8, 12, 16, 24, 32), blocks=(32, 64, 128),
+                 tiles=(32, 64)):
         """Choose the adjoint kernel's launch shape by timing right-hand-side
         VJPs of the state u: the block size (both directions share the launch),
         then the segment length per direction (one at a time, the other held),
-        twice over.  Returns [seg_x, seg_y, block]."""
+        twice over, then the tile form.  Returns [seg_x, seg_y, block] (seg -t:
+        tiles of t interfaces)."""
         import torch
         kb, ub = self.empty(), self.empty()
         kb.normal_()
@@ -128,6 +130,17 @@ class Adjoint:
             for which in (2, 3):
                 best = min((timed_with(self, which, seg, None, timed), seg) for seg in candidates)
                 self.set_launch(which, best[1])
+        # the tile form (one interface per thread, tiles of 32 or 64 interfaces) in both directions
+        walker = [self.get_launch(2)[0], self.get_launch(3)[0]]
+        t_best = timed()
+        for tile in tiles:
+            self.set_launch(2, -tile)
+            self.set_launch(3, -tile)
+            t = timed()
+            if t < t_best:
+                t_best, walker = t, [-tile, -tile]
+        self.set_launch(2, walker[0])
+        self.set_launch(3, walker[1])
         return [self.get_launch(2)[0], self.get_launch(3)[0], self.get_launch(2)[1]]
 
     def _pre(self):

@@ -491,6 +491,134 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
   for (int p = 0; p < 5; p++) flush(p);  // cells I1-2 .. I1+2
 }
 
+// The tile form of the reverse kernel (small grids): a block takes TI interfaces of
+// one grid line and the TI + 5 cells their windows touch.  The cells' states and
+// fluxes go to shared memory once; each thread reverses one interface (its flux
+// adjoint from both neighbouring cells' k_bar, so no interface is reversed twice as
+// at the walker's segment boundaries) and adds its stencil adjoints into per-cell
+// shared accumulators; then each cell is finished (u_bar += a + (df/du)^T f_bar) and
+// added atomically at its folded index, as in the walker.
+template <int D, bool WT, int TI>
+__device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const AdjTerms& kt, double* Ub,
+                                         const double* __restrict__ dxinv, const DevGeom& G, const PhysParams& pp,
+                                         long long tr, int tile, const double* __restrict__ tape) {
+  constexpr int T = 1 - D, NCELL = TI + 5;
+  __shared__ double su[NCELL][NV2], sf[NCELL][NV2], sa[NCELL][NV2], sfb[NCELL][NV2];
+  const long long pbase = (long long)(tr + G.g) * G.stride[T] + (long long)G.g * G.stride[D];
+  const int N = G.dim[D];
+  const long long sd = G.stride[D];
+  const int lo = G.bclo[D], hi = G.bchi[D];
+  const int I0 = tile * TI;
+  const double eps4 = 4.0 * pp.eps;
+  for (int c = threadIdx.x; c < NCELL; c += TI) {
+    const int i = I0 - 3 + c;
+    const double* src = U + (pbase + (long long)fold2(i, N, lo, hi) * sd) * NV2;
+    double uu[NV2], ff[NV2];
+#pragma unroll
+    for (int v = 0; v < NV2; v++) uu[v] = src[v];
+    Prim<MODEL_EULER2D> q = to_prim<MODEL_EULER2D>(uu, pp);
+    cell_flux<MODEL_EULER2D, D>(q, ff);
+#pragma unroll
+    for (int v = 0; v < NV2; v++) {
+      su[c][v] = uu[v];
+      sf[c][v] = ff[v];
+      sa[c][v] = 0.0;
+      sfb[c][v] = 0.0;
+    }
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int I = I0 + t;
+  if (I <= N) {
+    // rhs_c = -dxinv_c (F_{c+1/2} - F_{c-1/2}): interface I feeds cells I-1 (-) and I (+)
+    double Fb[NV2] = {0.0, 0.0, 0.0, 0.0};
+    double kb[NV2];
+    if (I > 0) {
+      terms_at(kt, (pbase + (long long)(I - 1) * sd) * NV2, kb);
+      const double dx = dxinv[G.g + I - 1];
+#pragma unroll
+      for (int v = 0; v < NV2; v++) Fb[v] = -dx * kb[v];
+    }
+    if (I < N) {
+      terms_at(kt, (pbase + (long long)I * sd) * NV2, kb);
+      const double dx = dxinv[G.g + I];
+#pragma unroll
+      for (int v = 0; v < NV2; v++) Fb[v] = fma(dx, kb[v], Fb[v]);
+    }
+    const double* tp = tape ? tape + (tr * (N + 1) + I) * (WT ? TAPE_WIDE : 8) : nullptr;
+    double uL[NV2], uR[NV2];
+    if (tp) {
+#pragma unroll
+      for (int v = 0; v < NV2; v++) {
+        uL[v] = tp[v];
+        uR[v] = tp[4 + v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV2; v++) {
+        double w6[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) w6[p] = su[t + p][v];
+        weno5_pair(w6, w6, eps4, uL[v], uR[v]);
+      }
+    }
+    double uLb[NV2] = {0.0, 0.0, 0.0, 0.0}, uRb[NV2] = {0.0, 0.0, 0.0, 0.0};
+    roe_vjp<D>(uL, uR, Fb, uLb, uRb, pp);
+#pragma unroll
+    for (int v = 0; v < NV2; v++) {
+      double wf6[6], wu6[6], gf[6] = {0, 0, 0, 0, 0, 0}, gu[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+      for (int p = 0; p < 6; p++) {
+        wf6[p] = sf[t + p][v];
+        wu6[p] = su[t + p][v];
+      }
+      if (WT) {
+        weno5_pair_vjp_impl<true>(wf6, wf6, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf, tp + 8 + v * 16);
+        weno5_pair_vjp_impl<true>(wu6, wu6, eps4, uLb[v], uRb[v], gu, gu, tp + 16 + v * 16);
+      } else {
+        weno5_pair_vjp(wf6, wf6, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf);
+        weno5_pair_vjp(wu6, wu6, eps4, uLb[v], uRb[v], gu, gu);
+      }
+#pragma unroll
+      for (int p = 0; p < 6; p++) {
+        atomicAdd(&sfb[t + p][v], gf[p]);
+        atomicAdd(&sa[t + p][v], gu[p]);
+      }
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < NCELL; c += TI) {
+    const int i = I0 - 3 + c;
+    if (i > N + 2) continue;
+    double ab[NV2], fb[NV2], uu[NV2];
+#pragma unroll
+    for (int v = 0; v < NV2; v++) {
+      ab[v] = sa[c][v];
+      fb[v] = sfb[c][v];
+      uu[v] = su[c][v];
+    }
+    flux_vjp<D>(uu, fb, ab, pp);
+    double* dst = Ub + (pbase + (long long)fold2(i, N, lo, hi) * sd) * NV2;
+#pragma unroll
+    for (int v = 0; v < NV2; v++) atomicAdd(dst + v, ab[v]);
+  }
+}
+
+template <bool WT, int TI>
+__global__ void __launch_bounds__(TI)
+rhs_vjp_tile_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
+                    const double* __restrict__ dx1, DevGeom G, PhysParams pp, int nt0, int nt1,
+                    const double* __restrict__ tape0, const double* __restrict__ tape1) {
+  const long long b = blockIdx.x;
+  const long long n0 = (long long)G.dim[1] * nt0;
+  if (b < n0) {
+    vjp_tile<0, WT, TI>(U, kt, Ub, dx0, G, pp, b % G.dim[1], (int)(b / G.dim[1]), tape0);
+  } else {
+    const long long t = b - n0;
+    vjp_tile<1, WT, TI>(U, kt, Ub, dx1, G, pp, t % G.dim[0], (int)(t / G.dim[0]), tape1);
+  }
+}
+
 // Both directions in one launch (they only add into Ub): threads
 // [0, n0) walk x-lines, [n0, n0 + n1) y-lines.
 template <bool WT>
@@ -813,6 +941,26 @@ static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* U
   int n0s = (G.dim[0] + s0 - 1) / s0, n1s = (G.dim[1] + s1 - 1) / s1;
   long long nthr = (long long)G.dim[1] * n0s + (long long)G.dim[0] * n1s;
   const int blk = a->vjp_block;
+  if (s0 < 0) {
+    // tiles of -s0 interfaces (32 or 64) in both directions
+    const int ti = -s0;
+    const int nt0 = (G.dim[0] + 1 + ti - 1) / ti, nt1 = (G.dim[1] + 1 + ti - 1) / ti;
+    const unsigned nblk = (unsigned)((long long)G.dim[1] * nt0 + (long long)G.dim[0] * nt1);
+    const bool wide = tape && a->tape_w == TAPE_WIDE;
+    const double* t0 = tape ? tape[0] : nullptr;
+    const double* t1 = tape ? tape[1] : nullptr;
+    const double* dx0 = a->d_dxinv + a->dx_off[0];
+    const double* dx1 = a->d_dxinv + a->dx_off[1];
+    if (ti == 32) {
+      if (wide) rhs_vjp_tile_kernel<true, 32><<<nblk, 32, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      else rhs_vjp_tile_kernel<false, 32><<<nblk, 32, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+    } else {
+      if (wide) rhs_vjp_tile_kernel<true, 64><<<nblk, 64, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      else rhs_vjp_tile_kernel<false, 64><<<nblk, 64, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+    }
+    AK(cudaGetLastError());
+    return GB_OK;
+  }
   if (tape && a->tape_w == TAPE_WIDE)
     rhs_vjp_kernel<true><<<(unsigned)((nthr + blk - 1) / blk), blk, 0, a->stream>>>(
         U, kt, Ub, a->d_dxinv + a->dx_off[0], a->d_dxinv + a->dx_off[1], G, a->pp, s0, n0s, s1, n1s, tape[0],
@@ -1080,13 +1228,13 @@ extern "C" int gb_adjoint_sync(gb_adjoint* a) {
 extern "C" int gb_adjoint_set_launch(gb_adjoint* a, int which, int seg, int block) {
   if (!a || which < 0 || which > 3) { gbh_set_error("gb_adjoint_set_launch: bad argument"); return GB_ERR_ARG; }
   if (which < 2) {
-    if (seg > 0) a->hl[which].seg = seg;
+    if (seg > 0 || seg == -32 || seg == -64 || seg == -128) a->hl[which].seg = seg;  // -t: tiles of t interfaces
     if (block > 0) {
       if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
       a->hl[which].block = block;
     }
   } else {
-    if (seg > 0) a->vjp_seg[which - 2] = seg;
+    if (seg > 0 || seg == -32 || seg == -64) a->vjp_seg[which - 2] = seg;  // -t: tiles of t interfaces
     if (block > 0) {  // one block size for the adjoint kernel's single launch
       if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
       a->vjp_block = block;

@@ -445,7 +445,7 @@ extern "C" int gb_solver_set_gravity_field(gb_solver* s, const double* fg) {
 
 extern "C" int gb_solver_set_launch(gb_solver* s, int dir, int seg, int block) {
   if (!s || dir < 0 || dir >= s->cfg.ndims) { gbh_set_error("gb_solver_set_launch: bad argument"); return GB_ERR_ARG; }
-  if (seg > 0) s->hl[dir].seg = seg;
+  if (seg > 0 || seg == -32 || seg == -64 || seg == -128) s->hl[dir].seg = seg;  // -t: tiles of t interfaces
   if (block > 0) {
     if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
     s->hl[dir].block = block;
@@ -617,11 +617,17 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
       for (int sg : {1, 2, 3}) segs.push_back(sg);
     std::vector<int> blocks = {128, 64};
     if (small) blocks.push_back(32);
+    // shared-memory tiles of 32 / 64 / 128 interfaces (seg = -tile; not with gravity
+    // or CRWENO5, whose kernels have no tile form)
+    if (!s->gravity && c.hyp_scheme == GB_SCHEME_WENO5)
+      for (int ti : {32, 64, 128}) segs.push_back(-ti);
     double best = 1e30;
     HypLaunch bestL = s->hl[d];
     for (int sg : segs) {
-      if (sg < (small ? 1 : 4) || sg > N) continue;
+      if (sg > 0 && (sg < (small ? 1 : 4) || sg > N)) continue;
+      if (sg < 0 && -sg > 2 * (N + 1)) continue;
       for (int blk : blocks) {
+        if (sg < 0 && blk != blocks[0]) continue;  // a tile's block is the tile
         s->hl[d].seg = sg;
         s->hl[d].block = blk;
         rc = gbh_rk_step(s);  // warm

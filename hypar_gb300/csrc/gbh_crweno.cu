@@ -470,41 +470,6 @@ cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, dou
   }
 }
 
-// The stage epilogue of the fused kernel for one cell (hyp_segment's): h is
-// this direction's dxinv (F_{j+1/2} - F_{j-1/2}).
-template <int NV>
-__device__ __forceinline__ void cr_epilogue(const StageEpi& ep, double* __restrict__ H, long long off,
-                                            const double* h) {
-  const bool finish = ep.last && ep.mode != EPI_HYP;
-  double kv[NV];
-#pragma unroll
-  for (int v = 0; v < NV; v++) {
-    const double hyp = ep.first ? h[v] : H[off + v] + h[v];
-    if (!finish) H[off + v] = hyp;
-    else kv[v] = (ep.par ? ep.par[off + v] : 0.0) - hyp;
-  }
-  if (!finish) return;
-  if (ep.mode == EPI_RHS) {
-#pragma unroll
-    for (int v = 0; v < NV; v++) ep.rhs[off + v] = kv[v];
-    return;
-  }
-#pragma unroll
-  for (int v = 0; v < NV; v++) {
-    const double uv = ep.need_u ? ep.u[off + v] : 0.0;
-    const double av = fma(ep.cb, kv[v], ep.stage == 0 ? uv : ep.acc[off + v]);
-    if (ep.stage == ep.nstages - 1) ep.uout[off + v] = av;
-    else ep.acc[off + v] = av;
-#pragma unroll
-    for (int t = 1; t < 4; t++) {
-      if (t > ep.stage && t < ep.nstages && ep.ca[t] != 0.0) {
-        const double base = ep.touched[t] ? ep.P[t][off + v] : uv;
-        ep.P[t][off + v] = fma(ep.ca[t], kv[v], base);
-      }
-    }
-  }
-}
-
 template <int M, int UPW, int DIR>
 __global__ void __launch_bounds__(128)
 cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
@@ -559,7 +524,7 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
       double h[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) h[v] = dxi * (fI[v] - fIp[v]);
-      cr_epilogue<NV>(ep, H, off, h);
+      stage_epilogue<NV>(ep, H, off, h);
     }
 #pragma unroll
     for (int v = 0; v < NV; v++) fIp[v] = fI[v];

@@ -275,6 +275,149 @@ __device__ __forceinline__ void wpair(const double* w, const double* v, double e
   else weno5_pair(w, v, eps4, oL, oR);
 }
 
+// The upwind flux of one interface from the six-cell window (cells j-3 .. j+2 of
+// interface j-1/2): the fused kernel's WENO5 reconstructions (component-wise or
+// characteristic) and upwinding, with the gravity source function's interface value SI
+// (GRAV, source direction) and the adjoint's tape at interface index tapeoff.
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV, bool WT>
+__device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>::NV],
+                                           const double (&wf)[6][ModelTraits<M>::NV], const double (&wuc)[6],
+                                           const double (&wgf)[6], const double (&wgg)[6],
+                                           const CellAux<M> (&ax)[6], const PhysParams& pp, const StageEpi& ep,
+                                           double eps4, bool src_dir, long long tapeoff, double (&fI)[ModelTraits<M>::NV],
+                                           double (&SI)[ModelTraits<M>::NV]) {
+  constexpr int NV = ModelTraits<M>::NV;
+  constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  Eig Ecc;
+  if (CC) Ecc = roe_eig<M, DIR>(ax[2].rs, ax[3].rs, pp);
+  if (!CHAR) {
+    // Component-wise WENO5: weights of the u-reconstruction from u, values from uC.
+    double fL[NV], fR[NV], uL[NV], uR[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double sf[6], su[6];
+#pragma unroll
+      for (int p = 0; p < 6; p++) {
+        sf[p] = wf[p][v];
+        su[p] = wu[p][v];
+      }
+      if (WT) {
+        double* t = ep.tape + tapeoff * TAPE_WIDE + 8 + v * 16;
+        weno5_pair_tape(sf, sf, eps4, fL[v], fR[v], t);
+        weno5_pair_tape(su, su, eps4, uL[v], uR[v], t + 8);
+        continue;
+      }
+      // the source function phi = g is reconstructed with this flux component's
+      // weights: evaluate them once and apply them to both
+      const bool srcv = src_dir && (v == 1 + DIR || v == NV - 1);
+      double omL[3], omR[3];
+      if (srcv) {
+        weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+        weno5_apply(omL, omR, sf, fL[v], fR[v]);
+      } else {
+        wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
+      }
+      if (M == MODEL_NS3D && v == NV - 1) {
+        double sc[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) sc[p] = wuc[p];
+        wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
+      } else if (GRAV) {
+        double sc[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) sc[p] = su[p] * wgf[p];
+        wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
+      } else {
+        wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
+      }
+      if (srcv) {
+        double sL, sR;
+        weno5_apply(omL, omR, wgg, sL, sR);
+        SI[v] = 0.5 * (sL + sR);
+      }
+    }
+    if (M == MODEL_EULER2D && (WT || ep.tape)) {
+      double* t = ep.tape + tapeoff * (WT ? TAPE_WIDE : 8);
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        t[v] = uL[v];
+        t[4 + v] = uR[v];
+      }
+    }
+    upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI,
+                                     GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
+  } else {
+    // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
+    // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
+    // from the Roe average of the two cell-centre states.
+    double cf[6][NV], cu[6][NV], cuc[6][GRAV ? NV : 3];
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+      projL<M, DIR>(Ecc, pp, wf[p], cf[p]);
+      projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
+      if (GRAV) {
+        // uC = f u + (uC_E - f u_E) e_E: f (L u) plus the energy column of L
+        const double fp = wgf[p], de = fma(-fp, wu[p][NV - 1], wuc[p]);
+        cuc[p][0] = fma(de, Ecc.gh, fp * cu[p][0]);
+        cuc[p][1] = fma(de, Ecc.gh, fp * cu[p][1]);
+        cuc[p][2] = fma(-de, Ecc.gi, fp * cu[p][2]);
+#pragma unroll
+        for (int k = 3; k < NV; k++) cuc[p][k] = fp * cu[p][k];
+      } else if (M == MODEL_NS3D) {
+        // uC differs from u in the energy only: add that column of L.
+        double de = wuc[p] - wu[p][NV - 1];
+        cuc[p][0] = fma(de, Ecc.gh, cu[p][0]);
+        cuc[p][1] = fma(de, Ecc.gh, cu[p][1]);
+        cuc[p][2] = fma(-de, Ecc.gi, cu[p][2]);
+      }
+    }
+    double lcol[NV];  // L (e_{1+DIR} + e_E): the projection of the source function per unit phi
+    if (src_dir) {
+      double ev[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) ev[v] = (v == 1 + DIR || v == NV - 1) ? 1.0 : 0.0;
+      projL<M, DIR>(Ecc, pp, ev, lcol);
+    }
+    double sch[NV];
+    double xfL[NV], xfR[NV], xuL[NV], xuR[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double sf[6], su[6];
+#pragma unroll
+      for (int p = 0; p < 6; p++) {
+        sf[p] = cf[p][v];
+        su[p] = cu[p][v];
+      }
+      double omL[3], omR[3];
+      if (src_dir) {
+        // one evaluation of the flux weights for the flux and the source function
+        weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
+        weno5_apply(omL, omR, sf, xfL[v], xfR[v]);
+      } else {
+        wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
+      }
+      if (M == MODEL_NS3D && (v < 3 || GRAV)) {
+        double sc[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
+        wpair<ALTW>(su, sc, eps4, pp.wtype, xuL[v], xuR[v]);
+      } else {
+        wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
+      }
+      if (src_dir) {
+        double sL, sR, ps[6];
+#pragma unroll
+        for (int p = 0; p < 6; p++) ps[p] = wgg[p] * lcol[v];
+        weno5_apply(omL, omR, ps, sL, sR);
+        sch[v] = 0.5 * (sL + sR);
+      }
+    }
+    if (src_dir) projR<M, DIR>(Ecc, sch, SI);
+    upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
+  }
+
+}
+
 // One thread's share of a launch: interfaces [sg*seg, min((sg+1)*seg, N)] of
 // the grid line with transverse index `tr` (other dimensions ascending, first
 // fastest), and the flux difference / epilogue of the cells in between.
@@ -363,136 +506,9 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
 
   for (int I = I0; I <= I1; I++) {
     load(I + 2);
-    double fL[NV], fR[NV], uL[NV], uR[NV];
-    Eig Ecc;
-    if (CC) Ecc = roe_eig<M, DIR>(ax[2].rs, ax[3].rs, pp);
-
     double fI[NV];
-    if (!CHAR) {
-      // Component-wise WENO5: weights of the u-reconstruction from u, values from uC.
-      double fL[NV], fR[NV], uL[NV], uR[NV];
-#pragma unroll
-      for (int v = 0; v < NV; v++) {
-        double sf[6], su[6];
-#pragma unroll
-        for (int p = 0; p < 6; p++) {
-          sf[p] = wf[p][v];
-          su[p] = wu[p][v];
-        }
-        if (WT) {
-          double* t = ep.tape + (line * (N + 1) + I) * TAPE_WIDE + 8 + v * 16;
-          weno5_pair_tape(sf, sf, eps4, fL[v], fR[v], t);
-          weno5_pair_tape(su, su, eps4, uL[v], uR[v], t + 8);
-          continue;
-        }
-        // the source function phi = g is reconstructed with this flux component's
-        // weights: evaluate them once and apply them to both
-        const bool srcv = src_dir && (v == 1 + DIR || v == NV - 1);
-        double omL[3], omR[3];
-        if (srcv) {
-          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
-          weno5_apply(omL, omR, sf, fL[v], fR[v]);
-        } else {
-          wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
-        }
-        if (M == MODEL_NS3D && v == NV - 1) {
-          double sc[6];
-#pragma unroll
-          for (int p = 0; p < 6; p++) sc[p] = wuc[p];
-          wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
-        } else if (GRAV) {
-          double sc[6];
-#pragma unroll
-          for (int p = 0; p < 6; p++) sc[p] = su[p] * wgf[p];
-          wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
-        } else {
-          wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
-        }
-        if (srcv) {
-          double sL, sR;
-          weno5_apply(omL, omR, wgg, sL, sR);
-          SI[v] = 0.5 * (sL + sR);
-        }
-      }
-      if (M == MODEL_EULER2D && (WT || ep.tape)) {
-        double* t = ep.tape + (line * (N + 1) + I) * (WT ? TAPE_WIDE : 8);
-#pragma unroll
-        for (int v = 0; v < NV; v++) {
-          t[v] = uL[v];
-          t[4 + v] = uR[v];
-        }
-      }
-      upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI,
-                                       GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
-    } else {
-      // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
-      // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
-      // from the Roe average of the two cell-centre states.
-      double cf[6][NV], cu[6][NV], cuc[6][GRAV ? NV : 3];
-#pragma unroll
-      for (int p = 0; p < 6; p++) {
-        projL<M, DIR>(Ecc, pp, wf[p], cf[p]);
-        projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
-        if (GRAV) {
-          // uC = f u + (uC_E - f u_E) e_E: f (L u) plus the energy column of L
-          const double fp = wgf[p], de = fma(-fp, wu[p][NV - 1], wuc[p]);
-          cuc[p][0] = fma(de, Ecc.gh, fp * cu[p][0]);
-          cuc[p][1] = fma(de, Ecc.gh, fp * cu[p][1]);
-          cuc[p][2] = fma(-de, Ecc.gi, fp * cu[p][2]);
-#pragma unroll
-          for (int k = 3; k < NV; k++) cuc[p][k] = fp * cu[p][k];
-        } else if (M == MODEL_NS3D) {
-          // uC differs from u in the energy only: add that column of L.
-          double de = wuc[p] - wu[p][NV - 1];
-          cuc[p][0] = fma(de, Ecc.gh, cu[p][0]);
-          cuc[p][1] = fma(de, Ecc.gh, cu[p][1]);
-          cuc[p][2] = fma(-de, Ecc.gi, cu[p][2]);
-        }
-      }
-      double lcol[NV];  // L (e_{1+DIR} + e_E): the projection of the source function per unit phi
-      if (src_dir) {
-        double ev[NV];
-#pragma unroll
-        for (int v = 0; v < NV; v++) ev[v] = (v == 1 + DIR || v == NV - 1) ? 1.0 : 0.0;
-        projL<M, DIR>(Ecc, pp, ev, lcol);
-      }
-      double sch[NV];
-      double xfL[NV], xfR[NV], xuL[NV], xuR[NV];
-#pragma unroll
-      for (int v = 0; v < NV; v++) {
-        double sf[6], su[6];
-#pragma unroll
-        for (int p = 0; p < 6; p++) {
-          sf[p] = cf[p][v];
-          su[p] = cu[p][v];
-        }
-        double omL[3], omR[3];
-        if (src_dir) {
-          // one evaluation of the flux weights for the flux and the source function
-          weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
-          weno5_apply(omL, omR, sf, xfL[v], xfR[v]);
-        } else {
-          wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
-        }
-        if (M == MODEL_NS3D && (v < 3 || GRAV)) {
-          double sc[6];
-#pragma unroll
-          for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
-          wpair<ALTW>(su, sc, eps4, pp.wtype, xuL[v], xuR[v]);
-        } else {
-          wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
-        }
-        if (src_dir) {
-          double sL, sR, ps[6];
-#pragma unroll
-          for (int p = 0; p < 6; p++) ps[p] = wgg[p] * lcol[v];
-          weno5_apply(omL, omR, ps, sL, sR);
-          sch[v] = 0.5 * (sL + sR);
-        }
-      }
-      if (src_dir) projR<M, DIR>(Ecc, sch, SI);
-      upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
-    }
+    iface_flux<M, CHAR, UPW, DIR, ALTW, GRAV, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, src_dir,
+                                                   line * (N + 1) + I, fI, SI);
 
     if (I > I0) {
       // Flux difference of cell I-1 and the stage epilogue.
@@ -549,6 +565,129 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
       SIp[v] = SI[v];
     }
     shift();
+  }
+}
+
+// The stage epilogue of the fused kernel for one cell (hyp_segment's): h is
+// this direction's dxinv (F_{j+1/2} - F_{j-1/2}).
+template <int NV>
+__device__ __forceinline__ void stage_epilogue(const StageEpi& ep, double* __restrict__ H, long long off,
+                                            const double* h) {
+  const bool finish = ep.last && ep.mode != EPI_HYP;
+  double kv[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double hyp = ep.first ? h[v] : H[off + v] + h[v];
+    if (!finish) H[off + v] = hyp;
+    else kv[v] = (ep.par ? ep.par[off + v] : 0.0) - hyp;
+  }
+  if (!finish) return;
+  if (ep.mode == EPI_RHS) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) ep.rhs[off + v] = kv[v];
+    return;
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double uv = ep.need_u ? ep.u[off + v] : 0.0;
+    const double av = fma(ep.cb, kv[v], ep.stage == 0 ? uv : ep.acc[off + v]);
+    if (ep.stage == ep.nstages - 1) ep.uout[off + v] = av;
+    else ep.acc[off + v] = av;
+#pragma unroll
+    for (int t = 1; t < 4; t++) {
+      if (t > ep.stage && t < ep.nstages && ep.ca[t] != 0.0) {
+        const double base = ep.touched[t] ? ep.P[t][off + v] : uv;
+        ep.P[t][off + v] = fma(ep.ca[t], kv[v], base);
+      }
+    }
+  }
+}
+
+// Small grids: a block takes a tile of TI interfaces of one grid line (TI - 1 cells):
+// its threads compute the data of the tile's TI + 5 cells once into shared memory
+// (flux, modified energy, Roe-average ingredients, wave speeds), then each thread the
+// flux of one interface from its six-cell window there, then each thread the flux
+// difference and stage epilogue of one cell.  The segment walker recomputes a
+// window's cells for every segment and one interface per segment boundary; with the
+// one-to-three-interface segments that small grids need to occupy the GPU that
+// redundancy is most of the work.  No gravity; WT: the adjoint's wide tape.
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
+__global__ void __launch_bounds__(TI)
+hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
+                PhysParams pp, StageEpi ep, long long ntrans) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  constexpr int TC = TI - 1, NCELL = TI + 5;
+  __shared__ double su[NCELL][NV], sf[NCELL][NV], suc[NCELL];
+  __shared__ CellAux<M> sax[NCELL];
+  __shared__ double sfI[TI][NV];
+  const long long line = blockIdx.x % ntrans;
+  const int I0 = (int)(blockIdx.x / ntrans) * TC;
+  long long tr = line, pbase = (long long)G.g * G.stride[DIR];
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    if (e == DIR) continue;
+    const int ie = (int)(tr % G.dim[e]);
+    tr /= G.dim[e];
+    pbase += (long long)(ie + G.g) * G.stride[e];
+  }
+  const int N = G.dim[DIR];
+  const long long sd = G.stride[DIR];
+  const int lo = G.bclo[DIR], hi = G.bchi[DIR];
+  const double eps4 = 4.0 * pp.eps;
+  // cells I0-3 .. I0+TI+1 (those within the line's reach)
+  for (int c = threadIdx.x; c < NCELL; c += TI) {
+    const int i = I0 - 3 + c;
+    if (i > N + 2) continue;
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    double uu[NV], ff[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = U[pt * NV + v];
+    Prim<M> q = to_prim<M>(uu, pp);
+    cell_flux<M, DIR>(q, ff);
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      su[c][v] = uu[v];
+      sf[c][v] = ff[v];
+    }
+    suc[c] = ufunc_energy<M>(q, pp, uu[NV - 1]);
+    CellAux<M> a;
+    if (CC) a.rs = roe_side<M>(q);
+    if (UPW == UPW_RUS) a.c = rusanov_speed<M, DIR>(q, pp);
+    else if (M == MODEL_EULER1D && UPW != UPW_ROE) a.c = sound_speed<M>(q, pp);
+    sax[c] = a;
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int I = I0 + t;
+  if (I <= N) {
+    double wu[6][NV], wf[6][NV], wuc[6], wgf[6], wgg[6];
+    CellAux<M> ax[6];
+#pragma unroll
+    for (int p = 0; p < 6; p++) {
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        wu[p][v] = su[t + p][v];
+        wf[p][v] = sf[t + p][v];
+      }
+      wuc[p] = suc[t + p];
+      ax[p] = sax[t + p];
+    }
+    double fI[NV], SI[NV];
+    iface_flux<M, CHAR, UPW, DIR, ALTW, false, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, false,
+                                                   line * (N + 1) + I, fI, SI);
+#pragma unroll
+    for (int v = 0; v < NV; v++) sfI[t][v] = fI[v];
+  }
+  __syncthreads();
+  const int c = I0 + t;
+  if (t < TC && c < N) {
+    const long long off = (pbase + (long long)c * sd) * NV;
+    const double dxi = dxinv[G.g + c];
+    double h[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) h[v] = dxi * (sfI[t + 1][v] - sfI[t][v]);
+    stage_epilogue<NV>(ep, H, off, h);
   }
 }
 
@@ -641,8 +780,30 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   long long ntrans = 1;
   for (int e = 0; e < G.nd; e++)
     if (e != DIR) ntrans *= G.dim[e];
-  int seg = L.seg > 0 ? L.seg : 32;
   int N = G.dim[DIR];
+  if (L.seg < 0 && !GRAV) {
+    // tiles of -seg interfaces (32, 64 or 128), one block each
+    const int ti = -L.seg;
+    const long long nblk = ntrans * ((N + ti - 2) / (ti - 1));
+    if (ti == 32)
+      hyp_tile_kernel<M, CHAR, UPW, DIR, ALTW, 32, WT><<<(unsigned)nblk, 32, 0, s>>>(U, H, dxinv_dir, G, pp, ep,
+                                                                                   ntrans);
+    else if (ti == 64)
+      hyp_tile_kernel<M, CHAR, UPW, DIR, ALTW, 64, WT><<<(unsigned)nblk, 64, 0, s>>>(U, H, dxinv_dir, G, pp, ep,
+                                                                                   ntrans);
+    else
+      hyp_tile_kernel<M, CHAR, UPW, DIR, ALTW, 128, WT><<<(unsigned)nblk, 128, 0, s>>>(U, H, dxinv_dir, G, pp, ep,
+                                                                                     ntrans);
+    return cudaGetLastError();
+  }
+  // a tile shape asked of a kernel without the tile form (gravity): segments that
+  // spread the line over about four warps per SM
+  int seg = L.seg > 0 ? L.seg : 32;
+  if (L.seg < 0) {
+    const long long want = 152LL * 4 * 32;
+    seg = (int)((ntrans * N + want - 1) / want);
+    seg = seg < 1 ? 1 : (seg > 64 ? 64 : seg);
+  }
   int nseg = (N + seg - 1) / seg;
   long long nthr = ntrans * nseg;
   int block = L.block > 0 ? L.block : 128;

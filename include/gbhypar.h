@@ -169,7 +169,9 @@ int gb_solver_cfl(gb_solver *s, double *cfl);
 int gb_solver_step_report(gb_solver *s, int nsteps, double *cfl, double *norm);
 int gb_solver_error(gb_solver *s, const double *uex, int layout, int mem, double *err);
 /* Launch shape of the fused kernels: interfaces walked per thread (seg) and
- * threads per block, per direction (values <= 0 keep the current ones). */
+ * threads per block, per direction (values <= 0 keep the current ones); seg = -32,
+ * -64 or -128 selects shared-memory tiles of that many interfaces per block (one
+ * interface per thread, for small grids; block is then the tile). */
 int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
 int gb_solver_get_launch(gb_solver *s, int dir, int *seg, int *block);
 /* Choose seg/block per direction by timing candidates on `reps` steps of the

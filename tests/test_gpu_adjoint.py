@@ -247,3 +247,35 @@ def test_autograd_functions(built_lib, problem):
     y = u0.clone().requires_grad_(True)
     (rhs(y, adj) * w).sum().backward()
     assert rel(idot(adj, Jv, w), idot(adj, v, y.grad)) <= DOT_RHS_TOL
+
+
+@pytest.mark.parametrize("tile", [32, 64])
+def test_tile_forms(built_lib, problem, tile):
+    """The tile forms of the forward (gb_adjoint_set_launch seg = -tile for the two
+    directions) and of the reverse kernel (seg = -tile for both directions): the RHS
+    dot-product test, and the checkpointed gradient against the walker forms'."""
+    case, _, _ = problem
+    adj = make(problem)
+    u = state(adj, case.u, seed=21, scale=0.02)
+    v, w = rand_interior(adj, 121), rand_interior(adj, 221)
+    k, Jv, JTw = adj.empty(), adj.empty(), adj.empty()
+    adj.set_launch(2, -tile)
+    adj.set_launch(3, -tile)
+    assert adj.get_launch(2)[0] == -tile
+    adj.rhs_jvp(u, v, k, Jv)
+    adj.rhs_vjp(u, w, JTw)
+    assert rel(idot(adj, Jv, w), idot(adj, v, JTw)) <= DOT_RHS_TOL
+    grads = []
+    for shapes in ((None, None), (-tile, -tile)):
+        a = make(problem, ncheck=0)
+        if shapes[0]:
+            for which in range(4):
+                a.set_launch(which, shapes[0])
+        u0 = state(a, case.u)
+        wt = rand_interior(a, 9)
+        uT, g = a.empty(), a.empty()
+        a.forward(u0, uT)
+        a.backward(wt, g)
+        grads.append(a.interior(g).cpu().numpy())
+        a.close()
+    assert np.linalg.norm(grads[1] - grads[0]) / np.linalg.norm(grads[0]) <= 1e-11

@@ -235,3 +235,30 @@ def test_nonfinite_state_is_reported(built_lib, tmp_path):
     s = solver_for(case, tmp_path)
     s.step(1)
     assert not s.check_finite()
+
+
+@pytest.mark.parametrize("tile", [32, 64, 128])
+@pytest.mark.parametrize("model,interp,upw", [("euler1d", "components", "roe"), ("euler1d", "characteristic", "rf-char"),
+                                              ("euler2d", "characteristic", "roe"),
+                                              ("euler2d", "components", "llf-char"),
+                                              ("navierstokes3d", "components", "roe"),
+                                              ("navierstokes3d", "characteristic", "rusanov")])
+def test_tile_kernel_matches_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw, tile):
+    """The shared-memory tile form of the direction kernels (gb_solver_set_launch seg = -tile):
+    per RHS and after steps, against the oracle."""
+    case = make(model, interp, upw, n_iter=3)
+    s = solver_for(case, tmp_path)
+    for d in range(case.ndims):
+        s.set_launch(d, -tile, 0)
+        assert s.get_launch(d)[0] == -tile
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    out = torch.zeros_like(u)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
+    assert relerr(got, O.interior(P.rhs(u0.copy()), case.size, case.nvars, 3)) <= RHS_TOL
+    s.set_state(O.interior(u0, case.size, case.nvars, 3).reshape(-1))
+    s.step(3)
+    ref = O.interior(P.rk(P.u0(), 3), case.size, case.nvars, 3).reshape(-1)
+    assert relerr(s.get_state(), ref) <= STEP_TOL
