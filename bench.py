@@ -42,9 +42,14 @@ UNIT = "cell-component updates/s"
 # per cell per step this is x (ndims * nstages).  FP64 instructions likewise.
 FP64_FLOPS_PER_INTERFACE = {"vortex": 1607.3}
 FP64_INSTR_PER_INTERFACE = {"vortex": 1005.6}
-# DRAM bytes (read + write) per cell of one launch, same capture (2048^2, traffic
-# proportional to cells at these sizes): x launch / y launch with the RK update.
-DRAM_BYTES_PER_CELL = {"vortex": {"hyp_x": 56.13, "hyp_y": 149.99}}
+# DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
+# update), per kernel form: the segment walker from the same 2048^2 capture (traffic
+# proportional to cells at these sizes), the tile form from a capture of the default
+# 1024^2 run (profiles/hyp_tile_kernel_euler2d_char_roe_vortex1024_ncu_full.md).
+DRAM_BYTES_PER_CELL = {"vortex": {("hyp_x", "walker"): 56.13, ("hyp_y", "walker"): 149.99,
+                                  ("hyp_y", "tile"): 112.57}}
+TRAFFIC_SOURCE = {"walker": "a 2048^2 capture of the segment-walker form, scaled by cells",
+                  "tile": "a 1024^2 capture of the tile form"}
 
 
 # The reference's published GPU numbers for the same decks (cell-component updates/s):
@@ -295,11 +300,14 @@ def run_ours(args, case, desc, ws, rank, local):
     else:
         bytes_per_launch = cells * 8.0 * nv * 2  # read U, write the partial hyperbolic term
     achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
-    traffic = DRAM_BYTES_PER_CELL.get(args.workload, {}).get(cls)
+    cls_dir = "xyz".index(cls[-1]) if cls.startswith("hyp_") else 0
+    form = "tile" if tuned and tuned[cls_dir][0] < 0 else "walker"
+    traffic = DRAM_BYTES_PER_CELL.get(args.workload, {}).get((cls, form))
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic * cells if traffic else None,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of a 2048^2 "
-                                  "capture, scaled by cells" if traffic else None, "kernel": cls,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of "
+                                   + TRAFFIC_SOURCE[form]) if traffic else None, "kernel": cls,
+                "kernel_form": form,
                 "avg_launch_ms": avg_launch_s * 1e3, "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": bytes_per_launch}
     step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
