@@ -55,8 +55,10 @@ class Case:
     # per-face boundary types: {(dim, face): (bctype, [values after the extents])};
     # faces not listed take `bc`
     bcs: Optional[dict] = None
-    # NavierStokes3D gravity (physics.inp gravity / rho_ref / p_ref / R / HB / N_bv)
+    # gravity: NavierStokes3D (physics.inp gravity gx gy gz / rho_ref / p_ref / R / HB /
+    # N_bv) or Euler1D (gravity g, gravity_type grav_type)
     gravity: Optional[Sequence[float]] = None
+    grav_type: int = 0
     rho_ref: float = 1.0
     p_ref: float = 1.0
     R_gas: float = 1.0
@@ -104,6 +106,8 @@ class Case:
 
     def physics_inp(self) -> str:
         lines = ["begin", f"  gamma      {float(self.gamma)!r}", f"  upwinding  {self.upwinding}"]
+        if self.model == "euler1d" and self.gravity is not None:
+            lines += [f"  gravity    {float(self.gravity[0])!r}", f"  gravity_type {int(self.grav_type)}"]
         if self.model == "navierstokes3d":
             lines += [f"  Pr         {float(self.Pr)!r}", f"  Minf       {float(self.Minf)!r}"]
             if self.Re is not None:
@@ -238,6 +242,32 @@ def tgv(n: int = 256, n_iter: int = 100, dt: float = 2e-3, mach: float = 0.1, Re
     u = np.stack([rho, rho * uu, rho * vv, rho * ww, e], axis=-1).reshape(n ** 3, 5)
     return Case("navierstokes3d", [n, n, n], [x, x.copy(), x.copy()], u, dt, n_iter, scheme,
                 interp, upwinding, gamma=gamma, Re=Re, Pr=Pr, Minf=mach)
+
+
+def stratified_1d(n: int = 64, n_iter: int = 10, dt: float = 2e-3, g: float = 1.0, grav_type: int = 0,
+                  interp: str = "components", upwinding: str = "roe", scheme: str = "44", perturb: float = 0.01,
+                  seed: int = 3) -> Case:
+    """A 1-D atmosphere in the gravity field of physics.inp (Xing & Shu, J. Sci. Comput. 54,
+    2013): isothermal hydrostatic rho = p = S with S = exp(-g x) (gravity_type 0, x_i =
+    i/(n-1), mirror ends) or S = exp(sin(2 pi x)/(2 pi)) (gravity_type 1, x_i = i/n,
+    periodic), at rest, with the pressure perturbed pointwise by 1 + perturb N(0,1)
+    (seeded, clipped at 3 sigma; perturb = 0: the balanced state)."""
+    gamma = 1.4
+    if grav_type == 0:
+        x = np.arange(n, dtype=np.float64) / float(n - 1)
+        S = np.exp(-g * x)
+        bc = "extrapolate"
+    else:
+        x = np.arange(n, dtype=np.float64) / float(n)
+        S = np.exp(np.sin(2.0 * math.pi * x) / (2.0 * math.pi))
+        bc = "periodic"
+    rho, P = S.copy(), S.copy()
+    if perturb > 0.0:
+        rng = np.random.default_rng(seed)
+        P = P * (1.0 + perturb * np.clip(rng.standard_normal(n), -3, 3))
+    u = np.stack([rho, np.zeros(n), P / (gamma - 1.0)], axis=-1)
+    return Case("euler1d", [n], [x], u, dt, n_iter, scheme, interp, upwinding, gamma=gamma, bc=bc,
+                gravity=(g, 0.0, 0.0), grav_type=grav_type)
 
 
 def rising_thermal_bubble(n: int = 64, n_iter: int = 100, dt: float = 0.01, interp: str = "components",

@@ -81,6 +81,8 @@ def _bind(path):
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double]
     L.orc_set_gravity.restype = ctypes.c_int
+    L.orc_set_gravity_1d.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_int]
+    L.orc_set_gravity_1d.restype = ctypes.c_int
     L.orc_get_gravity.argtypes = [ctypes.c_void_p, dp]
     L.orc_get_gravity.restype = None
     L.orc_cfl.argtypes = [ctypes.c_void_p, dp, ctypes.c_double]
@@ -270,9 +272,13 @@ class Problem:
         grav = getattr(case, "gravity", None)
         if grav is not None and any(float(v) != 0.0 for v in grav):
             xg = np.concatenate([grid_with_ghosts(x, ghosts) for x in xs])
-            if L.orc_set_gravity(self.h, _dp(xg), float(grav[0]), float(grav[1]), float(grav[2]),
-                                 case.rho_ref, case.p_ref, case.R_gas, int(case.HB), case.N_bv):
-                raise RuntimeError("orc_set_gravity failed")
+            if case.model == "euler1d":
+                rc = L.orc_set_gravity_1d(self.h, _dp(xg), float(grav[0]), int(case.grav_type))
+            else:
+                rc = L.orc_set_gravity(self.h, _dp(xg), float(grav[0]), float(grav[1]), float(grav[2]),
+                                       case.rho_ref, case.p_ref, case.R_gas, int(case.HB), case.N_bv)
+            if rc:
+                raise RuntimeError("setting the gravity field failed")
 
     def gravity_field(self) -> Optional[np.ndarray]:
         """The fields f then g with ghost points, as the reader computes them, or None."""

@@ -158,6 +158,44 @@ int orc_set_gravity(orc_problem *p, const double *xg, double gx, double gy, doub
   return 0;
 }
 
+/* Euler1DGravityField (Euler1DGravityField.c:23-95): S = exp(-g x) (type 0) or
+ * exp(-phi), phi = -sin(2 pi x)/(2 pi) (type 1), at every point with ghosts from the
+ * ghost-extrapolated grid; for type 0 the ghost layers copied from their mirror
+ * interior points.  Stored as gg = S and gf = 1.0 / S (the modified solution and the
+ * source scale by the latter, Euler1DModifiedSolution.c:48, Euler1DSource.c:71). */
+int orc_set_gravity_1d(orc_problem *p, const double *xg, double g, int type) {
+  if (p->model != ORC_EULER1D) return 1;
+  long np = orc_npoints_wghosts(p);
+  int gh = p->ghosts, N = p->dim[0];
+  free(p->gf);
+  free(p->gg);
+  p->gf = (double *)malloc(sizeof(double) * np);
+  p->gg = (double *)malloc(sizeof(double) * np);
+  for (long i = 0; i < np; i++) {
+    double x = xg[i];
+    if (type == 0) {
+      p->gg[i] = exp(-g * x);
+    } else if (type == 1) {
+      double pi = 4.0 * atan(1.0);
+      double phi = -sin(2 * pi * x) / (2 * pi);
+      p->gg[i] = exp(-phi);
+    } else {
+      return 1;
+    }
+  }
+  if (type != 1)
+    for (int b = 0; b < gh; b++) {
+      p->gg[b] = p->gg[gh + (gh - 1 - b)];
+      p->gg[N + gh + b] = p->gg[gh + (N - 1 - b)];
+    }
+  for (long i = 0; i < np; i++) p->gf[i] = 1.0 / p->gg[i];
+  p->grav[0] = g;
+  p->grav[1] = p->grav[2] = 0.0;
+  p->RT = 1.0;
+  p->has_grav = g != 0.0;
+  return 0;
+}
+
 /* f then g (each with ghost points); zeros when no field is set */
 void orc_get_gravity(const orc_problem *p, double *out) {
   long np = orc_npoints_wghosts(p);
@@ -680,7 +718,9 @@ static void m_ufunc(const orc_problem *p, double *uC, const double *u, long q) {
     uC[3] = u[3] * f;
     uC[4] = (P * inv_gamma_m1) * (1.0 / g) + (0.5 * rho * (uvel * uvel + vvel * vvel + wvel * wvel)) * f;
   } else if (p->model == ORC_EULER1D) {
-    for (int v = 0; v < nv; v++) uC[v] = u[v] * (1.0 / 1.0);
+    /* Euler1DModifiedSolution.c:48: uC = u / S (gf holds 1.0 / S) */
+    const double a = p->gf ? p->gf[q] : (1.0 / 1.0);
+    for (int v = 0; v < nv; v++) uC[v] = a * u[v];
   } else {
     for (int v = 0; v < nv; v++) uC[v] = u[v];
   }
@@ -891,7 +931,8 @@ static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, 
     m_left(p, L, uavg, dir);
     m_right(p, R, uavg, dir);
     if (p->model == ORC_EULER1D) {
-      double kappa = max2(1.0, 1.0);
+      /* Euler1DUpwind.c:79-82: the dissipation scaled by max(S_L, S_R) of the gravity field */
+      double kappa = p->gg ? max2(p->gg[qL], p->gg[qR]) : max2(1.0, 1.0);
       for (int k = 0; k < nv; k++) D[k] = kappa * absolute(D[k]);
     } else {
       double delta = 0.000001, delta2 = delta * delta;
@@ -926,7 +967,8 @@ static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, 
         if ((eigL[k] < 0) && (eigC[k] < 0) && (eigR[k] < 0)) { fc[k] = fcR[k]; continue; }
       }
       double alpha = max3(absolute(eigL[k]), absolute(eigC[k]), absolute(eigR[k]));
-      if (p->model == ORC_EULER1D && p->upwind == ORC_UPW_LLF) alpha = 1.0 * alpha;
+      if (p->model == ORC_EULER1D && p->upwind == ORC_UPW_LLF) /* Euler1DUpwind.c:249, :268 */
+        alpha = (p->gg ? max2(p->gg[qL], p->gg[qR]) : 1.0) * alpha;
       fc[k] = 0.5 * (fcL[k] + fcR[k] + alpha * (ucL[k] - ucR[k]));
     }
     matvec(nv, fI, R, fc);
@@ -1243,7 +1285,7 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
               weno_w(p->weights, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v], p->eps, &w1, &w2, &w3);
               fL[v] = weno_interp(w1, w2, w3, fC[nv * L3 + v], fC[nv * L2 + v], fC[nv * L1 + v], fC[nv * L4 + v], fC[nv * L5 + v]);
               double sL = 0.0, sR = 0.0;
-              int sv = dosrc && (v == 1 + d || v == 4);
+              int sv = dosrc && (v == 1 + d || v == nv - 1);
               if (dosrc)
                 sL = sv ? weno_interp(w1, w2, w3, p->gg[L3], p->gg[L2], p->gg[L1], p->gg[L4], p->gg[L5])
                         : weno_interp(w1, w2, w3, 0.0, 0.0, 0.0, 0.0, 0.0);
@@ -1281,8 +1323,8 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
             if (dosrc) {
               for (int k = 0; k < 5; k++) {
                 double phl[MAXV] = {0.0}, phr[MAXV] = {0.0};
-                phl[1 + d] = phl[4] = p->gg[sl[k]];
-                phr[1 + d] = phr[4] = p->gg[sr[k]];
+                phl[1 + d] = phl[nv - 1] = p->gg[sl[k]];
+                phr[1 + d] = phr[nv - 1] = p->gg[sr[k]];
                 matvec(nv, isl[k], L, phl);
                 matvec(nv, isr[k], L, phr);
               }
@@ -1322,12 +1364,24 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
         if (dosrc) {
           for (int i = 0; i < N; i++) {
             long q = base + (long)i * sd;
-            double rho, vel[3], E, P;
-            NS_FLOWVAR((u + nv * q), rho, vel[0], vel[1], vel[2], E, P, p->gamma);
-            (void)E;
-            (void)P;
-            double term[5] = {0.0, rho * p->RT * (d == 0), rho * p->RT * (d == 1), rho * p->RT * (d == 2),
-                              rho * p->RT * vel[d]};
+            double term[5];
+            if (p->model == ORC_EULER1D) {
+              /* Euler1DSource.c:67-72: [0, rho, rho v] (the field's 1/S applied below) */
+              double rho = u[nv * q], vel = u[nv * q + 1] / rho;
+              term[0] = 0.0;
+              term[1] = rho;
+              term[2] = rho * vel;
+            } else {
+              double rho, vel[3], E, P;
+              NS_FLOWVAR((u + nv * q), rho, vel[0], vel[1], vel[2], E, P, p->gamma);
+              (void)E;
+              (void)P;
+              term[0] = 0.0;
+              term[1] = rho * p->RT * (d == 0);
+              term[2] = rho * p->RT * (d == 1);
+              term[3] = rho * p->RT * (d == 2);
+              term[4] = rho * p->RT * vel[d];
+            }
             for (int v = 0; v < nv; v++)
               src[nv * q + v] += ((term[v] * p->gf[q]) * (SI[(long)(i + 1) * nv + v] - SI[(long)i * nv + v]) *
                                   dxinv[g + i]);

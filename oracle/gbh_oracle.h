@@ -68,6 +68,9 @@ void orc_set_scheme(orc_problem *p, int scheme);
 int orc_set_gravity(orc_problem *p, const double *xg, double gx, double gy, double gz, double rho0, double p0,
                     double R, int HB, double Nbv);
 void orc_get_gravity(const orc_problem *p, double *out);
+/* Euler1D gravity (physics.inp gravity, gravity_type 0 or 1) from the grid with ghost
+ * coordinates (Euler1DGravityField.c): gg = S, gf = 1/S. */
+int orc_set_gravity_1d(orc_problem *p, const double *xg, double g, int type);
 /* The values boundary.inp gives for zone z after its extents (8 doubles). */
 void orc_set_zone_data(orc_problem *p, int z, const double *data);
 

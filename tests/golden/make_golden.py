@@ -118,7 +118,20 @@ CASES = {
     "vortex24_crweno_char_roe_subsonic_io": lambda: _b(_cr(C.vortex(24, n_iter=4, dt=0.02)),
                                                        {(0, 1): ("subsonic-inflow", [1.0, 0.5, 0.0]),
                                                         (0, -1): ("subsonic-outflow", [1.0 / 1.4])}),
+    "strat64_grav0_roe_comp": lambda: C.stratified_1d(64, n_iter=10),
+    "strat64_grav0_llf_char_yc_ssprk3": lambda: _w(C.stratified_1d(64, n_iter=10, interp="characteristic",
+                                                                    upwinding="llf-char", scheme="ssprk3"), "yc"),
+    "strat64_grav1_roe_char": lambda: C.stratified_1d(64, n_iter=10, grav_type=1, interp="characteristic"),
+    "strat64_grav1_llf_comp_mapped": lambda: _w(C.stratified_1d(64, n_iter=10, grav_type=1, upwinding="llf-char",
+                                                                 g=2.0), "mapped"),
+    "sod64_grav_roe_comp": lambda: _g1(C.sod(64, n_iter=20, dt=1e-3), 1.0),
 }
+
+
+def _g1(case, g):
+    """An Euler1D deck in the gravity field exp(-g x) (gravity_type 0)."""
+    case.gravity, case.grav_type = (g, 0.0, 0.0), 0
+    return case
 
 
 def _visc(case, Re):
