@@ -28,6 +28,8 @@ cudaError_t launch_hyp_crweno(int, int, int, bool, const double*, double*, const
                               const PhysParams&, const StageEpi&, const HypLaunch&, double*, double*, double*,
                               cudaStream_t);
 size_t crweno_scratch_doubles(int, int, long long, bool, bool);
+cudaError_t launch_hyp_euler1d_grav(int, int, int, const double*, double*, const double*, const DevGeom&,
+                                   const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_grav(int, int, const double*, double*, const double*, const DevGeom&,
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_unfused_euler1d(int, int, int, double*, const double*, const double*, const double*,
@@ -115,6 +117,9 @@ static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const Stag
                              s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->d_crF, s->stream);
   if (s->gravity) {
     if (!s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
+    if (c.model == GB_MODEL_EULER1D)
+      return launch_hyp_euler1d_grav(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir],
+                                     s->stream);
     return launch_hyp_ns3d_grav(dir, c.interp, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir], s->stream);
   }
   if (s->pp.wtype != WENO_W_JS) {
@@ -210,13 +215,21 @@ int gbh_validate(const gb_config* c) {
   if (c->weno_weights < GB_WENO_JS || c->weno_weights > GB_WENO_NONE) { gbh_set_error("bad weno_weights"); return GB_ERR_ARG; }
   if (c->hyp_scheme != GB_SCHEME_WENO5 && c->hyp_scheme != GB_SCHEME_CRWENO5) { gbh_set_error("bad hyp_scheme"); return GB_ERR_ARG; }
   if (c->gravity[0] != 0.0 || c->gravity[1] != 0.0 || c->gravity[2] != 0.0) {
-    if (c->model != GB_MODEL_NS3D) { gbh_set_error("gravity: NavierStokes3D only on this path"); return GB_ERR_UNSUPPORTED; }
+    if (c->model == GB_MODEL_EULER2D) { gbh_set_error("gravity: Euler2D has none"); return GB_ERR_UNSUPPORTED; }
     if (c->hyp_scheme == GB_SCHEME_CRWENO5) { gbh_set_error("gravity with CRWENO5 is not available on this path"); return GB_ERR_UNSUPPORTED; }
-    if (c->upwind != GB_UPWIND_RUSANOV) {
-      gbh_set_error("flows with gravity need rusanov upwinding (NavierStokes3DInitialize.c:371)");
-      return GB_ERR_ARG;
+    if (c->model == GB_MODEL_EULER1D) {
+      if (c->upwind != GB_UPWIND_ROE && c->upwind != GB_UPWIND_LLF) {
+        gbh_set_error("flows with gravity need roe or llf-char upwinding (Euler1DInitialize.c:144)");
+        return GB_ERR_ARG;
+      }
+      if (c->grav_type != 0 && c->grav_type != 1) { gbh_set_error("gravity_type must be 0 or 1"); return GB_ERR_ARG; }
+    } else {
+      if (c->upwind != GB_UPWIND_RUSANOV) {
+        gbh_set_error("flows with gravity need rusanov upwinding (NavierStokes3DInitialize.c:371)");
+        return GB_ERR_ARG;
+      }
+      if (!(c->rho_ref > 0.0) || !(c->p_ref > 0.0)) { gbh_set_error("gravity needs positive rho_ref and p_ref"); return GB_ERR_ARG; }
     }
-    if (!(c->rho_ref > 0.0) || !(c->p_ref > 0.0)) { gbh_set_error("gravity needs positive rho_ref and p_ref"); return GB_ERR_ARG; }
   }
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
@@ -300,8 +313,9 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   s->pp.wtype = c.weno_weights;
   s->pp.gf = s->pp.gg = nullptr;
   for (int d = 0; d < 3; d++) s->pp.grav[d] = c.gravity[d];
-  s->pp.RT = c.rho_ref > 0 ? c.p_ref / c.rho_ref : 1.0;
-  s->gravity = c.model == GB_MODEL_NS3D && (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0);
+  // NavierStokes3D: RT = p0 / rho0; Euler1D's source has no such factor (RT = 1)
+  s->pp.RT = (c.model == GB_MODEL_NS3D && c.rho_ref > 0) ? c.p_ref / c.rho_ref : 1.0;
+  s->gravity = c.model != GB_MODEL_EULER2D && (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0);
   s->viscous = (c.model == GB_MODEL_NS3D) && (c.Re > 0);
   double Re_eff = c.Re / c.Minf;  // NavierStokes3DInitialize.c:368
   s->vp.gamma = c.gamma;
@@ -327,7 +341,7 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   A(&s->d_u, bytes);
   A(&s->d_acc, bytes);
   for (int k = 1; k < c.rk_nstages; k++) A(&s->d_P[k], bytes);
-  if (c.ndims > 1) A(&s->d_H, bytes);
+  if (c.ndims > 1 || s->gravity) A(&s->d_H, bytes);  // gravity: gb_SourceFunction's second pass
   if (c.hyp_scheme == GB_SCHEME_CRWENO5) {
     // the largest direction's interface values and elimination scratch
     const bool chr = c.interp == GB_INTERP_CHARACTERISTIC;

@@ -110,6 +110,8 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
       if (M != MODEL_EULER1D) {
         const double delta = 0.000001, delta2 = delta * delta;
         d = (d < delta) ? (lam[k] * lam[k] + delta2) * (0.5 / delta) : d;
+      } else {
+        d = kappa * d;  // Euler1DUpwind.c:79-82 (gravity field; 1 without)
       }
       w[k] *= d;
     }
@@ -152,6 +154,7 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
 #pragma unroll
       for (int k = 0; k < NV; k++) {
         double al = fmax(fmax(fabs(lamL[k]), fabs(lamC[k])), fabs(lamR[k]));
+        if (M == MODEL_EULER1D) al = kappa * al;  // Euler1DUpwind.c:268
         fc[k] = 0.5 * fma(al, wd[k], ws[k]);
       }
     } else {
@@ -211,6 +214,8 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
         if (M != MODEL_EULER1D) {
           const double delta = 0.000001, delta2 = delta * delta;
           d = (d < delta) ? (lamC[k] * lamC[k] + delta2) * (0.5 / delta) : d;
+        } else {
+          d = kappa * d;
         }
         fc[k] = 0.5 * fma(-d, xuR[k] - xuL[k], xfL[k] + xfR[k]);
       }
@@ -221,6 +226,7 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
 #pragma unroll
       for (int k = 0; k < NV; k++) {
         double al = fmax(fmax(fabs(lamL[k]), fabs(lamC[k])), fabs(lamR[k]));
+        if (M == MODEL_EULER1D) al = kappa * al;
         double llf = 0.5 * fma(al, xuL[k] - xuR[k], xfL[k] + xfR[k]);
         if (UPW == UPW_RF) {
           if (lamL[k] > 0 && lamC[k] > 0 && lamR[k] > 0) llf = xfL[k];
@@ -396,7 +402,7 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
       } else {
         wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
       }
-      if (M == MODEL_NS3D && (v < 3 || GRAV)) {
+      if ((M == MODEL_NS3D && v < 3) || GRAV) {
         double sc[6];
 #pragma unroll
         for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
@@ -469,8 +475,12 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
     if (GRAV) {
       wgf[5] = pp.gf[pt];
       wgg[5] = pp.gg[pt];
-      double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
-      wuc[5] = fma(q.P * pp.inv_gm1, nr_rcp(wgg[5]), (0.5 * q.rho * vsq) * wgf[5]);
+      if (M == MODEL_EULER1D) {
+        wuc[5] = wu[5][NV - 1] * wgf[5];  // u* = u / S (gf holds 1 / S)
+      } else {
+        double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
+        wuc[5] = fma(q.P * pp.inv_gm1, nr_rcp(wgg[5]), (0.5 * q.rho * vsq) * wgf[5]);
+      }
     } else {
       wuc[5] = ufunc_energy<M>(q, pp, wu[5][NV - 1]);
     }
@@ -827,6 +837,24 @@ cudaError_t launch_dir_any(int dir, const double* U, double* H, const double* dx
 
 // NavierStokes3D with gravity (Rusanov upwinding, as the reference requires):
 // ALTW selects the weight formulation as in launch_hyp_model.
+// Euler1D with gravity (Xing & Shu's well-balanced form): Roe or LLF, u* = u / S,
+// the dissipation scaled by max(S_L, S_R), the source [0, rho, rho v] / S times the
+// difference of the interface values of [0, S, S] (pp: gf = 1/S, gg = S, RT = 1).
+template <bool ALTW>
+cudaError_t launch_hyp_euler1d_gravity(int dir, int chr, int upw, const double* U, double* H,
+                                       const double* dxinv_dir, const DevGeom& G, const PhysParams& pp,
+                                       const StageEpi& ep, const HypLaunch& L, cudaStream_t s) {
+  if (dir != 0) return cudaErrorInvalidValue;
+  if (chr) {
+    if (upw == UPW_LLF)
+      return launch_dir<MODEL_EULER1D, true, UPW_LLF, 0, ALTW, true>(U, H, dxinv_dir, G, pp, ep, L, s);
+    return launch_dir<MODEL_EULER1D, true, UPW_ROE, 0, ALTW, true>(U, H, dxinv_dir, G, pp, ep, L, s);
+  }
+  if (upw == UPW_LLF)
+    return launch_dir<MODEL_EULER1D, false, UPW_LLF, 0, ALTW, true>(U, H, dxinv_dir, G, pp, ep, L, s);
+  return launch_dir<MODEL_EULER1D, false, UPW_ROE, 0, ALTW, true>(U, H, dxinv_dir, G, pp, ep, L, s);
+}
+
 template <bool ALTW>
 cudaError_t launch_hyp_ns3d_gravity(int dir, int chr, const double* U, double* H, const double* dxinv_dir,
                                     const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
@@ -883,6 +911,12 @@ __global__ void ufunc_kernel(double* __restrict__ uC, const double* __restrict__
 #pragma unroll
   for (int v = 0; v < NV; v++) uu[v] = u[p * NV + v];
   Prim<M> q = to_prim<M>(uu, pp);
+  if (M == MODEL_EULER1D && pp.gf) {
+    // Euler1DModifiedSolution.c:48: u* = u / S (gf holds 1 / S)
+  #pragma unroll
+    for (int v = 0; v < NV; v++) uC[p * NV + v] = uu[v] * pp.gf[p];
+    return;
+  }
   if (M == MODEL_NS3D && pp.gf) {
     // NavierStokes3DModifiedSolution.c:55-66: u* scaled by the hydrostatic fields
     const double f = pp.gf[p], g = pp.gg[p];
@@ -936,7 +970,7 @@ __global__ void upwind_kernel(double* __restrict__ fI, const double* __restrict_
   cr.c = UPW == UPW_RUS ? rusanov_speed<M, DIR>(qr, pp) : sound_speed<M>(qr, pp);
   Eig Ecc = roe_eig<M, DIR>(cl.rs, cr.rs, pp);
   // NavierStokes3DUpwind.c: Rusanov's dissipation scaled by max(g_L, g_R) of the gravity field
-  const double kappa = (UPW == UPW_RUS && pp.gg) ? fmax(pp.gg[pL], pp.gg[pR]) : 1.0;
+  const double kappa = ((UPW == UPW_RUS || M == MODEL_EULER1D) && pp.gg) ? fmax(pp.gg[pL], pp.gg[pR]) : 1.0;
   upwind_iface<M, true, UPW, DIR>(a, b, c, d, Ecc, cl, cr, pp, out, kappa);
 #pragma unroll
   for (int v = 0; v < NV; v++) fI[p * NV + v] = out[v];

@@ -280,6 +280,37 @@ static int gravity_fields(const gb_config *c, gb_inputs *res) {
   return GB_OK;
 }
 
+/* Euler1DGravityField (Euler1DGravityField.c:23-95): S = exp(-g x) (gravity_type 0) or
+ * exp(-phi), phi = -sin(2 pi x)/(2 pi) (type 1), from the grid with ghost coordinates;
+ * for type 0 the ghost layers copied from their mirror interior points.  Stored as
+ * 1.0/S then S (the modified solution and the source scale by the first, the
+ * dissipation by the second). */
+static int gravity_field_1d(const gb_config *c, gb_inputs *res) {
+  const int g = c->ghosts, N = c->dim[0];
+  const long n = N + 2 * g;
+  double *X = (double *)malloc(sizeof(double) * n);
+  grid_ghosts(res->x, N, g, X);
+  res->grav = (double *)malloc(sizeof(double) * 2 * n);
+  double *f = res->grav, *S = res->grav + n;
+  for (long i = 0; i < n; i++) {
+    if (c->grav_type == 0) {
+      S[i] = exp(-c->gravity[0] * X[i]);
+    } else {
+      double pi = 4.0 * atan(1.0);
+      double phi = -sin(2 * pi * X[i]) / (2 * pi);
+      S[i] = exp(-phi);
+    }
+  }
+  if (c->grav_type != 1)
+    for (int b = 0; b < g; b++) {
+      S[b] = S[g + (g - 1 - b)];
+      S[N + g + b] = S[g + (N - 1 - b)];
+    }
+  for (long i = 0; i < n; i++) f[i] = 1.0 / S[i];
+  free(X);
+  return GB_OK;
+}
+
 /* A solution file in HyPar's input format (ReadArray.c): binary = x then u
  * (point-major); ascii = x then u variable by variable.  Returns -1 (no error
  * message) when the file is absent and `required` is 0. */
@@ -516,17 +547,20 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   c.rho_ref = 1.0;
   c.p_ref = 1.0;
   c.R_gas = 1.0;
-  /* NavierStokes3DInitialize.c:141-260; Euler1D's scalar "gravity" is outside this path */
+  /* NavierStokes3DInitialize.c:141-260 (gravity gx gy gz, ...); Euler1DInitialize.c:98-130
+     (gravity g, gravity_type) */
   kv_t pk[] = {{"gamma", 'd', &c.gamma}, {"upwinding", 's', upw}, {"gravity", c.model == GB_MODEL_NS3D ? 'v' : 'd', grav},
                {"Pr", 'd', &c.Pr}, {"Re", 'd', &c.Re}, {"Minf", 'd', &c.Minf},
-               {"rho_ref", 'd', &c.rho_ref}, {"p_ref", 'd', &c.p_ref}, {"R", 'd', &c.R_gas}, {"HB", 'h', &hb}};
-  rc = read_kv_file(dir, "physics.inp", pk, 10, 0);
+               {"rho_ref", 'd', &c.rho_ref}, {"p_ref", 'd', &c.p_ref}, {"R", 'd', &c.R_gas}, {"HB", 'h', &hb},
+               {"gravity_type", 'i', &c.grav_type}};
+  rc = read_kv_file(dir, "physics.inp", pk, 11, 0);
   if (rc) return rc;
-  if (c.model != GB_MODEL_NS3D && grav[0] != 0.0) {
-    gbh_set_error("gravity is supported for NavierStokes3D only on this path");
+  if (c.model == GB_MODEL_EULER2D && grav[0] != 0.0) {
+    gbh_set_error("gravity: Euler2D has none");
     return GB_ERR_UNSUPPORTED;
   }
-  for (int d = 0; d < 3; d++) c.gravity[d] = c.model == GB_MODEL_NS3D ? grav[d] : 0.0;
+  for (int d = 0; d < 3; d++) c.gravity[d] = (c.model == GB_MODEL_NS3D || d == 0) ? grav[d] : 0.0;
+  if (c.model == GB_MODEL_EULER2D) c.gravity[0] = 0.0;
   c.HB = hb.hb;
   c.N_bv = hb.nbv;
   if (!strcmp(upw, "roe")) c.upwind = GB_UPWIND_ROE;
@@ -541,9 +575,19 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     gbh_set_error("gravity with CRWENO5 is not available on this path");
     return GB_ERR_UNSUPPORTED;
   }
-  if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.upwind != GB_UPWIND_RUSANOV) {
+  if (c.model == GB_MODEL_NS3D && (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) &&
+      c.upwind != GB_UPWIND_RUSANOV) {
     /* NavierStokes3DInitialize.c:370-378 */
     gbh_set_error("rusanov upwinding is needed for flows with gravitational forces");
+    return GB_ERR_INPUT;
+  }
+  if (c.model == GB_MODEL_EULER1D && c.gravity[0] != 0.0 && c.upwind != GB_UPWIND_ROE && c.upwind != GB_UPWIND_LLF) {
+    /* Euler1DInitialize.c:144-150 */
+    gbh_set_error("llf-char or roe upwinding is needed for flows with gravitational forces");
+    return GB_ERR_INPUT;
+  }
+  if (c.model == GB_MODEL_EULER1D && c.gravity[0] != 0.0 && c.grav_type != 0 && c.grav_type != 1) {
+    gbh_set_error("gravity_type %d not supported (0, 1)", c.grav_type);
     return GB_ERR_INPUT;
   }
   if (c.model == GB_MODEL_NS3D && c.Re > 0) {
@@ -628,9 +672,9 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     }
   }
 
-  /* gravity fields (NavierStokes3DGravityField.c:36-153) */
+  /* gravity fields (NavierStokes3DGravityField.c:36-153, Euler1DGravityField.c:23-95) */
   if (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) {
-    rc = gravity_fields(&c, res);
+    rc = c.model == GB_MODEL_EULER1D ? gravity_field_1d(&c, res) : gravity_fields(&c, res);
     if (rc) {
       gb_inputs_free(res);
       return rc;

@@ -89,6 +89,11 @@ typedef struct gb_config {
   double gravity[3], rho_ref, p_ref, R_gas, N_bv;
   int HB;
   int hyp_scheme;           /* GB_SCHEME_* (solver.inp hyp_space_scheme) */
+  /* Euler1D gravity: gravity[0] is physics.inp "gravity", grav_type its gravity_type (0:
+   * field exp(-g x), 1: exp(sin(2 pi x)/(2 pi))); needs roe or llf-char upwinding
+   * (Euler1DInitialize.c:144); the field comes through gb_solver_set_gravity_field as
+   * 1/S then S */
+  int grav_type;
 } gb_config;
 
 typedef struct gb_solver gb_solver;

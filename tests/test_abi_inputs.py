@@ -223,23 +223,23 @@ def _deck(d, case):
 
 def test_reader_gravity_errors(built_lib, tmp_path):
     """Gravity needs rusanov upwinding (NavierStokes3DInitialize.c:370-378); HB = 3 only
-    along z (NavierStokes3DGravityField.c:98-106); on this path only NavierStokes3D."""
+    along z (NavierStokes3DGravityField.c:98-106); Euler2D has none."""
     case = C.rising_thermal_bubble(8, n_iter=1)
     case.upwinding = "roe"
     _expect(3, str(_deck(tmp_path / "a", case)))
     case = C.rising_thermal_bubble(8, n_iter=1, HB=3)
     _expect(3, str(_deck(tmp_path / "b", case)))
-    d = _deck(tmp_path / "c", C.sod(16, n_iter=1))
+    d = _deck(tmp_path / "c", C.vortex(12, n_iter=1, dt=0.01))
     open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding roe\n gravity 1.0\nend\n")
-    _expect(4, str(d))
+    _expect(4, str(d))  # Euler2D has no gravity
 
 
 def test_solver_create_rejects_bad_gravity(built_lib):
     """gb_solver_create validates before touching a device: gravity outside
-    NavierStokes3D, or with another upwinding than rusanov, is refused."""
+    NavierStokes3D and Euler1D, or with another upwinding than rusanov (NavierStokes3D), is refused."""
     L = _lib.lib()
     dx = np.zeros(64)
-    for model, nd, upw, rc_want, msg in (("euler2d", 2, "roe", 4, b"NavierStokes3D only"),
+    for model, nd, upw, rc_want, msg in (("euler2d", 2, "roe", 4, b"Euler2D has none"),
                                          ("navierstokes3d", 3, "roe", 1, b"rusanov")):
         cfg = _lib.GbConfig()
         cfg.model, cfg.ndims, cfg.nvars, cfg.ghosts = _lib.MODEL[model], nd, nd + 2, 3
@@ -267,3 +267,15 @@ def test_reader_crweno(built_lib, tmp_path):
     case = C.rising_thermal_bubble(8, n_iter=1)
     case.hyp_scheme = "crweno5"
     _expect(4, str(_deck(tmp_path / "d", case)))
+
+
+@pytest.mark.parametrize("grav_type", [0, 1])
+def test_reader_euler1d_gravity(built_lib, oracle_lib, tmp_path, grav_type):
+    """physics.inp gravity / gravity_type for Euler1D: the field 1/S then S, bit-identical
+    to the oracle's (Euler1DGravityField.c); gravity needs roe or llf-char upwinding."""
+    case = C.stratified_1d(32, n_iter=1, grav_type=grav_type)
+    inp = Inputs(str(_deck(tmp_path / "a", case)))
+    assert inp.config.grav_type == grav_type and inp.config.gravity[0] == 1.0
+    assert np.array_equal(inp.gravity_field, O.Problem(case).gravity_field())
+    case.upwinding = "rusanov"
+    _expect(3, str(_deck(tmp_path / "b", case)))

@@ -211,3 +211,79 @@ def test_gravity_needs_the_field(built_lib, tmp_path):
     rc = _lib.lib().gb_rhs_explicit_noalloc(ctypes.byref(inp.config), ctypes.c_void_p(dx.data_ptr()),
                                             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(u.data_ptr()), None)
     assert rc == 4
+
+
+# ---------------------------------------------------------------------------
+# Euler1D in a gravity field (Xing & Shu's well-balanced form; Euler1DSource.c,
+# Euler1DModifiedSolution.c, Euler1DUpwind.c with kappa = max(S_L, S_R)).
+# ---------------------------------------------------------------------------
+E1_VARIANTS = [(0, "components", "roe", "js"), (0, "characteristic", "llf-char", "yc"),
+               (1, "characteristic", "roe", "mapped"), (1, "components", "llf-char", "borges"),
+               (0, "components", "llf-char", "none"), (1, "characteristic", "llf-char", "js")]
+
+
+def strat(grav_type, interp, upw, weights, **kw):
+    case = C.stratified_1d(kw.pop("n", 96), grav_type=grav_type, interp=interp, upwinding=upw, **kw)
+    case.weights = weights
+    return case
+
+
+@pytest.mark.parametrize("grav_type,interp,upw,weights", E1_VARIANTS)
+def test_euler1d_gravity_rhs_and_steps(built_lib, oracle_lib, tmp_path, grav_type, interp, upw, weights):
+    case = strat(grav_type, interp, upw, weights, n_iter=10, perturb=0.05)
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    out = torch.zeros_like(u)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, 3, 3)
+    assert relerr(got, O.interior(P.rhs(u0.copy()), case.size, 3, 3)) <= RHS_TOL
+    s.step(10)
+    ref = O.interior(P.rk(P.u0(), 10), case.size, 3, 3).reshape(-1)
+    assert relerr(s.get_state(), ref) <= STEP_TOL
+
+
+@pytest.mark.parametrize("grav_type", [0, 1])
+def test_euler1d_hydrostatic_state_is_preserved(built_lib, oracle_lib, tmp_path, grav_type):
+    """The isothermal atmosphere rho = p = S at rest: its right-hand side is rounding
+    noise while its gravity source alone is O(rho g); it stays at rest over steps."""
+    case = C.stratified_1d(200, n_iter=1, grav_type=grav_type, perturb=0.0)
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    out = torch.zeros_like(u)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, 3, 3)
+    src = O.interior(P.source(u0), case.size, 3, 3)
+    assert np.abs(src[:, 1]).max() > 0.1
+    assert np.abs(got).max() <= 1e-12, np.abs(got).max(axis=0)
+    s.step(20)
+    assert np.abs(s.get_state().reshape(-1, 3)[:, 1]).max() <= 1e-12
+
+
+def test_euler1d_gravity_function_pointers(built_lib, oracle_lib, tmp_path):
+    """HyperbolicFunction, SourceFunction, UFunction (u / S) and Upwind (Roe and LLF
+    dissipation scaled by max(S_L, S_R)) with Euler1D gravity."""
+    for upw in ("roe", "llf-char"):
+        case = strat(0, "components", upw, "js", n=64, perturb=0.05)
+        rng = np.random.default_rng(5)
+        case.u[:, 1] = 0.3 * rng.standard_normal(64) * case.u[:, 0]
+        s = solver_for(case, tmp_path / upw)
+        P = O.Problem(case)
+        u0 = P.u0()
+        u = torch.from_numpy(u0).cuda()
+        s.apply_bc(u)
+        hyp = torch.zeros_like(u)
+        s.hyperbolic(hyp, u)
+        assert relerr(hyp.cpu().numpy(), P.hyperbolic(u0)) <= RHS_TOL
+        src = torch.full_like(u, 3.0)
+        s.source(src, u)
+        assert relerr(src.cpu().numpy(), P.source(u0)) <= RHS_TOL
+        fg = P.gravity_field()
+        n = P.npts_wg
+        uc = torch.zeros_like(u)
+        s.ufunc(uc, u)
+        U = P.apply_bc(u0).reshape(-1, 3)
+        assert relerr(uc.cpu().numpy().reshape(-1, 3), U * fg[:n, None]) <= 1e-15
