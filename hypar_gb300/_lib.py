@@ -35,7 +35,7 @@ EXPORTS = [
     "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
     "gb_ensemble_set_state", "gb_ensemble_get_state", "gb_ensemble_step", "gb_ensemble_time",
     "gb_ensemble_set_launch", "gb_ensemble_get_launch", "gb_ensemble_autotune", "gb_rhs_explicit_noalloc",
-    "gb_adjoint_create", "gb_adjoint_destroy", "gb_adjoint_set_stream", "gb_adjoint_sync", "gb_adjoint_set_launch",
+    "gb_adjoint_create", "gb_adjoint_create_ex", "gb_adjoint_destroy", "gb_adjoint_set_stream", "gb_adjoint_sync", "gb_adjoint_set_launch",
     "gb_adjoint_get_launch", "gb_adjoint_info", "gb_adjoint_rhs_vjp", "gb_adjoint_rhs_jvp", "gb_adjoint_forward",
     "gb_adjoint_backward", "gb_adjoint_tlm", "gb_inputs_exact", "gb_solver_set_time", "gb_solver_cfl",
     "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
@@ -151,6 +151,8 @@ def lib():
     L.gb_op_to_initial.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
     L.gb_adjoint_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(VP)]
+    L.gb_adjoint_create_ex.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_longlong, ctypes.POINTER(VP)]
     L.gb_adjoint_destroy.argtypes = [VP]
     L.gb_adjoint_destroy.restype = None
     L.gb_adjoint_set_stream.argtypes = [VP, VP]

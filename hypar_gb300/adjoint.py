@@ -26,14 +26,17 @@ class Adjoint:
     """gb_adjoint: forward sweep with checkpoints, backward sweep, tangent-linear
     model, and the right-hand side's VJP / JVP."""
 
-    def __init__(self, config: GbConfig, dxinv: np.ndarray, nsteps: int, ncheck: int = 0, device: int = 0):
+    def __init__(self, config: GbConfig, dxinv: np.ndarray, nsteps: int, ncheck: int = 0, device: int = 0,
+                 wide_tape_max: int = -1):
+        """wide_tape_max: bytes allowed for the 72-double interface tapes (< 0: 60 % of
+        the free device memory; 0: always the 8-double tape)."""
         import torch
         self.config = config
         self.nsteps = nsteps
         self._dxinv = np.ascontiguousarray(dxinv, dtype=np.float64)
         h = ctypes.c_void_p()
-        check(lib().gb_adjoint_create(ctypes.byref(config), self._dxinv.ctypes.data_as(_lib.DP), nsteps, ncheck,
-                                      device, ctypes.byref(h)))
+        check(lib().gb_adjoint_create_ex(ctypes.byref(config), self._dxinv.ctypes.data_as(_lib.DP), nsteps, ncheck,
+                                         device, int(wide_tape_max), ctypes.byref(h)))
         self._h = h
         self.dxinv_dev = torch.from_numpy(self._dxinv).to(f"cuda:{device}")
         g = config.ghosts

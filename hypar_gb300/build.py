@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgbhypar.so")
 CLI = os.path.join(HERE, "gbhypar")
 
-CU_SOURCES = ["gbh_hyp_e1.cu", "gbh_hyp_e2.cu", "gbh_hyp_ns.cu", "gbh_hyp_e1w.cu", "gbh_hyp_e2w.cu", "gbh_hyp_nsw.cu", "gbh_hyp_nsg.cu", "gbh_visc.cu", "gbh_api.cu", "gbh_probe.cu", "gbh_ensemble.cu",
+CU_SOURCES = ["gbh_hyp_e1.cu", "gbh_hyp_e2.cu", "gbh_hyp_ns.cu", "gbh_hyp_e1w.cu", "gbh_hyp_e2w.cu", "gbh_hyp_nsw.cu", "gbh_hyp_nsg.cu", "gbh_hyp_e1b.cu", "gbh_hyp_e2b.cu", "gbh_hyp_nsb.cu", "gbh_visc.cu", "gbh_api.cu", "gbh_probe.cu", "gbh_ensemble.cu",
               "gbh_noalloc.cu", "gbh_adjoint.cu", "gbh_monitor.cu", "gbh_crweno.cu"]
 C_SOURCES = ["gbh_inputs.c", "gbh_run.c"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -72,7 +72,7 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc=None) -> str:
         if force or _stale(o, [s] + headers):
             jobs.append(["gcc", "-O2", "-std=c99", "-fPIC", "-Wall", "-I", INCLUDE, "-c", s, "-o", o])
     if jobs:
-        with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 8, 16, len(jobs)))) as ex:
             for out in ex.map(_run, jobs):
                 if verbose and out.strip():
                     print(out)

@@ -1068,6 +1068,11 @@ static double* const* tapes(gb_adjoint* a, int b, int i) { return &a->sT[b][(siz
 
 extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int nsteps, int ncheck, int device,
                                  gb_adjoint** out) {
+  return gb_adjoint_create_ex(cfg, dxinv, nsteps, ncheck, device, -1, out);
+}
+
+extern "C" int gb_adjoint_create_ex(const gb_config* cfg, const double* dxinv, int nsteps, int ncheck, int device,
+                                    long long wide_tape_max, gb_adjoint** out) {
   if (!out || !dxinv || nsteps < 1) { gbh_set_error("gb_adjoint_create: bad argument"); return GB_ERR_ARG; }
   *out = nullptr;
   int rc = gbh_validate(cfg);
@@ -1117,21 +1122,27 @@ extern "C" int gb_adjoint_create(const gb_config* cfg, const double* dxinv, int 
   a->nbuf = a->nseg > 1 ? 2 : 1;
   size_t narr = (size_t)a->nseg + (size_t)a->nbuf * ((a->seglen + 1) + (size_t)a->seglen * (ns - 1)) + 1 + 1 + 4 + 1;
   a->bytes = narr * a->nvals * sizeof(double);
-  // interface tapes: per buffer, step and stage, at every interface of both
-  // directions uL and uR (8 values), widened to TAPE_WIDE values (the WENO pairs'
-  // smoothness terms and normalisations) while that stays within kWideTapeBytes
-  const size_t nif = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) + (size_t)cfg->dim[0] * (cfg->dim[1] + 1);
-  const size_t kWideTapeBytes = (size_t)24 << 30;
-  a->tape_w = (size_t)a->nbuf * a->seglen * ns * nif * TAPE_WIDE * sizeof(double) <= kWideTapeBytes ? TAPE_WIDE : 8;
-  const size_t tape_x = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) * a->tape_w;
-  const size_t tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * a->tape_w;
-  const size_t tape_bytes = (size_t)a->nbuf * a->seglen * ns * (tape_x + tape_y) * sizeof(double);
-  a->bytes += tape_bytes;
   if (device >= 0) {
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { gbh_set_error("cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); delete a; return GB_ERR_CUDA; }
   }
   cudaGetDevice(&a->device);
+  // interface tapes: per buffer, step and stage, at every interface of both
+  // directions uL and uR (8 values), widened to TAPE_WIDE values (the WENO pairs'
+  // smoothness terms and normalisations) when the wide tapes take at most 60 % of
+  // the device memory left free by the state arrays (a 256^2 RK4 run of 400 steps
+  // keeping every state: 121 GB of wide tapes, within a GB300's 280 GB)
+  const size_t nif = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) + (size_t)cfg->dim[0] * (cfg->dim[1] + 1);
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+  const size_t room = free_b > a->bytes ? free_b - a->bytes : 0;
+  const size_t wide_bytes = (size_t)a->nbuf * a->seglen * ns * nif * TAPE_WIDE * sizeof(double);
+  const size_t cap = wide_tape_max < 0 ? room / 10 * 6 : (size_t)wide_tape_max;
+  a->tape_w = wide_bytes <= cap ? TAPE_WIDE : 8;
+  const size_t tape_x = (size_t)cfg->dim[1] * (cfg->dim[0] + 1) * a->tape_w;
+  const size_t tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * a->tape_w;
+  const size_t tape_bytes = (size_t)a->nbuf * a->seglen * ns * (tape_x + tape_y) * sizeof(double);
+  a->bytes += tape_bytes;
   cudaError_t e = cudaMalloc((void**)&a->block, a->bytes - tape_bytes);
   if (e == cudaSuccess) e = cudaMemset(a->block, 0, a->bytes - tape_bytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&a->tblock2, tape_bytes);

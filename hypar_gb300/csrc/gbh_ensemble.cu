@@ -8,7 +8,9 @@
 // are per member.  Their arrays are concatenated; every Runge-Kutta stage is
 // one launch per direction over all members (each thread finds its member in a
 // table of thread offsets), and a whole step is captured once in a CUDA graph
-// and replayed.  The segment length per direction is chosen by timing.
+// and replayed.  The launch form per direction -- segment walker (one thread per
+// segment of a grid line) or tiles of 32/64/128 interfaces (one block per tile,
+// set as a negative segment length) -- is chosen by timing.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -17,11 +19,11 @@
 
 namespace gbh {
 cudaError_t launch_batched_euler1d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                   const double*, const PhysParams&, const StageEpi&, int, cudaStream_t);
+                                   const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
 cudaError_t launch_batched_euler2d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                   const double*, const PhysParams&, const StageEpi&, int, cudaStream_t);
+                                   const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
 cudaError_t launch_batched_ns3d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                const double*, const PhysParams&, const StageEpi&, int, cudaStream_t);
+                                const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
 cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
 }  // namespace gbh
 
@@ -77,7 +79,9 @@ static void rebuild_table(gb_ensemble* e) {
       for (int k = 0; k < e->base.ndims; k++)
         if (k != d) ntr *= md.G.dim[k];
       md.ntrans[d] = ntr;
-      md.nseg[d] = (md.G.dim[d] + e->seg[d] - 1) / e->seg[d];
+      // walker: threads (segments x lines); tiles: blocks (tiles x lines)
+      const int ti = -e->seg[d];
+      md.nseg[d] = e->seg[d] > 0 ? (md.G.dim[d] + e->seg[d] - 1) / e->seg[d] : (md.G.dim[d] + ti - 2) / (ti - 1);
       md.start[d] = e->total_thr[d];
       e->total_thr[d] += ntr * md.nseg[d];
     }
@@ -94,14 +98,16 @@ static int upload_table(gb_ensemble* e) {
 
 static cudaError_t launch_dir(gb_ensemble* e, int d, const double* U, const StageEpi& ep) {
   const gb_config& c = e->base;
+  const int tile = e->seg[d] < 0 ? -e->seg[d] : 0;
+  if (tile && e->total_thr[d] > 0x7fffffffLL) return cudaErrorInvalidConfiguration;  // one block per tile
   if (c.model == GB_MODEL_EULER1D)
     return launch_batched_euler1d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx,
-                                  e->pp, ep, e->block[d], e->stream);
+                                  e->pp, ep, e->block[d], tile, e->stream);
   if (c.model == GB_MODEL_EULER2D)
     return launch_batched_euler2d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx,
-                                  e->pp, ep, e->block[d], e->stream);
+                                  e->pp, ep, e->block[d], tile, e->stream);
   return launch_batched_ns3d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx, e->pp,
-                             ep, e->block[d], e->stream);
+                             ep, e->block[d], tile, e->stream);
 }
 
 // The launches of one Runge-Kutta step (ns stages x ndims directions).
@@ -379,7 +385,11 @@ extern "C" int gb_ensemble_step(gb_ensemble* e, int nsteps) {
 
 extern "C" int gb_ensemble_set_launch(gb_ensemble* e, int dir, int seg, int block) {
   if (!e || dir < 0 || dir >= e->base.ndims) { gbh_set_error("gb_ensemble_set_launch: bad argument"); return GB_ERR_ARG; }
-  if (seg > 0) e->seg[dir] = seg;
+  if (seg < 0 && seg != -32 && seg != -64 && seg != -128) {
+    gbh_set_error("gb_ensemble_set_launch: a tile form is -32, -64 or -128 (got %d)", seg);
+    return GB_ERR_ARG;
+  }
+  if (seg != 0) e->seg[dir] = seg;
   if (block > 0) {
     if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
     e->block[dir] = block;
@@ -410,12 +420,13 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
   int rc = GB_OK;
-  const int cand[] = {8, 12, 16, 20, 24, 27, 32, 40, 48, 54, 64};
+  const int cand[] = {8, 12, 16, 20, 24, 27, 32, 40, 48, 54, 64, -32, -64, -128};
   for (int d = 0; d < e->base.ndims && !rc; d++) {
     float best = 1e30f;
     int bs = e->seg[d], bb = e->block[d];
     for (int sg : cand) {
       for (int blk : {128, 64}) {
+        if (sg < 0 && blk != 128) continue;  // a tile's block is its interfaces
         e->seg[d] = sg;
         e->block[d] = blk;
         rc = upload_table(e);

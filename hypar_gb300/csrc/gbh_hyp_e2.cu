@@ -21,9 +21,4 @@ cudaError_t launch_unfused_euler2d(int kind, int dir, int upw, double* out, cons
                                    const PhysParams& pp, cudaStream_t s) {
   return launch_unfused_model<MODEL_EULER2D>(kind, dir, upw, out, a, b, c, d, u, G, pp, s);
 }
-cudaError_t launch_batched_euler2d(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
-                                   const double* U, double* H, const double* dxinv, const PhysParams& pp,
-                                   const StageEpi& ep, int block, cudaStream_t s) {
-  return launch_batched_model<MODEL_EULER2D>(dir, chr, upw, mem, nmem, total, U, H, dxinv, pp, ep, block, s);
-}
 }  // namespace gbh

@@ -1,0 +1,10 @@
+// EULER2D instantiation of the batched (ensemble) kernels: the segment
+// walker and the tile form over all members of an ensemble.
+#include "gbh_hyp_impl.cuh"
+namespace gbh {
+cudaError_t launch_batched_euler2d(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
+                                   const double* U, double* H, const double* dxinv, const PhysParams& pp,
+                                   const StageEpi& ep, int block, int tile, cudaStream_t s) {
+  return launch_batched_model<MODEL_EULER2D>(dir, chr, upw, mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s);
+}
+}  // namespace gbh

@@ -621,18 +621,20 @@ __device__ __forceinline__ void stage_epilogue(const StageEpi& ep, double* __res
 // window's cells for every segment and one interface per segment boundary; with the
 // one-to-three-interface segments that small grids need to occupy the GPU that
 // redundancy is most of the work.  No gravity; WT: the adjoint's wide tape.
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
-__global__ void __launch_bounds__(TI)
-hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
-                PhysParams pp, StageEpi ep, long long ntrans) {
+// The tile of block `blk` of a grid (blocks ordered line-fastest, then tile index).
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT>
+__device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, double* __restrict__ H,
+                                              const double* __restrict__ dxinv, const DevGeom& G,
+                                              const PhysParams& pp, const StageEpi& ep, long long ntrans,
+                                              long long blk) {
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
   constexpr int TC = TI - 1, NCELL = TI + 5;
   __shared__ double su[NCELL][NV], sf[NCELL][NV], suc[NCELL];
   __shared__ CellAux<M> sax[NCELL];
   __shared__ double sfI[TI][NV];
-  const long long line = blockIdx.x % ntrans;
-  const int I0 = (int)(blockIdx.x / ntrans) * TC;
+  const long long line = blk % ntrans;
+  const int I0 = (int)(blk / ntrans) * TC;
   long long tr = line, pbase = (long long)G.g * G.stride[DIR];
 #pragma unroll
   for (int e = 0; e < ND; e++) {
@@ -701,6 +703,13 @@ hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
   }
 }
 
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
+__global__ void __launch_bounds__(TI)
+hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
+                PhysParams pp, StageEpi ep, long long ntrans) {
+  hyp_tile_body<M, CHAR, UPW, DIR, ALTW, TI, WT>(U, H, dxinv, G, pp, ep, ntrans, blockIdx.x);
+}
+
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV = false, bool WT = false>
 __global__ void __launch_bounds__(128)
 hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv,
@@ -713,22 +722,18 @@ hyp_dir_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
 // All members of an ensemble advanced by one launch per direction: a thread
 // finds its member by binary search over the start offsets, then walks its
 // segment exactly as in the single-grid kernel.
-template <int M, bool CHAR, int UPW, int DIR>
-__global__ void __launch_bounds__(128)
-hyp_batched_kernel(const MemberDev* __restrict__ mem, int nmem, long long total, const double* __restrict__ U,
-                   double* __restrict__ H, const double* __restrict__ dxinv, PhysParams pp, StageEpi ep) {
-  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid >= total) return;
+// The member that owns work item `w` of direction DIR (members' first items
+// ascending), with the stage pointers moved to its arrays.
+template <int DIR>
+__device__ __forceinline__ const MemberDev& batched_member(const MemberDev* __restrict__ mem, int nmem, long long w,
+                                                           StageEpi& e) {
   int lo = 0, hi = nmem - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (mem[mid].start[DIR] <= tid) lo = mid;
+    if (mem[mid].start[DIR] <= w) lo = mid;
     else hi = mid - 1;
   }
   const MemberDev& m = mem[lo];
-  long long lt = tid - m.start[DIR];
-  long long ntr = m.ntrans[DIR];
-  StageEpi e = ep;
   const long long o = m.off;
   if (e.par) e.par += o;
   if (e.rhs) e.rhs += o;
@@ -738,32 +743,72 @@ hyp_batched_kernel(const MemberDev* __restrict__ mem, int nmem, long long total,
 #pragma unroll
   for (int t = 0; t < 4; t++)
     if (e.P[t]) e.P[t] += o;
+  return m;
+}
+
+template <int M, bool CHAR, int UPW, int DIR>
+__global__ void __launch_bounds__(128)
+hyp_batched_kernel(const MemberDev* __restrict__ mem, int nmem, long long total, const double* __restrict__ U,
+                   double* __restrict__ H, const double* __restrict__ dxinv, PhysParams pp, StageEpi ep) {
+  long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= total) return;
+  StageEpi e = ep;
+  const MemberDev& m = batched_member<DIR>(mem, nmem, tid, e);
+  long long lt = tid - m.start[DIR];
+  long long ntr = m.ntrans[DIR];
+  const long long o = m.off;
   hyp_segment<M, CHAR, UPW, DIR>(U + o, H ? H + o : nullptr, dxinv + m.dx_off[DIR], m.G, pp, e, m.seg[DIR],
                                  lt % ntr, (int)(lt / ntr));
 }
 
+// Tile form of the batched kernel: one block per tile of TI interfaces of one
+// member's grid line; the members' tables count blocks instead of threads.
+template <int M, bool CHAR, int UPW, int DIR, int TI>
+__global__ void __launch_bounds__(TI)
+hyp_batched_tile_kernel(const MemberDev* __restrict__ mem, int nmem, const double* __restrict__ U,
+                        double* __restrict__ H, const double* __restrict__ dxinv, PhysParams pp, StageEpi ep) {
+  StageEpi e = ep;
+  const long long b = blockIdx.x;
+  const MemberDev& m = batched_member<DIR>(mem, nmem, b, e);
+  const long long o = m.off;
+  hyp_tile_body<M, CHAR, UPW, DIR, false, TI, false>(U + o, H ? H + o : nullptr, dxinv + m.dx_off[DIR], m.G, pp,
+                                                     e, m.ntrans[DIR], b - m.start[DIR]);
+}
+
+// total = threads (walker, tile == 0) or blocks (tiles of `tile` interfaces).
 template <int M, bool CHAR, int UPW, int DIR>
 cudaError_t launch_batched_dir(const MemberDev* mem, int nmem, long long total, const double* U, double* H,
-                               const double* dxinv, const PhysParams& pp, const StageEpi& ep, int block,
+                               const double* dxinv, const PhysParams& pp, const StageEpi& ep, int block, int tile,
                                cudaStream_t s) {
-  if (block <= 0) block = 128;
-  long long grid = (total + block - 1) / block;
-  hyp_batched_kernel<M, CHAR, UPW, DIR><<<(unsigned)grid, block, 0, s>>>(mem, nmem, total, U, H, dxinv, pp, ep);
+  if (total <= 0) return cudaSuccess;
+  if (tile == 32)
+    hyp_batched_tile_kernel<M, CHAR, UPW, DIR, 32><<<(unsigned)total, 32, 0, s>>>(mem, nmem, U, H, dxinv, pp, ep);
+  else if (tile == 64)
+    hyp_batched_tile_kernel<M, CHAR, UPW, DIR, 64><<<(unsigned)total, 64, 0, s>>>(mem, nmem, U, H, dxinv, pp, ep);
+  else if (tile == 128)
+    hyp_batched_tile_kernel<M, CHAR, UPW, DIR, 128><<<(unsigned)total, 128, 0, s>>>(mem, nmem, U, H, dxinv, pp, ep);
+  else if (tile != 0)
+    return cudaErrorInvalidValue;
+  else {
+    if (block <= 0) block = 128;
+    long long grid = (total + block - 1) / block;
+    hyp_batched_kernel<M, CHAR, UPW, DIR><<<(unsigned)grid, block, 0, s>>>(mem, nmem, total, U, H, dxinv, pp, ep);
+  }
   return cudaGetLastError();
 }
 
 template <int M>
 cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
                                  const double* U, double* H, const double* dxinv, const PhysParams& pp,
-                                 const StageEpi& ep, int block, cudaStream_t s) {
+                                 const StageEpi& ep, int block, int tile, cudaStream_t s) {
   constexpr int ND = ModelTraits<M>::ND;
 #define GBH_B(C, W)                                                                                          \
   do {                                                                                                       \
-    if (dir == 0) return launch_batched_dir<M, C, W, 0>(mem, nmem, total, U, H, dxinv, pp, ep, block, s);  \
+    if (dir == 0) return launch_batched_dir<M, C, W, 0>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
     if (ND > 1 && dir == 1)                                                                                  \
-      return launch_batched_dir<M, C, W, (ND > 1 ? 1 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, s); \
+      return launch_batched_dir<M, C, W, (ND > 1 ? 1 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
     if (ND > 2 && dir == 2)                                                                                  \
-      return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, s); \
+      return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
     return cudaErrorInvalidValue;                                                                            \
   } while (0)
   // Rusanov: Euler1D and NavierStokes3D (Euler2D offers none); the template

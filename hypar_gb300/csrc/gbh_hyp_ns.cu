@@ -11,9 +11,4 @@ cudaError_t launch_unfused_ns3d(int kind, int dir, int upw, double* out, const d
                                    const PhysParams& pp, cudaStream_t s) {
   return launch_unfused_model<MODEL_NS3D>(kind, dir, upw, out, a, b, c, d, u, G, pp, s);
 }
-cudaError_t launch_batched_ns3d(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
-                                   const double* U, double* H, const double* dxinv, const PhysParams& pp,
-                                   const StageEpi& ep, int block, cudaStream_t s) {
-  return launch_batched_model<MODEL_NS3D>(dir, chr, upw, mem, nmem, total, U, H, dxinv, pp, ep, block, s);
-}
 }  // namespace gbh

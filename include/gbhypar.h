@@ -212,9 +212,13 @@ int gb_ensemble_set_state(gb_ensemble *e, int member, const double *u, int layou
 int gb_ensemble_get_state(gb_ensemble *e, int member, double *u, int layout, int mem);
 int gb_ensemble_step(gb_ensemble *e, int nsteps);
 double gb_ensemble_time(const gb_ensemble *e);
+/* Launch shape per direction, as gb_solver_set_launch: seg > 0 interfaces walked per
+ * thread, seg = -32, -64 or -128 one block per tile of that many interfaces of a
+ * member's grid line; 0 keeps the current value. */
 int gb_ensemble_set_launch(gb_ensemble *e, int dir, int seg, int block);
 int gb_ensemble_get_launch(gb_ensemble *e, int dir, int *seg, int *block);
-/* Choose seg/block per direction by timing graph-replayed steps (state restored). */
+/* Choose seg/block (walker or tiles) per direction by timing graph-replayed steps
+ * (state restored). */
 int gb_ensemble_autotune(gb_ensemble *e, int reps);
 
 /* Read the deck in `dir`, run n_iter steps on the GPU and write op.bin (and
@@ -284,10 +288,17 @@ int gb_TimeRK(void *ts);
  * into ncheck segments: the forward sweep stores u at the start of each and
  * every stage state of the last; the backward sweep recomputes each earlier
  * segment once from its checkpoint with the fused forward kernels, keeping its
- * stage states, then reverses it step by step. */
+ * stage states, then reverses it step by step.  Per kept stage the forward
+ * kernels also record an interface tape for the reversal: 72 doubles per
+ * interface when those tapes fit in 60 % of the device memory left free by the
+ * states, else 8 (gb_adjoint_info reports the bytes held). */
 typedef struct gb_adjoint gb_adjoint;
 int gb_adjoint_create(const gb_config *cfg, const double *dxinv, int nsteps, int ncheck, int device,
                       gb_adjoint **out);
+/* As gb_adjoint_create with a cap on the wide tapes' bytes: < 0 the automatic
+ * choice above, 0 always the 8-double tape, > 0 wide tapes up to that many bytes. */
+int gb_adjoint_create_ex(const gb_config *cfg, const double *dxinv, int nsteps, int ncheck, int device,
+                         long long wide_tape_max, gb_adjoint **out);
 void gb_adjoint_destroy(gb_adjoint *a);
 int gb_adjoint_set_stream(gb_adjoint *a, void *stream);
 int gb_adjoint_sync(gb_adjoint *a);

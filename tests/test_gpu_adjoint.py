@@ -37,10 +37,11 @@ def problem(tmp_path_factory):
     return case, u_true, d
 
 
-def make(problem, ncheck=0, nsteps=None):
+def make(problem, ncheck=0, nsteps=None, wide_tape_max=-1):
     case, _, d = problem
     inp = Inputs(d)
-    return Adjoint(inp.config, inp.dxinv, nsteps or case.n_iter, ncheck=ncheck, device=0)
+    return Adjoint(inp.config, inp.dxinv, nsteps or case.n_iter, ncheck=ncheck, device=0,
+                   wide_tape_max=wide_tape_max)
 
 
 def state(adj, u_int, seed=None, scale=0.0):
@@ -166,8 +167,11 @@ def test_checkpoint_policies_agree(built_lib, problem):
     case, _, _ = problem
     w = None
     grads = []
-    for ncheck in (1, 0, 7, 24):
-        adj = make(problem, ncheck=ncheck)
+    held = {}
+    # every checkpoint policy with the wide (72-double) interface tape, and two with the 8-double one
+    for ncheck, wide in ((1, -1), (0, -1), (7, -1), (24, -1), (1, 0), (0, 0)):
+        adj = make(problem, ncheck=ncheck, wide_tape_max=wide)
+        held[(ncheck, wide)] = adj.info()["bytes"]
         u0 = state(adj, case.u)
         if w is None:
             w = rand_interior(adj, 9)
@@ -182,6 +186,7 @@ def test_checkpoint_policies_agree(built_lib, problem):
     # from run to run: the same policy twice differs by ~5e-13 after 24 steps
     for g in grads[1:]:
         assert np.linalg.norm(g - grads[0]) / np.linalg.norm(grads[0]) <= 1e-11
+    assert held[(1, 0)] < held[(1, -1)] and held[(0, 0)] < held[(0, -1)]  # the narrow tape is smaller
 
 
 def test_misfit_gradient_vs_central_differences(built_lib, problem):
