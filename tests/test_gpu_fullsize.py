@@ -1,0 +1,103 @@
+"""Parity at the benchmark configurations' full sizes.
+
+Sod 1024 (RK4, dt 1e-4, 1000 steps) is cheap enough for the oracle to run whole.
+For the 1024^2 vortex and the 256^3 Taylor-Green vortex the oracle evaluates one
+right-hand side at full size: relative L2 <= 1e-12, or, where the state's own
+conditioning puts rounding noise above that (a flux difference over a fine grid
+cancels O(1) fluxes to O(h)), within 4x the distance between the oracle and its
+FMA-contracted build, which measures that noise.  A size-independent
+property covers many steps: on a periodic grid the conservative flux difference
+telescopes, so the domain sums of the conserved variables stay constant to
+rounding.  (The viscous term does not telescope near the faces: on one rank the
+reference forms no cross derivative at ghost points,
+NavierStokes3DParabolicFunction.c:117-130, so the viscous fluxes there are not the
+periodic images of the interior ones; for the Taylor-Green vortex only the mass,
+which has no viscous flux, is conserved exactly.)"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from hypar_gb300 import cases as C
+from hypar_gb300.solver import Solver
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+RHS_TOL = 1e-12
+STEP_TOL = 1e-10
+
+
+def relerr(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+def solver_for(case, tmp_path):
+    d = str(tmp_path / "deck")
+    case.write(d)
+    return Solver.from_dir(d, device=0)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def oracle_threads(oracle_lib):
+    O.set_threads(os.cpu_count() or 1)
+
+
+def test_sod_full_configuration(built_lib, tmp_path):
+    """Sod shock tube, 1024 cells, comp-WENO5 + Roe, RK4, dt 1e-4, 1000 steps."""
+    case = C.sod(1024, n_iter=1000, dt=1e-4)
+    s = solver_for(case, tmp_path)
+    s.step(1000)
+    P = O.Problem(case)
+    ref = O.interior(P.rk(P.u0(), 1000), case.size, case.nvars, 3).reshape(-1)
+    assert relerr(s.get_state(), ref) <= STEP_TOL
+
+
+def _rhs_vs_oracle(s, case):
+    """(relative L2 distance GPU vs oracle, allowed distance)"""
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    out = torch.zeros_like(u)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
+    ref = O.interior(P.rhs(u0.copy()), case.size, case.nvars, 3)
+    noise = relerr(O.interior(O.Problem(case, fma=True).rhs(u0.copy()), case.size, case.nvars, 3), ref)
+    return relerr(got, ref), max(RHS_TOL, 4.0 * noise)
+
+
+def _sums(s, case):
+    u = s.get_state().reshape(-1, case.nvars)
+    return u.sum(axis=0), np.abs(u).sum(axis=0)
+
+
+def test_vortex_full_size(built_lib, tmp_path):
+    """Isentropic vortex 1024^2, char-WENO5 + Roe, SSPRK3 at CFL 0.5: one RHS against
+    the oracle; 20 steps conserve the domain sums of rho, rho u, rho v, e."""
+    case = C.vortex(1024, n_iter=20)
+    s = solver_for(case, tmp_path)
+    err, tol = _rhs_vs_oracle(s, case)
+    assert err <= tol, (err, tol)
+    s.set_state(case.u)
+    tot0, mag0 = _sums(s, case)
+    s.step(20)
+    tot, _ = _sums(s, case)
+    assert np.all(np.abs(tot - tot0) <= 1e-12 * mag0), (tot - tot0) / mag0
+
+
+def test_tgv_full_size(built_lib, tmp_path):
+    """Taylor-Green vortex 256^3, comp-WENO5 + Roe + viscous, RK4: one RHS of the
+    perturbed state against the oracle (the unperturbed t = 0 state's divergence is
+    rounding noise); 4 steps of the benchmark state conserve the mass."""
+    pert = C.tgv(256, n_iter=1, dt=2e-3, perturb=0.05)
+    s = solver_for(pert, tmp_path / "p")
+    err, tol = _rhs_vs_oracle(s, pert)
+    assert err <= tol, (err, tol)
+    s.close()
+    case = C.tgv(256, n_iter=4, dt=2e-3)
+    s = solver_for(case, tmp_path / "c")
+    tot0, mag0 = _sums(s, case)
+    s.step(4)
+    tot, _ = _sums(s, case)
+    assert abs(tot[0] - tot0[0]) <= 1e-12 * mag0[0], (tot[0] - tot0[0]) / mag0[0]
