@@ -39,7 +39,8 @@ EXPORTS = [
     "gb_adjoint_get_launch", "gb_adjoint_info", "gb_adjoint_rhs_vjp", "gb_adjoint_rhs_jvp", "gb_adjoint_forward",
     "gb_adjoint_backward", "gb_adjoint_tlm", "gb_inputs_exact", "gb_solver_set_time", "gb_solver_cfl",
     "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
-    "gb_solver_set_gravity_field",
+    "gb_solver_set_gravity_field", "gb_solver_conservation_begin", "gb_solver_conservation_error",
+    "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error",
 ]
 
 
@@ -57,7 +58,7 @@ class GbConfig(ctypes.Structure):
         ("zone_data", (ctypes.c_double * 8) * 12),
         ("gravity", ctypes.c_double * 3), ("rho_ref", ctypes.c_double), ("p_ref", ctypes.c_double),
         ("R_gas", ctypes.c_double), ("N_bv", ctypes.c_double), ("HB", ctypes.c_int), ("hyp_scheme", ctypes.c_int),
-        ("grav_type", ctypes.c_int),
+        ("grav_type", ctypes.c_int), ("cons_check", ctypes.c_int),
     ]
 
 
@@ -148,6 +149,10 @@ def lib():
     L.gb_solver_cfl.argtypes = [VP, DP]
     L.gb_solver_step_report.argtypes = [VP, ctypes.c_int, DP, DP]
     L.gb_solver_error.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, DP]
+    L.gb_solver_conservation_begin.argtypes = [VP]
+    L.gb_solver_conservation_error.argtypes = [VP, DP]
+    L.gb_ensemble_conservation_begin.argtypes = [VP]
+    L.gb_ensemble_conservation_error.argtypes = [VP, ctypes.c_int, DP]
     L.gb_op_to_initial.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
     L.gb_adjoint_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(VP)]

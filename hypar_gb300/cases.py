@@ -64,6 +64,7 @@ class Case:
     R_gas: float = 1.0
     HB: int = 0
     N_bv: float = 0.0
+    conservation_check: bool = False  # solver.inp conservation_check yes
 
     @property
     def ndims(self) -> int:
@@ -101,6 +102,8 @@ class Case:
         ]
         if self.restart_iter:
             lines.append(f"  restart_iter      {self.restart_iter}")
+        if self.conservation_check:
+            lines.append("  conservation_check yes")
         lines.append("end")
         return "\n".join(lines) + "\n"
 

@@ -188,6 +188,10 @@ static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
     StageEpi e = ep;
     e.first = (d == 0);
     e.last = (d == nd - 1);
+    if (ep.mode == EPI_RK && s->cons_on) {
+      e.bnd = s->d_bnd + s->bnd_off[d];
+      e.bw = ep.cb;
+    }
     int pr = prof_begin(s, GB_PROF_HYP_X + d);
     CK(launch_hyp(s, d, U, e));
     prof_end(s, pr);
@@ -395,6 +399,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_snap);
   cudaFree(s->d_red);
   cudaFree(s->d_grav);
+  cudaFree(s->d_bnd);
   prof_drain(s);
   for (cudaEvent_t e : s->pool) cudaEventDestroy(e);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
@@ -606,6 +611,8 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
   CK(cudaMemcpyAsync(save, s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
   double t0 = s->t;
   bool prof_was = s->prof;
+  const bool cons_was = s->cons_on;  // the trial steps add no boundary fluxes
+  s->cons_on = false;
   const gb_config& c = s->cfg;
   int rc = GB_OK;
   for (int d = 0; d < c.ndims && !rc; d++) {
@@ -668,6 +675,7 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
   CK(cudaFreeAsync(save, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   s->t = t0;
+  s->cons_on = cons_was;
   return rc;
 }
 

@@ -517,6 +517,7 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
     if (CC) Ecc = roe_eig<M, DIR>(axL.rs, axR.rs, pp);
     double fI[NV];
     upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, axL, axR, pp, fI);
+    boundary_flux<NV>(ep, I, N, line, ntrans, fI);
     if (I > I0) {
       const int c = I - 1;
       const long long off = (pbase + (long long)c * sd) * NV;

@@ -58,6 +58,13 @@ struct gb_ensemble {
   double* d_dx = nullptr;
   MemberDev* d_mem = nullptr;
   cudaGraphExec_t gexec = nullptr;
+  // conservation check: boundary-flux accumulators of every member (MemberDev
+  // bnd_off), the members' initial volume integrals, a reduction buffer
+  double* d_bnd = nullptr;
+  long long bnd_n = 0;
+  bool cons_on = false;
+  std::vector<double> V0;
+  double* d_red = nullptr;
   bool graph_dirty = true;
   bool use_graph = true;
   double t = 0.0;
@@ -139,6 +146,10 @@ static int step_launches(gb_ensemble* e) {
       StageEpi x = ep;
       x.first = (d == 0);
       x.last = (d == c.ndims - 1);
+      if (e->cons_on) {
+        x.bnd = e->d_bnd;  // each member's block at its bnd_off
+        x.bw = ep.cb;
+      }
       CK(launch_dir(e, d, U, x));
     }
     for (int t = st + 1; t < ns; t++)
@@ -263,6 +274,8 @@ extern "C" void gb_ensemble_destroy(gb_ensemble* e) {
   cudaFree(e->d_H);
   cudaFree(e->d_dx);
   cudaFree(e->d_mem);
+  cudaFree(e->d_bnd);
+  cudaFree(e->d_red);
   if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -416,6 +429,9 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
   CK(cudaMallocAsync((void**)&save, bytes, e->stream));
   CK(cudaMemcpyAsync(save, e->d_u, bytes, cudaMemcpyDeviceToDevice, e->stream));
   double t0 = e->t;
+  const bool cons_was = e->cons_on;  // the trial steps add no boundary fluxes
+  e->cons_on = false;
+  e->graph_dirty = true;
   cudaEvent_t a, b;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
@@ -459,5 +475,56 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
   CK(cudaFreeAsync(save, e->stream));
   CK(cudaStreamSynchronize(e->stream));
   e->t = t0;
+  e->cons_on = cons_was;
+  e->graph_dirty = true;
   return rc;
+}
+
+extern "C" int gb_ensemble_conservation_begin(gb_ensemble* e) {
+  if (!e) { gbh_set_error("gb_ensemble_conservation_begin: null ensemble"); return GB_ERR_ARG; }
+  if (!e->d_bnd) {
+    long long n = 0;
+    for (int m = 0; m < e->nm; m++)
+      for (int d = 0; d < e->cfg[m].ndims; d++) {
+        e->mem[m].bnd_off[d] = n;
+        n += 2 * cons_lines(e->cfg[m], d) * e->cfg[m].nvars;
+      }
+    e->bnd_n = n;
+    CK(cudaMalloc((void**)&e->d_bnd, n * sizeof(double)));
+    CK(cudaMalloc((void**)&e->d_red, CONS_RED_DOUBLES * sizeof(double)));
+    int rc = upload_table(e);
+    if (rc) return rc;
+  }
+  CK(cudaMemsetAsync(e->d_bnd, 0, e->bnd_n * sizeof(double), e->stream));
+  e->V0.assign((size_t)e->nm * 5, 0.0);
+  for (int m = 0; m < e->nm; m++) {
+    const MemberDev& md = e->mem[m];
+    const int nd = e->cfg[m].ndims;
+    int rc = cons_volume(e->d_u + md.off, e->d_dx + md.dx_off[0], md.G, nd > 1 ? md.dx_off[1] - md.dx_off[0] : 0,
+                         nd > 2 ? md.dx_off[2] - md.dx_off[0] : 0, e->cfg[m].nvars, e->d_red, e->stream,
+                         &e->V0[(size_t)m * 5]);
+    if (rc) return rc;
+  }
+  e->cons_on = true;
+  e->graph_dirty = true;
+  return GB_OK;
+}
+
+extern "C" int gb_ensemble_conservation_error(gb_ensemble* e, int member, double* err) {
+  if (!e || !err || member < 0 || member >= e->nm) {
+    gbh_set_error("gb_ensemble_conservation_error: bad argument");
+    return GB_ERR_ARG;
+  }
+  if (!e->cons_on) { gbh_set_error("gb_ensemble_conservation_error: no gb_ensemble_conservation_begin"); return GB_ERR_ARG; }
+  const MemberDev& md = e->mem[member];
+  const gb_config& c = e->cfg[member];
+  double V[5];
+  int rc = cons_volume(e->d_u + md.off, e->d_dx + md.dx_off[0], md.G, c.ndims > 1 ? md.dx_off[1] - md.dx_off[0] : 0,
+                       c.ndims > 2 ? md.dx_off[2] - md.dx_off[0] : 0, c.nvars, e->d_red, e->stream, V);
+  if (rc) return rc;
+  double mid[3] = {1.0, 1.0, 1.0};
+  for (int k = 0; k < c.ndims; k++)
+    CK(cudaMemcpyAsync(&mid[k], e->d_dx + md.dx_off[k] + c.ghosts + c.dim[k] / 2, sizeof(double),
+                       cudaMemcpyDeviceToHost, e->stream));
+  return cons_error(c, e->d_bnd, md.bnd_off, V, &e->V0[(size_t)member * 5], mid, e->d_red, e->stream, err);
 }

@@ -281,6 +281,19 @@ __device__ __forceinline__ void wpair(const double* w, const double* v, double e
   else weno5_pair(w, v, eps4, oL, oR);
 }
 
+// The conservation check's boundary fluxes: the flux leaving through face 0
+// (-F at interface 0) and face N (+F at interface N) of grid line `line`, times the
+// stage's dt b_s, added into that line's accumulators (one thread owns each).
+template <int NV>
+__device__ __forceinline__ void boundary_flux(const StageEpi& ep, int I, int N, long long line, long long ntrans,
+                                              const double* fI) {
+  if (!ep.bnd || (I != 0 && I != N)) return;
+  double* b = ep.bnd + ((I == N ? ntrans : 0) + line) * NV;
+  const double w = I == N ? ep.bw : -ep.bw;
+#pragma unroll
+  for (int v = 0; v < NV; v++) b[v] = fma(w, fI[v], b[v]);
+}
+
 // The upwind flux of one interface from the six-cell window (cells j-3 .. j+2 of
 // interface j-1/2): the fused kernel's WENO5 reconstructions (component-wise or
 // characteristic) and upwinding, with the gravity source function's interface value SI
@@ -519,6 +532,13 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
     double fI[NV];
     iface_flux<M, CHAR, UPW, DIR, ALTW, GRAV, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, src_dir,
                                                    line * (N + 1) + I, fI, SI);
+    if (ep.bnd && (I == 0 || I == N)) {
+      long long ntr = 1;
+#pragma unroll
+      for (int e = 0; e < ND; e++)
+        if (e != DIR) ntr *= G.dim[e];
+      boundary_flux<NV>(ep, I, N, line, ntr, fI);
+    }
 
     if (I > I0) {
       // Flux difference of cell I-1 and the stage epilogue.
@@ -688,6 +708,7 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
     double fI[NV], SI[NV];
     iface_flux<M, CHAR, UPW, DIR, ALTW, false, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, false,
                                                    line * (N + 1) + I, fI, SI);
+    boundary_flux<NV>(ep, I, N, line, ntrans, fI);
 #pragma unroll
     for (int v = 0; v < NV; v++) sfI[t][v] = fI[v];
   }
@@ -743,6 +764,7 @@ __device__ __forceinline__ const MemberDev& batched_member(const MemberDev* __re
 #pragma unroll
   for (int t = 0; t < 4; t++)
     if (e.P[t]) e.P[t] += o;
+  if (e.bnd) e.bnd += m.bnd_off[DIR];
   return m;
 }
 

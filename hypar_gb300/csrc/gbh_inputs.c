@@ -122,7 +122,7 @@ typedef struct {
   double dt;
   char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
   char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
-  char op_overwrite[MAXS], hyp_flux_split[MAXS];
+  char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS];
 } solver_inp;
 
 static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsims) {
@@ -144,6 +144,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   strcpy(si->op_overwrite, "no");
   strcpy(si->model, "none");
   strcpy(si->hyp_flux_split, "no");
+  strcpy(si->cons_check, "no");
   FILE *in = open_in(dir, "solver.inp", "r");
   if (!in) {
     gbh_set_error("file solver.inp not found");
@@ -192,12 +193,13 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
     else if (!strcmp(w, "ip_file_type")) r = fscanf(in, "%511s", si->ip_file_type);
     else if (!strcmp(w, "op_overwrite")) r = fscanf(in, "%511s", si->op_overwrite);
     else if (!strcmp(w, "model")) r = fscanf(in, "%511s", si->model);
+    else if (!strcmp(w, "conservation_check")) r = fscanf(in, "%511s", si->cons_check);
     else if (!strcmp(w, "input_mode") || !strcmp(w, "output_mode")) {
       char mode[MAXS];
       r = fscanf(in, "%511s", mode);
       if (r == 1 && strcmp(mode, "serial")) { int nio; r = fscanf(in, "%d", &nio); }
     } else {
-      char useless[MAXS];  /* every other keyword takes one value (conservation_check, ...) */
+      char useless[MAXS];  /* every other keyword takes one value */
       r = fscanf(in, "%511s", useless);
     }
     if (r != 1) ok = 0;
@@ -534,6 +536,7 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   c.file_op_iter = si.file_op_iter;
   c.restart_iter = si.restart_iter;
   c.screen_op_iter = si.screen_op_iter > 0 ? si.screen_op_iter : 1;
+  c.cons_check = !strcmp(si.cons_check, "yes");  /* ReadInputs.c:323: "yes" turns it on */
   c.write_residual = 0;  /* the reference reads no keyword for it either (ReadInputs.c:125) */
 
   /* physics.inp */

@@ -62,6 +62,11 @@ struct StageEpi {
   // EPI_HYP only: also subtract the gravity source (NavierStokes3D with gravity),
   // so that the hyperbolic term with and without it give the source by difference.
   int with_source;
+  // Conservation check (EPI_RK): when set, the interface flux at I = 0 and I = N of
+  // every line is accumulated here, times -bw and +bw: ntrans x nvars values for
+  // face 0, then as many for face N (HyperbolicFunction.c:101-106, TimeRK.c:188-192).
+  double* bnd;
+  double bw;
 };
 
 // NavierStokes3D viscous-term constants (NavierStokes3DParabolicFunction.c:76-79).
@@ -85,7 +90,16 @@ struct MemberDev {
   long long start[3];    // first thread of the member per direction
   long long ntrans[3];
   int nseg[3], seg[3];
+  long long bnd_off[3];  // the member's conservation-check accumulators per direction
 };
+
+// Conservation check reductions (gbh_monitor.cu).
+long long cons_lines(const gb_config& c, int d);
+int cons_volume(const double* u, const double* dxinv, const DevGeom& G, long long dxo1, long long dxo2, int nv,
+                double* red, cudaStream_t st, double* V);
+int cons_error(const gb_config& c, const double* bnd, const long long* off, const double* V, const double* V0,
+               const double* dxmid, double* red, cudaStream_t st, double* err);
+constexpr int CONS_RED_DOUBLES = 3 * 1024;  // the reduction buffer cons_volume / cons_error need
 
 }  // namespace gbh
 

@@ -8,6 +8,10 @@
 //     the interior (TimePostStep.c:38-60);
 //   * the relative L1 / L2 / Linf errors against an exact solution
 //     (CalculateError.c:27-110).
+//   * the conservation check: the volume integral sum u dV (VolumeIntegral.c) and
+//     the sums over the grid lines of the boundary-flux time integrals that the
+//     fused kernels accumulate per line (BoundaryIntegral.c,
+//     CalculateConservationError.c).
 // Sums are reduced in two passes in a fixed order (per-block partials, then
 // one block), so every result is deterministic.
 #include <cmath>
@@ -116,6 +120,77 @@ __global__ void __launch_bounds__(RED_BLOCK) finish_kernel(double* partials, int
   }
   __syncthreads();  // every thread has read its partials before block 0's slot is overwritten
   block_reduce3(a, b, c, partials);
+}
+
+// Block sums of NV values per thread into out[NV * blockIdx.x + v].
+template <int NV>
+__device__ void block_reduce_n(const double* x, double* out) {
+  __shared__ double sm[NV][RED_BLOCK];
+#pragma unroll
+  for (int v = 0; v < NV; v++) sm[v][threadIdx.x] = x[v];
+  __syncthreads();
+  for (int w = RED_BLOCK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int v = 0; v < NV; v++) sm[v][threadIdx.x] += sm[v][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int v = 0; v < NV; v++) out[NV * blockIdx.x + v] = sm[v][0];
+}
+
+// Volume integral partials: sum over the interior of u dV, dV = prod_d 1/dxinv_d
+// (VolumeIntegral.c: dV *= 1/dxinv per dimension, then u dV).
+template <int NV>
+__global__ void __launch_bounds__(RED_BLOCK) volume_kernel(const double* __restrict__ u,
+                                                           const double* __restrict__ dxinv, DevGeom G,
+                                                           long long dxo1, long long dxo2, double* partials) {
+  const long long n = (long long)G.dim[0] * G.dim[1] * G.dim[2];
+  const long long off[3] = {0, dxo1, dxo2};
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) acc[v] = 0.0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    int idx[3];
+    const long long q = interior_point(G, p, idx) * NV;
+    double dV = 1.0;
+    for (int d = 0; d < G.nd; d++) dV = __dmul_rn(dV, __ddiv_rn(1.0, dxinv[off[d] + idx[d] + G.g]));
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] += __dmul_rn(u[q + v], dV);
+  }
+  block_reduce_n<NV>(acc, partials);
+}
+
+// Second pass of volume_kernel: one block folds the partials in index order.
+template <int NV>
+__global__ void __launch_bounds__(RED_BLOCK) volume_finish_kernel(double* partials, int nblocks) {
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) acc[v] = 0.0;
+  for (int i = threadIdx.x; i < nblocks; i += RED_BLOCK)
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] += partials[NV * i + v];
+  __syncthreads();  // all partials read before block 0's slot is overwritten
+  block_reduce_n<NV>(acc, partials);
+}
+
+// Boundary-flux integrals: block b = 2 d + face sums its face's lines
+// (bnd + off[d] + face * nlines[d] * NV) into out[NV * b + v].
+template <int NV>
+__global__ void __launch_bounds__(RED_BLOCK) boundary_sum_kernel(const double* __restrict__ bnd, long long off0,
+                                                                 long long off1, long long off2, long long n0,
+                                                                 long long n1, long long n2, double* out) {
+  const int d = blockIdx.x / 2, face = blockIdx.x % 2;
+  const long long nl = d == 0 ? n0 : (d == 1 ? n1 : n2);
+  const double* b = bnd + (d == 0 ? off0 : (d == 1 ? off1 : off2)) + (long long)face * nl * NV;
+  double acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) acc[v] = 0.0;
+  for (long long l = threadIdx.x; l < nl; l += RED_BLOCK)
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] += b[l * NV + v];
+  block_reduce_n<NV>(acc, out);
 }
 
 }  // namespace gbh
@@ -256,4 +331,117 @@ extern "C" int gb_solver_error(gb_solver* s, const double* uex, int layout, int 
     err[2] /= nrm[2];
   }
   return GB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Conservation check (shared by the solver and the ensemble)
+// ---------------------------------------------------------------------------
+namespace gbh {
+
+long long cons_lines(const gb_config& c, int d) {
+  long long n = 1;
+  for (int e = 0; e < c.ndims; e++)
+    if (e != d) n *= c.dim[e];
+  return n;
+}
+
+// sum u dV over the interior of one grid, per variable; `red` holds
+// 3 * RED_MAX_BLOCKS doubles (synchronises `st`).
+int cons_volume(const double* u, const double* dxinv, const DevGeom& G, long long dxo1, long long dxo2, int nv,
+                double* red, cudaStream_t st, double* V) {
+  long long n = (long long)G.dim[0] * G.dim[1] * G.dim[2];
+  long long b = (n + RED_BLOCK - 1) / RED_BLOCK;
+  // at most RED_MAX_BLOCKS / 2 blocks: their nv <= 5 partials fit the buffer
+  const int nb = (int)(b < RED_MAX_BLOCKS / 2 ? (b < 1 ? 1 : b) : RED_MAX_BLOCKS / 2);
+  if (nv == 3) {
+    volume_kernel<3><<<nb, RED_BLOCK, 0, st>>>(u, dxinv, G, dxo1, dxo2, red);
+    volume_finish_kernel<3><<<1, RED_BLOCK, 0, st>>>(red, nb);
+  } else if (nv == 4) {
+    volume_kernel<4><<<nb, RED_BLOCK, 0, st>>>(u, dxinv, G, dxo1, dxo2, red);
+    volume_finish_kernel<4><<<1, RED_BLOCK, 0, st>>>(red, nb);
+  } else {
+    volume_kernel<5><<<nb, RED_BLOCK, 0, st>>>(u, dxinv, G, dxo1, dxo2, red);
+    volume_finish_kernel<5><<<1, RED_BLOCK, 0, st>>>(red, nb);
+  }
+  MK(cudaGetLastError());
+  MK(cudaMemcpyAsync(V, red, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MK(cudaStreamSynchronize(st));
+  return GB_OK;
+}
+
+// The conservation error per variable, |V + B - V0| / max(|V0|, 1), with B the
+// boundary-flux time integrals of the accumulators `bnd` (per direction d at
+// off[d]: face 0 then face N, lines x nv) summed over lines and times the face
+// areas dS_d = prod_{k != d} 1 / dxinv_k at the middle of dimension k
+// (BoundaryIntegral.c; CalculateConservationError.c).  `dxmid[k]` is that dxinv.
+int cons_error(const gb_config& c, const double* bnd, const long long* off, const double* V, const double* V0,
+               const double* dxmid, double* red, cudaStream_t st, double* err) {
+  const int nv = c.nvars;
+  const long long n0 = cons_lines(c, 0), n1 = c.ndims > 1 ? cons_lines(c, 1) : 0,
+                  n2 = c.ndims > 2 ? cons_lines(c, 2) : 0;
+  const long long o1 = c.ndims > 1 ? off[1] : 0, o2 = c.ndims > 2 ? off[2] : 0;
+  const int nblk = 2 * c.ndims;
+  if (nv == 3)
+    boundary_sum_kernel<3><<<nblk, RED_BLOCK, 0, st>>>(bnd, off[0], o1, o2, n0, n1, n2, red);
+  else if (nv == 4)
+    boundary_sum_kernel<4><<<nblk, RED_BLOCK, 0, st>>>(bnd, off[0], o1, o2, n0, n1, n2, red);
+  else
+    boundary_sum_kernel<5><<<nblk, RED_BLOCK, 0, st>>>(bnd, off[0], o1, o2, n0, n1, n2, red);
+  MK(cudaGetLastError());
+  double F[6 * 5];
+  MK(cudaMemcpyAsync(F, red, nblk * nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+  MK(cudaStreamSynchronize(st));
+  double B[5] = {0, 0, 0, 0, 0};
+  for (int d = 0; d < c.ndims; d++) {
+    double dS = 1.0;
+    for (int k = 0; k < c.ndims; k++)
+      if (k != d) dS *= (1.0 / dxmid[k]);
+    for (int v = 0; v < nv; v++) {
+      B[v] += F[(2 * d + 0) * nv + v] * dS;
+      B[v] += F[(2 * d + 1) * nv + v] * dS;
+    }
+  }
+  for (int v = 0; v < nv; v++) {
+    const double base = std::fabs(V0[v]) > 1.0 ? std::fabs(V0[v]) : 1.0;
+    const double e = V[v] + B[v] - V0[v];
+    err[v] = std::sqrt(e * e) / base;
+  }
+  return GB_OK;
+}
+
+}  // namespace gbh
+
+extern "C" int gb_solver_conservation_begin(gb_solver* s) {
+  if (!s) { gbh_set_error("gb_solver_conservation_begin: null solver"); return GB_ERR_ARG; }
+  const gb_config& c = s->cfg;
+  int rc = red_buffer(s);
+  if (rc) return rc;
+  if (!s->d_bnd) {
+    long long n = 0;
+    for (int d = 0; d < c.ndims; d++) {
+      s->bnd_off[d] = n;
+      n += 2 * cons_lines(c, d) * c.nvars;
+    }
+    s->bnd_n = n;
+    MK(cudaMalloc((void**)&s->d_bnd, n * sizeof(double)));
+  }
+  MK(cudaMemsetAsync(s->d_bnd, 0, s->bnd_n * sizeof(double), s->stream));
+  rc = cons_volume(s->d_u, s->d_dxinv, s->G, s->dx_off[1], s->dx_off[2], c.nvars, s->d_red, s->stream, s->V0);
+  if (rc) return rc;
+  s->cons_on = true;
+  return GB_OK;
+}
+
+extern "C" int gb_solver_conservation_error(gb_solver* s, double* err) {
+  if (!s || !err) { gbh_set_error("gb_solver_conservation_error: null argument"); return GB_ERR_ARG; }
+  if (!s->cons_on) { gbh_set_error("gb_solver_conservation_error: no gb_solver_conservation_begin"); return GB_ERR_ARG; }
+  const gb_config& c = s->cfg;
+  double V[5];
+  int rc = cons_volume(s->d_u, s->d_dxinv, s->G, s->dx_off[1], s->dx_off[2], c.nvars, s->d_red, s->stream, V);
+  if (rc) return rc;
+  double mid[3] = {1.0, 1.0, 1.0};
+  for (int k = 0; k < c.ndims; k++)
+    MK(cudaMemcpyAsync(&mid[k], s->d_dxinv + s->dx_off[k] + c.ghosts + c.dim[k] / 2, sizeof(double),
+                       cudaMemcpyDeviceToHost, s->stream));
+  return cons_error(c, s->d_bnd, s->bnd_off, V, s->V0, mid, s->d_red, s->stream, err);
 }

@@ -8,6 +8,7 @@
  * (src/Simulation/OutputSolution.cpp:50-140).
  */
 #define _POSIX_C_SOURCE 200809L /* clock_gettime */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -47,6 +48,41 @@ static int write_errors(const char *dir, const gb_config *c, const double *err, 
   return GB_OK;
 }
 
+/* SimulationWriteErrors.c:82-99: conservation<_k>.dat (sizes, iproc, dt, the
+   conservation error per variable, -1 without conservation_check) and
+   function_counts<_k>.dat (n_iter and the calls of the hyperbolic, parabolic and
+   source functions). */
+static int write_counts(const char *dir, const char *suffix, const gb_config *c, const double *cons, int nsteps) {
+  char path[4400];
+  const char *names[2] = {"conservation", "function_counts"};
+  for (int f = 0; f < 2; f++) {
+    if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s%s.dat", dir, names[f], suffix);
+    else snprintf(path, sizeof(path), "%s%s.dat", names[f], suffix);
+    FILE *out = fopen(path, "w");
+    if (!out) {
+      gbh_set_error("could not open %s for writing", path);
+      return GB_ERR_INPUT;
+    }
+    if (f == 0) {
+      for (int d = 0; d < c->ndims; d++) fprintf(out, "%4d ", c->dim[d]);
+      for (int d = 0; d < c->ndims; d++) fprintf(out, "%4d ", 1);
+      fprintf(out, "%1.16E  ", c->dt);
+      for (int v = 0; v < c->nvars; v++) fprintf(out, "%1.16E ", cons ? cons[v] : -1.0);
+      fprintf(out, "\n");
+    } else {
+      /* one hyperbolic term per stage; the parabolic one counts when it is not zero
+         (NavierStokes3DParabolicFunction.c:72, Re > 0), the source one when the model
+         has a source function (Euler1D, NavierStokes3D: SourceFunction.c:47) */
+      const int calls = nsteps * c->rk_nstages;
+      const int par = (c->model == GB_MODEL_NS3D && c->Re > 0.0) ? calls : 0;
+      const int sou = (c->model == GB_MODEL_EULER1D || c->model == GB_MODEL_NS3D) ? calls : 0;
+      fprintf(out, "%d\n%d\n%d\n%d\n", c->n_iter, calls, par, sou);
+    }
+    fclose(out);
+  }
+  return GB_OK;
+}
+
 static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
   gb_inputs **in = (gb_inputs **)calloc(nsims, sizeof(gb_inputs *));
   gb_config *cf = (gb_config *)calloc(nsims, sizeof(gb_config));
@@ -68,6 +104,7 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
     if (n > nmax) nmax = n;
     rc = gb_ensemble_set_state(e, m, gb_inputs_u0(in[m]), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
   }
+  if (!rc && cf[0].cons_check) rc = gb_ensemble_conservation_begin(e);
   double *buf = (double *)malloc(sizeof(double) * (nmax > 0 ? nmax : 1));
   int overwrite = !rc && !strcmp(gbh_inputs_op_overwrite(in[0]), "yes");
   int every = cf[0].file_op_iter > 0 ? cf[0].file_op_iter : cf[0].n_iter;
@@ -76,6 +113,8 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
   int k = 0;
   char name[160], path[4400];
   if (width > 9) width = 9;
+  struct timespec t0, t1;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
   for (int it = 0; !rc && it <= cf[0].n_iter;) {
     int write = (!overwrite && (it % every == 0 || it == cf[0].n_iter)) || (overwrite && it == cf[0].n_iter);
     for (int m = 0; write && m < nsims && !rc; m++) {
@@ -95,6 +134,34 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
     if (!rc && verbose) printf("gbhypar: ensemble of %d, iteration %d / %d\n", nsims, it, cf[0].n_iter);
   }
   if (!rc) rc = gb_ensemble_sync(e);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  const double runtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
+  /* per member: errors_<k>.dat (no exact solution: -1), conservation_<k>.dat,
+     function_counts_<k>.dat */
+  for (int m = 0; m < nsims && !rc; m++) {
+    char suffix[32];
+    snprintf(suffix, sizeof(suffix), "_%0*d", width, m);
+    double cons[5];
+    if (cf[m].cons_check) rc = gb_ensemble_conservation_error(e, m, cons);
+    if (!rc) rc = write_counts(dir, suffix, &cf[m], cf[m].cons_check ? cons : NULL, cf[m].n_iter);
+    if (!rc) {
+      char path[4400];
+      if (dir && dir[0]) snprintf(path, sizeof(path), "%s/errors%s.dat", dir, suffix);
+      else snprintf(path, sizeof(path), "errors%s.dat", suffix);
+      FILE *out = fopen(path, "w");
+      if (!out) {
+        gbh_set_error("could not open %s for writing", path);
+        rc = GB_ERR_INPUT;
+        break;
+      }
+      for (int d = 0; d < cf[m].ndims; d++) fprintf(out, "%4d ", cf[m].dim[d]);
+      for (int d = 0; d < cf[m].ndims; d++) fprintf(out, "%4d ", 1);
+      fprintf(out, "%1.16E  ", cf[m].dt);
+      fprintf(out, "%1.16E %1.16E %1.16E   ", -1.0, -1.0, -1.0);
+      fprintf(out, "%1.16E %1.16E\n", runtime, runtime);
+      fclose(out);
+    }
+  }
   free(buf);
   gb_ensemble_destroy(e);
   for (int m = 0; m < nsims; m++) gb_inputs_free(in[m]);
@@ -126,6 +193,8 @@ int gb_run_case(const char *dir, int device, int verbose) {
   double *buf = (double *)malloc(sizeof(double) * n);
   rc = gb_solver_set_state(s, gb_inputs_u0(in), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
   if (!rc && gb_inputs_gravity_field(in)) rc = gb_solver_set_gravity_field(s, gb_inputs_gravity_field(in));
+  /* InitialSolution.c:118: the volume integral of the initial solution */
+  if (!rc && c->cons_check) rc = gb_solver_conservation_begin(s);
   const int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");
   const int every = c->file_op_iter > 0 ? c->file_op_iter : c->n_iter;
   const int screen = c->screen_op_iter > 0 ? c->screen_op_iter : 1;
@@ -169,9 +238,19 @@ int gb_run_case(const char *dir, int device, int verbose) {
     it = target;
     if (rc) break;
     if (report) {
-      if (verbose)
-        printf("iter=%7d  t=%1.3E  CFL=%1.3E  norm=%1.4E  wctime: %1.1E (s)  \n", it, gb_solver_time(s), cfl,
-               norm, wc);
+      /* TimePrintStep.c:30-56, with the conservation error when it is checked */
+      double cons[5], ce = 0.0;
+      if (c->cons_check) {
+        rc = gb_solver_conservation_error(s, cons);
+        if (rc) break;
+        for (int v = 0; v < c->nvars; v++) ce += cons[v] * cons[v];
+        ce = sqrt(ce);
+      }
+      if (verbose) {
+        printf("iter=%7d  t=%1.3E  CFL=%1.3E  norm=%1.4E  wctime: %1.1E (s)  ", it, gb_solver_time(s), cfl, norm, wc);
+        if (c->cons_check) printf("  cons_err=%1.4E\n", ce);
+        else printf("\n");
+      }
       if (resid) fprintf(resid, "%10d\t%E\t%E\n", it, gb_solver_time(s), norm);
     }
     if (!overwrite && it % every == 0 && it < c->n_iter) {
@@ -207,6 +286,13 @@ int gb_run_case(const char *dir, int device, int verbose) {
       printf("  L1         Error           : %1.16E\n", err[0]);
       printf("  L2         Error           : %1.16E\n", err[1]);
       printf("  Linfinity  Error           : %1.16E\n", err[2]);
+    }
+    double cons[5];
+    if (!rc && c->cons_check) rc = gb_solver_conservation_error(s, cons);
+    if (!rc) rc = write_counts(dir, "", c, c->cons_check ? cons : NULL, c->n_iter - R);
+    if (!rc && verbose && c->cons_check) {
+      printf("Conservation Errors:\n");
+      for (int v = 0; v < c->nvars; v++) printf("\t%1.16E\n", cons[v]);
     }
   }
   free(buf);

@@ -31,6 +31,13 @@ struct gb_solver {
   double* d_crC = nullptr;   // CRWENO5: normalised super-diagonal of the elimination
   double* d_crF = nullptr;   // CRWENO5 (component-wise): cell fluxes of the current direction
   bool gravity = false;
+  // conservation check: per direction and face, the lines' boundary-flux time
+  // integrals (allocated by gb_solver_conservation_begin)
+  double* d_bnd = nullptr;
+  long long bnd_off[3] = {0, 0, 0};
+  long long bnd_n = 0;
+  bool cons_on = false;
+  double V0[5] = {0, 0, 0, 0, 0};
   int* d_flag = nullptr;
   std::vector<int> mem_zones;  // zone indices applied in memory before each RHS
   gbh::HypLaunch hl[3];

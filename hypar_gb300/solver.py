@@ -212,6 +212,17 @@ class Solver:
         check(lib().gb_solver_error(self._h, _ptr(uex), layout, mem, err))
         return tuple(err)
 
+    def conservation_begin(self):
+        """Start the conservation check from the current state (volume integral V0,
+        boundary-flux integrals cleared)."""
+        check(lib().gb_solver_conservation_begin(self._h))
+
+    def conservation_error(self) -> np.ndarray:
+        """|V + B - V0| / max(|V0|, 1) per variable (CalculateConservationError)."""
+        err = (ctypes.c_double * self.config.nvars)()
+        check(lib().gb_solver_conservation_error(self._h, err))
+        return np.array(err[:])
+
     def check_finite(self) -> bool:
         f = ctypes.c_int()
         check(lib().gb_solver_check_finite(self._h, ctypes.byref(f)))
@@ -365,6 +376,14 @@ class Ensemble:
     def autotune(self, reps: int = 2):
         check(lib().gb_ensemble_autotune(self._h, int(reps)))
         return [self.get_launch(d) for d in range(self.configs[0].ndims)]
+
+    def conservation_begin(self):
+        check(lib().gb_ensemble_conservation_begin(self._h))
+
+    def conservation_error(self, m: int) -> np.ndarray:
+        err = (ctypes.c_double * self.configs[m].nvars)()
+        check(lib().gb_ensemble_conservation_error(self._h, int(m), err))
+        return np.array(err[:])
 
     @property
     def time(self) -> float:

@@ -94,6 +94,9 @@ typedef struct gb_config {
    * (Euler1DInitialize.c:144); the field comes through gb_solver_set_gravity_field as
    * 1/S then S */
   int grav_type;
+  /* solver.inp conservation_check yes: the driver reports the conservation error
+   * (gb_solver_conservation_*) */
+  int cons_check;
 } gb_config;
 
 typedef struct gb_solver gb_solver;
@@ -173,6 +176,16 @@ int gb_solver_set_time(gb_solver *s, double t);
 int gb_solver_cfl(gb_solver *s, double *cfl);
 int gb_solver_step_report(gb_solver *s, int nsteps, double *cfl, double *norm);
 int gb_solver_error(gb_solver *s, const double *uex, int layout, int mem, double *err);
+/* The conservation check (solver.inp conservation_check; TimePostStep.c:78-92).
+ * _begin records the volume integral sum u dV of the current state
+ * (VolumeIntegral.c; InitialSolution.c:118) and from then on every step adds, per
+ * grid line and boundary face, dt b_s times the interface flux of the hyperbolic
+ * term leaving the domain (HyperbolicFunction.c:101-106, TimeRK.c:174-192).
+ * _error writes, per variable, |V + B - V0| / max(|V0|, 1) with V the volume
+ * integral now and B the time integral of the boundary fluxes times the faces'
+ * areas (BoundaryIntegral.c, CalculateConservationError.c). */
+int gb_solver_conservation_begin(gb_solver *s);
+int gb_solver_conservation_error(gb_solver *s, double *err);
 /* Launch shape of the fused kernels: interfaces walked per thread (seg) and
  * threads per block, per direction (values <= 0 keep the current ones); seg = -32,
  * -64 or -128 selects shared-memory tiles of that many interfaces per block (one
@@ -220,6 +233,9 @@ int gb_ensemble_get_launch(gb_ensemble *e, int dir, int *seg, int *block);
 /* Choose seg/block (walker or tiles) per direction by timing graph-replayed steps
  * (state restored). */
 int gb_ensemble_autotune(gb_ensemble *e, int reps);
+/* The conservation check of every member (as gb_solver_conservation_*). */
+int gb_ensemble_conservation_begin(gb_ensemble *e);
+int gb_ensemble_conservation_error(gb_ensemble *e, int member, double *err);
 
 /* Read the deck in `dir`, run n_iter steps on the GPU and write op.bin (and
  * op_NNNNN.bin every file_op_iter steps when op_overwrite is "no") in HyPar's

@@ -125,7 +125,27 @@ CASES = {
     "strat64_grav1_llf_comp_mapped": lambda: _w(C.stratified_1d(64, n_iter=10, grav_type=1, upwinding="llf-char",
                                                                  g=2.0), "mapped"),
     "sod64_grav_roe_comp": lambda: _g1(C.sod(64, n_iter=20, dt=1e-3), 1.0),
+    # the conservation check (solver.inp conservation_check yes): boundary fluxes through
+    # extrapolate / wall / inflow faces, a source (gravity), the viscous term
+    "sod64_cons_comp_roe": lambda: _cons(C.sod(64, n_iter=20, dt=1e-3)),
+    "sod64_cons_crweno_char_llf": lambda: _cons(_cr(C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                                         upwinding="llf-char"))),
+    "strat64_cons_grav1_roe_char": lambda: _cons(C.stratified_1d(64, n_iter=10, grav_type=1,
+                                                                 interp="characteristic")),
+    "vortex24_cons_comp_roe_subsonic_io": lambda: _cons(_b(C.vortex(24, n_iter=5, dt=0.02, interp="components"), {
+        (0, 1): ("subsonic-inflow", [1.0, 0.5, 0.0]), (0, -1): ("subsonic-outflow", [1.0])})),
+    "vortex24_cons_char_roe_slipwall": lambda: _cons(_b(C.vortex(24, n_iter=5, dt=0.02), {
+        (1, 1): ("slip-wall", [0.0, 0.0]), (1, -1): ("slip-wall", [0.0, 0.0])})),
+    "tgv12_cons_comp_roe_noslip": lambda: _cons(_b(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), {
+        (2, 1): ("noslip-wall", [0.0, 0.0, 0.0]), (2, -1): ("noslip-wall", [0.0, 0.0, 0.0])})),
+    "rtb12_cons_comp_rusanov_yc": lambda: _cons(C.rising_thermal_bubble(12, n_iter=3, dt=0.05, perturb=0.02)),
 }
+
+
+def _cons(case):
+    """The deck with solver.inp conservation_check yes."""
+    case.conservation_check = True
+    return case
 
 
 def _g1(case, g):
@@ -190,9 +210,13 @@ def main() -> None:
             dump = O.read_harness_dump(os.path.join(d, "dump.bin"))
             subprocess.check_call([os.path.join(O.REF_DIR, "HyPar")], cwd=d, stdout=subprocess.DEVNULL, env=env)
             op = C.read_op_bin(os.path.join(d, "op.bin"))
+            # conservation.dat: sizes, iproc, dt, then the conservation error per variable
+            cons = np.array(open(os.path.join(d, "conservation.dat")).read().split()[2 * case.ndims + 1:],
+                            dtype=np.float64)
+            counts = np.array(open(os.path.join(d, "function_counts.dat")).read().split()[:4], dtype=np.int64)
         rhs = O.interior(dump["rhs"], case.size, case.nvars, 3)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), u0=case.u, rhs=rhs, uN=op["u"],
-                            n_iter=case.n_iter, dt=case.dt, cfl=dump["cfl"])
+                            n_iter=case.n_iter, dt=case.dt, cfl=dump["cfl"], cons=cons, counts=counts)
         print(name, rhs.shape, op["u"].shape)
     for name, mk in ENSEMBLES.items():
         if only and name not in only:

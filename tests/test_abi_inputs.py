@@ -156,6 +156,20 @@ def test_reader_restart_screen_and_exact(built_lib, tmp_path):
     assert np.array_equal(got, ex.reshape(-1))
 
 
+def test_reader_conservation_check(built_lib, tmp_path):
+    """solver.inp conservation_check: "yes" turns it on, anything else (or absence) not."""
+    L = _lib.lib()
+    for flag, want in ((True, 1), (False, 0)):
+        case = C.sod(16, n_iter=2, dt=1e-3)
+        case.conservation_check = flag
+        d = str(tmp_path / f"deck{want}")
+        case.write(d)
+        inp_h = ctypes.c_void_p()
+        _lib.check(L.gb_inputs_read(d.encode(), ctypes.byref(inp_h)))
+        assert L.gb_inputs_config(inp_h).contents.cons_check == want
+        L.gb_inputs_free(inp_h)
+
+
 def test_op_to_initial_round_trip(built_lib, tmp_path):
     """gb_write_binary -> gb_op_to_initial -> the deck reader gives back x and u."""
     case = C.vortex(10, n_iter=1, dt=0.01)

@@ -133,3 +133,42 @@ def test_errors_dat(built_lib, tmp_path):
     os.remove(os.path.join(d, "exact.inp"))
     run_case(d)
     assert [float(t) for t in open(os.path.join(d, "errors.dat")).read().split()[5:8]] == [-1.0, -1.0, -1.0]
+
+
+def test_conservation_check_api(built_lib, tmp_path):
+    """gb_solver_conservation_*: a periodic vortex conserves to rounding, an
+    extrapolate-bounded Sod tube once its boundary fluxes are counted; the launch-shape
+    autotuner's trial steps add nothing; the ensemble gives each member's value."""
+    from hypar_gb300.solver import Ensemble
+    vort = C.vortex(32, n_iter=6, dt=0.02)
+    d = str(tmp_path / "v")
+    vort.write(d)
+    s = Solver.from_dir(d)
+    s.conservation_begin()
+    s.autotune(1)
+    s.step(6)
+    ev = s.conservation_error()
+    assert ev.shape == (4,) and np.all(ev < 1e-13), ev
+    sod = C.sod(64, n_iter=30, dt=1e-3)
+    d = str(tmp_path / "s")
+    sod.write(d)
+    s = Solver.from_dir(d)
+    with pytest.raises(RuntimeError):
+        s.conservation_error()  # no begin
+    s.conservation_begin()
+    s.step(30)
+    es = s.conservation_error()
+    assert np.all(es < 1e-13), es
+    members = C.ensemble_vortex(3, sizes=[16, 24, 20], n_iter=4, seed=7)
+    d = str(tmp_path / "e")
+    C.write_ensemble(members, d)
+    e = Ensemble.from_dir(d)
+    e.conservation_begin()
+    e.step(4)
+    for k, m in enumerate(members):
+        sd = str(tmp_path / f"m{k}")
+        m.write(sd)
+        one = Solver.from_dir(sd)
+        one.conservation_begin()
+        one.step(4)
+        assert np.allclose(e.conservation_error(k), one.conservation_error(), rtol=0, atol=1e-14)

@@ -190,6 +190,19 @@ def test_golden_reference(built_lib, tmp_path, name):
     run_case(d)
     op = C.read_op_bin(os.path.join(d, "op.bin"))
     assert relerr(op["u"], g["uN"]) <= STEP_TOL
+    # conservation.dat and function_counts.dat as the reference writes them.  The
+    # conservation error is |V + B - V0| / max(|V0|, 1): at the rounding level of the
+    # volume and boundary integrals (~1e-15 of the largest volume integral) it is noise
+    # in both codes; above it (sources, viscous fluxes at walls) it is compared
+    cons = np.array(open(os.path.join(d, "conservation.dat")).read().split()[2 * case.ndims + 1:], dtype=float)
+    counts = np.array(open(os.path.join(d, "function_counts.dat")).read().split(), dtype=np.int64)
+    assert np.array_equal(counts, g["counts"])
+    if case.conservation_check:
+        dV = float(np.prod([x[1] - x[0] for x in case.x]))
+        floor = 1e-13 + 1e-15 * float(np.max(np.abs(case.u.sum(axis=0)) * dV))
+        assert np.all(np.abs(cons - g["cons"]) <= floor + 1e-6 * np.abs(g["cons"])), (cons, g["cons"], floor)
+    else:
+        assert np.all(cons == -1.0) and np.all(g["cons"] == -1.0)
 
 
 @pytest.mark.parametrize("model,interp,upw", [("euler2d", "characteristic", "roe"),
