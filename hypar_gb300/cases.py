@@ -65,6 +65,7 @@ class Case:
     HB: int = 0
     N_bv: float = 0.0
     conservation_check: bool = False  # solver.inp conservation_check yes
+    op_format: str = "binary"         # solver.inp op_file_format: binary | text | tecplot2d | tecplot3d | none
 
     @property
     def ndims(self) -> int:
@@ -96,7 +97,7 @@ class Case:
             f"  screen_op_iter    {self.screen_op_iter or max(self.n_iter, 1)}",
             f"  file_op_iter      {self.file_op_iter or max(self.n_iter, 1)}",
             "  ip_file_type      binary",
-            "  op_file_format    binary",
+            f"  op_file_format    {self.op_format}",
             f"  op_overwrite      {self.op_overwrite}",
             f"  model             {self.model}",
         ]

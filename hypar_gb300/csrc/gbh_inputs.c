@@ -33,6 +33,7 @@ struct gb_inputs {
   double *uex;    /* exact solution (exact.inp), or NULL */
   double *grav;   /* gravity fields f then g at every point with ghosts, or NULL */
   char op_overwrite[64];
+  char op_format[64];
 };
 
 #define MAXS 512
@@ -122,7 +123,7 @@ typedef struct {
   double dt;
   char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
   char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
-  char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS];
+  char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS], op_format[MAXS];
 } solver_inp;
 
 static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsims) {
@@ -145,6 +146,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   strcpy(si->model, "none");
   strcpy(si->hyp_flux_split, "no");
   strcpy(si->cons_check, "no");
+  strcpy(si->op_format, "text");  /* ReadInputs.c:140 */
   FILE *in = open_in(dir, "solver.inp", "r");
   if (!in) {
     gbh_set_error("file solver.inp not found");
@@ -194,6 +196,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
     else if (!strcmp(w, "op_overwrite")) r = fscanf(in, "%511s", si->op_overwrite);
     else if (!strcmp(w, "model")) r = fscanf(in, "%511s", si->model);
     else if (!strcmp(w, "conservation_check")) r = fscanf(in, "%511s", si->cons_check);
+    else if (!strcmp(w, "op_file_format")) r = fscanf(in, "%511s", si->op_format);
     else if (!strcmp(w, "input_mode") || !strcmp(w, "output_mode")) {
       char mode[MAXS];
       r = fscanf(in, "%511s", mode);
@@ -432,6 +435,7 @@ const double *gb_inputs_u0(const gb_inputs *in) { return in ? in->u0 : NULL; }
 const double *gb_inputs_exact(const gb_inputs *in) { return in ? in->uex : NULL; }
 const double *gb_inputs_gravity_field(const gb_inputs *in) { return in ? in->grav : NULL; }
 const char *gbh_inputs_op_overwrite(const gb_inputs *in) { return in ? in->op_overwrite : "yes"; }
+const char *gbh_inputs_op_format(const gb_inputs *in) { return in ? in->op_format : "binary"; }
 
 int gb_inputs_nsims(const char *dir) {
   /* simulation.inp (src/Simulation/EnsembleSimulationsDefine.cpp:41-70): "begin nsims N end" */
@@ -621,6 +625,14 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
 
   gb_inputs *res = (gb_inputs *)calloc(1, sizeof(gb_inputs));
   snprintf(res->op_overwrite, sizeof(res->op_overwrite), "%s", si.op_overwrite);
+  snprintf(res->op_format, sizeof(res->op_format), "%s", si.op_format);
+  /* InitializeSolvers.c:419-436: text, tecplot2d, tecplot3d, binary / bin, none */
+  if (strcmp(si.op_format, "text") && strcmp(si.op_format, "tecplot2d") && strcmp(si.op_format, "tecplot3d") &&
+      strcmp(si.op_format, "binary") && strcmp(si.op_format, "bin") && strcmp(si.op_format, "none")) {
+    gbh_set_error("%s is not a supported file format", si.op_format);
+    gb_inputs_free(res);
+    return GB_ERR_INPUT;
+  }
   long nx = 0, nxg = 0, npts = 1;
   for (int d = 0; d < c.ndims; d++) {
     nx += c.dim[d];
@@ -793,6 +805,63 @@ int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, cons
   fwrite(dim, sizeof(int), ndims, out);
   fwrite(x, sizeof(double), nx, out);
   fwrite(u, sizeof(double), n * nvars, out);
+  fclose(out);
+  return GB_OK;
+}
+
+/* WriteText (src/IOFunctions/WriteText.c) and WriteTecplot2D / WriteTecplot3D
+ * (WriteTecplot2D.c, WriteTecplot3D.c): per point, dimension 0 fastest, the grid
+ * indices, the coordinates and the variables; the Tecplot forms first write a
+ * VARIABLES / ZONE header. */
+static int write_points(FILE *out, int ndims, int nvars, const int *dim, const double *x, const double *u) {
+  long n = 1;
+  for (int d = 0; d < ndims; d++) n *= dim[d];
+  int idx[3] = {0, 0, 0};
+  for (long p = 0; p < n; p++) {
+    long r = p;
+    for (int d = 0; d < ndims; d++) {
+      idx[d] = (int)(r % dim[d]);
+      r /= dim[d];
+    }
+    for (int d = 0; d < ndims; d++) fprintf(out, "%4d ", idx[d]);
+    int off = 0;
+    for (int d = 0; d < ndims; d++) {
+      fprintf(out, "%+1.16E ", x[off + idx[d]]);
+      off += dim[d];
+    }
+    for (int v = 0; v < nvars; v++) fprintf(out, "%+1.16E ", u[(long)nvars * p + v]);
+    fprintf(out, "\n");
+  }
+  return GB_OK;
+}
+
+int gb_write_text(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u) {
+  FILE *out = fopen(path, "w");
+  if (!out) {
+    gbh_set_error("could not open %s for writing", path);
+    return GB_ERR_INPUT;
+  }
+  write_points(out, ndims, nvars, dim, x, u);
+  fclose(out);
+  return GB_OK;
+}
+
+int gb_write_tecplot(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u) {
+  if (ndims != 2 && ndims != 3) {
+    gbh_set_error("gb_write_tecplot: 2-D or 3-D grids only (ndims = %d)", ndims);
+    return GB_ERR_ARG;
+  }
+  FILE *out = fopen(path, "w");
+  if (!out) {
+    gbh_set_error("could not open %s for writing", path);
+    return GB_ERR_INPUT;
+  }
+  fprintf(out, ndims == 2 ? "VARIABLES=\"I\",\"J\",\"X\",\"Y\"," : "VARIABLES=\"I\",\"J\",\"K\",\"X\",\"Y\",\"Z\",");
+  for (int v = 0; v < nvars; v++) fprintf(out, "\"%d%d\",", (v / 10) % 10, v % 10);  /* "00", "01", ... */
+  fprintf(out, "\n");
+  if (ndims == 2) fprintf(out, "ZONE I=%d,J=%d,F=POINT\n", dim[0], dim[1]);
+  else fprintf(out, "ZONE I=%d,J=%d,K=%d,F=POINT\n", dim[0], dim[1], dim[2]);
+  write_points(out, ndims, nvars, dim, x, u);
   fclose(out);
   return GB_OK;
 }

@@ -3,9 +3,9 @@
  *
  * Follows the reference driver's order (src/main.cpp:334-473): read the
  * inputs, set up the solver, run n_iter Runge-Kutta steps, and write the
- * solution in HyPar's binary format: op.bin when op_overwrite is "yes", else
- * op_00000.bin, op_00001.bin, ... every file_op_iter steps
- * (src/Simulation/OutputSolution.cpp:50-140).
+ * solution in solver.inp's op_file_format (binary .bin, text / Tecplot .dat):
+ * op.<ext> when op_overwrite is "yes", else op_00000.<ext>, op_00001.<ext>, ...
+ * every file_op_iter steps (src/Simulation/OutputSolution.cpp:25-140).
  */
 #define _POSIX_C_SOURCE 200809L /* clock_gettime */
 #include <math.h>
@@ -18,15 +18,38 @@
 
 void gbh_set_error(const char *fmt, ...);
 const char *gbh_inputs_op_overwrite(const gb_inputs *in);
+const char *gbh_inputs_op_format(const gb_inputs *in);
 
-static int write_op(const char *dir, const char *name, const gb_config *c, const double *x, gb_solver *s,
-                    double *buf) {
-  int rc = gb_solver_get_state(s, buf, GB_LAYOUT_INTERIOR, GB_MEM_HOST);
-  if (rc) return rc;
-  char path[4096];
+/* The solution file of op_file_format (InitializeSolvers.c:419-436, WriteArray.c:
+   root, "_" and the five-digit index unless op_overwrite is "yes", then ".bin" for
+   binary, ".dat" for text and Tecplot; nothing for "none").  A Tecplot form that
+   does not fit the grid's dimension writes nothing and says so, as the reference's
+   writers do. */
+static int write_file(const char *dir, const char *root, int index, const char *fmt, const gb_config *c,
+                      const double *x, const double *u) {
+  if (!strcmp(fmt, "none")) return GB_OK;
+  const int bin = !strcmp(fmt, "binary") || !strcmp(fmt, "bin");
+  char name[256], path[4400];
+  if (index >= 0) snprintf(name, sizeof(name), "%s_%05d%s", root, index, bin ? ".bin" : ".dat");
+  else snprintf(name, sizeof(name), "%s%s", root, bin ? ".bin" : ".dat");
   if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s", dir, name);
   else snprintf(path, sizeof(path), "%s", name);
-  return gb_write_binary(path, c->ndims, c->nvars, c->dim, x, buf);
+  if (bin) return gb_write_binary(path, c->ndims, c->nvars, c->dim, x, u);
+  if (!strcmp(fmt, "text")) return gb_write_text(path, c->ndims, c->nvars, c->dim, x, u);
+  if ((!strcmp(fmt, "tecplot2d") && c->ndims != 2) || (!strcmp(fmt, "tecplot3d") && c->ndims != 3)) {
+    fprintf(stderr, "Error: %s is for %s problems only (ndims = %d); %s not written.\n", fmt,
+            fmt[7] == '2' ? "2-dimensional" : "3-dimensional", c->ndims, name);
+    return GB_OK;
+  }
+  return gb_write_tecplot(path, c->ndims, c->nvars, c->dim, x, u);
+}
+
+static int write_op(const char *dir, int index, const char *fmt, const gb_config *c, const double *x,
+                    gb_solver *s, double *buf) {
+  if (!strcmp(fmt, "none")) return GB_OK;
+  int rc = gb_solver_get_state(s, buf, GB_LAYOUT_INTERIOR, GB_MEM_HOST);
+  if (rc) return rc;
+  return write_file(dir, "op", index, fmt, c, x, buf);
 }
 
 static int write_errors(const char *dir, const gb_config *c, const double *err, double runtime) {
@@ -111,19 +134,17 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
   int width = 1;
   for (int n = nsims; n >= 10; n /= 10) width++;
   int k = 0;
-  char name[160], path[4400];
+  const char *fmt = rc ? "none" : gbh_inputs_op_format(in[0]);
   if (width > 9) width = 9;
   struct timespec t0, t1;
   clock_gettime(CLOCK_MONOTONIC, &t0);
   for (int it = 0; !rc && it <= cf[0].n_iter;) {
     int write = (!overwrite && (it % every == 0 || it == cf[0].n_iter)) || (overwrite && it == cf[0].n_iter);
-    for (int m = 0; write && m < nsims && !rc; m++) {
+    for (int m = 0; write && strcmp(fmt, "none") && m < nsims && !rc; m++) {
+      char root[64];
+      snprintf(root, sizeof(root), "op_%0*d", width, m);  /* OutputSolution.cpp:53-58 */
       rc = gb_ensemble_get_state(e, m, buf, GB_LAYOUT_INTERIOR, GB_MEM_HOST);
-      if (overwrite) snprintf(name, sizeof(name), "op_%0*d.bin", width, m);
-      else snprintf(name, sizeof(name), "op_%0*d_%05d.bin", width, m, k);
-      if (dir && dir[0]) snprintf(path, sizeof(path), "%s/%s", dir, name);
-      else snprintf(path, sizeof(path), "%s", name);
-      if (!rc) rc = gb_write_binary(path, cf[m].ndims, cf[m].nvars, cf[m].dim, gb_inputs_x(in[m]), buf);
+      if (!rc) rc = write_file(dir, root, overwrite ? -1 : k, fmt, &cf[m], gb_inputs_x(in[m]), buf);
     }
     if (write && !overwrite) k++;
     if (it == cf[0].n_iter) break;
@@ -145,7 +166,7 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
     if (cf[m].cons_check) rc = gb_ensemble_conservation_error(e, m, cons);
     if (!rc) rc = write_counts(dir, suffix, &cf[m], cf[m].cons_check ? cons : NULL, cf[m].n_iter);
     if (!rc) {
-      char path[4400];
+      char path[4400];  /* errors_<k>.dat */
       if (dir && dir[0]) snprintf(path, sizeof(path), "%s/errors%s.dat", dir, suffix);
       else snprintf(path, sizeof(path), "errors%s.dat", suffix);
       FILE *out = fopen(path, "w");
@@ -196,6 +217,7 @@ int gb_run_case(const char *dir, int device, int verbose) {
   /* InitialSolution.c:118: the volume integral of the initial solution */
   if (!rc && c->cons_check) rc = gb_solver_conservation_begin(s);
   const int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");
+  const char *fmt = gbh_inputs_op_format(in);
   const int every = c->file_op_iter > 0 ? c->file_op_iter : c->n_iter;
   const int screen = c->screen_op_iter > 0 ? c->screen_op_iter : 1;
   const int R = c->restart_iter > 0 ? c->restart_iter : 0;
@@ -205,11 +227,7 @@ int gb_run_case(const char *dir, int device, int verbose) {
   for (int t = 0; t < R; t++)
     if ((t + 1) % every == 0) k++;
   if (!rc) rc = gb_solver_set_time(s, R * c->dt);
-  char name[64];
-  if (!rc && !overwrite && R == 0) {
-    snprintf(name, sizeof(name), "op_%05d.bin", k++);
-    rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
-  }
+  if (!rc && !overwrite && R == 0) rc = write_op(dir, k++, fmt, c, gb_inputs_x(in), s, buf);
   FILE *resid = NULL;
   if (!rc && c->write_residual) {
     char path[4200];
@@ -253,21 +271,12 @@ int gb_run_case(const char *dir, int device, int verbose) {
       }
       if (resid) fprintf(resid, "%10d\t%E\t%E\n", it, gb_solver_time(s), norm);
     }
-    if (!overwrite && it % every == 0 && it < c->n_iter) {
-      snprintf(name, sizeof(name), "op_%05d.bin", k++);
-      rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
-    }
+    if (!overwrite && it % every == 0 && it < c->n_iter) rc = write_op(dir, k++, fmt, c, gb_inputs_x(in), s, buf);
   }
   clock_gettime(CLOCK_MONOTONIC, &t1);
   const double solver_runtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
   if (resid) fclose(resid);
-  if (!rc) {
-    if (overwrite) rc = write_op(dir, "op.bin", c, gb_inputs_x(in), s, buf);
-    else {
-      snprintf(name, sizeof(name), "op_%05d.bin", k++);
-      rc = write_op(dir, name, c, gb_inputs_x(in), s, buf);
-    }
-  }
+  if (!rc) rc = write_op(dir, overwrite ? -1 : k++, fmt, c, gb_inputs_x(in), s, buf);
   if (!rc) {
     int fin = 1;
     rc = gb_solver_check_finite(s, &fin);

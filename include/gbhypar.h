@@ -245,6 +245,12 @@ int gb_ensemble_conservation_error(gb_ensemble *e, int member, double *err);
 int gb_run_case(const char *dir, int device, int verbose);
 /* Write a HyPar binary solution file from an interior solution. */
 int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
+/* The same as HyPar's text file (WriteText.c: per point the grid indices, the
+ * coordinates and the variables, dimension 0 fastest) and Tecplot point file
+ * (WriteTecplot2D.c / WriteTecplot3D.c: that with a VARIABLES / ZONE header; 2-D
+ * and 3-D grids). */
+int gb_write_text(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
+int gb_write_tecplot(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
 /* Convert a binary solution file (op*.bin) into a binary initial.inp, for a
  * restart (the reference's Extras/BinaryOPToInitialSolution.c). */
 int gb_op_to_initial(const char *op_path, const char *initial_path);

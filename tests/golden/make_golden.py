@@ -188,6 +188,33 @@ def _w(case, weights):
     return case
 
 
+def _fmt(case, fmt, overwrite="yes"):
+    """The deck with solver.inp op_file_format fmt (and op_overwrite)."""
+    case.op_format, case.op_overwrite = fmt, overwrite
+    return case
+
+
+# solution files in the text and Tecplot formats (op_file_format): file name -> deck
+OUTPUTS = {
+    "out_sod64_text": (lambda: _fmt(C.sod(64, n_iter=10, dt=1e-3), "text"), ["op.dat"]),
+    "out_vortex24_tecplot2d": (lambda: _fmt(C.vortex(24, n_iter=3, dt=0.02), "tecplot2d", "no"),
+                               ["op_00000.dat", "op_00001.dat"]),
+    "out_tgv8_tecplot3d": (lambda: _fmt(C.tgv(8, n_iter=2, dt=0.02, perturb=0.05), "tecplot3d"), ["op.dat"]),
+    "out_vortex16_text": (lambda: _fmt(C.vortex(16, n_iter=2, dt=0.02), "text"), ["op.dat"]),
+}
+
+
+def read_text_output(path):
+    """(header lines, numeric table) of a text / Tecplot solution file."""
+    header, rows = [], []
+    for line in open(path):
+        try:
+            rows.append([float(t) for t in line.split()])
+        except ValueError:
+            header.append(line.rstrip("\n"))
+    return header, np.array(rows, dtype=np.float64)
+
+
 ENSEMBLES = {
     "ens3_vortex_char_roe_ssprk3": lambda: C.ensemble_vortex(3, sizes=[16, 24, 20], n_iter=4, seed=7),
 }
@@ -218,6 +245,21 @@ def main() -> None:
         np.savez_compressed(os.path.join(HERE, name + ".npz"), u0=case.u, rhs=rhs, uN=op["u"],
                             n_iter=case.n_iter, dt=case.dt, cfl=dump["cfl"], cons=cons, counts=counts)
         print(name, rhs.shape, op["u"].shape)
+    for name, (mk, files) in OUTPUTS.items():
+        if only and name not in only:
+            continue
+        case = mk()
+        case.file_op_iter = case.n_iter if case.op_overwrite == "no" else None
+        with tempfile.TemporaryDirectory() as d:
+            case.write(d)
+            subprocess.check_call([os.path.join(O.REF_DIR, "HyPar")], cwd=d, stdout=subprocess.DEVNULL, env=env)
+            out = {}
+            for k, f in enumerate(files):
+                header, table = read_text_output(os.path.join(d, f))
+                out[f"header_{k}"] = np.array(header)
+                out[f"table_{k}"] = table
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, [out[f"table_{k}"].shape for k in range(len(files))])
     for name, mk in ENSEMBLES.items():
         if only and name not in only:
             continue
