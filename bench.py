@@ -219,7 +219,14 @@ def run_ours(args, case, desc, ws, rank, local):
     stream = torch.cuda.Stream()  # a real stream: handle 0 would mean "the solver's own"
     torch.cuda.set_stream(stream)
     s.set_stream(stream.cuda_stream)
-    tuned = s.autotune(2)  # launch shape per direction (state restored), outside the timed region
+    if args.launch:
+        # a fixed launch shape per direction (profiling: the autotuner's choice under a
+        # profiler's serialised replays can differ from its choice in a plain run)
+        for d, sg in enumerate(int(v) for v in args.launch.split(",")):
+            s.set_launch(d, sg, 0)
+        tuned = [s.get_launch(d) for d in range(case.ndims)]
+    else:
+        tuned = s.autotune(2)  # launch shape per direction (state restored), outside the timed region
     cells = int(np.prod(case.size))
     nv = case.nvars
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
@@ -765,6 +772,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--size", type=int, default=0, help="override the grid size (profiling of small cases)")
+    ap.add_argument("--launch", default="", help="fixed launch shape per direction instead of the autotuner's, "
+                                                 "e.g. -128,-128 (tiles of 128 interfaces)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
