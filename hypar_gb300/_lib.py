@@ -29,7 +29,7 @@ EXPORTS = [
     "gb_solver_set_stream", "gb_solver_sync", "gb_solver_set_state", "gb_solver_get_state", "gb_solver_state",
     "gb_solver_step", "gb_solver_time", "gb_solver_set_launch", "gb_solver_check_finite", "gb_run_case",
     "gb_write_binary", "gb_write_text", "gb_write_tecplot", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
-    "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
+    "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_SetInterpLimiterVar", "gb_InterpolateInterfacesHyp", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
     "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
     "gb_solver_get_launch", "gb_solver_autotune", "gb_inputs_nsims", "gb_inputs_read_member",
     "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
@@ -121,6 +121,8 @@ def lib():
         getattr(L, n).argtypes = [VP, VP, ctypes.c_int, VP, ctypes.c_double]
     L.gb_UFunction.argtypes = [VP, VP, ctypes.c_int, VP, VP, ctypes.c_double]
     L.gb_Upwind.argtypes = [VP, VP, VP, VP, VP, VP, ctypes.c_int, VP, ctypes.c_double]
+    L.gb_SetInterpLimiterVar.argtypes = [VP, VP, VP, ctypes.c_int, VP, VP]
+    L.gb_InterpolateInterfacesHyp.argtypes = [VP, VP, VP, VP, ctypes.c_int, ctypes.c_int, VP, VP, ctypes.c_int]
     L.gb_ApplyBoundaryConditions.argtypes = [VP, VP, VP, VP, ctypes.c_double]
     L.gb_TimeRK.argtypes = [VP]
     L.gb_probe_fp64_peak.argtypes = [DP]

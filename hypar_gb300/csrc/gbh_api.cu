@@ -38,6 +38,12 @@ cudaError_t launch_unfused_euler2d(int, int, int, double*, const double*, const 
                                    const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
 cudaError_t launch_unfused_ns3d(int, int, int, double*, const double*, const double*, const double*,
                                 const double*, const double*, const DevGeom&, const PhysParams&, cudaStream_t);
+cudaError_t launch_interp_euler1d(int, int, int, int, double*, const double*, const double*, const DevGeom&,
+                                  const PhysParams&, cudaStream_t);
+cudaError_t launch_interp_euler2d(int, int, int, int, double*, const double*, const double*, const DevGeom&,
+                                  const PhysParams&, cudaStream_t);
+cudaError_t launch_interp_ns3d(int, int, int, int, double*, const double*, const double*, const DevGeom&,
+                               const PhysParams&, cudaStream_t);
 cudaError_t launch_visc(const double*, double*, double*, double*, const double*, const DevGeom&,
                         const ViscParams&, int, cudaStream_t);
 cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, const double*, double, cudaStream_t);
@@ -832,6 +838,47 @@ extern "C" int gb_Upwind(double* fI, double* fL, double* fR, double* uL, double*
   }
   if (s->gravity && !s->d_grav) return gravity_ready(s);
   CK(launch_unfused(s, 2, dir, fI, fL, fR, uL, uR, u));
+  return GB_OK;
+}
+
+// SetInterpLimiterVar (include/hypar.h:234): the reference computes the WENO5
+// weights of fC and u here and stores them for the next four
+// InterpolateInterfacesHyp calls (HyperbolicFunction.c:201-215, which pass the
+// same fC and u); gb_InterpolateInterfacesHyp evaluates them from those arrays
+// itself, so this only checks its arguments.
+extern "C" int gb_SetInterpLimiterVar(double* fC, double* u, double* x, int dir, void* sv, void* m) {
+  (void)x;
+  (void)m;
+  gb_solver* s = S(sv);
+  if (!s || !fC || !u || dir < 0 || dir >= s->cfg.ndims) {
+    gbh_set_error("gb_SetInterpLimiterVar: bad argument");
+    return GB_ERR_ARG;
+  }
+  return GB_OK;
+}
+
+// InterpolateInterfacesHyp (include/hypar.h:224): WENO5 interface values of fC along
+// dir, left-biased for upw > 0, right-biased for upw < 0, with the weights of fC
+// (uflag 0) or of u (uflag 1), component-wise or characteristic as configured.
+extern "C" int gb_InterpolateInterfacesHyp(double* fI, double* fC, double* u, double* x, int upw, int dir, void* sv,
+                                           void* m, int uflag) {
+  (void)x;
+  (void)m;
+  gb_solver* s = S(sv);
+  if (!s || !fI || !fC || !u || dir < 0 || dir >= s->cfg.ndims || upw == 0) {
+    gbh_set_error("gb_InterpolateInterfacesHyp: bad argument");
+    return GB_ERR_ARG;
+  }
+  if (s->cfg.hyp_scheme != GB_SCHEME_WENO5) {
+    gbh_set_error("gb_InterpolateInterfacesHyp: WENO5 only (CRWENO5 runs through the fused kernels)");
+    return GB_ERR_UNSUPPORTED;
+  }
+  const gb_config& c = s->cfg;
+  const int chr = c.interp == GB_INTERP_CHARACTERISTIC, left = upw > 0, uf = uflag != 0;
+  if (c.model == GB_MODEL_EULER1D) CK(launch_interp_euler1d(dir, chr, left, uf, fI, fC, u, s->G, s->pp, s->stream));
+  else if (c.model == GB_MODEL_EULER2D)
+    CK(launch_interp_euler2d(dir, chr, left, uf, fI, fC, u, s->G, s->pp, s->stream));
+  else CK(launch_interp_ns3d(dir, chr, left, uf, fI, fC, u, s->G, s->pp, s->stream));
   return GB_OK;
 }
 

@@ -21,4 +21,8 @@ cudaError_t launch_unfused_euler2d(int kind, int dir, int upw, double* out, cons
                                    const PhysParams& pp, cudaStream_t s) {
   return launch_unfused_model<MODEL_EULER2D>(kind, dir, upw, out, a, b, c, d, u, G, pp, s);
 }
+cudaError_t launch_interp_euler2d(int dir, int chr, int left, int uf, double* fI, const double* fC, const double* u,
+                                const DevGeom& G, const PhysParams& pp, cudaStream_t s) {
+  return launch_interp_model<MODEL_EULER2D>(dir, chr, left, uf, fI, fC, u, G, pp, s);
+}
 }  // namespace gbh

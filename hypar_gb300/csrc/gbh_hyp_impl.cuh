@@ -1043,6 +1043,114 @@ __global__ void upwind_kernel(double* __restrict__ fI, const double* __restrict_
   for (int v = 0; v < NV; v++) fI[p * NV + v] = out[v];
 }
 
+// InterpolateInterfacesHyp (Interp1PrimFifthOrderWENO.c:74-168 and
+// Interp1PrimFifthOrderWENOChar.c:86-198): the WENO5 value at every interface of
+// the ghosted cell array fC along DIR, left-biased (LEFT) or right-biased, with the
+// nonlinear weights of the stencil of fC (!UF) or of u (UF), the weights the
+// reference stores in SetInterpLimiterVar from the same arrays
+// (WENOFifthOrderCalculateWeights.c).  CHAR: in the characteristic fields of the Roe
+// average of u at the interface's two cells.  One thread per interface; ghost points
+// are read as the caller left them.
+template <int M, bool CHAR, int DIR>
+__global__ void interp_kernel(double* __restrict__ fI, const double* __restrict__ fC, const double* __restrict__ u,
+                              DevGeom G, PhysParams pp, int left, int uf, long long nint) {
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nint) return;
+  int idx[3] = {0, 0, 0};
+  long long r = p;
+#pragma unroll
+  for (int e = 0; e < ND; e++) {
+    int n = G.dim[e] + (e == DIR ? 1 : 0);
+    idx[e] = (int)(r % n);
+    r /= n;
+  }
+  long long pc = 0;  // the cell right of the interface
+#pragma unroll
+  for (int e = 0; e < ND; e++) pc += (long long)(idx[e] + G.g) * G.stride[e];
+  const long long sd = G.stride[DIR];
+  const double eps4 = 4.0 * pp.eps;
+  // window: cells I-3 .. I+2 of interface I (left cell I-1, right cell I)
+  double wv[6][NV], ww[6][NV];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const long long q = (pc + (long long)(k - 3) * sd) * NV;
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      wv[k][v] = fC[q + v];
+      ww[k][v] = uf ? u[q + v] : wv[k][v];
+    }
+  }
+  double out[NV];
+  if (!CHAR) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double sw[6], sv[6], omL[3], omR[3], oL, oR;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        sw[k] = ww[k][v];
+        sv[k] = wv[k][v];
+      }
+      weno5_weights<true>(sw, eps4, pp.wtype, omL, omR);
+      weno5_apply(omL, omR, sv, oL, oR);
+      out[v] = left ? oL : oR;
+    }
+  } else {
+    double uu[NV];
+    RoeSide rs[2];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const long long q = (pc + (long long)(k - 1) * sd) * NV;
+#pragma unroll
+      for (int v = 0; v < NV; v++) uu[v] = u[q + v];
+      rs[k] = roe_side<M>(to_prim<M>(uu, pp));
+    }
+    const Eig E = roe_eig<M, DIR>(rs[0], rs[1], pp);
+    double cv[6][NV], cw[6][NV];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      projL<M, DIR>(E, pp, wv[k], cv[k]);
+      if (uf) projL<M, DIR>(E, pp, ww[k], cw[k]);
+    }
+    double ch[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      double sw[6], sv[6], omL[3], omR[3], oL, oR;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        sv[k] = cv[k][v];
+        sw[k] = uf ? cw[k][v] : cv[k][v];
+      }
+      weno5_weights<true>(sw, eps4, pp.wtype, omL, omR);
+      weno5_apply(omL, omR, sv, oL, oR);
+      ch[v] = left ? oL : oR;
+    }
+    projR<M, DIR>(E, ch, out);
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) fI[p * NV + v] = out[v];
+}
+
+template <int M>
+cudaError_t launch_interp_model(int dir, int chr, int left, int uf, double* fI, const double* fC, const double* u,
+                                const DevGeom& G, const PhysParams& pp, cudaStream_t s) {
+  constexpr int ND = ModelTraits<M>::ND;
+  if (dir < 0 || dir >= ND) return cudaErrorInvalidValue;
+  long long nint = 1;
+  for (int e = 0; e < ND; e++) nint *= G.dim[e] + (e == dir ? 1 : 0);
+  const unsigned grid = (unsigned)((nint + 127) / 128);
+#define GBH_I(D)                                                                                          \
+  do {                                                                                                    \
+    if (chr) interp_kernel<M, true, D><<<grid, 128, 0, s>>>(fI, fC, u, G, pp, left, uf, nint);          \
+    else interp_kernel<M, false, D><<<grid, 128, 0, s>>>(fI, fC, u, G, pp, left, uf, nint);             \
+  } while (0)
+  if (dir == 0) GBH_I(0);
+  else if (dir == 1) GBH_I((ND > 1 ? 1 : 0));
+  else GBH_I((ND > 2 ? 2 : 0));
+#undef GBH_I
+  return cudaGetLastError();
+}
+
 enum { UNFUSED_FLUX = 0, UNFUSED_UFUNC = 1, UNFUSED_UPWIND = 2 };
 
 template <int M, int DIR>

@@ -11,4 +11,8 @@ cudaError_t launch_unfused_ns3d(int kind, int dir, int upw, double* out, const d
                                    const PhysParams& pp, cudaStream_t s) {
   return launch_unfused_model<MODEL_NS3D>(kind, dir, upw, out, a, b, c, d, u, G, pp, s);
 }
+cudaError_t launch_interp_ns3d(int dir, int chr, int left, int uf, double* fI, const double* fC, const double* u,
+                                const DevGeom& G, const PhysParams& pp, cudaStream_t s) {
+  return launch_interp_model<MODEL_NS3D>(dir, chr, left, uf, fI, fC, u, G, pp, s);
+}
 }  // namespace gbh

@@ -270,6 +270,18 @@ class Solver:
         check(lib().gb_Upwind(_ptr(fI), _ptr(fL), _ptr(fR), _ptr(uL), _ptr(uR), _ptr(u), dim, self._h, t))
         self.sync()
 
+    def set_interp_limiter_var(self, fC, u, dim: int):
+        self._dev()
+        check(lib().gb_SetInterpLimiterVar(_ptr(fC), _ptr(u), None, dim, self._h, None))
+
+    def interpolate(self, fI, fC, u, upw: int, dim: int, uflag: int):
+        """InterpolateInterfacesHyp: WENO5 interface values of fC along dim (upw > 0
+        left-biased, < 0 right-biased; weights of fC for uflag 0, of u for uflag 1)."""
+        self._dev()
+        check(lib().gb_InterpolateInterfacesHyp(_ptr(fI), _ptr(fC), _ptr(u), None, int(upw), dim, self._h, None,
+                                                int(uflag)))
+        self.sync()
+
     def apply_bc(self, u, t: float = 0.0):
         self._dev()
         check(lib().gb_ApplyBoundaryConditions(self._h, None, _ptr(u), None, t))

@@ -272,7 +272,8 @@ int gb_HyperbolicFunction(double *hyp, double *u, void *s, void *m, double t, in
 /* ParabolicFunction (include/hypar.h:256; NavierStokes3DParabolicFunction.c:50).
  * Zero for the Euler models. */
 int gb_ParabolicFunction(double *par, double *u, void *s, void *m, double t);
-/* SourceFunction (include/hypar.h:259): zero (no gravity on this path). */
+/* SourceFunction (include/hypar.h:259): the gravity source term (Euler1D,
+ * NavierStokes3D with gravity: Euler1DSource.c, NavierStokes3DSource.c), else zero. */
 int gb_SourceFunction(double *source, double *u, void *s, void *m, double t);
 /* FFunction (include/hypar.h:276): cell flux along dir at every point. */
 int gb_FFunction(double *f, double *u, int dir, void *s, double t);
@@ -284,6 +285,19 @@ int gb_UFunction(double *uC, double *u, int dir, void *s, void *m, double t);
  * fI, fL, fR, uL, uR are interface arrays (no ghosts, dim[dir]+1 along dir). */
 int gb_Upwind(double *fI, double *fL, double *fR, double *uL, double *uR, double *u, int dir, void *s,
               double t);
+/* SetInterpLimiterVar (include/hypar.h:234): checks its arguments; the WENO5 weights
+ * the reference stores here are evaluated by gb_InterpolateInterfacesHyp from the same
+ * fC and u (HyperbolicFunction.c:201-215 passes the same arrays to both). */
+int gb_SetInterpLimiterVar(double *fC, double *u, double *x, int dir, void *s, void *m);
+/* InterpolateInterfacesHyp (include/hypar.h:224; Interp1PrimFifthOrderWENO.c,
+ * Interp1PrimFifthOrderWENOChar.c): WENO5 values fI at the interfaces along dir
+ * (interface array, dim[dir]+1 along dir, no ghosts) of the ghosted cell array fC,
+ * left-biased for upw > 0, right-biased for upw < 0, with the nonlinear weights of
+ * fC (uflag 0) or of u (uflag 1); characteristic in the Roe eigenvectors of u when
+ * configured.  Ghost points are read as they are (apply the boundaries first).
+ * WENO5 only. */
+int gb_InterpolateInterfacesHyp(double *fI, double *fC, double *u, double *x, int upw, int dir, void *s, void *m,
+                                int uflag);
 /* ApplyBoundaryConditions (include/hypar.h:214): fills ghost points of u in place. */
 int gb_ApplyBoundaryConditions(void *s, void *m, double *u, double *uref, double t);
 /* TimeIntegration.RHSFunction = TimeRHSFunctionExplicit

@@ -242,6 +242,55 @@ def test_function_pointer_surface(built_lib, oracle_lib, tmp_path, model, interp
     assert not gf.cpu().numpy().any()
 
 
+@pytest.mark.parametrize("model,interp,upw,weights", [("euler1d", "components", "roe", "js"),
+                                                      ("euler1d", "characteristic", "llf-char", "yc"),
+                                                      ("euler2d", "characteristic", "roe", "js"),
+                                                      ("euler2d", "components", "rf-char", "mapped"),
+                                                      ("navierstokes3d", "components", "roe", "borges"),
+                                                      ("navierstokes3d", "characteristic", "rusanov", "js")])
+def test_reconstruct_hyperbolic_from_the_pointers(built_lib, oracle_lib, tmp_path, model, interp, upw, weights):
+    """HyPar's own HyperbolicFunction / ReconstructHyperbolic sequence
+    (HyperbolicFunction.c:31-126, :201-219) driven through this library's function
+    pointers -- FFunction, SetInterpLimiterVar, UFunction, four InterpolateInterfacesHyp,
+    Upwind -- then hyp += dxinv (F[j+1/2] - F[j-1/2]), against the oracle's
+    hyperbolic term."""
+    from hypar_gb300.solver import Inputs
+    case = make(model, interp, upw)
+    case.weights = weights
+    s = solver_for(case, tmp_path)
+    dxinv = Inputs(str(tmp_path / "deck")).dxinv  # per dimension, with ghosts (InitialSolution.c:69-99)
+    P = O.Problem(case)
+    u0 = P.apply_bc(P.u0())
+    u = torch.from_numpy(u0).cuda()
+    nv, g, dims = case.nvars, 3, list(case.size)
+    hyp = np.zeros_like(u0).reshape([d + 2 * g for d in reversed(dims)] + [nv])
+    for d in range(case.ndims):
+        fC = torch.zeros_like(u)
+        s.flux(fC, u, d)
+        s.set_interp_limiter_var(fC, u, d)
+        uC = torch.zeros_like(u)
+        s.ufunc(uC, u, d)
+        idims = [n + (1 if e == d else 0) for e, n in enumerate(dims)]
+        nI = int(np.prod(idims)) * nv
+        uL, uR, fL, fR, fI = (torch.zeros(nI, dtype=torch.float64, device="cuda") for _ in range(5))
+        s.interpolate(uL, uC, u, 1, d, 1)
+        s.interpolate(uR, uC, u, -1, d, 1)
+        s.interpolate(fL, fC, u, 1, d, 0)
+        s.interpolate(fR, fC, u, -1, d, 0)
+        s.upwind(fI, fL, fR, uL, uR, u, d)
+        F = fI.cpu().numpy().reshape(list(reversed(idims)) + [nv])
+        ax = case.ndims - 1 - d  # numpy axis of dimension d (dimension 0 fastest)
+        diff = np.diff(F, axis=ax)
+        off = sum(dims[e] + 2 * g for e in range(d)) + g
+        shape = [1] * (case.ndims + 1)
+        shape[ax] = dims[d]
+        sl = tuple(slice(g, g + n) for n in reversed(dims))
+        hyp[sl] += dxinv[off:off + dims[d]].reshape(shape) * diff
+    ref = O.interior(P.hyperbolic(P.u0()), case.size, nv, g)
+    got = hyp[tuple(slice(g, g + n) for n in reversed(dims))].reshape(-1, nv)
+    assert relerr(got.reshape(-1), ref.reshape(-1)) <= RHS_TOL
+
+
 def test_nonfinite_state_is_reported(built_lib, tmp_path):
     case = C.vortex(16, n_iter=1, dt=0.01)
     case.u[5, 0] = float("nan")
