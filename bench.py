@@ -303,7 +303,8 @@ def run_ours(args, case, desc, ws, rank, local):
         bytes_per_launch = cells * 8.0 * nv * 2  # read U, write the partial hyperbolic term
     achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
     cls_dir = "xyz".index(cls[-1]) if cls.startswith("hyp_") else 0
-    form = "tile" if tuned and tuned[cls_dir][0] < 0 else "walker"
+    seg0 = tuned[cls_dir][0] if tuned else 0
+    form = "lanes" if seg0 in (-8, -16) else ("tile" if seg0 < 0 else "walker")
     traffic = DRAM_BYTES_PER_CELL.get(args.workload, {}).get((cls, form))
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic * cells if traffic else None,

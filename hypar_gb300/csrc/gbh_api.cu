@@ -470,7 +470,14 @@ extern "C" int gb_solver_set_gravity_field(gb_solver* s, const double* fg) {
 
 extern "C" int gb_solver_set_launch(gb_solver* s, int dir, int seg, int block) {
   if (!s || dir < 0 || dir >= s->cfg.ndims) { gbh_set_error("gb_solver_set_launch: bad argument"); return GB_ERR_ARG; }
-  if (seg > 0 || seg == -32 || seg == -64 || seg == -128) s->hl[dir].seg = seg;  // -t: tiles of t interfaces
+  // -t: tiles of t interfaces; -8 / -16: lane groups (Euler1D component-wise WENO5, no gravity)
+  const bool lanes_ok = s->cfg.model == GB_MODEL_EULER1D && s->cfg.interp == GB_INTERP_COMPONENTS && !s->gravity &&
+                        s->cfg.hyp_scheme == GB_SCHEME_WENO5;
+  if ((seg == -8 || seg == -16) && !lanes_ok) {
+    gbh_set_error("gb_solver_set_launch: lane groups (-8, -16) need Euler1D, component-wise WENO5, no gravity");
+    return GB_ERR_ARG;
+  }
+  if (seg > 0 || seg == -32 || seg == -64 || seg == -128 || seg == -8 || seg == -16) s->hl[dir].seg = seg;
   if (block > 0) {
     if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
     s->hl[dir].block = block;
@@ -648,6 +655,10 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
     // or CRWENO5, whose kernels have no tile form)
     if (!s->gravity && c.hyp_scheme == GB_SCHEME_WENO5)
       for (int ti : {32, 64, 128}) segs.push_back(-ti);
+    // lane groups of 8 / 16 interfaces (Euler1D component-wise: short lines)
+    if (!s->gravity && c.hyp_scheme == GB_SCHEME_WENO5 && c.model == GB_MODEL_EULER1D &&
+        c.interp == GB_INTERP_COMPONENTS)
+      for (int ti : {8, 16}) segs.push_back(-ti);
     double best = 1e30;
     HypLaunch bestL = s->hl[d];
     for (int sg : segs) {

@@ -724,6 +724,96 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
   }
 }
 
+// Short 1-D lines (a Sod tube of 10^3 cells leaves one warp per SM, which then runs an
+// interface's several hundred FP64 instructions back to back): the interface work
+// split over lanes.  A block takes TI interfaces (TI - 1 cells) of the line in
+// groups of 8 lanes; phase 1 computes the TI + 5 cells into shared memory, phase 2
+// gives each of the 2 NV reconstructions of an interface (the f or the u pair of one
+// component: left- and right-biased values) to its own lane, phase 3 upwinds each
+// interface, phase 4 differences and updates each cell.  Component-wise WENO5 of a
+// model whose u-reconstruction reads u itself (Euler1D without gravity).
+template <int M, int UPW, bool ALTW, int TI>
+__global__ void __launch_bounds__(TI * 8)
+hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
+                PhysParams pp, StageEpi ep) {
+  constexpr int NV = ModelTraits<M>::NV;
+  static_assert(2 * NV <= 8, "an interface's reconstructions fit a group of 8 lanes");
+  constexpr bool CC = NeedCC<M, false, UPW>::value;
+  constexpr int TC = TI - 1, NCELL = TI + 5, NT = TI * 8;
+  __shared__ double su[NCELL][NV], sf[NCELL][NV];
+  __shared__ CellAux<M> sax[NCELL];
+  __shared__ double srec[TI][2 * NV][2];
+  __shared__ double sfI[TI][NV];
+  const int I0 = (int)blockIdx.x * TC;
+  const int N = G.dim[0];
+  const long long sd = G.stride[0];
+  const long long pbase = (long long)G.g * sd;
+  const int lo = G.bclo[0], hi = G.bchi[0];
+  const double eps4 = 4.0 * pp.eps;
+  const int t = threadIdx.x;
+  for (int c = t; c < NCELL; c += NT) {
+    const int i = I0 - 3 + c;
+    if (i > N + 2) continue;
+    const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
+    double uu[NV], ff[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uu[v] = U[pt * NV + v];
+    Prim<M> q = to_prim<M>(uu, pp);
+    cell_flux<M, 0>(q, ff);
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      su[c][v] = uu[v];
+      sf[c][v] = ff[v];
+    }
+    CellAux<M> a;
+    if (CC) a.rs = roe_side<M>(q);
+    if (UPW == UPW_RUS) a.c = rusanov_speed<M, 0>(q, pp);
+    else if (M == MODEL_EULER1D && UPW != UPW_ROE) a.c = sound_speed<M>(q, pp);
+    sax[c] = a;
+  }
+  __syncthreads();
+  {
+    const int i = t >> 3, k = t & 7;
+    if (k < 2 * NV && I0 + i <= N) {
+      const int v = k >> 1;
+      double w[6];
+#pragma unroll
+      for (int p = 0; p < 6; p++) w[p] = (k & 1) ? su[i + p][v] : sf[i + p][v];
+      double oL, oR;
+      wpair<ALTW>(w, w, eps4, pp.wtype, oL, oR);
+      srec[i][k][0] = oL;
+      srec[i][k][1] = oR;
+    }
+  }
+  __syncthreads();
+  if (t < TI && I0 + t <= N) {
+    double fL[NV], fR[NV], uL[NV], uR[NV], fI[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      fL[v] = srec[t][2 * v][0];
+      fR[v] = srec[t][2 * v][1];
+      uL[v] = srec[t][2 * v + 1][0];
+      uR[v] = srec[t][2 * v + 1][1];
+    }
+    Eig Ecc;
+    if (CC) Ecc = roe_eig<M, 0>(sax[t + 2].rs, sax[t + 3].rs, pp);
+    upwind_iface<M, false, UPW, 0>(fL, fR, uL, uR, Ecc, sax[t + 2], sax[t + 3], pp, fI);
+    boundary_flux<NV>(ep, I0 + t, N, 0, 1, fI);
+#pragma unroll
+    for (int v = 0; v < NV; v++) sfI[t][v] = fI[v];
+  }
+  __syncthreads();
+  const int c = I0 + t;
+  if (t < TC && c < N) {
+    const long long off = (pbase + (long long)c * sd) * NV;
+    const double dxi = dxinv[G.g + c];
+    double h[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) h[v] = dxi * (sfI[t + 1][v] - sfI[t][v]);
+    stage_epilogue<NV>(ep, H, off, h);
+  }
+}
+
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
 __global__ void __launch_bounds__(TI)
 hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
@@ -858,6 +948,16 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   for (int e = 0; e < G.nd; e++)
     if (e != DIR) ntrans *= G.dim[e];
   int N = G.dim[DIR];
+  if constexpr (M == MODEL_EULER1D && !CHAR && !GRAV && !WT) {
+    if (L.seg == -8 || L.seg == -16) {
+      // lane groups: TI interfaces of the one line per block, 8 lanes per interface
+      const int ti = -L.seg;
+      const unsigned nblk = (unsigned)((N + ti - 2) / (ti - 1));
+      if (ti == 8) hyp_lane_kernel<M, UPW, ALTW, 8><<<nblk, 64, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
+      else hyp_lane_kernel<M, UPW, ALTW, 16><<<nblk, 128, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
+      return cudaGetLastError();
+    }
+  }
   if (L.seg < 0 && !GRAV) {
     // tiles of -seg interfaces (32, 64 or 128), one block each
     const int ti = -L.seg;

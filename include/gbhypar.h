@@ -189,7 +189,9 @@ int gb_solver_conservation_error(gb_solver *s, double *err);
 /* Launch shape of the fused kernels: interfaces walked per thread (seg) and
  * threads per block, per direction (values <= 0 keep the current ones); seg = -32,
  * -64 or -128 selects shared-memory tiles of that many interfaces per block (one
- * interface per thread, for small grids; block is then the tile). */
+ * interface per thread, for small grids; block is then the tile); seg = -8 or -16
+ * (Euler1D, component-wise WENO5, no gravity) tiles of that many interfaces with 8
+ * lanes per interface, one per reconstruction (for short 1-D lines). */
 int gb_solver_set_launch(gb_solver *s, int dir, int seg, int block);
 int gb_solver_get_launch(gb_solver *s, int dir, int *seg, int *block);
 /* Choose seg/block per direction by timing candidates on `reps` steps of the

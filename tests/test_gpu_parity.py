@@ -291,6 +291,35 @@ def test_reconstruct_hyperbolic_from_the_pointers(built_lib, oracle_lib, tmp_pat
     assert relerr(got.reshape(-1), ref.reshape(-1)) <= RHS_TOL
 
 
+@pytest.mark.parametrize("tile", [8, 16])
+@pytest.mark.parametrize("upw,weights", [("roe", "js"), ("llf-char", "mapped"), ("rf-char", "js"), ("rusanov", "yc")])
+def test_lane_groups_match_oracle(built_lib, oracle_lib, tmp_path, upw, weights, tile):
+    """The lane-group form for short 1-D lines (gb_solver_set_launch seg = -8 / -16):
+    per RHS and after steps against the oracle, on lines that are and are not a
+    multiple of the tile's cells."""
+    for n in (72, 7 * (tile - 1)):
+        case = make("euler1d", "components", upw, n=n, n_iter=3)
+        case.weights = weights
+        s = solver_for(case, tmp_path / f"n{n}")
+        s.set_launch(0, -tile, 0)
+        assert s.get_launch(0)[0] == -tile
+        P = O.Problem(case)
+        u0 = P.u0()
+        u = torch.from_numpy(u0).cuda()
+        out = torch.zeros_like(u)
+        s.rhs(out, u)
+        got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
+        assert relerr(got, O.interior(P.rhs(u0.copy()), case.size, case.nvars, 3)) <= RHS_TOL
+        s.set_state(O.interior(u0, case.size, case.nvars, 3).reshape(-1))
+        s.step(3)
+        ref = O.interior(P.rk(P.u0(), 3), case.size, case.nvars, 3).reshape(-1)
+        assert relerr(s.get_state(), ref) <= STEP_TOL
+    case = make("euler2d", "components", "roe")
+    s = solver_for(case, tmp_path / "e2")
+    with pytest.raises(RuntimeError):
+        s.set_launch(0, -8, 0)
+
+
 def test_nonfinite_state_is_reported(built_lib, tmp_path):
     case = C.vortex(16, n_iter=1, dt=0.01)
     case.u[5, 0] = float("nan")
