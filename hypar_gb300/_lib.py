@@ -40,7 +40,7 @@ EXPORTS = [
     "gb_adjoint_backward", "gb_adjoint_tlm", "gb_inputs_exact", "gb_solver_set_time", "gb_solver_cfl",
     "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
     "gb_solver_set_gravity_field", "gb_solver_conservation_begin", "gb_solver_conservation_error",
-    "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error",
+    "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error", "gb_ensemble_error",
 ]
 
 
@@ -157,6 +157,7 @@ def lib():
     L.gb_solver_conservation_error.argtypes = [VP, DP]
     L.gb_ensemble_conservation_begin.argtypes = [VP]
     L.gb_ensemble_conservation_error.argtypes = [VP, ctypes.c_int, DP]
+    L.gb_ensemble_error.argtypes = [VP, ctypes.c_int, VP, ctypes.c_int, ctypes.c_int, DP]
     L.gb_op_to_initial.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
     L.gb_adjoint_create.argtypes = [ctypes.POINTER(GbConfig), DP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(VP)]

@@ -480,6 +480,46 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
   return rc;
 }
 
+// CalculateError for one member against its exact solution (exact_<k>.inp).
+extern "C" int gb_ensemble_error(gb_ensemble* e, int member, const double* uex, int layout, int mem, double* err) {
+  if (!e || !uex || !err || member < 0 || member >= e->nm) {
+    gbh_set_error("gb_ensemble_error: bad argument");
+    return GB_ERR_ARG;
+  }
+  const MemberDev& md = e->mem[member];
+  const gb_config& c = e->cfg[member];
+  if (!e->d_red) CK(cudaMalloc((void**)&e->d_red, CONS_RED_DOUBLES * sizeof(double)));
+  const size_t nval = (size_t)e->nvals[member];
+  double* ex = nullptr;
+  CK(cudaMallocAsync((void**)&ex, nval * sizeof(double), e->stream));
+  double* tmp = nullptr;
+  cudaError_t ce = cudaSuccess;
+  if (layout == GB_LAYOUT_GHOSTED) {
+    ce = cudaMemcpyAsync(ex, uex, nval * sizeof(double), mem == GB_MEM_HOST ? cudaMemcpyHostToDevice
+                                                                             : cudaMemcpyDeviceToDevice, e->stream);
+  } else {
+    size_t nint = (size_t)c.nvars;
+    for (int d = 0; d < c.ndims; d++) nint *= c.dim[d];
+    const double* src = uex;
+    if (mem == GB_MEM_HOST) {
+      ce = cudaMallocAsync((void**)&tmp, nint * sizeof(double), e->stream);
+      if (ce == cudaSuccess) ce = cudaMemcpyAsync(tmp, uex, nint * sizeof(double), cudaMemcpyHostToDevice, e->stream);
+      src = tmp;
+    }
+    if (ce == cudaSuccess) ce = launch_pack(ex, src, md.G, c.nvars, 0, e->stream);
+  }
+  int rc = GB_OK;
+  if (ce != cudaSuccess) {
+    gbh_set_error("gb_ensemble_error: %s", cudaGetErrorString(ce));
+    rc = GB_ERR_CUDA;
+  } else {
+    rc = grid_error(e->d_u + md.off, ex, md.G, c.nvars, e->d_red, e->stream, err);
+  }
+  if (tmp) cudaFreeAsync(tmp, e->stream);
+  cudaFreeAsync(ex, e->stream);
+  return rc;
+}
+
 extern "C" int gb_ensemble_conservation_begin(gb_ensemble* e) {
   if (!e) { gbh_set_error("gb_ensemble_conservation_begin: null ensemble"); return GB_ERR_ARG; }
   if (!e->d_bnd) {

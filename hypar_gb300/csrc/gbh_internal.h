@@ -100,6 +100,8 @@ int cons_volume(const double* u, const double* dxinv, const DevGeom& G, long lon
 int cons_error(const gb_config& c, const double* bnd, const long long* off, const double* V, const double* V0,
                const double* dxmid, double* red, cudaStream_t st, double* err);
 constexpr int CONS_RED_DOUBLES = 3 * 1024;  // the reduction buffer cons_volume / cons_error need
+int grid_error(const double* u, const double* uex, const DevGeom& G, int nv, double* red, cudaStream_t st,
+               double* err);
 
 }  // namespace gbh
 

@@ -295,6 +295,38 @@ extern "C" int gb_solver_step_report(gb_solver* s, int nsteps, double* cfl, doub
   return GB_OK;
 }
 
+namespace gbh {
+// CalculateError.c:27-110 on one grid: relative L1 / L2 / Linf of u - uex (both
+// ghosted device arrays; relative when the exact solution's norms exceed 1e-15).
+int grid_error(const double* u, const double* uex, const DevGeom& G, int nv, double* red, cudaStream_t st,
+               double* err) {
+  long long n = (long long)G.dim[0] * G.dim[1] * G.dim[2];
+  long long b = (n + RED_BLOCK - 1) / RED_BLOCK;
+  const int nb = (int)(b < RED_MAX_BLOCKS ? (b < 1 ? 1 : b) : RED_MAX_BLOCKS);
+  double ex[3], df[3];
+  for (int pass = 0; pass < 2; pass++) {
+    norms_kernel<<<nb, RED_BLOCK, 0, st>>>(pass ? u : uex, pass ? uex : nullptr, G, nv, red);
+    finish_kernel<<<1, RED_BLOCK, 0, st>>>(red, nb);
+    MK(cudaGetLastError());
+    MK(cudaMemcpyAsync(pass ? df : ex, red, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    MK(cudaStreamSynchronize(st));
+  }
+  double np = 1.0;
+  for (int d = 0; d < G.nd; d++) np *= (double)G.dim[d];
+  const double nrm[3] = {ex[0] / np, std::sqrt(ex[1] / np), ex[2]};
+  err[0] = df[0] / np;
+  err[1] = std::sqrt(df[1] / np);
+  err[2] = df[2];
+  const double tol = 1e-15;  // CalculateError.c:48
+  if (nrm[0] > tol && nrm[1] > tol && nrm[2] > tol) {
+    err[0] /= nrm[0];
+    err[1] /= nrm[1];
+    err[2] /= nrm[2];
+  }
+  return GB_OK;
+}
+}  // namespace gbh
+
 extern "C" int gb_solver_error(gb_solver* s, const double* uex, int layout, int mem, double* err) {
   if (!s || !uex || !err) { gbh_set_error("gb_solver_error: null argument"); return GB_ERR_ARG; }
   if (!s->d_snap) MK(cudaMalloc((void**)&s->d_snap, s->nvals * sizeof(double)));

@@ -157,14 +157,23 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
   if (!rc) rc = gb_ensemble_sync(e);
   clock_gettime(CLOCK_MONOTONIC, &t1);
   const double runtime = (t1.tv_sec - t0.tv_sec) + 1e-9 * (t1.tv_nsec - t0.tv_nsec);
-  /* per member: errors_<k>.dat (no exact solution: -1), conservation_<k>.dat,
+  /* per member: errors_<k>.dat (-1 without exact_<k>.inp), conservation_<k>.dat,
      function_counts_<k>.dat */
   for (int m = 0; m < nsims && !rc; m++) {
     char suffix[32];
     snprintf(suffix, sizeof(suffix), "_%0*d", width, m);
-    double cons[5];
+    double cons[5], err[3] = {-1.0, -1.0, -1.0};
     if (cf[m].cons_check) rc = gb_ensemble_conservation_error(e, m, cons);
     if (!rc) rc = write_counts(dir, suffix, &cf[m], cf[m].cons_check ? cons : NULL, cf[m].n_iter);
+    /* CalculateError.c:42-47: exact_<k>.inp of each member */
+    if (!rc && gb_inputs_exact(in[m]))
+      rc = gb_ensemble_error(e, m, gb_inputs_exact(in[m]), GB_LAYOUT_INTERIOR, GB_MEM_HOST, err);
+    if (!rc && verbose && err[0] >= 0) {
+      printf("Computed errors for domain %d:\n", m);
+      printf("  L1         Error           : %1.16E\n", err[0]);
+      printf("  L2         Error           : %1.16E\n", err[1]);
+      printf("  Linfinity  Error           : %1.16E\n", err[2]);
+    }
     if (!rc) {
       char path[4400];  /* errors_<k>.dat */
       if (dir && dir[0]) snprintf(path, sizeof(path), "%s/errors%s.dat", dir, suffix);
@@ -178,7 +187,7 @@ static int run_ensemble(const char *dir, int device, int verbose, int nsims) {
       for (int d = 0; d < cf[m].ndims; d++) fprintf(out, "%4d ", cf[m].dim[d]);
       for (int d = 0; d < cf[m].ndims; d++) fprintf(out, "%4d ", 1);
       fprintf(out, "%1.16E  ", cf[m].dt);
-      fprintf(out, "%1.16E %1.16E %1.16E   ", -1.0, -1.0, -1.0);
+      fprintf(out, "%1.16E %1.16E %1.16E   ", err[0], err[1], err[2]);
       fprintf(out, "%1.16E %1.16E\n", runtime, runtime);
       fclose(out);
     }

@@ -235,6 +235,8 @@ int gb_ensemble_get_launch(gb_ensemble *e, int dir, int *seg, int *block);
 /* Choose seg/block (walker or tiles) per direction by timing graph-replayed steps
  * (state restored). */
 int gb_ensemble_autotune(gb_ensemble *e, int reps);
+/* CalculateError of one member against its exact solution (as gb_solver_error). */
+int gb_ensemble_error(gb_ensemble *e, int member, const double *uex, int layout, int mem, double *err);
 /* The conservation check of every member (as gb_solver_conservation_*). */
 int gb_ensemble_conservation_begin(gb_ensemble *e);
 int gb_ensemble_conservation_error(gb_ensemble *e, int member, double *err);

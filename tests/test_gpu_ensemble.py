@@ -103,3 +103,35 @@ def test_ensemble_golden_run_case(built_lib, tmp_path):
         for k in range(len(members)):
             op = C.read_op_bin(os.path.join(d, f"op_{k}.bin"))
             assert relerr(op["u"], g[f"uN_{k}"]) <= 1e-10
+
+
+def test_ensemble_error_and_counts_files(built_lib, tmp_path):
+    """An ensemble deck with exact_<k>.inp per member: errors_<k>.dat equals the
+    single-grid run's errors.dat (CalculateError per member), and conservation_<k>.dat /
+    function_counts_<k>.dat are written per member."""
+    members = C.ensemble_vortex(3, sizes=[16, 24, 20], n_iter=3, seed=9)
+    d = str(tmp_path / "ens")
+    C.write_ensemble(members, d)
+
+    def exact_bytes(c):
+        xs = np.concatenate([np.asarray(x, np.float64) for x in c.x])
+        return xs.tobytes() + np.ascontiguousarray(c.u * 1.01).tobytes()
+
+    for k, c in enumerate(members):
+        with open(os.path.join(d, f"exact_{k}.inp"), "wb") as f:
+            f.write(exact_bytes(c))
+    run_case(d)
+    for k, c in enumerate(members):
+        sd = str(tmp_path / f"m{k}")
+        c.write(sd)
+        with open(os.path.join(sd, "exact.inp"), "wb") as f:
+            f.write(exact_bytes(c))
+        run_case(sd)
+        ens = open(os.path.join(d, f"errors_{k}.dat")).read().split()
+        one = open(os.path.join(sd, "errors.dat")).read().split()
+        # sizes, iproc, dt, L1, L2, Linf (the runtimes differ)
+        assert ens[:2 * 2 + 4] == one[:2 * 2 + 4]
+        assert float(ens[2 * 2 + 1]) > 0
+        cons = open(os.path.join(d, f"conservation_{k}.dat")).read().split()[2 * 2 + 1:]
+        assert [float(v) for v in cons] == [-1.0] * 4
+        assert open(os.path.join(d, f"function_counts_{k}.dat")).read().split() == ["3", "9", "0", "0"]
