@@ -28,7 +28,7 @@ EXPORTS = [
     "gb_inputs_u0", "gb_rk_table", "gb_solver_create", "gb_solver_destroy", "gb_solver_config",
     "gb_solver_set_stream", "gb_solver_sync", "gb_solver_set_state", "gb_solver_get_state", "gb_solver_state",
     "gb_solver_step", "gb_solver_time", "gb_solver_set_launch", "gb_solver_check_finite", "gb_run_case",
-    "gb_write_binary", "gb_write_text", "gb_write_tecplot", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
+    "gb_write_binary", "gb_write_text", "gb_write_tecplot", "gb_diff_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
     "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_SetInterpLimiterVar", "gb_InterpolateInterfacesHyp", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
     "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
     "gb_solver_get_launch", "gb_solver_autotune", "gb_inputs_nsims", "gb_inputs_read_member",
@@ -113,6 +113,7 @@ def lib():
     L.gb_run_case.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int]
     L.gb_write_binary.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), DP, DP]
     L.gb_write_text.argtypes = L.gb_write_binary.argtypes
+    L.gb_diff_binary.argtypes = [ctypes.c_char_p, ctypes.c_char_p, DP, DP]
     L.gb_write_tecplot.argtypes = L.gb_write_binary.argtypes
     L.gb_HyperbolicFunction.argtypes = [VP, VP, VP, VP, ctypes.c_double, ctypes.c_int, VP, VP]
     for n in ("gb_ParabolicFunction", "gb_SourceFunction", "gb_RHSFunctionExplicit"):

@@ -866,6 +866,82 @@ int gb_write_tecplot(const char *path, int ndims, int nvars, const int *dim, con
   return GB_OK;
 }
 
+/* A binary solution file (WriteBinary.c layout): ndims, nvars, dims, x, u. */
+static int read_binary_solution(const char *path, int *ndims, int *nvars, int *dim, double **u, long *n) {
+  FILE *in = fopen(path, "rb");
+  if (!in) {
+    gbh_set_error("could not open %s", path);
+    return GB_ERR_INPUT;
+  }
+  int ok = fread(ndims, sizeof(int), 1, in) == 1 && fread(nvars, sizeof(int), 1, in) == 1 && *ndims >= 1 &&
+           *ndims <= 3 && *nvars >= 1 && fread(dim, sizeof(int), *ndims, in) == (size_t)*ndims;
+  long nx = 0, np = 1;
+  for (int d = 0; ok && d < *ndims; d++) {
+    if (dim[d] < 1) ok = 0;
+    nx += dim[d];
+    np *= dim[d];
+  }
+  double *buf = ok ? (double *)malloc(sizeof(double) * (nx + np * (*nvars))) : NULL;
+  ok = ok && buf && fread(buf, sizeof(double), nx + np * (*nvars), in) == (size_t)(nx + np * (*nvars));
+  fclose(in);
+  if (!ok) {
+    free(buf);
+    gbh_set_error("%s is not a HyPar binary solution file", path);
+    return GB_ERR_INPUT;
+  }
+  memmove(buf, buf + nx, sizeof(double) * np * (*nvars));
+  *u = buf;
+  *n = np;
+  return GB_OK;
+}
+
+int gb_diff_binary(const char *sol_path, const char *ref_path, double *abs_norms, double *rel_norms) {
+  /* Extras/hyparDiff.c:272-371: d = ref - sol; L1 = sum|d| / npoints, L2 = sqrt(sum d^2 /
+   * npoints), Linf = max|d| over every variable; relative to the reference's own norms
+   * when all three exceed 1e-14, else the absolute ones. */
+  if (!sol_path || !ref_path || !abs_norms || !rel_norms) {
+    gbh_set_error("gb_diff_binary: null argument");
+    return GB_ERR_ARG;
+  }
+  int nd1, nv1, nd2, nv2, d1[3], d2[3];
+  double *a = NULL, *b = NULL;
+  long n1, n2;
+  int rc = read_binary_solution(sol_path, &nd1, &nv1, d1, &a, &n1);
+  if (!rc) rc = read_binary_solution(ref_path, &nd2, &nv2, d2, &b, &n2);
+  if (!rc && (nd1 != nd2 || nv1 != nv2)) {
+    gbh_set_error("%s and %s differ in ndims or nvars", sol_path, ref_path);
+    rc = GB_ERR_INPUT;
+  }
+  for (int d = 0; !rc && d < nd1; d++)
+    if (d1[d] != d2[d]) {
+      gbh_set_error("%s and %s differ in size", sol_path, ref_path);
+      rc = GB_ERR_INPUT;
+    }
+  if (!rc) {
+    const long size = n2 * nv2;
+    double s1 = 0.0, s2 = 0.0, mx = 0.0, e1 = 0.0, e2 = 0.0, emx = 0.0;
+    for (long i = 0; i < size; i++) {
+      const double r = b[i], dd = r - a[i];
+      s1 += fabs(r);
+      s2 += r * r;
+      if (fabs(r) > mx) mx = fabs(r);
+      e1 += fabs(dd);
+      e2 += dd * dd;
+      if (fabs(dd) > emx) emx = fabs(dd);
+    }
+    const double np = (double)n2, tol = 1e-14;
+    const double nrm[3] = {s1 / np, sqrt(s2 / np), mx};
+    abs_norms[0] = e1 / np;
+    abs_norms[1] = sqrt(e2 / np);
+    abs_norms[2] = emx;
+    for (int k = 0; k < 3; k++)
+      rel_norms[k] = (nrm[0] > tol && nrm[1] > tol && nrm[2] > tol) ? abs_norms[k] / nrm[k] : abs_norms[k];
+  }
+  free(a);
+  free(b);
+  return rc;
+}
+
 int gb_op_to_initial(const char *op_path, const char *initial_path) {
   /* Extras/BinaryOPToInitialSolution.c: the header (ndims, nvars, dims) is
    * dropped, x and u are written as a binary initial.inp. */

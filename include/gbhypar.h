@@ -255,6 +255,11 @@ int gb_write_binary(const char *path, int ndims, int nvars, const int *dim, cons
  * and 3-D grids). */
 int gb_write_text(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
 int gb_write_tecplot(const char *path, int ndims, int nvars, const int *dim, const double *x, const double *u);
+/* Compare two binary solution files as the reference's Extras/hyparDiff.c does: the
+ * L1 / L2 / Linf norms of (ref - sol) over every variable, absolute and relative to the
+ * reference's norms (absolute when any of those is below 1e-14).  GB_ERR_INPUT when the
+ * files differ in ndims, nvars or size. */
+int gb_diff_binary(const char *sol_path, const char *ref_path, double *abs_norms, double *rel_norms);
 /* Convert a binary solution file (op*.bin) into a binary initial.inp, for a
  * restart (the reference's Extras/BinaryOPToInitialSolution.c). */
 int gb_op_to_initial(const char *op_path, const char *initial_path);

@@ -64,3 +64,51 @@ def test_run_case_writes_the_reference_formats(built_lib, tmp_path, name):
         assert np.array_equal(got[:, :2 * nd], ref[:, :2 * nd])
         err = np.linalg.norm(got[:, 2 * nd:] - ref[:, 2 * nd:]) / np.linalg.norm(ref[:, 2 * nd:])
         assert err <= 1e-10, err
+
+
+def _bin(path, case, u):
+    L = _lib.lib()
+    d = (ctypes.c_int * case.ndims)(*case.size)
+    x = np.concatenate([np.asarray(xx, dtype=np.float64) for xx in case.x])
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    _lib.check(L.gb_write_binary(path.encode(), case.ndims, case.nvars, d, x.ctypes.data_as(_lib.DP),
+                                 u.ctypes.data_as(_lib.DP)))
+
+
+def test_diff_binary_is_hypardiff(built_lib, tmp_path):
+    """gb_diff_binary / `gbhypar diff` against the norms of Extras/hyparDiff.c (restated
+    here with numpy) and, where the reference was built here, against its own tool's
+    output, line for line."""
+    import subprocess
+    from hypar_gb300 import cases as C
+    from hypar_gb300.build import CLI
+    case = C.vortex(12, n_iter=1, dt=0.01)
+    rng = np.random.default_rng(5)
+    ref = case.u.copy()
+    sol = ref * (1.0 + 1e-9 * rng.standard_normal(ref.shape))
+    a, b = str(tmp_path / "sol.bin"), str(tmp_path / "ref.bin")
+    _bin(a, case, sol)
+    _bin(b, case, ref)
+    L = _lib.lib()
+    ab, rl = (ctypes.c_double * 3)(), (ctypes.c_double * 3)()
+    _lib.check(L.gb_diff_binary(a.encode(), b.encode(), ab, rl))
+    d = (ref - sol).reshape(-1)
+    npts = ref.shape[0]
+    want_abs = [np.abs(d).sum() / npts, np.sqrt((d * d).sum() / npts), np.abs(d).max()]
+    r = ref.reshape(-1)
+    nrm = [np.abs(r).sum() / npts, np.sqrt((r * r).sum() / npts), np.abs(r).max()]
+    assert np.allclose(list(ab), want_abs, rtol=1e-12, atol=0)
+    assert np.allclose(list(rl), [x / y for x, y in zip(want_abs, nrm)], rtol=1e-12, atol=0)
+    # a size mismatch is an input error
+    small = C.vortex(8, n_iter=1, dt=0.01)
+    c = str(tmp_path / "small.bin")
+    _bin(c, small, small.u)
+    assert L.gb_diff_binary(a.encode(), c.encode(), ab, rl) != 0
+    out = subprocess.run([CLI, "diff", "-r", "1e-12", a, b], capture_output=True, text=True, check=True).stdout
+    assert "differ." in out and "(rel)" in out
+    same = subprocess.run([CLI, "diff", b, b], capture_output=True, text=True, check=True).stdout
+    assert same == ""
+    tool = os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "_ref", "hyparDiff")
+    if os.path.exists(tool):
+        theirs = subprocess.run([tool, "-r", "1e-12", a, b], capture_output=True, text=True, check=True).stdout
+        assert out == theirs
