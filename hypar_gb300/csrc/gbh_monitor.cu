@@ -346,23 +346,9 @@ extern "C" int gb_solver_error(gb_solver* s, const double* uex, int layout, int 
     MK(launch_pack(s->d_snap, src, s->G, s->cfg.nvars, 0, s->stream));
     if (tmp) MK(cudaFreeAsync(tmp, s->stream));
   }
-  int rc = GB_OK;
-  double ex[3], df[3];
-  rc = norms_launch(s, s->d_snap, nullptr, ex);
-  if (!rc) rc = norms_launch(s, s->d_u, s->d_snap, df);
+  int rc = red_buffer(s);
   if (rc) return rc;
-  const double np = npoints(s);
-  const double nrm[3] = {ex[0] / np, std::sqrt(ex[1] / np), ex[2]};
-  err[0] = df[0] / np;
-  err[1] = std::sqrt(df[1] / np);
-  err[2] = df[2];
-  const double tol = 1e-15;  // CalculateError.c:48, relative errors when the exact norms exceed it
-  if (nrm[0] > tol && nrm[1] > tol && nrm[2] > tol) {
-    err[0] /= nrm[0];
-    err[1] /= nrm[1];
-    err[2] /= nrm[2];
-  }
-  return GB_OK;
+  return grid_error(s->d_u, s->d_snap, s->G, s->cfg.nvars, s->d_red, s->stream, err);
 }
 
 // ---------------------------------------------------------------------------
