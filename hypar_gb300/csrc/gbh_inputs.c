@@ -123,7 +123,7 @@ typedef struct {
   double dt;
   char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
   char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
-  char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS], op_format[MAXS];
+  char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS], op_format[MAXS], input_mode[MAXS];
 } solver_inp;
 
 static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsims) {
@@ -147,6 +147,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   strcpy(si->hyp_flux_split, "no");
   strcpy(si->cons_check, "no");
   strcpy(si->op_format, "text");  /* ReadInputs.c:140 */
+  strcpy(si->input_mode, "serial");
   FILE *in = open_in(dir, "solver.inp", "r");
   if (!in) {
     gbh_set_error("file solver.inp not found");
@@ -201,6 +202,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
       char mode[MAXS];
       r = fscanf(in, "%511s", mode);
       if (r == 1 && strcmp(mode, "serial")) { int nio; r = fscanf(in, "%d", &nio); }
+      if (r == 1 && !strcmp(w, "input_mode")) snprintf(si->input_mode, MAXS, "%s", mode);
     } else {
       char useless[MAXS];  /* every other keyword takes one value */
       r = fscanf(in, "%511s", useless);
@@ -470,6 +472,25 @@ static void member_name(char *out, size_t sz, const char *root, int member, int 
   snprintf(out, sz, "%s_%0*d.inp", root, width, member);
 }
 
+/* The solution file of solver.inp's input_mode (ReadArray.c:41-56): serial reads
+ * <root>.inp in ip_file_type; "parallel" the one I/O rank's binary file
+ * <root>_par.inp.0000 (ReadArrayParallel, :355-380: its grid then its solution,
+ * which on one rank is the whole of each); "mpi-io" the binary <root>_mpi.inp
+ * (ReadArrayMPI_IO, :532-540). */
+static const char *input_file(char *out, size_t sz, const char *root, int member, int nsims, const char *mode,
+                              const char *ip_type) {
+  char base[240];
+  member_name(base, sizeof(base), root, member, nsims);
+  if (!strcmp(mode, "serial")) {
+    snprintf(out, sz, "%s", base);
+    return ip_type;
+  }
+  base[strlen(base) - 4] = 0;  /* drop ".inp" */
+  if (!strcmp(mode, "parallel")) snprintf(out, sz, "%s_par.inp.0000", base);
+  else snprintf(out, sz, "%s_mpi.inp", base);
+  return "binary";
+}
+
 int gb_inputs_read(const char *dir, gb_inputs **out) { return gb_inputs_read_member(dir, 0, 1, out); }
 
 int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **out) {
@@ -645,10 +666,15 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
 
   /* initial.inp, and exact.inp when present (ExactSolution.c, same format) */
   char iname[256], bname[256], ename[256];
-  member_name(iname, sizeof(iname), "initial", member, nsims);
+  if (strcmp(si.input_mode, "serial") && strcmp(si.input_mode, "parallel") && strcmp(si.input_mode, "mpi-io")) {
+    gbh_set_error("input_mode %s invalid (serial, parallel, mpi-io)", si.input_mode);
+    gb_inputs_free(res);
+    return GB_ERR_INPUT;
+  }
+  const char *itype = input_file(iname, sizeof(iname), "initial", member, nsims, si.input_mode, si.ip_file_type);
   member_name(bname, sizeof(bname), "boundary", member, nsims);
-  member_name(ename, sizeof(ename), "exact", member, nsims);
-  rc = read_solution(dir, iname, si.ip_file_type, nx, npts, c.nvars, res->x, res->u0, 1);
+  const char *etype = input_file(ename, sizeof(ename), "exact", member, nsims, si.input_mode, si.ip_file_type);
+  rc = read_solution(dir, iname, itype, nx, npts, c.nvars, res->x, res->u0, 1);
   if (rc) {
     gb_inputs_free(res);
     return rc;
@@ -656,7 +682,7 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   {
     double *xd = (double *)calloc(nx, sizeof(double));
     double *ue = (double *)calloc(npts * c.nvars, sizeof(double));
-    rc = read_solution(dir, ename, si.ip_file_type, nx, npts, c.nvars, xd, ue, 0);
+    rc = read_solution(dir, ename, etype, nx, npts, c.nvars, xd, ue, 0);
     free(xd);
     if (rc == GB_OK) {
       res->uex = ue;

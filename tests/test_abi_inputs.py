@@ -170,6 +170,31 @@ def test_reader_conservation_check(built_lib, tmp_path):
         L.gb_inputs_free(inp_h)
 
 
+@pytest.mark.parametrize("mode,fname", [("parallel", "initial_par.inp.0000"), ("mpi-io", "initial_mpi.inp")])
+def test_reader_input_modes(built_lib, tmp_path, mode, fname):
+    """solver.inp input_mode parallel / mpi-io: on one rank the initial solution comes from
+    initial_par.inp.0000 / initial_mpi.inp (binary: grid, then solution), exact.inp likewise."""
+    case = C.vortex(12, n_iter=1, dt=0.01)
+    d = str(tmp_path / "deck")
+    case.write(d)
+    txt = open(os.path.join(d, "solver.inp")).read().replace("end", f"  input_mode {mode} 1\nend")
+    open(os.path.join(d, "solver.inp"), "w").write(txt)
+    os.rename(os.path.join(d, "initial.inp"), os.path.join(d, fname))
+    xs = np.concatenate([np.asarray(x, np.float64) for x in case.x])
+    with open(os.path.join(d, fname.replace("initial", "exact")), "wb") as f:
+        f.write(xs.tobytes() + np.ascontiguousarray(case.u * 2.0).tobytes())
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    _lib.check(L.gb_inputs_read(d.encode(), ctypes.byref(h)))
+    n = case.u.size
+    assert np.array_equal(np.ctypeslib.as_array(L.gb_inputs_u0(h), shape=(n,)), case.u.reshape(-1))
+    assert np.array_equal(np.ctypeslib.as_array(L.gb_inputs_exact(h), shape=(n,)), 2.0 * case.u.reshape(-1))
+    L.gb_inputs_free(h)
+    # the serial file name is not read in these modes
+    os.rename(os.path.join(d, fname), os.path.join(d, "initial.inp"))
+    assert L.gb_inputs_read(d.encode(), ctypes.byref(h)) != 0
+
+
 def test_op_to_initial_round_trip(built_lib, tmp_path):
     """gb_write_binary -> gb_op_to_initial -> the deck reader gives back x and u."""
     case = C.vortex(10, n_iter=1, dt=0.01)
