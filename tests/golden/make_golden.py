@@ -5,8 +5,11 @@ compiled from the reference sources by oracle/Makefile.ref) on small input
 decks written by hypar_gb300.cases, single-threaded (OMP_NUM_THREADS=1: the
 reference's OpenMP build races on shared scratch in
 WENOFifthOrderCalculateWeightsCharJS), and stores, per case, the initial
-interior solution, the reference right-hand side of that state (interior) and
-the reference solution after n_iter Runge-Kutta steps (op.bin).
+interior solution, the reference right-hand side of that state (interior), the
+reference solution after n_iter Runge-Kutta steps (op.bin), its CFL, and the
+conservation errors and function counts it wrote (conservation.dat,
+function_counts.dat); for OUTPUTS the header lines and numbers of its text and
+Tecplot solution files; for ENSEMBLES every member's op_<k>.bin.
 
     make -f oracle/Makefile.ref REF=<hypar source tree> -j8
     python tests/golden/make_golden.py
