@@ -296,7 +296,9 @@ int gb_Upwind(double *fI, double *fL, double *fR, double *uL, double *uR, double
               double t);
 /* SetInterpLimiterVar (include/hypar.h:234): checks its arguments; the WENO5 weights
  * the reference stores here are evaluated by gb_InterpolateInterfacesHyp from the same
- * fC and u (HyperbolicFunction.c:201-215 passes the same arrays to both). */
+ * fC and u (HyperbolicFunction.c:201-215 passes the same arrays to both on the explicit
+ * path, LimFlag = 1).  Weights frozen across calls (LimFlag = 0, which only HyPar's
+ * implicit time integrators use) are not kept. */
 int gb_SetInterpLimiterVar(double *fC, double *u, double *x, int dir, void *s, void *m);
 /* InterpolateInterfacesHyp (include/hypar.h:224; Interp1PrimFifthOrderWENO.c,
  * Interp1PrimFifthOrderWENOChar.c): WENO5 values fI at the interfaces along dir
