@@ -7,7 +7,15 @@ characteristic WENO5 (Jiang-Shu) + Roe, SSPRK3, dt at CFL 0.5, FP64.  A
 "step" is one SSPRK3 step of that grid.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload vortex|tgv|sod|ensemble|adjoint|convergence]
+                  [--workload vortex|tgv|sod|rtb|rtb64|dns|dns64cr|ensemble|adjoint|
+                              convergence|parity|kernel-vjp|kernel-jvp|kernel-step]
+
+The default line also carries the metric's other two parts, measured after the
+timed region on reduced step counts: an "ensemble" block (batched vs one at a
+time) and an "adjoint" block (gradient and backward cost over the forward solve,
+central-difference and dot-product checks).  --workload parity prints where the
+per-right-hand-side distance from the oracle comes from; kernel-* only launch one
+entry point for profilers.
 
 --impl ours       the fused CUDA path through libgbhypar's C ABI (value: device
                   time of the resident solution; e2e: host buffers copied in and
@@ -38,14 +46,14 @@ UNIT = "cell-component updates/s"
 # FP64 floating-point operations per interface per direction of the fused
 # kernels (FMA = 2), from one ncu capture of the x and y launches (FP64-pipe
 # instructions x elapsed cycles, DFMA share from the dfma counter; mean of the
-# two directions, profiles/hyp_dir_kernel_euler2d_char_roe_vortex2048_ncu_full.md);
+# two directions of a 2048^2 capture of the segment-walker form);
 # per cell per step this is x (ndims * nstages).  FP64 instructions likewise.
 FP64_FLOPS_PER_INTERFACE = {"vortex": 1607.3}
 FP64_INSTR_PER_INTERFACE = {"vortex": 1005.6}
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
 # update), per kernel form: the segment walker from the same 2048^2 capture (traffic
 # proportional to cells at these sizes), the tile form from a capture of the default
-# 1024^2 run (profiles/hyp_tile_kernel_euler2d_char_roe_vortex1024_ncu_full.md).
+# 1024^2 run.
 DRAM_BYTES_PER_CELL = {"vortex": {("hyp_x", "walker"): 56.13, ("hyp_y", "walker"): 149.99,
                                   ("hyp_y", "tile"): 112.57}}
 TRAFFIC_SOURCE = {"walker": "a 2048^2 capture of the segment-walker form, scaled by cells",
@@ -200,6 +208,16 @@ def stage_bytes(cfg, s) -> float:
     return 8.0 * nv * (reads + writes)
 
 
+def common_config(case, desc, args, ws) -> dict:
+    """The config object both arms print (the same keys and values for the same
+    workload, so that the two lines can be matched)."""
+    import numpy as np
+    return {"workload": desc, "cells": int(np.prod(case.size)), "nvars": case.nvars, "dt": case.dt,
+            "steps": args.steps, "parallelism": f"replicas x{ws}" if ws > 1 else "one device",
+            "l2": ("GPU arm: a 256 MB buffer written between timed steps (L2 flush); CPU arm: state "
+                   "arrays larger than the host caches at the full sizes")}
+
+
 def run_ours(args, case, desc, ws, rank, local):
     import ctypes
     import numpy as np
@@ -337,10 +355,7 @@ def run_ours(args, case, desc, ws, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "cells": cells, "nvars": nv, "dt": case.dt, "steps": args.steps,
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                   "launch_seg_block_per_dir": tuned,
-                   "l2": "256 MB buffer written between timed steps (L2 flush)"},
+        "config": common_config(case, desc, args, ws), "launch_seg_block_per_dir": tuned,
         "hbm_pct_step": 100.0 * (step_bytes / (t_dev / args.steps)) / 1e9 / hbm_peak,
         "roofline": roofline, "roofline_fp64": roofline_fp64,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": cells * nv * 8,
@@ -353,6 +368,23 @@ def run_ours(args, case, desc, ws, rank, local):
     if pub and not args.size:
         out["vs_baseline"] = value / pub[0]
         out["baseline_published"] = {"value": pub[0], "unit": UNIT, "hardware": pub[1]}
+    if args.workload == "vortex" and ws == 1 and not args.size and not args.no_extras:
+        # the metric's other two parts, measured after the timed region on reduced step
+        # counts (stated in each block) so that the default run stays within minutes
+        from hypar_gb300 import cases as C
+        members = C.ensemble_vortex(64, n_iter=100)
+        m = ensemble_measure(members, steps=3, warmup=1, local=local)
+        out["ensemble"] = ensemble_summary(m, len(members), 3)
+        out["ensemble"]["workload"] = ENSEMBLE_DESC
+        out["ensemble"]["reduced"] = "3 timed steps (1 warm-up) per arm instead of 100"
+        torch.cuda.set_stream(stream)
+        block, _ = adjoint_measure(256, 400, 1, local, policies=("sqrt",), fd_directions=4,
+                                   fd_kinds=("smooth", "noise"))
+        block["workload"] = ADJOINT_DESC.format(n=256, nsteps=400)
+        block["reduced"] = ("1 timed gradient (2 warm-up), sqrt checkpointing only, 4 central-difference "
+                            "directions per kind instead of 16")
+        out["adjoint"] = block
+        torch.cuda.set_stream(stream)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, budget_s=args.cpu_budget)
     if dist:
@@ -360,30 +392,16 @@ def run_ours(args, case, desc, ws, rank, local):
     return out
 
 
-def run_ensemble(args, ws, rank, local):
-    """64 isentropic vortices of seeded sizes {128..1024}: one batched ensemble
-    (one launch per direction per stage, CUDA graph) against the same members
-    advanced one at a time by single-grid solvers (each autotuned).  Over N GPUs
-    the members are partitioned by cell count (every rank builds the whole
-    seeded ensemble, so dt is the full ensemble's, and keeps its share); the
-    job's time is the slowest rank's."""
-    import numpy as np
+def ensemble_measure(members, steps: int, warmup: int, local: int, dist=None):
+    """One batched ensemble (one launch per direction per stage, CUDA graph, autotuned)
+    against the same members advanced one at a time by single-grid solvers, each with
+    the default launch shape and with its size's autotuned shape.  Returns the times
+    per step (seconds, max over ranks) and the batched launch shape."""
     import torch
     from hypar_gb300 import cases as C
     from hypar_gb300 import replicas as R
     from hypar_gb300.solver import Ensemble, Solver
 
-    torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    everyone = C.ensemble_vortex(args.members, n_iter=100)
-    total_cells = sum(int(np.prod(c.size)) for c in everyone)
-    mine = R.shard_members([int(np.prod(c.size)) for c in everyone], ws)[rank]
-    if not mine:
-        raise SystemExit(f"rank {rank}: no ensemble member for this rank ({len(everyone)} members, {ws} ranks)")
-    members = [everyone[k] for k in mine]
     tmp = tempfile.mkdtemp(prefix="gbh_ens_")
     C.write_ensemble(members, tmp)
     stream = torch.cuda.Stream()
@@ -392,15 +410,15 @@ def run_ensemble(args, ws, rank, local):
     e.set_stream(stream.cuda_stream)
     tuned = e.autotune(1)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         e.step(1)
     torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for k in range(args.steps):
+        for k in range(steps):
             flush.fill_(float(k))
             ev[k][0].record(stream)
             e.step(1)
@@ -408,8 +426,8 @@ def run_ensemble(args, ws, rank, local):
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    t_b = R.max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps, dist, "cuda")
-    # one at a time: every member by its own single-grid solver, launch shape tuned per size
+    t_b = R.max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / 1e3 / steps, dist, "cuda")
+    e.close()
     tune_cache = {}
     t_s = 0.0   # one at a time, launch shape tuned per size (strongest single-grid baseline)
     t_d = 0.0   # one at a time, default launch shape (what gb_run_case does per deck)
@@ -429,10 +447,10 @@ def run_ensemble(args, ws, rank, local):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             flush.fill_(1.0)
             a.record(stream)
-            s.step(args.steps)
+            s.step(steps)
             b.record(stream)
             torch.cuda.synchronize()
-            dt_ = a.elapsed_time(b) / 1e3 / args.steps
+            dt_ = a.elapsed_time(b) / 1e3 / steps
             if tuned_run:
                 t_s += dt_
             else:
@@ -440,42 +458,81 @@ def run_ensemble(args, ws, rank, local):
         s.close()
     t_s = R.max_over_ranks(t_s, dist, "cuda")
     t_d = R.max_over_ranks(t_d, dist, "cuda")
+    return {"t_batched": t_b, "t_tuned": t_s, "t_default": t_d, "tuned": tuned, "clocks": clk.summary()}
+
+
+def ensemble_summary(m, nmembers: int, steps: int) -> dict:
+    return {"batched_ms_per_step": m["t_batched"] * 1e3,
+            "one_at_a_time_default_shape_ms_per_step": m["t_default"] * 1e3,
+            "batched_vs_one_at_a_time_default_shape_speedup": m["t_default"] / m["t_batched"],
+            "one_at_a_time_tuned_ms_per_step": m["t_tuned"] * 1e3,
+            "batched_vs_one_at_a_time_tuned_speedup": m["t_tuned"] / m["t_batched"],
+            "launches_per_step_batched": 2 * 3, "launches_per_step_one_at_a_time": 2 * 3 * nmembers,
+            "timed_steps": steps, "batched_launch_seg_block_per_dir": m["tuned"]}
+
+
+def run_ensemble(args, ws, rank, local):
+    """64 isentropic vortices of seeded sizes {128..1024}: one batched ensemble
+    (one launch per direction per stage, CUDA graph) against the same members
+    advanced one at a time by single-grid solvers (each autotuned).  Over N GPUs
+    the members are partitioned by cell count (every rank builds the whole
+    seeded ensemble, so dt is the full ensemble's, and keeps its share); the
+    job's time is the slowest rank's."""
+    import numpy as np
+    import torch
+    from hypar_gb300 import cases as C
+    from hypar_gb300 import replicas as R
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    everyone = C.ensemble_vortex(args.members, n_iter=100)
+    total_cells = sum(int(np.prod(c.size)) for c in everyone)
+    mine = R.shard_members([int(np.prod(c.size)) for c in everyone], ws)[rank]
+    if not mine:
+        raise SystemExit(f"rank {rank}: no ensemble member for this rank ({len(everyone)} members, {ws} ranks)")
+    members = [everyone[k] for k in mine]
+    m = ensemble_measure(members, args.steps, args.warmup, local, dist)
     if dist:
         dist.destroy_process_group()
     if rank != 0:
         return None
+    t_b = m["t_batched"]
     value = total_cells * 4 / t_b
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_b * 1e3, "higher_is_better": True,
         "scaling": "strong" if ws > 1 else "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": (f"ensemble of {len(everyone)} Euler2D isentropic vortices, sizes seeded from "
-                                "{128,192,...,1024}^2, b~U[1,5], centre~U[3,7]^2, char-WENO5(JS)+Roe, SSPRK3, "
-                                "common dt at CFL 0.5"), "members": len(everyone), "cells": total_cells,
+        "config": {"workload": ENSEMBLE_DESC, "members": len(everyone), "cells": total_cells,
                    "sizes": [c.size[0] for c in everyone], "dt": everyone[0].dt,
                    "parallelism": (f"members partitioned over {ws} GPUs by cell count (rank 0: {len(mine)} "
                                    "members), no data exchanged" if ws > 1 else "single GPU"),
-                   "launch_seg_block_per_dir": tuned, "l2": "256 MB buffer written between timed steps"},
-        "ensemble": {"batched_ms_per_step": t_b * 1e3,
-                     "one_at_a_time_default_shape_ms_per_step": t_d * 1e3,
-                     "batched_vs_one_at_a_time_default_shape_speedup": t_d / t_b,
-                     "one_at_a_time_tuned_ms_per_step": t_s * 1e3,
-                     "batched_vs_one_at_a_time_tuned_speedup": t_s / t_b,
-                     "launches_per_step_batched": 2 * 3, "launches_per_step_one_at_a_time": 2 * 3 * len(everyone)},
-        "gpu_launches": 6 * args.steps, "clocks": clk.summary(),
+                   "launch_seg_block_per_dir": m["tuned"], "l2": "256 MB buffer written between timed steps"},
+        "ensemble": ensemble_summary(m, len(everyone), args.steps),
+        "gpu_launches": 6 * args.steps, "clocks": m["clocks"],
     }
     return out
 
 
-def run_adjoint(args, ws, rank, local):
-    """Gradient of 0.5 ||rho(T) - rho_target||^2 with respect to the initial
-    density (2D Euler 256^2 periodic, comp-WENO5 + Roe, RK4, 400 steps,
-    ceil(sqrt(400)) = 20 checkpoints) against the plain fused forward solve of
-    the same 400 steps: a "step" is one gradient evaluation (forward sweep with
-    checkpoints + backward sweep).  Also checks the gradient against central
-    differences (h = 1e-6) on 16 random density directions and the adjoint
-    against the tangent-linear model (dot-product test), on the full problem."""
+ENSEMBLE_DESC = ("ensemble of 64 Euler2D isentropic vortices, sizes seeded from {128,192,...,1024}^2, b~U[1,5], "
+                 "centre~U[3,7]^2, char-WENO5(JS)+Roe, SSPRK3, common dt at CFL 0.5")
+ADJOINT_DESC = ("adjoint: d/d rho0 of 0.5||rho(T)-rho_target||^2, Euler2D {n}x{n} periodic [0,10)^2, target "
+                "from the b=5 vortex, guess b=4 shifted by U[-0.5,0.5]^2, comp-WENO5(JS)+Roe, RK4, {nsteps} "
+                "steps, sqrt checkpointing")
+
+
+def adjoint_measure(n: int, nsteps: int, K: int, local: int, policies=("sqrt", "store_all"),
+                    fd_directions: int = 16, fd_kinds=("smooth", "smooth_unit", "noise", "noise_unit")):
+    """Gradient of 0.5 ||rho(T) - rho_target||^2 with respect to the initial density
+    (2D Euler n^2 periodic, comp-WENO5 + Roe, RK4, nsteps steps) under each
+    checkpoint policy (sqrt: ceil(sqrt(nsteps)) checkpoints; store_all: every state),
+    timed as forward sweep + backward sweep over K gradients, against the plain fused
+    forward solve of the same steps; then the sqrt gradient against central
+    differences (h = 1e-6) on fd_directions random density directions per kind, and
+    the adjoint against the tangent-linear model (dot-product test)."""
     import numpy as np
     import torch
     from hypar_gb300 import cases as C
@@ -483,9 +540,6 @@ def run_adjoint(args, ws, rank, local):
     from hypar_gb300.adjoint import Adjoint
     from hypar_gb300.solver import Inputs, Solver
 
-    torch.cuda.set_device(local)
-    n = args.size or 256
-    nsteps = 400
     case, u_true = C.adjoint_problem(n, nsteps)
     tmp = tempfile.mkdtemp(prefix="gbh_adj_")
     case.write(tmp)
@@ -498,7 +552,9 @@ def run_adjoint(args, ws, rank, local):
     fwd_shape = s.autotune(1)
     L = _lib.lib()
     results = {}
-    for ncheck, tag in ((0, "sqrt"), (1, "store_all")):
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for tag in policies:
+        ncheck = {"sqrt": 0, "store_all": 1}[tag]
         adj = Adjoint(inp.config, inp.dxinv, nsteps, ncheck=ncheck, device=local)
         adj.set_stream(stream.cuda_stream)
         for d, (sg, bl) in enumerate(fwd_shape):
@@ -514,8 +570,6 @@ def run_adjoint(args, ws, rank, local):
         ubarT = adj.empty()
         adj.interior(ubarT)[..., 0] = adj.interior(uT)[..., 0] - rho_tgt
         ub0 = adj.empty()
-        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-        K = max(1, min(args.steps, 5))
         for _ in range(2):
             adj.forward(u0, uT)
             adj.backward(ubarT, ub0)
@@ -536,11 +590,11 @@ def run_adjoint(args, ws, rank, local):
         results[tag] = {"ncheck": ncheck, "adj": adj, "t_fs": t_fs, "t_bs": t_bs, "info": info,
                         "vjp_seg": vjp_shape, "clocks": clk.summary(), "u0": u0, "u0_int": u0_int,
                         "rho_tgt": rho_tgt, "ub0": ub0.clone()}
-    # the plain forward solve: the solver's fused steps over the same 400 steps
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        if tag != policies[0]:
+            adj.close()  # only the first policy's adjoint is kept for the checks below
+    # the plain forward solve: the solver's fused steps over the same steps
     s.set_state(case.u)
     s.step(nsteps)
-    K = max(1, min(args.steps, 5))
     tf = []
     for k in range(K):
         s.set_state(case.u)
@@ -552,8 +606,9 @@ def run_adjoint(args, ws, rank, local):
         torch.cuda.synchronize()
         tf.append(a.elapsed_time(b))
     t_f = sum(tf) / K
-    # accuracy on the full problem: central differences and the dot-product test
-    R = results["sqrt"]
+    s.close()
+    # accuracy: central differences and the dot-product test, with the first policy's adjoint
+    R = results[policies[0]]
     adj, u0_int, rho_tgt = R["adj"], R["u0_int"], R["rho_tgt"]
     grad = adj.interior(R["ub0"])[..., 0]
 
@@ -576,9 +631,9 @@ def run_adjoint(args, ws, rank, local):
             f += rng.normal() * np.sin(2 * np.pi * (kx * X + ky * Y) + rng.uniform(0, 2 * np.pi))
         return torch.from_numpy(f).cuda()
 
-    fd = {"smooth": [], "smooth_unit": [], "noise": [], "noise_unit": []}
+    fd = {k: [] for k in fd_kinds}
     for kind in fd:
-        for _ in range(16):
+        for _ in range(fd_directions):
             v = smooth_field() if kind.startswith("smooth") else torch.randn((n, n), generator=gen,
                                                                                 dtype=torch.float64).cuda()
             if kind.endswith("unit"):
@@ -598,44 +653,158 @@ def run_adjoint(args, ws, rank, local):
     lhs = float((adj.interior(Mv) * adj.interior(w)).sum())
     rhs_ = float((adj.interior(v) * adj.interior(MTw)).sum())
     dot_err = abs(lhs - rhs_) / max(abs(lhs), abs(rhs_))
-    grad_ms = R["t_fs"] + R["t_bs"]
-    SA = results["store_all"]
     ns = inp.config.rk_nstages
     launches_fs = nsteps * ns * 2
     launches_bs = R["info"]["recomputed_steps"] * ns * 2 + nsteps * (ns + 1)
-    out = {
-        "metric": METRIC, "value": grad_ms / t_f, "unit": "x (gradient time / forward solve time)",
-        "n_gpus": 1, "steps": K, "warmup": 2, "ms_per_step": grad_ms, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": (f"adjoint: d/d rho0 of 0.5||rho(T)-rho_target||^2, Euler2D {n}x{n} periodic "
-                                "[0,10)^2, target from the b=5 vortex, guess b=4 shifted by U[-0.5,0.5]^2, "
-                                "comp-WENO5(JS)+Roe, RK4, 400 steps, sqrt checkpointing"),
-                   "cells": n * n, "dt": case.dt, "nsteps": nsteps,
-                   "checkpoints": R["info"]["segments"], "segment_len": R["info"]["segment_len"],
-                   "l2": "256 MB buffer written between timed gradients"},
-        "adjoint": {
-            "forward_solve_ms": t_f,
-            "sqrt": {"forward_sweep_ms": R["t_fs"], "backward_sweep_ms": R["t_bs"], "gradient_ms": grad_ms,
-                     "gradient_over_forward": grad_ms / t_f, "backward_over_forward": R["t_bs"] / t_f,
-                     "recomputed_steps": R["info"]["recomputed_steps"], "device_bytes": R["info"]["bytes"],
-                     "vjp_seg": R["vjp_seg"]},
-            "store_all": {"forward_sweep_ms": SA["t_fs"], "backward_sweep_ms": SA["t_bs"],
-                          "gradient_ms": SA["t_fs"] + SA["t_bs"],
-                          "gradient_over_forward": (SA["t_fs"] + SA["t_bs"]) / t_f,
-                          "backward_over_forward": SA["t_bs"] / t_f, "device_bytes": SA["info"]["bytes"]},
-            "fd_check": {kind: {"directions": 16, "h": h, "max_rel_err": max(e), "median_rel_err":
-                                statistics.median(e)} for kind, e in fd.items()},
-            "fd_directions": ("smooth: 6 random Fourier modes |k| <= 4 of the initial density (amplitude "
+    adj.close()
+    block = {"forward_solve_ms": t_f, "timed_gradients": K, "nsteps": nsteps, "cells": n * n}
+    for tag in policies:
+        P = results[tag]
+        g_ms = P["t_fs"] + P["t_bs"]
+        block[tag] = {"forward_sweep_ms": P["t_fs"], "backward_sweep_ms": P["t_bs"], "gradient_ms": g_ms,
+                      "gradient_over_forward": g_ms / t_f, "backward_over_forward": P["t_bs"] / t_f,
+                      "checkpoints": P["info"]["segments"], "recomputed_steps": P["info"]["recomputed_steps"],
+                      "device_bytes": P["info"]["bytes"], "vjp_seg": P["vjp_seg"]}
+    block["fd_check"] = {kind: {"directions": fd_directions, "h": h, "max_rel_err": max(e),
+                                "median_rel_err": statistics.median(e)} for kind, e in fd.items()}
+    block["fd_directions"] = ("smooth: 6 random Fourier modes |k| <= 4 of the initial density (amplitude "
                               "O(1) per cell); noise: N(0,1) in every cell; *_unit: the same scaled to unit "
-                              "2-norm (a per-cell step near 1e-6/256, where rounding in the misfit dominates "
+                              "2-norm (a per-cell step near 1e-6/n, where rounding in the misfit dominates "
                               "the difference); central differences of the misfit through the fused forward "
-                              "solve"),
-            "dot_product_rel_err": dot_err,
-            "forward_launch_seg_block": fwd_shape,
-        },
-        "gpu_launches": K * (launches_fs + launches_bs), "clocks": R["clocks"],
+                              "solve")
+    block["dot_product_rel_err"] = dot_err
+    block["forward_launch_seg_block"] = fwd_shape
+    return block, {"grad_ms": R["t_fs"] + R["t_bs"], "t_f": t_f, "clocks": R["clocks"], "dt": case.dt,
+                   "info": R["info"], "launches": K * (launches_fs + launches_bs)}
+
+
+def run_adjoint(args, ws, rank, local):
+    """The adjoint configuration (256^2, RK4, 400 steps, sqrt checkpointing) as its own
+    line: a "step" is one gradient evaluation (forward sweep with checkpoints +
+    backward sweep); value = gradient time / plain forward solve time."""
+    import torch
+
+    torch.cuda.set_device(local)
+    n = args.size or 256
+    nsteps = 400
+    K = max(1, min(args.steps, 5))
+    block, extra = adjoint_measure(n, nsteps, K, local)
+    return {
+        "metric": METRIC, "value": extra["grad_ms"] / extra["t_f"], "unit": "x (gradient time / forward solve time)",
+        "n_gpus": 1, "steps": K, "warmup": 2, "ms_per_step": extra["grad_ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ADJOINT_DESC.format(n=n, nsteps=nsteps), "cells": n * n, "dt": extra["dt"],
+                   "nsteps": nsteps, "checkpoints": extra["info"]["segments"],
+                   "segment_len": extra["info"]["segment_len"],
+                   "l2": "256 MB buffer written between timed gradients"},
+        "adjoint": block,
+        "gpu_launches": extra["launches"], "clocks": extra["clocks"],
     }
-    return out
+
+
+def run_parity(args, ws, rank, local):
+    """Where the per-right-hand-side distance from the oracle comes from, on the
+    benchmark's vortex (char-WENO5 + Roe) at 128^2 .. 1024^2.  Three evaluations of
+    the same right-hand side: the GPU, the oracle (the reference's operation order,
+    no contraction) and the oracle compiled with FMA contraction (the same formulas
+    and order, rounded differently).  Their pairwise relative L2 distances d give,
+    if their rounding errors are independent, each one's own error against the
+    exact right-hand side: e_a^2 = (d_ab^2 + d_ac^2 - d_bc^2) / 2.  Then the 100-step
+    state distance at 1024^2 (the benchmark configuration)."""
+    import numpy as np
+    import torch
+    import oracle as O
+    from hypar_gb300 import cases as C
+    from hypar_gb300.solver import Solver
+
+    torch.cuda.set_device(local)
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    rows = []
+    sizes = [int(v) for v in args.parity_sizes.split(",")]
+    for n in sizes:
+        case = C.vortex(n, n_iter=1)
+        d = tempfile.mkdtemp(prefix=f"gbh_par{n}_")
+        case.write(d)
+        s = Solver.from_dir(d, device=local)
+        P, PF = O.Problem(case), O.Problem(case, fma=True)
+        u0 = P.u0()
+        out = torch.zeros(u0.size, dtype=torch.float64, device="cuda")
+        s.rhs(out, torch.from_numpy(u0).cuda())
+        g = O.interior(out.cpu().numpy(), case.size, 4, 3)
+        o = O.interior(P.rhs(u0.copy()), case.size, 4, 3)
+        f = O.interior(PF.rhs(u0.copy()), case.size, 4, 3)
+        d_go, d_gf, d_of = rel(g, o), rel(g, f), rel(f, o)
+        e2 = lambda a, b, c: max((a * a + b * b - c * c) / 2.0, 0.0) ** 0.5  # noqa: E731
+        rows.append({"n": n, "gpu_vs_oracle": d_go, "gpu_vs_oracle_fma": d_gf, "oracle_vs_oracle_fma": d_of,
+                     "own_error_gpu": e2(d_go, d_gf, d_of), "own_error_oracle": e2(d_go, d_of, d_gf),
+                     "own_error_oracle_fma": e2(d_gf, d_of, d_go),
+                     "per_variable_gpu_vs_oracle": [rel(g[:, k], o[:, k]) for k in range(4)]})
+        s.close()
+    state = None
+    if args.steps > 0:
+        n = sizes[-1]
+        case = C.vortex(n, n_iter=args.steps)
+        d = tempfile.mkdtemp(prefix="gbh_parsteps_")
+        case.write(d)
+        s = Solver.from_dir(d, device=local)
+        s.step(args.steps)
+        got = s.get_state()
+        s.close()
+        P = O.Problem(case)
+        ref = O.interior(P.rk(P.u0(), args.steps), case.size, 4, 3).reshape(-1)
+        state = {"n": n, "steps": args.steps, "gpu_vs_oracle_state": rel(got, ref)}
+    return {"metric": "relative L2 distance of one right-hand side, GPU vs oracle", "value": rows[-1]["gpu_vs_oracle"],
+            "unit": "relative L2", "n_gpus": 1, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "Euler2D isentropic vortex b=5, char-WENO5(JS)+Roe, t=0 state",
+                       "sizes": sizes},
+            "rhs": rows, "state": state}
+
+
+def run_kernel_probe(args, ws, rank, local):
+    """Single-entry-point launches for profilers (nothing timed, no JSON metric): the
+    adjoint test problem (Euler2D n^2, comp-WENO5 + Roe, RK4) and --steps calls of one
+    entry point: the right-hand side's VJP (gb_adjoint_rhs_vjp, --launch sx,sy sets the
+    reverse kernel's segment lengths), its dual-number JVP (gb_adjoint_rhs_jvp), or
+    one fused Runge-Kutta step (gb_solver_step).  Nothing else is launched besides
+    the set-up copies, so a profiler can select the launches by kernel name."""
+    import torch
+    from hypar_gb300 import cases as C
+    from hypar_gb300.adjoint import Adjoint
+    from hypar_gb300.solver import Inputs, Solver
+
+    torch.cuda.set_device(local)
+    what = args.workload.split("-", 1)[1]
+    n = args.size or 256
+    case, _ = C.adjoint_problem(n, 4)
+    d = tempfile.mkdtemp(prefix="gbh_kprobe_")
+    case.write(d)
+    inp = Inputs(d)
+    if what == "step":
+        s = Solver(inp.config, inp.dxinv, device=local)
+        s.set_state(case.u)
+        s.step(args.steps)
+        s.sync()
+        return {"probe": what, "size": n, "calls": args.steps, "ok": True}
+    adj = Adjoint(inp.config, inp.dxinv, 4, 0, local)
+    if args.launch and what == "vjp":
+        sx, sy = (int(v) for v in args.launch.split(","))
+        adj.set_launch(2, sx)
+        adj.set_launch(3, sy)
+    u = adj.ghosted(torch.from_numpy(case.u.reshape(n, n, 4).copy()).cuda()).contiguous()
+    a, b = adj.empty(), adj.empty()
+    a.normal_()
+    for _ in range(args.steps):
+        if what == "vjp":
+            adj.rhs_vjp(u, a, b)
+        else:
+            adj.rhs_jvp(u, a, b, adj.empty())
+    torch.cuda.synchronize()
+    return {"probe": what, "size": n, "calls": args.steps, "ok": True}
 
 
 def run_convergence(args, ws, rank, local):
@@ -754,9 +923,9 @@ def run_reference(args, case, desc, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "cells": cells, "nvars": sub.nvars, "sample": sample},
+        "config": common_config(case, desc, args, ws),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
-                         "sample": f"{args.steps} timed steps ({sample}), {n} OpenMP threads"},
+                         "sample": f"{args.steps} timed steps ({sample}, {cells} cells), {n} OpenMP threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -768,9 +937,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "rtb", "rtb64", "dns", "dns64cr", "ensemble", "adjoint",
-                                                          "convergence"])
+                                                          "convergence", "parity", "kernel-vjp", "kernel-jvp",
+                                                          "kernel-step"])
+    ap.add_argument("--parity-sizes", default="128,256,512,1024", help="grid sizes of --workload parity")
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: leave out the ensemble and adjoint blocks")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--size", type=int, default=0, help="override the grid size (profiling of small cases)")
     ap.add_argument("--launch", default="", help="fixed launch shape per direction instead of the autotuner's, "
@@ -778,10 +951,12 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
-    if args.workload in ("ensemble", "adjoint", "convergence"):
+    if args.workload in ("ensemble", "adjoint", "convergence", "parity", "kernel-vjp", "kernel-jvp", "kernel-step"):
         from hypar_gb300 import build as B
         B.build()
-        fn = {"ensemble": run_ensemble, "adjoint": run_adjoint, "convergence": run_convergence}[args.workload]
+        fn = {"ensemble": run_ensemble, "adjoint": run_adjoint, "convergence": run_convergence,
+              "parity": run_parity, "kernel-vjp": run_kernel_probe, "kernel-jvp": run_kernel_probe,
+              "kernel-step": run_kernel_probe}[args.workload]
         out = fn(args, ws, rank, local) if args.impl == "ours" else None
         if out is not None and rank == 0:
             print(json.dumps(out))

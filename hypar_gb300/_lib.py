@@ -13,7 +13,7 @@ LIB_PATH = os.path.join(HERE, "libgbhypar.so")
 
 GB_OK = 0
 GB_ERR = {1: "GB_ERR_ARG", 2: "GB_ERR_CUDA", 3: "GB_ERR_INPUT", 4: "GB_ERR_UNSUPPORTED", 5: "GB_ERR_NOMEM",
-          6: "GB_ERR_NONFINITE"}
+          6: "GB_ERR_NONFINITE", 7: "GB_ERR_HOOK"}
 MODEL = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
 UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3}
 INTERP = {"components": 0, "characteristic": 1}
@@ -30,7 +30,7 @@ EXPORTS = [
     "gb_solver_step", "gb_solver_time", "gb_solver_set_launch", "gb_solver_check_finite", "gb_run_case",
     "gb_write_binary", "gb_write_text", "gb_write_tecplot", "gb_diff_binary", "gb_HyperbolicFunction", "gb_ParabolicFunction", "gb_SourceFunction", "gb_FFunction",
     "gb_GFunction", "gb_UFunction", "gb_Upwind", "gb_SetInterpLimiterVar", "gb_InterpolateInterfacesHyp", "gb_ApplyBoundaryConditions", "gb_RHSFunctionExplicit",
-    "gb_TimeRK", "gb_probe_fp64_peak", "gb_solver_profile", "gb_solver_profile_read",
+    "gb_TimeRK", "gb_probe_fp64_peak", "gb_probe_rcp_sqrt", "gb_solver_profile", "gb_solver_profile_read",
     "gb_solver_get_launch", "gb_solver_autotune", "gb_inputs_nsims", "gb_inputs_read_member",
     "gb_ensemble_create", "gb_ensemble_destroy", "gb_ensemble_size", "gb_ensemble_set_stream", "gb_ensemble_sync",
     "gb_ensemble_set_state", "gb_ensemble_get_state", "gb_ensemble_step", "gb_ensemble_time",
@@ -41,6 +41,7 @@ EXPORTS = [
     "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
     "gb_solver_set_gravity_field", "gb_solver_conservation_begin", "gb_solver_conservation_error",
     "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error", "gb_ensemble_error",
+    "gb_solver_set_hooks",
 ]
 
 
@@ -73,6 +74,11 @@ _lib = None
 VP = ctypes.c_void_p
 DP = ctypes.POINTER(ctypes.c_double)
 FFUNC = ctypes.CFUNCTYPE(ctypes.c_int, DP, DP, ctypes.c_int, VP, ctypes.c_double)
+# HyPar's stage / step hooks (include/hypar.h:334-341)
+PRESTAGE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_int, ctypes.POINTER(DP), VP, VP, ctypes.c_double)
+POSTSTAGE = ctypes.CFUNCTYPE(ctypes.c_int, VP, VP, VP, ctypes.c_double)
+PRESTEP = ctypes.CFUNCTYPE(ctypes.c_int, VP, VP, VP, ctypes.c_double)
+POSTSTEP = ctypes.CFUNCTYPE(ctypes.c_int, VP, VP, VP, ctypes.c_double, ctypes.c_int)
 UPWFUNC = ctypes.CFUNCTYPE(ctypes.c_int, DP, DP, DP, DP, DP, DP, ctypes.c_int, VP, ctypes.c_double)
 
 
@@ -126,7 +132,9 @@ def lib():
     L.gb_InterpolateInterfacesHyp.argtypes = [VP, VP, VP, VP, ctypes.c_int, ctypes.c_int, VP, VP, ctypes.c_int]
     L.gb_ApplyBoundaryConditions.argtypes = [VP, VP, VP, VP, ctypes.c_double]
     L.gb_TimeRK.argtypes = [VP]
+    L.gb_solver_set_hooks.argtypes = [VP, PRESTAGE, POSTSTAGE, PRESTEP, POSTSTEP, VP, VP]
     L.gb_probe_fp64_peak.argtypes = [DP]
+    L.gb_probe_rcp_sqrt.argtypes = [VP, VP, VP, VP, VP, ctypes.c_longlong]
     L.gb_solver_profile.argtypes = [VP, ctypes.c_int]
     L.gb_solver_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gb_solver_autotune.argtypes = [VP, ctypes.c_int]

@@ -393,6 +393,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_u);
   cudaFree(s->d_acc);
   for (int k = 0; k < 4; k++) cudaFree(s->d_P[k]);
+  cudaFree(s->d_U0);
   cudaFree(s->d_H);
   cudaFree(s->d_crX);
   cudaFree(s->d_crC);
@@ -510,6 +511,7 @@ extern "C" int gb_solver_set_state(gb_solver* s, const double* u, int layout, in
   for (int k = 1; k < s->cfg.rk_nstages; k++)
     CK(cudaMemcpyAsync(s->d_P[k], s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
   s->t = 0.0;
+  s->iter = 0;
   return GB_OK;
 }
 
@@ -547,15 +549,48 @@ extern "C" int gb_solver_set_time(gb_solver* s, double t) {
   return GB_OK;
 }
 
+// A hook installed with gb_solver_set_hooks, called with the solver's queued work
+// finished; the device is synchronised again after it returns, so the hook may
+// use any stream.
+template <typename F>
+static int call_hook(gb_solver* s, const char* name, F&& f) {
+  CK(cudaStreamSynchronize(s->stream));
+  int r = f();
+  if (r) {
+    gbh_set_error("%s hook returned %d", name, r);
+    return GB_ERR_HOOK;
+  }
+  CK(cudaDeviceSynchronize());
+  return GB_OK;
+}
+
 // One Runge-Kutta step (TimeRK, src/TimeIntegration/TimeRK.c:126-195) as
-// nstages x ndims fused launches.
+// nstages x ndims fused launches.  With hooks installed: PreStep before the
+// step (TimePreStep.c:122-124), PostStage on every stage state before its
+// right-hand side (TimeRK.c:155-162), PostStep after it (TimePostStep.c:95-97).
 int gbh_rk_step(gb_solver* s) {
   const gb_config& c = s->cfg;
   const int ns = c.rk_nstages;
   const double dt = c.dt;
   int touched[4] = {0, 0, 0, 0};
+  if (s->pre_step) {
+    int rc = call_hook(s, "PreStep", [&] { return s->pre_step(s->d_u, s->hook_solver, s->hook_mpi, s->t); });
+    if (rc) return rc;
+  }
   for (int st = 0; st < ns; st++) {
     double* U = (st == 0 || !touched[st]) ? s->d_u : s->d_P[st];
+    if (s->post_stage) {
+      // the reference hands PostStage a copy of the stage state (U[stage] = u + ...),
+      // never u itself: a stage that reads u gets it copied first
+      if (U == s->d_u) {
+        if (!s->d_U0) CK(cudaMalloc((void**)&s->d_U0, s->nvals * sizeof(double)));
+        CK(cudaMemcpyAsync(s->d_U0, s->d_u, s->nvals * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+        U = s->d_U0;
+      }
+      const double ts = s->t + c.rk_c[st] * dt;
+      int rc = call_hook(s, "PostStage", [&] { return s->post_stage(U, s->hook_solver, s->hook_mpi, ts); });
+      if (rc) return rc;
+    }
     StageEpi ep;
     memset(&ep, 0, sizeof(ep));
     ep.mode = EPI_RK;
@@ -586,6 +621,32 @@ int gbh_rk_step(gb_solver* s) {
     s->d_acc = tmp;
   }
   s->t += dt;
+  const int done = s->iter++;
+  if (s->post_step) {
+    int rc = call_hook(s, "PostStep",
+                       [&] { return s->post_step(s->d_u, s->hook_solver, s->hook_mpi, s->t, done); });
+    if (rc) return rc;
+  }
+  return GB_OK;
+}
+
+extern "C" int gb_solver_set_hooks(gb_solver* s, int (*PreStage)(int, double**, void*, void*, double),
+                                   int (*PostStage)(double*, void*, void*, double),
+                                   int (*PreStep)(double*, void*, void*, double),
+                                   int (*PostStep)(double*, void*, void*, double, int), void* solver,
+                                   void* mpi) {
+  if (!s) { gbh_set_error("gb_solver_set_hooks: null solver"); return GB_ERR_ARG; }
+  if (PreStage) {
+    // TimeRK.c:144-152: the reference refuses a PreStage hook ("Call to
+    // solver->PreStage() commented out!")
+    gbh_set_error("gb_solver_set_hooks: PreStage is not called by the reference's TimeRK either");
+    return GB_ERR_UNSUPPORTED;
+  }
+  s->post_stage = PostStage;
+  s->pre_step = PreStep;
+  s->post_step = PostStep;
+  s->hook_solver = solver;
+  s->hook_mpi = mpi;
   return GB_OK;
 }
 
@@ -626,6 +687,14 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
   bool prof_was = s->prof;
   const bool cons_was = s->cons_on;  // the trial steps add no boundary fluxes
   s->cons_on = false;
+  // nor do they call the HyPar hooks: they are not steps of the run
+  auto post_stage = s->post_stage;
+  auto pre_step = s->pre_step;
+  auto post_step = s->post_step;
+  const int iter0 = s->iter;
+  s->post_stage = nullptr;
+  s->pre_step = nullptr;
+  s->post_step = nullptr;
   const gb_config& c = s->cfg;
   int rc = GB_OK;
   for (int d = 0; d < c.ndims && !rc; d++) {
@@ -693,6 +762,10 @@ extern "C" int gb_solver_autotune(gb_solver* s, int reps) {
   CK(cudaStreamSynchronize(s->stream));
   s->t = t0;
   s->cons_on = cons_was;
+  s->post_stage = post_stage;
+  s->pre_step = pre_step;
+  s->post_step = post_step;
+  s->iter = iter0;
   return rc;
 }
 

@@ -42,7 +42,10 @@ using namespace gbh;
 static __device__ __align__(256) double g_noalloc_scratch[GB_NOALLOC_SCRATCH_BYTES / sizeof(double)];
 
 // Address of g_noalloc_scratch per device, looked up on the first call made
-// with that device current.
+// with that device current.  The cache lives as long as the process: after
+// cudaDeviceReset (or anything else that destroys and re-creates the device's
+// primary context, which may load the module at a new address) it is stale, so
+// a process that resets a device must not call this entry point afterwards.
 static constexpr int kMaxDevices = 64;
 static std::mutex g_noalloc_mu;
 static double* g_noalloc_ptr[kMaxDevices];
@@ -88,7 +91,11 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
     gbh_set_error("gb_rhs_explicit_noalloc: null argument");
     return GB_ERR_ARG;
   }
-  int rc = gbh_validate(cfg);
+  // The Runge-Kutta fields play no part in a right-hand side: validate the rest
+  // of the configuration with a one-stage table in their place.
+  gb_config checked = *cfg;
+  checked.rk_nstages = 1;
+  int rc = gbh_validate(&checked);
   if (rc) return rc;
   const gb_config& c = *cfg;
   if (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) {
@@ -124,13 +131,14 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
   for (int z = 0; z < c.nzones; z++) NA_CK(launch_bc_zone(u, G, c.nvars, c.zones[z], c.zone_data[z], c.gamma, st));
   NA_CK(cudaMemsetAsync(rhs, 0, nvals * sizeof(double), st));
 
-  PhysParams pp;
+  PhysParams pp{};
   pp.gamma = c.gamma;
   pp.gm1 = c.gamma - 1.0;
   pp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   pp.eps = c.weno_eps;
   pp.wtype = c.weno_weights;
   pp.gf = pp.gg = nullptr;
+  pp.RT = 1.0;  // no gravity here: grav[] stays zero, as in a solver without gravity
   HypLaunch hl;
   hl.seg = 32;
   hl.block = 128;

@@ -1,9 +1,16 @@
-// gbh_probe.cu -- FP64 FMA throughput probe: the denominator of the FP64-pipe
+// gbh_probe.cu -- probes of the hardware the fused kernels rely on.
+//
+// gb_probe_fp64_peak: FP64 FMA throughput, the denominator of the FP64-pipe
 // roofline reported next to the fused kernels (the chip's measured DFMA rate,
 // not a datasheet figure).  Eight independent FMA chains per thread, all
 // operands in registers, enough blocks to fill every SM several times.
+//
+// gb_probe_rcp_sqrt: the Newton-Raphson reciprocal and square root of
+// gbh_device.cuh next to CUDA's correctly rounded 1.0/x and sqrt(x) on the same
+// inputs, so that their error bound can be checked directly.
 #include <cuda_runtime.h>
 
+#include "gbh_device.cuh"
 #include "gbhypar.h"
 
 extern "C" void gbh_set_error(const char* fmt, ...);
@@ -22,7 +29,38 @@ __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
   double s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
+
+__global__ void rcp_sqrt_probe_kernel(const double* __restrict__ x, double* __restrict__ rcp_nr,
+                                      double* __restrict__ rcp_ieee, double* __restrict__ sqrt_nr,
+                                      double* __restrict__ sqrt_ieee, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    rcp_nr[i] = nr_rcp(v);
+    rcp_ieee[i] = __drcp_rn(v);
+    sqrt_nr[i] = nr_sqrt(v);
+    sqrt_ieee[i] = __dsqrt_rn(v);
+  }
+}
 }  // namespace gbh
+
+extern "C" int gb_probe_rcp_sqrt(const double* x, double* rcp_nr, double* rcp_ieee, double* sqrt_nr,
+                                 double* sqrt_ieee, long long n) {
+  if (n < 0 || (n > 0 && (!x || !rcp_nr || !rcp_ieee || !sqrt_nr || !sqrt_ieee))) {
+    gbh_set_error("gb_probe_rcp_sqrt: null array or negative length");
+    return GB_ERR_ARG;
+  }
+  if (n == 0) return GB_OK;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  long long want = (n + 255) / 256;
+  int blocks = (int)(want < (long long)sms * 16 ? want : (long long)sms * 16);
+  gbh::rcp_sqrt_probe_kernel<<<blocks, 256>>>(x, rcp_nr, rcp_ieee, sqrt_nr, sqrt_ieee, n);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { gbh_set_error("gb_probe_rcp_sqrt: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
+  return GB_OK;
+}
 
 extern "C" int gb_probe_fp64_peak(double* tflops) {
   if (!tflops) { gbh_set_error("gb_probe_fp64_peak: null argument"); return GB_ERR_ARG; }

@@ -43,6 +43,15 @@ struct gb_solver {
   gbh::HypLaunch hl[3];
   int visc_seg = 16;
   double t = 0.0;
+  // HyPar's stage / step hooks (include/hypar.h:334-341), installed with
+  // gb_solver_set_hooks and called on the host by every fused step
+  int (*post_stage)(double*, void*, void*, double) = nullptr;
+  int (*pre_step)(double*, void*, void*, double) = nullptr;
+  int (*post_step)(double*, void*, void*, double, int) = nullptr;
+  void* hook_solver = nullptr;
+  void* hook_mpi = nullptr;
+  double* d_U0 = nullptr;  // stage state handed to PostStage where the stage reads u itself
+  int iter = 0;            // steps taken since the state was set (PostStep's iteration index)
   long long dx_off[3] = {0, 0, 0};
   bool viscous = false;
   // launch profiler: an event pair around every launch group, read on demand

@@ -35,6 +35,7 @@ extern "C" {
 #define GB_ERR_UNSUPPORTED 4  /* valid HyPar option outside this library's path */
 #define GB_ERR_NOMEM 5        /* device or host allocation failed */
 #define GB_ERR_NONFINITE 6    /* the solution contains NaN or Inf */
+#define GB_ERR_HOOK 7         /* a hook installed with gb_solver_set_hooks returned nonzero */
 
 enum { GB_MODEL_EULER1D = 1, GB_MODEL_EULER2D = 2, GB_MODEL_NS3D = 3 };
 enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2, GB_UPWIND_RUSANOV = 3 /* Euler1D, NS3D */ };
@@ -268,6 +269,12 @@ int gb_op_to_initial(const char *op_path, const char *initial_path);
  * counted as two operations) with a register-resident DFMA loop: the
  * denominator of the FP64-pipe roofline of the fused kernels. */
 int gb_probe_fp64_peak(double *tflops);
+/* No counterpart in the reference: evaluates, for n device doubles x, the fused
+ * kernels' Newton-Raphson reciprocal and square root (rcp_nr, sqrt_nr) beside the
+ * correctly rounded 1/x and sqrt(x) (rcp_ieee, sqrt_ieee), all device arrays, so
+ * the refinements' error bound can be checked directly.  Synchronises the device. */
+int gb_probe_rcp_sqrt(const double *x, double *rcp_nr, double *rcp_ieee, double *sqrt_nr, double *sqrt_ieee,
+                      long long n);
 
 /* ---- HyPar's function-pointer surface (device arrays, HyPar layout) ---- */
 
@@ -316,8 +323,29 @@ int gb_ApplyBoundaryConditions(void *s, void *m, double *u, double *uref, double
  * applies the boundary conditions to u in place, rhs = -hyp + par + source. */
 int gb_RHSFunctionExplicit(double *rhs, double *u, void *s, void *m, double t);
 /* TimeRK (src/TimeIntegration/TimeRK.c:35) for `ts` = a gb_solver: one
- * Runge-Kutta step of the resident solution. */
+ * Runge-Kutta step of the resident solution.  HyPar passes its TimeIntegration*
+ * here; a binding maps it to the gb_solver of each simulation (INTEGRATION.md's
+ * gbshim_TimeRK does, for the solution in HyPar's gpu_u array) and installs
+ * the physics model's stage / step hooks with gb_solver_set_hooks. */
 int gb_TimeRK(void *ts);
+/* HyPar's stage and step hooks (include/hypar.h:334-341) for the fused step
+ * (gb_TimeRK, gb_solver_step and the monitored step): PreStep(u, solver, mpi, t)
+ * before each step (TimePreStep.c:122-124); PostStage(U_s, solver, mpi, t_s) on
+ * every stage state before its right-hand side, t_s = t + c_s dt (TimeRK.c:155-162),
+ * with U_s a copy where the stage's state is the solution itself, as the
+ * reference's U[stage] is; PostStep(u, solver, mpi, t + dt, iter) after each step
+ * (TimePostStep.c:95-97), iter = the 0-based index of the step just taken since
+ * the last gb_solver_set_state.  `solver` and `mpi` are passed through (HyPar's
+ * HyPar* and MPIVariables*); arrays are the solver's DEVICE arrays.  Each hook is
+ * called on the host with the solver's stream synchronised, and the device is
+ * synchronised again after it returns.  NULL removes a hook.  A non-NULL
+ * PreStage returns GB_ERR_UNSUPPORTED, as the reference's TimeRK refuses it
+ * (TimeRK.c:144-152).  A hook returning nonzero stops the step with GB_ERR_HOOK.
+ * The autotuner's trial steps call no hook. */
+int gb_solver_set_hooks(gb_solver *s, int (*PreStage)(int, double **, void *, void *, double),
+                        int (*PostStage)(double *, void *, void *, double),
+                        int (*PreStep)(double *, void *, void *, double),
+                        int (*PostStep)(double *, void *, void *, double, int), void *solver, void *mpi);
 
 /* ---- discrete adjoint and tangent-linear model ----
  * No counterpart in the reference (which has no derivative code): derivatives
@@ -376,7 +404,7 @@ int gb_adjoint_tlm(gb_adjoint *a, const double *u0, const double *du0, double *u
  * with a locked-down allocator, allocation-free sections of a time loop): the
  * rhs of gb_RHSFunctionExplicit for an INVISCID configuration, with no
  * gb_solver and no device allocation.  cfg: the configuration (the
- * Runge-Kutta fields are ignored); dxinv: DEVICE array of sum_d
+ * Runge-Kutta fields are ignored, rk_nstages included); dxinv: DEVICE array of sum_d
  * (dim[d]+2*ghosts) values; u, rhs: DEVICE arrays in HyPar's ghosted layout
  * (u's ghost points are filled in place, as gb_RHSFunctionExplicit does);
  * stream: a cudaStream_t (NULL: the legacy default stream).  Work is queued on
@@ -384,13 +412,18 @@ int gb_adjoint_tlm(gb_adjoint *a, const double *u0, const double *du0, double *u
  * The directions before the last accumulate into a library-wide device array
  * of GB_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading the library
  * holds until exit; a 2-D or 3-D grid whose ghosted solution is larger is
- * rejected with GB_ERR_ARG (1-D grids need no scratch).  Viscous NS3D (Re > 0)
+ * rejected with GB_ERR_ARG (1-D grids need no scratch).  With 3 ghost points
+ * the largest grids that fit are 1442 x 1442 for Euler2D and 112^3 for
+ * NavierStokes3D (non-square grids: prod_d (dim[d]+6) * nvars * 8 bytes
+ * <= 64 MiB).  Viscous NS3D (Re > 0)
  * returns GB_ERR_UNSUPPORTED.  All calls on a device share that array: calls
  * whose work overlaps on the GPU (different streams, no ordering between
  * them) race and give wrong results; keep them on one stream or order them.
  * The first call on each device looks the array's address up
  * (cudaGetSymbolAddress) with that device current: make it before any stream
- * capture begins. */
+ * capture begins.  The address is cached for the life of the process; after a
+ * cudaDeviceReset of that device the cache is stale, so do not call this entry
+ * point on a device that has been reset. */
 #define GB_NOALLOC_SCRATCH_BYTES (64ull << 20)
 int gb_rhs_explicit_noalloc(const gb_config *cfg, const double *dxinv, double *rhs, double *u, void *stream);
 

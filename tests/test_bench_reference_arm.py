@@ -1,5 +1,6 @@
 """The reference arm of bench.py (`--impl reference`: the reference algorithm on the
-host cores, no GPU) prints one JSON line with the contract's keys."""
+host cores, no GPU) prints one JSON line with the contract's keys, and the same
+config object as the GPU arm prints for the same workload."""
 import json
 import os
 import subprocess
@@ -21,3 +22,9 @@ def test_reference_arm_json_line(oracle_lib):
     assert d["impl"] == "reference" and d["value"] > 0 and d["steps"] == 2
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    sys.path.insert(0, ROOT)
+    import argparse
+    import bench
+    case, desc = bench.workload("sod")
+    ours = bench.common_config(case, desc, argparse.Namespace(steps=2), 1)
+    assert d["config"] == json.loads(json.dumps(ours))

@@ -1,7 +1,11 @@
 """Parity at the benchmark configurations' full sizes.
 
-Sod 1024 (RK4, dt 1e-4, 1000 steps) is cheap enough for the oracle to run whole.
-For the 1024^2 vortex and the 256^3 Taylor-Green vortex the oracle evaluates one
+Sod 1024 (RK4, dt 1e-4, 1000 steps) is cheap enough for the oracle to run whole,
+and so is the 1024^2 vortex over 100 SSPRK3 steps (about 30 s on 16 host cores):
+both are held to relative L2 <= 1e-10 of the state.  The 256^3 Taylor-Green
+vortex over 100 RK4 steps takes the oracle about 11 minutes on 16 cores; that
+leg runs when HYPAR_LONG_VALIDATION=1 is set.
+For the 1024^2 vortex and the 256^3 Taylor-Green vortex the oracle also evaluates one
 right-hand side at full size: relative L2 <= 1e-12, or, where the state's own
 conditioning puts rounding noise above that (a flux difference over a fine grid
 cancels O(1) fluxes to O(h)), within 4x the distance between the oracle and its
@@ -101,3 +105,34 @@ def test_tgv_full_size(built_lib, tmp_path):
     s.step(4)
     tot, _ = _sums(s, case)
     assert abs(tot[0] - tot0[0]) <= 1e-12 * mag0[0], (tot[0] - tot0[0]) / mag0[0]
+
+
+def test_vortex_full_size_100_steps(built_lib, tmp_path):
+    """The benchmark configuration itself: isentropic vortex 1024^2, char-WENO5 + Roe,
+    SSPRK3 at CFL 0.5, 100 steps on the GPU and in the oracle; the states agree to
+    relative L2 <= 1e-10."""
+    case = C.vortex(1024, n_iter=100)
+    s = solver_for(case, tmp_path)
+    s.step(100)
+    got = s.get_state()
+    P = O.Problem(case)
+    ref = O.interior(P.rk(P.u0(), 100), case.size, case.nvars, 3).reshape(-1)
+    err = relerr(got, ref)
+    assert err <= STEP_TOL, err
+
+
+@pytest.mark.skipif(os.environ.get("HYPAR_LONG_VALIDATION") != "1",
+                    reason="about 11 minutes of oracle time on 16 cores: set HYPAR_LONG_VALIDATION=1")
+def test_tgv_full_size_100_steps(built_lib, tmp_path):
+    """Taylor-Green vortex 256^3, comp-WENO5 + Roe + viscous, RK4, dt 2e-3, 100 steps on
+    the GPU and in the oracle; the states agree to relative L2 <= 1e-10."""
+    case = C.tgv(256, n_iter=100, dt=2e-3)
+    s = solver_for(case, tmp_path)
+    s.step(100)
+    got = s.get_state()
+    s.close()
+    P = O.Problem(case)
+    ref = O.interior(P.rk(P.u0(), 100), case.size, case.nvars, 3).reshape(-1)
+    err = relerr(got, ref)
+    print(f"tgv 256^3 100 RK4 steps: relative L2 GPU vs oracle {err:.3e}")
+    assert err <= STEP_TOL, err
