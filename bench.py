@@ -240,8 +240,9 @@ def run_ours(args, case, desc, ws, rank, local):
     if args.launch:
         # a fixed launch shape per direction (profiling: the autotuner's choice under a
         # profiler's serialised replays can differ from its choice in a plain run)
-        for d, sg in enumerate(int(v) for v in args.launch.split(",")):
-            s.set_launch(d, sg, 0)
+        for d, item in enumerate(args.launch.split(",")):
+            sg, _, bl = item.partition(":")
+            s.set_launch(d, int(sg), int(bl or 0))
         tuned = [s.get_launch(d) for d in range(case.ndims)]
     else:
         tuned = s.autotune(2)  # launch shape per direction (state restored), outside the timed region
@@ -377,6 +378,11 @@ def run_ours(args, case, desc, ws, rank, local):
         out["ensemble"] = ensemble_summary(m, len(members), 3)
         out["ensemble"]["workload"] = ENSEMBLE_DESC
         out["ensemble"]["reduced"] = "3 timed steps (1 warm-up) per arm instead of 100"
+        # many small members: where per-member launches, not FP64 work, set the pace
+        small = C.ensemble_vortex(256, sizes=C.ensemble_sizes(256, 20261203, 32, 128, 16), n_iter=100)
+        ms = ensemble_measure(small, steps=5, warmup=2, local=local)
+        out["ensemble"]["small_members"] = ensemble_summary(ms, len(small), 5)
+        out["ensemble"]["small_members"]["workload"] = SMALL_ENSEMBLE_DESC
         torch.cuda.set_stream(stream)
         block, _ = adjoint_measure(256, 400, 1, local, policies=("sqrt",), fd_directions=4,
                                    fd_kinds=("smooth", "noise"))
@@ -519,6 +525,8 @@ def run_ensemble(args, ws, rank, local):
 
 ENSEMBLE_DESC = ("ensemble of 64 Euler2D isentropic vortices, sizes seeded from {128,192,...,1024}^2, b~U[1,5], "
                  "centre~U[3,7]^2, char-WENO5(JS)+Roe, SSPRK3, common dt at CFL 0.5")
+SMALL_ENSEMBLE_DESC = ("ensemble of 256 Euler2D isentropic vortices, sizes seeded from {32,48,...,128}^2, "
+                       "b~U[1,5], centre~U[3,7]^2, char-WENO5(JS)+Roe, SSPRK3, common dt at CFL 0.5")
 ADJOINT_DESC = ("adjoint: d/d rho0 of 0.5||rho(T)-rho_target||^2, Euler2D {n}x{n} periodic [0,10)^2, target "
                 "from the b=5 vortex, guess b=4 shifted by U[-0.5,0.5]^2, comp-WENO5(JS)+Roe, RK4, {nsteps} "
                 "steps, sqrt checkpointing")
@@ -947,7 +955,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--size", type=int, default=0, help="override the grid size (profiling of small cases)")
     ap.add_argument("--launch", default="", help="fixed launch shape per direction instead of the autotuner's, "
-                                                 "e.g. -128,-128 (tiles of 128 interfaces)")
+                                                 "seg[:block] per direction, e.g. -128,-128 (tiles of 128 "
+                                                 "interfaces) or 64:128,43:128,43:128")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -134,7 +134,7 @@ def lib():
     L.gb_TimeRK.argtypes = [VP]
     L.gb_solver_set_hooks.argtypes = [VP, PRESTAGE, POSTSTAGE, PRESTEP, POSTSTEP, VP, VP]
     L.gb_probe_fp64_peak.argtypes = [DP]
-    L.gb_probe_rcp_sqrt.argtypes = [VP, VP, VP, VP, VP, ctypes.c_longlong]
+    L.gb_probe_rcp_sqrt.argtypes = [VP, VP, VP, VP, VP, VP, ctypes.c_longlong]
     L.gb_solver_profile.argtypes = [VP, ctypes.c_int]
     L.gb_solver_get_launch.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
     L.gb_solver_autotune.argtypes = [VP, ctypes.c_int]

@@ -19,11 +19,14 @@
 
 namespace gbh {
 cudaError_t launch_batched_euler1d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                   const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
+                                   const double*, const PhysParams&, const StageEpi&, int, int, unsigned long long*,
+                                   cudaStream_t);
 cudaError_t launch_batched_euler2d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                   const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
+                                   const double*, const PhysParams&, const StageEpi&, int, int, unsigned long long*,
+                                   cudaStream_t);
 cudaError_t launch_batched_ns3d(int, int, int, const MemberDev*, int, long long, const double*, double*,
-                                const double*, const PhysParams&, const StageEpi&, int, int, cudaStream_t);
+                                const double*, const PhysParams&, const StageEpi&, int, int, unsigned long long*,
+                                cudaStream_t);
 cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
 }  // namespace gbh
 
@@ -51,6 +54,10 @@ struct gb_ensemble {
   long long total_vals = 0, total_dx = 0;
   long long total_thr[3] = {0, 0, 0};
   int seg[3] = {32, 32, 32}, block[3] = {128, 128, 128};
+  // tile forms only: the persistent work-list kernel (one counter per stage and
+  // direction, cleared at the start of every step) instead of one block per tile
+  bool persist[3] = {false, false, false};
+  unsigned long long* d_ctr = nullptr;
   double* d_u = nullptr;
   double* d_acc = nullptr;
   double* d_P[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -103,18 +110,19 @@ static int upload_table(gb_ensemble* e) {
   return GB_OK;
 }
 
-static cudaError_t launch_dir(gb_ensemble* e, int d, const double* U, const StageEpi& ep) {
+static cudaError_t launch_dir(gb_ensemble* e, int st, int d, const double* U, const StageEpi& ep) {
   const gb_config& c = e->base;
   const int tile = e->seg[d] < 0 ? -e->seg[d] : 0;
-  if (tile && e->total_thr[d] > 0x7fffffffLL) return cudaErrorInvalidConfiguration;  // one block per tile
+  unsigned long long* ctr = (tile && e->persist[d]) ? e->d_ctr + 3 * st + d : nullptr;
+  if (tile && !ctr && e->total_thr[d] > 0x7fffffffLL) return cudaErrorInvalidConfiguration;  // one block per tile
   if (c.model == GB_MODEL_EULER1D)
     return launch_batched_euler1d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx,
-                                  e->pp, ep, e->block[d], tile, e->stream);
+                                  e->pp, ep, e->block[d], tile, ctr, e->stream);
   if (c.model == GB_MODEL_EULER2D)
     return launch_batched_euler2d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx,
-                                  e->pp, ep, e->block[d], tile, e->stream);
+                                  e->pp, ep, e->block[d], tile, ctr, e->stream);
   return launch_batched_ns3d(d, c.interp, c.upwind, e->d_mem, e->nm, e->total_thr[d], U, e->d_H, e->d_dx, e->pp,
-                             ep, e->block[d], tile, e->stream);
+                             ep, e->block[d], tile, ctr, e->stream);
 }
 
 // The launches of one Runge-Kutta step (ns stages x ndims directions).
@@ -122,6 +130,8 @@ static int step_launches(gb_ensemble* e) {
   const gb_config& c = e->base;
   const int ns = c.rk_nstages;
   int touched[4] = {0, 0, 0, 0};
+  if (e->persist[0] || e->persist[1] || e->persist[2])
+    CK(cudaMemsetAsync(e->d_ctr, 0, sizeof(unsigned long long) * 12, e->stream));
   for (int st = 0; st < ns; st++) {
     double* U = (st == 0 || !touched[st]) ? e->d_u : e->d_P[st];
     StageEpi ep;
@@ -150,7 +160,7 @@ static int step_launches(gb_ensemble* e) {
         x.bnd = e->d_bnd;  // each member's block at its bnd_off
         x.bw = ep.cb;
       }
-      CK(launch_dir(e, d, U, x));
+      CK(launch_dir(e, st, d, U, x));
     }
     for (int t = st + 1; t < ns; t++)
       if (ep.ca[t] != 0.0) touched[t] = 1;
@@ -243,6 +253,7 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
   if (e->base.ndims > 1) A(&e->d_H, bytes);
   A(&e->d_dx, dxo * sizeof(double));
   if (ce == cudaSuccess) ce = cudaMalloc((void**)&e->d_mem, sizeof(MemberDev) * nsims);
+  if (ce == cudaSuccess) ce = cudaMalloc((void**)&e->d_ctr, sizeof(unsigned long long) * 12);
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
   if (ce == cudaSuccess) e->own_stream = true;
   for (int m = 0; m < nsims && ce == cudaSuccess; m++) {
@@ -274,6 +285,7 @@ extern "C" void gb_ensemble_destroy(gb_ensemble* e) {
   cudaFree(e->d_H);
   cudaFree(e->d_dx);
   cudaFree(e->d_mem);
+  cudaFree(e->d_ctr);
   cudaFree(e->d_bnd);
   cudaFree(e->d_red);
   if (e->own_stream && e->stream) cudaStreamDestroy(e->stream);
@@ -402,18 +414,29 @@ extern "C" int gb_ensemble_set_launch(gb_ensemble* e, int dir, int seg, int bloc
     gbh_set_error("gb_ensemble_set_launch: a tile form is -32, -64 or -128 (got %d)", seg);
     return GB_ERR_ARG;
   }
-  if (seg != 0) e->seg[dir] = seg;
-  if (block > 0) {
-    if (block % 32 || block > 128) { gbh_set_error("block must be a multiple of 32, at most 128"); return GB_ERR_ARG; }
-    e->block[dir] = block;
+  const int nseg = seg != 0 ? seg : e->seg[dir];
+  if (block == -1 && nseg >= 0) {
+    gbh_set_error("gb_ensemble_set_launch: the persistent work-list form (block -1) takes a tile form");
+    return GB_ERR_ARG;
   }
+  if (block < -1 || (block > 0 && (block % 32 || block > 128))) {
+    gbh_set_error("gb_ensemble_set_launch: block %d (a multiple of 32 up to 128, or -1)", block);
+    return GB_ERR_ARG;
+  }
+  e->seg[dir] = nseg;
+  if (block == -1) e->persist[dir] = true;
+  if (block > 0) {
+    e->block[dir] = block;
+    e->persist[dir] = false;
+  }
+  if (nseg >= 0) e->persist[dir] = false;
   return upload_table(e);
 }
 
 extern "C" int gb_ensemble_get_launch(gb_ensemble* e, int dir, int* seg, int* block) {
   if (!e || dir < 0 || dir >= e->base.ndims || !seg || !block) { gbh_set_error("bad argument"); return GB_ERR_ARG; }
   *seg = e->seg[dir];
-  *block = e->block[dir];
+  *block = e->persist[dir] ? -1 : e->block[dir];
   return GB_OK;
 }
 
@@ -440,11 +463,15 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
   for (int d = 0; d < e->base.ndims && !rc; d++) {
     float best = 1e30f;
     int bs = e->seg[d], bb = e->block[d];
+    bool bp = e->persist[d];
     for (int sg : cand) {
-      for (int blk : {128, 64}) {
-        if (sg < 0 && blk != 128) continue;  // a tile's block is its interfaces
+      for (int blk : {128, 64, -1}) {
+        // a tile's block is its interfaces; -1: the tile's persistent work-list form
+        if (sg < 0 && blk == 64) continue;
+        if (sg > 0 && blk < 0) continue;
         e->seg[d] = sg;
-        e->block[d] = blk;
+        e->block[d] = blk > 0 ? blk : 128;
+        e->persist[d] = blk < 0;
         rc = upload_table(e);
         if (!rc) rc = gb_ensemble_step(e, 1);
         if (rc) break;
@@ -457,13 +484,15 @@ extern "C" int gb_ensemble_autotune(gb_ensemble* e, int reps) {
         if (!rc && ms < best) {
           best = ms;
           bs = sg;
-          bb = blk;
+          bb = e->block[d];
+          bp = e->persist[d];
         }
       }
       if (rc) break;
     }
     e->seg[d] = bs;
     e->block[d] = bb;
+    e->persist[d] = bp;
     if (!rc) rc = upload_table(e);
   }
   cudaEventDestroy(a);

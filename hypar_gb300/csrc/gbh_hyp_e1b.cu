@@ -4,7 +4,8 @@
 namespace gbh {
 cudaError_t launch_batched_euler1d(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
                                    const double* U, double* H, const double* dxinv, const PhysParams& pp,
-                                   const StageEpi& ep, int block, int tile, cudaStream_t s) {
-  return launch_batched_model<MODEL_EULER1D>(dir, chr, upw, mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s);
+                                   const StageEpi& ep, int block, int tile, unsigned long long* counter,
+                                   cudaStream_t s) {
+  return launch_batched_model<MODEL_EULER1D>(dir, chr, upw, mem, nmem, total, U, H, dxinv, pp, ep, block, tile, counter, s);
 }
 }  // namespace gbh

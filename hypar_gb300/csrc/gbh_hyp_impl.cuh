@@ -814,8 +814,14 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
   }
 }
 
+// Resident blocks per SM the register allocation of the 128-interface tile kernels
+// must allow (1: as many registers as the kernel wants).
+#ifndef GBH_TILE_MINB
+#define GBH_TILE_MINB 1
+#endif
+
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
-__global__ void __launch_bounds__(TI)
+__global__ void __launch_bounds__(TI, (TI == 128 ? GBH_TILE_MINB : 1))
 hyp_tile_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
                 PhysParams pp, StageEpi ep, long long ntrans) {
   hyp_tile_body<M, CHAR, UPW, DIR, ALTW, TI, WT>(U, H, dxinv, G, pp, ep, ntrans, blockIdx.x);
@@ -887,12 +893,61 @@ hyp_batched_tile_kernel(const MemberDev* __restrict__ mem, int nmem, const doubl
                                                      e, m.ntrans[DIR], b - m.start[DIR]);
 }
 
+// Persistent work-list form of the batched tile kernel: a grid of as many blocks as
+// the SMs hold at once pulls tile indices from a work counter (one atomicAdd per
+// tile, by one thread of the block) until the launch's `total` tiles are taken.  The
+// loop is bounded: every fetch takes a new index, so a block stops after at most
+// total / gridDim + 1 fetches.  `counter` is zero when the launch starts.
+template <int M, bool CHAR, int UPW, int DIR, int TI>
+__global__ void __launch_bounds__(TI)
+hyp_batched_worklist_kernel(const MemberDev* __restrict__ mem, int nmem, long long total,
+                            unsigned long long* __restrict__ counter, const double* __restrict__ U,
+                            double* __restrict__ H, const double* __restrict__ dxinv, PhysParams pp, StageEpi ep) {
+  __shared__ long long s_tile;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (long long)atomicAdd(counter, 1ULL);
+    __syncthreads();
+    const long long b = s_tile;
+    __syncthreads();  // every thread holds b before thread 0 fetches the next one
+    if (b >= total) return;
+    StageEpi e = ep;
+    const MemberDev& m = batched_member<DIR>(mem, nmem, b, e);
+    const long long o = m.off;
+    hyp_tile_body<M, CHAR, UPW, DIR, false, TI, false>(U + o, H ? H + o : nullptr, dxinv + m.dx_off[DIR], m.G, pp,
+                                                       e, m.ntrans[DIR], b - m.start[DIR]);
+  }
+}
+
+template <typename K>
+unsigned worklist_grid(K kernel, int threads, long long total) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+  long long g = (long long)(per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+  return (unsigned)(g < total ? g : total);
+}
+
 // total = threads (walker, tile == 0) or blocks (tiles of `tile` interfaces).
+// counter != nullptr with a tile form: the persistent work-list kernel.
 template <int M, bool CHAR, int UPW, int DIR>
 cudaError_t launch_batched_dir(const MemberDev* mem, int nmem, long long total, const double* U, double* H,
                                const double* dxinv, const PhysParams& pp, const StageEpi& ep, int block, int tile,
-                               cudaStream_t s) {
+                               unsigned long long* counter, cudaStream_t s) {
   if (total <= 0) return cudaSuccess;
+  if (counter && tile) {
+#define GBH_WL(TI)                                                                                       \
+  do {                                                                                                   \
+    auto k = hyp_batched_worklist_kernel<M, CHAR, UPW, DIR, TI>;                                         \
+    k<<<worklist_grid(k, TI, total), TI, 0, s>>>(mem, nmem, total, counter, U, H, dxinv, pp, ep);        \
+  } while (0)
+    if (tile == 32) GBH_WL(32);
+    else if (tile == 64) GBH_WL(64);
+    else if (tile == 128) GBH_WL(128);
+    else return cudaErrorInvalidValue;
+#undef GBH_WL
+    return cudaGetLastError();
+  }
   if (tile == 32)
     hyp_batched_tile_kernel<M, CHAR, UPW, DIR, 32><<<(unsigned)total, 32, 0, s>>>(mem, nmem, U, H, dxinv, pp, ep);
   else if (tile == 64)
@@ -912,15 +967,19 @@ cudaError_t launch_batched_dir(const MemberDev* mem, int nmem, long long total, 
 template <int M>
 cudaError_t launch_batched_model(int dir, int chr, int upw, const MemberDev* mem, int nmem, long long total,
                                  const double* U, double* H, const double* dxinv, const PhysParams& pp,
-                                 const StageEpi& ep, int block, int tile, cudaStream_t s) {
+                                 const StageEpi& ep, int block, int tile, unsigned long long* counter,
+                                 cudaStream_t s) {
   constexpr int ND = ModelTraits<M>::ND;
 #define GBH_B(C, W)                                                                                          \
   do {                                                                                                       \
-    if (dir == 0) return launch_batched_dir<M, C, W, 0>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
+    if (dir == 0)                                                                                            \
+      return launch_batched_dir<M, C, W, 0>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, counter, s); \
     if (ND > 1 && dir == 1)                                                                                  \
-      return launch_batched_dir<M, C, W, (ND > 1 ? 1 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
+      return launch_batched_dir<M, C, W, (ND > 1 ? 1 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, \
+                                                           counter, s);                                      \
     if (ND > 2 && dir == 2)                                                                                  \
-      return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, s); \
+      return launch_batched_dir<M, C, W, (ND > 2 ? 2 : 0)>(mem, nmem, total, U, H, dxinv, pp, ep, block, tile, \
+                                                           counter, s);                                      \
     return cudaErrorInvalidValue;                                                                            \
   } while (0)
   // Rusanov: Euler1D and NavierStokes3D (Euler2D offers none); the template

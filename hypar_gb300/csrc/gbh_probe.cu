@@ -32,7 +32,8 @@ __global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
 
 __global__ void rcp_sqrt_probe_kernel(const double* __restrict__ x, double* __restrict__ rcp_nr,
                                       double* __restrict__ rcp_ieee, double* __restrict__ sqrt_nr,
-                                      double* __restrict__ sqrt_ieee, long long n) {
+                                      double* __restrict__ sqrt_ieee, double* __restrict__ rsqrt_nr,
+                                      long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const double v = x[i];
@@ -40,12 +41,13 @@ __global__ void rcp_sqrt_probe_kernel(const double* __restrict__ x, double* __re
     rcp_ieee[i] = __drcp_rn(v);
     sqrt_nr[i] = nr_sqrt(v);
     sqrt_ieee[i] = __dsqrt_rn(v);
+    if (rsqrt_nr) rsqrt_nr[i] = nr_rsqrt(v);
   }
 }
 }  // namespace gbh
 
 extern "C" int gb_probe_rcp_sqrt(const double* x, double* rcp_nr, double* rcp_ieee, double* sqrt_nr,
-                                 double* sqrt_ieee, long long n) {
+                                 double* sqrt_ieee, double* rsqrt_nr, long long n) {
   if (n < 0 || (n > 0 && (!x || !rcp_nr || !rcp_ieee || !sqrt_nr || !sqrt_ieee))) {
     gbh_set_error("gb_probe_rcp_sqrt: null array or negative length");
     return GB_ERR_ARG;
@@ -56,7 +58,7 @@ extern "C" int gb_probe_rcp_sqrt(const double* x, double* rcp_nr, double* rcp_ie
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   long long want = (n + 255) / 256;
   int blocks = (int)(want < (long long)sms * 16 ? want : (long long)sms * 16);
-  gbh::rcp_sqrt_probe_kernel<<<blocks, 256>>>(x, rcp_nr, rcp_ieee, sqrt_nr, sqrt_ieee, n);
+  gbh::rcp_sqrt_probe_kernel<<<blocks, 256>>>(x, rcp_nr, rcp_ieee, sqrt_nr, sqrt_ieee, rsqrt_nr, n);
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) { gbh_set_error("gb_probe_rcp_sqrt: %s", cudaGetErrorString(e)); return GB_ERR_CUDA; }
   return GB_OK;

@@ -230,7 +230,12 @@ int gb_ensemble_step(gb_ensemble *e, int nsteps);
 double gb_ensemble_time(const gb_ensemble *e);
 /* Launch shape per direction, as gb_solver_set_launch: seg > 0 interfaces walked per
  * thread, seg = -32, -64 or -128 one block per tile of that many interfaces of a
- * member's grid line; 0 keeps the current value. */
+ * member's grid line; 0 keeps the current value.  With a tile form, block = -1
+ * selects the persistent work-list kernel (HyPar's ensemble mode,
+ * src/TimeIntegration/TimeRK.c:164-170, as one launch per stage and direction of as
+ * many blocks as the SMs hold, taking the members' tiles from an atomic counter),
+ * block > 0 the grid launch of one block per tile; get_launch reports -1 for the
+ * persistent form. */
 int gb_ensemble_set_launch(gb_ensemble *e, int dir, int seg, int block);
 int gb_ensemble_get_launch(gb_ensemble *e, int dir, int *seg, int *block);
 /* Choose seg/block (walker or tiles) per direction by timing graph-replayed steps
@@ -270,11 +275,12 @@ int gb_op_to_initial(const char *op_path, const char *initial_path);
  * denominator of the FP64-pipe roofline of the fused kernels. */
 int gb_probe_fp64_peak(double *tflops);
 /* No counterpart in the reference: evaluates, for n device doubles x, the fused
- * kernels' Newton-Raphson reciprocal and square root (rcp_nr, sqrt_nr) beside the
- * correctly rounded 1/x and sqrt(x) (rcp_ieee, sqrt_ieee), all device arrays, so
- * the refinements' error bound can be checked directly.  Synchronises the device. */
+ * kernels' refined reciprocal, square root and reciprocal square root (rcp_nr,
+ * sqrt_nr, rsqrt_nr; rsqrt_nr may be NULL) beside the correctly rounded 1/x and
+ * sqrt(x) (rcp_ieee, sqrt_ieee), all device arrays, so the refinements' error
+ * bound can be checked directly.  Synchronises the device. */
 int gb_probe_rcp_sqrt(const double *x, double *rcp_nr, double *rcp_ieee, double *sqrt_nr, double *sqrt_ieee,
-                      long long n);
+                      double *rsqrt_nr, long long n);
 
 /* ---- HyPar's function-pointer surface (device arrays, HyPar layout) ---- */
 

@@ -45,6 +45,7 @@ def test_ensemble_autotune_keeps_results(built_lib, tmp_path):
     b = Ensemble.from_dir(d)
     tuned = b.autotune(1)
     assert all(s > 0 or s in (-32, -64, -128) for s, _ in tuned)
+    assert all(b > 0 or (b == -1 and s < 0) for s, b in tuned)
     b.step(2)
     for k in range(4):
         assert np.array_equal(b.get_state(k), ref[k])
@@ -75,6 +76,42 @@ def test_ensemble_tiles(built_lib, oracle_lib, tmp_path, tile, interp, upw):
         P = O.Problem(case)
         ref = O.interior(P.rk(P.u0(), 3), case.size, case.nvars, 3).reshape(-1)
         assert relerr(e.get_state(k), ref) <= 1e-10
+
+
+@pytest.mark.parametrize("tile", [32, 128])
+@pytest.mark.parametrize("interp,scheme", [("characteristic", "ssprk3"), ("components", "44")])
+def test_ensemble_worklist(built_lib, oracle_lib, tmp_path, tile, interp, scheme):
+    """The persistent work-list form (gb_ensemble_set_launch block = -1 with a tile
+    form): one launch per stage and direction of as many blocks as the SMs hold,
+    taking the members' tiles from a counter.  Each tile is computed by the same
+    device code as in the one-block-per-tile launch, so the members equal
+    single-grid runs in the tile form bit for bit, over many graph replays (the
+    counters are cleared every step)."""
+    members = C.ensemble_vortex(6, sizes=[16, 72, 40, 136, 24, 200], n_iter=5, seed=19, interp=interp,
+                                scheme=scheme)
+    d = str(tmp_path / "ens")
+    C.write_ensemble(members, d)
+    e = Ensemble.from_dir(d)
+    for dd in range(2):
+        e.set_launch(dd, -tile, -1)
+        assert e.get_launch(dd) == (-tile, -1)
+    e.step(5)
+    for k, case in enumerate(members):
+        sd = str(tmp_path / f"m{k}")
+        case.write(sd)
+        s = Solver.from_dir(sd)
+        for dd in range(2):
+            s.set_launch(dd, -tile, 0)
+        s.step(5)
+        assert np.array_equal(e.get_state(k), s.get_state())
+    P = O.Problem(members[2])
+    ref = O.interior(P.rk(P.u0(), 5), members[2].size, 4, 3).reshape(-1)
+    assert relerr(e.get_state(2), ref) <= 1e-10
+    # a walker shape cannot take the persistent form; back to one block per tile
+    with pytest.raises(Exception):
+        e.set_launch(0, 16, -1)
+    e.set_launch(0, -tile, 128)
+    assert e.get_launch(0) == (-tile, 128)
 
 
 def test_ensemble_vs_oracle(built_lib, oracle_lib, tmp_path):

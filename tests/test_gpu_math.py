@@ -1,11 +1,12 @@
 """Direct accuracy check of the fused kernels' reciprocal and square root.
 
-The kernels replace IEEE division and square root by Newton-Raphson refinements of
-the hardware estimates (nr_rcp / nr_sqrt in hypar_gb300/csrc/gbh_device.cuh) and
-claim a result within one unit in the last place.  gb_probe_rcp_sqrt evaluates them
-on the GPU beside CUDA's correctly rounded 1/x and sqrt(x); both are compared with
-numpy's correctly rounded results in units in the last place (ulp), over 1e6 inputs
-from each range the path feeds them:
+The kernels replace IEEE division and square root by refinements of the hardware
+estimates (nr_rcp / nr_sqrt / nr_rsqrt in hypar_gb300/csrc/gbh_device.cuh) and claim
+a result within one unit in the last place.  gb_probe_rcp_sqrt evaluates them on
+the GPU beside CUDA's correctly rounded 1/x and sqrt(x); both are compared with
+numpy's correctly rounded results in units in the last place (ulp), and 1/sqrt(x)
+with the extended-precision value rounded to double, over 1e6 inputs from each
+range the path feeds them:
 
   * reciprocals of densities and of sums of squared sound speeds: 1e-3 .. 1e3,
   * reciprocals of WENO5 weight normalisations (sums of products of (beta + eps)^2
@@ -35,7 +36,7 @@ def _ulps(a, b):
 def _probe(x):
     L = _lib.lib()
     xd = torch.from_numpy(x).cuda()
-    outs = [torch.empty_like(xd) for _ in range(4)]
+    outs = [torch.empty_like(xd) for _ in range(5)]
     _lib.check(L.gb_probe_rcp_sqrt(xd.data_ptr(), *[o.data_ptr() for o in outs], x.size))
     return [o.cpu().numpy() for o in outs]
 
@@ -44,7 +45,7 @@ def _probe(x):
 def test_rcp_sqrt_within_one_ulp(built_lib, lo, hi):
     rng = np.random.default_rng(20261204)
     x = _log_uniform(rng, lo, hi, N)
-    rcp_nr, rcp_ieee, sqrt_nr, sqrt_ieee = _probe(x)
+    rcp_nr, rcp_ieee, sqrt_nr, sqrt_ieee, rsqrt_nr = _probe(x)
     rcp_exact = 1.0 / x
     sqrt_exact = np.sqrt(x)
     # CUDA's round-to-nearest intrinsics are the correctly rounded results numpy computes
@@ -54,10 +55,13 @@ def test_rcp_sqrt_within_one_ulp(built_lib, lo, hi):
     us = _ulps(sqrt_nr, sqrt_exact)
     assert int(ur.max()) <= 1, (int(ur.max()), float(x[np.argmax(ur)]))
     assert int(us.max()) <= 1, (int(us.max()), float(x[np.argmax(us)]))
+    rsqrt_exact = (1.0 / np.sqrt(x.astype(np.longdouble))).astype(np.float64)
+    uq = _ulps(rsqrt_nr, rsqrt_exact)
+    assert int(uq.max()) <= 1, (int(uq.max()), float(x[np.argmax(uq)]))
 
 
 def test_rcp_sqrt_empty_and_bad_arguments(built_lib):
     L = _lib.lib()
-    _lib.check(L.gb_probe_rcp_sqrt(None, None, None, None, None, 0))
-    assert L.gb_probe_rcp_sqrt(None, None, None, None, None, 4) == 1
-    assert L.gb_probe_rcp_sqrt(None, None, None, None, None, -1) == 1
+    _lib.check(L.gb_probe_rcp_sqrt(None, None, None, None, None, None, 0))
+    assert L.gb_probe_rcp_sqrt(None, None, None, None, None, None, 4) == 1
+    assert L.gb_probe_rcp_sqrt(None, None, None, None, None, None, -1) == 1
