@@ -43,13 +43,22 @@ sys.path.insert(0, ROOT)
 METRIC = "FP64 cell-updates/s & HBM%; ensemble vs serial speedup; adjoint/forward cost"
 UNIT = "cell-component updates/s"
 
-# FP64 floating-point operations per interface per direction of the fused
-# kernels (FMA = 2), from one ncu capture of the x and y launches (FP64-pipe
-# instructions x elapsed cycles, DFMA share from the dfma counter; mean of the
-# two directions of a 2048^2 capture of the segment-walker form);
-# per cell per step this is x (ndims * nstages).  FP64 instructions likewise.
-FP64_FLOPS_PER_INTERFACE = {"vortex": 1607.3}
-FP64_INSTR_PER_INTERFACE = {"vortex": 1005.6}
+# FP64 work of one whole step per grid cell, summed over every kernel of the step:
+# floating-point operations (DFMA = 2, DMUL / DADD = 1) and FP64-pipe thread
+# instructions, from ncu's instruction counters (smsp__sass_thread_inst_executed_op_
+# {dfma,dmul,dadd}_pred_on.sum, sm__thread_inst_executed_pipe_fp64_pred_on.sum) over
+# the launches of one step, captured on the grid given (2-D / 3-D: a smaller grid
+# with the launch shapes the autotuner picks at full size, whose per-cell work is
+# that of the full grid to within the segment-boundary share).
+FP64_PER_CELL_STEP = {
+    "vortex": {"flops": 9606.8, "instr": 6034.4, "captured": "512^2, tiles of 128 interfaces both directions"},
+    "sod": {"flops": 4379.3, "instr": 2831.7, "captured": "1024 (the full grid), lane groups of 8"},
+    "tgv": {"flops": 20307.8, "instr": 13043.4, "captured": "128^3, segments 48/32/48 (the 256^3 shape)"},
+    "rtb": {"flops": 17058.9, "instr": 11874.7, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"},
+    "rtb64": {"flops": 26004.5, "instr": 18095.7, "captured": "64^3 (the full grid), segments 7/7/7"},
+    "dns": {"flops": 21856.8, "instr": 15093.0, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"},
+    "dns64cr": {"flops": 35997.0, "instr": 24360.8, "captured": "64^3 (the full grid), segments 5/5/4"},
+}
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
 # update), per kernel form: the segment walker from the same 2048^2 capture (traffic
 # proportional to cells at these sizes), the tile form from a capture of the default
@@ -334,17 +343,17 @@ def run_ours(args, case, desc, ws, rank, local):
                 "algorithmic_bytes_per_launch": bytes_per_launch}
     step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
                              for st in range(cfg.rk_nstages))
-    fl = FP64_FLOPS_PER_INTERFACE.get(args.workload)
+    fw = FP64_PER_CELL_STEP.get(args.workload) if not args.size else None
     roofline_fp64 = {"bound": "fp64", "peak": fp64_peak, "unit": "TFLOP/s",
                      "peak_source": "measured DFMA loop (gb_probe_fp64_peak) on this GPU"}
-    if fl:
-        fl_step = fl * cfg.ndims * cfg.rk_nstages
-        ach = fl_step * cells * args.steps / t_dev / 1e12
-        ins = FP64_INSTR_PER_INTERFACE[args.workload] * cfg.ndims * cfg.rk_nstages * cells * args.steps
-        pipe = ins / t_dev / (fp64_peak * 1e12 / 2.0)  # the pipe issues one FP64 instruction per FMA slot
-        roofline_fp64.update({"achieved": ach, "frac": ach / fp64_peak, "flops_per_cell_step": fl_step,
-                              "fp64_pipe_busy_frac": pipe,
-                              "flops_source": "ncu FP64 instruction counts (profiles/)"})
+    if fw:
+        ach = fw["flops"] * cells * args.steps / t_dev / 1e12
+        ins = fw["instr"] * cells * args.steps
+        pipe = ins / t_dev / (fp64_peak * 1e12 / 2.0)  # the pipe retires one FP64 instruction per FMA slot
+        roofline_fp64.update({"achieved": ach, "frac": ach / fp64_peak, "flops_per_cell_step": fw["flops"],
+                              "fp64_instr_per_cell_step": fw["instr"], "fp64_pipe_busy_frac": pipe,
+                              "scope": "every kernel of the step, over the step's device time",
+                              "flops_source": "ncu instruction counters of one step, " + fw["captured"]})
     launches_per_step = 0
     for k, (ms_k, n_k) in prof.items():
         # the viscous group is 5 kernels; a CRWENO5 direction is a solve and a flux kernel

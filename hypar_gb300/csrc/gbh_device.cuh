@@ -292,23 +292,30 @@ __device__ __forceinline__ void eigvals(double un, double a, double* lam) {
 // (they differ for the u-reconstruction, whose weights are computed from u
 // while the values are uC = UFunction(u), HyperbolicFunction.c:201-215).
 // ---------------------------------------------------------------------------
-template <bool TP>
+//
+// C0: the window is given relative to its centre cell p[2] (w[2] = v[2] = 0, not
+// read).  The weights depend on differences only and the interpolant reproduces
+// constants, so the pair of the shifted window is the pair of the original one minus
+// p[2]'s value; with a zero centre a third of the stencil terms drop out, and the
+// values stay of the size of the window's variation, so their rounding is far
+// smaller than that of reconstructions of O(1) values.
+template <bool TP, bool C0 = false>
 __device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v, double eps4, double& outL,
                                                 double& outR, double* tp) {
   const double k13 = 13.0 / 3.0;
   // second differences, sub-stencils centred at p1..p4
-  double d1 = fma(-2.0, w[1], w[0]) + w[2];
-  double d2 = fma(-2.0, w[2], w[1]) + w[3];
-  double d3 = fma(-2.0, w[3], w[2]) + w[4];
+  double d1 = C0 ? fma(-2.0, w[1], w[0]) : fma(-2.0, w[1], w[0]) + w[2];
+  double d2 = C0 ? w[1] + w[3] : fma(-2.0, w[2], w[1]) + w[3];
+  double d3 = C0 ? fma(-2.0, w[3], w[4]) : fma(-2.0, w[3], w[2]) + w[4];
   double d4 = fma(-2.0, w[4], w[3]) + w[5];
   double kd1 = k13 * d1, kd2 = k13 * d2, kd3 = k13 * d3, kd4 = k13 * d4;
   // first-difference terms
-  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
+  double gL1 = C0 ? fma(-4.0, w[1], w[0]) : fma(3.0, w[2], fma(-4.0, w[1], w[0]));
   double gL2 = w[1] - w[3];
-  double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
+  double gL3 = C0 ? fma(-4.0, w[3], w[4]) : fma(3.0, w[2], fma(-4.0, w[3], w[4]));
   double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
-  double gR2 = w[4] - w[2];
-  double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
+  double gR2 = C0 ? w[4] : w[4] - w[2];
+  double gR3 = C0 ? fma(3.0, w[3], w[1]) : fma(3.0, w[3], fma(-4.0, w[2], w[1]));
   double BL1 = fma(kd1, d1, fma(gL1, gL1, eps4));
   double BL2 = fma(kd2, d2, fma(gL2, gL2, eps4));
   double BL3 = fma(kd3, d3, fma(gL3, gL3, eps4));
@@ -320,10 +327,10 @@ __device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v
   double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;  // x (1, 1/6, 1/3) of the weights
   double aR1 = qR2 * qR3, aR2 = qR1 * qR3, aR3 = qR1 * qR2;
   // candidates (times 6): two of them shared between the sides
-  double cL1 = fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
+  double cL1 = C0 ? fma(2.0, v[0], -7.0 * v[1]) : fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
   double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3]));
-  double cA = fma(5.0, v[2], fma(2.0, v[3], -v[1]));  // left #2, right #3
-  double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4]));  // left #3, right #2
+  double cA = C0 ? fma(2.0, v[3], -v[1]) : fma(5.0, v[2], fma(2.0, v[3], -v[1]));  // left #2, right #3
+  double cB = C0 ? fma(5.0, v[3], -v[4]) : fma(5.0, v[3], fma(2.0, v[2], -v[4]));  // left #3, right #2
   double nL = fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
   double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
   double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
@@ -349,11 +356,18 @@ __device__ __forceinline__ void weno5_pair(const double* w, const double* v, dou
   weno5_pair_impl<false>(w, v, eps4, outL, outR, nullptr);
 }
 
-// weno5_pair that also stores its smoothness terms B (left 1-3, right 1-3) and the
-// reciprocals of the two normalisations in tp[0..7] (the adjoint's tape).
+// The pair of a window given relative to its centre cell (w[2] = v[2] = 0).
+__device__ __forceinline__ void weno5_pair_c0(const double* w, const double* v, double eps4, double& outL,
+                                              double& outR) {
+  weno5_pair_impl<false, true>(w, v, eps4, outL, outR, nullptr);
+}
+
+// weno5_pair(_c0) that also stores its smoothness terms B (left 1-3, right 1-3) and
+// the reciprocals of the two normalisations in tp[0..7] (the adjoint's tape).
+template <bool C0 = false>
 __device__ __forceinline__ void weno5_pair_tape(const double* w, const double* v, double eps4, double& outL,
                                                 double& outR, double* tp) {
-  weno5_pair_impl<true>(w, v, eps4, outL, outR, tp);
+  weno5_pair_impl<true, C0>(w, v, eps4, outL, outR, tp);
 }
 
 // Left/right WENO5 pair with the other weight formulations (runtime `wtype`).

@@ -73,12 +73,20 @@ __device__ __forceinline__ double rusanov_speed_avg(const Eig& E) {
 // two cell-centre neighbours (their Roe-average ingredients `cl`, `cr` and,
 // when CC, the eigen-system `Ecc` of their Roe average).
 // kappa: the Rusanov dissipation factor max(g_L, g_R) of the gravity field (1 without gravity).
+// ush: when given, uL and uR are relative to ush (and fL, fR relative to some common
+// value, which then carries over to fI): every scheme uses the values linearly
+// except through the states' own Roe average and sound speeds, which take
+// uL + ush and uR + ush.
 template <int M, bool CHAR, int UPW, int DIR>
 __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR, const double* uL,
                                              const double* uR, const Eig& Ecc, const CellAux<M>& cl,
                                              const CellAux<M>& cr, const PhysParams& pp, double* fI,
-                                             double kappa = 1.0) {
+                                             double kappa = 1.0, const double* ush = nullptr) {
   constexpr int NV = ModelTraits<M>::NV;
+  auto actual = [&](const double* x, double* y) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) y[v] = ush ? x[v] + ush[v] : x[v];
+  };
   if (UPW == UPW_RUS) {
     // Rusanov (Euler1DUpwind.c:362-424, NavierStokes3DUpwind.c:349-428):
     // fI = (fL+fR)/2 - alpha (uR-uL)/2, alpha = max of |v|+c over the two
@@ -94,7 +102,10 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
     // cell-centre states otherwise; Harten's fix except for Euler1D.
     Eig Eu;
     if (M == MODEL_EULER2D) {
-      Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+      double aL[NV], aR[NV];
+      actual(uL, aL);
+      actual(uR, aR);
+      Prim<M> qL = to_prim<M>(aL, pp), qR = to_prim<M>(aR, pp);
       Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
     } else {
       Eu = Ecc;
@@ -130,7 +141,10 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
       unR = cr.rs.vel[DIR];
       cR = cr.c;
     } else {
-      Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+      double aL[NV], aR[NV];
+      actual(uL, aL);
+      actual(uR, aR);
+      Prim<M> qL = to_prim<M>(aL, pp), qR = to_prim<M>(aR, pp);
       Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
       unL = qL.vel[DIR];
       cL = sound_speed<M>(qL, pp);
@@ -188,11 +202,12 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
 // cancel (L R = I): fI = R ((xfL+xfR)/2 - |Lambda| (xuR-xuL)/2).  Otherwise the
 // conserved interface values are rebuilt (fL+fR in one projection) and the
 // conserved-variable upwinding applies.
+// ush: as for upwind_iface, the characteristic u values are those of u - ush.
 template <int M, int UPW, int DIR>
 __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR, const double* xuL,
                                             const double* xuR, const Eig& Ecc, const CellAux<M>& cl,
                                             const CellAux<M>& cr, const PhysParams& pp, double* fI,
-                                            double kappa = 1.0) {
+                                            double kappa = 1.0, const double* ush = nullptr) {
   constexpr int NV = ModelTraits<M>::NV;
   if (UPW == UPW_RUS) {
     // a scalar dissipation commutes with the basis: fI = R ((xfL+xfR)/2 - alpha (xuR-xuL)/2)
@@ -247,7 +262,13 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
 #pragma unroll
     for (int k = 0; k < NV; k++) xs[k] = xfL[k] + xfR[k];
     projR<M, DIR>(Ecc, xs, fs);
-    Prim<M> qL = to_prim<M>(uL, pp), qR = to_prim<M>(uR, pp);
+    double aL[NV], aR[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      aL[v] = ush ? uL[v] + ush[v] : uL[v];
+      aR[v] = ush ? uR[v] + ush[v] : uR[v];
+    }
+    Prim<M> qL = to_prim<M>(aL, pp), qR = to_prim<M>(aR, pp);
     Eig Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
     double ud[NV], w[NV], lam[NV];
 #pragma unroll
@@ -268,16 +289,19 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
     double fL[NV], fR[NV];
     projR<M, DIR>(Ecc, xfL, fL);
     projR<M, DIR>(Ecc, xfR, fR);
-    upwind_iface<M, true, UPW, DIR>(fL, fR, uL, uR, Ecc, cl, cr, pp, fI);
+    upwind_iface<M, true, UPW, DIR>(fL, fR, uL, uR, Ecc, cl, cr, pp, fI, 1.0, ush);
   }
 }
 
 // Jiang-Shu pair (the benchmark path) or, in the kernels instantiated with
 // ALTW, the pair with the weight formulation selected at run time.
-template <bool ALTW>
+// C0: the window is relative to its centre cell (w[2] = v[2] = 0; the alternative
+// formulations read the zeros, which the caller stores).
+template <bool ALTW, bool C0 = false>
 __device__ __forceinline__ void wpair(const double* w, const double* v, double eps4, int wtype, double& oL,
                                       double& oR) {
   if (ALTW) weno5_pair_alt(w, v, eps4, wtype, oL, oR);
+  else if (C0) weno5_pair_c0(w, v, eps4, oL, oR);
   else weno5_pair(w, v, eps4, oL, oR);
 }
 
@@ -298,6 +322,23 @@ __device__ __forceinline__ void boundary_flux(const StageEpi& ep, int I, int N, 
 // interface j-1/2): the fused kernel's WENO5 reconstructions (component-wise or
 // characteristic) and upwinding, with the gravity source function's interface value SI
 // (GRAV, source direction) and the adjoint's tape at interface index tapeoff.
+//
+// Centre-relative form (every kernel but the gravity ones, `RelFlux`): the window's
+// cells enter relative to the interface's left cell p[2] = j-1 (its flux, state and
+// modified state subtracted), and fI returns F_{j-1/2} - f_{j-1}.  The reconstructions
+// and the upwinding are linear in the values apart from the weights (invariant under
+// the shift) and the Roe average and sound speeds of the reconstructed states (which
+// take the states with p[2] added back), so the result is the same interface flux
+// minus f_{j-1}; the caller differences it as
+//   F_{i+1/2} - F_{i-1/2} = (f_i - f_{i-1}) + (fI_{i+1/2} - fI_{i-1/2})
+// (HyperbolicFunction.c:94-101 in exact arithmetic).  Values of the size of the
+// window's variation instead of O(1) ones keep the rounding of the reconstruction out
+// of the flux difference, and a third of the WENO5 stencil terms vanish with p[2].
+template <bool GRAV>
+struct RelFlux {
+  static constexpr bool value = !GRAV;
+};
+
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV, bool WT>
 __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>::NV],
                                            const double (&wf)[6][ModelTraits<M>::NV], const double (&wuc)[6],
@@ -307,8 +348,15 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
                                            double (&SI)[ModelTraits<M>::NV]) {
   constexpr int NV = ModelTraits<M>::NV;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  constexpr bool REL = RelFlux<GRAV>::value;
   Eig Ecc;
   if (CC) Ecc = roe_eig<M, DIR>(ax[2].rs, ax[3].rs, pp);
+  // the modified state of the centre cell (the u-reconstruction's values): u with the
+  // UFunction energy (NavierStokes3D; the same as u for the Euler models)
+  double uc2[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) uc2[v] = wu[2][v];
+  uc2[NV - 1] = (M == MODEL_NS3D) ? wuc[2] : wu[2][NV - 1];
   if (!CHAR) {
     // Component-wise WENO5: weights of the u-reconstruction from u, values from uC.
     double fL[NV], fR[NV], uL[NV], uR[NV];
@@ -317,13 +365,13 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
       double sf[6], su[6];
 #pragma unroll
       for (int p = 0; p < 6; p++) {
-        sf[p] = wf[p][v];
-        su[p] = wu[p][v];
+        sf[p] = REL ? (p == 2 ? 0.0 : wf[p][v] - wf[2][v]) : wf[p][v];
+        su[p] = REL ? (p == 2 ? 0.0 : wu[p][v] - wu[2][v]) : wu[p][v];
       }
       if (WT) {
         double* t = ep.tape + tapeoff * TAPE_WIDE + 8 + v * 16;
-        weno5_pair_tape(sf, sf, eps4, fL[v], fR[v], t);
-        weno5_pair_tape(su, su, eps4, uL[v], uR[v], t + 8);
+        weno5_pair_tape<REL>(sf, sf, eps4, fL[v], fR[v], t);
+        weno5_pair_tape<REL>(su, su, eps4, uL[v], uR[v], t + 8);
         continue;
       }
       // the source function phi = g is reconstructed with this flux component's
@@ -334,20 +382,20 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
         weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
         weno5_apply(omL, omR, sf, fL[v], fR[v]);
       } else {
-        wpair<ALTW>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
+        wpair<ALTW, REL>(sf, sf, eps4, pp.wtype, fL[v], fR[v]);
       }
       if (M == MODEL_NS3D && v == NV - 1) {
         double sc[6];
 #pragma unroll
-        for (int p = 0; p < 6; p++) sc[p] = wuc[p];
-        wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
+        for (int p = 0; p < 6; p++) sc[p] = REL ? (p == 2 ? 0.0 : wuc[p] - wuc[2]) : wuc[p];
+        wpair<ALTW, REL>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
       } else if (GRAV) {
         double sc[6];
 #pragma unroll
         for (int p = 0; p < 6; p++) sc[p] = su[p] * wgf[p];
         wpair<ALTW>(su, sc, eps4, pp.wtype, uL[v], uR[v]);
       } else {
-        wpair<ALTW>(su, su, eps4, pp.wtype, uL[v], uR[v]);
+        wpair<ALTW, REL>(su, su, eps4, pp.wtype, uL[v], uR[v]);
       }
       if (srcv) {
         double sL, sR;
@@ -356,15 +404,16 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
       }
     }
     if (M == MODEL_EULER2D && (WT || ep.tape)) {
+      // the adjoint reads the reconstructed states themselves
       double* t = ep.tape + tapeoff * (WT ? TAPE_WIDE : 8);
 #pragma unroll
       for (int v = 0; v < NV; v++) {
-        t[v] = uL[v];
-        t[4 + v] = uR[v];
+        t[v] = REL ? uL[v] + uc2[v] : uL[v];
+        t[4 + v] = REL ? uR[v] + uc2[v] : uR[v];
       }
     }
     upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI,
-                                     GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
+                                     GRAV ? fmax(wgg[2], wgg[3]) : 1.0, REL ? uc2 : nullptr);
   } else {
     // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
     // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
@@ -372,6 +421,31 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
     double cf[6][NV], cu[6][NV], cuc[6][GRAV ? NV : 3];
 #pragma unroll
     for (int p = 0; p < 6; p++) {
+      if (REL && p == 2) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) cf[p][k] = cu[p][k] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) cuc[p][k] = 0.0;
+        continue;
+      }
+      if (REL) {
+        double df[NV], du[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) {
+          df[v] = wf[p][v] - wf[2][v];
+          du[v] = wu[p][v] - wu[2][v];
+        }
+        projL<M, DIR>(Ecc, pp, df, cf[p]);
+        projL<M, DIR>(Ecc, pp, du, cu[p]);
+        if (M == MODEL_NS3D) {
+          // uC differs from u in the energy only: add that column of L.
+          double de = (wuc[p] - wuc[2]) - du[NV - 1];
+          cuc[p][0] = fma(de, Ecc.gh, cu[p][0]);
+          cuc[p][1] = fma(de, Ecc.gh, cu[p][1]);
+          cuc[p][2] = fma(-de, Ecc.gi, cu[p][2]);
+        }
+        continue;
+      }
       projL<M, DIR>(Ecc, pp, wf[p], cf[p]);
       projL<M, DIR>(Ecc, pp, wu[p], cu[p]);
       if (GRAV) {
@@ -413,15 +487,15 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
         weno5_weights<ALTW>(sf, eps4, pp.wtype, omL, omR);
         weno5_apply(omL, omR, sf, xfL[v], xfR[v]);
       } else {
-        wpair<ALTW>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
+        wpair<ALTW, REL>(sf, sf, eps4, pp.wtype, xfL[v], xfR[v]);
       }
       if ((M == MODEL_NS3D && v < 3) || GRAV) {
         double sc[6];
 #pragma unroll
         for (int p = 0; p < 6; p++) sc[p] = cuc[p][v];
-        wpair<ALTW>(su, sc, eps4, pp.wtype, xuL[v], xuR[v]);
+        wpair<ALTW, REL>(su, sc, eps4, pp.wtype, xuL[v], xuR[v]);
       } else {
-        wpair<ALTW>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
+        wpair<ALTW, REL>(su, su, eps4, pp.wtype, xuL[v], xuR[v]);
       }
       if (src_dir) {
         double sL, sR, ps[6];
@@ -432,9 +506,9 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
       }
     }
     if (src_dir) projR<M, DIR>(Ecc, sch, SI);
-    upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0);
+    upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0,
+                             REL ? uc2 : nullptr);
   }
-
 }
 
 // One thread's share of a launch: interfaces [sg*seg, min((sg+1)*seg, N)] of
@@ -456,6 +530,7 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
                                             int sg) {
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
+  constexpr bool REL = RelFlux<GRAV>::value;
   const long long line = tr;
 
   long long pbase = (long long)G.g * G.stride[DIR];
@@ -537,7 +612,10 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
 #pragma unroll
       for (int e = 0; e < ND; e++)
         if (e != DIR) ntr *= G.dim[e];
-      boundary_flux<NV>(ep, I, N, line, ntr, fI);
+      double Fb[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) Fb[v] = REL ? fI[v] + wf[2][v] : fI[v];
+      boundary_flux<NV>(ep, I, N, line, ntr, Fb);
     }
 
     if (I > I0) {
@@ -558,7 +636,8 @@ __device__ __forceinline__ void hyp_segment(const double* __restrict__ U, double
       }
 #pragma unroll
       for (int v = 0; v < NV; v++) {
-        double h = dxi * (fI[v] - fIp[v]);
+        // centre-relative fluxes: F_I - F_{I-1} = (f_c - f_{c-1}) + (fI_I - fI_{I-1})
+        double h = REL ? dxi * ((wf[2][v] - wf[1][v]) + (fI[v] - fIp[v])) : dxi * (fI[v] - fIp[v]);
         if (src_dir) h = fma(-term[v] * (SI[v] - SIp[v]), dxi, h);  // rhs = -hyp + source
         double hyp = ep.first ? h : H[off + v] + h;
         if (!finish) {
@@ -708,7 +787,13 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
     double fI[NV], SI[NV];
     iface_flux<M, CHAR, UPW, DIR, ALTW, false, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, false,
                                                    line * (N + 1) + I, fI, SI);
-    boundary_flux<NV>(ep, I, N, line, ntrans, fI);
+    // fI is relative to the interface's left cell (window cell 2)
+    if (ep.bnd && (I == 0 || I == N)) {
+      double Fb[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) Fb[v] = fI[v] + wf[2][v];
+      boundary_flux<NV>(ep, I, N, line, ntrans, Fb);
+    }
 #pragma unroll
     for (int v = 0; v < NV; v++) sfI[t][v] = fI[v];
   }
@@ -718,8 +803,9 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
     const long long off = (pbase + (long long)c * sd) * NV;
     const double dxi = dxinv[G.g + c];
     double h[NV];
+    // cell c is tile cell t + 3; F_{c+1} - F_c = (f_c - f_{c-1}) + (fI_{t+1} - fI_t)
 #pragma unroll
-    for (int v = 0; v < NV; v++) h[v] = dxi * (sfI[t + 1][v] - sfI[t][v]);
+    for (int v = 0; v < NV; v++) h[v] = dxi * ((sf[t + 3][v] - sf[t + 2][v]) + (sfI[t + 1][v] - sfI[t][v]));
     stage_epilogue<NV>(ep, H, off, h);
   }
 }
@@ -776,11 +862,13 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
     const int i = t >> 3, k = t & 7;
     if (k < 2 * NV && I0 + i <= N) {
       const int v = k >> 1;
+      // the window relative to the interface's left cell (window cell 2)
       double w[6];
 #pragma unroll
-      for (int p = 0; p < 6; p++) w[p] = (k & 1) ? su[i + p][v] : sf[i + p][v];
+      for (int p = 0; p < 6; p++)
+        w[p] = p == 2 ? 0.0 : ((k & 1) ? su[i + p][v] - su[i + 2][v] : sf[i + p][v] - sf[i + 2][v]);
       double oL, oR;
-      wpair<ALTW>(w, w, eps4, pp.wtype, oL, oR);
+      wpair<ALTW, true>(w, w, eps4, pp.wtype, oL, oR);
       srec[i][k][0] = oL;
       srec[i][k][1] = oR;
     }
@@ -797,8 +885,16 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
     }
     Eig Ecc;
     if (CC) Ecc = roe_eig<M, 0>(sax[t + 2].rs, sax[t + 3].rs, pp);
-    upwind_iface<M, false, UPW, 0>(fL, fR, uL, uR, Ecc, sax[t + 2], sax[t + 3], pp, fI);
-    boundary_flux<NV>(ep, I0 + t, N, 0, 1, fI);
+    double uc2[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) uc2[v] = su[t + 2][v];
+    upwind_iface<M, false, UPW, 0>(fL, fR, uL, uR, Ecc, sax[t + 2], sax[t + 3], pp, fI, 1.0, uc2);
+    if (ep.bnd && (I0 + t == 0 || I0 + t == N)) {
+      double Fb[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) Fb[v] = fI[v] + sf[t + 2][v];
+      boundary_flux<NV>(ep, I0 + t, N, 0, 1, Fb);
+    }
 #pragma unroll
     for (int v = 0; v < NV; v++) sfI[t][v] = fI[v];
   }
@@ -808,16 +904,19 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
     const long long off = (pbase + (long long)c * sd) * NV;
     const double dxi = dxinv[G.g + c];
     double h[NV];
+    // centre-relative fluxes, as in hyp_tile_body
 #pragma unroll
-    for (int v = 0; v < NV; v++) h[v] = dxi * (sfI[t + 1][v] - sfI[t][v]);
+    for (int v = 0; v < NV; v++) h[v] = dxi * ((sf[t + 3][v] - sf[t + 2][v]) + (sfI[t + 1][v] - sfI[t][v]));
     stage_epilogue<NV>(ep, H, off, h);
   }
 }
 
 // Resident blocks per SM the register allocation of the 128-interface tile kernels
-// must allow (1: as many registers as the kernel wants).
+// must allow: 4 (at most 128 registers a thread) keeps four 128-thread blocks on an
+// SM, which the kernel needs to keep the FP64 pipe busy (1: as many registers as the
+// compiler wants).
 #ifndef GBH_TILE_MINB
-#define GBH_TILE_MINB 1
+#define GBH_TILE_MINB 4
 #endif
 
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, int TI, bool WT = false>
