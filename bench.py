@@ -897,6 +897,53 @@ def cpu_baseline(case, budget_s: float = 15.0, threads: int = 0):
             "seconds_per_step": el / steps}
 
 
+def run_ref_vs_port(args, case, desc):
+    """The reference's own CPU build (oracle/_ref/HyPar, compiled from the reference's
+    sources by oracle/Makefile.ref where they are present) against the oracle port on
+    the same deck, single-threaded and with every host thread: seconds per step of
+    each.  A step of the reference is timed as the difference of two runs of the same
+    deck (n_iter = 1 and 1 + steps), which cancels start-up, input and output.  The
+    reference's OpenMP build races in characteristic WENO5 (L and uavg shared in
+    WENOFifthOrderCalculateWeightsCharJS); its timing is still its own."""
+    import numpy as np
+    import oracle as O
+    exe = os.path.join(ROOT, "oracle", "_ref", "HyPar")
+    if not os.path.exists(exe):
+        return {"impl": "ref-vs-port", "unavailable": "oracle/_ref/HyPar is not built here (needs the reference's "
+                                                      "source tree, HYPAR_REF)"}
+    O.build()
+    steps = max(1, args.steps)
+    nthr = os.cpu_count() or 1
+    cells = int(np.prod(case.size))
+
+    def ref_time(n_iter, threads):
+        d = tempfile.mkdtemp(prefix="gbh_refrun_")
+        case.n_iter = n_iter
+        case.file_op_iter = 10 ** 6
+        case.write(d)
+        env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+        t0 = time.perf_counter()
+        subprocess.run([exe], cwd=d, env=env, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        return time.perf_counter() - t0
+
+    def port_time(threads):
+        O.set_threads(threads)
+        P = O.Problem(case)
+        u = P.rk(P.u0(), 1)
+        t0 = time.perf_counter()
+        P.rk(u, steps)
+        return (time.perf_counter() - t0) / steps
+
+    rows = {}
+    for threads in (1, nthr):
+        tr = (ref_time(1 + steps, threads) - ref_time(1, threads)) / steps
+        tp = port_time(threads)
+        rows[str(threads)] = {"reference_s_per_step": tr, "port_s_per_step": tp, "port_speedup": tr / tp}
+    return {"impl": "ref-vs-port", "config": {"workload": desc, "cells": cells, "timed_steps": steps},
+            "threads": rows,
+            "note": "reference = the reference's own serial+OpenMP build of its sources; port = oracle/gbh_oracle.c"}
+
+
 def run_reference(args, case, desc, ws, rank):
     if rank != 0:
         return None
@@ -952,7 +999,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "ref-vs-port"],
+                    help="ref-vs-port: the reference's own CPU build against the oracle port (CPU only, where "
+                         "the reference's sources were built into oracle/_ref)")
     ap.add_argument("--workload", default="vortex", choices=["vortex", "tgv", "sod", "rtb", "rtb64", "dns", "dns64cr", "ensemble", "adjoint",
                                                           "convergence", "parity", "kernel-vjp", "kernel-jvp",
                                                           "kernel-step"])
@@ -980,6 +1029,9 @@ def main():
             print(json.dumps(out))
         return
     case, desc = workload(args.workload, args.size)
+    if args.impl == "ref-vs-port":
+        print(json.dumps(run_ref_vs_port(args, case, desc)))
+        return
     if args.impl == "reference":
         out = run_reference(args, case, desc, ws, rank)
     else:

@@ -28,3 +28,18 @@ def test_reference_arm_json_line(oracle_lib):
     case, desc = bench.workload("sod")
     ours = bench.common_config(case, desc, argparse.Namespace(steps=2), 1)
     assert d["config"] == json.loads(json.dumps(ours))
+
+
+def test_reference_build_against_port(oracle_lib):
+    """bench.py --impl ref-vs-port times the reference's own CPU build (oracle/_ref/HyPar)
+    against the oracle port on one deck; skipped where the reference was not built."""
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_ref", "HyPar")):
+        import pytest
+        pytest.skip("oracle/_ref/HyPar is not built here")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "ref-vs-port", "--workload",
+                          "vortex", "--size", "48", "--steps", "1"], capture_output=True, text=True, check=True,
+                         cwd=ROOT, timeout=600).stdout
+    d = json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+    assert d["impl"] == "ref-vs-port"
+    for row in d["threads"].values():
+        assert row["reference_s_per_step"] > 0 and row["port_s_per_step"] > 0
