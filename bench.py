@@ -51,9 +51,9 @@ UNIT = "cell-component updates/s"
 # with the launch shapes the autotuner picks at full size, whose per-cell work is
 # that of the full grid to within the segment-boundary share).
 FP64_PER_CELL_STEP = {
-    "vortex": {"flops": 9606.8, "instr": 6034.4, "captured": "512^2, tiles of 128 interfaces both directions"},
-    "sod": {"flops": 4379.3, "instr": 2831.7, "captured": "1024 (the full grid), lane groups of 8"},
-    "tgv": {"flops": 20307.8, "instr": 13043.4, "captured": "128^3, segments 48/32/48 (the 256^3 shape)"},
+    "vortex": {"flops": 8745.8, "instr": 5698.9, "captured": "512^2, segments 54/27 (the 1024^2 shape)"},
+    "sod": {"flops": 3641.9, "instr": 2446.6, "captured": "1024 (the full grid), lane groups of 16"},
+    "tgv": {"flops": 18346.9, "instr": 12262.5, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"},
     "rtb": {"flops": 17058.9, "instr": 11874.7, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"},
     "rtb64": {"flops": 26004.5, "instr": 18095.7, "captured": "64^3 (the full grid), segments 7/7/7"},
     "dns": {"flops": 21856.8, "instr": 15093.0, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"},

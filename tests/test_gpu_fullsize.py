@@ -5,11 +5,13 @@ and so is the 1024^2 vortex over 100 SSPRK3 steps (about 30 s on 16 host cores):
 both are held to relative L2 <= 1e-10 of the state.  The 256^3 Taylor-Green
 vortex over 100 RK4 steps takes the oracle about 11 minutes on 16 cores; that
 leg runs when HYPAR_LONG_VALIDATION=1 is set.
-For the 1024^2 vortex and the 256^3 Taylor-Green vortex the oracle also evaluates one
-right-hand side at full size: relative L2 <= 1e-12, or, where the state's own
-conditioning puts rounding noise above that (a flux difference over a fine grid
-cancels O(1) fluxes to O(h)), within 4x the distance between the oracle and its
-FMA-contracted build, which measures that noise.  A size-independent
+For the 1024^2 vortex and a perturbed 256^3 Taylor-Green vortex the oracle also
+evaluates one right-hand side at full size: relative L2 <= 1e-12.  (A flux difference
+over a fine grid cancels O(1) fluxes to O(h), so rounding is amplified by the grid
+size; the kernels difference fluxes taken relative to each interface's left cell,
+which keeps their own share of that rounding below the reference's: at 1024^2 the
+oracle and its FMA-contracted build differ by 8e-13, the GPU and the oracle by
+7.6e-13.)  A size-independent
 property covers many steps: on a periodic grid the conservative flux difference
 telescopes, so the domain sums of the conserved variables stay constant to
 rounding.  (The viscous term does not telescope near the faces: on one rank the
@@ -67,8 +69,7 @@ def _rhs_vs_oracle(s, case):
     s.rhs(out, u)
     got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
     ref = O.interior(P.rhs(u0.copy()), case.size, case.nvars, 3)
-    noise = relerr(O.interior(O.Problem(case, fma=True).rhs(u0.copy()), case.size, case.nvars, 3), ref)
-    return relerr(got, ref), max(RHS_TOL, 4.0 * noise)
+    return relerr(got, ref), RHS_TOL
 
 
 def _sums(s, case):
