@@ -244,7 +244,7 @@ int gbh_validate(const gb_config* c) {
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
-    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SUPERSONIC_OUTFLOW || q[1] < 0 || q[1] >= nd ||
+    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SUBSONIC_AMBIVALENT || q[1] < 0 || q[1] >= nd ||
         (q[2] != 1 && q[2] != -1)) {
       gbh_set_error("bad zone %d", z);
       return GB_ERR_ARG;

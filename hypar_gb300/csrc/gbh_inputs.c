@@ -758,7 +758,8 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
           {"noslip-wall", GB_BC_NOSLIP_WALL, -2},    {"subsonic-inflow", GB_BC_SUBSONIC_INFLOW, -3},
           {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW, 1},
           {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW, -4},
-          {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW, 0}};
+          {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW, 0},
+          {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT, -4}};
       int tcode = 0, nvals = 0;
       for (size_t t = 0; t < sizeof(bct) / sizeof(bct[0]); t++)
         if (!strcmp(type, bct[t].name)) {

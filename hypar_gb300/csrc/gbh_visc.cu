@@ -219,7 +219,7 @@ struct ZoneDev {
 // BCSubsonicOutflow.c, BCSupersonicInflow.c, BCSupersonicOutflow.c; 2-D and 3-D
 // branches), in their operation order without contraction.
 template <int ND>
-__device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out) {
+__device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out, bool inflow = false) {
   constexpr int NV = ND + 2;
   const double gm1 = z.gamma - 1.0;
   const double inv_gm1 = __ddiv_rn(1.0, gm1);
@@ -246,6 +246,16 @@ __device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, doub
       rg = z.data[0];
       for (int d = 0; d < ND; d++) vg[d] = z.data[1 + d];
       Pg = z.data[1 + ND];
+      break;
+    case GB_BC_SUBSONIC_AMBIVALENT:
+      // BCSubsonicAmbivalent.c:105-117: inflow's rule (density, velocity given) or
+      // outflow's (pressure given) by the sign of the extrapolated face velocity
+      if (inflow) {
+        rg = z.data[0];
+        for (int d = 0; d < ND; d++) vg[d] = z.data[1 + d];
+      } else {
+        Pg = z.data[1 + ND];
+      }
       break;
     default: break;  // supersonic outflow: the interior state, energy recomputed
   }
@@ -281,9 +291,30 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
   } else if (z.type == GB_BC_DIRICHLET) {
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = z.data[v];
   } else {
+    bool inflow = false;
+    if (z.type == GB_BC_SUBSONIC_AMBIVALENT) {
+      // BCSubsonicAmbivalent.c:70-92: the face velocity extrapolated from the boundary
+      // cell and its neighbour at this transverse position, 1.5 v_1 - 0.5 v_2, on the
+      // inward normal face * e_dim (only interior points are read: no ordering with the
+      // ghost writes of other threads)
+      long long q1 = 0, q2 = 0;
+      for (int d = 0; d < G.nd; d++) {
+        const int i1 = d == dd ? (z.face == 1 ? 0 : N - 1) : ig[d];
+        const int i2 = d == dd ? (z.face == 1 ? 1 : N - 2) : ig[d];
+        q1 += (long long)(i1 + G.g) * G.stride[d];
+        q2 += (long long)(i2 + G.g) * G.stride[d];
+      }
+      const double *w1 = u + q1 * nv, *w2 = u + q2 * nv;
+      const double r1 = w1[0], r2 = w2[0];
+      const double m1 = w1[1 + dd], m2 = w2[1 + dd];
+      const double v1 = (G.nd == 3 && r1 == 0.0) ? 0.0 : __ddiv_rn(m1, r1);
+      const double v2 = (G.nd == 3 && r2 == 0.0) ? 0.0 : __ddiv_rn(m2, r2);
+      const double vb = __dsub_rn(__dmul_rn(1.5, v1), __dmul_rn(0.5, v2));
+      inflow = (z.face == 1) ? vb > 0.0 : vb < 0.0;
+    }
     double g[5];
-    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g);
-    else bc_ghost<3>(z, u + p2 * nv, g);
+    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow);
+    else bc_ghost<3>(z, u + p2 * nv, g, inflow);
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = g[v];
   }
 }

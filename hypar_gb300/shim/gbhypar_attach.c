@@ -151,7 +151,7 @@ int gbshim_config(void *s, gb_config *c) {
         {"dirichlet", GB_BC_DIRICHLET},        {"slip-wall", GB_BC_SLIP_WALL},
         {"noslip-wall", GB_BC_NOSLIP_WALL},    {"subsonic-inflow", GB_BC_SUBSONIC_INFLOW},
         {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW}, {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW},
-        {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}};
+        {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}, {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT}};
     int code = 0;
     for (size_t t = 0; t < sizeof(types) / sizeof(types[0]); t++)
       if (!strcmp(B->bctype, types[t].name)) code = types[t].code;
@@ -182,6 +182,7 @@ int gbshim_config(void *s, gb_config *c) {
         v[0] = B->FlowPressure;
         break;
       case GB_BC_SUPERSONIC_INFLOW:
+      case GB_BC_SUBSONIC_AMBIVALENT:
         v[0] = B->FlowDensity;
         for (int k = 0; k < nd; k++) v[1 + k] = B->FlowVelocity[k];
         v[1 + nd] = B->FlowPressure;

@@ -41,11 +41,13 @@ enum { GB_MODEL_EULER1D = 1, GB_MODEL_EULER2D = 2, GB_MODEL_NS3D = 3 };
 enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2, GB_UPWIND_RUSANOV = 3 /* Euler1D, NS3D */ };
 enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
 /* boundary.inp types (include/boundaryconditions.h): periodic and extrapolate for every
- * model; dirichlet for every model; the wall and inflow/outflow types for Euler2D and
- * NavierStokes3D (the reference's 1-D branches of those are incomplete). */
+ * model; dirichlet for every model; the wall and inflow/outflow types, and the
+ * subsonic "ambivalent" one (inflow or outflow point by point, by the sign of the
+ * extrapolated face velocity), for Euler2D and NavierStokes3D (the reference's 1-D
+ * branches of those are incomplete). */
 enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2, GB_BC_DIRICHLET = 3, GB_BC_SLIP_WALL = 4,
        GB_BC_NOSLIP_WALL = 5, GB_BC_SUBSONIC_INFLOW = 6, GB_BC_SUBSONIC_OUTFLOW = 7,
-       GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9 };
+       GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9, GB_BC_SUBSONIC_AMBIVALENT = 10 };
 enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
 /* WENO5 nonlinear weights (weno.inp: yc > borges > mapped > Jiang-Shu, and
  * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
@@ -82,7 +84,8 @@ typedef struct gb_config {
   int write_residual;       /* solver.inp write_residual: residual.out with the norms */
   /* per zone, the values boundary.inp gives after the extents: dirichlet: nvars values;
    * slip-wall / noslip-wall: wall velocity (ndims); subsonic-inflow: rho, velocity;
-   * subsonic-outflow: pressure; supersonic-inflow: rho, velocity, pressure */
+   * subsonic-outflow: pressure; supersonic-inflow and subsonic-ambivalent: rho, velocity,
+   * pressure */
   double zone_data[GB_MAX_ZONES][8];
   /* NavierStokes3D gravity (physics.inp gravity, rho_ref, p_ref, R, HB, N_bv); a nonzero
    * acceleration needs upwinding rusanov (NavierStokes3DInitialize.c:371) and the

@@ -35,7 +35,8 @@ UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3}
 INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,
-          "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9}
+          "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9,
+          "subsonic-ambivalent": 10}
 
 
 SCHEMES = {"weno5": 0, "crweno5": 1}
@@ -44,7 +45,8 @@ SCHEMES = {"weno5": 0, "crweno5": 1}
 def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
     """How many values boundary.inp gives after a zone's extents (InitializeBoundaries.c:109-188)."""
     return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
-            "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims}.get(bctype, 0)
+            "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims,
+            "subsonic-ambivalent": 2 + ndims}.get(bctype, 0)
 
 _lib = None
 

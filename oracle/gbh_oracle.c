@@ -246,8 +246,10 @@ static long pidx(const orc_problem *p, const long *s, const int *i) {
 /* Ghost state of the wall and inflow / outflow types from the mirror interior
  * state w, 2-D (Euler2D/NavierStokes2D flow variables) and 3-D branches of
  * BCSlipWall.c, BCNoslipWall.c, BCSubsonicInflow.c, BCSubsonicOutflow.c,
- * BCSupersonicInflow.c and BCSupersonicOutflow.c. */
-static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, double *out) {
+ * BCSupersonicInflow.c, BCSupersonicOutflow.c and BCSubsonicAmbivalent.c (which
+ * takes inflow's or outflow's rule by `inflow`, the sign of the extrapolated face
+ * velocity along the inward normal). */
+static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, double *out, int inflow) {
   double inv_gamma_m1 = 1.0 / (gamma - 1.0);
   double rho = 0, vel[3] = {0, 0, 0}, energy, pressure = 0, vsq;
   if (b->type != ORC_BC_SUPERSONIC_INFLOW) {
@@ -283,6 +285,16 @@ static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, do
       p_g = b->data[1 + nd];
       break;
     case ORC_BC_SUPERSONIC_OUTFLOW: break;
+    case ORC_BC_SUBSONIC_AMBIVALENT:
+      /* BCSubsonicAmbivalent.c:105-117: inflow takes density and velocity, outflow the
+       * pressure (data: rho, velocity, pressure) */
+      if (inflow) {
+        rho_g = b->data[0];
+        for (int d = 0; d < nd; d++) v_g[d] = b->data[1 + d];
+      } else {
+        p_g = b->data[1 + nd];
+      }
+      break;
     default: return 1;
   }
   double e_g;
@@ -329,7 +341,26 @@ int orc_apply_bc(const orc_problem *p, double *u) {
         /* BCDirichletU (BCDirichlet.c:27-41) */
         for (int v = 0; v < nv; v++) u[nv * p1 + v] = b->data[v];
       } else if (nd == 2 || nd == 3) {
-        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1)) return 1;
+        int inflow = 0;
+        if (b->type == ORC_BC_SUBSONIC_AMBIVALENT) {
+          /* BCSubsonicAmbivalent.c:70-92: the face velocity extrapolated (second order)
+           * from the boundary cell and its neighbour at this transverse position,
+           * 1.5 v_1 - 0.5 v_2, projected on the inward normal face * e_dim */
+          int i1[3], i2[3];
+          for (int d = 0; d < nd; d++) i1[d] = i2[d] = ig[d];
+          i1[dd] = b->face == 1 ? 0 : N - 1;
+          i2[dd] = b->face == 1 ? 1 : N - 2;
+          const double *w1 = u + nv * pidx(p, s, i1), *w2 = u + nv * pidx(p, s, i2);
+          double vb[3] = {0, 0, 0}, vn = 0.0;
+          for (int d = 0; d < nd; d++) {
+            double v1 = (nd == 3 && w1[0] == 0) ? 0 : w1[1 + d] / w1[0];
+            double v2 = (nd == 3 && w2[0] == 0) ? 0 : w2[1 + d] / w2[0];
+            vb[d] = 1.5 * v1 - 0.5 * v2;
+          }
+          for (int d = 0; d < nd; d++) vn = vn + vb[d] * (d == dd ? (double)b->face : 0.0);
+          inflow = vn > 0;
+        }
+        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1, inflow)) return 1;
       } else {
         return 1;
       }

@@ -24,7 +24,7 @@ enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2, ORC_UPW_RUSANOV = 3 };
 enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
 enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
        ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,
-       ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9 };
+       ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9, ORC_BC_SUBSONIC_AMBIVALENT = 10 };
 
 /* One boundary zone, as DomainBoundary after CalculateLocalExtent
  * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index

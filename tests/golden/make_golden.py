@@ -142,7 +142,23 @@ CASES = {
     "tgv12_cons_comp_roe_noslip": lambda: _cons(_b(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), {
         (2, 1): ("noslip-wall", [0.0, 0.0, 0.0]), (2, -1): ("noslip-wall", [0.0, 0.0, 0.0])})),
     "rtb12_cons_comp_rusanov_yc": lambda: _cons(C.rising_thermal_bubble(12, n_iter=3, dt=0.05, perturb=0.02)),
+    # subsonic "ambivalent" faces: inflow or outflow point by point by the sign of the
+    # extrapolated face velocity (random velocities make both occur on every face)
+    "vortex24_char_roe_ambivalent": lambda: _b(_stir2(C.vortex(24, n_iter=4, dt=0.01)), {
+        (0, 1): ("subsonic-ambivalent", [1.0, 0.5, 0.0, 1.0]), (0, -1): ("subsonic-ambivalent", [1.0, 0.5, 0.0, 1.0]),
+        (1, 1): ("subsonic-ambivalent", [1.1, 0.0, 0.2, 0.9]), (1, -1): ("subsonic-ambivalent", [0.9, 0.1, 0.0, 1.1])}),
+    "tgv12_comp_llf_ambivalent_rk4": lambda: _b(_stir(C.tgv(12, n_iter=3, dt=0.02, upwinding="llf-char",
+                                                            perturb=0.05), speed=0.3), {
+        (2, 1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, 0.1, 1.0 / 1.4]),
+        (2, -1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, -0.1, 1.0 / 1.4])}),
 }
+
+
+def _stir2(case, speed=0.3, seed=13):
+    """Random velocities of about `speed` on a 2-D deck's state, the energy kept."""
+    rng = np.random.default_rng(seed)
+    case.u[:, 1:3] = speed * rng.standard_normal((case.u.shape[0], 2)) * case.u[:, :1]
+    return case
 
 
 def _cons(case):
