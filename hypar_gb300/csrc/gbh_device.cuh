@@ -178,6 +178,11 @@ __device__ __forceinline__ double nr_rsqrt(double x) {
   return fma(y, e * fma(0.375, e, 0.5), y);
 }
 
+// The eigen-system's remaining quantities once the Roe-averaged velocity, enthalpy
+// and density (E.vel, E.H, E.rho) and |v|^2 are set.
+template <int M, int DIR>
+__device__ __forceinline__ void roe_eig_finish(Eig& E, double vsq, const PhysParams& pp);
+
 template <int M, int DIR>
 __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const PhysParams& pp) {
   constexpr int ND = ModelTraits<M>::ND;
@@ -192,13 +197,53 @@ __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const
     vsq = fma(E.vel[k], E.vel[k], vsq);
   }
   E.H = fma(L.t, L.H, R.t * R.H) * inv;
+  E.rho = L.t * R.t;
+  roe_eig_finish<M, DIR>(E, vsq, pp);
+  return E;
+}
+
+// Roe average of two conserved states in one pass (the reconstructed states of
+// Euler2D's Roe upwinding, Euler2DUpwind.c:39): with r = 1/sqrt(rho) of each state,
+// sqrt(rho) = rho r, sqrt(rho) v = m r and sqrt(rho) H = (e + P) r, where
+// P = (e - |m r|^2 / 2) (gamma - 1); so neither 1/rho nor the velocities are formed.
+template <int M, int DIR>
+__device__ __forceinline__ Eig roe_eig_cons(const double* a, const double* b, const PhysParams& pp) {
+  constexpr int ND = ModelTraits<M>::ND, NV = ModelTraits<M>::NV;
+  const double ra = nr_rsqrt(a[0]), rb = nr_rsqrt(b[0]);
+  const double ta = a[0] * ra, tb = b[0] * rb;
+  double wa[3], wb[3], qa = 0.0, qb = 0.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    wa[k] = a[1 + k] * ra;
+    wb[k] = b[1 + k] * rb;
+    qa = fma(wa[k], wa[k], qa);
+    qb = fma(wb[k], wb[k], qb);
+  }
+  const double Pa = fma(-0.5, qa, a[NV - 1]) * pp.gm1, Pb = fma(-0.5, qb, b[NV - 1]) * pp.gm1;
+  Eig E;
+  const double inv = nr_rcp(ta + tb);
+  double vsq = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) E.vel[k] = 0.0;
+#pragma unroll
+  for (int k = 0; k < ND; k++) {
+    E.vel[k] = (wa[k] + wb[k]) * inv;
+    vsq = fma(E.vel[k], E.vel[k], vsq);
+  }
+  E.H = fma(a[NV - 1] + Pa, ra, (b[NV - 1] + Pb) * rb) * inv;
+  E.rho = ta * tb;
+  roe_eig_finish<M, DIR>(E, vsq, pp);
+  return E;
+}
+
+template <int M, int DIR>
+__device__ __forceinline__ void roe_eig_finish(Eig& E, double vsq, const PhysParams& pp) {
   E.ek = 0.5 * vsq;
   double a2 = pp.gm1 * (E.H - E.ek);
   double ia = nr_rsqrt(a2);  // 1/a
   E.a = a2 * ia;
   E.inv_a2 = ia * ia;
   E.un = E.vel[DIR];
-  E.rho = L.t * R.t;
   if (M == MODEL_EULER1D) {
     // hac = 1/(rho a), rs = rho/(2a) = 1/(2 a^2 hac)
     E.hac = nr_rcp(E.rho) * ia;
@@ -211,7 +256,16 @@ __device__ __forceinline__ Eig roe_eig(const RoeSide& L, const RoeSide& R, const
   E.gi = pp.gm1 * E.inv_a2;
   E.ah = E.a * E.hac;
   E.aun = E.a * E.un;
-  return E;
+}
+
+// Harten's entropy fix of |lambda| with delta = 1e-6 (Euler2DUpwind.c:45-51,
+// NavierStokes3DUpwind.c:97-102): (lambda^2 + delta^2) / (2 delta) inside |lambda| < delta.
+// The comparison is made on the bit patterns (non-negative doubles order as their
+// integers do; a NaN compares above), which keeps it off the FP64 pipe.
+__device__ __forceinline__ double harten_abs(double lam) {
+  const double delta = 0.000001, delta2 = delta * delta;
+  const double d = fabs(lam);
+  return (__double_as_longlong(d) < __double_as_longlong(delta)) ? fma(lam, lam, delta2) * (0.5 / delta) : d;
 }
 
 // Characteristic fields, in this order: 0 acoustic (u_n - a), 1 acoustic

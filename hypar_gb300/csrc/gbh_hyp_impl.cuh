@@ -105,8 +105,7 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
       double aL[NV], aR[NV];
       actual(uL, aL);
       actual(uR, aR);
-      Prim<M> qL = to_prim<M>(aL, pp), qR = to_prim<M>(aR, pp);
-      Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
+      Eu = roe_eig_cons<M, DIR>(aL, aR, pp);
     } else {
       Eu = Ecc;
     }
@@ -117,13 +116,9 @@ __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR,
     eigvals<M>(Eu.un, Eu.a, lam);
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-      double d = fabs(lam[k]);
-      if (M != MODEL_EULER1D) {
-        const double delta = 0.000001, delta2 = delta * delta;
-        d = (d < delta) ? (lam[k] * lam[k] + delta2) * (0.5 / delta) : d;
-      } else {
-        d = kappa * d;  // Euler1DUpwind.c:79-82 (gravity field; 1 without)
-      }
+      // Harten's fix (Euler2D, NavierStokes3D); Euler1D: |lambda| times the gravity
+      // field's factor (Euler1DUpwind.c:79-82; 1 without gravity)
+      const double d = (M != MODEL_EULER1D) ? harten_abs(lam[k]) : kappa * fabs(lam[k]);
       w[k] *= d;
     }
     projR<M, DIR>(Eu, w, ud);
@@ -225,13 +220,7 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
     if (UPW == UPW_ROE) {
 #pragma unroll
       for (int k = 0; k < NV; k++) {
-        double d = fabs(lamC[k]);
-        if (M != MODEL_EULER1D) {
-          const double delta = 0.000001, delta2 = delta * delta;
-          d = (d < delta) ? (lamC[k] * lamC[k] + delta2) * (0.5 / delta) : d;
-        } else {
-          d = kappa * d;
-        }
+        const double d = (M != MODEL_EULER1D) ? harten_abs(lamC[k]) : kappa * fabs(lamC[k]);
         fc[k] = 0.5 * fma(-d, xuR[k] - xuL[k], xfL[k] + xfR[k]);
       }
     } else {
@@ -268,20 +257,14 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
       aL[v] = ush ? uL[v] + ush[v] : uL[v];
       aR[v] = ush ? uR[v] + ush[v] : uR[v];
     }
-    Prim<M> qL = to_prim<M>(aL, pp), qR = to_prim<M>(aR, pp);
-    Eig Eu = roe_eig<M, DIR>(roe_side<M>(qL), roe_side<M>(qR), pp);
+    Eig Eu = roe_eig_cons<M, DIR>(aL, aR, pp);
     double ud[NV], w[NV], lam[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) ud[v] = 0.5 * (uR[v] - uL[v]);
     projL<M, DIR>(Eu, pp, ud, w);
     eigvals<M>(Eu.un, Eu.a, lam);
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-      double d = fabs(lam[k]);
-      const double delta = 0.000001, delta2 = delta * delta;
-      d = (d < delta) ? (lam[k] * lam[k] + delta2) * (0.5 / delta) : d;
-      w[k] *= d;
-    }
+    for (int k = 0; k < NV; k++) w[k] *= harten_abs(lam[k]);
     projR<M, DIR>(Eu, w, ud);
 #pragma unroll
     for (int v = 0; v < NV; v++) fI[v] = fma(0.5, fs[v], -ud[v]);
