@@ -495,15 +495,30 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
 // one grid line and the TI + 5 cells their windows touch.  The cells' states and
 // fluxes go to shared memory once; each thread reverses one interface (its flux
 // adjoint from both neighbouring cells' k_bar, so no interface is reversed twice as
-// at the walker's segment boundaries) and adds its stencil adjoints into per-cell
-// shared accumulators; then each cell is finished (u_bar += a + (df/du)^T f_bar) and
-// added atomically at its folded index, as in the walker.
+// at the walker's segment boundaries) and stores its six cells' stencil adjoints in
+// shared memory; after a barrier each cell sums the contributions of the interfaces
+// that touch it, in a fixed order (no shared-memory atomics, and the same sum on
+// every run), is finished (u_bar += a + (df/du)^T f_bar) and added atomically at its
+// folded index, as in the walker.
+// Shared memory of the tile reverse (both directions use the same block of it): the
+// tile's cell states and fluxes, and per interface t the adjoints of its window cells
+// t .. t+5, of the flux (gf) and of the state (gu).
+template <int TI>
+struct VjpTileSmem {
+  double su[TI + 5][NV2], sf[TI + 5][NV2];
+  double sgf[TI][6][NV2], sgu[TI][6][NV2];
+};
+
 template <int D, bool WT, int TI>
 __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const AdjTerms& kt, double* Ub,
                                          const double* __restrict__ dxinv, const DevGeom& G, const PhysParams& pp,
-                                         long long tr, int tile, const double* __restrict__ tape) {
+                                         long long tr, int tile, const double* __restrict__ tape,
+                                         VjpTileSmem<TI>& sm) {
   constexpr int T = 1 - D, NCELL = TI + 5;
-  __shared__ double su[NCELL][NV2], sf[NCELL][NV2], sa[NCELL][NV2], sfb[NCELL][NV2];
+  auto& su = sm.su;
+  auto& sf = sm.sf;
+  auto& sgf = sm.sgf;
+  auto& sgu = sm.sgu;
   const long long pbase = (long long)(tr + G.g) * G.stride[T] + (long long)G.g * G.stride[D];
   const int N = G.dim[D];
   const long long sd = G.stride[D];
@@ -522,8 +537,6 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
     for (int v = 0; v < NV2; v++) {
       su[c][v] = uu[v];
       sf[c][v] = ff[v];
-      sa[c][v] = 0.0;
-      sfb[c][v] = 0.0;
     }
   }
   __syncthreads();
@@ -581,22 +594,28 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
       }
 #pragma unroll
       for (int p = 0; p < 6; p++) {
-        atomicAdd(&sfb[t + p][v], gf[p]);
-        atomicAdd(&sa[t + p][v], gu[p]);
+        sgf[t][p][v] = gf[p];
+        sgu[t][p][v] = gu[p];
       }
     }
   }
   __syncthreads();
+  // interfaces of this tile that exist (I <= N); cell c is window cell c - t of interface t
+  const int nI = min(TI, N + 1 - I0);
   for (int c = threadIdx.x; c < NCELL; c += TI) {
     const int i = I0 - 3 + c;
     if (i > N + 2) continue;
-    double ab[NV2], fb[NV2], uu[NV2];
+    double ab[NV2] = {0.0, 0.0, 0.0, 0.0}, fb[NV2] = {0.0, 0.0, 0.0, 0.0}, uu[NV2];
+    const int t0 = max(0, c - 5), t1 = min(c, nI - 1);
+    for (int tt = t0; tt <= t1; tt++) {
 #pragma unroll
-    for (int v = 0; v < NV2; v++) {
-      ab[v] = sa[c][v];
-      fb[v] = sfb[c][v];
-      uu[v] = su[c][v];
+      for (int v = 0; v < NV2; v++) {
+        fb[v] += sgf[tt][c - tt][v];
+        ab[v] += sgu[tt][c - tt][v];
+      }
     }
+#pragma unroll
+    for (int v = 0; v < NV2; v++) uu[v] = su[c][v];
     flux_vjp<D>(uu, fb, ab, pp);
     double* dst = Ub + (pbase + (long long)fold2(i, N, lo, hi) * sd) * NV2;
 #pragma unroll
@@ -609,13 +628,14 @@ __global__ void __launch_bounds__(TI)
 rhs_vjp_tile_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
                     const double* __restrict__ dx1, DevGeom G, PhysParams pp, int nt0, int nt1,
                     const double* __restrict__ tape0, const double* __restrict__ tape1) {
+  __shared__ VjpTileSmem<TI> sm;
   const long long b = blockIdx.x;
   const long long n0 = (long long)G.dim[1] * nt0;
   if (b < n0) {
-    vjp_tile<0, WT, TI>(U, kt, Ub, dx0, G, pp, b % G.dim[1], (int)(b / G.dim[1]), tape0);
+    vjp_tile<0, WT, TI>(U, kt, Ub, dx0, G, pp, b % G.dim[1], (int)(b / G.dim[1]), tape0, sm);
   } else {
     const long long t = b - n0;
-    vjp_tile<1, WT, TI>(U, kt, Ub, dx1, G, pp, t % G.dim[0], (int)(t / G.dim[0]), tape1);
+    vjp_tile<1, WT, TI>(U, kt, Ub, dx1, G, pp, t % G.dim[0], (int)(t / G.dim[0]), tape1, sm);
   }
 }
 
