@@ -60,10 +60,10 @@ FP64_PER_CELL_STEP = {
     "dns64cr": {"flops": 35997.0, "instr": 24360.8, "captured": "64^3 (the full grid), segments 5/5/4"},
 }
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
-# update), per kernel form: the segment walker from the same 2048^2 capture (traffic
-# proportional to cells at these sizes), the tile form from a capture of the default
-# 1024^2 run.
-DRAM_BYTES_PER_CELL = {"vortex": {("hyp_x", "walker"): 56.13, ("hyp_y", "walker"): 149.99,
+# update), per kernel form: the segment walker from a 2048^2 capture of the
+# centre-relative kernels (traffic proportional to cells at these sizes), the tile form
+# from a capture of the default 1024^2 run.
+DRAM_BYTES_PER_CELL = {"vortex": {("hyp_x", "walker"): 57.32, ("hyp_y", "walker"): 153.39,
                                   ("hyp_y", "tile"): 112.57}}
 TRAFFIC_SOURCE = {"walker": "a 2048^2 capture of the segment-walker form, scaled by cells",
                   "tile": "a 1024^2 capture of the tile form"}
