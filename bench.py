@@ -51,13 +51,15 @@ UNIT = "cell-component updates/s"
 # with the launch shapes the autotuner picks at full size, whose per-cell work is
 # that of the full grid to within the segment-boundary share).
 FP64_PER_CELL_STEP = {
-    "vortex": {"flops": 8745.8, "instr": 5698.9, "captured": "512^2, segments 54/27 (the 1024^2 shape)"},
-    "sod": {"flops": 3641.9, "instr": 2446.6, "captured": "1024 (the full grid), lane groups of 16"},
-    "tgv": {"flops": 18346.9, "instr": 12262.5, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"},
-    "rtb": {"flops": 17058.9, "instr": 11874.7, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"},
-    "rtb64": {"flops": 26004.5, "instr": 18095.7, "captured": "64^3 (the full grid), segments 7/7/7"},
-    "dns": {"flops": 21856.8, "instr": 15093.0, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"},
-    "dns64cr": {"flops": 35997.0, "instr": 24360.8, "captured": "64^3 (the full grid), segments 5/5/4"},
+    "vortex": {"tile": {"flops": 8454.6, "instr": 5494.4, "captured": "512^2, tiles of 128 interfaces"},
+               "walker": {"flops": 8745.8, "instr": 5698.9, "captured": "512^2, segments 54/27"}},
+    "sod": {"lanes": {"flops": 3654.7, "instr": 2455.2, "captured": "1024 (the full grid), lane groups of 16"}},
+    "tgv": {"walker": {"flops": 18445.5, "instr": 12291.2,
+                       "captured": "128^3, segments 48/32/32 (the 256^3 shape)"}},
+    "rtb": {"walker": {"flops": 16583.3, "instr": 11627.6, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"}},
+    "rtb64": {"walker": {"flops": 25265.3, "instr": 17712.2, "captured": "64^3 (the full grid), segments 7/7/7"}},
+    "dns": {"walker": {"flops": 20731.2, "instr": 14902.2, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"}},
+    "dns64cr": {"walker": {"flops": 34233.9, "instr": 23443.6, "captured": "64^3 (the full grid), segments 5/8/5"}},
 }
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
 # update), per kernel form: the segment walker from a 2048^2 capture of the
@@ -343,7 +345,15 @@ def run_ours(args, case, desc, ws, rank, local):
                 "algorithmic_bytes_per_launch": bytes_per_launch}
     step_bytes = cells * sum(stage_bytes(cfg, st) + (8.0 * nv * 2) * (cfg.ndims - 1)
                              for st in range(cfg.rk_nstages))
-    fw = FP64_PER_CELL_STEP.get(args.workload) if not args.size else None
+    forms = ["lanes" if sg in (-8, -16) else ("tile" if sg < 0 else "walker") for sg, _ in tuned]
+    known = FP64_PER_CELL_STEP.get(args.workload, {}) if not args.size else {}
+    fw = None
+    if known and all(f in known for f in forms):
+        # per direction the form's share of the step (directions of one form each do half
+        # of a 2-D step's work, a third of a 3-D step's)
+        fw = {"flops": sum(known[f]["flops"] for f in forms) / len(forms),
+              "instr": sum(known[f]["instr"] for f in forms) / len(forms),
+              "captured": "; ".join(sorted({known[f]["captured"] for f in forms}))}
     roofline_fp64 = {"bound": "fp64", "peak": fp64_peak, "unit": "TFLOP/s",
                      "peak_source": "measured DFMA loop (gb_probe_fp64_peak) on this GPU"}
     if fw:
