@@ -41,7 +41,7 @@ EXPORTS = [
     "gb_solver_step_report", "gb_solver_error", "gb_op_to_initial", "gb_inputs_gravity_field",
     "gb_solver_set_gravity_field", "gb_solver_conservation_begin", "gb_solver_conservation_error",
     "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error", "gb_ensemble_error",
-    "gb_solver_set_hooks",
+    "gb_solver_set_hooks", "gb_inputs_zone_temperature", "gb_solver_set_zone_temperature",
 ]
 
 
@@ -159,6 +159,9 @@ def lib():
     L.gb_rhs_explicit_noalloc.argtypes = [ctypes.POINTER(GbConfig), VP, VP, VP, VP]
     L.gb_solver_set_time.argtypes = [VP, ctypes.c_double]
     L.gb_solver_set_gravity_field.argtypes = [VP, VP]
+    L.gb_inputs_zone_temperature.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(DP),
+                                             ctypes.POINTER(DP)]
+    L.gb_solver_set_zone_temperature.argtypes = [VP, ctypes.c_int, ctypes.c_int, DP, DP]
     L.gb_solver_cfl.argtypes = [VP, DP]
     L.gb_solver_step_report.argtypes = [VP, ctypes.c_int, DP, DP]
     L.gb_solver_error.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, DP]

@@ -53,7 +53,10 @@ class Case:
     restart_iter: int = 0           # solver.inp restart_iter
     screen_op_iter: Optional[int] = None
     # per-face boundary types: {(dim, face): (bctype, [values after the extents])};
-    # faces not listed take `bc`
+    # faces not listed take `bc`.  Thermal walls add a third item, the wall
+    # temperature (times, field): field has the face's size per transverse dimension
+    # and len(times) along the wall's own dimension, dimension 0 fastest (the
+    # reference's temperature file layout, written beside the deck by `write`)
     bcs: Optional[dict] = None
     # gravity: NavierStokes3D (physics.inp gravity gx gy gz / rho_ref / p_ref / R / HB /
     # N_bv) or Euler1D (gravity g, gravity_type grav_type)
@@ -141,9 +144,29 @@ class Case:
                 ext = []
                 for e in range(nd):
                     ext += ["0", "0"] if e == d else [repr(lo[e]), repr(hi[e])]
-                bctype, vals = (self.bcs or {}).get((d, face), (self.bc, []))
-                rows.append(f"{bctype} {d} {face} " + " ".join(ext + [repr(float(v)) for v in vals]))
+                spec = (self.bcs or {}).get((d, face), (self.bc, []))
+                bctype, vals = spec[0], spec[1]
+                items = ext + [repr(float(v)) for v in vals]
+                if bctype.startswith("thermal-"):
+                    items.append(self.temperature_file(d, face))
+                rows.append(f"{bctype} {d} {face} " + " ".join(items))
         return f"{len(rows)}\n" + "\n".join(rows) + "\n"
+
+    @staticmethod
+    def temperature_file(d: int, face: int) -> str:
+        return f"temperature_{d}_{'lo' if face == 1 else 'hi'}.bin"
+
+    def temperature_bytes(self, d: int, face: int) -> bytes:
+        """The wall temperature of a thermal-wall face in the reference's binary format
+        (BCReadTemperatureData, src/BoundaryConditions/BCIO.c:147-260, one rank): int
+        rank[ndims], int size[ndims], double times[size[d]], double field[prod(size)]."""
+        times, field = self.bcs[(d, face)][2]
+        times = np.asarray(times, np.float64)
+        size = [len(times) if e == d else self.size[e] for e in range(self.ndims)]
+        field = np.asarray(field, np.float64).reshape(-1)
+        assert field.size == int(np.prod(size)), (field.size, size)
+        rank = np.zeros(self.ndims, np.int32)
+        return rank.tobytes() + np.asarray(size, np.int32).tobytes() + times.tobytes() + field.tobytes()
 
     def initial_bytes(self) -> bytes:
         xs = np.concatenate([np.asarray(xx, dtype=np.float64) for xx in self.x])
@@ -162,6 +185,10 @@ class Case:
                 f.write(text)
         with open(os.path.join(directory, "initial.inp"), "wb") as f:
             f.write(self.initial_bytes())
+        for (d, face), spec in (self.bcs or {}).items():
+            if spec[0].startswith("thermal-"):
+                with open(os.path.join(directory, self.temperature_file(d, face)), "wb") as f:
+                    f.write(self.temperature_bytes(d, face))
         return directory
 
 

@@ -47,6 +47,8 @@ cudaError_t launch_interp_ns3d(int, int, int, int, double*, const double*, const
 cudaError_t launch_visc(const double*, double*, double*, double*, const double*, const DevGeom&,
                         const ViscParams&, int, cudaStream_t);
 cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, const double*, double, cudaStream_t);
+cudaError_t launch_bc_zone_t(double*, const DevGeom&, int, const int*, const double*, double, const double*, int, int,
+                             cudaStream_t);
 cudaError_t launch_finite_check(const double*, const DevGeom&, int, int*, cudaStream_t);
 cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
 }  // namespace gbh
@@ -152,7 +154,8 @@ static cudaError_t launch_unfused(gb_solver* s, int kind, int dir, double* out, 
   return launch_unfused_ns3d(kind, dir, c.upwind, out, a, b, c2, d, u, s->G, s->pp, s->stream);
 }
 
-static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
+// The boundary zones kept in memory (all zones: `all`) applied to u at time t.
+static int apply_mem_bcs(gb_solver* s, double* u, bool all, double t) {
   int pr = -1;
   for (int z = 0; z < s->cfg.nzones; z++) {
     bool use = all;
@@ -160,11 +163,49 @@ static int apply_mem_bcs(gb_solver* s, double* u, bool all) {
       for (int k : s->mem_zones)
         if (k == z) use = true;
     if (use) {
+      const int type = s->cfg.zones[z][0];
+      const double* tf = nullptr;
+      int tn = 0, it = 0;
+      if (type == GB_BC_THERMAL_SLIP_WALL || type == GB_BC_THERMAL_NOSLIP_WALL) {
+        if (!s->d_tfield[z]) {
+          gbh_set_error("boundary zone %d is a thermal wall: call gb_solver_set_zone_temperature first", z);
+          return GB_ERR_ARG;
+        }
+        // the last time level at or before t (BCThermalNoslipWall.c:55-57)
+        tn = (int)s->ttimes[z].size();
+        it = tn - 1;
+        while (it > 0 && s->ttimes[z][it] > t) it--;
+        tf = s->d_tfield[z];
+      }
       if (pr < 0) pr = prof_begin(s, GB_PROF_BC);
-      CK(launch_bc_zone(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->cfg.zone_data[z], s->cfg.gamma, s->stream));
+      CK(launch_bc_zone_t(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->cfg.zone_data[z], s->cfg.gamma, tf, tn, it,
+                          s->stream));
     }
   }
   prof_end(s, pr);
+  return GB_OK;
+}
+
+extern "C" int gb_solver_set_zone_temperature(gb_solver* s, int zone, int ntimes, const double* times,
+                                              const double* field) {
+  if (!s || zone < 0 || zone >= s->cfg.nzones || ntimes < 1 || !times || !field) {
+    gbh_set_error("gb_solver_set_zone_temperature: bad argument");
+    return GB_ERR_ARG;
+  }
+  const int* q = s->cfg.zones[zone];
+  if (q[0] != GB_BC_THERMAL_SLIP_WALL && q[0] != GB_BC_THERMAL_NOSLIP_WALL) {
+    gbh_set_error("gb_solver_set_zone_temperature: zone %d is not a thermal wall", zone);
+    return GB_ERR_ARG;
+  }
+  size_t n = (size_t)ntimes;
+  for (int d = 0; d < s->cfg.ndims; d++)
+    if (d != q[1]) n *= (size_t)(q[6 + d] - q[3 + d] > 0 ? q[6 + d] - q[3 + d] : 0);
+  if (n == 0) return GB_OK;  // an empty zone
+  cudaFree(s->d_tfield[zone]);
+  s->d_tfield[zone] = nullptr;
+  CK(cudaMalloc((void**)&s->d_tfield[zone], n * sizeof(double)));
+  CK(cudaMemcpy(s->d_tfield[zone], field, n * sizeof(double), cudaMemcpyHostToDevice));
+  s->ttimes[zone].assign(times, times + ntimes);
   return GB_OK;
 }
 
@@ -178,9 +219,9 @@ static int gravity_ready(gb_solver* s) {
   return GB_OK;
 }
 
-static int rhs_launches(gb_solver* s, double* U, StageEpi ep) {
+static int rhs_launches(gb_solver* s, double* U, StageEpi ep, double t) {
   if (int rc = gravity_ready(s)) return rc;
-  int rc = apply_mem_bcs(s, U, false);
+  int rc = apply_mem_bcs(s, U, false, t);
   if (rc) return rc;
   ep.par = nullptr;
   if (s->viscous) {
@@ -244,13 +285,17 @@ int gbh_validate(const gb_config* c) {
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
-    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SUBSONIC_AMBIVALENT || q[1] < 0 || q[1] >= nd ||
+    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_THERMAL_NOSLIP_WALL || q[1] < 0 || q[1] >= nd ||
         (q[2] != 1 && q[2] != -1)) {
       gbh_set_error("bad zone %d", z);
       return GB_ERR_ARG;
     }
     if (q[0] > GB_BC_DIRICHLET && nd < 2) {
       gbh_set_error("zone %d: wall / inflow / outflow boundaries need Euler2D or NavierStokes3D", z);
+      return GB_ERR_UNSUPPORTED;
+    }
+    if ((q[0] == GB_BC_THERMAL_SLIP_WALL || q[0] == GB_BC_THERMAL_NOSLIP_WALL) && c->model != GB_MODEL_NS3D) {
+      gbh_set_error("zone %d: thermal walls need NavierStokes3D", z);
       return GB_ERR_UNSUPPORTED;
     }
     for (int d = 0; d < nd; d++) {
@@ -394,6 +439,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_acc);
   for (int k = 0; k < 4; k++) cudaFree(s->d_P[k]);
   cudaFree(s->d_U0);
+  for (int z = 0; z < GB_MAX_ZONES; z++) cudaFree(s->d_tfield[z]);
   cudaFree(s->d_H);
   cudaFree(s->d_crX);
   cudaFree(s->d_crC);
@@ -610,7 +656,7 @@ int gbh_rk_step(gb_solver* s) {
     ep.u = s->d_u;
     ep.acc = s->d_acc;
     ep.uout = (ns == 1) ? s->d_acc : s->d_u;
-    int rc = rhs_launches(s, U, ep);
+    int rc = rhs_launches(s, U, ep, s->t + c.rk_c[st] * dt);
     if (rc) return rc;
     for (int t = st + 1; t < ns; t++)
       if (ep.ca[t] != 0.0) touched[t] = 1;
@@ -969,18 +1015,16 @@ extern "C" int gb_InterpolateInterfacesHyp(double* fI, double* fC, double* u, do
 extern "C" int gb_ApplyBoundaryConditions(void* sv, void* m, double* u, double* uref, double t) {
   (void)m;
   (void)uref;
-  (void)t;
   gb_solver* s = S(sv);
   if (!s || !u) { gbh_set_error("gb_ApplyBoundaryConditions: null argument"); return GB_ERR_ARG; }
-  return apply_mem_bcs(s, u, true);
+  return apply_mem_bcs(s, u, true, t);
 }
 
 extern "C" int gb_RHSFunctionExplicit(double* rhs, double* u, void* sv, void* m, double t) {
   (void)m;
-  (void)t;
   gb_solver* s = S(sv);
   if (!s || !rhs || !u) { gbh_set_error("gb_RHSFunctionExplicit: null argument"); return GB_ERR_ARG; }
-  int rc = apply_mem_bcs(s, u, true);  // TimeRHSFunctionExplicit.c:46 fills u's ghosts in place
+  int rc = apply_mem_bcs(s, u, true, t);  // TimeRHSFunctionExplicit.c:46 fills u's ghosts in place
   if (rc) return rc;
   CK(cudaMemsetAsync(rhs, 0, s->nvals * sizeof(double), s->stream));
   StageEpi ep;
@@ -989,7 +1033,7 @@ extern "C" int gb_RHSFunctionExplicit(double* rhs, double* u, void* sv, void* m,
   ep.rhs = rhs;
   std::vector<int> keep;
   keep.swap(s->mem_zones);  // already applied above
-  rc = rhs_launches(s, u, ep);
+  rc = rhs_launches(s, u, ep, t);
   keep.swap(s->mem_zones);
   return rc;
 }

@@ -32,6 +32,9 @@ struct gb_inputs {
   double *u0;     /* interior solution */
   double *uex;    /* exact solution (exact.inp), or NULL */
   double *grav;   /* gravity fields f then g at every point with ghosts, or NULL */
+  /* thermal walls: per zone the wall temperature's time levels and field, or NULL */
+  int tn[GB_MAX_ZONES];
+  double *ttimes[GB_MAX_ZONES], *tfield[GB_MAX_ZONES];
   char op_overwrite[64];
   char op_format[64];
 };
@@ -427,7 +430,62 @@ void gb_inputs_free(gb_inputs *in) {
   free(in->u0);
   free(in->uex);
   free(in->grav);
+  for (int z = 0; z < GB_MAX_ZONES; z++) {
+    free(in->ttimes[z]);
+    free(in->tfield[z]);
+  }
   free(in);
+}
+
+int gb_inputs_zone_temperature(const gb_inputs *in, int zone, int *ntimes, const double **times,
+                               const double **field) {
+  if (!in || !ntimes || !times || !field || zone < 0 || zone >= GB_MAX_ZONES) {
+    gbh_set_error("gb_inputs_zone_temperature: bad argument");
+    return GB_ERR_ARG;
+  }
+  *ntimes = in->tn[zone];
+  *times = in->ttimes[zone];
+  *field = in->tfield[zone];
+  return GB_OK;
+}
+
+/* The wall temperature file of a thermal-wall zone (BCReadTemperatureData,
+ * src/BoundaryConditions/BCIO.c:147-260, one rank): int rank[ndims], int size[ndims]
+ * (size[dim]: the number of time levels; the other sizes: the zone's extent), double
+ * times[size[dim]], double field[prod size], dimension 0 fastest. */
+static int read_temperature(const char *dir, const char *name, const gb_config *c, const int *zone,
+                            gb_inputs *res, int z) {
+  FILE *f = open_in(dir, name, "rb");
+  if (!f) {
+    gbh_set_error("boundary.inp zone %d: cannot open the temperature file %s", z, name);
+    return GB_ERR_INPUT;
+  }
+  const int nd = c->ndims, dim = zone[1];
+  int rank[3] = {0, 0, 0}, size[3] = {1, 1, 1};
+  int bad = fread(rank, sizeof(int), nd, f) != (size_t)nd || fread(size, sizeof(int), nd, f) != (size_t)nd;
+  long total = 1;
+  for (int d = 0; d < nd && !bad; d++) {
+    if (size[d] < 1) bad = 1;
+    else if (d != dim && size[d] != zone[6 + d] - zone[3 + d]) bad = 2;
+    total *= size[d];
+  }
+  if (bad) {
+    fclose(f);
+    gbh_set_error("temperature file %s: %s", name,
+                  bad == 2 ? "its size does not match the zone's extent" : "malformed header");
+    return GB_ERR_INPUT;
+  }
+  res->tn[z] = size[dim];
+  res->ttimes[z] = (double *)malloc(sizeof(double) * size[dim]);
+  res->tfield[z] = (double *)malloc(sizeof(double) * total);
+  if (fread(res->ttimes[z], sizeof(double), size[dim], f) != (size_t)size[dim] ||
+      fread(res->tfield[z], sizeof(double), total, f) != (size_t)total) {
+    fclose(f);
+    gbh_set_error("temperature file %s: truncated", name);
+    return GB_ERR_INPUT;
+  }
+  fclose(f);
+  return GB_OK;
 }
 
 const gb_config *gb_inputs_config(const gb_inputs *in) { return in ? &in->cfg : NULL; }
@@ -759,7 +817,9 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
           {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW, 1},
           {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW, -4},
           {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW, 0},
-          {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT, -4}};
+          {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT, -4},
+          {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL, -2},
+          {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL, -2}};
       int tcode = 0, nvals = 0;
       for (size_t t = 0; t < sizeof(bct) / sizeof(bct[0]); t++)
         if (!strcmp(type, bct[t].name)) {
@@ -776,6 +836,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
       }
       for (int k = 0; k < 8; k++) c.zone_data[z][k] = 0.0;
       for (int k = 0; k < nvals && !bad; k++) bad = fscanf(in, "%lf", &c.zone_data[z][k]) != 1;
+      /* thermal walls: then the name of the wall temperature file (InitializeBoundaries.c:180-187) */
+      const int thermal = tcode == GB_BC_THERMAL_SLIP_WALL || tcode == GB_BC_THERMAL_NOSLIP_WALL;
+      char tname[MAXS] = "";
+      if (!bad && thermal) bad = fscanf(in, "%511s", tname) != 1;
       if (bad) {
         fclose(in);
         gb_inputs_free(res);
@@ -786,6 +850,12 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         fclose(in);
         gb_inputs_free(res);
         gbh_set_error("boundary type %s needs Euler2D or NavierStokes3D", type);
+        return GB_ERR_UNSUPPORTED;
+      }
+      if (thermal && c.model != GB_MODEL_NS3D) {
+        fclose(in);
+        gb_inputs_free(res);
+        gbh_set_error("boundary type %s needs NavierStokes3D (BCThermal*WallU have 3-D branches only)", type);
         return GB_ERR_UNSUPPORTED;
       }
       int *zz = c.zones[z];
@@ -806,6 +876,14 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         }
         zz[3 + d] = is;
         zz[6 + d] = ie;
+      }
+      if (thermal) {
+        int rc = read_temperature(dir, tname, &c, zz, res, z);
+        if (rc) {
+          fclose(in);
+          gb_inputs_free(res);
+          return rc;
+        }
       }
     }
     fclose(in);

@@ -223,6 +223,13 @@ int gb_run_case(const char *dir, int device, int verbose) {
   double *buf = (double *)malloc(sizeof(double) * n);
   rc = gb_solver_set_state(s, gb_inputs_u0(in), GB_LAYOUT_INTERIOR, GB_MEM_HOST);
   if (!rc && gb_inputs_gravity_field(in)) rc = gb_solver_set_gravity_field(s, gb_inputs_gravity_field(in));
+  /* thermal walls: the wall temperature read with the deck */
+  for (int z = 0; !rc && z < gb_inputs_config(in)->nzones; z++) {
+    int nt = 0;
+    const double *tt = NULL, *tf = NULL;
+    rc = gb_inputs_zone_temperature(in, z, &nt, &tt, &tf);
+    if (!rc && nt) rc = gb_solver_set_zone_temperature(s, z, nt, tt, tf);
+  }
   /* InitialSolution.c:118: the volume integral of the initial solution */
   if (!rc && c->cons_check) rc = gb_solver_conservation_begin(s);
   const int overwrite = !strcmp(gbh_inputs_op_overwrite(in), "yes");

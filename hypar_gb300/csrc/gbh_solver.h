@@ -51,6 +51,9 @@ struct gb_solver {
   void* hook_solver = nullptr;
   void* hook_mpi = nullptr;
   double* d_U0 = nullptr;  // stage state handed to PostStage where the stage reads u itself
+  // thermal walls: per zone the wall temperature's time levels (host) and field (device)
+  std::vector<double> ttimes[GB_MAX_ZONES];
+  double* d_tfield[GB_MAX_ZONES] = {};
   int iter = 0;            // steps taken since the state was set (PostStep's iteration index)
   long long dx_off[3] = {0, 0, 0};
   bool viscous = false;

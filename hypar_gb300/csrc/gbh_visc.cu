@@ -212,6 +212,9 @@ struct ZoneDev {
   int type, dim, face, is[3], ie[3];
   double data[8];
   double gamma;
+  // thermal walls: the wall temperature field (all time levels) and the level in use
+  const double* tfield;
+  int tn, it;
 };
 
 // Ghost state from the mirror interior state w, for the wall and inflow /
@@ -219,7 +222,8 @@ struct ZoneDev {
 // BCSubsonicOutflow.c, BCSupersonicInflow.c, BCSupersonicOutflow.c; 2-D and 3-D
 // branches), in their operation order without contraction.
 template <int ND>
-__device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out, bool inflow = false) {
+__device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out, bool inflow = false,
+                                         double Tb = 0.0) {
   constexpr int NV = ND + 2;
   const double gm1 = z.gamma - 1.0;
   const double inv_gm1 = __ddiv_rn(1.0, gm1);
@@ -246,6 +250,17 @@ __device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, doub
       rg = z.data[0];
       for (int d = 0; d < ND; d++) vg[d] = z.data[1 + d];
       Pg = z.data[1 + ND];
+      break;
+    case GB_BC_THERMAL_SLIP_WALL:
+      // BCThermalSlipWall.c:86-105: the normal velocity mirrored about the wall's, the
+      // pressure from the extrapolated density and the wall temperature
+      vg[z.dim] = __dsub_rn(__dmul_rn(2.0, z.data[z.dim]), vel[z.dim]);
+      Pg = __dmul_rn(rg, Tb);
+      break;
+    case GB_BC_THERMAL_NOSLIP_WALL:
+      // BCThermalNoslipWall.c:86-105: every velocity component mirrored
+      for (int d = 0; d < ND; d++) vg[d] = __dsub_rn(__dmul_rn(2.0, z.data[d]), vel[d]);
+      Pg = __dmul_rn(rg, Tb);
       break;
     case GB_BC_SUBSONIC_AMBIVALENT:
       // BCSubsonicAmbivalent.c:105-117: inflow's rule (density, velocity given) or
@@ -312,16 +327,42 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
       const double vb = __dsub_rn(__dmul_rn(1.5, v1), __dmul_rn(0.5, v2));
       inflow = (z.face == 1) ? vb > 0.0 : vb < 0.0;
     }
+    double Tb = 0.0;
+    if (z.type == GB_BC_THERMAL_SLIP_WALL || z.type == GB_BC_THERMAL_NOSLIP_WALL) {
+      // the temperature at this point: zone-relative index, the time level along dim
+      // (BCThermalNoslipWall.c:80-84)
+      long long q = 0, stride = 1;
+      for (int d = 0; d < G.nd; d++) {
+        q += stride * (d == dd ? z.it : ib[d]);
+        stride *= (d == dd ? z.tn : b[d]);
+      }
+      Tb = z.tfield[q];
+    }
     double g[5];
-    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow);
-    else bc_ghost<3>(z, u + p2 * nv, g, inflow);
+    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow, Tb);
+    else bc_ghost<3>(z, u + p2 * nv, g, inflow, Tb);
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = g[v];
   }
 }
 
+cudaError_t launch_bc_zone_t(double* u, const DevGeom& G, int nv, const int* zone9, const double* data8,
+                             double gamma, const double* tfield, int tn, int it, cudaStream_t s);
+
 cudaError_t launch_bc_zone(double* u, const DevGeom& G, int nv, const int* zone9, const double* data8, double gamma,
                            cudaStream_t s) {
+  return launch_bc_zone_t(u, G, nv, zone9, data8, gamma, nullptr, 0, 0, s);
+}
+
+// As launch_bc_zone, with a thermal wall's temperature field (tn time levels, device
+// array) and the level `it` in use.
+cudaError_t launch_bc_zone_t(double* u, const DevGeom& G, int nv, const int* zone9, const double* data8,
+                             double gamma, const double* tfield, int tn, int it, cudaStream_t s) {
   ZoneDev z;
+  z.tfield = tfield;
+  z.tn = tn;
+  z.it = it;
+  if ((zone9[0] == GB_BC_THERMAL_SLIP_WALL || zone9[0] == GB_BC_THERMAL_NOSLIP_WALL) && (!tfield || tn < 1))
+    return cudaErrorInvalidValue;  // a thermal wall without its temperature field
   z.type = zone9[0];
   z.dim = zone9[1];
   z.face = zone9[2];

@@ -151,7 +151,8 @@ int gbshim_config(void *s, gb_config *c) {
         {"dirichlet", GB_BC_DIRICHLET},        {"slip-wall", GB_BC_SLIP_WALL},
         {"noslip-wall", GB_BC_NOSLIP_WALL},    {"subsonic-inflow", GB_BC_SUBSONIC_INFLOW},
         {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW}, {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW},
-        {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}, {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT}};
+        {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}, {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT},
+        {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL}, {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL}};
     int code = 0;
     for (size_t t = 0; t < sizeof(types) / sizeof(types[0]); t++)
       if (!strcmp(B->bctype, types[t].name)) code = types[t].code;
@@ -172,6 +173,8 @@ int gbshim_config(void *s, gb_config *c) {
         break;
       case GB_BC_SLIP_WALL:
       case GB_BC_NOSLIP_WALL:
+      case GB_BC_THERMAL_SLIP_WALL:
+      case GB_BC_THERMAL_NOSLIP_WALL:
         for (int k = 0; k < nd; k++) v[k] = B->FlowVelocity[k];
         break;
       case GB_BC_SUBSONIC_INFLOW:
@@ -289,6 +292,19 @@ int gbshim_attach(void *s, void *mpi) {
   if (fg) {
     rc = gb_solver_set_gravity_field(gb, fg);
     free(fg);
+    if (rc) {
+      fprintf(stderr, "gbhypar: %s\n", gb_last_error());
+      gb_solver_destroy(gb);
+      return rc;
+    }
+  }
+  /* thermal walls: the wall temperature HyPar read (BCReadTemperatureData), time levels
+   * and field over the zone's extent */
+  for (int z = 0; z < c.nzones; z++) {
+    const DomainBoundary *B = &((const DomainBoundary *)solver->boundary)[z];
+    if (c.zones[z][0] != GB_BC_THERMAL_SLIP_WALL && c.zones[z][0] != GB_BC_THERMAL_NOSLIP_WALL) continue;
+    rc = gb_solver_set_zone_temperature(gb, z, B->UnsteadyTemperatureSize[B->dim], B->UnsteadyTimeLevels,
+                                        B->UnsteadyTemperatureData);
     if (rc) {
       fprintf(stderr, "gbhypar: %s\n", gb_last_error());
       gb_solver_destroy(gb);

@@ -49,6 +49,19 @@ class Inputs:
         gp = lib().gb_inputs_gravity_field(h)
         # hydrostatic density and pressure fields f, g with ghost points (NavierStokes3D gravity)
         self.gravity_field = np.ctypeslib.as_array(gp, shape=(2 * npts_wg,)).copy() if gp else None
+        # thermal walls: per zone (times, field) of the wall temperature
+        self.zone_temperature = {}
+        for z in range(c.nzones):
+            n, tp, fp = ctypes.c_int(), _lib.DP(), _lib.DP()
+            check(lib().gb_inputs_zone_temperature(h, z, ctypes.byref(n), ctypes.byref(tp), ctypes.byref(fp)))
+            if n.value:
+                q = c.zones[z]
+                size = n.value
+                for d in range(nd):
+                    if d != q[1]:
+                        size *= q[6 + d] - q[3 + d]
+                self.zone_temperature[z] = (np.ctypeslib.as_array(tp, shape=(n.value,)).copy(),
+                                            np.ctypeslib.as_array(fp, shape=(size,)).copy())
         lib().gb_inputs_free(h)
         self._h = None
 
@@ -79,7 +92,17 @@ class Solver:
         s.set_state(inp.u0)
         if inp.gravity_field is not None:
             s.set_gravity_field(inp.gravity_field)
+        for z, (times, field) in inp.zone_temperature.items():
+            s.set_zone_temperature(z, times, field)
         return s
+
+    def set_zone_temperature(self, zone: int, times, field):
+        """A thermal wall's temperature: time levels and the field over the zone's extent
+        (the level along the zone's own dimension, dimension 0 fastest)."""
+        times = np.ascontiguousarray(times, dtype=np.float64)
+        field = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
+        check(lib().gb_solver_set_zone_temperature(self._h, int(zone), len(times), times.ctypes.data_as(_lib.DP),
+                                                   field.ctypes.data_as(_lib.DP)))
 
     def set_gravity_field(self, fg: np.ndarray):
         """Upload the hydrostatic fields f then g (ghosted layout, x fastest) that the

@@ -44,10 +44,13 @@ enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
  * model; dirichlet for every model; the wall and inflow/outflow types, and the
  * subsonic "ambivalent" one (inflow or outflow point by point, by the sign of the
  * extrapolated face velocity), for Euler2D and NavierStokes3D (the reference's 1-D
- * branches of those are incomplete). */
+ * branches of those are incomplete); the thermal walls (slip / no-slip, the ghost
+ * pressure from the extrapolated density and a wall temperature given per time
+ * level in a file) for NavierStokes3D (BCThermalSlipWall.c, BCThermalNoslipWall.c). */
 enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2, GB_BC_DIRICHLET = 3, GB_BC_SLIP_WALL = 4,
        GB_BC_NOSLIP_WALL = 5, GB_BC_SUBSONIC_INFLOW = 6, GB_BC_SUBSONIC_OUTFLOW = 7,
-       GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9, GB_BC_SUBSONIC_AMBIVALENT = 10 };
+       GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9, GB_BC_SUBSONIC_AMBIVALENT = 10,
+       GB_BC_THERMAL_SLIP_WALL = 11, GB_BC_THERMAL_NOSLIP_WALL = 12 };
 enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
 /* WENO5 nonlinear weights (weno.inp: yc > borges > mapped > Jiang-Shu, and
  * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
@@ -85,7 +88,8 @@ typedef struct gb_config {
   /* per zone, the values boundary.inp gives after the extents: dirichlet: nvars values;
    * slip-wall / noslip-wall: wall velocity (ndims); subsonic-inflow: rho, velocity;
    * subsonic-outflow: pressure; supersonic-inflow and subsonic-ambivalent: rho, velocity,
-   * pressure */
+   * pressure; thermal-slip-wall / thermal-noslip-wall: wall velocity (the temperature
+   * comes through gb_inputs_zone_temperature / gb_solver_set_zone_temperature) */
   double zone_data[GB_MAX_ZONES][8];
   /* NavierStokes3D gravity (physics.inp gravity, rho_ref, p_ref, R, HB, N_bv); a nonzero
    * acceleration needs upwinding rusanov (NavierStokes3DInitialize.c:371) and the
@@ -131,6 +135,13 @@ const double *gb_inputs_exact(const gb_inputs *in);
  * (NavierStokes3DGravityField.c) at every point with ghosts, f then g (2 x the
  * points with ghosts), or NULL without gravity. */
 const double *gb_inputs_gravity_field(const gb_inputs *in);
+/* Thermal walls: the wall temperature the deck's file gives for boundary zone `zone`
+ * (BCReadTemperatureData, src/BoundaryConditions/BCIO.c:147): ntimes time levels
+ * (times), and the field over the zone's extent with the time level along the zone's
+ * own dimension, dimension 0 fastest; ntimes = 0 and NULL arrays for other zones.
+ * The arrays belong to `in`. */
+int gb_inputs_zone_temperature(const gb_inputs *in, int zone, int *ntimes, const double **times,
+                               const double **field);
 /* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
  * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
  * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
@@ -155,6 +166,12 @@ int gb_solver_set_stream(gb_solver *s, void *stream);
  * ghosts, as gb_inputs_gravity_field); required before stepping a configuration
  * with gravity. */
 int gb_solver_set_gravity_field(gb_solver *s, const double *fg);
+/* Thermal walls: upload the wall temperature of boundary zone `zone` (host arrays, as
+ * gb_inputs_zone_temperature gives them: ntimes time levels, the field over the zone's
+ * extent with the time level along the zone's own dimension, dimension 0 fastest).
+ * Each right-hand side at time t uses the last level at or before t
+ * (BCThermalNoslipWall.c:55-57); required before stepping such a configuration. */
+int gb_solver_set_zone_temperature(gb_solver *s, int zone, int ntimes, const double *times, const double *field);
 /* Wait for all work queued by the solver. */
 int gb_solver_sync(gb_solver *s);
 /* Copy a solution in or out (layout GB_LAYOUT_*, memory GB_MEM_*). */

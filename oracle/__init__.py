@@ -36,7 +36,7 @@ INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,
           "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9,
-          "subsonic-ambivalent": 10}
+          "subsonic-ambivalent": 10, "thermal-slip-wall": 11, "thermal-noslip-wall": 12}
 
 
 SCHEMES = {"weno5": 0, "crweno5": 1}
@@ -46,7 +46,8 @@ def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
     """How many values boundary.inp gives after a zone's extents (InitializeBoundaries.c:109-188)."""
     return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
             "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims,
-            "subsonic-ambivalent": 2 + ndims}.get(bctype, 0)
+            "subsonic-ambivalent": 2 + ndims, "thermal-slip-wall": ndims,
+            "thermal-noslip-wall": ndims}.get(bctype, 0)
 
 _lib = None
 
@@ -79,6 +80,10 @@ def _bind(path):
     L.orc_set_weights.restype = None
     L.orc_set_zone_data.argtypes = [ctypes.c_void_p, ctypes.c_int, dp]
     L.orc_set_zone_data.restype = None
+    L.orc_set_zone_temperature.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp, dp]
+    L.orc_set_zone_temperature.restype = ctypes.c_int
+    L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double]
+    L.orc_set_time.restype = None
     L.orc_set_gravity.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double]
@@ -207,6 +212,8 @@ def parse_boundary_inp(text: str, ndims: int, nvars: int = 0):
         nvals = bc_nvalues(bctype, ndims, nvars)
         vals = [float(t) for t in tok[k:k + nvals]]
         k += nvals
+        if bctype.startswith("thermal-"):
+            k += 1  # the temperature file's name
         rows.append((bctype, dim, face, ext, vals))
     return rows
 
@@ -271,6 +278,12 @@ class Problem:
             data = np.zeros(8)
             data[:len(vals)] = vals
             L.orc_set_zone_data(self.h, z, _dp(data))
+            if row[0].startswith("thermal-"):
+                times, field = case.bcs[(row[1], row[2])][2]
+                times = np.ascontiguousarray(times, np.float64)
+                field = np.ascontiguousarray(field, np.float64).reshape(-1)
+                if L.orc_set_zone_temperature(self.h, z, len(times), _dp(times), _dp(field)):
+                    raise RuntimeError("orc_set_zone_temperature failed")
         grav = getattr(case, "gravity", None)
         if grav is not None and any(float(v) != 0.0 for v in grav):
             xg = np.concatenate([grid_with_ghosts(x, ghosts) for x in xs])
@@ -306,9 +319,11 @@ class Problem:
     def u0(self) -> np.ndarray:
         return embed(self.case.u, self.size, self.nvars, self.g)
 
-    def rhs(self, u_wg: np.ndarray) -> np.ndarray:
+    def rhs(self, u_wg: np.ndarray, t: float = 0.0) -> np.ndarray:
+        """TimeRHSFunctionExplicit at time t (the time matters to time-dependent boundaries)."""
         u = np.ascontiguousarray(u_wg, np.float64).copy()
         out = np.zeros_like(u)
+        self._L.orc_set_time(self.h, float(t))
         if self._L.orc_rhs(self.h, _dp(u), _dp(out)):
             raise RuntimeError("orc_rhs failed (a zero pivot, or a configuration the oracle does not restate)")
         return out
@@ -332,17 +347,21 @@ class Problem:
         u = np.ascontiguousarray(u_wg, np.float64)
         return float(self._L.orc_cfl(self.h, _dp(u), float(self.case.dt if dt is None else dt)))
 
-    def apply_bc(self, u_wg: np.ndarray) -> np.ndarray:
+    def apply_bc(self, u_wg: np.ndarray, t: float = 0.0) -> np.ndarray:
         u = np.ascontiguousarray(u_wg, np.float64).copy()
+        self._L.orc_set_time(self.h, float(t))
         self._L.orc_apply_bc(self.h, _dp(u))
         return u
 
-    def rk(self, u_wg: np.ndarray, nsteps: int, dt: Optional[float] = None, scheme: Optional[str] = None):
+    def rk(self, u_wg: np.ndarray, nsteps: int, dt: Optional[float] = None, scheme: Optional[str] = None,
+           t0: float = 0.0):
+        """nsteps steps of TimeRK from time t0 (stage times t + c_s dt)."""
         scheme = scheme or self.case.time_scheme_type
         ns, A, b = RK_TABLES[scheme]
         A = np.asarray(A, np.float64)
         b = np.asarray(b, np.float64)
         u = np.ascontiguousarray(u_wg, np.float64).copy()
+        self._L.orc_set_time(self.h, float(t0))
         if self._L.orc_rk(self.h, ns, _dp(A), _dp(b), _dp(u), float(self.case.dt if dt is None else dt),
                           int(nsteps)):
             raise RuntimeError("orc_rk failed")

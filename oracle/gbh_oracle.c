@@ -210,8 +210,30 @@ void orc_set_zone_data(orc_problem *p, int z, const double *data) {
   for (int k = 0; k < 8; k++) p->zones[z].data[k] = data[k];
 }
 
+int orc_set_zone_temperature(orc_problem *p, int z, int n, const double *times, const double *field) {
+  if (z < 0 || z >= p->nzones || n < 1) return 1;
+  const orc_zone *b = &p->zones[z];
+  long size = n;
+  for (int d = 0; d < p->ndims; d++)
+    if (d != b->dim) size *= (b->ie[d] - b->is[d]);
+  free(p->ttimes[z]);
+  free(p->tfield[z]);
+  p->tn[z] = n;
+  p->ttimes[z] = (double *)malloc(sizeof(double) * n);
+  p->tfield[z] = (double *)malloc(sizeof(double) * size);
+  memcpy(p->ttimes[z], times, sizeof(double) * n);
+  memcpy(p->tfield[z], field, sizeof(double) * size);
+  return 0;
+}
+
+void orc_set_time(orc_problem *p, double t) { p->t = t; }
+
 void orc_problem_destroy(orc_problem *p) {
   if (!p) return;
+  for (int z = 0; z < 12; z++) {
+    free(p->ttimes[z]);
+    free(p->tfield[z]);
+  }
   free(p->gf);
   free(p->gg);
   free(p->dxinv);
@@ -249,7 +271,8 @@ static long pidx(const orc_problem *p, const long *s, const int *i) {
  * BCSupersonicInflow.c, BCSupersonicOutflow.c and BCSubsonicAmbivalent.c (which
  * takes inflow's or outflow's rule by `inflow`, the sign of the extrapolated face
  * velocity along the inward normal). */
-static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, double *out, int inflow) {
+static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, double *out, int inflow,
+                    double Tb) {
   double inv_gamma_m1 = 1.0 / (gamma - 1.0);
   double rho = 0, vel[3] = {0, 0, 0}, energy, pressure = 0, vsq;
   if (b->type != ORC_BC_SUPERSONIC_INFLOW) {
@@ -285,6 +308,17 @@ static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, do
       p_g = b->data[1 + nd];
       break;
     case ORC_BC_SUPERSONIC_OUTFLOW: break;
+    case ORC_BC_THERMAL_SLIP_WALL:
+      /* BCThermalSlipWall.c:86-105 (3-D): the normal velocity mirrored about the wall's,
+       * the pressure from the extrapolated density and the wall temperature */
+      v_g[b->dim] = 2.0 * b->data[b->dim] - vel[b->dim];
+      p_g = rho_g * Tb;
+      break;
+    case ORC_BC_THERMAL_NOSLIP_WALL:
+      /* BCThermalNoslipWall.c:86-105 (3-D): every velocity component mirrored */
+      for (int d = 0; d < nd; d++) v_g[d] = 2.0 * b->data[d] - vel[d];
+      p_g = rho_g * Tb;
+      break;
     case ORC_BC_SUBSONIC_AMBIVALENT:
       /* BCSubsonicAmbivalent.c:105-117: inflow takes density and velocity, outflow the
        * pressure (data: rho, velocity, pressure) */
@@ -306,7 +340,7 @@ static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, do
   return 0;
 }
 
-int orc_apply_bc(const orc_problem *p, double *u) {
+static int apply_bc_at(const orc_problem *p, double *u, double t) {
   long s[3];
   strides_wg(p, s);
   int nd = p->ndims, nv = p->nvars, g = p->ghosts;
@@ -320,6 +354,14 @@ int orc_apply_bc(const orc_problem *p, double *u) {
       count *= (bounds[d] > 0 ? bounds[d] : 0);
     }
     if (!count) continue;
+    /* thermal walls: the time level in use, the last one at or before t
+     * (BCThermalNoslipWall.c:55-57) */
+    int it = 0;
+    if (b->type == ORC_BC_THERMAL_SLIP_WALL || b->type == ORC_BC_THERMAL_NOSLIP_WALL) {
+      if (!p->tn[z]) return 1;
+      it = p->tn[z] - 1;
+      while (p->ttimes[z][it] > t && it > 0) it--;
+    }
     for (long c = 0; c < count; c++) {
       long r = c;
       for (int d = 0; d < nd; d++) { ib[d] = (int)(r % bounds[d]); r /= bounds[d]; }
@@ -360,7 +402,17 @@ int orc_apply_bc(const orc_problem *p, double *u) {
           for (int d = 0; d < nd; d++) vn = vn + vb[d] * (d == dd ? (double)b->face : 0.0);
           inflow = vn > 0;
         }
-        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1, inflow)) return 1;
+        double Tb = 0.0;
+        if (b->type == ORC_BC_THERMAL_SLIP_WALL || b->type == ORC_BC_THERMAL_NOSLIP_WALL) {
+          /* the field index of this point: zone-relative indices, the time level along dim */
+          long q = 0, stride = 1;
+          for (int d = 0; d < nd; d++) {
+            q += stride * (d == dd ? it : ib[d]);
+            stride *= (d == dd ? p->tn[z] : bounds[d]);
+          }
+          Tb = p->tfield[z][q];
+        }
+        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1, inflow, Tb)) return 1;
       } else {
         return 1;
       }
@@ -368,6 +420,9 @@ int orc_apply_bc(const orc_problem *p, double *u) {
   }
   return 0;
 }
+
+
+int orc_apply_bc(const orc_problem *p, double *u) { return apply_bc_at(p, u, p->t); }
 
 /* ------------------------------------------------------------------------ */
 /* physical models: flux, Roe average, eigen-structure                        */
@@ -1624,12 +1679,17 @@ int orc_source(const orc_problem *p, const double *u, double *src) {
   return rc;
 }
 
-int orc_rhs(const orc_problem *p, double *u, double *rhs) {
+static int rhs_at(const orc_problem *p, double *u, double *rhs, double t) {
   long n = orc_npoints_wghosts(p) * p->nvars;
   double *hyp = (double *)malloc(sizeof(double) * n);
   double *par = (double *)malloc(sizeof(double) * n);
   double *src = (double *)calloc(n, sizeof(double));
-  orc_apply_bc(p, u);
+  if (apply_bc_at(p, u, t)) {
+    free(hyp);
+    free(par);
+    free(src);
+    return -1;
+  }
   int rc = hyperbolic_source(p, u, hyp, src);
   orc_parabolic(p, u, par);
 #pragma omp parallel for schedule(static) num_threads(NTHR)
@@ -1646,6 +1706,8 @@ int orc_rhs(const orc_problem *p, double *u, double *rhs) {
   return rc;
 }
 
+int orc_rhs(const orc_problem *p, double *u, double *rhs) { return rhs_at(p, u, rhs, p->t); }
+
 /* TimeRK (src/TimeIntegration/TimeRK.c:126-195) for one simulation:
  * U[s] = u + sum_{i<s} (dt*A[s][i]) Udot[i];  Udot[s] = RHS(U[s]);
  * u += (dt*b[s]) Udot[s], all over the full array including ghost points. */
@@ -1654,17 +1716,20 @@ int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
   long n = orc_npoints_wghosts(p) * p->nvars;
   double *U = (double *)malloc(sizeof(double) * n);
   double *Udot = (double *)malloc(sizeof(double) * n * nstages);
+  double t = p->t;
   for (int step = 0; step < nsteps; step++) {
-    orc_apply_bc(p, u); /* TimePreStep */
+    apply_bc_at(p, u, t); /* TimePreStep */
     for (int st = 0; st < nstages; st++) {
       memcpy(U, u, sizeof(double) * n);
+      double c = 0.0; /* the stage's time fraction: the row sum of A (c of the tableau) */
       for (int i = 0; i < st; i++) {
         double a = dt * A[st * nstages + i];
+        c += A[st * nstages + i];
         const double *k = Udot + (long)i * n;
 #pragma omp parallel for schedule(static) num_threads(NTHR)
         for (long q = 0; q < n; q++) U[q] += a * k[q];
       }
-      if (orc_rhs(p, U, Udot + (long)st * n)) {
+      if (rhs_at(p, U, Udot + (long)st * n, t + c * dt)) {
         free(U);
         free(Udot);
         return -1;
@@ -1676,6 +1741,7 @@ int orc_rk(const orc_problem *p, int nstages, const double *A, const double *b,
 #pragma omp parallel for schedule(static) num_threads(NTHR)
       for (long q = 0; q < n; q++) u[q] += a * k[q];
     }
+    t += dt;
   }
   free(U);
   free(Udot);

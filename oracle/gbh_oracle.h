@@ -24,7 +24,8 @@ enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2, ORC_UPW_RUSANOV = 3 };
 enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
 enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
        ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,
-       ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9, ORC_BC_SUBSONIC_AMBIVALENT = 10 };
+       ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9, ORC_BC_SUBSONIC_AMBIVALENT = 10,
+       ORC_BC_THERMAL_SLIP_WALL = 11, ORC_BC_THERMAL_NOSLIP_WALL = 12 };
 
 /* One boundary zone, as DomainBoundary after CalculateLocalExtent
  * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index
@@ -51,6 +52,13 @@ typedef struct {
   int has_grav;
   double grav[3], RT;
   double *gf, *gg;
+  /* the time the boundaries of orc_apply_bc / orc_rhs are evaluated at (orc_rk
+   * starts its steps there), and per thermal-wall zone the wall temperature's time
+   * levels and field (BCReadTemperatureData layout: the zone's extent with the time
+   * level along its own dimension) */
+  double t;
+  int tn[12];
+  double *ttimes[12], *tfield[12];
 } orc_problem;
 
 /* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
@@ -73,6 +81,12 @@ void orc_get_gravity(const orc_problem *p, double *out);
 int orc_set_gravity_1d(orc_problem *p, const double *xg, double g, int type);
 /* The values boundary.inp gives for zone z after its extents (8 doubles). */
 void orc_set_zone_data(orc_problem *p, int z, const double *data);
+/* Thermal walls: the wall temperature of zone z at n time levels (times[n]) over the
+ * zone's extent (field: the zone's extent per dimension, n along the zone's own
+ * dimension, dimension 0 fastest); copied. */
+int orc_set_zone_temperature(orc_problem *p, int z, int n, const double *times, const double *field);
+/* The time of orc_apply_bc and orc_rhs and the start time of orc_rk. */
+void orc_set_time(orc_problem *p, double t);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

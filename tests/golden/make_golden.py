@@ -147,11 +147,45 @@ CASES = {
     "vortex24_char_roe_ambivalent": lambda: _b(_stir2(C.vortex(24, n_iter=4, dt=0.01)), {
         (0, 1): ("subsonic-ambivalent", [1.0, 0.5, 0.0, 1.0]), (0, -1): ("subsonic-ambivalent", [1.0, 0.5, 0.0, 1.0]),
         (1, 1): ("subsonic-ambivalent", [1.1, 0.0, 0.2, 0.9]), (1, -1): ("subsonic-ambivalent", [0.9, 0.1, 0.0, 1.1])}),
+    # thermal walls (NavierStokes3D): the pressure from the extrapolated density and a wall
+    # temperature read from file, at the time level of each stage's time
+    "tgv12_comp_roe_thermal_noslip_rk4": lambda: _thermal(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05),
+                                                          "thermal-noslip-wall", [0.0, 0.0, 0.0]),
+    "tgv12_char_llf_thermal_slip_ssprk3": lambda: _thermal(C.tgv(12, n_iter=3, dt=0.02, interp="characteristic",
+                                                                 upwinding="llf-char", scheme="ssprk3",
+                                                                 perturb=0.05),
+                                                           "thermal-slip-wall", [0.0, 0.05, 0.0], dim=1),
     "tgv12_comp_llf_ambivalent_rk4": lambda: _b(_stir(C.tgv(12, n_iter=3, dt=0.02, upwinding="llf-char",
                                                             perturb=0.05), speed=0.3), {
         (2, 1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, 0.1, 1.0 / 1.4]),
         (2, -1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, -0.1, 1.0 / 1.4])}),
 }
+
+
+def _thermal(case, kind, vel, dim=2):
+    """Thermal walls on both faces along `dim` of a 3-D deck: two time levels of the wall
+    temperature (t = 0 and t = 0.03, so that a 3-step run with dt = 0.02 changes level
+    inside a step), varying over the face."""
+    n = case.size
+    other = [e for e in range(3) if e != dim]
+    a = np.arange(n[other[0]]) / n[other[0]]
+    b = np.arange(n[other[1]]) / n[other[1]]
+    B, A = np.meshgrid(b, a, indexing="ij")  # [index along other[1], index along other[0]]
+    levels = [0.70 + 0.02 * np.sin(2 * np.pi * A) * np.cos(2 * np.pi * B),
+              0.74 + 0.01 * np.cos(2 * np.pi * A)]
+    bcs = {}
+    for face, shift in ((1, 0.0), (-1, 0.01)):
+        field = np.stack([lv + shift for lv in levels])  # [level, other[1], other[0]]
+        # the reference's layout: dimension 0 fastest, the time level along `dim`
+        if dim == 2:
+            arr = field
+        elif dim == 1:
+            arr = np.transpose(field, (1, 0, 2))  # [z, level, x]
+        else:
+            arr = np.transpose(field, (1, 2, 0))  # [z, y, level]
+        bcs[(dim, face)] = (kind, vel, ([0.0, 0.03], arr.reshape(-1)))
+    case.bcs = bcs
+    return case
 
 
 def _stir2(case, speed=0.3, seed=13):
