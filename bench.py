@@ -52,14 +52,14 @@ UNIT = "cell-component updates/s"
 # that of the full grid to within the segment-boundary share).
 FP64_PER_CELL_STEP = {
     "vortex": {"tile": {"flops": 8454.6, "instr": 5494.4, "captured": "512^2, tiles of 128 interfaces"},
-               "walker": {"flops": 8745.8, "instr": 5698.9, "captured": "512^2, segments 54/27"}},
+               "walker": {"flops": 8585.4, "instr": 5575.5, "captured": "512^2, segments 54/27"}},
     "sod": {"lanes": {"flops": 3654.7, "instr": 2455.2, "captured": "1024 (the full grid), lane groups of 16"}},
     "tgv": {"walker": {"flops": 18445.5, "instr": 12291.2,
                        "captured": "128^3, segments 48/32/32 (the 256^3 shape)"}},
     "rtb": {"walker": {"flops": 16583.3, "instr": 11627.6, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"}},
     "rtb64": {"walker": {"flops": 25265.3, "instr": 17712.2, "captured": "64^3 (the full grid), segments 7/7/7"}},
-    "dns": {"walker": {"flops": 20731.2, "instr": 14902.2, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"}},
-    "dns64cr": {"walker": {"flops": 34233.9, "instr": 23443.6, "captured": "64^3 (the full grid), segments 5/8/5"}},
+    "dns": {"walker": {"flops": 20731.2, "instr": 14874.6, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"}},
+    "dns64cr": {"walker": {"flops": 34332.9, "instr": 23470.2, "captured": "64^3 (the full grid), segments 5/5/4"}},
 }
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
 # update), per kernel form: the segment walker from a 2048^2 capture of the

@@ -58,6 +58,9 @@ class Case:
     # and len(times) along the wall's own dimension, dimension 0 fastest (the
     # reference's temperature file layout, written beside the deck by `write`)
     bcs: Optional[dict] = None
+    # sponge zones after the face zones: [(dim, face, [(xmin, xmax) per dim], [nvars values])],
+    # the state the sponge relaxes to over the box xmin..xmax (BCSponge.c)
+    sponges: Optional[list] = None
     # gravity: NavierStokes3D (physics.inp gravity gx gy gz / rho_ref / p_ref / R / HB /
     # N_bv) or Euler1D (gravity g, gravity_type grav_type)
     gravity: Optional[Sequence[float]] = None
@@ -150,6 +153,9 @@ class Case:
                 if bctype.startswith("thermal-"):
                     items.append(self.temperature_file(d, face))
                 rows.append(f"{bctype} {d} {face} " + " ".join(items))
+        for d, face, box, vals in (self.sponges or []):
+            items = [repr(float(v)) for lohi in box for v in lohi] + [repr(float(v)) for v in vals]
+            rows.append(f"sponge {d} {face} " + " ".join(items))
         return f"{len(rows)}\n" + "\n".join(rows) + "\n"
 
     @staticmethod

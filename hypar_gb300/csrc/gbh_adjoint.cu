@@ -1106,8 +1106,11 @@ extern "C" int gb_adjoint_create_ex(const gb_config* cfg, const double* dxinv, i
   DevGeom G;
   std::vector<int> mem;
   long long npts = gbh_geometry(*cfg, G, &mem);
+  for (int z = 0; z < cfg->nzones; z++)
+    if (cfg->zones[z][0] == GB_BC_SPONGE) mem.push_back(z);
   if (!mem.empty()) {
-    gbh_set_error("gb_adjoint_create: every boundary face must be one whole-face periodic or extrapolate zone");
+    gbh_set_error("gb_adjoint_create: every boundary face must be one whole-face periodic or extrapolate zone, "
+                  "with no sponge zone");
     return GB_ERR_UNSUPPORTED;
   }
   gb_adjoint* a = new gb_adjoint();

@@ -49,6 +49,8 @@ cudaError_t launch_visc(const double*, double*, double*, double*, const double*,
 cudaError_t launch_bc_zone(double*, const DevGeom&, int, const int*, const double*, double, cudaStream_t);
 cudaError_t launch_bc_zone_t(double*, const DevGeom&, int, const int*, const double*, double, const double*, int, int,
                              cudaStream_t);
+cudaError_t launch_sponge(double*, const double*, const DevGeom&, int, const int*, const double*, const double*,
+                          cudaStream_t);
 cudaError_t launch_finite_check(const double*, const DevGeom&, int, int*, cudaStream_t);
 cudaError_t launch_pack(double*, const double*, const DevGeom&, int, int, cudaStream_t);
 }  // namespace gbh
@@ -209,6 +211,48 @@ extern "C" int gb_solver_set_zone_temperature(gb_solver* s, int zone, int ntimes
   return GB_OK;
 }
 
+extern "C" int gb_solver_set_zone_sponge(gb_solver* s, int zone, const double* sigma) {
+  if (!s || zone < 0 || zone >= s->cfg.nzones) {
+    gbh_set_error("gb_solver_set_zone_sponge: bad argument");
+    return GB_ERR_ARG;
+  }
+  const int* q = s->cfg.zones[zone];
+  if (q[0] != GB_BC_SPONGE) {
+    gbh_set_error("gb_solver_set_zone_sponge: zone %d is not a sponge", zone);
+    return GB_ERR_ARG;
+  }
+  const int n = q[6 + q[1]] - q[3 + q[1]];
+  if (n <= 0) return GB_OK;  // an empty zone
+  if (!sigma) {
+    gbh_set_error("gb_solver_set_zone_sponge: null sigma");
+    return GB_ERR_ARG;
+  }
+  cudaFree(s->d_sigma[zone]);
+  s->d_sigma[zone] = nullptr;
+  CK(cudaMalloc((void**)&s->d_sigma[zone], n * sizeof(double)));
+  CK(cudaMemcpy(s->d_sigma[zone], sigma, n * sizeof(double), cudaMemcpyHostToDevice));
+  return GB_OK;
+}
+
+static bool zone_empty(const gb_config& c, int z) {
+  for (int d = 0; d < c.ndims; d++)
+    if (c.zones[z][6 + d] <= c.zones[z][3 + d]) return true;
+  return false;
+}
+
+// Every sponge zone's source term added into src (SourceFunction.c:50-76, zone order).
+static int add_sponges(gb_solver* s, double* src, const double* U) {
+  for (int z = 0; z < s->cfg.nzones; z++) {
+    if (s->cfg.zones[z][0] != GB_BC_SPONGE || zone_empty(s->cfg, z)) continue;
+    if (!s->d_sigma[z]) {
+      gbh_set_error("boundary zone %d is a sponge: call gb_solver_set_zone_sponge first", z);
+      return GB_ERR_ARG;
+    }
+    CK(launch_sponge(src, U, s->G, s->cfg.nvars, s->cfg.zones[z], s->cfg.zone_data[z], s->d_sigma[z], s->stream));
+  }
+  return GB_OK;
+}
+
 // Right-hand side of U into `epi` (EPI_RHS or EPI_RK): boundary zones kept in
 // memory, the viscous term, then one fused hyperbolic launch per direction.
 static int gravity_ready(gb_solver* s) {
@@ -228,6 +272,15 @@ static int rhs_launches(gb_solver* s, double* U, StageEpi ep, double t) {
     int pr = prof_begin(s, GB_PROF_VISC);
     CK(launch_visc(U, s->d_Q, s->d_Gr, s->d_par, s->d_dxinv, s->G, s->vp, s->visc_seg, s->stream));
     prof_end(s, pr);
+    ep.par = s->d_par;
+  }
+  if (s->sponge) {
+    // the sponge joins the parabolic term the stage epilogue adds (rhs = par - hyp)
+    int pr = prof_begin(s, GB_PROF_BC);
+    if (!s->viscous) CK(cudaMemsetAsync(s->d_par, 0, s->nvals * sizeof(double), s->stream));
+    rc = add_sponges(s, s->d_par, U);
+    prof_end(s, pr);
+    if (rc) return rc;
     ep.par = s->d_par;
   }
   int nd = s->cfg.ndims;
@@ -285,10 +338,20 @@ int gbh_validate(const gb_config* c) {
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
-    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_THERMAL_NOSLIP_WALL || q[1] < 0 || q[1] >= nd ||
+    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SPONGE || q[1] < 0 || q[1] >= nd ||
         (q[2] != 1 && q[2] != -1)) {
       gbh_set_error("bad zone %d", z);
       return GB_ERR_ARG;
+    }
+    if (q[0] == GB_BC_SPONGE) {
+      // interior points only (CalculateLocalExtent, InitializeBoundaries.c:382-393)
+      bool empty = false, inside = true;
+      for (int d = 0; d < nd; d++) {
+        if (q[6 + d] <= q[3 + d]) empty = true;
+        if (q[3 + d] < 0 || q[6 + d] > c->dim[d]) inside = false;
+      }
+      if (!empty && !inside) { gbh_set_error("sponge zone %d must cover interior points only", z); return GB_ERR_ARG; }
+      continue;
     }
     if (q[0] > GB_BC_DIRICHLET && nd < 2) {
       gbh_set_error("zone %d: wall / inflow / outflow boundaries need Euler2D or NavierStokes3D", z);
@@ -326,7 +389,7 @@ long long gbh_geometry(const gb_config& c, DevGeom& G, std::vector<int>* mem_zon
     for (int side = 0; side < 2; side++) {
       int face = side == 0 ? 1 : -1, cnt = 0, which = -1;
       for (int z = 0; z < c.nzones; z++)
-        if (c.zones[z][1] == d && c.zones[z][2] == face) { cnt++; which = z; }
+        if (c.zones[z][0] != GB_BC_SPONGE && c.zones[z][1] == d && c.zones[z][2] == face) { cnt++; which = z; }
       bool full = false;
       // only periodic and extrapolate (a copy of one interior cell) fold into the loads
       if (cnt == 1 && c.zones[which][0] != GB_BC_PERIODIC && c.zones[which][0] != GB_BC_EXTRAPOLATE) cnt = 0;
@@ -340,7 +403,8 @@ long long gbh_geometry(const gb_config& c, DevGeom& G, std::vector<int>* mem_zon
       if (side == 0) G.bclo[d] = mode; else G.bchi[d] = mode;
       if (mem_zones)
         for (int z = 0; z < c.nzones; z++)
-          if (c.zones[z][1] == d && c.zones[z][2] == face && !full) mem_zones->push_back(z);
+          if (c.zones[z][0] != GB_BC_SPONGE && c.zones[z][1] == d && c.zones[z][2] == face && !full)
+            mem_zones->push_back(z);
     }
   return st;
 }
@@ -414,8 +478,10 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
     A(&s->d_crC, nc * sizeof(double));
     if (!chr) A(&s->d_crF, bytes);
   }
+  for (int z = 0; z < c.nzones; z++)
+    if (c.zones[z][0] == GB_BC_SPONGE && !zone_empty(c, z)) s->sponge = true;
+  if (s->viscous || s->sponge) A(&s->d_par, bytes);
   if (s->viscous) {
-    A(&s->d_par, bytes);
     A(&s->d_Q, (size_t)st * 6 * sizeof(double));
     A(&s->d_Gr, (size_t)st * 12 * sizeof(double));
   }
@@ -439,7 +505,10 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
   cudaFree(s->d_acc);
   for (int k = 0; k < 4; k++) cudaFree(s->d_P[k]);
   cudaFree(s->d_U0);
-  for (int z = 0; z < GB_MAX_ZONES; z++) cudaFree(s->d_tfield[z]);
+  for (int z = 0; z < GB_MAX_ZONES; z++) {
+    cudaFree(s->d_tfield[z]);
+    cudaFree(s->d_sigma[z]);
+  }
   cudaFree(s->d_H);
   cudaFree(s->d_crX);
   cudaFree(s->d_crC);
@@ -925,9 +994,13 @@ extern "C" int gb_SourceFunction(double* source, double* u, void* sv, void* m, d
     const long long n = (long long)s->nvals;
     sub_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s->stream>>>(source, H, n);
     CK(cudaGetLastError());
-    return GB_OK;
+    return u ? add_sponges(s, source, u) : GB_OK;
   }
   CK(cudaMemsetAsync(source, 0, s->nvals * sizeof(double), s->stream));
+  if (s->sponge) {
+    if (!u) { gbh_set_error("gb_SourceFunction: null argument"); return GB_ERR_ARG; }
+    return add_sponges(s, source, u);
+  }
   return GB_OK;
 }
 

@@ -178,6 +178,11 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
   for (int m = 0; m < nsims; m++) {
     int rc = gbh_validate(&cfgs[m]);
     if (rc) return rc;
+    for (int z = 0; z < cfgs[m].nzones; z++)
+      if (cfgs[m].zones[z][0] == GB_BC_SPONGE) {
+        gbh_set_error("ensemble member %d: sponge zones are not available in the ensemble; use a gb_solver", m);
+        return GB_ERR_UNSUPPORTED;
+      }
     const gb_config &a = cfgs[0], &b = cfgs[m];
     if (a.model != b.model || a.interp != b.interp || a.upwind != b.upwind || a.gamma != b.gamma ||
         a.weno_eps != b.weno_eps || a.rk_nstages != b.rk_nstages || a.dt != b.dt ||

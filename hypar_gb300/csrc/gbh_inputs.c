@@ -35,6 +35,9 @@ struct gb_inputs {
   /* thermal walls: per zone the wall temperature's time levels and field, or NULL */
   int tn[GB_MAX_ZONES];
   double *ttimes[GB_MAX_ZONES], *tfield[GB_MAX_ZONES];
+  /* sponge zones: per zone sigma along the zone's dimension, or NULL */
+  int sn[GB_MAX_ZONES];
+  double *sigma[GB_MAX_ZONES];
   char op_overwrite[64];
   char op_format[64];
 };
@@ -433,8 +436,19 @@ void gb_inputs_free(gb_inputs *in) {
   for (int z = 0; z < GB_MAX_ZONES; z++) {
     free(in->ttimes[z]);
     free(in->tfield[z]);
+    free(in->sigma[z]);
   }
   free(in);
+}
+
+int gb_inputs_zone_sponge(const gb_inputs *in, int zone, int *n, const double **sigma) {
+  if (!in || !n || !sigma || zone < 0 || zone >= GB_MAX_ZONES) {
+    gbh_set_error("gb_inputs_zone_sponge: bad argument");
+    return GB_ERR_ARG;
+  }
+  *n = in->sn[zone];
+  *sigma = in->sigma[zone];
+  return GB_OK;
 }
 
 int gb_inputs_zone_temperature(const gb_inputs *in, int zone, int *ntimes, const double **times,
@@ -819,7 +833,8 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
           {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW, 0},
           {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT, -4},
           {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL, -2},
-          {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL, -2}};
+          {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL, -2},
+          {"sponge", GB_BC_SPONGE, -1}};
       int tcode = 0, nvals = 0;
       for (size_t t = 0; t < sizeof(bct) / sizeof(bct[0]); t++)
         if (!strcmp(type, bct[t].name)) {
@@ -846,7 +861,7 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         gbh_set_error("boundary.inp: zone %d (%s) lacks its values", z, type);
         return GB_ERR_INPUT;
       }
-      if (tcode > GB_BC_DIRICHLET && c.ndims < 2) {
+      if (tcode > GB_BC_DIRICHLET && tcode != GB_BC_SPONGE && c.ndims < 2) {
         fclose(in);
         gb_inputs_free(res);
         gbh_set_error("boundary type %s needs Euler2D or NavierStokes3D", type);
@@ -866,7 +881,7 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
       for (int d = 0; d < 3; d++) {
         int is = 0, ie = 1;
         if (d < c.ndims) {
-          if (d == dim) {
+          if (d == dim && tcode != GB_BC_SPONGE) {
             if (face == 1) { is = -c.ghosts; ie = 0; }
             else { is = c.dim[d]; ie = c.dim[d] + c.ghosts; }
           } else {
@@ -876,6 +891,27 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         }
         zz[3 + d] = is;
         zz[6 + d] = ie;
+      }
+      if (tcode == GB_BC_SPONGE) {
+        /* sigma over the zone's indices along its dimension (BCSponge.c:49-54) */
+        long xo = 0;
+        for (int d = 0; d < dim; d++) xo += c.dim[d];
+        const int n = zz[6 + dim] > zz[3 + dim] ? zz[6 + dim] - zz[3 + dim] : 0;
+        res->sn[z] = n;
+        if (n) {
+          res->sigma[z] = (double *)malloc(sizeof(double) * n);
+          if (!res->sigma[z]) {
+            fclose(in);
+            gb_inputs_free(res);
+            gbh_set_error("out of host memory");
+            return GB_ERR_NOMEM;
+          }
+          const double xs = xmin[dim], xe = xmax[dim];
+          for (int k = 0; k < n; k++) {
+            const double xk = res->x[xo + zz[3 + dim] + k];
+            res->sigma[z][k] = face > 0 ? (xk - xs) / (xe - xs) : (xk - xe) / (xs - xe);
+          }
+        }
       }
       if (thermal) {
         int rc = read_temperature(dir, tname, &c, zz, res, z);

@@ -229,6 +229,11 @@ int gb_run_case(const char *dir, int device, int verbose) {
     const double *tt = NULL, *tf = NULL;
     rc = gb_inputs_zone_temperature(in, z, &nt, &tt, &tf);
     if (!rc && nt) rc = gb_solver_set_zone_temperature(s, z, nt, tt, tf);
+    /* sponge zones: sigma computed with the deck */
+    int ns = 0;
+    const double *sg = NULL;
+    if (!rc) rc = gb_inputs_zone_sponge(in, z, &ns, &sg);
+    if (!rc && ns) rc = gb_solver_set_zone_sponge(s, z, sg);
   }
   /* InitialSolution.c:118: the volume integral of the initial solution */
   if (!rc && c->cons_check) rc = gb_solver_conservation_begin(s);

@@ -54,6 +54,9 @@ struct gb_solver {
   // thermal walls: per zone the wall temperature's time levels (host) and field (device)
   std::vector<double> ttimes[GB_MAX_ZONES];
   double* d_tfield[GB_MAX_ZONES] = {};
+  // sponge zones: sigma along the zone's dimension (device), and whether any zone is one
+  double* d_sigma[GB_MAX_ZONES] = {};
+  bool sponge = false;
   int iter = 0;            // steps taken since the state was set (PostStep's iteration index)
   long long dx_off[3] = {0, 0, 0};
   bool viscous = false;

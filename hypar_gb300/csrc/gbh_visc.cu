@@ -357,6 +357,7 @@ cudaError_t launch_bc_zone(double* u, const DevGeom& G, int nv, const int* zone9
 // array) and the level `it` in use.
 cudaError_t launch_bc_zone_t(double* u, const DevGeom& G, int nv, const int* zone9, const double* data8,
                              double gamma, const double* tfield, int tn, int it, cudaStream_t s) {
+  if (zone9[0] == GB_BC_SPONGE) return cudaSuccess;  // a source term, no ghost points (BCSpongeUDummy)
   ZoneDev z;
   z.tfield = tfield;
   z.tn = tn;
@@ -376,6 +377,48 @@ cudaError_t launch_bc_zone_t(double* u, const DevGeom& G, int nv, const int* zon
   }
   if (n <= 0) return cudaSuccess;
   bc_zone_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(u, G, nv, z);
+  return cudaGetLastError();
+}
+
+// The sponge zone's source (BCSponge.c:34-61): src -= sigma_i (u - u_ref) at every
+// interior point of the zone's extent, sigma indexed along the zone's dimension.  The
+// three roundings of the reference's expression are kept (no contraction).  Zones may
+// overlap: one launch per zone, in zone order, on one stream.
+__global__ void sponge_kernel(double* __restrict__ src, const double* __restrict__ u, DevGeom G, int nv,
+                              ZoneDev z, const double* __restrict__ sigma) {
+  int b[3] = {1, 1, 1};
+  for (int d = 0; d < G.nd; d++) b[d] = z.ie[d] - z.is[d];
+  const long long n = (long long)b[0] * b[1] * b[2];
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int ib[3] = {(int)(t % b[0]), (int)((t / b[0]) % b[1]), (int)(t / ((long long)b[0] * b[1]))};
+  long long p = 0;
+  for (int d = 0; d < G.nd; d++) p += (long long)(ib[d] + z.is[d] + G.g) * G.stride[d];
+  const double sg = sigma[ib[z.dim]];
+  for (int v = 0; v < nv; v++)
+    src[p * nv + v] = __dsub_rn(src[p * nv + v], __dmul_rn(sg, __dsub_rn(u[p * nv + v], z.data[v])));
+}
+
+cudaError_t launch_sponge(double* src, const double* u, const DevGeom& G, int nv, const int* zone9,
+                          const double* uref8, const double* sigma, cudaStream_t s) {
+  if (zone9[0] != GB_BC_SPONGE) return cudaErrorInvalidValue;
+  ZoneDev z;
+  z.tfield = nullptr;
+  z.tn = z.it = 0;
+  z.type = zone9[0];
+  z.dim = zone9[1];
+  z.face = zone9[2];
+  z.gamma = 0.0;
+  for (int k = 0; k < 8; k++) z.data[k] = uref8[k];
+  long long n = 1;
+  for (int d = 0; d < 3; d++) {
+    z.is[d] = zone9[3 + d];
+    z.ie[d] = zone9[6 + d];
+    if (d < G.nd) n *= (z.ie[d] - z.is[d] > 0 ? z.ie[d] - z.is[d] : 0);
+  }
+  if (n <= 0) return cudaSuccess;
+  if (!sigma) return cudaErrorInvalidValue;
+  sponge_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(src, u, G, nv, z, sigma);
   return cudaGetLastError();
 }
 

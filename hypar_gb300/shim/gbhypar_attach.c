@@ -152,7 +152,8 @@ int gbshim_config(void *s, gb_config *c) {
         {"noslip-wall", GB_BC_NOSLIP_WALL},    {"subsonic-inflow", GB_BC_SUBSONIC_INFLOW},
         {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW}, {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW},
         {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}, {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT},
-        {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL}, {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL}};
+        {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL}, {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL},
+        {"sponge", GB_BC_SPONGE}};
     int code = 0;
     for (size_t t = 0; t < sizeof(types) / sizeof(types[0]); t++)
       if (!strcmp(B->bctype, types[t].name)) code = types[t].code;
@@ -170,6 +171,9 @@ int gbshim_config(void *s, gb_config *c) {
     switch (code) {
       case GB_BC_DIRICHLET:
         for (int k = 0; k < c->nvars; k++) v[k] = B->DirichletValue[k];
+        break;
+      case GB_BC_SPONGE:
+        for (int k = 0; k < c->nvars; k++) v[k] = B->SpongeValue[k];
         break;
       case GB_BC_SLIP_WALL:
       case GB_BC_NOSLIP_WALL:
@@ -305,6 +309,33 @@ int gbshim_attach(void *s, void *mpi) {
     if (c.zones[z][0] != GB_BC_THERMAL_SLIP_WALL && c.zones[z][0] != GB_BC_THERMAL_NOSLIP_WALL) continue;
     rc = gb_solver_set_zone_temperature(gb, z, B->UnsteadyTemperatureSize[B->dim], B->UnsteadyTimeLevels,
                                         B->UnsteadyTemperatureData);
+    if (rc) {
+      fprintf(stderr, "gbhypar: %s\n", gb_last_error());
+      gb_solver_destroy(gb);
+      return rc;
+    }
+  }
+  /* sponge zones: sigma over the zone's indices along its dimension, from HyPar's grid
+   * (solver->x, ghost points included) and the zone's bounds (BCSponge.c:49-54) */
+  for (int z = 0; z < c.nzones; z++) {
+    const DomainBoundary *B = &((const DomainBoundary *)solver->boundary)[z];
+    if (c.zones[z][0] != GB_BC_SPONGE || !B->on_this_proc) continue;
+    const int dim = B->dim, n = B->ie[dim] - B->is[dim];
+    if (n <= 0) continue;
+    int off = 0;
+    for (int d = 0; d < dim; d++) off += solver->dim_local[d] + 2 * solver->ghosts;
+    double *sigma = (double *)malloc(sizeof(double) * n);
+    if (!sigma) {
+      gb_solver_destroy(gb);
+      return GB_ERR_NOMEM;
+    }
+    const double xs = B->xmin[dim], xe = B->xmax[dim];
+    for (int k = 0; k < n; k++) {
+      const double x = solver->x[off + solver->ghosts + B->is[dim] + k];
+      sigma[k] = B->face > 0 ? (x - xs) / (xe - xs) : (x - xe) / (xs - xe);
+    }
+    rc = gb_solver_set_zone_sponge(gb, z, sigma);
+    free(sigma);
     if (rc) {
       fprintf(stderr, "gbhypar: %s\n", gb_last_error());
       gb_solver_destroy(gb);

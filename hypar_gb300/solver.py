@@ -62,6 +62,13 @@ class Inputs:
                         size *= q[6 + d] - q[3 + d]
                 self.zone_temperature[z] = (np.ctypeslib.as_array(tp, shape=(n.value,)).copy(),
                                             np.ctypeslib.as_array(fp, shape=(size,)).copy())
+        # sponge zones: per zone sigma along the zone's dimension
+        self.zone_sponge = {}
+        for z in range(c.nzones):
+            n, sp = ctypes.c_int(), _lib.DP()
+            check(lib().gb_inputs_zone_sponge(h, z, ctypes.byref(n), ctypes.byref(sp)))
+            if n.value:
+                self.zone_sponge[z] = np.ctypeslib.as_array(sp, shape=(n.value,)).copy()
         lib().gb_inputs_free(h)
         self._h = None
 
@@ -94,6 +101,8 @@ class Solver:
             s.set_gravity_field(inp.gravity_field)
         for z, (times, field) in inp.zone_temperature.items():
             s.set_zone_temperature(z, times, field)
+        for z, sigma in inp.zone_sponge.items():
+            s.set_zone_sponge(z, sigma)
         return s
 
     def set_zone_temperature(self, zone: int, times, field):
@@ -103,6 +112,11 @@ class Solver:
         field = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
         check(lib().gb_solver_set_zone_temperature(self._h, int(zone), len(times), times.ctypes.data_as(_lib.DP),
                                                    field.ctypes.data_as(_lib.DP)))
+
+    def set_zone_sponge(self, zone: int, sigma):
+        """A sponge zone's sigma, one value per index of the zone along its dimension."""
+        sigma = np.ascontiguousarray(sigma, dtype=np.float64)
+        check(lib().gb_solver_set_zone_sponge(self._h, int(zone), sigma.ctypes.data_as(_lib.DP)))
 
     def set_gravity_field(self, fg: np.ndarray):
         """Upload the hydrostatic fields f then g (ghosted layout, x fastest) that the

@@ -46,11 +46,17 @@ enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
  * extrapolated face velocity), for Euler2D and NavierStokes3D (the reference's 1-D
  * branches of those are incomplete); the thermal walls (slip / no-slip, the ghost
  * pressure from the extrapolated density and a wall temperature given per time
- * level in a file) for NavierStokes3D (BCThermalSlipWall.c, BCThermalNoslipWall.c). */
+ * level in a file) for NavierStokes3D (BCThermalSlipWall.c, BCThermalNoslipWall.c).
+ * sponge (every model) fills no ghost point: over its extent of interior points it adds
+ * -sigma (u - u_ref) to the source term, sigma rising linearly from 0 at the zone's inner
+ * edge to 1 at its outer one along the zone's dimension (BCSponge.c:34-61); its extent is
+ * an interior index range in every dimension (CalculateLocalExtent,
+ * InitializeBoundaries.c:382-393) and sigma comes through gb_inputs_zone_sponge /
+ * gb_solver_set_zone_sponge. */
 enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2, GB_BC_DIRICHLET = 3, GB_BC_SLIP_WALL = 4,
        GB_BC_NOSLIP_WALL = 5, GB_BC_SUBSONIC_INFLOW = 6, GB_BC_SUBSONIC_OUTFLOW = 7,
        GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9, GB_BC_SUBSONIC_AMBIVALENT = 10,
-       GB_BC_THERMAL_SLIP_WALL = 11, GB_BC_THERMAL_NOSLIP_WALL = 12 };
+       GB_BC_THERMAL_SLIP_WALL = 11, GB_BC_THERMAL_NOSLIP_WALL = 12, GB_BC_SPONGE = 13 };
 enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
 /* WENO5 nonlinear weights (weno.inp: yc > borges > mapped > Jiang-Shu, and
  * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
@@ -89,7 +95,8 @@ typedef struct gb_config {
    * slip-wall / noslip-wall: wall velocity (ndims); subsonic-inflow: rho, velocity;
    * subsonic-outflow: pressure; supersonic-inflow and subsonic-ambivalent: rho, velocity,
    * pressure; thermal-slip-wall / thermal-noslip-wall: wall velocity (the temperature
-   * comes through gb_inputs_zone_temperature / gb_solver_set_zone_temperature) */
+   * comes through gb_inputs_zone_temperature / gb_solver_set_zone_temperature); sponge:
+   * the nvars values of the state it relaxes to */
   double zone_data[GB_MAX_ZONES][8];
   /* NavierStokes3D gravity (physics.inp gravity, rho_ref, p_ref, R, HB, N_bv); a nonzero
    * acceleration needs upwinding rusanov (NavierStokes3DInitialize.c:371) and the
@@ -142,6 +149,11 @@ const double *gb_inputs_gravity_field(const gb_inputs *in);
  * The arrays belong to `in`. */
 int gb_inputs_zone_temperature(const gb_inputs *in, int zone, int *ntimes, const double **times,
                                const double **field);
+/* Sponge zones: sigma at each index of the zone's extent along its own dimension,
+ * n = ie - is values, (x - x_start) / (x_end - x_start) from the grid coordinates and
+ * the zone's bounds as boundary.inp gives them (BCSponge.c:49-54); n = 0 and NULL for
+ * other zones.  The array belongs to `in`. */
+int gb_inputs_zone_sponge(const gb_inputs *in, int zone, int *n, const double **sigma);
 /* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
  * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
  * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
@@ -172,6 +184,11 @@ int gb_solver_set_gravity_field(gb_solver *s, const double *fg);
  * Each right-hand side at time t uses the last level at or before t
  * (BCThermalNoslipWall.c:55-57); required before stepping such a configuration. */
 int gb_solver_set_zone_temperature(gb_solver *s, int zone, int ntimes, const double *times, const double *field);
+/* Sponge zones: upload sigma of boundary zone `zone` (host array of ie - is values along
+ * the zone's own dimension, as gb_inputs_zone_sponge gives it); required before
+ * evaluating a right-hand side of such a configuration.  The sponge term joins the
+ * source term of every right-hand side (SourceFunction.c:50-76). */
+int gb_solver_set_zone_sponge(gb_solver *s, int zone, const double *sigma);
 /* Wait for all work queued by the solver. */
 int gb_solver_sync(gb_solver *s);
 /* Copy a solution in or out (layout GB_LAYOUT_*, memory GB_MEM_*). */

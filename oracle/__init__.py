@@ -36,7 +36,7 @@ INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,
           "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9,
-          "subsonic-ambivalent": 10, "thermal-slip-wall": 11, "thermal-noslip-wall": 12}
+          "subsonic-ambivalent": 10, "thermal-slip-wall": 11, "thermal-noslip-wall": 12, "sponge": 13}
 
 
 SCHEMES = {"weno5": 0, "crweno5": 1}
@@ -47,7 +47,7 @@ def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
     return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
             "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims,
             "subsonic-ambivalent": 2 + ndims, "thermal-slip-wall": ndims,
-            "thermal-noslip-wall": ndims}.get(bctype, 0)
+            "thermal-noslip-wall": ndims, "sponge": nvars}.get(bctype, 0)
 
 _lib = None
 
@@ -84,6 +84,8 @@ def _bind(path):
     L.orc_set_zone_temperature.restype = ctypes.c_int
     L.orc_set_time.argtypes = [ctypes.c_void_p, ctypes.c_double]
     L.orc_set_time.restype = None
+    L.orc_set_zone_sponge.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double]
+    L.orc_set_zone_sponge.restype = ctypes.c_int
     L.orc_set_gravity.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double]
@@ -187,7 +189,7 @@ def zones_from_boundary(rows, xs: Sequence[np.ndarray], g: int) -> np.ndarray:
         is_ = [0, 0, 0]
         ie = [1, 1, 1]
         for d in range(nd):
-            if d == dim:
+            if d == dim and bctype != "sponge":
                 n = len(xs[d])
                 is_[d], ie[d] = (-g, 0) if face == 1 else (n, n + g)
             else:
@@ -284,6 +286,11 @@ class Problem:
                 field = np.ascontiguousarray(field, np.float64).reshape(-1)
                 if L.orc_set_zone_temperature(self.h, z, len(times), _dp(times), _dp(field)):
                     raise RuntimeError("orc_set_zone_temperature failed")
+            if row[0] == "sponge":
+                dim = row[1]
+                if L.orc_set_zone_sponge(self.h, z, _dp(np.ascontiguousarray(xs[dim])), float(row[3][dim][0]),
+                                         float(row[3][dim][1])):
+                    raise RuntimeError("orc_set_zone_sponge failed")
         grav = getattr(case, "gravity", None)
         if grav is not None and any(float(v) != 0.0 for v in grav):
             xg = np.concatenate([grid_with_ghosts(x, ghosts) for x in xs])

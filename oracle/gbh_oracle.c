@@ -228,11 +228,61 @@ int orc_set_zone_temperature(orc_problem *p, int z, int n, const double *times, 
 
 void orc_set_time(orc_problem *p, double t) { p->t = t; }
 
+int orc_set_zone_sponge(orc_problem *p, int z, const double *x, double xmin, double xmax) {
+  if (z < 0 || z >= p->nzones || p->zones[z].type != ORC_BC_SPONGE) return 1;
+  const int n = p->dim[p->zones[z].dim];
+  free(p->sx[z]);
+  p->sx[z] = (double *)malloc(sizeof(double) * n);
+  memcpy(p->sx[z], x, sizeof(double) * n);
+  p->sxmin[z] = xmin;
+  p->sxmax[z] = xmax;
+  return 0;
+}
+
+/* BCSpongeSource (src/BoundaryConditions/BCSponge.c:34-61) for every sponge zone, in
+ * zone order (SourceFunction.c:63-76): over the zone's interior points,
+ * src -= sigma (u - u_ref), sigma = (x - x_start) / (x_end - x_start) on face +1 and
+ * (x - x_end) / (x_start - x_end) on face -1. */
+static int sponge_source(const orc_problem *p, const double *u, double *src) {
+  long s[3];
+  strides_wg(p, s);
+  const int nd = p->ndims, nv = p->nvars;
+  for (int z = 0; z < p->nzones; z++) {
+    const orc_zone *b = &p->zones[z];
+    if (b->type != ORC_BC_SPONGE) continue;
+    int bounds[3] = {1, 1, 1}, ib[3] = {0, 0, 0};
+    long count = 1;
+    for (int d = 0; d < nd; d++) {
+      bounds[d] = b->ie[d] - b->is[d];
+      count *= (bounds[d] > 0 ? bounds[d] : 0);
+    }
+    if (!count) continue;
+    if (!p->sx[z]) return 1;
+    for (long c = 0; c < count; c++) {
+      long r = c;
+      int ig[3] = {0, 0, 0};
+      for (int d = 0; d < nd; d++) {
+        ib[d] = (int)(r % bounds[d]);
+        r /= bounds[d];
+        ig[d] = ib[d] + b->is[d];
+      }
+      const double x = p->sx[z][ig[b->dim]], xs = p->sxmin[z], xe = p->sxmax[z];
+      double sigma;
+      if (b->face > 0) sigma = (x - xs) / (xe - xs);
+      else sigma = (x - xe) / (xs - xe);
+      const long q = pidx(p, s, ig);
+      for (int v = 0; v < nv; v++) src[nv * q + v] -= (sigma * (u[nv * q + v] - b->data[v]));
+    }
+  }
+  return 0;
+}
+
 void orc_problem_destroy(orc_problem *p) {
   if (!p) return;
   for (int z = 0; z < 12; z++) {
     free(p->ttimes[z]);
     free(p->tfield[z]);
+    free(p->sx[z]);
   }
   free(p->gf);
   free(p->gg);
@@ -346,6 +396,7 @@ static int apply_bc_at(const orc_problem *p, double *u, double t) {
   int nd = p->ndims, nv = p->nvars, g = p->ghosts;
   for (int z = 0; z < p->nzones; z++) {
     const orc_zone *b = &p->zones[z];
+    if (b->type == ORC_BC_SPONGE) continue; /* a source term (BCSpongeUDummy) */
     int bounds[3] = {1, 1, 1}, ib[3] = {0, 0, 0};
     long count = 1;
     for (int d = 0; d < nd; d++) {
@@ -1675,6 +1726,7 @@ int orc_source(const orc_problem *p, const double *u, double *src) {
   double *hyp = (double *)malloc(sizeof(double) * n);
   for (long i = 0; i < n; i++) src[i] = 0.0;
   int rc = hyperbolic_source(p, u, hyp, src);
+  if (!rc) rc = sponge_source(p, u, src);
   free(hyp);
   return rc;
 }
@@ -1691,6 +1743,7 @@ static int rhs_at(const orc_problem *p, double *u, double *rhs, double t) {
     return -1;
   }
   int rc = hyperbolic_source(p, u, hyp, src);
+  if (!rc) rc = sponge_source(p, u, src);
   orc_parabolic(p, u, par);
 #pragma omp parallel for schedule(static) num_threads(NTHR)
   for (long i = 0; i < n; i++) {

@@ -25,7 +25,7 @@ enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
 enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
        ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,
        ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9, ORC_BC_SUBSONIC_AMBIVALENT = 10,
-       ORC_BC_THERMAL_SLIP_WALL = 11, ORC_BC_THERMAL_NOSLIP_WALL = 12 };
+       ORC_BC_THERMAL_SLIP_WALL = 11, ORC_BC_THERMAL_NOSLIP_WALL = 12, ORC_BC_SPONGE = 13 };
 
 /* One boundary zone, as DomainBoundary after CalculateLocalExtent
  * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index
@@ -59,6 +59,9 @@ typedef struct {
   double t;
   int tn[12];
   double *ttimes[12], *tfield[12];
+  /* per sponge zone the interior grid coordinates along its dimension and its bounds
+   * there (boundary.inp xmin, xmax) */
+  double *sx[12], sxmin[12], sxmax[12];
 } orc_problem;
 
 /* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
@@ -87,6 +90,9 @@ void orc_set_zone_data(orc_problem *p, int z, const double *data);
 int orc_set_zone_temperature(orc_problem *p, int z, int n, const double *times, const double *field);
 /* The time of orc_apply_bc and orc_rhs and the start time of orc_rk. */
 void orc_set_time(orc_problem *p, double t);
+/* Sponge zones: the interior grid coordinates along zone z's dimension (dim[dim] values)
+ * and the zone's bounds there, boundary.inp's xmin and xmax of that dimension. */
+int orc_set_zone_sponge(orc_problem *p, int z, const double *x, double xmin, double xmax);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

@@ -159,7 +159,22 @@ CASES = {
                                                             perturb=0.05), speed=0.3), {
         (2, 1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, 0.1, 1.0 / 1.4]),
         (2, -1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, -0.1, 1.0 / 1.4])}),
+    # sponge zones: a relaxation source over boxes of interior points (two overlapping
+    # in the 2-D deck), beside periodic and extrapolate faces
+    "sod64_comp_roe_sponge": lambda: _sponge(C.sod(64, n_iter=20, dt=1e-3), [
+        (0, -1, [(0.75, 1.5)], [0.2, 0.1, 0.3])]),
+    "vortex24_char_roe_sponge_ssprk3": lambda: _sponge(C.vortex(24, n_iter=5, dt=0.02, scheme="ssprk3"), [
+        (0, -1, [(6.0, 9.6), (-1.0, 11.0)], [1.1, 0.4, 0.05, 2.7]),
+        (1, 1, [(-1.0, 11.0), (0.0, 2.5)], [0.9, 0.55, -0.05, 2.5])]),
+    "tgv12_comp_roe_sponge_rk4": lambda: _sponge(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), [
+        (2, 1, [(-1.0, 7.0), (-1.0, 7.0), (0.0, 2.0)], [1.05, 0.1, 0.0, -0.1, 1.9])]),
 }
+
+
+def _sponge(case, sponges):
+    """The deck with sponge zones [(dim, face, box per dim, reference state)]."""
+    case.sponges = sponges
+    return case
 
 
 def _thermal(case, kind, vel, dim=2):
