@@ -42,7 +42,7 @@ EXPORTS = [
     "gb_solver_set_gravity_field", "gb_solver_conservation_begin", "gb_solver_conservation_error",
     "gb_ensemble_conservation_begin", "gb_ensemble_conservation_error", "gb_ensemble_error",
     "gb_solver_set_hooks", "gb_inputs_zone_temperature", "gb_solver_set_zone_temperature",
-    "gb_inputs_zone_sponge", "gb_solver_set_zone_sponge",
+    "gb_inputs_zone_sponge", "gb_solver_set_zone_sponge", "gb_inputs_zone_inflow", "gb_solver_set_zone_inflow",
 ]
 
 
@@ -165,6 +165,8 @@ def lib():
     L.gb_solver_set_zone_temperature.argtypes = [VP, ctypes.c_int, ctypes.c_int, DP, DP]
     L.gb_inputs_zone_sponge.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(DP)]
     L.gb_solver_set_zone_sponge.argtypes = [VP, ctypes.c_int, DP]
+    L.gb_inputs_zone_inflow.argtypes = [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(DP)]
+    L.gb_solver_set_zone_inflow.argtypes = [VP, ctypes.c_int, ctypes.c_int, DP]
     L.gb_solver_cfl.argtypes = [VP, DP]
     L.gb_solver_step_report.argtypes = [VP, ctypes.c_int, DP, DP]
     L.gb_solver_error.argtypes = [VP, VP, ctypes.c_int, ctypes.c_int, DP]

@@ -56,7 +56,10 @@ class Case:
     # faces not listed take `bc`.  Thermal walls add a third item, the wall
     # temperature (times, field): field has the face's size per transverse dimension
     # and len(times) along the wall's own dimension, dimension 0 fastest (the
-    # reference's temperature file layout, written beside the deck by `write`)
+    # reference's temperature file layout, written beside the deck by `write`).
+    # turbulent-supersonic-inflow adds (n, data): n slices along the zone's dimension,
+    # the grid across, nvars values per point, dimension 0 fastest (the reference's
+    # inflow data file layout, also written by `write`)
     bcs: Optional[dict] = None
     # sponge zones after the face zones: [(dim, face, [(xmin, xmax) per dim], [nvars values])],
     # the state the sponge relaxes to over the box xmin..xmax (BCSponge.c)
@@ -152,6 +155,8 @@ class Case:
                 items = ext + [repr(float(v)) for v in vals]
                 if bctype.startswith("thermal-"):
                     items.append(self.temperature_file(d, face))
+                if bctype == "turbulent-supersonic-inflow":
+                    items.append(self.inflow_file(d, face))
                 rows.append(f"{bctype} {d} {face} " + " ".join(items))
         for d, face, box, vals in (self.sponges or []):
             items = [repr(float(v)) for lohi in box for v in lohi] + [repr(float(v)) for v in vals]
@@ -161,6 +166,21 @@ class Case:
     @staticmethod
     def temperature_file(d: int, face: int) -> str:
         return f"temperature_{d}_{'lo' if face == 1 else 'hi'}.bin"
+
+    @staticmethod
+    def inflow_file(d: int, face: int) -> str:
+        return f"inflow_{d}_{'lo' if face == 1 else 'hi'}.bin"
+
+    def inflow_bytes(self, d: int, face: int) -> bytes:
+        """A turbulent inflow face's data in the reference's binary format
+        (BCReadTurbulentInflowData, src/BoundaryConditions/BCIO.c:19-139, one rank): int
+        rank[ndims], int size[ndims], double data[nvars * prod(size)]."""
+        n, data = self.bcs[(d, face)][2]
+        size = [int(n) if e == d else self.size[e] for e in range(self.ndims)]
+        data = np.asarray(data, np.float64).reshape(-1)
+        assert data.size == self.nvars * int(np.prod(size)), (data.size, size)
+        rank = np.zeros(self.ndims, np.int32)
+        return rank.tobytes() + np.asarray(size, np.int32).tobytes() + data.tobytes()
 
     def temperature_bytes(self, d: int, face: int) -> bytes:
         """The wall temperature of a thermal-wall face in the reference's binary format
@@ -195,6 +215,9 @@ class Case:
             if spec[0].startswith("thermal-"):
                 with open(os.path.join(directory, self.temperature_file(d, face)), "wb") as f:
                     f.write(self.temperature_bytes(d, face))
+            if spec[0] == "turbulent-supersonic-inflow":
+                with open(os.path.join(directory, self.inflow_file(d, face)), "wb") as f:
+                    f.write(self.inflow_bytes(d, face))
         return directory
 
 

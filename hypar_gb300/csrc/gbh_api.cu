@@ -178,6 +178,23 @@ static int apply_mem_bcs(gb_solver* s, double* u, bool all, double t) {
         it = tn - 1;
         while (it > 0 && s->ttimes[z][it] > t) it--;
         tf = s->d_tfield[z];
+      } else if (type == GB_BC_TURBULENT_INFLOW) {
+        if (!s->d_tfield[z]) {
+          gbh_set_error("boundary zone %d is a turbulent inflow: call gb_solver_set_zone_inflow first", z);
+          return GB_ERR_ARG;
+        }
+        // the slice the mean flow has carried in by time t, over a period of 2 pi
+        // (BCTurbulentSupersonicInflow.c:44-48)
+        tn = s->fn[z];
+        const double xt = s->cfg.zone_data[z][1 + s->cfg.zones[z][1]] * t;
+        const double L = 2.0 * (4.0 * atan(1.0));
+        const double pos = (xt / L) * ((double)tn);
+        if (!(pos > -1.0 && pos < 2147483648.0)) {  // int(pos) >= 0 and representable
+          gbh_set_error("turbulent inflow zone %d: slice position %g at t = %g is outside the data", z, pos, t);
+          return GB_ERR_ARG;
+        }
+        it = ((int)pos) % tn;
+        tf = s->d_tfield[z];
       }
       if (pr < 0) pr = prof_begin(s, GB_PROF_BC);
       CK(launch_bc_zone_t(u, s->G, s->cfg.nvars, s->cfg.zones[z], s->cfg.zone_data[z], s->cfg.gamma, tf, tn, it,
@@ -208,6 +225,28 @@ extern "C" int gb_solver_set_zone_temperature(gb_solver* s, int zone, int ntimes
   CK(cudaMalloc((void**)&s->d_tfield[zone], n * sizeof(double)));
   CK(cudaMemcpy(s->d_tfield[zone], field, n * sizeof(double), cudaMemcpyHostToDevice));
   s->ttimes[zone].assign(times, times + ntimes);
+  return GB_OK;
+}
+
+extern "C" int gb_solver_set_zone_inflow(gb_solver* s, int zone, int n, const double* data) {
+  if (!s || zone < 0 || zone >= s->cfg.nzones || n < 1 || !data) {
+    gbh_set_error("gb_solver_set_zone_inflow: bad argument");
+    return GB_ERR_ARG;
+  }
+  const int* q = s->cfg.zones[zone];
+  if (q[0] != GB_BC_TURBULENT_INFLOW) {
+    gbh_set_error("gb_solver_set_zone_inflow: zone %d is not a turbulent inflow", zone);
+    return GB_ERR_ARG;
+  }
+  size_t cnt = (size_t)n * s->cfg.nvars;
+  for (int d = 0; d < s->cfg.ndims; d++)
+    if (d != q[1]) cnt *= (size_t)s->cfg.dim[d];
+  cudaFree(s->d_tfield[zone]);
+  s->d_tfield[zone] = nullptr;
+  s->fn[zone] = 0;
+  CK(cudaMalloc((void**)&s->d_tfield[zone], cnt * sizeof(double)));
+  CK(cudaMemcpy(s->d_tfield[zone], data, cnt * sizeof(double), cudaMemcpyHostToDevice));
+  s->fn[zone] = n;
   return GB_OK;
 }
 
@@ -338,7 +377,7 @@ int gbh_validate(const gb_config* c) {
   if (c->nzones < 0 || c->nzones > GB_MAX_ZONES) { gbh_set_error("bad nzones"); return GB_ERR_ARG; }
   for (int z = 0; z < c->nzones; z++) {
     const int* q = c->zones[z];
-    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_SPONGE || q[1] < 0 || q[1] >= nd ||
+    if (q[0] < GB_BC_PERIODIC || q[0] > GB_BC_REFLECT || q[1] < 0 || q[1] >= nd ||
         (q[2] != 1 && q[2] != -1)) {
       gbh_set_error("bad zone %d", z);
       return GB_ERR_ARG;
@@ -353,13 +392,25 @@ int gbh_validate(const gb_config* c) {
       if (!empty && !inside) { gbh_set_error("sponge zone %d must cover interior points only", z); return GB_ERR_ARG; }
       continue;
     }
-    if (q[0] > GB_BC_DIRICHLET && nd < 2) {
+    if (q[0] > GB_BC_DIRICHLET && q[0] != GB_BC_REFLECT && nd < 2) {
       gbh_set_error("zone %d: wall / inflow / outflow boundaries need Euler2D or NavierStokes3D", z);
       return GB_ERR_UNSUPPORTED;
     }
     if ((q[0] == GB_BC_THERMAL_SLIP_WALL || q[0] == GB_BC_THERMAL_NOSLIP_WALL) && c->model != GB_MODEL_NS3D) {
       gbh_set_error("zone %d: thermal walls need NavierStokes3D", z);
       return GB_ERR_UNSUPPORTED;
+    }
+    if (q[0] == GB_BC_TURBULENT_INFLOW) {
+      if (c->model != GB_MODEL_NS3D) {
+        gbh_set_error("zone %d: turbulent inflow needs NavierStokes3D", z);
+        return GB_ERR_UNSUPPORTED;
+      }
+      // the inflow data spans the grid across the zone's dimension
+      for (int d = 0; d < nd; d++)
+        if (d != q[1] && q[6 + d] > q[3 + d] && (q[3 + d] < 0 || q[6 + d] > c->dim[d])) {
+          gbh_set_error("zone %d: a turbulent inflow's transverse extent must lie within the grid", z);
+          return GB_ERR_ARG;
+        }
     }
     for (int d = 0; d < nd; d++) {
       int lo = -c->ghosts, hi = c->dim[d] + c->ghosts;

@@ -38,6 +38,9 @@ struct gb_inputs {
   /* sponge zones: per zone sigma along the zone's dimension, or NULL */
   int sn[GB_MAX_ZONES];
   double *sigma[GB_MAX_ZONES];
+  /* turbulent inflow zones: per zone the number of slices and the inflow data, or NULL */
+  int fn[GB_MAX_ZONES];
+  double *fdata[GB_MAX_ZONES];
   char op_overwrite[64];
   char op_format[64];
 };
@@ -437,8 +440,19 @@ void gb_inputs_free(gb_inputs *in) {
     free(in->ttimes[z]);
     free(in->tfield[z]);
     free(in->sigma[z]);
+    free(in->fdata[z]);
   }
   free(in);
+}
+
+int gb_inputs_zone_inflow(const gb_inputs *in, int zone, int *n, const double **data) {
+  if (!in || !n || !data || zone < 0 || zone >= GB_MAX_ZONES) {
+    gbh_set_error("gb_inputs_zone_inflow: bad argument");
+    return GB_ERR_ARG;
+  }
+  *n = in->fn[zone];
+  *data = in->fdata[zone];
+  return GB_OK;
 }
 
 int gb_inputs_zone_sponge(const gb_inputs *in, int zone, int *n, const double **sigma) {
@@ -496,6 +510,45 @@ static int read_temperature(const char *dir, const char *name, const gb_config *
       fread(res->tfield[z], sizeof(double), total, f) != (size_t)total) {
     fclose(f);
     gbh_set_error("temperature file %s: truncated", name);
+    return GB_ERR_INPUT;
+  }
+  fclose(f);
+  return GB_OK;
+}
+
+/* The inflow data file of a turbulent supersonic inflow zone (BCReadTurbulentInflowData,
+ * src/BoundaryConditions/BCIO.c:19-139, one rank): int rank[ndims] (all 0), int
+ * size[ndims] (size[dim]: the number of slices; the other sizes: the grid's), then
+ * nvars doubles per point, dimension 0 fastest. */
+static int read_inflow(const char *dir, const char *name, const gb_config *c, const int *zone, gb_inputs *res,
+                       int z) {
+  FILE *f = open_in(dir, name, "rb");
+  if (!f) {
+    gbh_set_error("boundary.inp zone %d: cannot open the inflow data file %s", z, name);
+    return GB_ERR_INPUT;
+  }
+  const int nd = c->ndims, dim = zone[1];
+  int rank[3] = {0, 0, 0}, size[3] = {1, 1, 1};
+  int bad = fread(rank, sizeof(int), nd, f) != (size_t)nd || fread(size, sizeof(int), nd, f) != (size_t)nd;
+  long total = c->nvars;
+  for (int d = 0; d < nd && !bad; d++) {
+    if (size[d] < 1) bad = 1;
+    else if (rank[d] != 0) bad = 3;
+    else if (d != dim && size[d] != c->dim[d]) bad = 2;
+    total *= size[d];
+  }
+  if (bad) {
+    fclose(f);
+    gbh_set_error("inflow data file %s: %s", name,
+                  bad == 2 ? "its size does not match the grid" : bad == 3 ? "data of a rank other than 0"
+                                                                        : "malformed header");
+    return GB_ERR_INPUT;
+  }
+  res->fn[z] = size[dim];
+  res->fdata[z] = (double *)malloc(sizeof(double) * total);
+  if (!res->fdata[z] || fread(res->fdata[z], sizeof(double), total, f) != (size_t)total) {
+    fclose(f);
+    gbh_set_error("inflow data file %s: truncated", name);
     return GB_ERR_INPUT;
   }
   fclose(f);
@@ -834,7 +887,9 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
           {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT, -4},
           {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL, -2},
           {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL, -2},
-          {"sponge", GB_BC_SPONGE, -1}};
+          {"sponge", GB_BC_SPONGE, -1},
+          {"turbulent-supersonic-inflow", GB_BC_TURBULENT_INFLOW, -4},
+          {"reflect", GB_BC_REFLECT, 0}};
       int tcode = 0, nvals = 0;
       for (size_t t = 0; t < sizeof(bct) / sizeof(bct[0]); t++)
         if (!strcmp(type, bct[t].name)) {
@@ -853,24 +908,25 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
       for (int k = 0; k < nvals && !bad; k++) bad = fscanf(in, "%lf", &c.zone_data[z][k]) != 1;
       /* thermal walls: then the name of the wall temperature file (InitializeBoundaries.c:180-187) */
       const int thermal = tcode == GB_BC_THERMAL_SLIP_WALL || tcode == GB_BC_THERMAL_NOSLIP_WALL;
+      const int turbulent = tcode == GB_BC_TURBULENT_INFLOW;
       char tname[MAXS] = "";
-      if (!bad && thermal) bad = fscanf(in, "%511s", tname) != 1;
+      if (!bad && (thermal || turbulent)) bad = fscanf(in, "%511s", tname) != 1;
       if (bad) {
         fclose(in);
         gb_inputs_free(res);
         gbh_set_error("boundary.inp: zone %d (%s) lacks its values", z, type);
         return GB_ERR_INPUT;
       }
-      if (tcode > GB_BC_DIRICHLET && tcode != GB_BC_SPONGE && c.ndims < 2) {
+      if (tcode > GB_BC_DIRICHLET && tcode != GB_BC_SPONGE && tcode != GB_BC_REFLECT && c.ndims < 2) {
         fclose(in);
         gb_inputs_free(res);
         gbh_set_error("boundary type %s needs Euler2D or NavierStokes3D", type);
         return GB_ERR_UNSUPPORTED;
       }
-      if (thermal && c.model != GB_MODEL_NS3D) {
+      if ((thermal || turbulent) && c.model != GB_MODEL_NS3D) {
         fclose(in);
         gb_inputs_free(res);
-        gbh_set_error("boundary type %s needs NavierStokes3D (BCThermal*WallU have 3-D branches only)", type);
+        gbh_set_error("boundary type %s needs NavierStokes3D (the reference's branch is 3-D only)", type);
         return GB_ERR_UNSUPPORTED;
       }
       int *zz = c.zones[z];
@@ -911,6 +967,14 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
             const double xk = res->x[xo + zz[3 + dim] + k];
             res->sigma[z][k] = face > 0 ? (xk - xs) / (xe - xs) : (xk - xe) / (xs - xe);
           }
+        }
+      }
+      if (turbulent) {
+        int rc = read_inflow(dir, tname, &c, zz, res, z);
+        if (rc) {
+          fclose(in);
+          gb_inputs_free(res);
+          return rc;
         }
       }
       if (thermal) {

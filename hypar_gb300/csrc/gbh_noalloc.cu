@@ -107,6 +107,10 @@ extern "C" int gb_rhs_explicit_noalloc(const gb_config* cfg, const double* dxinv
       gbh_set_error("gb_rhs_explicit_noalloc: thermal walls need the temperature field of a gb_solver; "
                     "use gb_RHSFunctionExplicit");
       return GB_ERR_UNSUPPORTED;
+    } else if (c.zones[z][0] == GB_BC_TURBULENT_INFLOW) {
+      gbh_set_error("gb_rhs_explicit_noalloc: turbulent inflow needs the inflow data of a gb_solver; "
+                    "use gb_RHSFunctionExplicit");
+      return GB_ERR_UNSUPPORTED;
     } else if (c.zones[z][0] == GB_BC_SPONGE) {
       gbh_set_error("gb_rhs_explicit_noalloc: sponge zones need the sigma of a gb_solver; use gb_RHSFunctionExplicit");
       return GB_ERR_UNSUPPORTED;

@@ -234,6 +234,11 @@ int gb_run_case(const char *dir, int device, int verbose) {
     const double *sg = NULL;
     if (!rc) rc = gb_inputs_zone_sponge(in, z, &ns, &sg);
     if (!rc && ns) rc = gb_solver_set_zone_sponge(s, z, sg);
+    /* turbulent inflow zones: the inflow data read with the deck */
+    int nf = 0;
+    const double *fd = NULL;
+    if (!rc) rc = gb_inputs_zone_inflow(in, z, &nf, &fd);
+    if (!rc && nf) rc = gb_solver_set_zone_inflow(s, z, nf, fd);
   }
   /* InitialSolution.c:118: the volume integral of the initial solution */
   if (!rc && c->cons_check) rc = gb_solver_conservation_begin(s);

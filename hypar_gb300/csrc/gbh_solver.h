@@ -56,6 +56,8 @@ struct gb_solver {
   double* d_tfield[GB_MAX_ZONES] = {};
   // sponge zones: sigma along the zone's dimension (device), and whether any zone is one
   double* d_sigma[GB_MAX_ZONES] = {};
+  // turbulent inflow zones: the number of slices of the inflow data (held in d_tfield)
+  int fn[GB_MAX_ZONES] = {};
   bool sponge = false;
   int iter = 0;            // steps taken since the state was set (PostStep's iteration index)
   long long dx_off[3] = {0, 0, 0};

@@ -212,7 +212,8 @@ struct ZoneDev {
   int type, dim, face, is[3], ie[3];
   double data[8];
   double gamma;
-  // thermal walls: the wall temperature field (all time levels) and the level in use
+  // thermal walls: the wall temperature field (all time levels) and the level in use;
+  // turbulent inflow: the inflow data (all slices), their number and the slice in use
   const double* tfield;
   int tn, it;
 };
@@ -223,12 +224,12 @@ struct ZoneDev {
 // branches), in their operation order without contraction.
 template <int ND>
 __device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, double* out, bool inflow = false,
-                                         double Tb = 0.0) {
+                                         double Tb = 0.0, const double* fluct = nullptr) {
   constexpr int NV = ND + 2;
   const double gm1 = z.gamma - 1.0;
   const double inv_gm1 = __ddiv_rn(1.0, gm1);
   double rho = 0.0, vel[3] = {0.0, 0.0, 0.0}, P = 0.0;
-  if (z.type != GB_BC_SUPERSONIC_INFLOW) {
+  if (z.type != GB_BC_SUPERSONIC_INFLOW && z.type != GB_BC_TURBULENT_INFLOW) {
     rho = w[0];
     for (int d = 0; d < ND; d++) vel[d] = (ND == 3 && rho == 0.0) ? 0.0 : __ddiv_rn(w[1 + d], rho);
     double vsq = __dadd_rn(__dmul_rn(vel[0], vel[0]), __dmul_rn(vel[1], vel[1]));
@@ -261,6 +262,13 @@ __device__ __forceinline__ void bc_ghost(const ZoneDev& z, const double* w, doub
       // BCThermalNoslipWall.c:86-105: every velocity component mirrored
       for (int d = 0; d < ND; d++) vg[d] = __dsub_rn(__dmul_rn(2.0, z.data[d]), vel[d]);
       Pg = __dmul_rn(rg, Tb);
+      break;
+    case GB_BC_TURBULENT_INFLOW:
+      // BCTurbulentSupersonicInflow.c:54-85: the supersonic inflow state with the data's
+      // velocity fluctuations added
+      rg = z.data[0];
+      for (int d = 0; d < ND; d++) vg[d] = __dadd_rn(z.data[1 + d], fluct[d]);
+      Pg = z.data[1 + ND];
       break;
     case GB_BC_SUBSONIC_AMBIVALENT:
       // BCSubsonicAmbivalent.c:105-117: inflow's rule (density, velocity given) or
@@ -303,6 +311,8 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
   }
   if (z.type == GB_BC_PERIODIC || z.type == GB_BC_EXTRAPOLATE) {
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = u[p2 * nv + v];
+  } else if (z.type == GB_BC_REFLECT) {
+    for (int v = 0; v < nv; v++) u[p1 * nv + v] = -u[p2 * nv + v];
   } else if (z.type == GB_BC_DIRICHLET) {
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = z.data[v];
   } else {
@@ -338,9 +348,20 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
       }
       Tb = z.tfield[q];
     }
+    const double* fl = nullptr;
+    if (z.type == GB_BC_TURBULENT_INFLOW) {
+      // the slice in use along dim, the zone-relative indices across it (the data spans
+      // the grid across, BCTurbulentSupersonicInflow.c:66-72)
+      long long q = 0, stride = 1;
+      for (int d = 0; d < G.nd; d++) {
+        q += stride * (d == dd ? z.it : ib[d]);
+        stride *= (d == dd ? z.tn : G.dim[d]);
+      }
+      fl = z.tfield + q * nv + 1;
+    }
     double g[5];
-    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow, Tb);
-    else bc_ghost<3>(z, u + p2 * nv, g, inflow, Tb);
+    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow, Tb, fl);
+    else bc_ghost<3>(z, u + p2 * nv, g, inflow, Tb, fl);
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = g[v];
   }
 }
@@ -362,8 +383,9 @@ cudaError_t launch_bc_zone_t(double* u, const DevGeom& G, int nv, const int* zon
   z.tfield = tfield;
   z.tn = tn;
   z.it = it;
-  if ((zone9[0] == GB_BC_THERMAL_SLIP_WALL || zone9[0] == GB_BC_THERMAL_NOSLIP_WALL) && (!tfield || tn < 1))
-    return cudaErrorInvalidValue;  // a thermal wall without its temperature field
+  if ((zone9[0] == GB_BC_THERMAL_SLIP_WALL || zone9[0] == GB_BC_THERMAL_NOSLIP_WALL ||
+       zone9[0] == GB_BC_TURBULENT_INFLOW) && (!tfield || tn < 1 || it < 0 || it >= tn))
+    return cudaErrorInvalidValue;  // a thermal wall or turbulent inflow without its field
   z.type = zone9[0];
   z.dim = zone9[1];
   z.face = zone9[2];

@@ -153,7 +153,8 @@ int gbshim_config(void *s, gb_config *c) {
         {"subsonic-outflow", GB_BC_SUBSONIC_OUTFLOW}, {"supersonic-inflow", GB_BC_SUPERSONIC_INFLOW},
         {"supersonic-outflow", GB_BC_SUPERSONIC_OUTFLOW}, {"subsonic-ambivalent", GB_BC_SUBSONIC_AMBIVALENT},
         {"thermal-slip-wall", GB_BC_THERMAL_SLIP_WALL}, {"thermal-noslip-wall", GB_BC_THERMAL_NOSLIP_WALL},
-        {"sponge", GB_BC_SPONGE}};
+        {"sponge", GB_BC_SPONGE}, {"turbulent-supersonic-inflow", GB_BC_TURBULENT_INFLOW},
+        {"reflect", GB_BC_REFLECT}};
     int code = 0;
     for (size_t t = 0; t < sizeof(types) / sizeof(types[0]); t++)
       if (!strcmp(B->bctype, types[t].name)) code = types[t].code;
@@ -190,6 +191,7 @@ int gbshim_config(void *s, gb_config *c) {
         break;
       case GB_BC_SUPERSONIC_INFLOW:
       case GB_BC_SUBSONIC_AMBIVALENT:
+      case GB_BC_TURBULENT_INFLOW:
         v[0] = B->FlowDensity;
         for (int k = 0; k < nd; k++) v[1 + k] = B->FlowVelocity[k];
         v[1 + nd] = B->FlowPressure;
@@ -309,6 +311,17 @@ int gbshim_attach(void *s, void *mpi) {
     if (c.zones[z][0] != GB_BC_THERMAL_SLIP_WALL && c.zones[z][0] != GB_BC_THERMAL_NOSLIP_WALL) continue;
     rc = gb_solver_set_zone_temperature(gb, z, B->UnsteadyTemperatureSize[B->dim], B->UnsteadyTimeLevels,
                                         B->UnsteadyTemperatureData);
+    if (rc) {
+      fprintf(stderr, "gbhypar: %s\n", gb_last_error());
+      gb_solver_destroy(gb);
+      return rc;
+    }
+  }
+  /* turbulent inflow zones: the inflow data HyPar read (BCReadTurbulentInflowData) */
+  for (int z = 0; z < c.nzones; z++) {
+    const DomainBoundary *B = &((const DomainBoundary *)solver->boundary)[z];
+    if (c.zones[z][0] != GB_BC_TURBULENT_INFLOW || !B->UnsteadyDirichletData) continue;
+    rc = gb_solver_set_zone_inflow(gb, z, B->UnsteadyDirichletSize[B->dim], B->UnsteadyDirichletData);
     if (rc) {
       fprintf(stderr, "gbhypar: %s\n", gb_last_error());
       gb_solver_destroy(gb);

@@ -69,6 +69,17 @@ class Inputs:
             check(lib().gb_inputs_zone_sponge(h, z, ctypes.byref(n), ctypes.byref(sp)))
             if n.value:
                 self.zone_sponge[z] = np.ctypeslib.as_array(sp, shape=(n.value,)).copy()
+        # turbulent inflow zones: per zone (slices, data), nvars values per point
+        self.zone_inflow = {}
+        for z in range(c.nzones):
+            n, dp = ctypes.c_int(), _lib.DP()
+            check(lib().gb_inputs_zone_inflow(h, z, ctypes.byref(n), ctypes.byref(dp)))
+            if n.value:
+                cnt = n.value * c.nvars
+                for d in range(nd):
+                    if d != c.zones[z][1]:
+                        cnt *= dims[d]
+                self.zone_inflow[z] = (n.value, np.ctypeslib.as_array(dp, shape=(cnt,)).copy())
         lib().gb_inputs_free(h)
         self._h = None
 
@@ -103,6 +114,8 @@ class Solver:
             s.set_zone_temperature(z, times, field)
         for z, sigma in inp.zone_sponge.items():
             s.set_zone_sponge(z, sigma)
+        for z, (n, data) in inp.zone_inflow.items():
+            s.set_zone_inflow(z, n, data)
         return s
 
     def set_zone_temperature(self, zone: int, times, field):
@@ -112,6 +125,12 @@ class Solver:
         field = np.ascontiguousarray(field, dtype=np.float64).reshape(-1)
         check(lib().gb_solver_set_zone_temperature(self._h, int(zone), len(times), times.ctypes.data_as(_lib.DP),
                                                    field.ctypes.data_as(_lib.DP)))
+
+    def set_zone_inflow(self, zone: int, n: int, data):
+        """A turbulent inflow's data: n slices along the zone's dimension, the grid across,
+        nvars values per point, dimension 0 fastest."""
+        data = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        check(lib().gb_solver_set_zone_inflow(self._h, int(zone), int(n), data.ctypes.data_as(_lib.DP)))
 
     def set_zone_sponge(self, zone: int, sigma):
         """A sponge zone's sigma, one value per index of the zone along its dimension."""

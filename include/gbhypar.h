@@ -52,11 +52,16 @@ enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
  * edge to 1 at its outer one along the zone's dimension (BCSponge.c:34-61); its extent is
  * an interior index range in every dimension (CalculateLocalExtent,
  * InitializeBoundaries.c:382-393) and sigma comes through gb_inputs_zone_sponge /
- * gb_solver_set_zone_sponge. */
+ * gb_solver_set_zone_sponge.  turbulent-supersonic-inflow (NavierStokes3D): the supersonic
+ * inflow state with velocity fluctuations added, taken from a slice of inflow data that
+ * advances with the mean flow (BCTurbulentSupersonicInflow.c); the data comes through
+ * gb_inputs_zone_inflow / gb_solver_set_zone_inflow.  reflect (every model): the ghost
+ * points take the negated mirror interior values, every component (BCReflect.c:22-44). */
 enum { GB_BC_PERIODIC = 1, GB_BC_EXTRAPOLATE = 2, GB_BC_DIRICHLET = 3, GB_BC_SLIP_WALL = 4,
        GB_BC_NOSLIP_WALL = 5, GB_BC_SUBSONIC_INFLOW = 6, GB_BC_SUBSONIC_OUTFLOW = 7,
        GB_BC_SUPERSONIC_INFLOW = 8, GB_BC_SUPERSONIC_OUTFLOW = 9, GB_BC_SUBSONIC_AMBIVALENT = 10,
-       GB_BC_THERMAL_SLIP_WALL = 11, GB_BC_THERMAL_NOSLIP_WALL = 12, GB_BC_SPONGE = 13 };
+       GB_BC_THERMAL_SLIP_WALL = 11, GB_BC_THERMAL_NOSLIP_WALL = 12, GB_BC_SPONGE = 13,
+       GB_BC_TURBULENT_INFLOW = 14, GB_BC_REFLECT = 15 };
 enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
 /* WENO5 nonlinear weights (weno.inp: yc > borges > mapped > Jiang-Shu, and
  * no_limiting = 1 keeps the optimal weights; WENOFifthOrderCalculateWeights.c:40-64). */
@@ -93,8 +98,8 @@ typedef struct gb_config {
   int write_residual;       /* solver.inp write_residual: residual.out with the norms */
   /* per zone, the values boundary.inp gives after the extents: dirichlet: nvars values;
    * slip-wall / noslip-wall: wall velocity (ndims); subsonic-inflow: rho, velocity;
-   * subsonic-outflow: pressure; supersonic-inflow and subsonic-ambivalent: rho, velocity,
-   * pressure; thermal-slip-wall / thermal-noslip-wall: wall velocity (the temperature
+   * subsonic-outflow: pressure; supersonic-inflow, subsonic-ambivalent and
+   * turbulent-supersonic-inflow: rho, velocity, pressure; thermal-slip-wall / thermal-noslip-wall: wall velocity (the temperature
    * comes through gb_inputs_zone_temperature / gb_solver_set_zone_temperature); sponge:
    * the nvars values of the state it relaxes to */
   double zone_data[GB_MAX_ZONES][8];
@@ -154,6 +159,12 @@ int gb_inputs_zone_temperature(const gb_inputs *in, int zone, int *ntimes, const
  * the zone's bounds as boundary.inp gives them (BCSponge.c:49-54); n = 0 and NULL for
  * other zones.  The array belongs to `in`. */
 int gb_inputs_zone_sponge(const gb_inputs *in, int zone, int *n, const double **sigma);
+/* Turbulent supersonic inflow zones: the inflow data file of boundary zone `zone`
+ * (BCReadTurbulentInflowData, src/BoundaryConditions/BCIO.c:19-139, one rank): n slices
+ * along the zone's dimension, the grid's size along the others, nvars values per point
+ * (components 1..3 are the velocity fluctuations), dimension 0 fastest; n = 0 and NULL
+ * for other zones.  The array belongs to `in`. */
+int gb_inputs_zone_inflow(const gb_inputs *in, int zone, int *n, const double **data);
 /* Ensemble decks (simulation.inp "nsims", one "size" per simulation in
  * solver.inp, initial_<k>.inp and boundary_<k>.inp or boundary.inp; index k
  * zero-padded to (int)log10(nsims)+1 digits, src/Simulation/InitialSolution.c:36-41):
@@ -189,6 +200,14 @@ int gb_solver_set_zone_temperature(gb_solver *s, int zone, int ntimes, const dou
  * evaluating a right-hand side of such a configuration.  The sponge term joins the
  * source term of every right-hand side (SourceFunction.c:50-76). */
 int gb_solver_set_zone_sponge(gb_solver *s, int zone, const double *sigma);
+/* Turbulent supersonic inflow zones: upload the inflow data of boundary zone `zone` (host
+ * array laid out as gb_inputs_zone_inflow gives it, n slices).  At time t the ghost
+ * points take slice int(u_dim t / (2 pi) * n) mod n (BCTurbulentSupersonicInflow.c:44-48);
+ * a time at which that index is negative (inflow velocity against the zone's dimension)
+ * is refused with GB_ERR_ARG, where the reference would read outside its data.  The
+ * zone's transverse extent must lie within the grid.  Required before stepping such a
+ * configuration. */
+int gb_solver_set_zone_inflow(gb_solver *s, int zone, int n, const double *data);
 /* Wait for all work queued by the solver. */
 int gb_solver_sync(gb_solver *s);
 /* Copy a solution in or out (layout GB_LAYOUT_*, memory GB_MEM_*). */

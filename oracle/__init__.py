@@ -36,7 +36,8 @@ INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,
           "subsonic-inflow": 6, "subsonic-outflow": 7, "supersonic-inflow": 8, "supersonic-outflow": 9,
-          "subsonic-ambivalent": 10, "thermal-slip-wall": 11, "thermal-noslip-wall": 12, "sponge": 13}
+          "subsonic-ambivalent": 10, "thermal-slip-wall": 11, "thermal-noslip-wall": 12, "sponge": 13,
+          "turbulent-supersonic-inflow": 14, "reflect": 15}
 
 
 SCHEMES = {"weno5": 0, "crweno5": 1}
@@ -47,7 +48,8 @@ def bc_nvalues(bctype: str, ndims: int, nvars: int) -> int:
     return {"dirichlet": nvars, "slip-wall": ndims, "noslip-wall": ndims, "subsonic-inflow": 1 + ndims,
             "subsonic-outflow": 1, "supersonic-inflow": 2 + ndims,
             "subsonic-ambivalent": 2 + ndims, "thermal-slip-wall": ndims,
-            "thermal-noslip-wall": ndims, "sponge": nvars}.get(bctype, 0)
+            "thermal-noslip-wall": ndims, "sponge": nvars,
+            "turbulent-supersonic-inflow": 2 + ndims}.get(bctype, 0)
 
 _lib = None
 
@@ -86,6 +88,8 @@ def _bind(path):
     L.orc_set_time.restype = None
     L.orc_set_zone_sponge.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, ctypes.c_double, ctypes.c_double]
     L.orc_set_zone_sponge.restype = ctypes.c_int
+    L.orc_set_zone_inflow.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
+    L.orc_set_zone_inflow.restype = ctypes.c_int
     L.orc_set_gravity.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double]
@@ -214,8 +218,8 @@ def parse_boundary_inp(text: str, ndims: int, nvars: int = 0):
         nvals = bc_nvalues(bctype, ndims, nvars)
         vals = [float(t) for t in tok[k:k + nvals]]
         k += nvals
-        if bctype.startswith("thermal-"):
-            k += 1  # the temperature file's name
+        if bctype.startswith("thermal-") or bctype == "turbulent-supersonic-inflow":
+            k += 1  # the temperature or inflow data file's name
         rows.append((bctype, dim, face, ext, vals))
     return rows
 
@@ -286,6 +290,11 @@ class Problem:
                 field = np.ascontiguousarray(field, np.float64).reshape(-1)
                 if L.orc_set_zone_temperature(self.h, z, len(times), _dp(times), _dp(field)):
                     raise RuntimeError("orc_set_zone_temperature failed")
+            if row[0] == "turbulent-supersonic-inflow":
+                n, data = case.bcs[(row[1], row[2])][2]
+                data = np.ascontiguousarray(data, np.float64).reshape(-1)
+                if L.orc_set_zone_inflow(self.h, z, int(n), _dp(data)):
+                    raise RuntimeError("orc_set_zone_inflow failed")
             if row[0] == "sponge":
                 dim = row[1]
                 if L.orc_set_zone_sponge(self.h, z, _dp(np.ascontiguousarray(xs[dim])), float(row[3][dim][0]),

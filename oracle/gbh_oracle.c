@@ -228,6 +228,18 @@ int orc_set_zone_temperature(orc_problem *p, int z, int n, const double *times, 
 
 void orc_set_time(orc_problem *p, double t) { p->t = t; }
 
+int orc_set_zone_inflow(orc_problem *p, int z, int n, const double *data) {
+  if (z < 0 || z >= p->nzones || p->zones[z].type != ORC_BC_TURBULENT_INFLOW || n < 1) return 1;
+  long cnt = (long)n * p->nvars;
+  for (int d = 0; d < p->ndims; d++)
+    if (d != p->zones[z].dim) cnt *= p->dim[d];
+  free(p->fdata[z]);
+  p->fdata[z] = (double *)malloc(sizeof(double) * cnt);
+  memcpy(p->fdata[z], data, sizeof(double) * cnt);
+  p->fn[z] = n;
+  return 0;
+}
+
 int orc_set_zone_sponge(orc_problem *p, int z, const double *x, double xmin, double xmax) {
   if (z < 0 || z >= p->nzones || p->zones[z].type != ORC_BC_SPONGE) return 1;
   const int n = p->dim[p->zones[z].dim];
@@ -283,6 +295,7 @@ void orc_problem_destroy(orc_problem *p) {
     free(p->ttimes[z]);
     free(p->tfield[z]);
     free(p->sx[z]);
+    free(p->fdata[z]);
   }
   free(p->gf);
   free(p->gg);
@@ -413,6 +426,16 @@ static int apply_bc_at(const orc_problem *p, double *u, double t) {
       it = p->tn[z] - 1;
       while (p->ttimes[z][it] > t && it > 0) it--;
     }
+    if (b->type == ORC_BC_TURBULENT_INFLOW) {
+      /* BCTurbulentSupersonicInflow.c:44-48: the slice the mean flow carried in by t,
+       * the data spanning a length of 2 pi */
+      if (!p->fn[z] || nd != 3) return 1;
+      double xt = b->data[1 + b->dim] * t;
+      int N = p->fn[z];
+      double L = 2.0 * (4.0 * atan(1.0));
+      it = ((int)((xt / L) * ((double)N))) % N;
+      if (it < 0) return 1; /* the reference would read outside its data */
+    }
     for (long c = 0; c < count; c++) {
       long r = c;
       for (int d = 0; d < nd; d++) { ib[d] = (int)(r % bounds[d]); r /= bounds[d]; }
@@ -430,9 +453,37 @@ static int apply_bc_at(const orc_problem *p, double *u, double t) {
       long p1 = pidx(p, s, ig), p2 = pidx(p, s, isrc);
       if (b->type == ORC_BC_PERIODIC || b->type == ORC_BC_EXTRAPOLATE) {
         for (int v = 0; v < nv; v++) u[nv * p1 + v] = u[nv * p2 + v];
+      } else if (b->type == ORC_BC_REFLECT) {
+        /* BCReflectU (BCReflect.c:22-44): the mirror point scaled by -1 */
+        for (int v = 0; v < nv; v++) u[nv * p1 + v] = -1.0 * u[nv * p2 + v];
       } else if (b->type == ORC_BC_DIRICHLET) {
         /* BCDirichletU (BCDirichlet.c:27-41) */
         for (int v = 0; v < nv; v++) u[nv * p1 + v] = b->data[v];
+      } else if (b->type == ORC_BC_TURBULENT_INFLOW) {
+        /* BCTurbulentSupersonicInflowU (BCTurbulentSupersonicInflow.c:54-85): the mean
+         * supersonic inflow plus the velocity fluctuations of slice `it` at the zone-
+         * relative transverse indices */
+        int index1[3] = {ib[0], ib[1], ib[2]};
+        index1[dd] = it;
+        long q = 0, stride = 1;
+        for (int d = 0; d < nd; d++) {
+          q += stride * index1[d];
+          stride *= (d == dd ? p->fn[z] : p->dim[d]);
+        }
+        const double *fl = p->fdata[z] + q * nv;
+        double inv_gamma_m1 = 1.0 / (p->gamma - 1.0);
+        double rho_gpt = b->data[0], pressure_gpt = b->data[4];
+        double uvel_gpt = b->data[1], vvel_gpt = b->data[2], wvel_gpt = b->data[3];
+        uvel_gpt += fl[1];
+        vvel_gpt += fl[2];
+        wvel_gpt += fl[3];
+        double energy_gpt = inv_gamma_m1 * pressure_gpt +
+                            0.5 * rho_gpt * (uvel_gpt * uvel_gpt + vvel_gpt * vvel_gpt + wvel_gpt * wvel_gpt);
+        u[nv * p1 + 0] = rho_gpt;
+        u[nv * p1 + 1] = rho_gpt * uvel_gpt;
+        u[nv * p1 + 2] = rho_gpt * vvel_gpt;
+        u[nv * p1 + 3] = rho_gpt * wvel_gpt;
+        u[nv * p1 + 4] = energy_gpt;
       } else if (nd == 2 || nd == 3) {
         int inflow = 0;
         if (b->type == ORC_BC_SUBSONIC_AMBIVALENT) {

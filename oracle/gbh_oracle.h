@@ -25,7 +25,8 @@ enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
 enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
        ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,
        ORC_BC_SUPERSONIC_INFLOW = 8, ORC_BC_SUPERSONIC_OUTFLOW = 9, ORC_BC_SUBSONIC_AMBIVALENT = 10,
-       ORC_BC_THERMAL_SLIP_WALL = 11, ORC_BC_THERMAL_NOSLIP_WALL = 12, ORC_BC_SPONGE = 13 };
+       ORC_BC_THERMAL_SLIP_WALL = 11, ORC_BC_THERMAL_NOSLIP_WALL = 12, ORC_BC_SPONGE = 13,
+       ORC_BC_TURBULENT_INFLOW = 14, ORC_BC_REFLECT = 15 };
 
 /* One boundary zone, as DomainBoundary after CalculateLocalExtent
  * (src/Simulation/InitializeBoundaries.c:365-420): the slab covers index
@@ -62,6 +63,9 @@ typedef struct {
   /* per sponge zone the interior grid coordinates along its dimension and its bounds
    * there (boundary.inp xmin, xmax) */
   double *sx[12], sxmin[12], sxmax[12];
+  /* per turbulent inflow zone the number of slices and the inflow data */
+  int fn[12];
+  double *fdata[12];
 } orc_problem;
 
 /* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
@@ -93,6 +97,9 @@ void orc_set_time(orc_problem *p, double t);
 /* Sponge zones: the interior grid coordinates along zone z's dimension (dim[dim] values)
  * and the zone's bounds there, boundary.inp's xmin and xmax of that dimension. */
 int orc_set_zone_sponge(orc_problem *p, int z, const double *x, double xmin, double xmax);
+/* Turbulent inflow zones: n slices of inflow data (the grid's size across the zone's
+ * dimension, n along it, nvars values per point, dimension 0 fastest). */
+int orc_set_zone_inflow(orc_problem *p, int z, int n, const double *data);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

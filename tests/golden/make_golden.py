@@ -168,7 +168,32 @@ CASES = {
         (1, 1, [(-1.0, 11.0), (0.0, 2.5)], [0.9, 0.55, -0.05, 2.5])]),
     "tgv12_comp_roe_sponge_rk4": lambda: _sponge(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), [
         (2, 1, [(-1.0, 7.0), (-1.0, 7.0), (0.0, 2.0)], [1.05, 0.1, 0.0, -0.1, 1.9])]),
+    # turbulent supersonic inflow (NavierStokes3D): a supersonic mean inflow with velocity
+    # fluctuations from inflow data whose slice advances with the mean flow (slice 0 to 1
+    # inside the run), supersonic outflow opposite
+    "tgv12_comp_llf_turbulent_inflow_rk4": lambda: _turb(C.tgv(12, n_iter=3, dt=0.02, upwinding="llf-char",
+                                                                perturb=0.05)),
+    "tgv12_char_rusanov_turbulent_inflow_ssprk3": lambda: _turb(C.tgv(12, n_iter=3, dt=0.02,
+                                                                       interp="characteristic",
+                                                                       upwinding="rusanov", scheme="ssprk3",
+                                                                       perturb=0.05), dim=1),
 }
+
+
+def _turb(case, dim=0, nslices=64, speed=2.0, seed=17):
+    """Turbulent supersonic inflow on the low face along `dim` (mean velocity `speed`
+    along it), supersonic outflow on the high face; random fluctuations of 0.05."""
+    rng = np.random.default_rng(seed)
+    size = [nslices if e == dim else case.size[e] for e in range(3)]
+    data = np.zeros((size[2], size[1], size[0], case.nvars))
+    data[..., 0] = 1.0 + 0.1 * rng.standard_normal(data.shape[:3])
+    data[..., 1:4] = 0.05 * rng.standard_normal(data.shape[:3] + (3,))
+    data[..., 4] = 2.0 + 0.1 * rng.standard_normal(data.shape[:3])
+    vel = [0.0, 0.0, 0.0]
+    vel[dim] = speed
+    case.bcs = {(dim, 1): ("turbulent-supersonic-inflow", [1.0] + vel + [1.0 / 1.4], (nslices, data.reshape(-1))),
+                (dim, -1): ("supersonic-outflow", [])}
+    return case
 
 
 def _sponge(case, sponges):

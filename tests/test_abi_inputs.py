@@ -83,7 +83,7 @@ def test_reader_errors(built_lib, tmp_path):
     case = C.vortex(12, n_iter=1, dt=0.01)
     d = tmp_path / "b"
     case.write(str(d))
-    t = open(d / "boundary.inp").read().replace("periodic", "turbulent-supersonic-inflow", 1)
+    t = open(d / "boundary.inp").read().replace("periodic", "numa-nfbc", 1)
     open(d / "boundary.inp", "w").write(t)
     _expect(4, str(d))
     d = tmp_path / "c"
