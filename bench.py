@@ -64,9 +64,9 @@ FP64_PER_CELL_STEP = {
 # DRAM bytes (read + write) per cell of one launch (x launch / y launch with the RK
 # update), per kernel form: the segment walker from a 2048^2 capture of the
 # centre-relative kernels (traffic proportional to cells at these sizes), the tile form
-# from a capture of the default 1024^2 run.
+# from a capture of the default 1024^2 run (the 34 MB state partly stays in L2 there).
 DRAM_BYTES_PER_CELL = {"vortex": {("hyp_x", "walker"): 57.32, ("hyp_y", "walker"): 153.39,
-                                  ("hyp_y", "tile"): 112.57}}
+                                  ("hyp_x", "tile"): 32.35, ("hyp_y", "tile"): 110.18}}
 TRAFFIC_SOURCE = {"walker": "a 2048^2 capture of the segment-walker form, scaled by cells",
                   "tile": "a 1024^2 capture of the tile form"}
 
