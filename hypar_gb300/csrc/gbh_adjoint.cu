@@ -131,109 +131,6 @@ __device__ __forceinline__ void weno5_pair_vjp(const double* w, const double* v,
   weno5_pair_vjp_impl<false>(w, v, eps4, gL, gR, wb, vb, nullptr);
 }
 
-// The pair's reverse in two parts, for kernels in which neighbouring interfaces share
-// smoothness terms.  The three terms B of a side belong to one cell: the left side of
-// interface I (cells I-3 .. I+1 of its window w0..w4) takes those of cell I-1 (w2), the
-// right side those of cell I (w3), in the order (stencil ending at the cell, centred on
-// it, starting at it) = (BL1, BL2, BL3) and (BR3, BR2, BR1).  So the right triple of
-// interface I is the left triple of interface I+1, and the reverse of a triple through
-// its second differences and first-difference terms into the window can run once for
-// both interfaces, on the sum of their adjoints.
-//
-// Part 1: from the adjoints gL, gR of the two outputs to the adjoints of the two
-// triples (tL = (BL1, BL2, BL3)-bar, tR = (BR3, BR2, BR1)-bar, each per cell in the order
-// above) and the value stencil's adjoint (added into vb).
-template <bool TP>
-__device__ __forceinline__ void weno5_pair_vjp_weights(const double* w, const double* v, double eps4, double gL,
-                                                       double gR, double* vb, const double* tp, double* tL,
-                                                       double* tR) {
-  double BL1, BL2, BL3, BR1, BR2, BR3, rL, rR;
-  if (TP) {
-    BL1 = tp[0];
-    BL2 = tp[1];
-    BL3 = tp[2];
-    BR1 = tp[3];
-    BR2 = tp[4];
-    BR3 = tp[5];
-    rL = tp[6];
-    rR = tp[7];
-  } else {
-    const double k13 = 13.0 / 3.0;
-    double d1 = fma(-2.0, w[1], w[0]) + w[2];
-    double d2 = fma(-2.0, w[2], w[1]) + w[3];
-    double d3 = fma(-2.0, w[3], w[2]) + w[4];
-    double d4 = fma(-2.0, w[4], w[3]) + w[5];
-    double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
-    double gL2 = w[1] - w[3];
-    double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
-    double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
-    double gR2 = w[4] - w[2];
-    double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
-    BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
-    BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
-    BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
-    BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
-    BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
-    BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
-  }
-  double qL1 = BL1 * BL1, qL2 = BL2 * BL2, qL3 = BL3 * BL3;
-  double qR1 = BR1 * BR1, qR2 = BR2 * BR2, qR3 = BR3 * BR3;
-  double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;
-  double aR1 = qR2 * qR3, aR2 = qR1 * qR3, aR3 = qR1 * qR2;
-  if (!TP) {
-    rL = nr_rcp(fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1)));
-    rR = nr_rcp(fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1)));
-  }
-  double cL1 = fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
-  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3]));
-  double cA = fma(5.0, v[2], fma(2.0, v[3], -v[1]));
-  double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4]));
-  double nL6 = 6.0 * gL * rL, nL3 = 3.0 * gL * rL, nR6 = 6.0 * gR * rR, nR3 = 3.0 * gR * rR;
-  double nLb = gL * rL, nRb = gR * rR;
-  // the normalisation's adjoint of each side: -g out r with out = n r
-  double DLb = -nLb * rL * fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
-  double DRb = -nRb * rR * fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
-  double aL1b = fma(nLb, cL1, 6.0 * DLb), aL2b = fma(nL6, cA, 36.0 * DLb), aL3b = fma(nL3, cB, 18.0 * DLb);
-  double aR1b = fma(nRb, cR1, 6.0 * DRb), aR2b = fma(nR6, cB, 36.0 * DRb), aR3b = fma(nR3, cA, 18.0 * DRb);
-  double cL1b = nLb * aL1, cR1b = nRb * aR1;
-  double cAb = fma(nL6, aL2, nR3 * aR3);
-  double cBb = fma(nL3, aL3, nR6 * aR2);
-  // B-bar = 2 B q-bar, q-bar from the products a
-  tL[0] = 2.0 * BL1 * fma(aL2b, qL3, aL3b * qL2);
-  tL[1] = 2.0 * BL2 * fma(aL1b, qL3, aL3b * qL1);
-  tL[2] = 2.0 * BL3 * fma(aL1b, qL2, aL2b * qL1);
-  tR[2] = 2.0 * BR1 * fma(aR2b, qR3, aR3b * qR2);
-  tR[1] = 2.0 * BR2 * fma(aR1b, qR3, aR3b * qR1);
-  tR[0] = 2.0 * BR3 * fma(aR1b, qR2, aR2b * qR1);
-  vb[0] = fma(2.0, cL1b, vb[0]);
-  vb[1] += fma(-7.0, cL1b, -cAb);
-  vb[2] += fma(11.0, cL1b, fma(5.0, cAb, 2.0 * cBb));
-  vb[3] += fma(11.0, cR1b, fma(2.0, cAb, 5.0 * cBb));
-  vb[4] += fma(-7.0, cR1b, -cBb);
-  vb[5] = fma(2.0, cR1b, vb[5]);
-}
-
-// Part 2: the reverse of one cell's triple of smoothness terms (x: the five cells
-// around it, t: the triple's adjoint in the order of part 1) into the cells' adjoints.
-// B = 13/3 d^2 + g^2 + 4 eps with d the second difference and g the term of the
-// stencil: (x0 - 4 x1 + 3 x2), (x1 - x3), (3 x2 - 4 x3 + x4).
-__device__ __forceinline__ void weno5_triple_vjp(const double* x, const double* t, double* xb) {
-  const double k26 = 26.0 / 3.0;
-  const double da = fma(-2.0, x[1], x[0]) + x[2];
-  const double db = fma(-2.0, x[2], x[1]) + x[3];
-  const double dc = fma(-2.0, x[3], x[2]) + x[4];
-  const double ga = fma(3.0, x[2], fma(-4.0, x[1], x[0]));
-  const double gb = x[1] - x[3];
-  const double gc = fma(3.0, x[2], fma(-4.0, x[3], x[4]));
-  const double dab = k26 * da * t[0], dbb = k26 * db * t[1], dcb = k26 * dc * t[2];
-  const double gab = 2.0 * ga * t[0], gbb = 2.0 * gb * t[1], gcb = 2.0 * gc * t[2];
-  xb[0] += dab + gab;
-  xb[1] += fma(-2.0, dab, dbb) + fma(-4.0, gab, gbb);
-  xb[2] += (dab + fma(-2.0, dbb, dcb)) + 3.0 * (gab + gcb);
-  xb[3] += fma(-2.0, dcb, dbb) + fma(-4.0, gcb, -gbb);
-  xb[4] += dcb + gcb;
-}
-
 // ---------------------------------------------------------------------------
 // Reverse of the Euler2D cell flux along D: u_bar += (df/du)^T f_bar.
 // ---------------------------------------------------------------------------
@@ -645,8 +542,6 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
   __syncthreads();
   const int t = threadIdx.x;
   const int I = I0 + t;
-  // the lanes of this warp with an interface (a prefix of the warp)
-  const unsigned act = __ballot_sync(0xffffffffu, I <= N);
   if (I <= N) {
     // rhs_c = -dxinv_c (F_{c+1/2} - F_{c-1/2}): interface I feeds cells I-1 (-) and I (+)
     double Fb[NV2] = {0.0, 0.0, 0.0, 0.0};
@@ -682,14 +577,6 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
     }
     double uLb[NV2] = {0.0, 0.0, 0.0, 0.0}, uRb[NV2] = {0.0, 0.0, 0.0, 0.0};
     roe_vjp<D>(uL, uR, Fb, uLb, uRb, pp);
-    // The smoothness-term triple of cell I (this interface's right side) is the left
-    // side's of interface I+1, the next lane: that lane's adjoint of it comes over a
-    // shuffle and the triple is reversed once, here.  The first lane of a warp also
-    // reverses its own left triple (its left neighbour is in another warp or tile); the
-    // last active lane reverses its right triple alone (interface I+1 does the same
-    // with its left one).
-    const int lane = threadIdx.x & 31;
-    const bool has_next = lane < 31 && ((act >> (lane + 1)) & 1u);
 #pragma unroll
     for (int v = 0; v < NV2; v++) {
       double wf6[6], wu6[6], gf[6] = {0, 0, 0, 0, 0, 0}, gu[6] = {0, 0, 0, 0, 0, 0};
@@ -698,25 +585,12 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
         wf6[p] = sf[t + p][v];
         wu6[p] = su[t + p][v];
       }
-      double tLf[3], tRf[3], tLu[3], tRu[3];
-      weno5_pair_vjp_weights<WT>(wf6, wf6, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, WT ? tp + 8 + v * 16 : nullptr,
-                                 tLf, tRf);
-      weno5_pair_vjp_weights<WT>(wu6, wu6, eps4, uLb[v], uRb[v], gu, WT ? tp + 16 + v * 16 : nullptr, tLu,
-                                 tRu);
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        const double nf = __shfl_down_sync(act, tLf[k], 1);
-        const double nu = __shfl_down_sync(act, tLu[k], 1);
-        if (has_next) {
-          tRf[k] += nf;
-          tRu[k] += nu;
-        }
-      }
-      weno5_triple_vjp(wf6 + 1, tRf, gf + 1);
-      weno5_triple_vjp(wu6 + 1, tRu, gu + 1);
-      if (lane == 0) {
-        weno5_triple_vjp(wf6, tLf, gf);
-        weno5_triple_vjp(wu6, tLu, gu);
+      if (WT) {
+        weno5_pair_vjp_impl<true>(wf6, wf6, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf, tp + 8 + v * 16);
+        weno5_pair_vjp_impl<true>(wu6, wu6, eps4, uLb[v], uRb[v], gu, gu, tp + 16 + v * 16);
+      } else {
+        weno5_pair_vjp(wf6, wf6, eps4, 0.5 * Fb[v], 0.5 * Fb[v], gf, gf);
+        weno5_pair_vjp(wu6, wu6, eps4, uLb[v], uRb[v], gu, gu);
       }
 #pragma unroll
       for (int p = 0; p < 6; p++) {
@@ -749,13 +623,8 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
   }
 }
 
-// Blocks per SM the tile reverse is compiled for (registers capped at 64K / (TI x this)).
-#ifndef GBH_VJP_TILE_MINB
-#define GBH_VJP_TILE_MINB 1
-#endif
-
 template <bool WT, int TI>
-__global__ void __launch_bounds__(TI, GBH_VJP_TILE_MINB)
+__global__ void __launch_bounds__(TI)
 rhs_vjp_tile_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
                     const double* __restrict__ dx1, DevGeom G, PhysParams pp, int nt0, int nt1,
                     const double* __restrict__ tape0, const double* __restrict__ tape1) {
