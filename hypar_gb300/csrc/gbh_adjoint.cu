@@ -510,10 +510,10 @@ struct VjpTileSmem {
 };
 
 template <int D, bool WT, int TI>
-__device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const AdjTerms& kt, double* Ub,
-                                         const double* __restrict__ dxinv, const DevGeom& G, const PhysParams& pp,
-                                         long long tr, int tile, const double* __restrict__ tape,
-                                         VjpTileSmem<TI>& sm) {
+__device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const AdjTerms& kt, double* __restrict__ slot,
+                                         int ntile, const double* __restrict__ dxinv, const DevGeom& G,
+                                         const PhysParams& pp, long long tr, int tile,
+                                         const double* __restrict__ tape, VjpTileSmem<TI>& sm) {
   constexpr int T = 1 - D, NCELL = TI + 5;
   auto& su = sm.su;
   auto& sf = sm.sf;
@@ -617,27 +617,60 @@ __device__ __forceinline__ void vjp_tile(const double* __restrict__ U, const Adj
 #pragma unroll
     for (int v = 0; v < NV2; v++) uu[v] = su[c][v];
     flux_vjp<D>(uu, fb, ab, pp);
-    double* dst = Ub + (pbase + (long long)fold2(i, N, lo, hi) * sd) * NV2;
+    // this tile's share of the cell, summed with the other tiles' by vjp_slot_gather_kernel
+    double* dst = slot + (((long long)tr * ntile + tile) * NCELL + c) * NV2;
 #pragma unroll
-    for (int v = 0; v < NV2; v++) atomicAdd(dst + v, ab[v]);
+    for (int v = 0; v < NV2; v++) dst[v] = ab[v];
   }
 }
 
 template <bool WT, int TI>
 __global__ void __launch_bounds__(TI)
-rhs_vjp_tile_kernel(const double* __restrict__ U, AdjTerms kt, double* Ub, const double* __restrict__ dx0,
-                    const double* __restrict__ dx1, DevGeom G, PhysParams pp, int nt0, int nt1,
-                    const double* __restrict__ tape0, const double* __restrict__ tape1) {
+rhs_vjp_tile_kernel(const double* __restrict__ U, AdjTerms kt, double* __restrict__ slot0,
+                    double* __restrict__ slot1, const double* __restrict__ dx0, const double* __restrict__ dx1,
+                    DevGeom G, PhysParams pp, int nt0, int nt1, const double* __restrict__ tape0,
+                    const double* __restrict__ tape1) {
   __shared__ VjpTileSmem<TI> sm;
   const long long b = blockIdx.x;
   const long long n0 = (long long)G.dim[1] * nt0;
   if (b < n0) {
-    vjp_tile<0, WT, TI>(U, kt, Ub, dx0, G, pp, b % G.dim[1], (int)(b / G.dim[1]), tape0, sm);
+    vjp_tile<0, WT, TI>(U, kt, slot0, nt0, dx0, G, pp, b % G.dim[1], (int)(b / G.dim[1]), tape0, sm);
   } else {
     const long long t = b - n0;
-    vjp_tile<1, WT, TI>(U, kt, Ub, dx1, G, pp, t % G.dim[0], (int)(t / G.dim[0]), tape1, sm);
+    vjp_tile<1, WT, TI>(U, kt, slot1, nt1, dx1, G, pp, t % G.dim[0], (int)(t / G.dim[0]), tape1, sm);
   }
 }
+
+// The tile reverse's cells summed in a fixed order, so that repeated gradients are
+// bit-identical.  Along direction D, interior cell i of a line receives the shares of
+// every tile whose window holds one of its images: i itself and, through the folded
+// boundaries, the ghost cell that copies it (periodic: i - N, i + N; mirror: -1 - i,
+// 2N - 1 - i).  Tile T's window is cells T TI - 3 .. T TI + TI + 1 (at most N + 2).
+template <int TI>
+__device__ __forceinline__ void slot_sum(const double* __restrict__ slot, long long line, int ntile, int i, int N,
+                                         int lo, int hi, double* acc) {
+  constexpr int NCELL = TI + 5;
+  int img[3] = {i, INT_MIN, INT_MIN};
+  if (lo == FOLD_PERIODIC && i >= N - 3) img[1] = i - N;
+  if (lo == FOLD_MIRROR && i <= 2) img[1] = -1 - i;
+  if (hi == FOLD_PERIODIC && i <= 2) img[2] = i + N;
+  if (hi == FOLD_MIRROR && i >= N - 3) img[2] = 2 * N - 1 - i;
+#pragma unroll
+  for (int m = 0; m < 3; m++) {
+    const int ip = img[m];
+    if (ip == INT_MIN || ip < -3 || ip > N + 2) continue;
+    // tiles T with T TI - 3 <= ip <= T TI + TI + 1
+    const int tmax = min(ntile - 1, (ip + 3) / TI);
+    for (int T = max(0, (ip - TI - 1 + TI - 1) / TI); T <= tmax; T++) {
+      const int c = ip - T * TI + 3;
+      if (c < 0 || c >= NCELL) continue;
+      const double* src = slot + ((line * ntile + T) * NCELL + c) * NV2;
+#pragma unroll
+      for (int v = 0; v < NV2; v++) acc[v] += src[v];
+    }
+  }
+}
+
 
 // Both directions in one launch (they only add into Ub): threads
 // [0, n0) walk x-lines, [n0, n0 + n1) y-lines.
@@ -846,6 +879,20 @@ __device__ __forceinline__ bool interior_offset(const DevGeom& G, long long p, l
   return true;
 }
 
+template <int TI>
+__global__ void vjp_slot_gather_kernel(double* Ub, const double* __restrict__ slot0, const double* __restrict__ slot1,
+                                       DevGeom G, int nt0, int nt1) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long q;
+  if (!interior_offset(G, p, q)) return;
+  const int i = (int)(p % G.dim[0]), j = (int)(p / G.dim[0]);
+  double ax[NV2] = {0.0, 0.0, 0.0, 0.0}, ay[NV2] = {0.0, 0.0, 0.0, 0.0};
+  slot_sum<TI>(slot0, j, nt0, i, G.dim[0], G.bclo[0], G.bchi[0], ax);  // x-line j
+  slot_sum<TI>(slot1, i, nt1, j, G.dim[1], G.bclo[1], G.bchi[1], ay);  // y-line i
+#pragma unroll
+  for (int v = 0; v < NV2; v++) Ub[q + v] += ax[v] + ay[v];
+}
+
 // out = base + sum_j c_j X_j at interior points (out may be base).
 __global__ void lincomb_kernel(double* out, const double* base, AdjTerms t, DevGeom G) {
   long long q;
@@ -920,6 +967,8 @@ struct gb_adjoint {
   double* H = nullptr;            // x-direction hyperbolic term of the fused step
   double* Ub[4] = {nullptr, nullptr, nullptr, nullptr};
   double* ubar = nullptr;
+  // the tile reverse's per-tile cell shares, x and y (sized for tiles of 32 or 64)
+  double* slot[2] = {nullptr, nullptr};
   // tangent-linear model arrays (allocated on first use)
   double* tblock = nullptr;
   double *tu = nullptr, *tdu = nullptr, *tU = nullptr, *tdU = nullptr, *tK[4] = {}, *tdK[4] = {};
@@ -971,12 +1020,17 @@ static int adj_vjp(gb_adjoint* a, const double* U, const AdjTerms& kt, double* U
     const double* t1 = tape ? tape[1] : nullptr;
     const double* dx0 = a->d_dxinv + a->dx_off[0];
     const double* dx1 = a->d_dxinv + a->dx_off[1];
+    double *s0 = a->slot[0], *s1 = a->slot[1];
     if (ti == 32) {
-      if (wide) rhs_vjp_tile_kernel<true, 32><<<nblk, 32, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
-      else rhs_vjp_tile_kernel<false, 32><<<nblk, 32, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      if (wide) rhs_vjp_tile_kernel<true, 32><<<nblk, 32, 0, a->stream>>>(U, kt, s0, s1, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      else rhs_vjp_tile_kernel<false, 32><<<nblk, 32, 0, a->stream>>>(U, kt, s0, s1, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      AK(cudaGetLastError());
+      vjp_slot_gather_kernel<32><<<interior_grid(a), 256, 0, a->stream>>>(Ub, s0, s1, G, nt0, nt1);
     } else {
-      if (wide) rhs_vjp_tile_kernel<true, 64><<<nblk, 64, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
-      else rhs_vjp_tile_kernel<false, 64><<<nblk, 64, 0, a->stream>>>(U, kt, Ub, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      if (wide) rhs_vjp_tile_kernel<true, 64><<<nblk, 64, 0, a->stream>>>(U, kt, s0, s1, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      else rhs_vjp_tile_kernel<false, 64><<<nblk, 64, 0, a->stream>>>(U, kt, s0, s1, dx0, dx1, G, a->pp, nt0, nt1, t0, t1);
+      AK(cudaGetLastError());
+      vjp_slot_gather_kernel<64><<<interior_grid(a), 256, 0, a->stream>>>(Ub, s0, s1, G, nt0, nt1);
     }
     AK(cudaGetLastError());
     return GB_OK;
@@ -1166,8 +1220,17 @@ extern "C" int gb_adjoint_create_ex(const gb_config* cfg, const double* dxinv, i
   const size_t tape_y = (size_t)cfg->dim[0] * (cfg->dim[1] + 1) * a->tape_w;
   const size_t tape_bytes = (size_t)a->nbuf * a->seglen * ns * (tape_x + tape_y) * sizeof(double);
   a->bytes += tape_bytes;
-  cudaError_t e = cudaMalloc((void**)&a->block, a->bytes - tape_bytes);
-  if (e == cudaSuccess) e = cudaMemset(a->block, 0, a->bytes - tape_bytes);
+  const size_t block_bytes = a->bytes - tape_bytes;
+  cudaError_t e = cudaMalloc((void**)&a->block, block_bytes);
+  if (e == cudaSuccess) e = cudaMemset(a->block, 0, block_bytes);
+  // tile shares: per line, tiles x (TI + 5) cells x 4, the larger of tiles of 32 and 64
+  for (int d = 0; d < 2 && e == cudaSuccess; d++) {
+    const long long n = a->G.dim[d] + 1, lines = a->G.dim[1 - d];
+    const long long c32 = (n + 31) / 32 * 37, c64 = (n + 63) / 64 * 69;
+    const size_t sb = (size_t)(lines * (c32 > c64 ? c32 : c64) * NV2) * sizeof(double);
+    e = cudaMalloc((void**)&a->slot[d], sb);
+    a->bytes += sb;
+  }
   if (e == cudaSuccess) e = cudaMalloc((void**)&a->tblock2, tape_bytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&a->d_dxinv, ndx * sizeof(double));
   if (e == cudaSuccess) e = cudaMemcpy(a->d_dxinv, dxinv, ndx * sizeof(double), cudaMemcpyHostToDevice);
@@ -1230,6 +1293,8 @@ extern "C" void gb_adjoint_destroy(gb_adjoint* a) {
   if (a->ev_start) cudaEventDestroy(a->ev_start);
   if (a->aux) cudaStreamDestroy(a->aux);
   cudaFree(a->block);
+  cudaFree(a->slot[0]);
+  cudaFree(a->slot[1]);
   cudaFree(a->tblock);
   cudaFree(a->tblock2);
   cudaFree(a->d_dxinv);

@@ -284,3 +284,26 @@ def test_tile_forms(built_lib, problem, tile):
         grads.append(a.interior(g).cpu().numpy())
         a.close()
     assert np.linalg.norm(grads[1] - grads[0]) / np.linalg.norm(grads[0]) <= 1e-11
+
+
+@pytest.mark.parametrize("tile", [32, 64])
+def test_tile_reverse_is_deterministic(built_lib, problem, tile):
+    """The tile form of the reverse kernel sums every cell's shares in a fixed order
+    (per-tile shares, then a gather), so repeated gradients are bit-identical, in one
+    adjoint object and across two."""
+    case, _, _ = problem
+    grads = []
+    for _ in range(2):
+        a = make(problem, ncheck=0)
+        a.set_launch(2, -tile)
+        a.set_launch(3, -tile)
+        u0 = state(a, case.u)
+        wt = rand_interior(a, 9)
+        for _ in range(2):
+            uT, g = a.empty(), a.empty()
+            a.forward(u0, uT)
+            a.backward(wt, g)
+            grads.append(a.interior(g).cpu().numpy())
+        a.close()
+    for g in grads[1:]:
+        assert np.array_equal(g, grads[0])
