@@ -9,7 +9,9 @@
 //    and the cell flux.  Each thread walks a segment of a grid line like the
 //    forward kernel, recomputing the forward values of each interface, and
 //    scatters the stencil adjoints with atomic adds (ghost cells fold onto the
-//    interior cells they copy).
+//    interior cells they copy).  Its tile form (rhs_vjp_tile_kernel, small grids)
+//    stores per-tile shares instead, summed in a fixed order by
+//    vjp_slot_gather_kernel: bit-identical results from run to run.
 //  * rhs_jvp_kernel: forward mode (du -> (F(u), dF/du du)) in dual numbers,
 //    written independently in the reference's own form (per-side Jiang-Shu
 //    weights, dense eigenvector matrices and R |Lambda| L of the Roe flux,
@@ -498,8 +500,10 @@ __device__ __forceinline__ void vjp_segment(const double* __restrict__ U, const 
 // at the walker's segment boundaries) and stores its six cells' stencil adjoints in
 // shared memory; after a barrier each cell sums the contributions of the interfaces
 // that touch it, in a fixed order (no shared-memory atomics, and the same sum on
-// every run), is finished (u_bar += a + (df/du)^T f_bar) and added atomically at its
-// folded index, as in the walker.
+// every run), is finished (u_bar += a + (df/du)^T f_bar) and stored as this tile's
+// share of the cell; vjp_slot_gather_kernel then adds the shares of all tiles and both
+// directions into u_bar in a fixed order, so the result does not depend on the order
+// in which blocks run.
 // Shared memory of the tile reverse (both directions use the same block of it): the
 // tile's cell states and fluxes, and per interface t the adjoints of its window cells
 // t .. t+5, of the flux (gf) and of the state (gu).
