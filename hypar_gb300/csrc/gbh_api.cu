@@ -560,6 +560,7 @@ extern "C" void gb_solver_destroy(gb_solver* s) {
     cudaFree(s->d_tfield[z]);
     cudaFree(s->d_sigma[z]);
   }
+  cudaFree(s->d_stage);
   cudaFree(s->d_H);
   cudaFree(s->d_crX);
   cudaFree(s->d_crC);
@@ -663,14 +664,14 @@ extern "C" int gb_solver_set_state(gb_solver* s, const double* u, int layout, in
     size_t nint = 1;
     for (int d = 0; d < s->cfg.ndims; d++) nint *= s->cfg.dim[d];
     const double* src = u;
-    double* tmp = nullptr;
     if (mem == GB_MEM_HOST) {
-      CK(cudaMallocAsync((void**)&tmp, nint * s->cfg.nvars * sizeof(double), s->stream));
-      CK(cudaMemcpyAsync(tmp, u, nint * s->cfg.nvars * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-      src = tmp;
+      // a kept staging array: allocating and freeing one per call made every call
+      // pay for the memory pool's trimming at the next synchronisation
+      if (!s->d_stage) CK(cudaMalloc((void**)&s->d_stage, nint * s->cfg.nvars * sizeof(double)));
+      CK(cudaMemcpyAsync(s->d_stage, u, nint * s->cfg.nvars * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+      src = s->d_stage;
     }
     CK(launch_pack(s->d_u, src, s->G, s->cfg.nvars, 0, s->stream));
-    if (tmp) CK(cudaFreeAsync(tmp, s->stream));
   }
   // every work array starts with the same ghost values as u
   CK(cudaMemcpyAsync(s->d_acc, s->d_u, bytes, cudaMemcpyDeviceToDevice, s->stream));
@@ -692,16 +693,12 @@ extern "C" int gb_solver_get_state(gb_solver* s, double* u, int layout, int mem)
     for (int d = 0; d < s->cfg.ndims; d++) nint *= s->cfg.dim[d];
     size_t ib = nint * s->cfg.nvars * sizeof(double);
     double* dst = u;
-    double* tmp = nullptr;
     if (mem == GB_MEM_HOST) {
-      CK(cudaMallocAsync((void**)&tmp, ib, s->stream));
-      dst = tmp;
+      if (!s->d_stage) CK(cudaMalloc((void**)&s->d_stage, ib));
+      dst = s->d_stage;
     }
     CK(launch_pack(dst, s->d_u, s->G, s->cfg.nvars, 1, s->stream));
-    if (tmp) {
-      CK(cudaMemcpyAsync(u, tmp, ib, cudaMemcpyDeviceToHost, s->stream));
-      CK(cudaFreeAsync(tmp, s->stream));
-    }
+    if (mem == GB_MEM_HOST) CK(cudaMemcpyAsync(u, s->d_stage, ib, cudaMemcpyDeviceToHost, s->stream));
   }
   CK(cudaStreamSynchronize(s->stream));
   return GB_OK;

@@ -56,6 +56,8 @@ struct gb_solver {
   double* d_tfield[GB_MAX_ZONES] = {};
   // sponge zones: sigma along the zone's dimension (device), and whether any zone is one
   double* d_sigma[GB_MAX_ZONES] = {};
+  // staging array for interior-layout host copies (allocated on first use, kept)
+  double* d_stage = nullptr;
   // turbulent inflow zones: the number of slices of the inflow data (held in d_tfield)
   int fn[GB_MAX_ZONES] = {};
   bool sponge = false;
