@@ -51,6 +51,10 @@ struct gb_ensemble {
   bool own_stream = false;
   std::vector<MemberDev> mem;
   std::vector<long long> nvals;  // values per member (with ghosts)
+  // staging array for interior-layout host copies of one member (the largest
+  // member's size; allocated on first use, kept)
+  double* d_stage = nullptr;
+  size_t stage_vals = 0;
   long long total_vals = 0, total_dx = 0;
   long long total_thr[3] = {0, 0, 0};
   int seg[3] = {32, 32, 32}, block[3] = {128, 128, 128};
@@ -285,6 +289,7 @@ extern "C" void gb_ensemble_destroy(gb_ensemble* e) {
   if (!e) return;
   if (e->gexec) cudaGraphExecDestroy(e->gexec);
   cudaFree(e->d_u);
+  cudaFree(e->d_stage);
   cudaFree(e->d_acc);
   for (int k = 0; k < 4; k++) cudaFree(e->d_P[k]);
   cudaFree(e->d_H);
@@ -322,6 +327,19 @@ extern "C" int gb_ensemble_sync(gb_ensemble* e) {
   return GB_OK;
 }
 
+// The kept staging array, grown to n values if needed.
+static cudaError_t stage_array(gb_ensemble* e, size_t n) {
+  if (e->d_stage && e->stage_vals >= n) return cudaSuccess;
+  cudaError_t ce = cudaStreamSynchronize(e->stream);
+  if (ce != cudaSuccess) return ce;
+  cudaFree(e->d_stage);
+  e->d_stage = nullptr;
+  e->stage_vals = 0;
+  ce = cudaMalloc((void**)&e->d_stage, n * sizeof(double));
+  if (ce == cudaSuccess) e->stage_vals = n;
+  return ce;
+}
+
 extern "C" int gb_ensemble_set_state(gb_ensemble* e, int m, const double* u, int layout, int mem) {
   if (!e || !u || m < 0 || m >= e->nm) { gbh_set_error("gb_ensemble_set_state: bad argument"); return GB_ERR_ARG; }
   const gb_config& c = e->cfg[m];
@@ -334,14 +352,12 @@ extern "C" int gb_ensemble_set_state(gb_ensemble* e, int m, const double* u, int
     size_t nint = c.nvars;
     for (int d = 0; d < c.ndims; d++) nint *= c.dim[d];
     const double* src = u;
-    double* tmp = nullptr;
     if (mem == GB_MEM_HOST) {
-      CK(cudaMallocAsync((void**)&tmp, nint * sizeof(double), e->stream));
-      CK(cudaMemcpyAsync(tmp, u, nint * sizeof(double), cudaMemcpyHostToDevice, e->stream));
-      src = tmp;
+      CK(stage_array(e, nint));
+      CK(cudaMemcpyAsync(e->d_stage, u, nint * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+      src = e->d_stage;
     }
     CK(launch_pack(dst, src, e->mem[m].G, c.nvars, 0, e->stream));
-    if (tmp) CK(cudaFreeAsync(tmp, e->stream));
   }
   CK(cudaMemcpyAsync(e->d_acc + e->mem[m].off, dst, bytes, cudaMemcpyDeviceToDevice, e->stream));
   for (int k = 1; k < e->base.rk_nstages; k++)
@@ -362,16 +378,12 @@ extern "C" int gb_ensemble_get_state(gb_ensemble* e, int m, double* u, int layou
     size_t nint = c.nvars;
     for (int d = 0; d < c.ndims; d++) nint *= c.dim[d];
     double* dst = u;
-    double* tmp = nullptr;
     if (mem == GB_MEM_HOST) {
-      CK(cudaMallocAsync((void**)&tmp, nint * sizeof(double), e->stream));
-      dst = tmp;
+      CK(stage_array(e, nint));
+      dst = e->d_stage;
     }
     CK(launch_pack(dst, src, e->mem[m].G, c.nvars, 1, e->stream));
-    if (tmp) {
-      CK(cudaMemcpyAsync(u, tmp, nint * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
-      CK(cudaFreeAsync(tmp, e->stream));
-    }
+    if (mem == GB_MEM_HOST) CK(cudaMemcpyAsync(u, e->d_stage, nint * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
   }
   CK(cudaStreamSynchronize(e->stream));
   return GB_OK;
