@@ -94,8 +94,13 @@ class Case:
             "  iproc             " + " ".join("1" for _ in self.size),
             "  ghost             3",
             f"  n_iter            {self.n_iter}",
-            "  time_scheme       rk",
-            f"  time_scheme_type  {self.time_scheme_type}",
+        ]
+        # "euler": forward Euler (time_scheme euler, HyPar's default), else an RK table
+        if self.time_scheme_type == "euler":
+            lines.append("  time_scheme       euler")
+        else:
+            lines += ["  time_scheme       rk", f"  time_scheme_type  {self.time_scheme_type}"]
+        lines += [
             f"  hyp_space_scheme  {self.hyp_scheme}",
             f"  hyp_interp_type   {self.interp}",
         ]

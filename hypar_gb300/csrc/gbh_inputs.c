@@ -675,11 +675,14 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     gbh_set_error("hyp_interp_type %s invalid", si.interp_type);
     return GB_ERR_INPUT;
   }
-  if (strcmp(si.time_scheme, "rk")) {
-    gbh_set_error("time_scheme %s not supported (rk only)", si.time_scheme);
+  /* forward Euler (solver.inp's default, TimeForwardEuler.c: u += dt RHS(u)) is the
+   * one-stage table: the same update, bit for bit (dt b_0 = dt) */
+  const int euler = !strcmp(si.time_scheme, "euler");
+  if (strcmp(si.time_scheme, "rk") && !euler) {
+    gbh_set_error("time_scheme %s not supported (rk and euler only)", si.time_scheme);
     return GB_ERR_UNSUPPORTED;
   }
-  rc = gb_rk_table(si.time_scheme_type, &c.rk_nstages, c.rk_A, c.rk_b, c.rk_c);
+  rc = gb_rk_table(euler ? "1fe" : si.time_scheme_type, &c.rk_nstages, c.rk_A, c.rk_b, c.rk_c);
   if (rc) return rc;
   c.dt = si.dt;
   c.n_iter = si.n_iter;

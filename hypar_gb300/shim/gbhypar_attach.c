@@ -201,15 +201,23 @@ int gbshim_config(void *s, gb_config *c) {
     }
   }
 
-  /* time integration: explicit Runge-Kutta only (solver->msti, TimeExplicitRKInitialize) */
-  if (strcmp(solver->time_scheme, "rk")) return unsupported("time_scheme", solver->time_scheme);
-  const ExplicitRKParameters *rk = (const ExplicitRKParameters *)solver->msti;
-  if (!rk || rk->nstages < 1 || rk->nstages > 4) return unsupported("time_scheme_type", solver->time_scheme_type);
-  c->rk_nstages = rk->nstages;
-  for (int i = 0; i < rk->nstages; i++) {
-    for (int j = 0; j < rk->nstages; j++) c->rk_A[4 * i + j] = rk->A[i * rk->nstages + j];
-    c->rk_b[i] = rk->b[i];
-    c->rk_c[i] = rk->c[i];
+  /* time integration: explicit Runge-Kutta (solver->msti, TimeExplicitRKInitialize), or
+   * forward Euler (TimeForwardEuler.c), which is the one-stage table */
+  if (!strcmp(solver->time_scheme, "euler")) {
+    c->rk_nstages = 1;
+    c->rk_A[0] = 0.0;
+    c->rk_b[0] = 1.0;
+    c->rk_c[0] = 0.0;
+  } else {
+    if (strcmp(solver->time_scheme, "rk")) return unsupported("time_scheme", solver->time_scheme);
+    const ExplicitRKParameters *rk = (const ExplicitRKParameters *)solver->msti;
+    if (!rk || rk->nstages < 1 || rk->nstages > 4) return unsupported("time_scheme_type", solver->time_scheme_type);
+    c->rk_nstages = rk->nstages;
+    for (int i = 0; i < rk->nstages; i++) {
+      for (int j = 0; j < rk->nstages; j++) c->rk_A[4 * i + j] = rk->A[i * rk->nstages + j];
+      c->rk_b[i] = rk->b[i];
+      c->rk_c[i] = rk->c[i];
+    }
   }
   c->dt = solver->dt;
   c->n_iter = solver->n_iter;

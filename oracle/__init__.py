@@ -248,6 +248,8 @@ RK_TABLES = {
     "44": (4, [0, 0, 0, 0, 0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1.0, 0],
            [1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0]),
     "ssprk3": (3, [0, 0, 0, 1.0, 0, 0, 0.25, 0.25, 0], [1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0]),
+    # time_scheme euler (TimeForwardEuler.c): u += dt RHS(u), the one-stage table
+    "euler": (1, [0.0], [1.0]),
 }
 """Butcher tables of TimeExplicitRKInitialize (src/TimeIntegration/TimeExplicitRKInitialize.c:28-80)."""
 

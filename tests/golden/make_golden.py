@@ -161,6 +161,9 @@ CASES = {
         (2, -1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, -0.1, 1.0 / 1.4])}),
     # sponge zones: a relaxation source over boxes of interior points (two overlapping
     # in the 2-D deck), beside periodic and extrapolate faces
+    # time_scheme euler (HyPar's default time integrator, TimeForwardEuler.c)
+    "sod64_comp_roe_euler": lambda: C.sod(64, n_iter=20, dt=1e-3, scheme="euler"),
+    "vortex24_char_llf_euler": lambda: C.vortex(24, n_iter=5, dt=0.01, upwinding="llf-char", scheme="euler"),
     "sod64_comp_roe_sponge": lambda: _sponge(C.sod(64, n_iter=20, dt=1e-3), [
         (0, -1, [(0.75, 1.5)], [0.2, 0.1, 0.3])]),
     "vortex24_char_roe_sponge_ssprk3": lambda: _sponge(C.vortex(24, n_iter=5, dt=0.02, scheme="ssprk3"), [
