@@ -60,7 +60,7 @@ class GbConfig(ctypes.Structure):
         ("zone_data", (ctypes.c_double * 8) * 12),
         ("gravity", ctypes.c_double * 3), ("rho_ref", ctypes.c_double), ("p_ref", ctypes.c_double),
         ("R_gas", ctypes.c_double), ("N_bv", ctypes.c_double), ("HB", ctypes.c_int), ("hyp_scheme", ctypes.c_int),
-        ("grav_type", ctypes.c_int), ("cons_check", ctypes.c_int),
+        ("grav_type", ctypes.c_int), ("cons_check", ctypes.c_int), ("par_scheme", ctypes.c_int),
     ]
 
 

@@ -74,6 +74,7 @@ class Case:
     HB: int = 0
     N_bv: float = 0.0
     conservation_check: bool = False  # solver.inp conservation_check yes
+    par_scheme: str = "4"             # NavierStokes3D solver.inp par_space_scheme: "4" or "2"
     op_format: str = "binary"         # solver.inp op_file_format: binary | text | tecplot2d | tecplot3d | none
 
     @property
@@ -105,7 +106,7 @@ class Case:
             f"  hyp_interp_type   {self.interp}",
         ]
         if self.model == "navierstokes3d":
-            lines += ["  par_space_type    nonconservative-2stage", "  par_space_scheme  4"]
+            lines += ["  par_space_type    nonconservative-2stage", f"  par_space_scheme  {self.par_scheme}"]
         lines += [
             f"  dt                {float(self.dt)!r}",
             f"  screen_op_iter    {self.screen_op_iter or max(self.n_iter, 1)}",

@@ -493,6 +493,7 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
   s->vp.inv_gm1 = 1.0 / (c.gamma - 1.0);
   s->vp.inv_Re = 1.0 / Re_eff;
   s->vp.inv_Pr = 1.0 / c.Pr;
+  s->vp.order = c.par_scheme == 2 ? 2 : 4;
   for (int d = 0; d < 3; d++) {
     s->hl[d].seg = 32;
     s->hl[d].block = 128;

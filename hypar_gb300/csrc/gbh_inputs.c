@@ -751,10 +751,11 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
       gbh_set_error("NavierStokes3D needs par_space_type nonconservative-2stage");
       return GB_ERR_INPUT;
     }
-    if (strcmp(si.par_space_scheme, "4")) {
-      gbh_set_error("par_space_scheme %s not supported (4 only)", si.par_space_scheme);
+    if (strcmp(si.par_space_scheme, "4") && strcmp(si.par_space_scheme, "2")) {
+      gbh_set_error("par_space_scheme %s not supported (2 or 4)", si.par_space_scheme);
       return GB_ERR_UNSUPPORTED;
     }
+    c.par_scheme = !strcmp(si.par_space_scheme, "2") ? 2 : 4;
   }
 
   /* weno.inp */

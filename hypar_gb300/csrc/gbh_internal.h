@@ -72,6 +72,7 @@ struct StageEpi {
 // NavierStokes3D viscous-term constants (NavierStokes3DParabolicFunction.c:76-79).
 struct ViscParams {
   double gamma, gm1, inv_Re, inv_Pr, inv_gm1;
+  int order;  // first derivatives: 4 (fourth-order central) or 2 (first-order one-sided)
 };
 
 // Per-launch configuration of the hyperbolic kernels.

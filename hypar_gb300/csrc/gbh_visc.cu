@@ -66,9 +66,21 @@ __device__ __forceinline__ double d4(int i, int N, int g, F f) {
   return (3.0 * f(-4) - 16.0 * f(-3) + 36.0 * f(-2) - 48.0 * f(-1) + 25.0 * f(0)) * one_twelve;
 }
 
+// First-order one-sided first derivative (FirstDerivativeFirstOrder.c:50-84): bias 1
+// forward, -1 backward in the interior of the ghost-extended line, forward at its first
+// point and backward at its last, in the reference's expression
+// max(bias,0) f(1) - bias f(0) + min(bias,0) f(-1).
+template <class F>
+__device__ __forceinline__ double d1(int i, int N, int g, int bias, F f) {
+  if (i == -g) return f(1) - f(0);
+  if (i == N + g - 1) return f(0) - f(-1);
+  return (bias > 0) ? __dadd_rn(__dsub_rn(f(1), f(0)), __dmul_rn(0.0, f(-1)))
+                    : __dsub_rn(__dadd_rn(__dmul_rn(0.0, f(1)), f(0)), f(-1));
+}
+
 // Scaled gradients of (u, v, w, T): Gr[p*12 + d*4 + c].
 __global__ void visc_grad_kernel(const double* __restrict__ Q, double* __restrict__ Gr, const double* __restrict__ dxinv,
-                                 DevGeom G) {
+                                 DevGeom G, int order) {
   int ng[3] = {G.dim[0] + 2 * G.g, G.dim[1] + 2 * G.g, G.dim[2] + 2 * G.g};
   long long n = (long long)ng[0] * ng[1] * ng[2];
   long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -90,7 +102,8 @@ __global__ void visc_grad_kernel(const double* __restrict__ Q, double* __restric
       double di = dxinv[off + G.g + idx[d]];
       for (int c = 0; c < 4; c++) {
         const double* base = Q + p * 6 + 1 + c;
-        double v = d4(idx[d], G.dim[d], G.g, [&](int k) { return base[(long long)k * sd * 6]; });
+        auto fk = [&](int k) { return base[(long long)k * sd * 6]; };
+        double v = order == 2 ? d1(idx[d], G.dim[d], G.g, 1, fk) : d4(idx[d], G.dim[d], G.g, fk);
         out[c] = v * di;
       }
     }
@@ -173,7 +186,10 @@ __global__ void visc_dir_kernel(const double* __restrict__ Q, const double* __re
     if (first) out[0] = 0.0;
 #pragma unroll
     for (int v = 0; v < 4; v++) {
-      double fd = (W[0][v] - 8.0 * W[1][v] + 8.0 * W[3][v] - W[4][v]) * one_twelve;
+      // interior points: the central fourth-order difference, or the backward
+      // first-order one of the second-order scheme
+      double fd = vp.order == 2 ? __dsub_rn(__dadd_rn(__dmul_rn(0.0, W[3][v]), W[2][v]), W[1][v])
+                                : (W[0][v] - 8.0 * W[1][v] + 8.0 * W[3][v] - W[4][v]) * one_twelve;
       double val = di * fd;
       out[1 + v] = first ? val : out[1 + v] + val;
     }
@@ -185,7 +201,7 @@ cudaError_t launch_visc(const double* u, double* Q, double* Gr, double* par, con
   long long n = (long long)(G.dim[0] + 2 * G.g) * (G.dim[1] + 2 * G.g) * (G.dim[2] + 2 * G.g);
   int blk = 256;
   visc_q_kernel<<<(unsigned)((n + blk - 1) / blk), blk, 0, s>>>(u, Q, G, vp);
-  visc_grad_kernel<<<(unsigned)((n + blk - 1) / blk), blk, 0, s>>>(Q, Gr, dxinv, G);
+  visc_grad_kernel<<<(unsigned)((n + blk - 1) / blk), blk, 0, s>>>(Q, Gr, dxinv, G, vp.order);
   int off = 0;
   for (int d = 0; d < 3; d++) {
     long long ntrans = 1;

@@ -129,6 +129,14 @@ int gbshim_config(void *s, gb_config *c) {
   if (!strcmp(solver->spatial_scheme_hyp, "weno5")) c->hyp_scheme = GB_SCHEME_WENO5;
   else if (!strcmp(solver->spatial_scheme_hyp, "crweno5")) c->hyp_scheme = GB_SCHEME_CRWENO5;
   else return unsupported("hyp_space_scheme", solver->spatial_scheme_hyp);
+  /* the viscous term's first derivatives (nonconservative-2stage, InitializeSolvers.c:129-141) */
+  if (c->model == GB_MODEL_NS3D && c->Re > 0) {
+    if (strcmp(solver->spatial_type_par, "nonconservative-2stage"))
+      return unsupported("par_space_type", solver->spatial_type_par);
+    if (!strcmp(solver->spatial_scheme_par, "2")) c->par_scheme = 2;
+    else if (!strcmp(solver->spatial_scheme_par, "4")) c->par_scheme = 4;
+    else return unsupported("par_space_scheme", solver->spatial_scheme_par);
+  }
 
   /* weno.inp, with the reader's precedence: no_limiting > yc > borges > mapped > JS */
   const WENOParameters *w = (const WENOParameters *)solver->interp;

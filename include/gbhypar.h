@@ -117,6 +117,11 @@ typedef struct gb_config {
   /* solver.inp conservation_check yes: the driver reports the conservation error
    * (gb_solver_conservation_*) */
   int cons_check;
+  /* NavierStokes3D viscous term, solver.inp par_space_scheme of the
+   * nonconservative-2stage form (InitializeSolvers.c:129-141): 4 (or 0): fourth-order
+   * central first derivatives; 2: first-order one-sided ones, forward for the
+   * gradients and backward for the flux divergence (FirstDerivativeFirstOrder.c) */
+  int par_scheme;
 } gb_config;
 
 typedef struct gb_solver gb_solver;

@@ -90,6 +90,8 @@ def _bind(path):
     L.orc_set_zone_sponge.restype = ctypes.c_int
     L.orc_set_zone_inflow.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, dp]
     L.orc_set_zone_inflow.restype = ctypes.c_int
+    L.orc_set_par_scheme.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.orc_set_par_scheme.restype = None
     L.orc_set_gravity.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_double]
@@ -281,6 +283,7 @@ class Problem:
             raise RuntimeError("orc_problem_create failed")
         L.orc_set_weights(self.h, WEIGHTS[getattr(case, "weights", "js")])
         L.orc_set_scheme(self.h, SCHEMES[getattr(case, "hyp_scheme", "weno5")])
+        L.orc_set_par_scheme(self.h, int(getattr(case, "par_scheme", "4")))
         for z, row in enumerate(boundary_rows):
             vals = list(row[4]) if len(row) > 4 else []
             data = np.zeros(8)

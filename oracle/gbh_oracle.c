@@ -1633,6 +1633,49 @@ static void deriv4(const orc_problem *p, double *Df, const double *f, int dir) {
   }
 }
 
+/* FirstDerivativeFirstOrder (src/FirstDerivative/FirstDerivativeFirstOrder.c:36-86):
+ * forward at the first point of the ghost-extended line, backward at its last, and in
+ * between bias 1 (forward) or -1 (backward), as the reference writes it; lines with
+ * interior transverse indices only. */
+static void deriv1(const orc_problem *p, double *Df, const double *f, int dir, int bias) {
+  int nd = p->ndims, nv = p->nvars, g = p->ghosts;
+  long s[3];
+  strides_wg(p, s);
+  int N = p->dim[dir];
+  long sd = s[dir];
+  long nouter = 1;
+  int ob[3] = {1, 1, 1};
+  for (int e = 0; e < nd; e++) if (e != dir) { ob[e] = p->dim[e]; nouter *= p->dim[e]; }
+#pragma omp parallel for schedule(static) num_threads(NTHR)
+  for (long lo = 0; lo < nouter; lo++) {
+    int idx[3] = {0, 0, 0};
+    long r = lo;
+    for (int e = 0; e < nd; e++) if (e != dir) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
+    idx[dir] = -g;
+    long b = pidx(p, s, idx);
+    for (int i = -g; i < N + g; i++) {
+      long qC = b + (long)(i + g) * sd;
+      for (int v = 0; v < nv; v++) {
+        double val;
+#define F(k) f[(qC + (long)(k) * sd) * nv + v]
+        if (i == -g) val = F(1) - F(0);
+        else if (i == N + g - 1) val = F(0) - F(-1);
+        else val = (bias > 0 ? bias : 0) * F(1) - bias * F(0) + (bias < 0 ? bias : 0) * F(-1);
+#undef F
+        Df[qC * nv + v] = val;
+      }
+    }
+  }
+}
+
+void orc_set_par_scheme(orc_problem *p, int scheme) { p->par_scheme = scheme; }
+
+/* the first derivative of par_space_scheme (InitializeSolvers.c:129-141) */
+static void deriv_par(const orc_problem *p, double *Df, const double *f, int dir, int bias) {
+  if (p->par_scheme == 2) deriv1(p, Df, f, dir, bias);
+  else deriv4(p, Df, f, dir);
+}
+
 /* NavierStokes3DParabolicFunction (NavierStokes3DParabolicFunction.c:50-325),
  * including its single-rank behaviour: derivative arrays start at zero and are
  * filled only on lines with interior transverse indices, so cross derivatives
@@ -1663,9 +1706,9 @@ int orc_parabolic(const orc_problem *p, const double *u, double *par) {
     (void)energy;
     Qp[4] = p->gamma * pressure / Qp[0];
   }
-  deriv4(p, QX, Q, 0);
-  deriv4(p, QY, Q, 1);
-  deriv4(p, QZ, Q, 2);
+  deriv_par(p, QX, Q, 0, 1);
+  deriv_par(p, QY, Q, 1, 1);
+  deriv_par(p, QZ, Q, 2, 1);
   const double *dxi = p->dxinv, *dyi = p->dxinv + imax + 2 * g, *dzi = dyi + jmax + 2 * g;
 #pragma omp parallel for schedule(static) num_threads(NTHR)
   for (int k = -g; k < kmax + g; k++)
@@ -1711,7 +1754,7 @@ int orc_parabolic(const orc_problem *p, const double *u, double *par) {
         Fv[4] = uvel * tau_zx + vvel * tau_zy + wvel * tau_zz + qz;
       }
     }
-    deriv4(p, FD, FV, dir);
+    deriv_par(p, FD, FV, dir, -1);
     const double *di = (dir == 0) ? dxi : (dir == 1 ? dyi : dzi);
 #pragma omp parallel for schedule(static) num_threads(NTHR)
     for (int k = 0; k < kmax; k++)

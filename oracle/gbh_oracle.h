@@ -66,6 +66,8 @@ typedef struct {
   /* per turbulent inflow zone the number of slices and the inflow data */
   int fn[12];
   double *fdata[12];
+  /* NavierStokes3D par_space_scheme: 4 (0: 4) or 2 */
+  int par_scheme;
 } orc_problem;
 
 /* WENO5 weights: Jiang-Shu, mapped (Henrick-Aslam-Powers), Borges (WENO-Z),
@@ -100,6 +102,8 @@ int orc_set_zone_sponge(orc_problem *p, int z, const double *x, double xmin, dou
 /* Turbulent inflow zones: n slices of inflow data (the grid's size across the zone's
  * dimension, n along it, nvars values per point, dimension 0 fastest). */
 int orc_set_zone_inflow(orc_problem *p, int z, int n, const double *data);
+/* NavierStokes3D viscous term: par_space_scheme 2 or 4. */
+void orc_set_par_scheme(orc_problem *p, int scheme);
 
 /* Create/destroy a problem.  zones: nzones x 9 ints (type,dim,face,is[3],ie[3]);
  * dxinv: sum_d (dim[d]+2g) doubles (copied). */

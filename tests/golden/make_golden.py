@@ -161,6 +161,11 @@ CASES = {
         (2, -1): ("subsonic-ambivalent", [1.0, 0.0, 0.0, -0.1, 1.0 / 1.4])}),
     # sponge zones: a relaxation source over boxes of interior points (two overlapping
     # in the 2-D deck), beside periodic and extrapolate faces
+    # NavierStokes3D viscous term with par_space_scheme 2 (first-order one-sided
+    # derivatives, FirstDerivativeFirstOrder.c)
+    "tgv12_comp_roe_par2_rk4": lambda: _par2(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05)),
+    "rtb12_comp_rusanov_visc_par2": lambda: _par2(_visc(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                               perturb=0.02), 500.0)),
     # time_scheme euler (HyPar's default time integrator, TimeForwardEuler.c)
     "sod64_comp_roe_euler": lambda: C.sod(64, n_iter=20, dt=1e-3, scheme="euler"),
     "vortex24_char_llf_euler": lambda: C.vortex(24, n_iter=5, dt=0.01, upwinding="llf-char", scheme="euler"),
@@ -196,6 +201,12 @@ def _turb(case, dim=0, nslices=64, speed=2.0, seed=17):
     vel[dim] = speed
     case.bcs = {(dim, 1): ("turbulent-supersonic-inflow", [1.0] + vel + [1.0 / 1.4], (nslices, data.reshape(-1))),
                 (dim, -1): ("supersonic-outflow", [])}
+    return case
+
+
+def _par2(case):
+    """The deck with par_space_scheme 2."""
+    case.par_scheme = "2"
     return case
 
 

@@ -51,8 +51,8 @@ int main() {
   for (int k = 0; k < 4; k++) printf(" %.17g", c.rk_b[k]);
   printf("\nrk_c");
   for (int k = 0; k < 4; k++) printf(" %.17g", c.rk_c[k]);
-  printf("\ndt %.17g\nn_iter %d\nfile_op_iter %d\nrestart_iter %d\nscreen_op_iter %d\ncons_check %d\n", c.dt,
-         c.n_iter, c.file_op_iter, c.restart_iter, c.screen_op_iter, c.cons_check);
+  printf("\ndt %.17g\nn_iter %d\nfile_op_iter %d\nrestart_iter %d\nscreen_op_iter %d\ncons_check %d\npar_scheme %d\n",
+         c.dt, c.n_iter, c.file_op_iter, c.restart_iter, c.screen_op_iter, c.cons_check, c.par_scheme);
   printf("attach_rc %d\n", gbshim_attach(solver, &h.obj()->mpi));
   return 0;
 }

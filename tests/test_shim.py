@@ -74,6 +74,7 @@ DECKS = {
     "sod_no_limiting_rf": lambda: _with(C.sod(48, n_iter=2, dt=1e-3, upwinding="rf-char"), weights="none"),
     "rtb_gravity_hb2": lambda: C.rising_thermal_bubble(12, n_iter=2),
     "stratified_euler1d_gravity": lambda: C.stratified_1d(32, n_iter=2, g=1.0, grav_type=0),
+    "tgv_second_order_viscous": lambda: _with(C.tgv(12, n_iter=2, dt=0.02), par_scheme="2"),
     "sod_forward_euler": lambda: C.sod(48, n_iter=2, dt=1e-3, scheme="euler"),
     "vortex_sponges": lambda: _with(C.vortex(24, n_iter=2, dt=0.02), sponges=[
         (0, -1, [(6.0, 9.6), (-1.0, 11.0)], [1.1, 0.4, 0.05, 2.7]),
@@ -104,7 +105,7 @@ def test_shim_config_matches_reader(shim_exe, tmp_path, name):
     assert got["config_rc"] == ["0"], p.stdout + p.stderr
     want = Inputs(d).config
     ints = ["model", "ndims", "nvars", "ghosts", "interp", "upwind", "hyp_scheme", "weno_weights", "nzones",
-            "rk_nstages", "n_iter", "file_op_iter", "restart_iter", "screen_op_iter", "cons_check"]
+            "rk_nstages", "n_iter", "file_op_iter", "restart_iter", "screen_op_iter", "cons_check", "par_scheme"]
     for k in ints:
         assert int(got[k][0]) == getattr(want, k), k
     assert [int(v) for v in got["dim"]] == list(want.dim)
