@@ -133,6 +133,8 @@ typedef struct {
   char time_scheme[MAXS], time_scheme_type[MAXS], hyp_space_scheme[MAXS], interp_type[MAXS];
   char par_space_type[MAXS], par_space_scheme[MAXS], model[MAXS], ip_file_type[MAXS];
   char op_overwrite[MAXS], hyp_flux_split[MAXS], cons_check[MAXS], op_format[MAXS], input_mode[MAXS];
+  char ib_file[MAXS];      /* immersed_body ("none": no immersed body) */
+  int size_ex[3], have_size_ex;
 } solver_inp;
 
 static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsims) {
@@ -154,6 +156,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
   strcpy(si->op_overwrite, "no");
   strcpy(si->model, "none");
   strcpy(si->hyp_flux_split, "no");
+  strcpy(si->ib_file, "none");
   strcpy(si->cons_check, "no");
   strcpy(si->op_format, "text");  /* ReadInputs.c:140 */
   strcpy(si->input_mode, "serial");
@@ -180,7 +183,8 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
       if (!have_ndims || si->ndims < 1 || si->ndims > 3) { ok = 0; break; }
       /* "size" lists ndims values for every simulation of an ensemble
          (ReadInputs.c:189-206); "iproc" and "size_exact" likewise per simulation */
-      int *dst = !strcmp(w, "size") ? si->size : (!strcmp(w, "iproc") ? si->iproc : NULL);
+      int *dst = !strcmp(w, "size") ? si->size : (!strcmp(w, "iproc") ? si->iproc : si->size_ex);
+      if (!strcmp(w, "size_exact")) si->have_size_ex = 1;
       for (int n = 0; n < si->nsims && r == 1; n++)
         for (int d = 0; d < si->ndims; d++) {
           int val;
@@ -207,6 +211,7 @@ static int read_solver_inp(const char *dir, solver_inp *si, int member, int nsim
     else if (!strcmp(w, "model")) r = fscanf(in, "%511s", si->model);
     else if (!strcmp(w, "conservation_check")) r = fscanf(in, "%511s", si->cons_check);
     else if (!strcmp(w, "op_file_format")) r = fscanf(in, "%511s", si->op_format);
+    else if (!strcmp(w, "immersed_body")) r = fscanf(in, "%511s", si->ib_file);
     else if (!strcmp(w, "input_mode") || !strcmp(w, "output_mode")) {
       char mode[MAXS];
       r = fscanf(in, "%511s", mode);
@@ -665,10 +670,24 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
     gbh_set_error("hyp_space_scheme %s not supported (weno5, crweno5)", si.hyp_space_scheme);
     return GB_ERR_UNSUPPORTED;
   }
-  if (strcmp(si.hyp_flux_split, "no")) {
-    gbh_set_error("hyp_flux_split %s not supported", si.hyp_flux_split);
+  /* hyp_flux_split yes: only the implicit-explicit integrators split the flux
+   * (ComputeRHSOperators.c); explicit Runge-Kutta evaluates the whole flux, so for
+   * Euler1D and NavierStokes3D it changes nothing, and Euler2D refuses it
+   * (Euler2DInitialize.c:79-85) */
+  if (strcmp(si.hyp_flux_split, "no") && c.model == GB_MODEL_EULER2D) {
+    gbh_set_error("hyp_flux_split %s: Euler2D has no splitting of the hyperbolic term", si.hyp_flux_split);
+    return GB_ERR_INPUT;
+  }
+  if (strcmp(si.ib_file, "none")) {
+    gbh_set_error("immersed_body %s: immersed boundaries are not available in this library", si.ib_file);
     return GB_ERR_UNSUPPORTED;
   }
+  if (si.have_size_ex)
+    for (int d = 0; d < si.ndims; d++)
+      if (si.size_ex[d] != si.size[d]) {
+        gbh_set_error("size_exact differs from size: an exact solution on another grid is not available");
+        return GB_ERR_UNSUPPORTED;
+      }
   if (!strcmp(si.interp_type, "components")) c.interp = GB_INTERP_COMPONENTS;
   else if (!strcmp(si.interp_type, "characteristic")) c.interp = GB_INTERP_CHARACTERISTIC;
   else {

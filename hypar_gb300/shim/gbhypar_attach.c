@@ -129,6 +129,7 @@ int gbshim_config(void *s, gb_config *c) {
   if (!strcmp(solver->spatial_scheme_hyp, "weno5")) c->hyp_scheme = GB_SCHEME_WENO5;
   else if (!strcmp(solver->spatial_scheme_hyp, "crweno5")) c->hyp_scheme = GB_SCHEME_CRWENO5;
   else return unsupported("hyp_space_scheme", solver->spatial_scheme_hyp);
+  if (solver->flag_ib) return unsupported("immersed_body", solver->ib_filename);
   /* the viscous term's first derivatives (nonconservative-2stage, InitializeSolvers.c:129-141) */
   if (c->model == GB_MODEL_NS3D && c->Re > 0) {
     if (strcmp(solver->spatial_type_par, "nonconservative-2stage"))

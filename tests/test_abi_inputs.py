@@ -318,3 +318,32 @@ def test_reader_euler1d_gravity(built_lib, oracle_lib, tmp_path, grav_type):
     assert np.array_equal(inp.gravity_field, O.Problem(case).gravity_field())
     case.upwinding = "rusanov"
     _expect(3, str(_deck(tmp_path / "b", case)))
+
+
+def _solver_inp_with(d, extra):
+    t = open(d + "/solver.inp").read().replace("end\n", extra + "\nend\n")
+    open(d + "/solver.inp", "w").write(t)
+
+
+def test_solver_inp_keywords_outside_the_flux(built_lib, tmp_path):
+    """hyp_flux_split yes changes nothing for explicit Runge-Kutta on Euler1D and
+    NavierStokes3D and is refused for Euler2D (Euler2DInitialize.c:79-85);
+    immersed_body and a size_exact other than size are refused; size_exact equal to
+    size, plot_solution, use_gpu and gpu_device_no are read and change nothing."""
+    for name, case in (("sod", C.sod(16, n_iter=1)), ("tgv", C.tgv(6, n_iter=1))):
+        d = str(tmp_path / name)
+        case.write(d)
+        base = Inputs(d).config
+        _solver_inp_with(d, "  hyp_flux_split yes\n  plot_solution no\n  use_gpu yes\n  gpu_device_no 0\n"
+                            "  size_exact " + " ".join(str(s) for s in case.size))
+        cfg = Inputs(d).config
+        assert bytes(cfg) == bytes(base)
+    d = str(tmp_path / "vortex")
+    C.vortex(12, n_iter=1, dt=0.01).write(d)
+    _solver_inp_with(d, "  hyp_flux_split yes")
+    _expect(3, d)
+    for extra in ("  immersed_body body.stl", "  size_exact 32 32"):
+        d = str(tmp_path / ("v" + str(abs(hash(extra)))))
+        C.vortex(12, n_iter=1, dt=0.01).write(d)
+        _solver_inp_with(d, extra)
+        _expect(4, d)
