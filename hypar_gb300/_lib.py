@@ -15,7 +15,7 @@ GB_OK = 0
 GB_ERR = {1: "GB_ERR_ARG", 2: "GB_ERR_CUDA", 3: "GB_ERR_INPUT", 4: "GB_ERR_UNSUPPORTED", 5: "GB_ERR_NOMEM",
           6: "GB_ERR_NONFINITE", 7: "GB_ERR_HOOK"}
 MODEL = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
-UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3}
+UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3, "steger-warming": 4}
 INTERP = {"components": 0, "characteristic": 1}
 WENO_WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 SCHEME = {"weno5": 0, "crweno5": 1}

@@ -347,9 +347,13 @@ int gbh_validate(const gb_config* c) {
   for (int d = 0; d < nd; d++)
     if (c->dim[d] < 4) { gbh_set_error("dim[%d] = %d < 4", d, c->dim[d]); return GB_ERR_ARG; }
   if (c->interp != GB_INTERP_COMPONENTS && c->interp != GB_INTERP_CHARACTERISTIC) { gbh_set_error("bad interp"); return GB_ERR_ARG; }
-  if (c->upwind < 0 || c->upwind > 3) { gbh_set_error("bad upwind"); return GB_ERR_ARG; }
+  if (c->upwind < 0 || c->upwind > 4) { gbh_set_error("bad upwind"); return GB_ERR_ARG; }
   if (c->upwind == GB_UPWIND_RUSANOV && c->model == GB_MODEL_EULER2D) {
     gbh_set_error("Euler2D offers no Rusanov upwinding");
+    return GB_ERR_UNSUPPORTED;
+  }
+  if (c->upwind == GB_UPWIND_SWFS && c->model == GB_MODEL_NS3D) {
+    gbh_set_error("NavierStokes3D offers no Steger-Warming upwinding");
     return GB_ERR_UNSUPPORTED;
   }
   if (c->rk_nstages < 1 || c->rk_nstages > 4) { gbh_set_error("rk_nstages must be 1..4"); return GB_ERR_ARG; }

@@ -573,6 +573,9 @@ static cudaError_t cr_dir_upw(bool chr, int upw, const double* U, double* H, con
     case UPW_ROE: return cr_dir<M, DIR, ALTW, UPW_ROE>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
     case UPW_LLF: return cr_dir<M, DIR, ALTW, UPW_LLF>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
     case UPW_RF: return cr_dir<M, DIR, ALTW, UPW_RF>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    case UPW_SWFS:
+      if (M == MODEL_NS3D) return cudaErrorInvalidValue;  // NavierStokes3D has no Steger-Warming
+      return cr_dir<M, DIR, ALTW, (M != MODEL_NS3D ? UPW_SWFS : UPW_RF)>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
     default:
       if (M == MODEL_EULER2D) return cudaErrorInvalidValue;  // Euler2D has no Rusanov
       return cr_dir<M, DIR, ALTW, (M == MODEL_EULER2D ? UPW_ROE : UPW_RUS)>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);

@@ -13,7 +13,7 @@
 namespace gbh {
 
 enum { MODEL_EULER1D = 1, MODEL_EULER2D = 2, MODEL_NS3D = 3 };
-enum { UPW_ROE = 0, UPW_LLF = 1, UPW_RF = 2, UPW_RUS = 3 };
+enum { UPW_ROE = 0, UPW_LLF = 1, UPW_RF = 2, UPW_RUS = 3, UPW_SWFS = 4 };
 
 template <int M> struct ModelTraits;
 template <> struct ModelTraits<MODEL_EULER1D> { static constexpr int NV = 3, ND = 1; };
@@ -234,6 +234,55 @@ __device__ __forceinline__ Eig roe_eig_cons(const double* a, const double* b, co
   E.rho = ta * tb;
   roe_eig_finish<M, DIR>(E, vsq, pp);
   return E;
+}
+
+// Steger-Warming flux vector splitting of one conserved state along DIR (PLUS: the
+// part of the non-negative eigenvalues, else of the non-positive ones), in the
+// reference's expressions: Euler1DUpwind.c:336-350 (Euler1D, whose split takes v + c
+// for the plus part and v - c for the minus part) and Euler2DUpwind.c:244-276.
+template <int M, int DIR, bool PLUS>
+__device__ __forceinline__ void swfs_half(const double* u, const PhysParams& pp, double* f) {
+  const double gamma = pp.gamma;
+  const double rho = u[0];
+  if (M == MODEL_EULER1D) {
+    const double v = u[1] / rho, e = u[2];
+    const double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+    const double c = sqrt(gamma * P / rho);
+    const double term = rho / (2.0 * gamma);
+    if (PLUS) {
+      f[0] = term * (2 * gamma * v + c - v);
+      f[1] = term * (2 * (gamma - 1.0) * v * v + (v + c) * (v + c));
+      f[2] = term * ((gamma - 1.0) * v * v * v + 0.5 * (v + c) * (v + c) * (v + c) +
+                     ((3.0 - gamma) * (v + c) * c * c) / (2.0 * (gamma - 1.0)));
+    } else {
+      f[0] = term * (v - c);
+      f[1] = term * (v - c) * (v - c);
+      f[2] = term * (0.5 * (v - c) * (v - c) * (v - c) + ((3.0 - gamma) * (v - c) * c * c) / (2.0 * (gamma - 1.0)));
+    }
+  } else {
+    const double vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+    const double P = (e - 0.5 * rho * ((vx * vx) + (vy * vy))) * (gamma - 1.0);
+    const double c = sqrt(gamma * P / rho);
+    const double term = rho / (2.0 * gamma);
+    const double kx = DIR == 0 ? 1.0 : 0.0, ky = DIR == 1 ? 1.0 : 0.0;
+    double l0 = kx * vx + ky * vy, l2 = l0 + c, l3 = l0 - c;
+    if (PLUS) {
+      l0 = l0 < 0.0 ? 0.0 : l0;
+      l2 = l2 < 0.0 ? 0.0 : l2;
+      l3 = l3 < 0.0 ? 0.0 : l3;
+    } else {
+      l0 = l0 > 0.0 ? 0.0 : l0;
+      l2 = l2 > 0.0 ? 0.0 : l2;
+      l3 = l3 > 0.0 ? 0.0 : l3;
+    }
+    f[0] = term * (2.0 * (gamma - 1.0) * l0 + l2 + l3);
+    f[1] = term * (2.0 * (gamma - 1.0) * l0 * vx + l2 * (vx + c * kx) + l3 * (vx - c * kx));
+    f[2] = term * (2.0 * (gamma - 1.0) * l0 * vy + l2 * (vy + c * ky) + l3 * (vy - c * ky));
+    f[3] = term * ((gamma - 1.0) * l0 * (vx * vx + vy * vy) +
+                   0.5 * l2 * ((vx + c * kx) * (vx + c * kx) + (vy + c * ky) * (vy + c * ky)) +
+                   0.5 * l3 * ((vx - c * kx) * (vx - c * kx) + (vy - c * ky) * (vy - c * ky)) +
+                   ((3.0 - gamma) * (l2 + l3) * c * c) / (2.0 * (gamma - 1.0)));
+  }
 }
 
 template <int M, int DIR>

@@ -182,6 +182,10 @@ extern "C" int gb_ensemble_create(const gb_config* cfgs, const double* const* dx
   for (int m = 0; m < nsims; m++) {
     int rc = gbh_validate(&cfgs[m]);
     if (rc) return rc;
+    if (cfgs[m].upwind == GB_UPWIND_SWFS) {
+      gbh_set_error("ensemble member %d: Steger-Warming upwinding is not available in the ensemble; use a gb_solver", m);
+      return GB_ERR_UNSUPPORTED;
+    }
     for (int z = 0; z < cfgs[m].nzones; z++)
       if (cfgs[m].zones[z][0] == GB_BC_SPONGE) {
         gbh_set_error("ensemble member %d: sponge zones are not available in the ensemble; use a gb_solver", m);

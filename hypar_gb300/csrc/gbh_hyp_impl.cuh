@@ -81,12 +81,39 @@ template <int M, bool CHAR, int UPW, int DIR>
 __device__ __forceinline__ void upwind_iface(const double* fL, const double* fR, const double* uL,
                                              const double* uR, const Eig& Ecc, const CellAux<M>& cl,
                                              const CellAux<M>& cr, const PhysParams& pp, double* fI,
-                                             double kappa = 1.0, const double* ush = nullptr) {
+                                             double kappa = 1.0, const double* ush = nullptr,
+                                             const double* fsh = nullptr) {
   constexpr int NV = ModelTraits<M>::NV;
   auto actual = [&](const double* x, double* y) {
 #pragma unroll
     for (int v = 0; v < NV; v++) y[v] = ush ? x[v] + ush[v] : x[v];
   };
+  if (UPW == UPW_SWFS) {
+    // Steger-Warming (Euler1DUpwind.c:293-362, Euler2DUpwind.c:211-291): by the Mach
+    // number of the Roe average of the reconstructed states, fR (below -1), fL (1 and
+    // above), or F+(uL) + F-(uR).  In the centre-relative form (ush, fsh: the centre
+    // cell's state and flux) the split fluxes are taken of the actual states and the
+    // centre flux is subtracted like the other fluxes.
+    double aL[NV], aR[NV];
+    actual(uL, aL);
+    actual(uR, aR);
+    const Eig Ea = roe_eig_cons<M, DIR>(aL, aR, pp);
+    const double mach = Ea.un / Ea.a;
+    if (mach < -1.0) {
+#pragma unroll
+      for (int v = 0; v < NV; v++) fI[v] = fR[v];
+    } else if (mach < 1.0) {
+      double fp[NV], fm[NV];
+      swfs_half<M, DIR, true>(aL, pp, fp);
+      swfs_half<M, DIR, false>(aR, pp, fm);
+#pragma unroll
+      for (int v = 0; v < NV; v++) fI[v] = fsh ? (fp[v] + fm[v]) - fsh[v] : fp[v] + fm[v];
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; v++) fI[v] = fL[v];
+    }
+    return;
+  }
   if (UPW == UPW_RUS) {
     // Rusanov (Euler1DUpwind.c:362-424, NavierStokes3DUpwind.c:349-428):
     // fI = (fL+fR)/2 - alpha (uR-uL)/2, alpha = max of |v|+c over the two
@@ -202,7 +229,8 @@ template <int M, int UPW, int DIR>
 __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR, const double* xuL,
                                             const double* xuR, const Eig& Ecc, const CellAux<M>& cl,
                                             const CellAux<M>& cr, const PhysParams& pp, double* fI,
-                                            double kappa = 1.0, const double* ush = nullptr) {
+                                            double kappa = 1.0, const double* ush = nullptr,
+                                            const double* fsh = nullptr) {
   constexpr int NV = ModelTraits<M>::NV;
   if (UPW == UPW_RUS) {
     // a scalar dissipation commutes with the basis: fI = R ((xfL+xfR)/2 - alpha (xuR-xuL)/2)
@@ -213,7 +241,7 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
     projR<M, DIR>(Ecc, fc, fI);
     return;
   }
-  constexpr bool SAME_BASIS = (M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE);
+  constexpr bool SAME_BASIS = UPW != UPW_SWFS && ((M == MODEL_EULER1D) || (M == MODEL_NS3D && UPW == UPW_ROE));
   if (SAME_BASIS) {
     double lamC[NV], fc[NV];
     eigvals<M>(Ecc.un, Ecc.a, lamC);
@@ -272,7 +300,7 @@ __device__ __forceinline__ void upwind_char(const double* xfL, const double* xfR
     double fL[NV], fR[NV];
     projR<M, DIR>(Ecc, xfL, fL);
     projR<M, DIR>(Ecc, xfR, fR);
-    upwind_iface<M, true, UPW, DIR>(fL, fR, uL, uR, Ecc, cl, cr, pp, fI, 1.0, ush);
+    upwind_iface<M, true, UPW, DIR>(fL, fR, uL, uR, Ecc, cl, cr, pp, fI, 1.0, ush, fsh);
   }
 }
 
@@ -396,7 +424,7 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
       }
     }
     upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, ax[2], ax[3], pp, fI,
-                                     GRAV ? fmax(wgg[2], wgg[3]) : 1.0, REL ? uc2 : nullptr);
+                                     GRAV ? fmax(wgg[2], wgg[3]) : 1.0, REL ? uc2 : nullptr, REL ? wf[2] : nullptr);
   } else {
     // Characteristic WENO5 (WENOFifthOrderCalculateWeightsCharJS :760-896 and
     // Interp1PrimFifthOrderWENOChar :86-198): one eigen-system per interface
@@ -490,7 +518,7 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
     }
     if (src_dir) projR<M, DIR>(Ecc, sch, SI);
     upwind_char<M, UPW, DIR>(xfL, xfR, xuL, xuR, Ecc, ax[2], ax[3], pp, fI, GRAV ? fmax(wgg[2], wgg[3]) : 1.0,
-                             REL ? uc2 : nullptr);
+                             REL ? uc2 : nullptr, REL ? wf[2] : nullptr);
   }
 }
 
@@ -871,7 +899,7 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
     double uc2[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) uc2[v] = su[t + 2][v];
-    upwind_iface<M, false, UPW, 0>(fL, fR, uL, uR, Ecc, sax[t + 2], sax[t + 3], pp, fI, 1.0, uc2);
+    upwind_iface<M, false, UPW, 0>(fL, fR, uL, uR, Ecc, sax[t + 2], sax[t + 3], pp, fI, 1.0, uc2, sf[t + 2]);
     if (ep.bnd && (I0 + t == 0 || I0 + t == N)) {
       double Fb[NV];
 #pragma unroll
@@ -1177,13 +1205,17 @@ cudaError_t launch_hyp_model(int dir, int chr, int upw, const double* U, double*
                              const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
                              cudaStream_t s) {
   constexpr int RUS = (M != MODEL_EULER2D) ? UPW_RUS : UPW_RF;  // Euler2D offers no Rusanov
+  constexpr int SW = (M != MODEL_NS3D) ? UPW_SWFS : UPW_RF;     // nor NavierStokes3D Steger-Warming
+  if (upw == UPW_SWFS && M == MODEL_NS3D) return cudaErrorInvalidValue;
   if (chr) {
+    if (upw == UPW_SWFS) return launch_dir_any<M, true, SW, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_ROE) return launch_dir_any<M, true, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_LLF) return launch_dir_any<M, true, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_RUS && M != MODEL_EULER2D)
       return launch_dir_any<M, true, RUS, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     return launch_dir_any<M, true, UPW_RF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
   } else {
+    if (upw == UPW_SWFS) return launch_dir_any<M, false, SW, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_ROE) return launch_dir_any<M, false, UPW_ROE, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_LLF) return launch_dir_any<M, false, UPW_LLF, ALTW>(dir, U, H, dxinv_dir, G, pp, ep, L, s);
     if (upw == UPW_RUS && M != MODEL_EULER2D)
@@ -1410,7 +1442,9 @@ cudaError_t launch_unfused_dir(int kind, int upw, double* out, const double* a, 
     ufunc_kernel<M><<<(unsigned)((npts + blk - 1) / blk), blk, 0, s>>>(out, u, npts, pp);
   } else {
     unsigned grid = (unsigned)((nint + blk - 1) / blk);
-    if (upw == UPW_ROE) upwind_kernel<M, UPW_ROE, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+    if (upw == UPW_SWFS && M != MODEL_NS3D)
+      upwind_kernel<M, (M != MODEL_NS3D ? UPW_SWFS : UPW_RF), DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
+    else if (upw == UPW_ROE) upwind_kernel<M, UPW_ROE, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
     else if (upw == UPW_LLF) upwind_kernel<M, UPW_LLF, DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp, nint);
     else if (upw == UPW_RUS && M != MODEL_EULER2D)
       upwind_kernel<M, (M != MODEL_EULER2D ? UPW_RUS : UPW_RF), DIR><<<grid, blk, 0, s>>>(out, a, b, c, d, u, G, pp,

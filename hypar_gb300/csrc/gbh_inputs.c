@@ -742,8 +742,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   else if (!strcmp(upw, "llf-char")) c.upwind = GB_UPWIND_LLF;
   else if (!strcmp(upw, "rf-char")) c.upwind = GB_UPWIND_RF;
   else if (!strcmp(upw, "rusanov") && c.model != GB_MODEL_EULER2D) c.upwind = GB_UPWIND_RUSANOV;
+  else if (!strcmp(upw, "steger-warming") && c.model != GB_MODEL_NS3D) c.upwind = GB_UPWIND_SWFS;
   else {
-    gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char; rusanov for Euler1D / NavierStokes3D)", upw);
+    gbh_set_error("upwinding %s not supported (roe, llf-char, rf-char; rusanov for Euler1D / NavierStokes3D; "
+                  "steger-warming for Euler1D / Euler2D)", upw);
     return GB_ERR_UNSUPPORTED;
   }
   if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.hyp_scheme == GB_SCHEME_CRWENO5) {

@@ -125,6 +125,7 @@ int gbshim_config(void *s, gb_config *c) {
   else if (!strcmp(upw, "llf-char")) c->upwind = GB_UPWIND_LLF;
   else if (!strcmp(upw, "rf-char")) c->upwind = GB_UPWIND_RF;
   else if (!strcmp(upw, "rusanov")) c->upwind = GB_UPWIND_RUSANOV;
+  else if (!strcmp(upw, "steger-warming")) c->upwind = GB_UPWIND_SWFS;
   else return unsupported("upwinding", upw);
   if (!strcmp(solver->spatial_scheme_hyp, "weno5")) c->hyp_scheme = GB_SCHEME_WENO5;
   else if (!strcmp(solver->spatial_scheme_hyp, "crweno5")) c->hyp_scheme = GB_SCHEME_CRWENO5;

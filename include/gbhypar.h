@@ -38,7 +38,8 @@ extern "C" {
 #define GB_ERR_HOOK 7         /* a hook installed with gb_solver_set_hooks returned nonzero */
 
 enum { GB_MODEL_EULER1D = 1, GB_MODEL_EULER2D = 2, GB_MODEL_NS3D = 3 };
-enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2, GB_UPWIND_RUSANOV = 3 /* Euler1D, NS3D */ };
+enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2, GB_UPWIND_RUSANOV = 3 /* Euler1D, NS3D */,
+       GB_UPWIND_SWFS = 4 /* physics.inp "steger-warming": Euler1D, Euler2D */ };
 enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
 /* boundary.inp types (include/boundaryconditions.h): periodic and extrapolate for every
  * model; dirichlet for every model; the wall and inflow/outflow types, and the

@@ -31,7 +31,7 @@ FMA_LIB_PATH = os.path.join(HERE, "liboracle_fma.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 MODELS = {"euler1d": 1, "euler2d": 2, "navierstokes3d": 3}
-UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3}
+UPWIND = {"roe": 0, "llf-char": 1, "rf-char": 2, "rusanov": 3, "steger-warming": 4}
 INTERP = {"components": 0, "characteristic": 1}
 WEIGHTS = {"js": 0, "mapped": 1, "borges": 2, "yc": 3, "none": 4}
 BCTYPE = {"periodic": 1, "extrapolate": 2, "dirichlet": 3, "slip-wall": 4, "noslip-wall": 5,

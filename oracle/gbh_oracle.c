@@ -1092,10 +1092,79 @@ static double rusanov_speed(const orc_problem *p, const double *u, int dir) {
   return c + absolute(vel[dir]);
 }
 
+/* Steger-Warming flux vector splitting of one state: Euler1DUpwindSWFS
+ * (src/PhysicalModels/Euler1D/Euler1DUpwind.c:336-350) and Euler2DUpwindSWFS
+ * (src/PhysicalModels/Euler2D/Euler2DUpwind.c:244-276), plus (plus = 1) or minus part. */
+static void swfs_split(const orc_problem *p, int dir, const double *u, int plus, double *f) {
+  double gamma = p->gamma;
+  if (p->model == ORC_EULER1D) {
+    double rho = u[0], v = u[1] / rho, e = u[2];
+    double P = (e - 0.5 * rho * v * v) * (gamma - 1.0);
+    double c = sqrt(gamma * P / rho);
+    double term = rho / (2.0 * gamma);
+    if (plus) {
+      f[0] = term * (2 * gamma * v + c - v);
+      f[1] = term * (2 * (gamma - 1.0) * v * v + (v + c) * (v + c));
+      f[2] = term * ((gamma - 1.0) * v * v * v + 0.5 * (v + c) * (v + c) * (v + c) +
+                     ((3.0 - gamma) * (v + c) * c * c) / (2.0 * (gamma - 1.0)));
+    } else {
+      f[0] = term * (v - c);
+      f[1] = term * (v - c) * (v - c);
+      f[2] = term * (0.5 * (v - c) * (v - c) * (v - c) + ((3.0 - gamma) * (v - c) * c * c) / (2.0 * (gamma - 1.0)));
+    }
+    return;
+  }
+  double rho = u[0], vx = u[1] / rho, vy = u[2] / rho, e = u[3];
+  double vsq = (vx * vx) + (vy * vy);
+  double P = (e - 0.5 * rho * vsq) * (gamma - 1.0);
+  double c = sqrt(gamma * P / rho);
+  double term = rho / (2.0 * gamma);
+  double kx = (dir == 0 ? 1.0 : 0.0), ky = (dir == 1 ? 1.0 : 0.0), l[4];
+  l[0] = l[1] = kx * vx + ky * vy;
+  l[2] = l[0] + c;
+  l[3] = l[0] - c;
+  for (int k = 0; k < 4; k++) {
+    if (plus && l[k] < 0.0) l[k] = 0.0;
+    if (!plus && l[k] > 0.0) l[k] = 0.0;
+  }
+  f[0] = term * (2.0 * (gamma - 1.0) * l[0] + l[2] + l[3]);
+  f[1] = term * (2.0 * (gamma - 1.0) * l[0] * vx + l[2] * (vx + c * kx) + l[3] * (vx - c * kx));
+  f[2] = term * (2.0 * (gamma - 1.0) * l[0] * vy + l[2] * (vy + c * ky) + l[3] * (vy - c * ky));
+  f[3] = term * ((gamma - 1.0) * l[0] * (vx * vx + vy * vy) +
+                 0.5 * l[2] * ((vx + c * kx) * (vx + c * kx) + (vy + c * ky) * (vy + c * ky)) +
+                 0.5 * l[3] * ((vx - c * kx) * (vx - c * kx) + (vy - c * ky) * (vy - c * ky)) +
+                 ((3.0 - gamma) * (l[2] + l[3]) * c * c) / (2.0 * (gamma - 1.0)));
+}
+
 static void upwind(const orc_problem *p, int dir, double *fI, const double *fL, const double *fR,
                    const double *uL, const double *uR, const double *uCL, const double *uCR, long qL, long qR) {
   int nv = p->nvars;
   double uavg[MAXV], D[MAXV], L[MAXV * MAXV], R[MAXV * MAXV];
+  if (p->upwind == ORC_UPW_SWFS) {
+    /* by the Mach number of the Roe average of the reconstructed states: fR, fL or
+     * F+(uL) + F-(uR) */
+    m_roeavg(p, uavg, uL, uR);
+    double rho = uavg[0], vn = uavg[1 + dir] / rho, P;
+    if (p->model == ORC_EULER1D) {
+      P = (uavg[2] - 0.5 * rho * vn * vn) * (p->gamma - 1.0); /* _Euler1DGetFlowVar_ */
+    } else {
+      double vx = uavg[1] / rho, vy = uavg[2] / rho;
+      double vsq = (vx * vx) + (vy * vy);
+      P = (uavg[3] - 0.5 * rho * vsq) * (p->gamma - 1.0); /* _Euler2DGetFlowVar_ */
+    }
+    double mach = vn / sqrt(p->gamma * P / rho);
+    if (mach < -1.0) {
+      for (int v = 0; v < nv; v++) fI[v] = fR[v];
+    } else if (mach < 1.0) {
+      double fp[MAXV], fm[MAXV];
+      swfs_split(p, dir, uL, 1, fp);
+      swfs_split(p, dir, uR, 0, fm);
+      for (int v = 0; v < nv; v++) fI[v] = fp[v] + fm[v];
+    } else {
+      for (int v = 0; v < nv; v++) fI[v] = fL[v];
+    }
+    return;
+  }
   if (p->upwind == ORC_UPW_RUSANOV) {
     /* fI = (fL+fR)/2 - kappa max3(speeds of the cell-centre states and their
      * Roe average) (uR-uL)/2, kappa = 1 without gravity */

@@ -20,7 +20,7 @@ extern "C" {
 #endif
 
 enum { ORC_EULER1D = 1, ORC_EULER2D = 2, ORC_NS3D = 3 };
-enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2, ORC_UPW_RUSANOV = 3 };
+enum { ORC_UPW_ROE = 0, ORC_UPW_LLF = 1, ORC_UPW_RF = 2, ORC_UPW_RUSANOV = 3, ORC_UPW_SWFS = 4 };
 enum { ORC_INTERP_COMP = 0, ORC_INTERP_CHAR = 1 };
 enum { ORC_BC_PERIODIC = 1, ORC_BC_EXTRAPOLATE = 2, ORC_BC_DIRICHLET = 3, ORC_BC_SLIP_WALL = 4,
        ORC_BC_NOSLIP_WALL = 5, ORC_BC_SUBSONIC_INFLOW = 6, ORC_BC_SUBSONIC_OUTFLOW = 7,

@@ -166,6 +166,15 @@ CASES = {
     "tgv12_comp_roe_par2_rk4": lambda: _par2(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05)),
     "rtb12_comp_rusanov_visc_par2": lambda: _par2(_visc(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
                                                                                perturb=0.02), 500.0)),
+    # Steger-Warming flux vector splitting (Euler1D, Euler2D), component-wise and
+    # characteristic; the Sod tube crosses Mach 1 nowhere, the stirred vortex does
+    "sod64_comp_swfs": lambda: C.sod(64, n_iter=20, dt=1e-3, upwinding="steger-warming"),
+    "sod64_char_swfs_ssprk3": lambda: C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                            upwinding="steger-warming", scheme="ssprk3"),
+    "vortex24_comp_swfs_rk4": lambda: C.vortex(24, n_iter=5, dt=0.02, interp="components",
+                                               upwinding="steger-warming", scheme="44"),
+    "vortex24_char_swfs_ssprk3": lambda: _boost(C.vortex(24, n_iter=5, dt=0.01, upwinding="steger-warming"),
+                                                1.0),
     # time_scheme euler (HyPar's default time integrator, TimeForwardEuler.c)
     "sod64_comp_roe_euler": lambda: C.sod(64, n_iter=20, dt=1e-3, scheme="euler"),
     "vortex24_char_llf_euler": lambda: C.vortex(24, n_iter=5, dt=0.01, upwinding="llf-char", scheme="euler"),
@@ -239,6 +248,19 @@ def _thermal(case, kind, vel, dim=2):
             arr = np.transpose(field, (1, 2, 0))  # [z, y, level]
         bcs[(dim, face)] = (kind, vel, ([0.0, 0.03], arr.reshape(-1)))
     case.bcs = bcs
+    return case
+
+
+def _boost(case, du):
+    """A 2-D deck with du added to every x-velocity at the same pressure (the vortex
+    then moves at Mach 0.5 to 2 across the grid)."""
+    u = case.u
+    rho = u[:, 0]
+    vx, vy = u[:, 1] / rho, u[:, 2] / rho
+    P = (u[:, 3] - 0.5 * rho * (vx * vx + vy * vy)) * (case.gamma - 1.0)
+    vx = vx + du
+    u[:, 1] = rho * vx
+    u[:, 3] = P / (case.gamma - 1.0) + 0.5 * rho * (vx * vx + vy * vy)
     return case
 
 

@@ -103,7 +103,7 @@ def test_reader_errors(built_lib, tmp_path):
     _expect(3, str(d))
     d = tmp_path / "g"
     case.write(str(d))
-    open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding steger-warming\nend\n")
+    open(d / "physics.inp", "w").write("begin\n gamma 1.4\n upwinding ausm\nend\n")
     _expect(4, str(d))
 
 

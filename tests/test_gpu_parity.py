@@ -39,8 +39,9 @@ def make(model, interp, upw, **kw):
 
 
 COMBOS = [(m, i, u) for m in ("euler1d", "euler2d", "navierstokes3d")
-          for i in ("components", "characteristic") for u in ("roe", "llf-char", "rf-char", "rusanov")
-          if not (m == "euler2d" and u == "rusanov")]
+          for i in ("components", "characteristic")
+          for u in ("roe", "llf-char", "rf-char", "rusanov", "steger-warming")
+          if not (m == "euler2d" and u == "rusanov") and not (m == "navierstokes3d" and u == "steger-warming")]
 
 
 def solver_for(case, tmp_path):

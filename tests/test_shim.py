@@ -75,6 +75,7 @@ DECKS = {
     "rtb_gravity_hb2": lambda: C.rising_thermal_bubble(12, n_iter=2),
     "stratified_euler1d_gravity": lambda: C.stratified_1d(32, n_iter=2, g=1.0, grav_type=0),
     "tgv_second_order_viscous": lambda: _with(C.tgv(12, n_iter=2, dt=0.02), par_scheme="2"),
+    "vortex_steger_warming_char": lambda: C.vortex(20, n_iter=2, dt=0.02, upwinding="steger-warming"),
     "sod_forward_euler": lambda: C.sod(48, n_iter=2, dt=1e-3, scheme="euler"),
     "vortex_sponges": lambda: _with(C.vortex(24, n_iter=2, dt=0.02), sponges=[
         (0, -1, [(6.0, 9.6), (-1.0, 11.0)], [1.1, 0.4, 0.05, 2.7]),
