@@ -556,6 +556,44 @@ __device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v,
   weno5_side_alt(wtype, BR1, BR2, BR3, tR, cR1, cB, cA, outR);
 }
 
+// One side of weno5_pair / weno5_pair_alt: the left-biased value on the five-point
+// stencil m0..m4 (the right-biased value of a window w0..w5 is this of the mirrored
+// stencil w5..w1), with Jiang-Shu weights or, when ALT, the formulation `wtype`.
+template <bool ALT>
+__device__ __forceinline__ double weno5_one_side(const double* m, double eps4, int wtype) {
+  const double k13 = 13.0 / 3.0;
+  const double d1 = fma(-2.0, m[1], m[0]) + m[2];
+  const double d2 = fma(-2.0, m[2], m[1]) + m[3];
+  const double d3 = fma(-2.0, m[3], m[2]) + m[4];
+  const double g1 = fma(3.0, m[2], fma(-4.0, m[1], m[0]));
+  const double g2 = m[1] - m[3];
+  const double g3 = fma(3.0, m[2], fma(-4.0, m[3], m[4]));
+  const double B1 = fma(k13 * d1, d1, fma(g1, g1, eps4));
+  const double B2 = fma(k13 * d2, d2, fma(g2, g2, eps4));
+  const double B3 = fma(k13 * d3, d3, fma(g3, g3, eps4));
+  const double c1 = fma(2.0, m[0], fma(-7.0, m[1], 11.0 * m[2]));
+  const double cA = fma(5.0, m[2], fma(2.0, m[3], -m[1]));
+  const double cB = fma(5.0, m[3], fma(2.0, m[2], -m[4]));
+  if (ALT) {
+    double t = 0.0;
+    if (wtype == WENO_W_BORGES) {
+      t = fabs(B1 - B3);
+    } else if (wtype == WENO_W_YC) {
+      const double e = d1 - 2.0 * d2 + d3;
+      t = 4.0 * (e * e);
+    }
+    const double s6 = 1.0 / 6.0;
+    double out;
+    weno5_side_alt(wtype, B1, B2, B3, t, c1 * s6, cA * s6, cB * s6, out);
+    return out;
+  }
+  const double q1 = B1 * B1, q2 = B2 * B2, q3 = B3 * B3;
+  const double a1 = q2 * q3, a2 = q1 * q3, a3 = q1 * q2;
+  const double n = fma(a1, c1, fma(6.0 * a2, cA, (3.0 * a3) * cB));
+  const double D = fma(36.0, a2, fma(18.0, a3, 6.0 * a1));
+  return n * nr_rcp(D);
+}
+
 // Normalised WENO5 weights of the left- and right-biased stencils of a six-point
 // window (Jiang-Shu, or the formulation `wtype` when ALT), for reconstructing other
 // values with the weights of this stencil (InterpolateInterfacesHyp with stored weights).

@@ -824,23 +824,28 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
 // Short 1-D lines (a Sod tube of 10^3 cells leaves one warp per SM, which then runs an
 // interface's several hundred FP64 instructions back to back): the interface work
 // split over lanes.  A block takes TI interfaces (TI - 1 cells) of the line in
-// groups of 8 lanes; phase 1 computes the TI + 5 cells into shared memory, phase 2
-// gives each of the 2 NV reconstructions of an interface (the f or the u pair of one
-// component: left- and right-biased values) to its own lane, phase 3 upwinds each
-// interface, phase 4 differences and updates each cell.  Component-wise WENO5 of a
-// model whose u-reconstruction reads u itself (Euler1D without gravity).
+// groups of 16 lanes; phase 1 computes the TI + 5 cells into shared memory, phase 2
+// gives each side (left- or right-biased value) of each of the 2 NV reconstructions of
+// an interface (the f or the u pair of one component) to its own lane, and the Roe
+// average of the interface's two cells to the next lane, phase 3 upwinds each
+// interface, phase 4 differences and updates each cell.  On GB300 an SM's FP64 unit
+// takes a warp instruction every 16 cycles, so the time of a short line is the length
+// of the longest dependent FP64 chain of a lane; splitting the pairs into sides and
+// moving the Roe average off the upwinding lane shortens it.  Component-wise WENO5 of
+// a model whose u-reconstruction reads u itself (Euler1D without gravity).
 template <int M, int UPW, bool ALTW, int TI>
-__global__ void __launch_bounds__(TI * 8)
+__global__ void __launch_bounds__(TI * 16)
 hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
                 PhysParams pp, StageEpi ep) {
   constexpr int NV = ModelTraits<M>::NV;
-  static_assert(2 * NV <= 8, "an interface's reconstructions fit a group of 8 lanes");
+  static_assert(4 * NV + 1 <= 16, "an interface's reconstruction sides fit a group of 16 lanes");
   constexpr bool CC = NeedCC<M, false, UPW>::value;
-  constexpr int TC = TI - 1, NCELL = TI + 5, NT = TI * 8;
+  constexpr int TC = TI - 1, NCELL = TI + 5, NT = TI * 16;
   __shared__ double su[NCELL][NV], sf[NCELL][NV];
   __shared__ CellAux<M> sax[NCELL];
   __shared__ double srec[TI][2 * NV][2];
   __shared__ double sfI[TI][NV];
+  __shared__ Eig secc[TI];
   const int I0 = (int)blockIdx.x * TC;
   const int N = G.dim[0];
   const long long sd = G.stride[0];
@@ -870,18 +875,21 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
   }
   __syncthreads();
   {
-    const int i = t >> 3, k = t & 7;
-    if (k < 2 * NV && I0 + i <= N) {
-      const int v = k >> 1;
-      // the window relative to the interface's left cell (window cell 2)
-      double w[6];
+    const int i = t >> 4, k = t & 15;
+    if (k < 4 * NV && I0 + i <= N) {
+      // lane k: component v, the u (bit 1) or f reconstruction, its right (bit 0) or
+      // left side; the window relative to the interface's left cell (window cell 2),
+      // mirrored for the right side
+      const int v = k >> 2, isu = (k >> 1) & 1, right = k & 1;
+      double m[5];
 #pragma unroll
-      for (int p = 0; p < 6; p++)
-        w[p] = p == 2 ? 0.0 : ((k & 1) ? su[i + p][v] - su[i + 2][v] : sf[i + p][v] - sf[i + 2][v]);
-      double oL, oR;
-      wpair<ALTW, true>(w, w, eps4, pp.wtype, oL, oR);
-      srec[i][k][0] = oL;
-      srec[i][k][1] = oR;
+      for (int p = 0; p < 5; p++) {
+        const int c = i + (right ? 5 - p : p);
+        m[p] = c == i + 2 ? 0.0 : (isu ? su[c][v] - su[i + 2][v] : sf[c][v] - sf[i + 2][v]);
+      }
+      srec[i][2 * v + isu][right] = weno5_one_side<ALTW>(m, eps4, pp.wtype);
+    } else if (CC && k == 4 * NV && I0 + i <= N) {
+      secc[i] = roe_eig<M, 0>(sax[i + 2].rs, sax[i + 3].rs, pp);
     }
   }
   __syncthreads();
@@ -895,7 +903,7 @@ hyp_lane_kernel(const double* __restrict__ U, double* __restrict__ H, const doub
       uR[v] = srec[t][2 * v + 1][1];
     }
     Eig Ecc;
-    if (CC) Ecc = roe_eig<M, 0>(sax[t + 2].rs, sax[t + 3].rs, pp);
+    if (CC) Ecc = secc[t];
     double uc2[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) uc2[v] = su[t + 2][v];
@@ -1119,11 +1127,11 @@ cudaError_t launch_dir(const double* U, double* H, const double* dxinv_dir, cons
   int N = G.dim[DIR];
   if constexpr (M == MODEL_EULER1D && !CHAR && !GRAV && !WT) {
     if (L.seg == -8 || L.seg == -16) {
-      // lane groups: TI interfaces of the one line per block, 8 lanes per interface
+      // lane groups: TI interfaces of the one line per block, 16 lanes per interface
       const int ti = -L.seg;
       const unsigned nblk = (unsigned)((N + ti - 2) / (ti - 1));
-      if (ti == 8) hyp_lane_kernel<M, UPW, ALTW, 8><<<nblk, 64, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
-      else hyp_lane_kernel<M, UPW, ALTW, 16><<<nblk, 128, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
+      if (ti == 8) hyp_lane_kernel<M, UPW, ALTW, 8><<<nblk, 128, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
+      else hyp_lane_kernel<M, UPW, ALTW, 16><<<nblk, 256, 0, s>>>(U, H, dxinv_dir, G, pp, ep);
       return cudaGetLastError();
     }
   }
