@@ -345,7 +345,7 @@ int gbh_validate(const gb_config* c) {
   if (c->ndims != nd || c->nvars != nd + 2) { gbh_set_error("ndims/nvars do not match the model"); return GB_ERR_ARG; }
   if (c->ghosts != 3) { gbh_set_error("ghosts must be 3"); return GB_ERR_ARG; }
   for (int d = 0; d < nd; d++)
-    if (c->dim[d] < 4) { gbh_set_error("dim[%d] = %d < 4", d, c->dim[d]); return GB_ERR_ARG; }
+    if (c->dim[d] < 3) { gbh_set_error("dim[%d] = %d < 3", d, c->dim[d]); return GB_ERR_ARG; }
   if (c->interp != GB_INTERP_COMPONENTS && c->interp != GB_INTERP_CHARACTERISTIC) { gbh_set_error("bad interp"); return GB_ERR_ARG; }
   if (c->upwind < 0 || c->upwind > 4) { gbh_set_error("bad upwind"); return GB_ERR_ARG; }
   if (c->upwind == GB_UPWIND_RUSANOV && c->model == GB_MODEL_EULER2D) {

@@ -652,8 +652,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
   c.ghosts = si.ghosts;
   for (int d = 0; d < 3; d++) c.dim[d] = d < c.ndims ? si.size[d] : 1;
   for (int d = 0; d < c.ndims; d++) {
-    if (c.dim[d] < 4) {
-      gbh_set_error("size along dimension %d is %d (at least 4 needed)", d, c.dim[d]);
+    /* three points are the fewest whose ghost layers (3 deep) the boundaries fill from
+     * interior points: the quasi-2-D NavierStokes3D decks run with 3 along z */
+    if (c.dim[d] < 3) {
+      gbh_set_error("size along dimension %d is %d (at least 3 needed)", d, c.dim[d]);
       return GB_ERR_INPUT;
     }
     if (si.iproc[d] > 1) fprintf(stderr, "gbhypar: iproc %d along dimension %d ignored (one GPU holds the whole domain)\n", si.iproc[d], d);

@@ -175,6 +175,11 @@ CASES = {
                                                upwinding="steger-warming", scheme="44"),
     "vortex24_char_swfs_ssprk3": lambda: _boost(C.vortex(24, n_iter=5, dt=0.01, upwinding="steger-warming"),
                                                 1.0),
+    # three points along one dimension (the quasi-2-D NavierStokes3D decks run with
+    # size N M 3): ghost layers as deep as the line, every ghost a folded interior point
+    "tgv12x12x3_comp_roe_rk4": lambda: _slab(C.tgv(12, n_iter=3, dt=0.02, perturb=0.05), 2, 3),
+    "rtb12x12x3_comp_rusanov_yc": lambda: _slab(C.rising_thermal_bubble(12, n_iter=3, dt=0.05, perturb=0.02), 2, 3),
+    "vortex24x3_char_roe_ssprk3": lambda: _slab(C.vortex(24, n_iter=5, dt=0.02), 1, 3, start=11),
     # time_scheme euler (HyPar's default time integrator, TimeForwardEuler.c)
     "sod64_comp_roe_euler": lambda: C.sod(64, n_iter=20, dt=1e-3, scheme="euler"),
     "vortex24_char_llf_euler": lambda: C.vortex(24, n_iter=5, dt=0.01, upwinding="llf-char", scheme="euler"),
@@ -210,6 +215,20 @@ def _turb(case, dim=0, nslices=64, speed=2.0, seed=17):
     vel[dim] = speed
     case.bcs = {(dim, 1): ("turbulent-supersonic-inflow", [1.0] + vel + [1.0 / 1.4], (nslices, data.reshape(-1))),
                 (dim, -1): ("supersonic-outflow", [])}
+    return case
+
+
+def _slab(case, dim, n, start=0):
+    """n grid planes of a deck along dimension dim, from plane `start`."""
+    shape = [s for s in reversed(case.size)] + [case.nvars]
+    u = case.u.reshape(shape)
+    sl = [slice(None)] * len(shape)
+    sl[len(case.size) - 1 - dim] = slice(start, start + n)
+    case.u = np.ascontiguousarray(u[tuple(sl)]).reshape(-1, case.nvars)
+    case.size = list(case.size)
+    case.size[dim] = n
+    case.x = list(case.x)
+    case.x[dim] = np.asarray(case.x[dim])[start:start + n]
     return case
 
 
