@@ -24,10 +24,10 @@ cudaError_t launch_hyp_euler2d_w(int, int, int, const double*, double*, const do
                                  const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_w(int, int, int, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
-cudaError_t launch_hyp_crweno(int, int, int, bool, const double*, double*, const double*, const DevGeom&,
+cudaError_t launch_hyp_crweno(int, int, int, bool, bool, const double*, double*, const double*, const DevGeom&,
                               const PhysParams&, const StageEpi&, const HypLaunch&, double*, double*, double*,
                               cudaStream_t);
-size_t crweno_scratch_doubles(int, int, long long, bool, bool);
+size_t crweno_scratch_doubles(int, int, long long, bool, bool, bool);
 cudaError_t launch_hyp_euler1d_grav(int, int, int, const double*, double*, const double*, const DevGeom&,
                                    const PhysParams&, const StageEpi&, const HypLaunch&, cudaStream_t);
 cudaError_t launch_hyp_ns3d_grav(int, int, const double*, double*, const double*, const DevGeom&,
@@ -122,11 +122,11 @@ static int prof_drain(gb_solver* s) {
 static cudaError_t launch_hyp(gb_solver* s, int dir, const double* U, const StageEpi& ep) {
   const gb_config& c = s->cfg;
   const double* dx = s->d_dxinv + s->dx_off[dir];
+  if (s->gravity && !s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
   if (c.hyp_scheme == GB_SCHEME_CRWENO5)
-    return launch_hyp_crweno(c.model, dir, c.upwind, c.interp == GB_INTERP_CHARACTERISTIC, U, s->d_H, dx, s->G,
-                             s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->d_crF, s->stream);
+    return launch_hyp_crweno(c.model, dir, c.upwind, c.interp == GB_INTERP_CHARACTERISTIC, s->gravity, U, s->d_H,
+                             dx, s->G, s->pp, ep, s->hl[dir], s->d_crX, s->d_crC, s->d_crF, s->stream);
   if (s->gravity) {
-    if (!s->d_grav) return cudaErrorInvalidValue;  // gb_solver_set_gravity_field not called (checked by callers)
     if (c.model == GB_MODEL_EULER1D)
       return launch_hyp_euler1d_grav(dir, c.interp, c.upwind, U, s->d_H, dx, s->G, s->pp, ep, s->hl[dir],
                                      s->stream);
@@ -363,7 +363,6 @@ int gbh_validate(const gb_config* c) {
   if (c->hyp_scheme != GB_SCHEME_WENO5 && c->hyp_scheme != GB_SCHEME_CRWENO5) { gbh_set_error("bad hyp_scheme"); return GB_ERR_ARG; }
   if (c->gravity[0] != 0.0 || c->gravity[1] != 0.0 || c->gravity[2] != 0.0) {
     if (c->model == GB_MODEL_EULER2D) { gbh_set_error("gravity: Euler2D has none"); return GB_ERR_UNSUPPORTED; }
-    if (c->hyp_scheme == GB_SCHEME_CRWENO5) { gbh_set_error("gravity with CRWENO5 is not available on this path"); return GB_ERR_UNSUPPORTED; }
     if (c->model == GB_MODEL_EULER1D) {
       if (c->upwind != GB_UPWIND_ROE && c->upwind != GB_UPWIND_LLF) {
         gbh_set_error("flows with gravity need roe or llf-char upwinding (Euler1DInitialize.c:144)");
@@ -396,8 +395,8 @@ int gbh_validate(const gb_config* c) {
       if (!empty && !inside) { gbh_set_error("sponge zone %d must cover interior points only", z); return GB_ERR_ARG; }
       continue;
     }
-    if (q[0] > GB_BC_DIRICHLET && q[0] != GB_BC_REFLECT && nd < 2) {
-      gbh_set_error("zone %d: wall / inflow / outflow boundaries need Euler2D or NavierStokes3D", z);
+    if (q[0] > GB_BC_DIRICHLET && q[0] != GB_BC_REFLECT && q[0] != GB_BC_SLIP_WALL && nd < 2) {
+      gbh_set_error("zone %d: inflow / outflow / no-slip boundaries need Euler2D or NavierStokes3D", z);
       return GB_ERR_UNSUPPORTED;
     }
     if ((q[0] == GB_BC_THERMAL_SLIP_WALL || q[0] == GB_BC_THERMAL_NOSLIP_WALL) && c->model != GB_MODEL_NS3D) {
@@ -525,8 +524,8 @@ extern "C" int gb_solver_create(const gb_config* cfg, const double* dxinv, int d
       long long lines = 1;
       for (int e = 0; e < c.ndims; e++)
         if (e != d) lines *= c.dim[e];
-      size_t a = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, false);
-      size_t b = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, true);
+      size_t a = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, false, s->gravity);
+      size_t b = crweno_scratch_doubles(c.nvars, c.dim[d] + 1, lines, chr, true, s->gravity);
       nx = a > nx ? a : nx;
       nc = b > nc ? b : nc;
     }

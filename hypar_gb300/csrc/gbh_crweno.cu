@@ -29,6 +29,9 @@
 //                     upwind flux of each interface from the solved values and the
 //                     cell-centre states, the flux difference and the stage epilogue.
 //
+// With gravity two more reconstructions, sL and sR of the source function with the
+// flux's weights, feed the well-balanced source term in cr_flux_kernel.
+//
 // Layout of the interface values (and of the elimination scratch):
 // [interface I][reconstruction k][component v][line], so that the threads of a
 // warp, which take consecutive lines, read and write consecutive addresses.
@@ -119,16 +122,49 @@ __device__ __forceinline__ long long line_base(const DevGeom& G, long long tr) {
   return pbase;
 }
 
+// The modified solution's last component at a point with gravity (the other components
+// are u f): Euler1D u_E / S (Euler1DModifiedSolution.c:48, f = 1 / S), NavierStokes3D
+// P / (gamma - 1) / g + f rho |v|^2 / 2 (NavierStokes3DModifiedSolution.c:52-66).
+template <int M>
+__device__ __forceinline__ double grav_ufunc_last(const double* uu, const Prim<M>& q, double f, double g,
+                                                  const PhysParams& pp) {
+  constexpr int NV = ModelTraits<M>::NV;
+  if (M == MODEL_EULER1D) return uu[NV - 1] * f;
+  const double vsq = q.vel[0] * q.vel[0] + q.vel[1] * q.vel[1] + q.vel[2] * q.vel[2];
+  return fma(q.P * pp.inv_gm1, nr_rcp(g), (0.5 * q.rho * vsq) * f);
+}
+
 // The quantity thread (k, v) reconstructs at a cell, and the one its weights see:
 // the cell flux component (read from F, the fluxes of this direction computed once
 // per point), or the state component and, for the NavierStokes3D energy, the
-// modified solution's energy.
-template <int M, int DIR>
+// modified solution's energy.  GRAV: the u values are the modified solution with
+// gravity, and k = 4, 5 reconstruct the source function [0, g e_DIR, g] (g the
+// gravity field at the point) with the weights of the flux component.
+template <int M, int DIR, bool GRAV>
 __device__ __forceinline__ void cr_cell(const double* __restrict__ src, const double* __restrict__ fsrc, int k,
-                                        int v, const PhysParams& pp, double& val, double& wv) {
+                                        int v, const PhysParams& pp, long long pt, double& val, double& wv) {
   constexpr int NV = ModelTraits<M>::NV;
   if (k < 2) {
     val = wv = fsrc[v];
+  } else if (GRAV && k >= 4) {
+    wv = fsrc[v];
+    val = (v == 1 + DIR || v == NV - 1) ? pp.gg[pt] : 0.0;
+  } else if (GRAV) {
+    double uu[NV];
+#pragma unroll
+    for (int e = 0; e < NV; e++) uu[e] = src[e];
+    double x = uu[0];
+#pragma unroll
+    for (int e = 1; e < NV; e++)
+      if (v == e) x = uu[e];
+    wv = x;
+    const double f = pp.gf[pt];
+    if (v == NV - 1) {
+      Prim<M> q = to_prim<M>(uu, pp);
+      val = grav_ufunc_last<M>(uu, q, f, pp.gg[pt], pp);
+    } else {
+      val = x * f;
+    }
   } else {
     double uu[NV];
 #pragma unroll
@@ -148,12 +184,12 @@ __device__ __forceinline__ void cr_cell(const double* __restrict__ src, const do
   }
 }
 
-template <int M, int DIR, bool ALTW>
+template <int M, int DIR, bool ALTW, bool GRAV>
 __global__ void __launch_bounds__(128)
 cr_solve_kernel(const double* __restrict__ U, const double* __restrict__ F, DevGeom G, PhysParams pp,
                 double* __restrict__ X, double* __restrict__ Cp, long long ntrans) {
-  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
-  const long long nsys = ntrans * 4 * NV;
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND, R = GRAV ? 6 : 4;
+  const long long nsys = ntrans * R * NV;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= nsys) return;
   const long long line = tid % ntrans;
@@ -171,7 +207,7 @@ cr_solve_kernel(const double* __restrict__ U, const double* __restrict__ F, DevG
   double wval[6], wwv[6];
   auto load = [&](int i, int slot) {
     const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
-    cr_cell<M, DIR>(U + pt * NV, F + pt * NV, k, v, pp, wval[slot], wwv[slot]);
+    cr_cell<M, DIR, GRAV>(U + pt * NV, F + pt * NV, k, v, pp, pt, wval[slot], wwv[slot]);
   };
 #pragma unroll
   for (int p = 0; p < 5; p++) load(p - 3, p + 1);
@@ -244,28 +280,34 @@ cr_solve_kernel(const double* __restrict__ U, const double* __restrict__ F, DevG
 // interface (nvars^2 + nvars doubles, [interface][entry][system] for coalescing),
 // then F_I = y'_I - C'_I F_{I+1}
 // backwards into X in the component-wise layout, which cr_flux_kernel reads.
-template <int M, int DIR, bool ALTW>
+// GRAV: the u values are the modified solution with gravity, and reconstructions
+// k = 4, 5 solve for the source function [0, g e_DIR, g] with the flux's weights
+// (the same blocks as k = 0, 1, another right-hand side).
+template <int M, int DIR, bool ALTW, bool GRAV>
 __global__ void __launch_bounds__(64)
 cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, double* __restrict__ X,
                      double* __restrict__ S, long long ntrans) {
-  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND, NE = NV * NV + NV;
-  const long long nsys = ntrans * 4;
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND, NE = NV * NV + NV, R = GRAV ? 6 : 4;
+  const long long nsys = ntrans * R;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= nsys) return;
   const long long line = tid % ntrans;
   const int k = (int)(tid / ntrans);
-  const bool left = (k % 2) == 0, fx = k < 2;
+  const bool sx = GRAV && k >= 4;
+  const bool left = (k % 2) == 0, fx = k < 2 || sx;
   const long long pbase = line_base<ND, DIR>(G, line);
   const int N = G.dim[DIR];
   const long long sd = G.stride[DIR];
   const int lo = G.bclo[DIR], hi = G.bchi[DIR];
   const double eps4 = 4.0 * pp.eps;
   const double s6 = 1.0 / 6.0;
-  const long long nX = ntrans * 4 * NV;
+  const long long nX = ntrans * R * NV;
 
   // window of cells I-3 .. I+2: the weights' quantity (f or u), the modified energy
-  // (u reconstructions of NavierStokes3D), and the Roe-average ingredients
-  double wq[6][NV], wE[6];
+  // (u reconstructions of NavierStokes3D; with GRAV of both models) or the gravity
+  // field (source reconstructions), the modified solution's factor f (GRAV), and the
+  // Roe-average ingredients
+  double wq[6][NV], wE[6], wF[6];
   RoeSide rs[6];
   auto load = [&](int i, int slot) {
     const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
@@ -280,7 +322,12 @@ cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, dou
 #pragma unroll
       for (int e = 0; e < NV; e++) wq[slot][e] = uu[e];
     }
-    wE[slot] = (!fx && M == MODEL_NS3D) ? ufunc_energy<M>(q, pp, uu[NV - 1]) : wq[slot][NV - 1];
+    if (GRAV) {
+      wF[slot] = pp.gf[pt];
+      wE[slot] = sx ? pp.gg[pt] : (fx ? wq[slot][NV - 1] : grav_ufunc_last<M>(uu, q, wF[slot], pp.gg[pt], pp));
+    } else {
+      wE[slot] = (!fx && M == MODEL_NS3D) ? ufunc_energy<M>(q, pp, uu[NV - 1]) : wq[slot][NV - 1];
+    }
   };
 #pragma unroll
   for (int p = 0; p < 5; p++) load(p - 3, p + 1);
@@ -298,6 +345,7 @@ cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, dou
 #pragma unroll
       for (int e = 0; e < NV; e++) wq[p][e] = wq[p + 1][e];
       wE[p] = wE[p + 1];
+      if (GRAV) wF[p] = wF[p + 1];
       rs[p] = rs[p + 1];
     }
     load(I + 2, 5);
@@ -309,7 +357,18 @@ cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, dou
     for (int m = 0; m < 5; m++) {
       const int slot = left ? m : 5 - m;
       projL<M, DIR>(E, pp, wq[slot], pw[m]);
-      if (!fx && M == MODEL_NS3D) {
+      if (GRAV && sx) {
+        double t[NV];
+#pragma unroll
+        for (int e = 0; e < NV; e++) t[e] = (e == 1 + DIR || e == NV - 1) ? wE[slot] : 0.0;
+        projL<M, DIR>(E, pp, t, pv[m]);
+      } else if (GRAV && !fx) {
+        double t[NV];
+#pragma unroll
+        for (int e = 0; e < NV - 1; e++) t[e] = wq[slot][e] * wF[slot];
+        t[NV - 1] = wE[slot];
+        projL<M, DIR>(E, pp, t, pv[m]);
+      } else if (!fx && M == MODEL_NS3D) {
         double t[NV];
 #pragma unroll
         for (int e = 0; e < NV; e++) t[e] = wq[slot][e];
@@ -470,11 +529,17 @@ cr_char_solve_kernel(const double* __restrict__ U, DevGeom G, PhysParams pp, dou
   }
 }
 
-template <int M, int UPW, int DIR>
+// GRAV: the dissipation scaled by max(g_L, g_R) of the gravity field (Euler1DUpwind.c:79-82,
+// NavierStokes3DUpwind.c:407) and, along a direction with gravity, the well-balanced
+// source term (Euler1DSource.c:58-76, NavierStokes3DSource.c:73-101): the average of
+// the source function's left and right values (SourceUpwind) differenced per cell and
+// scaled by [0, rho RT e_DIR, rho RT v_DIR] f (RT = 1, f = 1 / S for Euler1D), subtracted
+// from this direction's term.
+template <int M, int UPW, int DIR, bool GRAV>
 __global__ void __launch_bounds__(128)
 cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const double* __restrict__ dxinv, DevGeom G,
                PhysParams pp, StageEpi ep, const double* __restrict__ X, int seg, int nseg, long long ntrans) {
-  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
+  constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND, R = GRAV ? 6 : 4;
   constexpr bool CC = NeedCC<M, false, UPW>::value;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tid >= ntrans * (long long)nseg) return;
@@ -486,9 +551,11 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
   const int lo = G.bclo[DIR], hi = G.bchi[DIR];
   const int I0 = sg * seg;
   const int I1 = min(I0 + seg, N);
-  const long long nsys = ntrans * 4 * NV;
+  const long long nsys = ntrans * R * NV;
+  const bool src_dir = GRAV && pp.grav[DIR] != 0.0 && (ep.mode != EPI_HYP || ep.with_source);
 
-  auto aux = [&](int i) {
+  // gL, gR: the gravity field at the interface's two cells (GRAV)
+  auto aux = [&](int i, double& gv) {
     CellAux<M> a;
     const long long pt = pbase + (long long)fold_index(i, N, lo, hi) * sd;
     double uu[NV];
@@ -498,12 +565,16 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
     if (CC) a.rs = roe_side<M>(q);
     if (UPW == UPW_RUS) a.c = rusanov_speed<M, DIR>(q, pp);
     else if (M == MODEL_EULER1D && UPW != UPW_ROE) a.c = sound_speed<M>(q, pp);
+    if (GRAV) gv = pp.gg[pt];
     return a;
   };
-  CellAux<M> axL = aux(I0 - 1);
-  double fIp[NV];
+  double gL = 1.0, gR = 1.0;
+  CellAux<M> axL = aux(I0 - 1, gL);
+  double fIp[NV], SI[NV], SIp[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) SI[v] = SIp[v] = 0.0;
   for (int I = I0; I <= I1; I++) {
-    const CellAux<M> axR = aux(I);
+    const CellAux<M> axR = aux(I, gR);
     double fL[NV], fR[NV], uL[NV], uR[NV];
     const double* q = X + (long long)I * nsys + line;
 #pragma unroll
@@ -512,39 +583,56 @@ cr_flux_kernel(const double* __restrict__ U, double* __restrict__ H, const doubl
       fR[v] = q[(1 * NV + v) * ntrans];
       uL[v] = q[(2 * NV + v) * ntrans];
       uR[v] = q[(3 * NV + v) * ntrans];
+      if (src_dir) SI[v] = 0.5 * (q[(4 * NV + v) * ntrans] + q[(5 * NV + v) * ntrans]);
     }
     Eig Ecc;
     if (CC) Ecc = roe_eig<M, DIR>(axL.rs, axR.rs, pp);
     double fI[NV];
-    upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, axL, axR, pp, fI);
+    upwind_iface<M, false, UPW, DIR>(fL, fR, uL, uR, Ecc, axL, axR, pp, fI, GRAV ? fmax(gL, gR) : 1.0);
     boundary_flux<NV>(ep, I, N, line, ntrans, fI);
     if (I > I0) {
       const int c = I - 1;
-      const long long off = (pbase + (long long)c * sd) * NV;
+      const long long pc = pbase + (long long)c * sd, off = pc * NV;
       const double dxi = dxinv[G.g + c];
       double h[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) h[v] = dxi * (fI[v] - fIp[v]);
+      if (src_dir) {
+        // [0, rho RT e_DIR, rho RT v_DIR] f of the cell, as the fused WENO5 kernel
+        const double rho = U[off], rRT = rho * pp.RT, f = pp.gf[pc];
+        const double vd = rho == 0.0 ? 0.0 : U[off + 1 + DIR] * nr_rcp(rho);
+        double term[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) term[v] = 0.0;
+        term[1 + DIR] = rRT * f;
+        term[NV - 1] = (rRT * vd) * f;
+#pragma unroll
+        for (int v = 0; v < NV; v++) h[v] = fma(-term[v] * (SI[v] - SIp[v]), dxi, h[v]);  // rhs = -hyp + source
+      }
       stage_epilogue<NV>(ep, H, off, h);
     }
 #pragma unroll
-    for (int v = 0; v < NV; v++) fIp[v] = fI[v];
+    for (int v = 0; v < NV; v++) {
+      fIp[v] = fI[v];
+      SIp[v] = SI[v];
+    }
     axL = axR;
+    gL = gR;
   }
 }
 
-template <int M, int DIR, bool ALTW, int UPW>
+template <int M, int DIR, bool ALTW, int UPW, bool GRAV = false>
 static cudaError_t cr_dir(bool chr, const double* U, double* H, const double* dxinv_dir, const DevGeom& G,
                           const PhysParams& pp, const StageEpi& ep, const HypLaunch& L, double* X, double* Cp,
                           double* Fc, cudaStream_t s) {
-  constexpr int NV = ModelTraits<M>::NV;
+  constexpr int NV = ModelTraits<M>::NV, R = GRAV ? 6 : 4;
   long long ntrans = 1;
   for (int e = 0; e < G.nd; e++)
     if (e != DIR) ntrans *= G.dim[e];
-  const long long nsys = ntrans * 4 * NV;
+  const long long nsys = ntrans * R * NV;
   if (chr) {
-    const long long nchr = ntrans * 4;
-    cr_char_solve_kernel<M, DIR, ALTW><<<(unsigned)((nchr + 63) / 64), 64, 0, s>>>(U, G, pp, X, Cp, ntrans);
+    const long long nchr = ntrans * R;
+    cr_char_solve_kernel<M, DIR, ALTW, GRAV><<<(unsigned)((nchr + 63) / 64), 64, 0, s>>>(U, G, pp, X, Cp, ntrans);
   } else {
     // the cell fluxes of this direction once per point, then the solves
     long long npts = 1;
@@ -552,7 +640,7 @@ static cudaError_t cr_dir(bool chr, const double* U, double* H, const double* dx
     flux_kernel<M, DIR><<<(unsigned)((npts + 127) / 128), 128, 0, s>>>(Fc, U, npts, pp);
     cudaError_t e0 = cudaGetLastError();
     if (e0 != cudaSuccess) return e0;
-    cr_solve_kernel<M, DIR, ALTW><<<(unsigned)((nsys + 127) / 128), 128, 0, s>>>(U, Fc, G, pp, X, Cp, ntrans);
+    cr_solve_kernel<M, DIR, ALTW, GRAV><<<(unsigned)((nsys + 127) / 128), 128, 0, s>>>(U, Fc, G, pp, X, Cp, ntrans);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -560,8 +648,8 @@ static cudaError_t cr_dir(bool chr, const double* U, double* H, const double* dx
   const int nseg = (G.dim[DIR] + seg - 1) / seg;
   const long long nthr = ntrans * nseg;
   const int block = L.block > 0 ? L.block : 128;
-  cr_flux_kernel<M, UPW, DIR><<<(unsigned)((nthr + block - 1) / block), block, 0, s>>>(U, H, dxinv_dir, G, pp, ep, X,
-                                                                                     seg, nseg, ntrans);
+  cr_flux_kernel<M, UPW, DIR, GRAV><<<(unsigned)((nthr + block - 1) / block), block, 0, s>>>(U, H, dxinv_dir, G, pp,
+                                                                                           ep, X, seg, nseg, ntrans);
   return cudaGetLastError();
 }
 
@@ -593,20 +681,55 @@ static cudaError_t cr_model(bool chr, int dir, int upw, const double* U, double*
   return cudaErrorInvalidValue;
 }
 
-// Scratch per direction (doubles): X holds (N+1) * lines * 4 * nvars interface values;
-// the second array the elimination: (N+1) * lines * 4 * nvars (component-wise) or
-// (N+1) * lines * 4 * (nvars^2 + nvars) (characteristic).
-size_t crweno_scratch_doubles(int nvars, int n_interfaces, long long lines, bool chr, bool second) {
-  if (!second || !chr) return (size_t)n_interfaces * (size_t)lines * 4 * (size_t)nvars;
-  return (size_t)n_interfaces * (size_t)lines * 4 * (size_t)(nvars * nvars + nvars);
+// With gravity: Euler1D (Roe, LLF) and NavierStokes3D (Rusanov, the only upwinding the
+// reference allows with gravity), any direction.
+template <int M, bool ALTW>
+static cudaError_t cr_model_grav(bool chr, int dir, int upw, const double* U, double* H, const double* dx,
+                                 const DevGeom& G, const PhysParams& pp, const StageEpi& ep, const HypLaunch& L,
+                                 double* X, double* Cp, double* Fc, cudaStream_t s) {
+  if constexpr (M == MODEL_EULER1D) {
+    if (dir != 0) return cudaErrorInvalidValue;
+    if (upw == UPW_LLF) return cr_dir<M, 0, ALTW, UPW_LLF, true>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    if (upw == UPW_ROE) return cr_dir<M, 0, ALTW, UPW_ROE, true>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    return cudaErrorInvalidValue;
+  } else if constexpr (M == MODEL_NS3D) {
+    if (upw != UPW_RUS) return cudaErrorInvalidValue;
+    if (dir == 0) return cr_dir<M, 0, ALTW, UPW_RUS, true>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    if (dir == 1) return cr_dir<M, 1, ALTW, UPW_RUS, true>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    if (dir == 2) return cr_dir<M, 2, ALTW, UPW_RUS, true>(chr, U, H, dx, G, pp, ep, L, X, Cp, Fc, s);
+    return cudaErrorInvalidValue;
+  } else {
+    return cudaErrorInvalidValue;  // Euler2D has no gravity
+  }
 }
 
-// One direction of the hyperbolic term with CRWENO5, component-wise or characteristic.
+// Scratch per direction (doubles), with R = 4 reconstructions (6 with gravity: the
+// source function's two): X holds (N+1) * lines * R * nvars interface values; the
+// second array the elimination: (N+1) * lines * R * nvars (component-wise) or
+// (N+1) * lines * R * (nvars^2 + nvars) (characteristic).
+size_t crweno_scratch_doubles(int nvars, int n_interfaces, long long lines, bool chr, bool second, bool grav) {
+  const size_t R = grav ? 6 : 4;
+  if (!second || !chr) return (size_t)n_interfaces * (size_t)lines * R * (size_t)nvars;
+  return (size_t)n_interfaces * (size_t)lines * R * (size_t)(nvars * nvars + nvars);
+}
+
+// One direction of the hyperbolic term with CRWENO5, component-wise or characteristic,
+// with gravity when `grav` (pp's gravity fields set).
 // Fc: a ghosted state-sized array for the cell fluxes (component-wise form).
-cudaError_t launch_hyp_crweno(int model, int dir, int upw, bool chr, const double* U, double* H,
+cudaError_t launch_hyp_crweno(int model, int dir, int upw, bool chr, bool grav, const double* U, double* H,
                               const double* dxinv_dir, const DevGeom& G, const PhysParams& pp, const StageEpi& ep,
                               const HypLaunch& L, double* X, double* Cp, double* Fc, cudaStream_t s) {
   const bool alt = pp.wtype != WENO_W_JS;
+  if (grav) {
+    if (!pp.gf || !pp.gg) return cudaErrorInvalidValue;
+    if (model == MODEL_EULER1D)
+      return alt ? cr_model_grav<MODEL_EULER1D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s)
+                 : cr_model_grav<MODEL_EULER1D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s);
+    if (model == MODEL_NS3D)
+      return alt ? cr_model_grav<MODEL_NS3D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s)
+                 : cr_model_grav<MODEL_NS3D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s);
+    return cudaErrorInvalidValue;
+  }
   if (model == MODEL_EULER1D)
     return alt ? cr_model<MODEL_EULER1D, true>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s)
                : cr_model<MODEL_EULER1D, false>(chr, dir, upw, U, H, dxinv_dir, G, pp, ep, L, X, Cp, Fc, s);

@@ -750,10 +750,6 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
                   "steger-warming for Euler1D / Euler2D)", upw);
     return GB_ERR_UNSUPPORTED;
   }
-  if ((c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) && c.hyp_scheme == GB_SCHEME_CRWENO5) {
-    gbh_set_error("gravity with CRWENO5 is not available on this path");
-    return GB_ERR_UNSUPPORTED;
-  }
   if (c.model == GB_MODEL_NS3D && (c.gravity[0] != 0.0 || c.gravity[1] != 0.0 || c.gravity[2] != 0.0) &&
       c.upwind != GB_UPWIND_RUSANOV) {
     /* NavierStokes3DInitialize.c:370-378 */
@@ -944,7 +940,10 @@ int gb_inputs_read_member(const char *dir, int member, int nsims, gb_inputs **ou
         gbh_set_error("boundary.inp: zone %d (%s) lacks its values", z, type);
         return GB_ERR_INPUT;
       }
-      if (tcode > GB_BC_DIRICHLET && tcode != GB_BC_SPONGE && tcode != GB_BC_REFLECT && c.ndims < 2) {
+      /* BCSlipWall.c has a 1-D branch (Euler1D); the other wall and inflow / outflow
+       * types have 2-D and 3-D ones only */
+      if (tcode > GB_BC_DIRICHLET && tcode != GB_BC_SPONGE && tcode != GB_BC_REFLECT && tcode != GB_BC_SLIP_WALL &&
+          c.ndims < 2) {
         fclose(in);
         gb_inputs_free(res);
         gbh_set_error("boundary type %s needs Euler2D or NavierStokes3D", type);

@@ -376,8 +376,23 @@ __global__ void bc_zone_kernel(double* u, DevGeom G, int nv, ZoneDev z) {
       fl = z.tfield + q * nv + 1;
     }
     double g[5];
-    if (G.nd == 2) bc_ghost<2>(z, u + p2 * nv, g, inflow, Tb, fl);
-    else bc_ghost<3>(z, u + p2 * nv, g, inflow, Tb, fl);
+    if (G.nd == 1) {
+      // BCSlipWall.c:38-76 (Euler1D, the one wall type with a 1-D branch): density and
+      // pressure extrapolated, the velocity mirrored about the wall's, in the 1-D flow
+      // variables' operation order
+      const double* w = u + p2 * nv;
+      const double gm1 = z.gamma - 1.0, inv_gm1 = __ddiv_rn(1.0, gm1);
+      const double rho = w[0], vel = __ddiv_rn(w[1], rho);
+      const double P = __dmul_rn(__dsub_rn(w[2], __dmul_rn(__dmul_rn(__dmul_rn(0.5, rho), vel), vel)), gm1);
+      const double vg = __dsub_rn(__dmul_rn(2.0, z.data[0]), vel);
+      g[0] = rho;
+      g[1] = __dmul_rn(rho, vg);
+      g[2] = __dadd_rn(__dmul_rn(inv_gm1, P), __dmul_rn(__dmul_rn(__dmul_rn(0.5, rho), vg), vg));
+    } else if (G.nd == 2) {
+      bc_ghost<2>(z, u + p2 * nv, g, inflow, Tb, fl);
+    } else {
+      bc_ghost<3>(z, u + p2 * nv, g, inflow, Tb, fl);
+    }
     for (int v = 0; v < nv; v++) u[p1 * nv + v] = g[v];
   }
 }

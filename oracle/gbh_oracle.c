@@ -338,6 +338,18 @@ static int bc_ghost(const orc_zone *b, int nd, double gamma, const double *w, do
                     double Tb) {
   double inv_gamma_m1 = 1.0 / (gamma - 1.0);
   double rho = 0, vel[3] = {0, 0, 0}, energy, pressure = 0, vsq;
+  if (nd == 1) {
+    /* BCSlipWall.c:38-76, the 1-D branch (Euler1D flow variables, euler1d.h:81-88) */
+    if (b->type != ORC_BC_SLIP_WALL) return 1;
+    rho = w[0];
+    vel[0] = w[1] / rho;
+    pressure = (w[2] - 0.5 * rho * vel[0] * vel[0]) * (gamma - 1.0);
+    const double ug = 2.0 * b->data[0] - vel[0];
+    out[0] = rho;
+    out[1] = rho * ug;
+    out[2] = inv_gamma_m1 * pressure + 0.5 * rho * ug * ug;
+    return 0;
+  }
   if (b->type != ORC_BC_SUPERSONIC_INFLOW) {
     rho = w[0];
     if (nd == 2) {
@@ -515,6 +527,9 @@ static int apply_bc_at(const orc_problem *p, double *u, double t) {
           Tb = p->tfield[z][q];
         }
         if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1, inflow, Tb)) return 1;
+      } else if (b->type == ORC_BC_SLIP_WALL) {
+        /* the 1-D slip wall */
+        if (bc_ghost(b, nd, p->gamma, u + nv * p2, u + nv * p1, 0, 0.0)) return 1;
       } else {
         return 1;
       }
@@ -1266,7 +1281,10 @@ static int tridiag_solve(int n, double *a, double *b, double *c, double *x) {
 
 /* Interp1PrimFifthOrderCRWENO (Interp1PrimFifthOrderCRWENO.c:124-199) on one grid
  * line of N cells, for the four interface reconstructions k = 0 fL, 1 fR (values fC,
- * weights from fC), 2 uL, 3 uR (values uC, weights from u), every component: at the
+ * weights from fC), 2 uL, 3 uR (values uC, weights from u) and, with a source function
+ * sC (gravity), k = 4 sL, 5 sR (values sC, the weights of fL and fR: the source's
+ * InterpolateInterfacesHyp calls pass uflag 0, Euler1DSource.c:55-56,
+ * NavierStokes3DSource.c:70-71), every component: at the
  * N+1 interfaces the rows
  *   left-biased:  (2/3 w1 + 1/3 w2) F_{j-1/2} + (1/3 w1 + 2/3 w2 + 2/3 w3) F_{j+1/2}
  *                 + 1/3 w3 F_{j+3/2} = w1 (f_{j-1} + 5 f_j)/6 + w2 (5 f_j + f_{j+1})/6
@@ -1274,15 +1292,15 @@ static int tridiag_solve(int n, double *a, double *b, double *c, double *x) {
  * (right-biased: mirrored), the weights with the CRWENO5 optimal weights
  * (WENOFifthOrderCalculateWeights.c:205-225); the first and last interfaces take the
  * explicit WENO5 value (identity rows, WENO5 optimal weights) on a single rank.
- * out[(I*4 + k)*nv + v]; work: 4 (N+1) doubles. */
-static int crweno_line(const orc_problem *p, const double *fC, const double *u, const double *uC, long base,
-                       long sd, int N, double *out, double *work) {
+ * out[(I*nk + k)*nv + v], nk = 4 (6 with sC); work: 4 (N+1) doubles. */
+static int crweno_line(const orc_problem *p, const double *fC, const double *u, const double *uC,
+                       const double *sC, long base, long sd, int N, double *out, double *work) {
   static const double one_third = 1.0 / 3.0;
   static const double one_sixth = 1.0 / 6.0;
-  const int nv = p->nvars, n = N + 1;
+  const int nv = p->nvars, n = N + 1, nk = sC ? 6 : 4;
   double *a = work, *b = work + n, *c = work + 2 * n, *x = work + 3 * n;
-  for (int k = 0; k < 4; k++) {
-    const double *val = k < 2 ? fC : uC, *wv = k < 2 ? fC : u;
+  for (int k = 0; k < nk; k++) {
+    const double *val = k < 2 ? fC : (k < 4 ? uC : sC), *wv = (k < 2 || k >= 4) ? fC : u;
     const int upw = (k % 2 == 0) ? 1 : -1;
     for (int v = 0; v < nv; v++) {
       for (int I = 0; I <= N; I++) {
@@ -1331,7 +1349,7 @@ static int crweno_line(const orc_problem *p, const double *fC, const double *u, 
         x[I] = w1 * f1 + w2 * f2 + w3 * f3;
       }
       if (tridiag_solve(n, a, b, c, x)) return -1;
-      for (int I = 0; I <= N; I++) out[((long)I * 4 + k) * nv + v] = x[I];
+      for (int I = 0; I <= N; I++) out[((long)I * nk + k) * nv + v] = x[I];
     }
   }
   return 0;
@@ -1407,15 +1425,17 @@ static void block_tridiag_solve(int n, int bs, double *a, double *b, double *c, 
  * rows with b = w1/3 + 2 (w2 + w3)/3), right-hand side sum_k w_k f_k; the first and last
  * interfaces: B = L and the explicit WENO5 value.  Weights: the characteristic weights
  * (WENOFifthOrderCalculateWeightsChar*, projections of f and u) with the CRWENO5 /
- * WENO5 optimal weights.  out[(I*4 + k)*nv + v]; work: (N+1) (3 nv^2 + nv) doubles. */
-static int crweno_char_line(const orc_problem *p, const double *fC, const double *u, const double *uC, long base,
-                            long sd, int N, int dir, double *out, double *work) {
+ * WENO5 optimal weights.  With a source function sC (gravity): k = 4, 5 its left and
+ * right values with the flux's weights, as crweno_line.
+ * out[(I*nk + k)*nv + v], nk = 4 (6 with sC); work: (N+1) (3 nv^2 + nv) doubles. */
+static int crweno_char_line(const orc_problem *p, const double *fC, const double *u, const double *uC,
+                            const double *sC, long base, long sd, int N, int dir, double *out, double *work) {
   static const double one_third = 1.0 / 3.0;
   static const double one_sixth = 1.0 / 6.0;
-  const int nv = p->nvars, n = N + 1, nv2 = nv * nv;
+  const int nv = p->nvars, n = N + 1, nv2 = nv * nv, nk = sC ? 6 : 4;
   double *A = work, *B = work + (long)n * nv2, *Cm = work + 2L * n * nv2, *F = work + 3L * n * nv2;
-  for (int k = 0; k < 4; k++) {
-    const double *val = k < 2 ? fC : uC, *wv = k < 2 ? fC : u;
+  for (int k = 0; k < nk; k++) {
+    const double *val = k < 2 ? fC : (k < 4 ? uC : sC), *wv = (k < 2 || k >= 4) ? fC : u;
     const int upw = (k % 2 == 0) ? 1 : -1;
     for (int I = 0; I <= N; I++) {
       const long qm1 = upw > 0 ? base + (long)(I - 1) * sd : base + (long)I * sd;
@@ -1465,7 +1485,7 @@ static int crweno_char_line(const orc_problem *p, const double *fC, const double
     }
     block_tridiag_solve(n, nv, A, B, Cm, F);
     for (int I = 0; I <= N; I++)
-      for (int v = 0; v < nv; v++) out[((long)I * 4 + k) * nv + v] = F[(long)I * nv + v];
+      for (int v = 0; v < nv; v++) out[((long)I * nk + k) * nv + v] = F[(long)I * nv + v];
   }
   return 0;
 }
@@ -1486,16 +1506,18 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
   double *uC = (double *)malloc(sizeof(double) * np * nv);
   long offset = 0;
   int crweno_failed = 0;
-  if (p->scheme == ORC_SCHEME_CRWENO5 && p->has_grav) {
-    free(fC);
-    free(uC);
-    return -1; /* gravity with CRWENO5: not restated */
-  }
+  const int crweno = p->scheme == ORC_SCHEME_CRWENO5;
+  /* CRWENO5 with gravity: the source function [0, phi e_d, phi] as a point array,
+   * solved for beside the flux (Euler1DSourceFunction, NavierStokes3DSourceFunction) */
+  double *sC = (crweno && src && p->has_grav) ? (double *)malloc(sizeof(double) * np * nv) : NULL;
   for (int d = 0; d < nd; d++) {
+    const int dosrc = src && p->has_grav && p->grav[d] != 0.0;
 #pragma omp parallel for schedule(static) num_threads(NTHR)
     for (long q = 0; q < np; q++) {
       m_flux(p, fC + nv * q, u + nv * q, d);
       m_ufunc(p, uC + nv * q, u + nv * q, q);
+      if (sC && dosrc)
+        for (int v = 0; v < nv; v++) sC[nv * q + v] = (v == 1 + d || v == nv - 1) ? p->gg[q] : 0.0;
     }
     int N = p->dim[d];
     long sd = s[d];
@@ -1503,14 +1525,14 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
     int ob[3] = {1, 1, 1};
     for (int e = 0; e < nd; e++) if (e != d) { ob[e] = p->dim[e]; nouter *= p->dim[e]; }
     const double *dxinv = p->dxinv + offset;
-    const int dosrc = src && p->has_grav && p->grav[d] != 0.0;
+    const double *sCd = dosrc ? sC : NULL;
+    const int nk = sCd ? 6 : 4;
 #pragma omp parallel num_threads(NTHR)
     {
       double *FI = (double *)malloc(sizeof(double) * (N + 1) * nv);
       double *SI = (double *)malloc(sizeof(double) * (N + 1) * nv);
-      const int crweno = p->scheme == ORC_SCHEME_CRWENO5;
       const int crchar = crweno && p->interp == ORC_INTERP_CHAR && nv > 1;
-      double *CR = crweno ? (double *)malloc(sizeof(double) * (N + 1) * nv * 4) : NULL;
+      double *CR = crweno ? (double *)malloc(sizeof(double) * (N + 1) * nv * 6) : NULL;
       double *CW = crweno ? (double *)malloc(sizeof(double) * (N + 1) * (crchar ? 3 * nv * nv + nv : 4)) : NULL;
 #pragma omp for schedule(static)
       for (long lo = 0; lo < nouter; lo++) {
@@ -1519,8 +1541,8 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
         for (int e = 0; e < nd; e++) if (e != d) { idx[e] = (int)(r % ob[e]); r /= ob[e]; }
         idx[d] = 0;
         long base = pidx(p, s, idx); /* cell 0 of this line */
-        if (crchar ? crweno_char_line(p, fC, u, uC, base, sd, N, d, CR, CW)
-                   : (crweno && crweno_line(p, fC, u, uC, base, sd, N, CR, CW))) {
+        if (crchar ? crweno_char_line(p, fC, u, uC, sCd, base, sd, N, d, CR, CW)
+                   : (crweno && crweno_line(p, fC, u, uC, sCd, base, sd, N, CR, CW))) {
           crweno_failed = 1;
           continue;
         }
@@ -1531,10 +1553,12 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
           double fL[MAXV], fR[MAXV], uL[MAXV], uR[MAXV];
           if (crweno) {
             for (int v = 0; v < nv; v++) {
-              fL[v] = CR[((long)I * 4 + 0) * nv + v];
-              fR[v] = CR[((long)I * 4 + 1) * nv + v];
-              uL[v] = CR[((long)I * 4 + 2) * nv + v];
-              uR[v] = CR[((long)I * 4 + 3) * nv + v];
+              fL[v] = CR[((long)I * nk + 0) * nv + v];
+              fR[v] = CR[((long)I * nk + 1) * nv + v];
+              uL[v] = CR[((long)I * nk + 2) * nv + v];
+              uR[v] = CR[((long)I * nk + 3) * nv + v];
+              /* SourceUpwind (Euler1DSourceUpwind.c, NavierStokes3DSourceUpwind.c): the average */
+              if (dosrc) SI[(long)I * nv + v] = 0.5 * (CR[((long)I * nk + 4) * nv + v] + CR[((long)I * nk + 5) * nv + v]);
             }
           } else if (p->interp == ORC_INTERP_COMP) {
             for (int v = 0; v < nv; v++) {
@@ -1654,6 +1678,7 @@ static int hyperbolic_source(const orc_problem *p, const double *u, double *hyp,
   }
   free(fC);
   free(uC);
+  free(sC);
   return crweno_failed ? -1 : 0;
 }
 

@@ -128,6 +128,24 @@ CASES = {
     "strat64_grav1_llf_comp_mapped": lambda: _w(C.stratified_1d(64, n_iter=10, grav_type=1, upwinding="llf-char",
                                                                  g=2.0), "mapped"),
     "sod64_grav_roe_comp": lambda: _g1(C.sod(64, n_iter=20, dt=1e-3), 1.0),
+    # gravity with CRWENO5: the source function solved with the flux's weights
+    "strat64_crweno_grav0_roe_comp": lambda: _cr(C.stratified_1d(64, n_iter=10, perturb=0.05)),
+    "strat64_crweno_grav1_roe_char_mapped": lambda: _w(_cr(C.stratified_1d(64, n_iter=10, grav_type=1,
+                                                                           interp="characteristic",
+                                                                           perturb=0.05)), "mapped"),
+    "sod64_crweno_grav_llf_char": lambda: _g1(_cr(C.sod(64, n_iter=20, dt=1e-3, interp="characteristic",
+                                                        upwinding="llf-char")), 1.0),
+    # slip walls in 1-D (BCSlipWall.c's Euler1D branch), with and without gravity
+    "sod64_slipwall_comp_roe": lambda: _b(C.sod(64, n_iter=20, dt=1e-3),
+                                          {(0, 1): ("slip-wall", [0.0]), (0, -1): ("slip-wall", [0.1])}),
+    "sod64_crweno_grav_slipwall_char_roe_mapped": lambda: _w(_b(_g1(_cr(C.sod(64, n_iter=20, dt=1e-3,
+                                                                            interp="characteristic")), 1.0),
+                                                                {(0, 1): ("slip-wall", [0.0]),
+                                                                 (0, -1): ("slip-wall", [0.0])}), "mapped"),
+    "rtb12_crweno_comp_rusanov_stir": lambda: _stir(_cr(C.rising_thermal_bubble(12, n_iter=3, dt=0.05,
+                                                                                perturb=0.02))),
+    "rtb12_crweno_char_rusanov_hb3z_stir": lambda: _stir(_g(_cr(C.rising_thermal_bubble(
+        12, n_iter=3, dt=0.05, interp="characteristic", perturb=0.02)), (0.0, 0.0, 9.8), 3, 0.01)),
     # the conservation check (solver.inp conservation_check yes): boundary fluxes through
     # extrapolate / wall / inflow faces, a source (gravity), the viscous term
     "sod64_cons_comp_roe": lambda: _cons(C.sod(64, n_iter=20, dt=1e-3)),

@@ -227,10 +227,16 @@ def test_reader_boundary_values(built_lib, tmp_path):
     assert c.zone_data[1][0] == 0.9
     assert list(c.zone_data[2])[:2] == [0.0, 0.125]
     assert list(c.zone_data[3])[:4] == [1.0, 0.5, 0.0, 2.625]
-    # the wall / inflow / outflow types are 2-D / 3-D only (the reference's 1-D branches are incomplete)
+    # of the wall / inflow / outflow types only the slip wall has a 1-D branch
+    # (BCSlipWall.c:38-76); the others are 2-D / 3-D only
     sod = C.sod(16, n_iter=1, dt=1e-3)
-    sod.bcs = {(0, 1): ("slip-wall", [0.0])}
+    sod.bcs = {(0, 1): ("slip-wall", [0.0]), (0, -1): ("slip-wall", [0.5])}
     d = str(tmp_path / "sod")
+    sod.write(d)
+    c = Inputs(d).config
+    assert [c.zones[z][0] for z in range(2)] == [4, 4] and c.zone_data[1][0] == 0.5
+    sod.bcs = {(0, 1): ("noslip-wall", [0.0])}
+    d = str(tmp_path / "sod_noslip")
     sod.write(d)
     _expect(4, d)
 
@@ -294,7 +300,7 @@ def test_solver_create_rejects_bad_gravity(built_lib):
 
 def test_reader_crweno(built_lib, tmp_path):
     """hyp_space_scheme crweno5 -> gb_config.hyp_scheme (component-wise and
-    characteristic); gravity with it is not on this path."""
+    characteristic), with gravity too (both models that have it)."""
     case = C.sod(16, n_iter=1)
     case.hyp_scheme = "crweno5"
     assert Inputs(str(_deck(tmp_path / "a", case))).config.hyp_scheme == _lib.SCHEME["crweno5"]
@@ -305,7 +311,12 @@ def test_reader_crweno(built_lib, tmp_path):
     assert c.hyp_scheme == _lib.SCHEME["crweno5"] and c.interp == _lib.INTERP["characteristic"]
     case = C.rising_thermal_bubble(8, n_iter=1)
     case.hyp_scheme = "crweno5"
-    _expect(4, str(_deck(tmp_path / "d", case)))
+    c = Inputs(str(_deck(tmp_path / "d", case))).config
+    assert c.hyp_scheme == _lib.SCHEME["crweno5"] and c.gravity[1] == 9.8
+    case = C.stratified_1d(16, n_iter=1, interp="characteristic")
+    case.hyp_scheme = "crweno5"
+    c = Inputs(str(_deck(tmp_path / "e", case))).config
+    assert c.hyp_scheme == _lib.SCHEME["crweno5"] and c.gravity[0] == 1.0
 
 
 @pytest.mark.parametrize("grav_type", [0, 1])

@@ -1,5 +1,5 @@
-"""Turbulent supersonic inflow (BCTurbulentSupersonicInflow.c) and reflect (BCReflect.c)
-boundaries.
+"""Turbulent supersonic inflow (BCTurbulentSupersonicInflow.c), reflect (BCReflect.c)
+and 1-D slip-wall (BCSlipWall.c) boundaries.
 
 CPU: the reader's inflow data and slice count against the file the deck wrote, the zone
 codes, the validation of a turbulent inflow whose transverse extent leaves the grid.
@@ -130,3 +130,14 @@ def test_turbulent_inflow_against_the_flow_refused(built_lib, tmp_path):
 @pytest.mark.parametrize("model", ["euler1d", "euler2d", "navierstokes3d"])
 def test_reflect_ghosts_bit_exact(built_lib, oracle_lib, tmp_path, model):
     _ghost_parity(reflect(model), tmp_path, [0.0])
+
+
+@pytest.mark.gpu
+def test_euler1d_slip_wall_ghosts_bit_exact(built_lib, oracle_lib, tmp_path):
+    """BCSlipWall.c's 1-D branch: density and pressure extrapolated, the velocity
+    mirrored about the wall's (a moving wall on one face)."""
+    case = C.sod(40, n_iter=1, dt=1e-3)
+    rng = np.random.default_rng(2)
+    case.u[:, 1] = 0.3 * rng.standard_normal(40) * case.u[:, 0]
+    case.bcs = {(0, 1): ("slip-wall", [0.0]), (0, -1): ("slip-wall", [0.25])}
+    _ghost_parity(case, tmp_path, [0.0])

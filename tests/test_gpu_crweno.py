@@ -154,3 +154,98 @@ def test_crweno_function_pointers(built_lib, oracle_lib, tmp_path, interp):
     hyp = torch.zeros_like(u)
     s.hyperbolic(hyp, u)
     assert relerr(hyp.cpu().numpy(), P.hyperbolic(u0)) <= rhs_tol(case, u0, P.rhs(u0.copy()))
+
+
+# ---------------------------------------------------------------------------
+# Gravity with CRWENO5 (Euler1DSource.c, NavierStokes3DSource.c): the source function
+# [0, g e_d, g] solved for with the flux's weights (the same rows, another right-hand
+# side), averaged, differenced and scaled per cell; the modified solution as the u
+# values; the dissipation scaled by max(g_L, g_R).
+# ---------------------------------------------------------------------------
+GRAV = [("euler1d", "components", "roe", "js", 0), ("euler1d", "characteristic", "roe", "mapped", 1),
+        ("euler1d", "characteristic", "llf-char", "yc", 0), ("euler1d", "components", "llf-char", "borges", 1),
+        ("euler1d", "characteristic", "llf-char", "none", 1),
+        ("navierstokes3d", "components", "rusanov", "yc", 2), ("navierstokes3d", "characteristic", "rusanov", "js", 3),
+        ("navierstokes3d", "characteristic", "rusanov", "borges", 1),
+        ("navierstokes3d", "components", "rusanov", "mapped", 3)]
+
+
+def grav_case(model, interp, upw, weights, k, n_iter=1, stir=0.5):
+    """Euler1D: the stratified atmosphere (gravity_type k), perturbed; NavierStokes3D: the
+    rising-bubble deck (balance type HB k, gravity along z for k = 3), perturbed and
+    stirred (at rest its energy right-hand side is rounding noise)."""
+    if model == "euler1d":
+        case = C.stratified_1d(96, n_iter=n_iter, grav_type=k, interp=interp, upwinding=upw, perturb=0.05)
+    else:
+        case = C.rising_thermal_bubble(14, n_iter=n_iter, dt=0.05, interp=interp, HB=k, perturb=0.02)
+        if k == 3:
+            case.gravity, case.N_bv = (0.0, 0.0, 9.8), 0.01
+        if stir:
+            rng = np.random.default_rng(11)
+            case.u[:, 1:4] = stir * rng.standard_normal((case.u.shape[0], 3)) * case.u[:, :1]
+    return crweno(case, weights)
+
+
+@pytest.mark.parametrize("model,interp,upw,weights,k", GRAV)
+def test_crweno_gravity_rhs_matches_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw, weights, k):
+    case = grav_case(model, interp, upw, weights, k)
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    got = O.interior(gpu_rhs(s, u0), case.size, case.nvars, 3)
+    ref_full = P.rhs(u0.copy())
+    ref = O.interior(ref_full, case.size, case.nvars, 3)
+    src = O.interior(P.source(u0), case.size, case.nvars, 3)
+    tol = rhs_tol(case, u0, ref_full)
+    assert relerr(ref - src, ref) > 1e6 * tol  # without the source the result would be far off
+    assert relerr(got, ref) <= tol
+
+
+@pytest.mark.parametrize("model,interp,upw,weights,k", [GRAV[0], GRAV[1], GRAV[5], GRAV[6]])
+def test_crweno_gravity_steps_match_oracle(built_lib, oracle_lib, tmp_path, model, interp, upw, weights, k):
+    case = grav_case(model, interp, upw, weights, k, n_iter=8)
+    s = solver_for(case, tmp_path)
+    s.step(8)
+    P = O.Problem(case)
+    ref = O.interior(P.rk(P.u0(), 8), case.size, case.nvars, 3).reshape(-1)
+    assert relerr(s.get_state(), ref) <= STEP_TOL
+
+
+@pytest.mark.parametrize("interp", ["components", "characteristic"])
+@pytest.mark.parametrize("grav_type", [0, 1])
+def test_crweno_euler1d_hydrostatic_state_is_preserved(built_lib, oracle_lib, tmp_path, interp, grav_type):
+    """Well-balanced with the compact scheme too: the flux's pressure and the source
+    function go through the same line solves, so the atmosphere at rest has a
+    right-hand side of rounding noise while its gravity source alone is O(rho g)."""
+    case = crweno(C.stratified_1d(200, n_iter=1, grav_type=grav_type, interp=interp, perturb=0.0))
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    got = O.interior(gpu_rhs(s, u0), case.size, 3, 3)
+    src = O.interior(P.source(u0), case.size, 3, 3)
+    assert np.abs(src[:, 1]).max() > 0.1
+    assert np.abs(got).max() <= 1e-11, np.abs(got).max(axis=0)
+    s.step(20)
+    assert np.abs(s.get_state().reshape(-1, 3)[:, 1]).max() <= 1e-11
+
+
+@pytest.mark.parametrize("model,interp,upw,weights,k", [GRAV[1], GRAV[5]])
+def test_crweno_gravity_function_pointers(built_lib, oracle_lib, tmp_path, model, interp, upw, weights, k):
+    """gb_HyperbolicFunction (the hyperbolic term alone) and gb_SourceFunction (the
+    gravity source, the difference of the terms with and without it) with CRWENO5."""
+    case = grav_case(model, interp, upw, weights, k)
+    s = solver_for(case, tmp_path)
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    s.apply_bc(u)
+    hyp = torch.zeros_like(u)
+    s.hyperbolic(hyp, u)
+    tol = rhs_tol(case, u0, P.rhs(u0.copy()))
+    assert relerr(hyp.cpu().numpy(), P.hyperbolic(u0)) <= tol
+    src = torch.full_like(u, 3.0)
+    s.source(src, u)
+    # the source is a difference of two hyperbolic terms: its error is relative to them
+    ref = P.source(u0)
+    assert np.linalg.norm(src.cpu().numpy() - ref) <= tol * np.linalg.norm(P.hyperbolic(u0)) + 1e-14
+    assert np.linalg.norm(ref) > 0.0
