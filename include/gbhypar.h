@@ -42,10 +42,11 @@ enum { GB_UPWIND_ROE = 0, GB_UPWIND_LLF = 1, GB_UPWIND_RF = 2, GB_UPWIND_RUSANOV
        GB_UPWIND_SWFS = 4 /* physics.inp "steger-warming": Euler1D, Euler2D */ };
 enum { GB_INTERP_COMPONENTS = 0, GB_INTERP_CHARACTERISTIC = 1 };
 /* boundary.inp types (include/boundaryconditions.h): periodic and extrapolate for every
- * model; dirichlet for every model; the wall and inflow/outflow types, and the
- * subsonic "ambivalent" one (inflow or outflow point by point, by the sign of the
- * extrapolated face velocity), for Euler2D and NavierStokes3D (the reference's 1-D
- * branches of those are incomplete); the thermal walls (slip / no-slip, the ghost
+ * model; dirichlet for every model; slip-wall for every model (BCSlipWall.c has a
+ * 1-D branch); the other wall and inflow/outflow types, and the subsonic "ambivalent"
+ * one (inflow or outflow point by point, by the sign of the extrapolated face
+ * velocity), for Euler2D and NavierStokes3D (the reference has no 1-D branch for
+ * them); the thermal walls (slip / no-slip, the ghost
  * pressure from the extrapolated density and a wall temperature given per time
  * level in a file) for NavierStokes3D (BCThermalSlipWall.c, BCThermalNoslipWall.c).
  * sponge (every model) fills no ghost point: over its extent of interior points it adds
