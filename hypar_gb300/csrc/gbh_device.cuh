@@ -402,6 +402,31 @@ __device__ __forceinline__ void eigvals(double un, double a, double* lam) {
 // p[2]'s value; with a zero centre a third of the stencil terms drop out, and the
 // values stay of the size of the window's variation, so their rounding is far
 // smaller than that of reconstructions of O(1) values.
+//
+// The second half of a pair, from the squared smoothness terms q = B^2 of its six
+// sub-stencils: the unnormalised weights (products of the other two q's), the
+// candidates of the values v and the two normalisations (rL, rR: their reciprocals).
+template <bool C0>
+__device__ __forceinline__ void weno5_pair_finish(const double* v, double qL1, double qL2, double qL3, double qR1,
+                                                  double qR2, double qR3, double& outL, double& outR, double& rL,
+                                                  double& rR) {
+  double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;  // x (1, 1/6, 1/3) of the weights
+  double aR1 = qR2 * qR3, aR2 = qR1 * qR3, aR3 = qR1 * qR2;
+  // candidates (times 6): two of them shared between the sides
+  double cL1 = C0 ? fma(2.0, v[0], -7.0 * v[1]) : fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
+  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3]));
+  double cA = C0 ? fma(2.0, v[3], -v[1]) : fma(5.0, v[2], fma(2.0, v[3], -v[1]));  // left #2, right #3
+  double cB = C0 ? fma(5.0, v[3], -v[4]) : fma(5.0, v[3], fma(2.0, v[2], -v[4]));  // left #3, right #2
+  double nL = fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
+  double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
+  double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
+  double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
+  rL = nr_rcp(DL);
+  rR = nr_rcp(DR);
+  outL = nL * rL;
+  outR = nR * rR;
+}
+
 template <bool TP, bool C0 = false>
 __device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v, double eps4, double& outL,
                                                 double& outR, double* tp) {
@@ -427,20 +452,8 @@ __device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v
   double BR3 = fma(kd2, d2, fma(gR3, gR3, eps4));
   double qL1 = BL1 * BL1, qL2 = BL2 * BL2, qL3 = BL3 * BL3;
   double qR1 = BR1 * BR1, qR2 = BR2 * BR2, qR3 = BR3 * BR3;
-  double aL1 = qL2 * qL3, aL2 = qL1 * qL3, aL3 = qL1 * qL2;  // x (1, 1/6, 1/3) of the weights
-  double aR1 = qR2 * qR3, aR2 = qR1 * qR3, aR3 = qR1 * qR2;
-  // candidates (times 6): two of them shared between the sides
-  double cL1 = C0 ? fma(2.0, v[0], -7.0 * v[1]) : fma(2.0, v[0], fma(-7.0, v[1], 11.0 * v[2]));
-  double cR1 = fma(2.0, v[5], fma(-7.0, v[4], 11.0 * v[3]));
-  double cA = C0 ? fma(2.0, v[3], -v[1]) : fma(5.0, v[2], fma(2.0, v[3], -v[1]));  // left #2, right #3
-  double cB = C0 ? fma(5.0, v[3], -v[4]) : fma(5.0, v[3], fma(2.0, v[2], -v[4]));  // left #3, right #2
-  double nL = fma(aL1, cL1, fma(6.0 * aL2, cA, (3.0 * aL3) * cB));
-  double nR = fma(aR1, cR1, fma(6.0 * aR2, cB, (3.0 * aR3) * cA));
-  double DL = fma(36.0, aL2, fma(18.0, aL3, 6.0 * aL1));
-  double DR = fma(36.0, aR2, fma(18.0, aR3, 6.0 * aR1));
-  const double rL = nr_rcp(DL), rR = nr_rcp(DR);
-  outL = nL * rL;
-  outR = nR * rR;
+  double rL, rR;
+  weno5_pair_finish<C0>(v, qL1, qL2, qL3, qR1, qR2, qR3, outL, outR, rL, rR);
   if (TP) {
     // the values the reverse pass would otherwise recompute first
     tp[0] = BL1;
@@ -457,6 +470,39 @@ __device__ __forceinline__ void weno5_pair_impl(const double* w, const double* v
 __device__ __forceinline__ void weno5_pair(const double* w, const double* v, double eps4, double& outL,
                                            double& outR) {
   weno5_pair_impl<false>(w, v, eps4, outL, outR, nullptr);
+}
+
+// The squared smoothness terms of the three-point sub-stencil (a, b, c) centred at a
+// cell, for each of the three places it takes in the pairs around it:
+//   ql, g = a - 4b + 3c: the left sub-stencil of a left-biased stencil (BL1 of the
+//       interface two cells to its right) and the right-biased stencil's third (BR3 of
+//       the interface to its right);
+//   qc, g = a - c: the central one (BL2 of the interface to its right, BR2 of the one
+//       to its left);
+//   qr, g = 3a - 4b + c: BL3 of the interface to its left, BR1 of the one two cells to
+//       its left;
+// each q = B^2 with B = (13/3) d^2 + g^2 + 4 eps and d = a - 2b + c, as in the pair.
+// Interface j+1/2 (window cells j-2 .. j+3) then takes
+//   qL = (ql[j-1], qc[j], qr[j+1]),  qR = (qr[j+2], qc[j+1], ql[j]).
+__device__ __forceinline__ void weno5_cell_q(double a, double b, double c, double eps4, double& ql, double& qc,
+                                             double& qr) {
+  const double d = fma(-2.0, b, a) + c;
+  const double kde = fma((13.0 / 3.0) * d, d, eps4);
+  const double gl = fma(3.0, c, fma(-4.0, b, a));
+  const double gc = a - c;
+  const double gr = fma(3.0, a, fma(-4.0, b, c));
+  const double Bl = fma(gl, gl, kde), Bc = fma(gc, gc, kde), Br = fma(gr, gr, kde);
+  ql = Bl * Bl;
+  qc = Bc * Bc;
+  qr = Br * Br;
+}
+
+// A pair from the per-cell table of weno5_cell_q (q's given) and the values v.
+template <bool C0>
+__device__ __forceinline__ void weno5_pair_q(const double* v, double qL1, double qL2, double qL3, double qR1,
+                                             double qR2, double qR3, double& outL, double& outR) {
+  double rL, rR;
+  weno5_pair_finish<C0>(v, qL1, qL2, qL3, qR1, qR2, qR3, outL, outR, rL, rR);
 }
 
 // The pair of a window given relative to its centre cell (w[2] = v[2] = 0).

@@ -350,13 +350,19 @@ struct RelFlux {
   static constexpr bool value = !GRAV;
 };
 
-template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV, bool WT>
+// CQ (component-wise, Jiang-Shu, no gravity, no tape: the tile form): the squared
+// smoothness terms come from the tile's per-cell table (weno5_cell_q), `qt` pointing at
+// the entry of window cell 0 in row 0, rows of `nc` cells, row 3k + role for quantity k
+// (the NV flux components, then the NV state components) and role l, c, r.
+template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV, bool WT, bool CQ = false>
 __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>::NV],
                                            const double (&wf)[6][ModelTraits<M>::NV], const double (&wuc)[6],
                                            const double (&wgf)[6], const double (&wgg)[6],
                                            const CellAux<M> (&ax)[6], const PhysParams& pp, const StageEpi& ep,
                                            double eps4, bool src_dir, long long tapeoff, double (&fI)[ModelTraits<M>::NV],
-                                           double (&SI)[ModelTraits<M>::NV]) {
+                                           double (&SI)[ModelTraits<M>::NV], const double* qt = nullptr,
+                                           int nc = 0) {
+  static_assert(!CQ || (!CHAR && !ALTW && !GRAV && !WT), "the per-cell table serves the plain component-wise form");
   constexpr int NV = ModelTraits<M>::NV;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
   constexpr bool REL = RelFlux<GRAV>::value;
@@ -383,6 +389,21 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
         double* t = ep.tape + tapeoff * TAPE_WIDE + 8 + v * 16;
         weno5_pair_tape<REL>(sf, sf, eps4, fL[v], fR[v], t);
         weno5_pair_tape<REL>(su, su, eps4, uL[v], uR[v], t + 8);
+        continue;
+      }
+      if (CQ) {
+        // qL = (ql[1], qc[2], qr[3]), qR = (qr[4], qc[3], ql[2]) of the window cells
+        const double* qf = qt + (3 * v) * nc;
+        const double* qu = qt + (3 * (NV + v)) * nc;
+        weno5_pair_q<REL>(sf, qf[1], qf[nc + 2], qf[2 * nc + 3], qf[2 * nc + 4], qf[nc + 3], qf[2], fL[v], fR[v]);
+        if (M == MODEL_NS3D && v == NV - 1) {
+          double sc[6];
+#pragma unroll
+          for (int p = 0; p < 6; p++) sc[p] = REL ? (p == 2 ? 0.0 : wuc[p] - wuc[2]) : wuc[p];
+          weno5_pair_q<REL>(sc, qu[1], qu[nc + 2], qu[2 * nc + 3], qu[2 * nc + 4], qu[nc + 3], qu[2], uL[v], uR[v]);
+        } else {
+          weno5_pair_q<REL>(su, qu[1], qu[nc + 2], qu[2 * nc + 3], qu[2 * nc + 4], qu[nc + 3], qu[2], uL[v], uR[v]);
+        }
         continue;
       }
       // the source function phi = g is reconstructed with this flux component's
@@ -740,9 +761,16 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
   constexpr int TC = TI - 1, NCELL = TI + 5;
+  // component-wise with Jiang-Shu weights: the squared smoothness terms of every
+  // cell's sub-stencil, once per cell instead of six times per interface pair, where
+  // the table keeps the block's static shared memory within 48 KB
+  constexpr size_t SMEM0 = sizeof(double) * NCELL * (2 * NV + 1) + sizeof(CellAux<M>) * NCELL +
+                           sizeof(double) * TI * NV;
+  constexpr bool CQ = !CHAR && !ALTW && !WT && SMEM0 + sizeof(double) * 6 * NV * NCELL <= 48 * 1024;
   __shared__ double su[NCELL][NV], sf[NCELL][NV], suc[NCELL];
   __shared__ CellAux<M> sax[NCELL];
   __shared__ double sfI[TI][NV];
+  __shared__ double sq[CQ ? 6 * NV : 1][CQ ? NCELL : 1];
   const long long line = blk % ntrans;
   const int I0 = (int)(blk / ntrans) * TC;
   long long tr = line, pbase = (long long)G.g * G.stride[DIR];
@@ -780,6 +808,19 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
     sax[c] = a;
   }
   __syncthreads();
+  if constexpr (CQ) {
+    // cells 1 .. TI+3 (those whose terms the tile's interfaces read), each from its
+    // two neighbours; cells past the line's reach hold terms no interface reads
+    for (int c = 1 + threadIdx.x; c <= TI + 3; c += TI) {
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        weno5_cell_q(sf[c - 1][k], sf[c][k], sf[c + 1][k], eps4, sq[3 * k][c], sq[3 * k + 1][c], sq[3 * k + 2][c]);
+        weno5_cell_q(su[c - 1][k], su[c][k], su[c + 1][k], eps4, sq[3 * (NV + k)][c], sq[3 * (NV + k) + 1][c],
+                     sq[3 * (NV + k) + 2][c]);
+      }
+    }
+    __syncthreads();
+  }
   const int t = threadIdx.x;
   const int I = I0 + t;
   if (I <= N) {
@@ -796,8 +837,8 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
       ax[p] = sax[t + p];
     }
     double fI[NV], SI[NV];
-    iface_flux<M, CHAR, UPW, DIR, ALTW, false, WT>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, false,
-                                                   line * (N + 1) + I, fI, SI);
+    iface_flux<M, CHAR, UPW, DIR, ALTW, false, WT, CQ>(wu, wf, wuc, wgf, wgg, ax, pp, ep, eps4, false,
+                                                       line * (N + 1) + I, fI, SI, CQ ? &sq[0][t] : nullptr, NCELL);
     // fI is relative to the interface's left cell (window cell 2)
     if (ep.bnd && (I == 0 || I == N)) {
       double Fb[NV];
