@@ -70,8 +70,9 @@ enum { GB_LAYOUT_INTERIOR = 0, GB_LAYOUT_GHOSTED = 1 };
 enum { GB_WENO_JS = 0, GB_WENO_MAPPED = 1, GB_WENO_BORGES = 2, GB_WENO_YC = 3, GB_WENO_NONE = 4 };
 enum { GB_MEM_HOST = 0, GB_MEM_DEVICE = 1 };
 /* hyp_space_scheme: weno5, or crweno5 (compact WENO5, a tridiagonal solve per grid
- * line, block tridiagonal for the characteristic form; without gravity;
- * Interp1PrimFifthOrderCRWENO.c, Interp1PrimFifthOrderCRWENOChar.c) */
+ * line, block tridiagonal for the characteristic form; with gravity the source
+ * function is solved for with the flux's rows; Interp1PrimFifthOrderCRWENO.c,
+ * Interp1PrimFifthOrderCRWENOChar.c) */
 enum { GB_SCHEME_WENO5 = 0, GB_SCHEME_CRWENO5 = 1 };
 
 #define GB_MAX_ZONES 12
