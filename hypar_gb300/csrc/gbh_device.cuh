@@ -565,25 +565,14 @@ __device__ __forceinline__ void weno5_side_alt(int wtype, double B1, double B2, 
   out = fma(a1, p1, fma(a2, p2, a3 * p3)) * nr_rcp(a1 + a2 + a3);
 }
 
-__device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v, double eps4, int wtype,
-                                               double& outL, double& outR) {
-  const double k13 = 13.0 / 3.0, s6 = 1.0 / 6.0;
-  double d1 = fma(-2.0, w[1], w[0]) + w[2];
-  double d2 = fma(-2.0, w[2], w[1]) + w[3];
-  double d3 = fma(-2.0, w[3], w[2]) + w[4];
-  double d4 = fma(-2.0, w[4], w[3]) + w[5];
-  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
-  double gL2 = w[1] - w[3];
-  double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
-  double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
-  double gR2 = w[4] - w[2];
-  double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
-  double BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
-  double BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
-  double BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
-  double BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
-  double BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
-  double BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
+// The second half of weno5_pair_alt: from the six smoothness terms B, the second
+// differences d1..d4 centred at window cells 1..4 (Yamaleev-Carpenter's tau), and the
+// values v.
+__device__ __forceinline__ void weno5_pair_alt_finish(const double* v, int wtype, double BL1, double BL2,
+                                                      double BL3, double BR1, double BR2, double BR3, double d1,
+                                                      double d2, double d3, double d4, double& outL,
+                                                      double& outR) {
+  const double s6 = 1.0 / 6.0;
   double tL = 0.0, tR = 0.0;
   if (wtype == WENO_W_BORGES) {
     tL = fabs(BL1 - BL3);
@@ -600,6 +589,42 @@ __device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v,
   double cB = fma(5.0, v[3], fma(2.0, v[2], -v[4])) * s6;
   weno5_side_alt(wtype, BL1, BL2, BL3, tL, cL1, cA, cB, outL);
   weno5_side_alt(wtype, BR1, BR2, BR3, tR, cR1, cB, cA, outR);
+}
+
+// The per-cell table of the alternative formulations: B (not squared) for the three
+// places of the sub-stencil (a, b, c), as weno5_cell_q, and its second difference d.
+__device__ __forceinline__ void weno5_cell_b(double a, double b, double c, double eps4, double& Bl, double& Bc,
+                                             double& Br, double& d) {
+  d = fma(-2.0, b, a) + c;
+  const double kde = fma((13.0 / 3.0) * d, d, eps4);
+  const double gl = fma(3.0, c, fma(-4.0, b, a));
+  const double gc = a - c;
+  const double gr = fma(3.0, a, fma(-4.0, b, c));
+  Bl = fma(gl, gl, kde);
+  Bc = fma(gc, gc, kde);
+  Br = fma(gr, gr, kde);
+}
+
+__device__ __forceinline__ void weno5_pair_alt(const double* w, const double* v, double eps4, int wtype,
+                                               double& outL, double& outR) {
+  const double k13 = 13.0 / 3.0;
+  double d1 = fma(-2.0, w[1], w[0]) + w[2];
+  double d2 = fma(-2.0, w[2], w[1]) + w[3];
+  double d3 = fma(-2.0, w[3], w[2]) + w[4];
+  double d4 = fma(-2.0, w[4], w[3]) + w[5];
+  double gL1 = fma(3.0, w[2], fma(-4.0, w[1], w[0]));
+  double gL2 = w[1] - w[3];
+  double gL3 = fma(3.0, w[2], fma(-4.0, w[3], w[4]));
+  double gR1 = fma(3.0, w[3], fma(-4.0, w[4], w[5]));
+  double gR2 = w[4] - w[2];
+  double gR3 = fma(3.0, w[3], fma(-4.0, w[2], w[1]));
+  double BL1 = fma(k13 * d1, d1, fma(gL1, gL1, eps4));
+  double BL2 = fma(k13 * d2, d2, fma(gL2, gL2, eps4));
+  double BL3 = fma(k13 * d3, d3, fma(gL3, gL3, eps4));
+  double BR1 = fma(k13 * d4, d4, fma(gR1, gR1, eps4));
+  double BR2 = fma(k13 * d3, d3, fma(gR2, gR2, eps4));
+  double BR3 = fma(k13 * d2, d2, fma(gR3, gR3, eps4));
+  weno5_pair_alt_finish(v, wtype, BL1, BL2, BL3, BR1, BR2, BR3, d1, d2, d3, d4, outL, outR);
 }
 
 // One side of weno5_pair / weno5_pair_alt: the left-biased value on the five-point

@@ -350,10 +350,12 @@ struct RelFlux {
   static constexpr bool value = !GRAV;
 };
 
-// CQ (component-wise, Jiang-Shu, no gravity, no tape: the tile form): the squared
-// smoothness terms come from the tile's per-cell table (weno5_cell_q), `qt` pointing at
-// the entry of window cell 0 in row 0, rows of `nc` cells, row 3k + role for quantity k
-// (the NV flux components, then the NV state components) and role l, c, r.
+// CQ (component-wise, no gravity, no tape: the tile form): the smoothness terms come
+// from the tile's per-cell table, `qt` pointing at the entry of window cell 0 in row 0,
+// rows of `nc` cells; for quantity k (the NV flux components, then the NV state
+// components) rows QR k + role: Jiang-Shu (QR = 3) q = B^2 for the places l, c, r
+// (weno5_cell_q); the other formulations (QR = 4) B for l, c, r and the second
+// difference (weno5_cell_b).
 template <int M, bool CHAR, int UPW, int DIR, bool ALTW, bool GRAV, bool WT, bool CQ = false>
 __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>::NV],
                                            const double (&wf)[6][ModelTraits<M>::NV], const double (&wuc)[6],
@@ -362,7 +364,7 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
                                            double eps4, bool src_dir, long long tapeoff, double (&fI)[ModelTraits<M>::NV],
                                            double (&SI)[ModelTraits<M>::NV], const double* qt = nullptr,
                                            int nc = 0) {
-  static_assert(!CQ || (!CHAR && !ALTW && !GRAV && !WT), "the per-cell table serves the plain component-wise form");
+  static_assert(!CQ || (!CHAR && !GRAV && !WT), "the per-cell table serves the plain component-wise form");
   constexpr int NV = ModelTraits<M>::NV;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
   constexpr bool REL = RelFlux<GRAV>::value;
@@ -392,17 +394,23 @@ __device__ __forceinline__ void iface_flux(const double (&wu)[6][ModelTraits<M>:
         continue;
       }
       if (CQ) {
-        // qL = (ql[1], qc[2], qr[3]), qR = (qr[4], qc[3], ql[2]) of the window cells
-        const double* qf = qt + (3 * v) * nc;
-        const double* qu = qt + (3 * (NV + v)) * nc;
-        weno5_pair_q<REL>(sf, qf[1], qf[nc + 2], qf[2 * nc + 3], qf[2 * nc + 4], qf[nc + 3], qf[2], fL[v], fR[v]);
-        if (M == MODEL_NS3D && v == NV - 1) {
-          double sc[6];
+        // left (l[1], c[2], r[3]), right (r[4], c[3], l[2]) of the window cells
+        constexpr int QR = ALTW ? 4 : 3;
+        double sc[6];
 #pragma unroll
-          for (int p = 0; p < 6; p++) sc[p] = REL ? (p == 2 ? 0.0 : wuc[p] - wuc[2]) : wuc[p];
-          weno5_pair_q<REL>(sc, qu[1], qu[nc + 2], qu[2 * nc + 3], qu[2 * nc + 4], qu[nc + 3], qu[2], uL[v], uR[v]);
-        } else {
-          weno5_pair_q<REL>(su, qu[1], qu[nc + 2], qu[2 * nc + 3], qu[2 * nc + 4], qu[nc + 3], qu[2], uL[v], uR[v]);
+        for (int p = 0; p < 6; p++) sc[p] = REL ? (p == 2 ? 0.0 : wuc[p] - wuc[2]) : wuc[p];
+        const double* vu = (M == MODEL_NS3D && v == NV - 1) ? sc : su;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const double* q = qt + (QR * (h * NV + v)) * nc;
+          const double* vals = h ? vu : sf;
+          double& oL = h ? uL[v] : fL[v];
+          double& oR = h ? uR[v] : fR[v];
+          if (ALTW)
+            weno5_pair_alt_finish(vals, pp.wtype, q[1], q[nc + 2], q[2 * nc + 3], q[2 * nc + 4], q[nc + 3], q[2],
+                                  q[3 * nc + 1], q[3 * nc + 2], q[3 * nc + 3], q[3 * nc + 4], oL, oR);
+          else
+            weno5_pair_q<REL>(vals, q[1], q[nc + 2], q[2 * nc + 3], q[2 * nc + 4], q[nc + 3], q[2], oL, oR);
         }
         continue;
       }
@@ -761,16 +769,18 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
   constexpr int NV = ModelTraits<M>::NV, ND = ModelTraits<M>::ND;
   constexpr bool CC = NeedCC<M, CHAR, UPW>::value;
   constexpr int TC = TI - 1, NCELL = TI + 5;
-  // component-wise with Jiang-Shu weights: the squared smoothness terms of every
-  // cell's sub-stencil, once per cell instead of six times per interface pair, where
-  // the table keeps the block's static shared memory within 48 KB
+  // component-wise: the smoothness terms of every cell's sub-stencil, once per cell
+  // instead of six times per interface pair (QR rows per quantity: q for l, c, r with
+  // Jiang-Shu weights; B for l, c, r and the second difference otherwise), where the
+  // table keeps the block's static shared memory within 48 KB
+  constexpr int QR = ALTW ? 4 : 3;
   constexpr size_t SMEM0 = sizeof(double) * NCELL * (2 * NV + 1) + sizeof(CellAux<M>) * NCELL +
                            sizeof(double) * TI * NV;
-  constexpr bool CQ = !CHAR && !ALTW && !WT && SMEM0 + sizeof(double) * 6 * NV * NCELL <= 48 * 1024;
+  constexpr bool CQ = !CHAR && !WT && SMEM0 + sizeof(double) * QR * 2 * NV * NCELL <= 48 * 1024;
   __shared__ double su[NCELL][NV], sf[NCELL][NV], suc[NCELL];
   __shared__ CellAux<M> sax[NCELL];
   __shared__ double sfI[TI][NV];
-  __shared__ double sq[CQ ? 6 * NV : 1][CQ ? NCELL : 1];
+  __shared__ double sq[CQ ? QR * 2 * NV : 1][CQ ? NCELL : 1];
   const long long line = blk % ntrans;
   const int I0 = (int)(blk / ntrans) * TC;
   long long tr = line, pbase = (long long)G.g * G.stride[DIR];
@@ -813,10 +823,14 @@ __device__ __forceinline__ void hyp_tile_body(const double* __restrict__ U, doub
     // two neighbours; cells past the line's reach hold terms no interface reads
     for (int c = 1 + threadIdx.x; c <= TI + 3; c += TI) {
 #pragma unroll
-      for (int k = 0; k < NV; k++) {
-        weno5_cell_q(sf[c - 1][k], sf[c][k], sf[c + 1][k], eps4, sq[3 * k][c], sq[3 * k + 1][c], sq[3 * k + 2][c]);
-        weno5_cell_q(su[c - 1][k], su[c][k], su[c + 1][k], eps4, sq[3 * (NV + k)][c], sq[3 * (NV + k) + 1][c],
-                     sq[3 * (NV + k) + 2][c]);
+      for (int k = 0; k < 2 * NV; k++) {
+        const double a = k < NV ? sf[c - 1][k] : su[c - 1][k - NV];
+        const double b = k < NV ? sf[c][k] : su[c][k - NV];
+        const double e = k < NV ? sf[c + 1][k] : su[c + 1][k - NV];
+        if (ALTW)
+          weno5_cell_b(a, b, e, eps4, sq[QR * k][c], sq[QR * k + 1][c], sq[QR * k + 2][c], sq[QR * k + 3][c]);
+        else
+          weno5_cell_q(a, b, e, eps4, sq[QR * k][c], sq[QR * k + 1][c], sq[QR * k + 2][c]);
       }
     }
     __syncthreads();

@@ -330,6 +330,27 @@ def test_nonfinite_state_is_reported(built_lib, tmp_path):
 
 
 @pytest.mark.parametrize("tile", [32, 64, 128])
+@pytest.mark.parametrize("weights", ["mapped", "borges", "yc", "none"])
+@pytest.mark.parametrize("model", ["euler1d", "euler2d", "navierstokes3d"])
+def test_tile_kernel_weights_match_oracle(built_lib, oracle_lib, tmp_path, model, weights, tile):
+    """The component-wise tile form with the other weight formulations, whose
+    smoothness terms and second differences come from the tile's per-cell table
+    (where it fits the block's shared memory), per RHS against the oracle."""
+    case = make(model, "components", "roe")
+    case.weights = weights
+    s = solver_for(case, tmp_path)
+    for d in range(case.ndims):
+        s.set_launch(d, -tile, 0)
+    P = O.Problem(case)
+    u0 = P.u0()
+    u = torch.from_numpy(u0).cuda()
+    out = torch.zeros_like(u)
+    s.rhs(out, u)
+    got = O.interior(out.cpu().numpy(), case.size, case.nvars, 3)
+    assert relerr(got, O.interior(P.rhs(u0.copy()), case.size, case.nvars, 3)) <= RHS_TOL
+
+
+@pytest.mark.parametrize("tile", [32, 64, 128])
 @pytest.mark.parametrize("model,interp,upw", [("euler1d", "components", "roe"), ("euler1d", "characteristic", "rf-char"),
                                               ("euler2d", "characteristic", "roe"),
                                               ("euler2d", "components", "llf-char"),
