@@ -55,7 +55,8 @@ FP64_PER_CELL_STEP = {
                "walker": {"flops": 8585.4, "instr": 5575.5, "captured": "512^2, segments 54/27"}},
     "sod": {"lanes": {"flops": 3654.7, "instr": 2455.2, "captured": "1024 (the full grid), lane groups of 16"}},
     "tgv": {"walker": {"flops": 18445.5, "instr": 12291.2,
-                       "captured": "128^3, segments 48/32/32 (the 256^3 shape)"}},
+                       "captured": "128^3, segments 48/32/32 (the earlier 256^3 shape)"},
+            "tile": {"flops": 16107.9, "instr": 10815.0, "captured": "128^3, tiles of 64 (the 256^3 shape)"}},
     "rtb": {"walker": {"flops": 16583.3, "instr": 11627.6, "captured": "128^3, segments 32/32/32 (the 201^3 shape)"}},
     "rtb64": {"walker": {"flops": 25265.3, "instr": 17712.2, "captured": "64^3 (the full grid), segments 7/7/7"}},
     "dns": {"walker": {"flops": 20731.2, "instr": 14874.6, "captured": "128^3, segments 48/48/48 (the 256^3 shape)"}},
