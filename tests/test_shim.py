@@ -74,6 +74,8 @@ DECKS = {
     "sod_no_limiting_rf": lambda: _with(C.sod(48, n_iter=2, dt=1e-3, upwinding="rf-char"), weights="none"),
     "rtb_gravity_hb2": lambda: C.rising_thermal_bubble(12, n_iter=2),
     "stratified_euler1d_gravity": lambda: C.stratified_1d(32, n_iter=2, g=1.0, grav_type=0),
+    "sod_slip_walls_1d": lambda: _with(C.sod(48, n_iter=2, dt=1e-3),
+                                       bcs={(0, 1): ("slip-wall", [0.0]), (0, -1): ("slip-wall", [0.2])}),
     "stratified_euler1d_gravity_crweno_char": lambda: _with(C.stratified_1d(32, n_iter=2, grav_type=1,
                                                                           interp="characteristic"),
                                                           hyp_scheme="crweno5"),
